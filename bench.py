@@ -1,0 +1,322 @@
+"""Benchmark of the planner hot path: exact nearest-neighbour queries against
+a 1M-node tree (planar 10-link arm workload, SO(2)^10 metric), one JSON line.
+
+A step = one batch of 65,536 seeded query states answered by the device
+kd-tree (warp-per-query FP32 sweep + FP64 re-rank, bit-exact ids).  The tree
+holds 1,048,576 seeded configurations inserted in batches of 65,536 (the
+planner's wavefront size).  Secondary figures in the same line: edge checks/s
+for the arm's DiscreteMotionValidator edges (max joint step 0.01 rad).
+
+  value  -- queries/s with queries resident in HBM, CUDA events around each
+            step, L2 flushed (256 MiB write) between steps
+  e2e    -- the same metric through the C ABI with pinned host buffers
+            (H2D of the queries and D2H of ids + distances inside the timing)
+  --impl reference -- the CPU kd-tree of the oracle (the reference's nigh is
+            not vendored) on all host cores, same tree and queries.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_TREE = 1 << 20
+BATCH = 65536
+N_EDGES = 65536
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device=0):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        cmd = ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+               "-lms", "200"]
+        try:
+            p = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            return
+        try:
+            while not self._stop.is_set():
+                line = p.stdout.readline()
+                if not line:
+                    break
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) == 6:
+                    self.samples.append(parts)
+        finally:
+            p.terminate()
+            try:
+                p.wait(timeout=2)
+            except Exception:
+                p.kill()
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=3)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[2 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons}
+
+
+def _dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _workload(seed_base=20261205):
+    from mpt_gb300 import scenes
+    sc = scenes.arm_scene()
+    tree_pts = scenes.uniform_states(sc, N_TREE, seed_base + 1)
+    return sc, tree_pts
+
+
+def _queries(sc, nbatches, seed):
+    from mpt_gb300 import scenes
+    return [scenes.uniform_states(sc, BATCH, seed + i) for i in range(nbatches)]
+
+
+def run_reference(args):
+    """CPU kd-tree (oracle port) on all host cores, bounded sample per step."""
+    ws, rank, _ = _dist_env()
+    if rank != 0:
+        return
+    import oracle
+    sc, pts = _workload()
+    sp = oracle.make_space(sc["metric"], sc["dim"])
+    t0 = time.perf_counter()
+    tree = oracle.KDTree(sp, pts, 8)
+    build_s = time.perf_counter() - t0
+    cores = os.cpu_count()
+    sample = 4096
+    qs = _queries(sc, 1, 777)[0][:sample]
+    for _ in range(max(1, args.warmup)):
+        tree.nearest(qs[:512], cores)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        tree.nearest(qs, cores)
+        times.append(time.perf_counter() - t0)
+    qps = sample * len(times) / sum(times)
+    line = {"metric": "NN queries/s @1M nodes (SO(2)^10, 10-link arm)", "value": qps, "unit": "queries/s",
+            "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform SO(2)^10 states)",
+            "config": {"workload": "nn_so2x10_1M", "tree_nodes": N_TREE, "queries_per_step": sample},
+            "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": cores, "kind": "port",
+                             "sample": "%d queries per step against the full 1,048,576-node tree" % sample},
+            "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "tree_build_s": build_s}
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+    import mpt_gb300 as m
+    ws, rank, local = _dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    ctx = m.Context(local)
+    sc, pts = _workload()
+    tree = m.Tree(ctx, sc["metric"], sc["dim"], N_TREE)
+    t0 = time.perf_counter()
+    dpts = torch.from_numpy(pts).cuda()
+    for lo in range(0, N_TREE, BATCH):
+        tree.insert(dpts[lo:lo + BATCH])
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    del dpts
+
+    nbuf = 4
+    hq = _queries(sc, nbuf, 1000 + 97 * rank)
+    dq = [torch.from_numpy(x).cuda() for x in hq]
+    di = torch.empty(BATCH, dtype=torch.int32, device="cuda")
+    dd = torch.empty(BATCH, dtype=torch.float64, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    for i in range(max(3, args.warmup)):
+        tree.nearest(dq[i % nbuf], di, dd, stream=stream)
+    torch.cuda.synchronize()
+    tree.counters(reset=True)
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    launches0 = ctx.kernel_launches()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for s in range(args.steps):
+            flush.fill_(s & 0xff)  # L2 flush between steps (outside the events)
+            starts[s].record(stream)
+            tree.nearest(dq[s % nbuf], di, dd, stream=stream)
+            ends[s].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    launches = ctx.kernel_launches() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    if ws > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    cnt = tree.counters(reset=True)
+    value = ws * BATCH * args.steps / (total_ms / 1000.0)
+
+    # roofline of k_nearest: algorithmic bytes per launch from the device counters
+    D = sc["dim"]
+    per_launch = {k: v / args.steps for k, v in cnt.items()}
+    alg_bytes = (per_launch["points_evaluated"] * (4 * D + 4) + per_launch["internal_visited"] * (16 + 8 * D)
+                 + per_launch["leaves_visited"] * 16 + per_launch["reranked"] * 8 * D + BATCH * (8 * D + 12))
+    avg_s = total_ms / 1000.0 / args.steps
+    peak, peak_kind = _peaks()
+    achieved = alg_bytes / avg_s / 1e9
+
+    # end to end through the C ABI with pinned host buffers
+    hq_pinned = [torch.from_numpy(x).pin_memory() for x in hq]
+    hi = torch.empty(BATCH, dtype=torch.int32).pin_memory()
+    hd = torch.empty(BATCH, dtype=torch.float64).pin_memory()
+    qn = [x.numpy() for x in hq_pinned]
+    for i in range(3):
+        ctx.lib.mptg_nearest(tree.h, qn[i % nbuf].ctypes.data, BATCH, hi.data_ptr(), hd.data_ptr(), None)
+    torch.cuda.synchronize()
+    e2e_t = []
+    for s in range(args.steps):
+        flush.fill_(s & 0xff)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = ctx.lib.mptg_nearest(tree.h, qn[s % nbuf].ctypes.data, BATCH, hi.data_ptr(), hd.data_ptr(), None)
+        e2e_t.append(time.perf_counter() - t0)
+        assert st == 0
+    e2e_total = sum(e2e_t)
+    if ws > 1:
+        t = torch.tensor([e2e_total], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_val = ws * BATCH * args.steps / e2e_total
+    # results of the host path equal the device path
+    assert np.array_equal(hi.numpy(), tree.nearest(hq[(args.steps - 1) % nbuf])[0])
+
+    # secondary: edge checks/s on the arm scene (DMV at 0.01 rad joint steps)
+    from mpt_gb300 import scenes
+    scene = m.Scene(ctx, sc)
+    ea, eb = scenes.steered_edges(sc, 8192, 555)
+    reps = N_EDGES // len(ea)
+    da = torch.from_numpy(np.tile(ea, (reps, 1))).cuda()
+    db = torch.from_numpy(np.tile(eb, (reps, 1))).cuda()
+    eo = torch.empty(N_EDGES, dtype=torch.uint8, device="cuda")
+    for _ in range(2):
+        scene.link(da, db, sc["edge_step"], sc["resolution"], out=eo, stream=stream)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    esteps = 3
+    for _ in range(esteps):
+        scene.link(da, db, sc["edge_step"], sc["resolution"], out=eo, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    edge_rate = N_EDGES * esteps / (e0.elapsed_time(e1) / 1000.0)
+
+    # CPU baseline: oracle kd-tree on the host cores, bounded sample
+    cpu = None
+    if rank == 0:
+        import oracle
+        osp = oracle.make_space(sc["metric"], sc["dim"])
+        ot = oracle.KDTree(osp, pts, 8)
+        sample = 2048
+        cores = os.cpu_count()
+        ot.nearest(hq[0][:256], cores)
+        t0 = time.perf_counter()
+        ci, _ = ot.nearest(hq[0][:sample], cores)
+        cpu_s = time.perf_counter() - t0
+        gi, _ = tree.nearest(hq[0][:sample])
+        cpu = {"value": sample / cpu_s, "unit": "queries/s", "cores": cores, "kind": "port",
+               "sample": "%d queries against the full 1,048,576-node tree" % sample,
+               "ids_equal_gpu": bool(np.array_equal(ci, gi))}
+
+    if rank == 0:
+        line = {"metric": "NN queries/s @1M nodes (SO(2)^10, 10-link arm)", "value": value, "unit": "queries/s",
+                "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+                "data": "synthetic (seeded uniform SO(2)^10 states)",
+                "config": {"workload": "nn_so2x10_1M", "tree_nodes": N_TREE, "queries_per_step": BATCH,
+                           "l2": "flushed (256 MiB write) between steps", "parallelism": "replicas"},
+                "e2e": {"value": e2e_val, "unit": "queries/s", "h2d_bytes_per_step": BATCH * D * 8,
+                        "d2h_bytes_per_step": BATCH * 12},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                             "kernel": "k_nearest<SO2,16>", "alg_bytes_per_launch": alg_bytes,
+                             "counters_per_launch": per_launch},
+                "cpu_baseline": cpu,
+                "edge_checks": {"value": edge_rate, "unit": "edges/s", "workload": "arm DMV, 0.01 rad joint step",
+                                "edges_per_launch": N_EDGES},
+                "clocks": clk.summary(), "gpu_launches": launches, "tree_build_s": build_s,
+                "wall_s_timed": wall}
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

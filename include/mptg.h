@@ -1,0 +1,154 @@
+/*
+ * mptg.h - C ABI of the GB300-native MPT planner hot path.
+ *
+ * Plain C: pointers, sizes and opaque handles only.  Every call returns an
+ * mptg_status; no C++ exception crosses this boundary.  Buffers are owned by
+ * the caller and may live in host memory (pageable or pinned) or in device
+ * memory of the context's GPU: the library inspects each pointer.  A call
+ * whose buffers are all in device memory is asynchronous on `stream`
+ * (a cudaStream_t passed as void*, NULL = the legacy default stream); a call
+ * that touches host memory copies through a staging buffer and returns after
+ * the results are in the caller's buffer.
+ *
+ * Each entry point names the reference interface it replaces (paths inside
+ * the MPT project, file:line).
+ */
+#ifndef MPTG_H
+#define MPTG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    MPTG_OK = 0,
+    MPTG_ERR_INVALID_ARG = 1,
+    MPTG_ERR_OOM = 2,
+    MPTG_ERR_CUDA = 3,
+    MPTG_ERR_TIMEOUT = 4,
+    MPTG_ERR_QUEUE_OVERFLOW = 5,
+    MPTG_ERR_UNSUPPORTED_METRIC = 6,
+    MPTG_ERR_CAPACITY = 7,
+    MPTG_ERR_NO_START = 8,
+    MPTG_ERR_ALREADY_SOLVING = 9
+} mptg_status;
+
+/* Metric spaces (nigh::metric::Space<T, M> as used through
+ * src/mpt/lp_space.hpp, so2_space.hpp, so3_space.hpp, se3_space.hpp):
+ *  L2   sqrt(sum (a_i-b_i)^2)                      LPSpace<double, D, 2>
+ *  SO2  sum_i min(|a_i-b_i|, 2pi-|a_i-b_i|)        SO2LPSpace<double, D, 1>
+ *  SO3  acos(|a.b|), a,b unit quaternions (x,y,z,w)  SO3Space<double>
+ *  SE3  w0*acos(|qa.qb|) + w1*|pa-pb|, state (qx,qy,qz,qw,px,py,pz)
+ *                                                  SE3Space<double, w0, w1>
+ *  L1   sum |a_i-b_i|                              L1Space<double, D> */
+typedef enum {
+    MPTG_METRIC_L2 = 0,
+    MPTG_METRIC_SO2 = 1,
+    MPTG_METRIC_SO3 = 2,
+    MPTG_METRIC_SE3 = 3,
+    MPTG_METRIC_L1 = 4
+} mptg_metric;
+
+typedef struct mptg_ctx mptg_ctx;
+typedef struct mptg_tree mptg_tree;
+typedef struct mptg_scene mptg_scene;
+
+/* ---- context ------------------------------------------------------- */
+mptg_status mptg_create(mptg_ctx** ctx, int device);
+mptg_status mptg_destroy(mptg_ctx* ctx);
+/* Message of the last failed call on this context (static storage). */
+const char* mptg_last_error(mptg_ctx* ctx);
+/* Number of kernels this library has launched on the context (for audits). */
+uint64_t mptg_kernel_launches(mptg_ctx* ctx);
+
+/* ---- nearest-neighbour tree ----------------------------------------
+ * Replaces nigh::Nigh<Node*, Space, NodeKey, Concurrency, KDTreeBatch<>>
+ * as constructed in src/mpt/impl/prrt/prrt.hpp:121-122 and
+ * src/mpt/impl/prrt_star/prrt_star.hpp:182-183. */
+mptg_status mptg_tree_create(mptg_ctx* ctx, mptg_metric metric, int dim, const double* weights,
+                             size_t capacity, mptg_tree** tree);
+mptg_status mptg_tree_destroy(mptg_tree* tree);
+/* nigh insert (src/mpt/impl/prrt/prrt.hpp:186,447): appends n states
+ * (row-major n x dim doubles); their ids are size()..size()+n-1. */
+mptg_status mptg_tree_insert(mptg_tree* tree, const double* states, size_t n, void* stream);
+mptg_status mptg_tree_size(mptg_tree* tree, size_t* n);
+/* Copy states [first, first+n) out of the tree (row-major doubles). */
+mptg_status mptg_tree_states(mptg_tree* tree, size_t first, size_t n, double* out, void* stream);
+/* nigh nearest(q) (src/mpt/impl/prrt/prrt.hpp:406-409): for each of nq
+ * queries the id of the nearest state and its exact FP64 distance; ties go to
+ * the lowest id.  idx = -1 and dist = +inf when the tree is empty. */
+mptg_status mptg_nearest(mptg_tree* tree, const double* queries, size_t nq, int32_t* idx_out,
+                         double* dist_out, void* stream);
+/* nigh nearest(nbh, q, k, r) (src/mpt/impl/rrg_rewire_neighbors.hpp:64-67,
+ * 124-128): the k nearest states within distance r (r <= 0 or inf = no
+ * limit), sorted by (distance, id); unused slots hold id -1 and +inf.
+ * k <= 64. */
+mptg_status mptg_nearest_k(mptg_tree* tree, const double* queries, size_t nq, int k, double r,
+                           int32_t* idx_out, double* dist_out, void* stream);
+/* Brute-force exact 1-NN over every stored state (same contract as
+ * mptg_nearest); the reference nigh::Linear strategy (src/mpt/impl/
+ * nearest_strategy.hpp:44-72). */
+mptg_status mptg_nearest_linear(mptg_tree* tree, const double* queries, size_t nq, int32_t* idx_out,
+                                double* dist_out, void* stream);
+
+/* Per-tree search counters accumulated since the last reset:
+ * [0] queries, [1] internal nodes visited, [2] leaves visited,
+ * [3] points evaluated in FP32, [4] candidates re-ranked in FP64. */
+mptg_status mptg_tree_counters(mptg_tree* tree, uint64_t out[5], int reset);
+
+/* ---- scenes and validity ------------------------------------------- */
+typedef enum { MPTG_SCENE_GRID = 0, MPTG_SCENE_PLANAR_ARM = 1, MPTG_SCENE_RIGID_MESH = 2 } mptg_scene_kind;
+
+/* Scene descriptor (all arrays are host memory, copied at creation).
+ *  GRID:        width x height uint8 cells, non-zero = obstacle, row-major by y;
+ *               state (x, y), L2 metric; valid(q) per
+ *               demo/png_2d_scenario.hpp:104-110 with out-of-grid = invalid.
+ *  PLANAR_ARM:  nlinks links of link_len[i], base at the origin, discs
+ *               (cx, cy, r) x ndiscs; state = nlinks joint angles, SO2 metric;
+ *               valid(q) per demo/link_manipulator_scenario.hpp:99-116 plus,
+ *               when self_collision != 0, no two non-adjacent links touching.
+ *  RIGID_MESH:  robot and environment triangle soups (9 doubles per
+ *               triangle); state (qx,qy,qz,qw,px,py,pz), SE3 metric with
+ *               weights w0 (rotation) and w1 (translation); valid(q) iff the
+ *               robot placed at T(q) intersects no environment triangle
+ *               (demo/se3_rigid_body_scenario.hpp:282-312). */
+typedef struct {
+    int kind;
+    /* grid */
+    const uint8_t* grid; int width; int height;
+    /* planar arm */
+    int nlinks; const double* link_len; int ndiscs; const double* discs;
+    double robot_radius; int self_collision;
+    /* rigid mesh */
+    int64_t nrobot; const double* robot_tris; int64_t nenv; const double* env_tris;
+    double w_rot; double w_pos;
+} mptg_scene_desc;
+
+mptg_status mptg_scene_create(mptg_ctx* ctx, const mptg_scene_desc* desc, mptg_scene** scene);
+mptg_status mptg_scene_destroy(mptg_scene* scene);
+/* State dimension and metric of a scene's configuration space. */
+mptg_status mptg_scene_space(mptg_scene* scene, int* dim, int* metric, double weights[2]);
+
+/* Scenario::valid(q) batched (src/mpt/impl/prrt/prrt.hpp:439). */
+mptg_status mptg_valid_states(mptg_scene* scene, const double* states, size_t n, uint8_t* out,
+                              void* stream);
+
+/* Scenario::link(a, b) through DiscreteMotionValidator
+ * (src/mpt/discrete_motion_validator.hpp:71-130) batched: out[i] = 1 iff
+ * valid(b_i) and every interpolate(a_i, b_i, j/steps), 1 <= j < steps, is
+ * valid, where steps = ceil(m(a_i, b_i) / step).  resolution 0: m is the
+ * space metric (the reference DMV); resolution 1: m is the largest wrapped
+ * joint difference (planar-arm edges at a maximum joint step).  a_i is
+ * assumed valid, as the reference asserts (:73).  samples_out (may be NULL)
+ * receives the number of states checked per edge when every sample is
+ * evaluated. */
+mptg_status mptg_valid_edges(mptg_scene* scene, const double* a, const double* b, size_t n,
+                             double step, int resolution, uint8_t* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPTG_H */

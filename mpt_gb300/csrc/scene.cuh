@@ -1,0 +1,52 @@
+// scene.cuh - scene storage shared by the validity, mesh and planner units.
+#pragma once
+#include "common.cuh"
+
+struct MeshData;  // rigid-mesh BVHs (mesh.cu)
+
+struct mptg_scene {
+    mptg_ctx* ctx = nullptr;
+    int kind = 0, metric = 0, D = 0;
+    double w0 = 1.0, w1 = 1.0;
+    // grid
+    uint8_t* grid = nullptr;
+    int width = 0, height = 0;
+    // planar arm
+    int nlinks = 0, ndiscs = 0, self_collision = 0;
+    double robot_radius = 0.0;
+    double* link_len64 = nullptr;
+    double* discs64 = nullptr;
+    // rigid mesh
+    MeshData* mesh = nullptr;
+};
+
+// POD view passed to kernels by value
+struct SceneView {
+    int kind, metric, D;
+    double w0, w1;
+    const uint8_t* grid;
+    int width, height;
+    int nlinks, ndiscs, self_collision;
+    double robot_radius;
+    const double* link_len64;
+    const double* discs64;
+    // rigid mesh (see mesh.cu)
+    const double* robot_tris;   // [nrobot][9]
+    int nrobot;
+    const double* env_tris;     // [nenv][9], BVH leaf order
+    const float4* env_nodes;    // [2*nenv] {lo.xyz, left|leaf}, {hi.xyz, right|count}
+    int nenv;
+};
+
+SceneView scene_view(const mptg_scene* s);
+mptg_status scene_edges_dev(mptg_scene* sc, const double* da, const double* db, int n, double step, int resolution,
+                            uint8_t* dout, cudaStream_t s, unsigned long long* nsamp);
+mptg_status scene_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* dout, cudaStream_t s);
+
+// rigid-mesh hooks (mesh.cu)
+mptg_status mesh_scene_create(mptg_ctx* ctx, const mptg_scene_desc* d, mptg_scene* s);
+void mesh_scene_free(mptg_scene* s);
+void mesh_fill_view(const mptg_scene* s, SceneView* v);
+mptg_status mesh_edges_dev(mptg_scene* sc, const double* da, const double* db, int n, double step, int resolution,
+                           uint8_t* dout, cudaStream_t s, unsigned long long* nsamp);
+mptg_status mesh_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* dout, cudaStream_t s);

@@ -1,0 +1,1046 @@
+// tree.cu - device-resident bucketed kd-tree: batched incremental insert and
+// warp-per-query exact nearest-neighbour search.
+//
+// Replaces nigh::Nigh<..., KDTreeBatch<>> behind src/mpt/impl/prrt/prrt.hpp
+// (insert :186,447; nearest :406-409) and nearest(nbh,q,k,r) behind
+// src/mpt/impl/rrg_rewire_neighbors.hpp:64-67,124-128.
+//
+// Layout in HBM (per tree, capacity N states of dimension D):
+//   states64 [N][D]  double  master copy, ids = insertion order
+//   pts32    [N][D]  float   FP32 copy used by the builder
+//   nodes    [M]     int4    {split dim | -1 for a leaf, left child | bucket,
+//                             split value bits, leaf point count}
+//                             right child = left child + 1
+//   cell_lo/hi [M][D] float  closed cell bounds of every node
+//   bpts  [B][D][32] float   leaf buckets, SoA per bucket: lane j reads point j
+//   bids  [B][32]    int     point ids of the bucket entries
+// A leaf holds at most 32 points.  Inserting a batch descends every new point
+// to its leaf (k_locate) and appends it (k_append); leaves that overflow are
+// rebuilt into subtrees by a level-synchronous segment builder (sliding
+// midpoint split on the widest axis of the points), so the tree is exact and
+// complete after every insert.
+#include "metrics.cuh"
+
+namespace {
+
+enum { CNT_NODES = 0, CNT_BUCKETS = 1, CNT_NSEG_NEXT = 2, CNT_ERR = 3, CNT_OVF = 4, CNT_NREG = 5,
+       CNT_PERM = 6, CNT_MAXABS = 7, CNT_N = 8 };
+
+enum { SEG_SPLIT = 0, SEG_LEAF = 1 };
+
+struct SegState {
+    int node, start, count, depth;
+    int parent, side, kind, dim;
+    float split;
+    int lc, rc, next;
+    int bucket, degenerate, pad0, pad1;
+};
+
+}  // namespace
+
+struct mptg_tree {
+    mptg_ctx* ctx = nullptr;
+    int metric = 0, D = 0;
+    double w0 = 1, w1 = 1;
+    size_t cap = 0, n = 0;
+    int node_cap = 0, bucket_cap = 0, seg_cap = 0;
+    double* states64 = nullptr;
+    float* pts32 = nullptr;
+    int4* nodes = nullptr;
+    float* cell_lo = nullptr;
+    float* cell_hi = nullptr;
+    int* node_depth = nullptr;
+    float* bpts = nullptr;
+    int* bids = nullptr;
+    int* dcnt = nullptr;
+    unsigned long long* dstats = nullptr;
+    int* perm = nullptr; int* perm2 = nullptr; int* pseg = nullptr; int* pseg2 = nullptr;
+    SegState* segA = nullptr; SegState* segB = nullptr;
+    int* seg_box = nullptr;
+    int* leaf_of = nullptr; int* ovf_pts = nullptr; int* ovf_leaf = nullptr; int* leaf_reg = nullptr;
+    int* seg_cursor = nullptr;
+    int* hcnt = nullptr;  // pinned
+};
+
+struct TreeView {
+    int metric, D;
+    float w0f, w1f;
+    double w0, w1;
+    const int4* __restrict__ nodes;
+    const float* __restrict__ cell_lo;
+    const float* __restrict__ cell_hi;
+    const float* __restrict__ bpts;
+    const int* __restrict__ bids;
+    const double* __restrict__ states64;
+    const float* __restrict__ pts32;
+    const int* __restrict__ dcnt;
+    unsigned long long* stats;
+    int n;
+};
+
+static TreeView view_of(const mptg_tree* t) {
+    TreeView v;
+    v.metric = t->metric; v.D = t->D;
+    v.w0 = t->w0; v.w1 = t->w1; v.w0f = (float)t->w0; v.w1f = (float)t->w1;
+    v.nodes = t->nodes; v.cell_lo = t->cell_lo; v.cell_hi = t->cell_hi;
+    v.bpts = t->bpts; v.bids = t->bids; v.states64 = t->states64; v.pts32 = t->pts32;
+    v.dcnt = t->dcnt; v.stats = t->dstats; v.n = (int)t->n;
+    return v;
+}
+
+// ------------------------------------------------------------------ insert
+
+// FP64 -> FP32 copy plus input checks (NaN, SO2 range, unit quaternions) and
+// the running maximum |coordinate| of the Lp / translation part.
+__global__ void k_convert(const double* __restrict__ in, float* __restrict__ out, int n, int D, int metric,
+                          int* __restrict__ dcnt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* s = in + (size_t)i * D;
+    float* o = out + (size_t)i * D;
+    bool bad = false;
+    float mx = 0.f;
+    for (int d = 0; d < D; ++d) {
+        double v = s[d];
+        if (!(v == v) || isinf(v)) bad = true;
+        o[d] = __double2float_rn(v);
+        bool lp = metric == MPTG_METRIC_L2 || metric == MPTG_METRIC_L1 || (metric == MPTG_METRIC_SE3 && d >= 4);
+        if (lp) mx = fmaxf(mx, __double2float_ru(fabs(v)));
+        if (metric == MPTG_METRIC_SO2 && !(v >= -MPTG_PI && v <= MPTG_PI)) bad = true;
+    }
+    if (metric == MPTG_METRIC_SO3 || metric == MPTG_METRIC_SE3) {
+        double nn = quat_dot64(s, s);
+        if (!(fabs(nn - 1.0) <= MPTG_QUAT_NORM_TOL)) bad = true;
+    }
+    if (bad) atomicOr((unsigned*)&dcnt[CNT_ERR], MPTG_DEVERR_BAD_STATE);
+    if (mx > 0.f) atomicMax(&dcnt[CNT_MAXABS], __float_as_int(mx));
+}
+
+__global__ void k_locate(const int4* __restrict__ nodes, const float* __restrict__ pts32, int first, int n, int D,
+                         int* __restrict__ leaf_of) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* p = pts32 + (size_t)(first + i) * D;
+    int node = 0;
+    for (int guard = 0; guard < 4 * MPTG_MAX_DEPTH; ++guard) {
+        int4 nd = nodes[node];
+        if (nd.x < 0) break;
+        node = p[nd.x] < __int_as_float(nd.z) ? nd.y : nd.y + 1;
+    }
+    leaf_of[i] = node;
+}
+
+__global__ void k_append(int4* __restrict__ nodes, const float* __restrict__ pts32, float* __restrict__ bpts,
+                         int* __restrict__ bids, int first, int n, int D, const int* __restrict__ leaf_of,
+                         int* __restrict__ dcnt, int* __restrict__ ovf_pts, int* __restrict__ ovf_leaf,
+                         int* __restrict__ leaf_reg) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int L = leaf_of[i];
+    int slot = atomicAdd(&nodes[L].w, 1);
+    if (slot < MPTG_BUCKET) {
+        int b = nodes[L].y;
+        const float* p = pts32 + (size_t)(first + i) * D;
+        for (int d = 0; d < D; ++d) bpts[((size_t)b * D + d) * MPTG_BUCKET + slot] = p[d];
+        bids[(size_t)b * MPTG_BUCKET + slot] = first + i;
+    } else {
+        int k = atomicAdd(&dcnt[CNT_OVF], 1);
+        ovf_pts[k] = i;
+        if (slot == MPTG_BUCKET) {
+            int r = atomicAdd(&dcnt[CNT_NREG], 1);
+            ovf_leaf[r] = L;
+            leaf_reg[L] = r;
+        }
+    }
+}
+
+// one thread per overflowing leaf: open a build segment holding the leaf's
+// bucket points followed by its overflow points
+__global__ void k_ovf_segs(const int4* __restrict__ nodes, const int* __restrict__ bids,
+                           const int* __restrict__ node_depth, int nreg, const int* __restrict__ ovf_leaf,
+                           int* __restrict__ dcnt, SegState* __restrict__ seg, int* __restrict__ perm,
+                           int* __restrict__ pseg, int* __restrict__ seg_cursor) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nreg) return;
+    int L = ovf_leaf[r];
+    int4 nd = nodes[L];
+    int total = nd.w;
+    int base = atomicAdd(&dcnt[CNT_PERM], total);
+    SegState s;
+    memset(&s, 0, sizeof(s));
+    s.node = L; s.start = base; s.count = total; s.depth = node_depth[L]; s.parent = -1;
+    seg[r] = s;
+    for (int j = 0; j < MPTG_BUCKET; ++j) {
+        perm[base + j] = bids[(size_t)nd.y * MPTG_BUCKET + j];
+        pseg[base + j] = r;
+    }
+    seg_cursor[r] = MPTG_BUCKET;
+}
+
+__global__ void k_ovf_scatter(int novf, int first, const int* __restrict__ ovf_pts, const int* __restrict__ leaf_of,
+                              const int* __restrict__ leaf_reg, const SegState* __restrict__ seg,
+                              int* __restrict__ seg_cursor, int* __restrict__ perm, int* __restrict__ pseg) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= novf) return;
+    int i = ovf_pts[k];
+    int r = leaf_reg[leaf_of[i]];
+    int pos = seg[r].start + atomicAdd(&seg_cursor[r], 1);
+    perm[pos] = first + i;
+    pseg[pos] = r;
+}
+
+// level step A (per segment): finalise start/count from the parent split and
+// decide leaf vs split
+__global__ void k_seg_a(SegState* __restrict__ cur, int nseg, const SegState* __restrict__ prev,
+                        int4* __restrict__ nodes, int* __restrict__ dcnt, int bucket_cap, int* __restrict__ box,
+                        int D) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nseg) return;
+    SegState S = cur[s];
+    if (S.parent >= 0) {
+        const SegState& P = prev[S.parent];
+        if (S.side == 0) { S.start = P.start; S.count = P.lc; }
+        else { S.start = P.start + P.lc; S.count = P.count - P.lc; }
+    }
+    if (S.count <= MPTG_BUCKET || S.depth >= MPTG_MAX_DEPTH) {
+        if (S.count > MPTG_BUCKET) atomicOr((unsigned*)&dcnt[CNT_ERR], MPTG_DEVERR_DEPTH);
+        int b = atomicAdd(&dcnt[CNT_BUCKETS], 1);
+        if (b >= bucket_cap) {
+            atomicOr((unsigned*)&dcnt[CNT_ERR], MPTG_DEVERR_CAPACITY);
+            b = -1;
+        }
+        int c = S.count < MPTG_BUCKET ? S.count : MPTG_BUCKET;
+        nodes[S.node] = make_int4(-1, b < 0 ? 0 : b, 0, b < 0 ? 0 : c);
+        S.kind = SEG_LEAF;
+        S.bucket = b;
+    } else {
+        S.kind = SEG_SPLIT;
+        S.lc = 0; S.rc = 0;
+        int* bx = box + (size_t)s * 2 * D;
+        for (int d = 0; d < D; ++d) {
+            bx[d] = mptg_f2ord(INFINITY);
+            bx[D + d] = mptg_f2ord(-INFINITY);
+        }
+    }
+    cur[s] = S;
+}
+
+// level step B (per position): fill leaf buckets, accumulate split boxes
+__global__ void k_seg_b(const SegState* __restrict__ cur, const int* __restrict__ perm, const int* __restrict__ pseg,
+                        int* __restrict__ pseg2, int total, const float* __restrict__ pts32, int D,
+                        float* __restrict__ bpts, int* __restrict__ bids, int* __restrict__ box) {
+    int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    int lane = threadIdx.x & 31;
+    int s = pos < total ? pseg[pos] : -1;
+    bool split = false;
+    int p = -1;
+    if (s >= 0) {
+        const SegState& S = cur[s];
+        p = perm[pos];
+        if (S.kind == SEG_LEAF) {
+            int slot = pos - S.start;
+            if (S.bucket >= 0 && slot < MPTG_BUCKET) {
+                for (int d = 0; d < D; ++d)
+                    bpts[((size_t)S.bucket * D + d) * MPTG_BUCKET + slot] = pts32[(size_t)p * D + d];
+                bids[(size_t)S.bucket * MPTG_BUCKET + slot] = p;
+            }
+            pseg2[pos] = -1;
+        } else {
+            split = true;
+        }
+    } else if (pos < total) {
+        pseg2[pos] = -1;
+    }
+    unsigned act = __ballot_sync(0xffffffffu, split);
+    if (split) {
+        unsigned grp = __match_any_sync(act, s);
+        int leader = __ffs(grp) - 1;
+        int* bx = box + (size_t)s * 2 * D;
+        for (int d = 0; d < D; ++d) {
+            int o = mptg_f2ord(pts32[(size_t)p * D + d]);
+            int mn = __reduce_min_sync(grp, o);
+            int mx = __reduce_max_sync(grp, o);
+            if (lane == leader) {
+                atomicMin(&bx[d], mn);
+                atomicMax(&bx[D + d], mx);
+            }
+        }
+    }
+}
+
+// level step C (per segment): choose the split, allocate children
+__global__ void k_seg_c(SegState* __restrict__ cur, int nseg, SegState* __restrict__ next,
+                        int4* __restrict__ nodes, float* __restrict__ cell_lo, float* __restrict__ cell_hi,
+                        int* __restrict__ node_depth, int* __restrict__ dcnt, int node_cap, int seg_cap,
+                        const int* __restrict__ box, int D, int metric, float w0, float w1) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nseg) return;
+    SegState S = cur[s];
+    if (S.kind != SEG_SPLIT) return;
+    const int* bx = box + (size_t)s * 2 * D;
+    int dim = 0;
+    float bext = -1.f, blo = 0.f, bhi = 0.f;
+    for (int d = 0; d < D; ++d) {
+        float lo = mptg_ord2f(bx[d]), hi = mptg_ord2f(bx[D + d]);
+        float sc = 1.f;
+        if (metric == MPTG_METRIC_SE3) sc = d < 4 ? w0 : w1;
+        float ext = (hi - lo) * sc;
+        if (ext > bext) { bext = ext; dim = d; blo = lo; bhi = hi; }
+    }
+    float split;
+    int degenerate = 0;
+    if (bext > 0.f) {
+        split = blo + (bhi - blo) * 0.5f;
+        if (!(split > blo)) split = bhi;
+        if (split > bhi) split = bhi;
+    } else {
+        degenerate = 1;
+        dim = 0;
+        split = mptg_ord2f(bx[0]);
+    }
+    int c = atomicAdd(&dcnt[CNT_NODES], 2);
+    if (c + 2 > node_cap) {
+        atomicOr((unsigned*)&dcnt[CNT_ERR], MPTG_DEVERR_CAPACITY);
+        // make the segment a truncated leaf so that the build terminates
+        S.kind = SEG_LEAF; S.bucket = -1;
+        cur[s] = S;
+        nodes[S.node] = make_int4(-1, 0, 0, 0);
+        return;
+    }
+    nodes[S.node] = make_int4(dim, c, __float_as_int(split), 0);
+    node_depth[c] = S.depth + 1;
+    node_depth[c + 1] = S.depth + 1;
+    for (int d = 0; d < D; ++d) {
+        float lo = cell_lo[(size_t)S.node * D + d], hi = cell_hi[(size_t)S.node * D + d];
+        cell_lo[(size_t)c * D + d] = lo;
+        cell_hi[(size_t)c * D + d] = d == dim ? split : hi;
+        cell_lo[(size_t)(c + 1) * D + d] = d == dim ? split : lo;
+        cell_hi[(size_t)(c + 1) * D + d] = hi;
+    }
+    int nx = atomicAdd(&dcnt[CNT_NSEG_NEXT], 2);
+    if (nx + 2 > seg_cap) {
+        // no room for the children's segments: stop here (the insert reports
+        // a capacity error); k_seg_d skips non-split segments
+        atomicOr((unsigned*)&dcnt[CNT_ERR], MPTG_DEVERR_CAPACITY);
+        S.kind = SEG_LEAF; S.bucket = -1;
+        cur[s] = S;
+        return;
+    }
+    SegState a;
+    memset(&a, 0, sizeof(a));
+    a.node = c; a.parent = s; a.side = 0; a.depth = S.depth + 1;
+    next[nx] = a;
+    a.node = c + 1; a.side = 1;
+    next[nx + 1] = a;
+    S.dim = dim; S.split = split; S.degenerate = degenerate; S.next = nx;
+    cur[s] = S;
+}
+
+// level step D (per position): partition the points of split segments
+__global__ void k_seg_d(SegState* __restrict__ cur, const int* __restrict__ perm, const int* __restrict__ pseg,
+                        int* __restrict__ perm2, int* __restrict__ pseg2, int total, const float* __restrict__ pts32,
+                        int D) {
+    int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    int lane = threadIdx.x & 31;
+    int s = pos < total ? pseg[pos] : -1;
+    bool act = false;
+    bool left = false;
+    int p = -1;
+    SegState S;
+    if (s >= 0) {
+        S = cur[s];
+        if (S.kind == SEG_SPLIT) {
+            act = true;
+            p = perm[pos];
+            left = S.degenerate ? (pos - S.start < S.count / 2) : (pts32[(size_t)p * D + S.dim] < S.split);
+        }
+    }
+    if (s >= 0 && !act) pseg2[pos] = -1;
+    unsigned am = __ballot_sync(0xffffffffu, act);
+    if (act) {
+        unsigned grp = __match_any_sync(am, s);
+        unsigned lm = __ballot_sync(grp, left);
+        unsigned rm = grp & ~lm;
+        int leader = __ffs(grp) - 1;
+        int lbase = 0, rbase = 0;
+        if (lane == leader) {
+            if (lm) lbase = atomicAdd(&cur[s].lc, __popc(lm));
+            if (rm) rbase = atomicAdd(&cur[s].rc, __popc(rm));
+        }
+        lbase = __shfl_sync(grp, lbase, leader);
+        rbase = __shfl_sync(grp, rbase, leader);
+        unsigned below = (1u << lane) - 1u;
+        int slot;
+        if (left) slot = S.start + lbase + __popc(lm & below);
+        else slot = S.start + S.count - 1 - (rbase + __popc(rm & below));
+        perm2[slot] = p;
+        pseg2[slot] = S.next + (left ? 0 : 1);
+    }
+}
+
+// ------------------------------------------------------------------ search
+
+__device__ __forceinline__ float warp_sum16(float v) {
+    v += __shfl_xor_sync(0xffffffffu, v, 8);
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+
+__device__ __forceinline__ float so2_w32(float x) {
+    x = fabsf(x);
+    return fminf(x, TWO_PI_F - x);
+}
+
+// lower bound of the distance from the query to node `c`'s cell
+template <int MK>
+__device__ __forceinline__ float cell_lb(const TreeView& t, int c, float myq, int lane) {
+    const int D = t.D;
+    float lo = 0.f, hi = 0.f;
+    if (lane < D) {
+        lo = __ldg(&t.cell_lo[(size_t)c * D + lane]);
+        hi = __ldg(&t.cell_hi[(size_t)c * D + lane]);
+    }
+    if constexpr (MK == MPTG_METRIC_L2 || MK == MPTG_METRIC_L1) {
+        float o = lane < D ? fmaxf(fmaxf(lo - myq, myq - hi), 0.f) : 0.f;
+        if constexpr (MK == MPTG_METRIC_L2) return sqrtf(warp_sum16(o * o));
+        else return warp_sum16(o);
+    } else if constexpr (MK == MPTG_METRIC_SO2) {
+        float o = 0.f;
+        if (lane < D && (myq < lo || myq > hi)) o = fminf(so2_w32(myq - lo), so2_w32(myq - hi));
+        return warp_sum16(o);
+    } else {
+        float cp = 0.f, cm = 0.f, tt = 0.f;
+        if (lane < 4) {
+            float o = fmaxf(fmaxf(lo - myq, myq - hi), 0.f);
+            float om = fmaxf(fmaxf(lo + myq, -myq - hi), 0.f);
+            cp = o * o; cm = om * om;
+        } else if (lane < 7 && MK == MPTG_METRIC_SE3) {
+            float o = fmaxf(fmaxf(lo - myq, myq - hi), 0.f);
+            tt = o * o;
+        }
+        cp = warp_sum16(cp);
+        cm = warp_sum16(cm);
+        float rot = 2.f * asinf(fminf(1.f, 0.5f * sqrtf(fminf(cp, cm))));
+        if constexpr (MK == MPTG_METRIC_SO3) {
+            return rot;
+        } else {
+            tt = warp_sum16(tt);
+            return t.w0f * rot + t.w1f * sqrtf(tt);
+        }
+    }
+}
+
+// Candidate step shared by the tree and the linear scan: each lane holds one
+// point (id pid, FP32 distance d32).  Every point that could beat or tie the
+// current best in exact arithmetic is re-ranked in FP64.
+__device__ __forceinline__ void rerank_step(const TreeView& t, const double* __restrict__ qd, int lane, bool have,
+                                            int pid, float d32, float E, double& best, int& bidx, float& bestf_up,
+                                            unsigned long long& nrerank) {
+    float m = d32;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    float thr = __fadd_ru(m, __fmul_ru(2.f, E));
+    bool cand = have && __fsub_rd(d32, E) <= bestf_up && d32 <= thr;
+    unsigned cm = __ballot_sync(0xffffffffu, cand);
+    if (!cm) return;
+    nrerank += __popc(cm);
+    double dd = INFINITY;
+    int pp = INT_MAX;
+    if (cand) {
+        dd = dist64(t.metric, t.D, t.w0, t.w1, qd, t.states64 + (size_t)pid * t.D);
+        pp = pid;
+        if (!(dd == dd)) { dd = INFINITY; pp = INT_MAX; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        double od = __shfl_xor_sync(0xffffffffu, dd, o);
+        int op = __shfl_xor_sync(0xffffffffu, pp, o);
+        if (od < dd || (od == dd && op < pp)) { dd = od; pp = op; }
+    }
+    if (pp != INT_MAX && (dd < best || (dd == best && pp < bidx))) {
+        best = dd;
+        bidx = pp;
+        bestf_up = __double2float_ru(best);
+    }
+}
+
+template <int MK, int DMAX>
+__device__ __forceinline__ void load_query(const double* __restrict__ qd, int D, int lane, float (&q)[DMAX],
+                                           float& myq, float& M, const TreeView& t) {
+    M = __int_as_float(t.dcnt[CNT_MAXABS]);
+#pragma unroll
+    for (int d = 0; d < DMAX; ++d) {
+        float v = 0.f;
+        if (d < D) v = __double2float_rn(qd[d]);
+        q[d] = v;
+        bool lp = MK == MPTG_METRIC_L2 || MK == MPTG_METRIC_L1 || (MK == MPTG_METRIC_SE3 && d >= 4 && d < 7);
+        if (lp && d < D) M = fmaxf(M, __double2float_ru(fabs(qd[d])));
+    }
+    myq = 0.f;
+#pragma unroll
+    for (int d = 0; d < DMAX; ++d)
+        if (lane == d) myq = q[d];
+}
+
+template <int MK, int DMAX>
+__global__ void __launch_bounds__(256) k_nearest(TreeView t, const double* __restrict__ q64, int nq,
+                                                 int* __restrict__ out_idx, double* __restrict__ out_d) {
+    const int lane = threadIdx.x & 31;
+    const int qi = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    if (qi >= nq) return;
+    const int D = t.D;
+    const double* qd = q64 + (size_t)qi * D;
+    float q[DMAX];
+    float myq, M;
+    load_query<MK, DMAX>(qd, D, lane, q, myq, M, t);
+    const float E = err32<MK>(D, M, t.w0f, t.w1f);
+
+    double best = INFINITY;
+    int bidx = INT_MAX;
+    float bestf_up = INFINITY;
+    unsigned long long n_int = 0, n_leaf = 0, n_pts = 0, n_rr = 0;
+
+    int sp = 0;
+    int s0n = 0, s1n = 0;
+    float s0l = 0.f, s1l = 0.f;
+    int node = 0;
+    while (true) {
+        int4 nd = __ldg(&t.nodes[node]);
+        if (nd.x >= 0) {
+            ++n_int;
+            float qv = __shfl_sync(0xffffffffu, myq, nd.x);
+            float split = __int_as_float(nd.z);
+            int nearc = qv < split ? nd.y : nd.y + 1;
+            int farc = 2 * nd.y + 1 - nearc;
+            float lb = cell_lb<MK>(t, farc, myq, lane);
+            // the builder keeps depth <= MPTG_MAX_DEPTH < 64, so the stack never fills
+            if (__fsub_rd(lb, E) <= bestf_up && sp < 64) {
+                if (sp < 32) {
+                    if (lane == sp) { s0n = farc; s0l = lb; }
+                } else {
+                    if (lane == sp - 32) { s1n = farc; s1l = lb; }
+                }
+                ++sp;
+            }
+            node = nearc;
+            continue;
+        }
+        // leaf
+        ++n_leaf;
+        int cnt = nd.w < MPTG_BUCKET ? nd.w : MPTG_BUCKET;
+        n_pts += cnt;
+        bool have = lane < cnt;
+        float d32 = INFINITY;
+        int pid = -1;
+        if (have) {
+            size_t b = (size_t)nd.y;
+            pid = __ldg(&t.bids[b * MPTG_BUCKET + lane]);
+            float p[DMAX];
+#pragma unroll
+            for (int d = 0; d < DMAX; ++d) p[d] = d < D ? __ldg(&t.bpts[(b * D + d) * MPTG_BUCKET + lane]) : 0.f;
+            d32 = dist32<MK, DMAX>(q, p, t.w0f, t.w1f);
+            if (!(d32 == d32)) d32 = INFINITY;
+        }
+        rerank_step(t, qd, lane, have, pid, d32, E, best, bidx, bestf_up, n_rr);
+        // pop the next far child whose bound can still beat the best
+        bool found = false;
+        while (sp > 0) {
+            --sp;
+            int src = sp & 31;
+            int nn;
+            float lb;
+            if (sp < 32) { nn = __shfl_sync(0xffffffffu, s0n, src); lb = __shfl_sync(0xffffffffu, s0l, src); }
+            else { nn = __shfl_sync(0xffffffffu, s1n, src); lb = __shfl_sync(0xffffffffu, s1l, src); }
+            if (__fsub_rd(lb, E) <= bestf_up) { node = nn; found = true; break; }
+        }
+        if (!found) break;
+    }
+    if (lane == 0) {
+        out_idx[qi] = bidx == INT_MAX ? -1 : bidx;
+        out_d[qi] = best;
+        if (t.stats) {
+            atomicAdd(&t.stats[0], 1ull);
+            atomicAdd(&t.stats[1], n_int);
+            atomicAdd(&t.stats[2], n_leaf);
+            atomicAdd(&t.stats[3], n_pts);
+            atomicAdd(&t.stats[4], n_rr);
+        }
+    }
+}
+
+// exhaustive scan (nigh::Linear): warp per query, 32 points per step
+template <int MK, int DMAX>
+__global__ void __launch_bounds__(256) k_nearest_linear(TreeView t, const double* __restrict__ q64, int nq,
+                                                        int* __restrict__ out_idx, double* __restrict__ out_d) {
+    const int lane = threadIdx.x & 31;
+    const int qi = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    if (qi >= nq) return;
+    const int D = t.D;
+    const double* qd = q64 + (size_t)qi * D;
+    float q[DMAX];
+    float myq, M;
+    load_query<MK, DMAX>(qd, D, lane, q, myq, M, t);
+    const float E = err32<MK>(D, M, t.w0f, t.w1f);
+    double best = INFINITY;
+    int bidx = INT_MAX;
+    float bestf_up = INFINITY;
+    unsigned long long nrr = 0;
+    for (int base = 0; base < t.n; base += 32) {
+        int j = base + lane;
+        bool have = j < t.n;
+        float d32 = INFINITY;
+        if (have) {
+            float p[DMAX];
+#pragma unroll
+            for (int d = 0; d < DMAX; ++d) p[d] = d < D ? t.pts32[(size_t)j * D + d] : 0.f;
+            d32 = dist32<MK, DMAX>(q, p, t.w0f, t.w1f);
+            if (!(d32 == d32)) d32 = INFINITY;
+        }
+        rerank_step(t, qd, lane, have, j, d32, E, best, bidx, bestf_up, nrr);
+    }
+    if (lane == 0) {
+        out_idx[qi] = bidx == INT_MAX ? -1 : bidx;
+        out_d[qi] = best;
+    }
+}
+
+// ------------------------------------------------------------------ k-NN
+
+// Exact k nearest (k <= 64) sorted by (distance, id), warp per query.  The
+// running list lives in registers: entry j in lane j (j < 32) / lane j-32 of
+// the second slot.  tau = the k-th best exact distance (or the radius).
+template <int MK, int DMAX>
+__global__ void __launch_bounds__(256) k_nearest_k(TreeView t, const double* __restrict__ q64, int nq, int k,
+                                                   double radius, int* __restrict__ out_idx,
+                                                   double* __restrict__ out_d) {
+    const int lane = threadIdx.x & 31;
+    const int qi = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    if (qi >= nq) return;
+    const int D = t.D;
+    const double* qd = q64 + (size_t)qi * D;
+    float q[DMAX];
+    float myq, M;
+    load_query<MK, DMAX>(qd, D, lane, q, myq, M, t);
+    const float E = err32<MK>(D, M, t.w0f, t.w1f);
+    // sorted list: (d, id) in two register slots
+    double ld0 = INFINITY, ld1 = INFINITY;
+    int li0 = INT_MAX, li1 = INT_MAX;
+    int cnt = 0;
+    double tau = radius;  // prune bound: k-th distance once full, else radius
+    float tauf = __double2float_ru(tau);
+
+    int sp = 0;
+    int s0n = 0, s1n = 0;
+    float s0l = 0.f, s1l = 0.f;
+    int node = 0;
+    while (true) {
+        int4 nd = __ldg(&t.nodes[node]);
+        if (nd.x >= 0) {
+            float qv = __shfl_sync(0xffffffffu, myq, nd.x);
+            float split = __int_as_float(nd.z);
+            int nearc = qv < split ? nd.y : nd.y + 1;
+            int farc = 2 * nd.y + 1 - nearc;
+            float lb = cell_lb<MK>(t, farc, myq, lane);
+            if (__fsub_rd(lb, E) <= tauf && sp < 64) {
+                if (sp < 32) { if (lane == sp) { s0n = farc; s0l = lb; } }
+                else if (lane == sp - 32) { s1n = farc; s1l = lb; }
+                ++sp;
+            }
+            node = nearc;
+            continue;
+        }
+        int c = nd.w < MPTG_BUCKET ? nd.w : MPTG_BUCKET;
+        bool have = lane < c;
+        float d32 = INFINITY;
+        int pid = -1;
+        if (have) {
+            size_t b = (size_t)nd.y;
+            pid = __ldg(&t.bids[b * MPTG_BUCKET + lane]);
+            float p[DMAX];
+#pragma unroll
+            for (int d = 0; d < DMAX; ++d) p[d] = d < D ? __ldg(&t.bpts[(b * D + d) * MPTG_BUCKET + lane]) : 0.f;
+            d32 = dist32<MK, DMAX>(q, p, t.w0f, t.w1f);
+            if (!(d32 == d32)) d32 = INFINITY;
+        }
+        bool cand = have && __fsub_rd(d32, E) <= tauf;
+        double dd = INFINITY;
+        if (cand) {
+            dd = dist64(t.metric, D, t.w0, t.w1, qd, t.states64 + (size_t)pid * D);
+            cand = dd <= tau;
+        }
+        unsigned cmask = __ballot_sync(0xffffffffu, cand);
+        while (cmask) {
+            int src = __ffs(cmask) - 1;
+            cmask &= cmask - 1;
+            double cd = __shfl_sync(0xffffffffu, dd, src);
+            int ci = __shfl_sync(0xffffffffu, pid, src);
+            // insert (cd, ci) into the sorted list if it ranks among the k best
+            if (cnt == k) {
+                double kd = (k - 1) < 32 ? __shfl_sync(0xffffffffu, ld0, k - 1) : __shfl_sync(0xffffffffu, ld1, k - 33);
+                int ki = (k - 1) < 32 ? __shfl_sync(0xffffffffu, li0, k - 1) : __shfl_sync(0xffffffffu, li1, k - 33);
+                if (!(cd < kd || (cd == kd && ci < ki))) continue;
+            }
+            // rank position = number of entries strictly ahead of (cd, ci)
+            bool ahead0 = lane < cnt && (ld0 < cd || (ld0 == cd && li0 < ci));
+            bool ahead1 = lane + 32 < cnt && (ld1 < cd || (ld1 == cd && li1 < ci));
+            int pos = __popc(__ballot_sync(0xffffffffu, ahead0)) + __popc(__ballot_sync(0xffffffffu, ahead1));
+            // shift entries at >= pos one place back
+            double p0d = __shfl_up_sync(0xffffffffu, ld0, 1);
+            int p0i = __shfl_up_sync(0xffffffffu, li0, 1);
+            double p1d = __shfl_up_sync(0xffffffffu, ld1, 1);
+            int p1i = __shfl_up_sync(0xffffffffu, li1, 1);
+            double last0d = __shfl_sync(0xffffffffu, ld0, 31);
+            int last0i = __shfl_sync(0xffffffffu, li0, 31);
+            if (lane == 0) { p1d = last0d; p1i = last0i; }
+            // slot 0 entries (index = lane)
+            if (lane > pos) { ld0 = p0d; li0 = p0i; }
+            else if (lane == pos) { ld0 = cd; li0 = ci; }
+            int j1 = lane + 32;
+            if (j1 > pos) { ld1 = p1d; li1 = p1i; }
+            else if (j1 == pos) { ld1 = cd; li1 = ci; }
+            if (cnt < k) ++cnt;
+            if (cnt == k) {
+                double kd = (k - 1) < 32 ? __shfl_sync(0xffffffffu, ld0, k - 1) : __shfl_sync(0xffffffffu, ld1, k - 33);
+                tau = fmin(kd, radius);
+                tauf = __double2float_ru(tau);
+            }
+        }
+        bool found = false;
+        while (sp > 0) {
+            --sp;
+            int src = sp & 31;
+            int nn;
+            float lb;
+            if (sp < 32) { nn = __shfl_sync(0xffffffffu, s0n, src); lb = __shfl_sync(0xffffffffu, s0l, src); }
+            else { nn = __shfl_sync(0xffffffffu, s1n, src); lb = __shfl_sync(0xffffffffu, s1l, src); }
+            if (__fsub_rd(lb, E) <= tauf) { node = nn; found = true; break; }
+        }
+        if (!found) break;
+    }
+    int* oi = out_idx + (size_t)qi * k;
+    double* od = out_d + (size_t)qi * k;
+    if (lane < k) { bool v = lane < cnt; oi[lane] = v ? li0 : -1; od[lane] = v ? ld0 : INFINITY; }
+    if (lane + 32 < k) { bool v = lane + 32 < cnt; oi[lane + 32] = v ? li1 : -1; od[lane + 32] = v ? ld1 : INFINITY; }
+}
+
+// ------------------------------------------------------------------ host side
+
+#define DISPATCH_METRIC(metric, D, KERNEL, grid, block, stream, ...)                                      \
+    do {                                                                                                \
+        switch (metric) {                                                                               \
+        case MPTG_METRIC_L2:                                                                            \
+            if (D <= 2) KERNEL<MPTG_METRIC_L2, 2><<<grid, block, 0, stream>>>(__VA_ARGS__);             \
+            else if (D <= 4) KERNEL<MPTG_METRIC_L2, 4><<<grid, block, 0, stream>>>(__VA_ARGS__);        \
+            else if (D <= 8) KERNEL<MPTG_METRIC_L2, 8><<<grid, block, 0, stream>>>(__VA_ARGS__);        \
+            else KERNEL<MPTG_METRIC_L2, 16><<<grid, block, 0, stream>>>(__VA_ARGS__);                   \
+            break;                                                                                      \
+        case MPTG_METRIC_L1:                                                                            \
+            if (D <= 2) KERNEL<MPTG_METRIC_L1, 2><<<grid, block, 0, stream>>>(__VA_ARGS__);             \
+            else if (D <= 4) KERNEL<MPTG_METRIC_L1, 4><<<grid, block, 0, stream>>>(__VA_ARGS__);        \
+            else if (D <= 8) KERNEL<MPTG_METRIC_L1, 8><<<grid, block, 0, stream>>>(__VA_ARGS__);        \
+            else KERNEL<MPTG_METRIC_L1, 16><<<grid, block, 0, stream>>>(__VA_ARGS__);                   \
+            break;                                                                                      \
+        case MPTG_METRIC_SO2:                                                                           \
+            if (D <= 2) KERNEL<MPTG_METRIC_SO2, 2><<<grid, block, 0, stream>>>(__VA_ARGS__);            \
+            else if (D <= 4) KERNEL<MPTG_METRIC_SO2, 4><<<grid, block, 0, stream>>>(__VA_ARGS__);       \
+            else if (D <= 8) KERNEL<MPTG_METRIC_SO2, 8><<<grid, block, 0, stream>>>(__VA_ARGS__);       \
+            else KERNEL<MPTG_METRIC_SO2, 16><<<grid, block, 0, stream>>>(__VA_ARGS__);                  \
+            break;                                                                                      \
+        case MPTG_METRIC_SO3: KERNEL<MPTG_METRIC_SO3, 4><<<grid, block, 0, stream>>>(__VA_ARGS__); break; \
+        case MPTG_METRIC_SE3: KERNEL<MPTG_METRIC_SE3, 8><<<grid, block, 0, stream>>>(__VA_ARGS__); break; \
+        }                                                                                               \
+    } while (0)
+
+static void tree_free(mptg_tree* t) {
+    void* ptrs[] = {t->states64, t->pts32, t->nodes, t->cell_lo, t->cell_hi, t->node_depth, t->bpts, t->bids,
+                    t->dcnt, t->dstats, t->perm, t->perm2, t->pseg, t->pseg2, t->segA, t->segB, t->seg_box,
+                    t->leaf_of, t->ovf_pts, t->ovf_leaf, t->leaf_reg, t->seg_cursor};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (t->hcnt) cudaFreeHost(t->hcnt);
+    delete t;
+}
+
+extern "C" {
+
+mptg_status mptg_tree_create(mptg_ctx* ctx, mptg_metric metric, int dim, const double* weights, size_t capacity,
+                             mptg_tree** out) {
+    if (!ctx || !out) return MPTG_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (metric < MPTG_METRIC_L2 || metric > MPTG_METRIC_L1)
+        return mptg_fail(ctx, MPTG_ERR_UNSUPPORTED_METRIC, "unknown metric %d", (int)metric);
+    if (metric == MPTG_METRIC_SO3 && dim != 4) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "SO3 needs dim 4");
+    if (metric == MPTG_METRIC_SE3 && dim != 7) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "SE3 needs dim 7");
+    if (dim < 1 || dim > MPTG_MAX_DIM) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "dim %d out of [1,16]", dim);
+    if (capacity < 1 || capacity > (size_t)1 << 30)
+        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "capacity %zu out of range", capacity);
+    MPTG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    mptg_tree* t = new mptg_tree();
+    t->ctx = ctx;
+    t->metric = metric;
+    t->D = dim;
+    if (weights) { t->w0 = weights[0]; t->w1 = weights[1]; }
+    if (metric == MPTG_METRIC_SE3 && !(t->w0 > 0 && t->w1 > 0)) {
+        delete t;
+        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "SE3 weights must be positive");
+    }
+    t->cap = capacity;
+    t->bucket_cap = (int)(capacity / 2 + 1024);
+    t->node_cap = 2 * t->bucket_cap + 16;
+    t->seg_cap = (int)(capacity / 16 + 1024);
+    size_t N = capacity, D = dim;
+    cudaError_t e = cudaSuccess;
+#define ALLOC(ptr, bytes) if (e == cudaSuccess) e = cudaMalloc((void**)&(ptr), (bytes))
+    ALLOC(t->states64, N * D * sizeof(double));
+    ALLOC(t->pts32, N * D * sizeof(float));
+    ALLOC(t->nodes, (size_t)t->node_cap * sizeof(int4));
+    ALLOC(t->cell_lo, (size_t)t->node_cap * D * sizeof(float));
+    ALLOC(t->cell_hi, (size_t)t->node_cap * D * sizeof(float));
+    ALLOC(t->node_depth, (size_t)t->node_cap * sizeof(int));
+    ALLOC(t->bpts, (size_t)t->bucket_cap * D * MPTG_BUCKET * sizeof(float));
+    ALLOC(t->bids, (size_t)t->bucket_cap * MPTG_BUCKET * sizeof(int));
+    ALLOC(t->dcnt, CNT_N * sizeof(int));
+    ALLOC(t->dstats, 8 * sizeof(unsigned long long));
+    ALLOC(t->perm, N * sizeof(int));
+    ALLOC(t->perm2, N * sizeof(int));
+    ALLOC(t->pseg, N * sizeof(int));
+    ALLOC(t->pseg2, N * sizeof(int));
+    ALLOC(t->segA, (size_t)t->seg_cap * sizeof(SegState));
+    ALLOC(t->segB, (size_t)t->seg_cap * sizeof(SegState));
+    ALLOC(t->seg_box, (size_t)t->seg_cap * 2 * D * sizeof(int));
+    ALLOC(t->leaf_of, N * sizeof(int));
+    ALLOC(t->ovf_pts, N * sizeof(int));
+    ALLOC(t->ovf_leaf, N * sizeof(int));
+    ALLOC(t->leaf_reg, (size_t)t->node_cap * sizeof(int));
+    ALLOC(t->seg_cursor, (size_t)t->seg_cap * sizeof(int));
+#undef ALLOC
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&t->hcnt, CNT_N * sizeof(int));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        tree_free(t);
+        return mptg_fail(ctx, MPTG_ERR_OOM, "tree allocation failed: %s", cudaGetErrorString(e));
+    }
+    // root = empty leaf on bucket 0; root cell = the metric's domain
+    int hc[CNT_N] = {1, 1, 0, 0, 0, 0, 0, 0};
+    int4 root = make_int4(-1, 0, 0, 0);
+    std::vector<float> lo(D), hi(D);
+    for (size_t d = 0; d < D; ++d) {
+        lo[d] = -INFINITY; hi[d] = INFINITY;
+        if (metric == MPTG_METRIC_SO2) { lo[d] = -PI_F; hi[d] = PI_F; }
+        if ((metric == MPTG_METRIC_SO3 || metric == MPTG_METRIC_SE3) && d < 4) { lo[d] = -1.f; hi[d] = 1.f; }
+    }
+    // -pi/pi as floats may round inward of the double range: widen by one ulp
+    for (size_t d = 0; d < D; ++d) {
+        if (metric == MPTG_METRIC_SO2) { lo[d] = nextafterf(lo[d], -INFINITY); hi[d] = nextafterf(hi[d], INFINITY); }
+    }
+    int zero = 0;
+    e = cudaMemcpy(t->dcnt, hc, sizeof(hc), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(t->nodes, &root, sizeof(root), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(t->cell_lo, lo.data(), D * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(t->cell_hi, hi.data(), D * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(t->node_depth, &zero, sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(t->dstats, 0, 8 * sizeof(unsigned long long));
+    if (e != cudaSuccess) {
+        tree_free(t);
+        return mptg_fail(ctx, MPTG_ERR_CUDA, "tree init failed: %s", cudaGetErrorString(e));
+    }
+    *out = t;
+    return MPTG_OK;
+}
+
+mptg_status mptg_tree_destroy(mptg_tree* t) {
+    if (!t) return MPTG_ERR_INVALID_ARG;
+    cudaDeviceSynchronize();
+    tree_free(t);
+    return MPTG_OK;
+}
+
+mptg_status mptg_tree_size(mptg_tree* t, size_t* n) {
+    if (!t || !n) return MPTG_ERR_INVALID_ARG;
+    *n = t->n;
+    return MPTG_OK;
+}
+
+static mptg_status read_counters(mptg_tree* t, cudaStream_t s) {
+    mptg_ctx* ctx = t->ctx;
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(t->hcnt, t->dcnt, CNT_N * sizeof(int), cudaMemcpyDeviceToHost, s));
+    MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    return MPTG_OK;
+}
+
+mptg_status mptg_tree_insert(mptg_tree* t, const double* states, size_t n, void* stream) {
+    if (!t) return MPTG_ERR_INVALID_ARG;
+    mptg_ctx* ctx = t->ctx;
+    if (n == 0) return MPTG_OK;
+    if (!states) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "null states");
+    if (t->n + n > t->cap) return mptg_fail(ctx, MPTG_ERR_CAPACITY, "tree capacity %zu exceeded", t->cap);
+    cudaStream_t s = (cudaStream_t)stream;
+    const int D = t->D;
+    const int first = (int)t->n;
+    const int nn = (int)n;
+    MPTG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(t->states64 + (size_t)first * D, states, n * D * sizeof(double),
+                                       cudaMemcpyDefault, s));
+    // clear per-insert counters and the error word
+    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(t->dcnt + CNT_ERR, 0, 4 * sizeof(int), s));
+    k_convert<<<mptg_blocks(n, 256), 256, 0, s>>>(t->states64 + (size_t)first * D, t->pts32 + (size_t)first * D, nn,
+                                                  D, t->metric, t->dcnt);
+    MPTG_LAUNCHED(ctx);
+    mptg_status st = read_counters(t, s);
+    if (st) return st;
+    if (t->hcnt[CNT_ERR] & MPTG_DEVERR_BAD_STATE)
+        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG,
+                         "invalid state (NaN/inf, SO2 angle outside [-pi,pi], or non-unit quaternion)");
+    k_locate<<<mptg_blocks(n, 256), 256, 0, s>>>(t->nodes, t->pts32, first, nn, D, t->leaf_of);
+    k_append<<<mptg_blocks(n, 256), 256, 0, s>>>(t->nodes, t->pts32, t->bpts, t->bids, first, nn, D, t->leaf_of,
+                                                 t->dcnt, t->ovf_pts, t->ovf_leaf, t->leaf_reg);
+    ctx->launches += 2;
+    st = read_counters(t, s);
+    if (st) return st;
+    int nreg = t->hcnt[CNT_NREG];
+    int novf = t->hcnt[CNT_OVF];
+    if (nreg > 0) {
+        if (nreg > t->seg_cap) return mptg_fail(ctx, MPTG_ERR_CAPACITY, "too many overflowing leaves");
+        k_ovf_segs<<<mptg_blocks(nreg, 128), 128, 0, s>>>(t->nodes, t->bids, t->node_depth, nreg, t->ovf_leaf,
+                                                          t->dcnt, t->segA, t->perm, t->pseg, t->seg_cursor);
+        k_ovf_scatter<<<mptg_blocks(novf, 256), 256, 0, s>>>(novf, first, t->ovf_pts, t->leaf_of, t->leaf_reg,
+                                                             t->segA, t->seg_cursor, t->perm, t->pseg);
+        ctx->launches += 2;
+        int total = MPTG_BUCKET * nreg + novf;
+        int nseg = nreg;
+        SegState* cur = t->segA;
+        SegState* prev = t->segB;
+        int* perm = t->perm; int* perm2 = t->perm2; int* pseg = t->pseg; int* pseg2 = t->pseg2;
+        const unsigned tb = 256;
+        for (int level = 0; nseg > 0 && level < 4 * MPTG_MAX_DEPTH; ++level) {
+            MPTG_CUDA_TRY(ctx, cudaMemsetAsync(t->dcnt + CNT_NSEG_NEXT, 0, sizeof(int), s));
+            k_seg_a<<<mptg_blocks(nseg, 128), 128, 0, s>>>(cur, nseg, prev, t->nodes, t->dcnt, t->bucket_cap,
+                                                           t->seg_box, D);
+            k_seg_b<<<mptg_blocks(total, tb), tb, 0, s>>>(cur, perm, pseg, pseg2, total, t->pts32, D, t->bpts,
+                                                          t->bids, t->seg_box);
+            k_seg_c<<<mptg_blocks(nseg, 128), 128, 0, s>>>(cur, nseg, prev, t->nodes, t->cell_lo, t->cell_hi,
+                                                           t->node_depth, t->dcnt, t->node_cap, t->seg_cap,
+                                                           t->seg_box, D, t->metric, (float)t->w0, (float)t->w1);
+            k_seg_d<<<mptg_blocks(total, tb), tb, 0, s>>>(cur, perm, pseg, perm2, pseg2, total, t->pts32, D);
+            ctx->launches += 4;
+            st = read_counters(t, s);
+            if (st) return st;
+            nseg = t->hcnt[CNT_NSEG_NEXT];
+            if (nseg > t->seg_cap || (t->hcnt[CNT_ERR] & MPTG_DEVERR_CAPACITY))
+                return mptg_fail(ctx, MPTG_ERR_CAPACITY, "kd-tree build ran out of node/segment capacity");
+            // next level: the children just written to `prev` become current
+            SegState* tmp = cur; cur = prev; prev = tmp;
+            int* tp = perm; perm = perm2; perm2 = tp;
+            tp = pseg; pseg = pseg2; pseg2 = tp;
+        }
+        if (nseg > 0) return mptg_fail(ctx, MPTG_ERR_CAPACITY, "kd-tree build did not converge");
+    }
+    MPTG_CUDA_TRY(ctx, cudaGetLastError());
+    st = read_counters(t, s);
+    if (st) return st;
+    int err = t->hcnt[CNT_ERR];
+    t->n += n;  // points are stored even when the tree reports a structural error
+    if (err & MPTG_DEVERR_CAPACITY) return mptg_fail(ctx, MPTG_ERR_CAPACITY, "kd-tree node/bucket capacity exceeded");
+    if (err & MPTG_DEVERR_DEPTH) return mptg_fail(ctx, MPTG_ERR_CAPACITY, "kd-tree depth limit reached");
+    return MPTG_OK;
+}
+
+mptg_status mptg_tree_states(mptg_tree* t, size_t first, size_t n, double* out, void* stream) {
+    if (!t || (!out && n)) return MPTG_ERR_INVALID_ARG;
+    if (first + n > t->n) return mptg_fail(t->ctx, MPTG_ERR_INVALID_ARG, "range beyond tree size");
+    cudaStream_t s = (cudaStream_t)stream;
+    MPTG_CUDA_TRY(t->ctx, cudaMemcpyAsync(out, t->states64 + first * t->D, n * t->D * sizeof(double),
+                                          cudaMemcpyDefault, s));
+    if (!mptg_is_device_ptr(out)) MPTG_CUDA_TRY(t->ctx, cudaStreamSynchronize(s));
+    return MPTG_OK;
+}
+
+mptg_status mptg_tree_counters(mptg_tree* t, uint64_t out[5], int reset) {
+    if (!t || !out) return MPTG_ERR_INVALID_ARG;
+    unsigned long long h[8];
+    MPTG_CUDA_TRY(t->ctx, cudaDeviceSynchronize());
+    MPTG_CUDA_TRY(t->ctx, cudaMemcpy(h, t->dstats, sizeof(h), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < 5; ++i) out[i] = h[i];
+    if (reset) MPTG_CUDA_TRY(t->ctx, cudaMemset(t->dstats, 0, sizeof(h)));
+    return MPTG_OK;
+}
+
+// internal: launch the 1-NN search on device buffers (used by the planner too)
+mptg_status mptg_tree_nearest_dev(mptg_tree* t, const double* dq, int nq, int* didx, double* dd, cudaStream_t s,
+                                  bool count) {
+    if (nq <= 0) return MPTG_OK;
+    TreeView v = view_of(t);
+    if (!count) v.stats = nullptr;
+    unsigned grid = mptg_blocks((size_t)nq * 32, 256);
+    DISPATCH_METRIC(t->metric, t->D, k_nearest, grid, 256, s, v, dq, nq, didx, dd);
+    MPTG_LAUNCHED(t->ctx);
+    return MPTG_OK;
+}
+
+mptg_status mptg_nearest(mptg_tree* t, const double* q, size_t nq, int32_t* idx, double* dist, void* stream) {
+    if (!t) return MPTG_ERR_INVALID_ARG;
+    mptg_ctx* ctx = t->ctx;
+    if (nq == 0) return MPTG_OK;
+    if (!q || !idx || !dist) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "null buffer");
+    if (nq > (size_t)INT32_MAX / 32) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "too many queries");
+    cudaStream_t s = (cudaStream_t)stream;
+    DevBuf bq, bi, bd;
+    mptg_status st;
+    if ((st = mptg_stage_in(ctx, q, nq * t->D * sizeof(double), s, &bq))) return st;
+    if ((st = mptg_stage_out_alloc(ctx, idx, nq * sizeof(int32_t), s, &bi))) return st;
+    if ((st = mptg_stage_out_alloc(ctx, dist, nq * sizeof(double), s, &bd))) return st;
+    mptg_tree_nearest_dev(t, (const double*)bq.dptr, (int)nq, (int*)bi.dptr, (double*)bd.dptr, s, true);
+    MPTG_CUDA_TRY(ctx, cudaGetLastError());
+    DevBuf outs[2] = {bi, bd};
+    return mptg_stage_finish(ctx, s, outs, 2, &bq, 1);
+}
+
+mptg_status mptg_nearest_linear(mptg_tree* t, const double* q, size_t nq, int32_t* idx, double* dist,
+                                void* stream) {
+    if (!t) return MPTG_ERR_INVALID_ARG;
+    mptg_ctx* ctx = t->ctx;
+    if (nq == 0) return MPTG_OK;
+    if (!q || !idx || !dist) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "null buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    DevBuf bq, bi, bd;
+    mptg_status st;
+    if ((st = mptg_stage_in(ctx, q, nq * t->D * sizeof(double), s, &bq))) return st;
+    if ((st = mptg_stage_out_alloc(ctx, idx, nq * sizeof(int32_t), s, &bi))) return st;
+    if ((st = mptg_stage_out_alloc(ctx, dist, nq * sizeof(double), s, &bd))) return st;
+    TreeView v = view_of(t);
+    unsigned grid = mptg_blocks(nq * 32, 256);
+    DISPATCH_METRIC(t->metric, t->D, k_nearest_linear, grid, 256, s, v, (const double*)bq.dptr, (int)nq,
+                    (int*)bi.dptr, (double*)bd.dptr);
+    MPTG_LAUNCHED(ctx);
+    MPTG_CUDA_TRY(ctx, cudaGetLastError());
+    DevBuf outs[2] = {bi, bd};
+    return mptg_stage_finish(ctx, s, outs, 2, &bq, 1);
+}
+
+mptg_status mptg_nearest_k(mptg_tree* t, const double* q, size_t nq, int k, double r, int32_t* idx, double* dist,
+                           void* stream) {
+    if (!t) return MPTG_ERR_INVALID_ARG;
+    mptg_ctx* ctx = t->ctx;
+    if (k < 1 || k > 64) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "k=%d outside [1,64]", k);
+    if (nq == 0) return MPTG_OK;
+    if (!q || !idx || !dist) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "null buffer");
+    if (!(r > 0)) r = INFINITY;
+    cudaStream_t s = (cudaStream_t)stream;
+    DevBuf bq, bi, bd;
+    mptg_status st;
+    if ((st = mptg_stage_in(ctx, q, nq * t->D * sizeof(double), s, &bq))) return st;
+    if ((st = mptg_stage_out_alloc(ctx, idx, nq * k * sizeof(int32_t), s, &bi))) return st;
+    if ((st = mptg_stage_out_alloc(ctx, dist, nq * k * sizeof(double), s, &bd))) return st;
+    TreeView v = view_of(t);
+    unsigned grid = mptg_blocks(nq * 32, 256);
+    DISPATCH_METRIC(t->metric, t->D, k_nearest_k, grid, 256, s, v, (const double*)bq.dptr, (int)nq, k, r,
+                    (int*)bi.dptr, (double*)bd.dptr);
+    MPTG_LAUNCHED(ctx);
+    MPTG_CUDA_TRY(ctx, cudaGetLastError());
+    DevBuf outs[2] = {bi, bd};
+    return mptg_stage_finish(ctx, s, outs, 2, &bq, 1);
+}
+
+}  // extern "C"

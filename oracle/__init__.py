@@ -1,0 +1,231 @@
+"""CPU oracle for the MPT planner hot path -- TEST INFRASTRUCTURE ONLY.
+
+This package is the checker.  Only ``tests/``, ``__graft_entry__.smoke()`` and
+``bench.py``'s CPU-baseline / reference legs may import it; the ``mpt_gb300``
+product never imports, links or calls anything here.
+
+``oracle.c`` restates the reference algorithms in plain C (each function cites
+the reference file:line it follows) and is built into ``oracle/_build/liborc.so``
+with ``-O2 -ffp-contract=off -fopenmp``.  ``ref/`` builds the reference's own
+DiscreteMotionValidator / GoalState headers against a project-written nigh
+stand-in into ``oracle/_ref/`` (only where the reference sources are present).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "liborc.so")
+ROOT = os.path.dirname(HERE)
+
+L2, SO2, SO3, SE3, L1 = 0, 1, 2, 3, 4
+
+
+def build(force: bool = False) -> str:
+    """Compile oracle.c into _build/liborc.so (gcc, OpenMP, no FP contraction)."""
+    src = os.path.join(HERE, "oracle.c")
+    hdrs = [os.path.join(HERE, "oracle.h"), os.path.join(ROOT, "include", "mptg_detmath.h")]
+    if not force and os.path.exists(LIB_PATH):
+        mt = os.path.getmtime(LIB_PATH)
+        if all(os.path.getmtime(p) <= mt for p in [src] + hdrs):
+            return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    tmp = LIB_PATH + ".tmp%d" % os.getpid()
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
+           "-std=c11", "-o", tmp, src, "-lm"]
+    subprocess.check_call(cmd)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+class Space(ctypes.Structure):
+    _fields_ = [("metric", ctypes.c_int), ("dim", ctypes.c_int), ("w", ctypes.c_double * 2)]
+
+
+class Scene(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int),
+        ("grid", ctypes.c_void_p), ("width", ctypes.c_int), ("height", ctypes.c_int),
+        ("nlinks", ctypes.c_int), ("link_len", ctypes.c_void_p), ("ndiscs", ctypes.c_int),
+        ("discs", ctypes.c_void_p), ("robot_radius", ctypes.c_double), ("self_collision", ctypes.c_int),
+        ("nrobot", ctypes.c_int64), ("robot_tris", ctypes.c_void_p), ("nenv", ctypes.c_int64),
+        ("env_tris", ctypes.c_void_p),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build()
+        L = ctypes.CDLL(path)
+        P = ctypes.c_void_p
+        L.orc_distance.restype = ctypes.c_double
+        L.orc_distance.argtypes = [P, P, P]
+        L.orc_interpolate.argtypes = [P, P, P, ctypes.c_double, P]
+        L.orc_so2_ccw.restype = ctypes.c_double
+        L.orc_so2_ccw.argtypes = [ctypes.c_double, ctypes.c_double]
+        L.orc_so2_bound.restype = ctypes.c_double
+        L.orc_so2_bound.argtypes = [ctypes.c_double]
+        L.orc_nn_brute.argtypes = [P, P, ctypes.c_int64, P, ctypes.c_int64, P, P, ctypes.c_int]
+        L.orc_knn_brute.argtypes = [P, P, ctypes.c_int64, P, ctypes.c_int64, ctypes.c_int, P, P, ctypes.c_int]
+        L.orc_kd_build.restype = P
+        L.orc_kd_build.argtypes = [P, P, ctypes.c_int64, ctypes.c_int]
+        L.orc_kd_nearest.argtypes = [P, P, ctypes.c_int64, P, P, ctypes.c_int, P]
+        L.orc_kd_free.argtypes = [P]
+        L.orc_valid_states.argtypes = [P, P, P, ctypes.c_int64, P, ctypes.c_int]
+        L.orc_valid_edges.argtypes = [P, P, P, P, ctypes.c_int64, ctypes.c_double, ctypes.c_int, P, P,
+                                      ctypes.c_int]
+        L.orc_tri_tri.restype = ctypes.c_int
+        L.orc_tri_tri.argtypes = [P, P]
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def make_space(metric: int, dim: int, w=(1.0, 1.0)) -> Space:
+    s = Space()
+    s.metric = metric
+    s.dim = dim
+    s.w[0] = float(w[0])
+    s.w[1] = float(w[1])
+    return s
+
+
+def distance(space: Space, a, b) -> float:
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    return lib().orc_distance(ctypes.byref(space), _ptr(a), _ptr(b))
+
+
+def interpolate(space: Space, a, b, t: float) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    out = np.empty(space.dim, dtype=np.float64)
+    lib().orc_interpolate(ctypes.byref(space), _ptr(a), _ptr(b), float(t), _ptr(out))
+    return out
+
+
+def nn_brute(space: Space, pts: np.ndarray, q: np.ndarray, nthreads: int = 0):
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    nq = q.shape[0]
+    idx = np.empty(nq, dtype=np.int32)
+    dist = np.empty(nq, dtype=np.float64)
+    lib().orc_nn_brute(ctypes.byref(space), _ptr(pts), pts.shape[0], _ptr(q), nq, _ptr(idx), _ptr(dist),
+                       nthreads or os.cpu_count())
+    return idx, dist
+
+
+def knn_brute(space: Space, pts: np.ndarray, q: np.ndarray, k: int, nthreads: int = 0):
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    nq = q.shape[0]
+    idx = np.empty((nq, k), dtype=np.int32)
+    dist = np.empty((nq, k), dtype=np.float64)
+    lib().orc_knn_brute(ctypes.byref(space), _ptr(pts), pts.shape[0], _ptr(q), nq, k, _ptr(idx), _ptr(dist),
+                        nthreads or os.cpu_count())
+    return idx, dist
+
+
+class KDTree:
+    """The CPU kd-tree that stands in for nigh's KDTreeBatch in the baseline."""
+
+    def __init__(self, space: Space, pts: np.ndarray, leaf: int = 8):
+        self.space = space
+        self.pts = np.ascontiguousarray(pts, dtype=np.float64)
+        self.h = lib().orc_kd_build(ctypes.byref(space), _ptr(self.pts), self.pts.shape[0], leaf)
+
+    def nearest(self, q: np.ndarray, nthreads: int = 0):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        nq = q.shape[0]
+        idx = np.empty(nq, dtype=np.int32)
+        dist = np.empty(nq, dtype=np.float64)
+        ev = ctypes.c_int64(0)
+        lib().orc_kd_nearest(self.h, _ptr(q), nq, _ptr(idx), _ptr(dist), nthreads or os.cpu_count(),
+                             ctypes.byref(ev))
+        self.last_evals = ev.value
+        return idx, dist
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().orc_kd_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+def make_scene(desc: dict):
+    """Build an oracle Scene from a scene dict produced by mpt_gb300.scenes.
+
+    Returns (Scene, keepalive) -- keep the second value alive while using it."""
+    sc = Scene()
+    keep = []
+    kind = desc["kind"]
+    if kind == "grid":
+        g = np.ascontiguousarray(desc["grid"], dtype=np.uint8)
+        keep.append(g)
+        sc.kind = 0
+        sc.grid = g.ctypes.data
+        sc.height, sc.width = g.shape
+    elif kind == "arm":
+        lens = np.ascontiguousarray(desc["link_len"], dtype=np.float64)
+        discs = np.ascontiguousarray(desc["discs"], dtype=np.float64)
+        keep += [lens, discs]
+        sc.kind = 1
+        sc.nlinks = lens.shape[0]
+        sc.link_len = lens.ctypes.data
+        sc.ndiscs = discs.shape[0]
+        sc.discs = discs.ctypes.data
+        sc.robot_radius = float(desc.get("robot_radius", 0.0))
+        sc.self_collision = int(desc.get("self_collision", 1))
+    elif kind == "mesh":
+        rt = np.ascontiguousarray(desc["robot_tris"], dtype=np.float64)
+        et = np.ascontiguousarray(desc["env_tris"], dtype=np.float64)
+        keep += [rt, et]
+        sc.kind = 2
+        sc.nrobot = rt.shape[0]
+        sc.robot_tris = rt.ctypes.data
+        sc.nenv = et.shape[0]
+        sc.env_tris = et.ctypes.data
+    else:
+        raise ValueError(kind)
+    return sc, keep
+
+
+def valid_states(desc: dict, space: Space, q: np.ndarray, nthreads: int = 0) -> np.ndarray:
+    sc, keep = make_scene(desc)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    out = np.empty(q.shape[0], dtype=np.uint8)
+    lib().orc_valid_states(ctypes.byref(sc), ctypes.byref(space), _ptr(q), q.shape[0], _ptr(out),
+                           nthreads or os.cpu_count())
+    return out
+
+
+def valid_edges(desc: dict, space: Space, a: np.ndarray, b: np.ndarray, step: float, resolution: int = 0,
+                nthreads: int = 0):
+    sc, keep = make_scene(desc)
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    out = np.empty(a.shape[0], dtype=np.uint8)
+    ns = ctypes.c_int64(0)
+    lib().orc_valid_edges(ctypes.byref(sc), ctypes.byref(space), _ptr(a), _ptr(b), a.shape[0], float(step),
+                          int(resolution), _ptr(out), ctypes.byref(ns), nthreads or os.cpu_count())
+    return out, ns.value
+
+
+def tri_tri(t1, t2) -> bool:
+    t1 = np.ascontiguousarray(t1, dtype=np.float64).reshape(9)
+    t2 = np.ascontiguousarray(t2, dtype=np.float64).reshape(9)
+    return bool(lib().orc_tri_tri(_ptr(t1), _ptr(t2)))

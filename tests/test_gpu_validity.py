@@ -1,0 +1,73 @@
+"""GPU parity: batched Scenario::valid and DiscreteMotionValidator edges
+through the C ABI against the oracle (bit-exact booleans)."""
+import math
+
+import numpy as np
+import pytest
+
+from mpt_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene(ctx, sc):
+    import mpt_gb300 as m
+    return m.Scene(ctx, sc)
+
+
+@pytest.mark.parametrize("mk", [scenes.grid_scene, scenes.arm_scene])
+def test_states_match_oracle(ctx, orc, mk):
+    sc = mk()
+    q = scenes.uniform_states(sc, 20000, 401)
+    if sc["kind"] == "grid":
+        # include cell boundaries (x.5), the grid border and outside points
+        extra = np.array([[0.5, 0.5], [1023.5, 10.0], [1023.49, 10.0], [-0.5, 3.0], [-1.0, 3.0], [1024.0, 1024.0],
+                          [-0.99, -0.99], [511.5, 511.5], [np.nan, 3.0], [1e300, 2.0]])
+        q = np.concatenate([q, extra])
+    g = _scene(ctx, sc)
+    sp = orc.make_space(sc["metric"], sc["dim"], sc["weights"])
+    want = orc.valid_states(sc, sp, q)
+    got = g.valid(q)
+    assert np.array_equal(got, want), np.nonzero(got != want)[0][:10]
+    assert 0.05 < want.mean() < 0.97
+
+
+@pytest.mark.parametrize("mk", [scenes.grid_scene, scenes.arm_scene])
+def test_edges_match_oracle(ctx, orc, mk):
+    sc = mk()
+    a, b = scenes.steered_edges(sc, 4000, 402)
+    g = _scene(ctx, sc)
+    sp = orc.make_space(sc["metric"], sc["dim"], sc["weights"])
+    want, _ = orc.valid_edges(sc, sp, a, b, sc["edge_step"], sc["resolution"])
+    got = g.link(a, b, sc["edge_step"], sc["resolution"])
+    assert np.array_equal(got, want), np.nonzero(got != want)[0][:10]
+    assert 0.05 < want.mean() < 0.97
+
+
+def test_edges_degenerate(ctx, orc):
+    sc = scenes.grid_scene()
+    g = _scene(ctx, sc)
+    sp = orc.make_space(0, 2)
+    a = np.array([[10.0, 10.0], [10.0, 10.0], [10.0, 10.0], [100.0, 500.0]])
+    b = np.array([[10.0, 10.0], [10.5, 10.0], [10.0, 200.0], [100.0, 500.0 + 1e-9]])
+    want, _ = orc.valid_edges(sc, sp, a, b, 1.0)
+    got = g.link(a, b, 1.0)
+    assert np.array_equal(got, want)
+
+
+def test_arm_long_edges(ctx, orc):
+    """Edges up to pi per joint (hundreds of samples, several warp rounds)."""
+    sc = scenes.arm_scene()
+    rng = np.random.default_rng(7)
+    a = scenes.uniform_states(sc, 600, 403)
+    b = scenes.uniform_states(sc, 600, 404)
+    g = _scene(ctx, sc)
+    sp = orc.make_space(1, 10)
+    want, _ = orc.valid_edges(sc, sp, a, b, 0.01, 1)
+    got = g.link(a, b, 0.01, 1)
+    assert np.array_equal(got, want)
+    # also the space-metric resolution (reference DMV semantics)
+    want0, _ = orc.valid_edges(sc, sp, a, b, 0.05, 0)
+    got0 = g.link(a, b, 0.05, 0)
+    assert np.array_equal(got0, want0)
+    assert rng is not None
