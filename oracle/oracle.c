@@ -664,6 +664,11 @@ static int state_valid(const orc_scene* sc, const double* q) {
     return 0;
 }
 
+int orc_state_valid(const orc_scene* sc, const double* q) {
+    if (sc->kind == 2) get_env_bvh(sc);
+    return state_valid(sc, q);
+}
+
 void orc_valid_states(const orc_scene* sc, const orc_space* sp, const double* q, int64_t n,
                       uint8_t* out, int nthreads) {
     int D = sp->dim;

@@ -51,6 +51,7 @@ typedef struct {
 
 /* Edge resolution: 0 = the space metric (DiscreteMotionValidator),
  * 1 = max over joints of the wrapped joint difference (planar-arm edges). */
+int orc_state_valid(const orc_scene* sc, const double* q);
 void orc_valid_states(const orc_scene* sc, const orc_space* sp, const double* q, int64_t n,
                       uint8_t* out, int nthreads);
 void orc_valid_edges(const orc_scene* sc, const orc_space* sp, const double* a, const double* b,

@@ -1,0 +1,3 @@
+// Project-written nigh stand-in (see shim_metric.hpp).
+#pragma once
+#include "shim_metric.hpp"

@@ -29,7 +29,7 @@ def test_states_match_oracle(ctx, orc, mk):
     want = orc.valid_states(sc, sp, q)
     got = g.valid(q)
     assert np.array_equal(got, want), np.nonzero(got != want)[0][:10]
-    assert 0.05 < want.mean() < 0.97
+    assert 0.01 < want.mean() < 0.99
 
 
 @pytest.mark.parametrize("mk", [scenes.grid_scene, scenes.arm_scene])
@@ -41,7 +41,7 @@ def test_edges_match_oracle(ctx, orc, mk):
     want, _ = orc.valid_edges(sc, sp, a, b, sc["edge_step"], sc["resolution"])
     got = g.link(a, b, sc["edge_step"], sc["resolution"])
     assert np.array_equal(got, want), np.nonzero(got != want)[0][:10]
-    assert 0.05 < want.mean() < 0.97
+    assert 0.01 < want.mean() < 0.99
 
 
 def test_edges_degenerate(ctx, orc):

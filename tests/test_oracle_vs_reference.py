@@ -1,0 +1,100 @@
+"""CPU: the oracle's restatement against the reference's OWN code, compiled
+in place from the MPT headers (oracle/ref, skipped where the reference
+sources are absent)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from mpt_gb300 import scenes
+
+ref = pytest.importorskip("oracle.ref")
+if not ref.available():
+    pytest.skip("reference sources not present", allow_module_level=True)
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+@pytest.mark.parametrize("metric,dim", [(0, 2), (0, 3), (1, 1), (1, 10)])
+def test_interpolate_bit_exact(orc, metric, dim):
+    L = ref.lib()
+    rng = np.random.default_rng(metric * 100 + dim)
+    sp = orc.make_space(metric, dim)
+    lo, hi = (-np.pi, np.pi) if metric == 1 else (-50.0, 50.0)
+    for _ in range(3000):
+        a = rng.uniform(lo, hi, dim)
+        b = rng.uniform(lo, hi, dim)
+        t = float(rng.choice([rng.uniform(0, 1), rng.uniform(-3, 4), 0.0, 1.0]))
+        want = np.empty(dim)
+        assert L.ref_interpolate(metric, dim, _p(a), _p(b), t, _p(want)) == 0
+        got = orc.interpolate(sp, a, b, t)
+        assert np.array_equal(got.view(np.int64), want.view(np.int64)), (a, b, t, got, want)
+
+
+def test_so3_slerp_against_glibc(orc):
+    """The reference slerp calls std::acos/std::sin (glibc); the oracle and the
+    device call the deterministic mptg_acos/mptg_sin.  They agree to a few ulp;
+    the fraction of bit-identical results is reported."""
+    L = ref.lib()
+    sc = {"metric": 2, "dim": 4}
+    qa = scenes.uniform_states(sc, 4000, 1)
+    qb = scenes.uniform_states(sc, 4000, 2)
+    sp = orc.make_space(2, 4)
+    rng = np.random.default_rng(3)
+    worst, same = 0.0, 0
+    for i in range(len(qa)):
+        t = float(rng.uniform(0, 1))
+        want = np.empty(4)
+        L.ref_interpolate(2, 4, _p(qa[i]), _p(qb[i]), t, _p(want))
+        got = orc.interpolate(sp, qa[i], qb[i], t)
+        worst = max(worst, float(np.abs(got - want).max()))
+        same += int(np.array_equal(got, want))
+    assert worst < 4e-15, worst
+    assert same > 0.5 * len(qa), same
+
+
+@pytest.mark.parametrize("mk", [scenes.grid_scene, scenes.arm_scene])
+def test_dmv_bit_exact_with_sample_counts(orc, mk):
+    """Booleans AND the number of valid() calls per edge match the reference's
+    DiscreteMotionValidator (bisection ring queue, discrete_motion_validator.hpp:71-130)."""
+    L = ref.lib()
+    sc = mk()
+    step = 1.0 if sc["kind"] == "grid" else 0.02
+    a, b = scenes.steered_edges(sc, 400, 77)
+    if sc["kind"] == "arm":
+        # long edges too: more than 256 interior samples exercise the queue's
+        # switch to sequential scanning
+        a2 = scenes.uniform_states(sc, 100, 78)
+        b2 = scenes.uniform_states(sc, 100, 79)
+        a, b = np.concatenate([a, a2]), np.concatenate([b, b2])
+        step = 0.005
+    csc, keep = orc.make_scene(sc)
+    n = len(a)
+    out = np.empty(n, np.uint8)
+    cnt = np.empty(n, np.int64)
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    assert L.ref_dmv_edges(ctypes.byref(csc), sc["metric"], sc["dim"], _p(a), _p(b), n, step, _p(out), _p(cnt)) == 0
+    sp = orc.make_space(sc["metric"], sc["dim"])
+    got = np.empty(n, np.uint8)
+    gcnt = np.empty(n, np.int64)
+    for i in range(n):
+        g, c = orc.valid_edges(sc, sp, a[i:i + 1], b[i:i + 1], step, 0, nthreads=1)
+        got[i], gcnt[i] = g[0], c
+    assert np.array_equal(got, out)
+    assert np.array_equal(gcnt, cnt)
+    assert cnt.max() > 258 or sc["kind"] == "grid"
+
+
+def test_goal_state(orc):
+    L = ref.lib()
+    g = np.array([1014.0, 1014.0])
+    for q, r in [([1014.0, 1014.0], 8.0), ([1010.0, 1010.0], 8.0), ([1000.0, 1014.0], 8.0), ([1014.0, 1006.0], 8.0)]:
+        q = np.array(q)
+        d = ctypes.c_double()
+        hit = L.ref_goal_l2(_p(g), r, _p(q), ctypes.byref(d))
+        dist = orc.distance(orc.make_space(0, 2), q, g)
+        assert hit == int(dist <= r)
+        assert d.value == (0.0 if dist <= r else dist - r)
