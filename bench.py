@@ -173,10 +173,11 @@ def run_gpu(args):
     del dpts
 
     nbuf = 4
-    hq = _queries(sc, nbuf, 1000 + 97 * rank)
-    dq = [torch.from_numpy(x).cuda() for x in hq]
-    di = torch.empty(BATCH, dtype=torch.int32, device="cuda")
-    dd = torch.empty(BATCH, dtype=torch.float64, device="cuda")
+    nqb = min(args.queries, BATCH)
+    hq = [x[:nqb] for x in _queries(sc, nbuf, 1000 + 97 * rank)]
+    dq = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in hq]
+    di = torch.empty(nqb, dtype=torch.int32, device="cuda")
+    dd = torch.empty(nqb, dtype=torch.float64, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
 
@@ -208,31 +209,38 @@ def run_gpu(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     cnt = tree.counters(reset=True)
-    value = ws * BATCH * args.steps / (total_ms / 1000.0)
+    value = ws * nqb * args.steps / (total_ms / 1000.0)
 
     # roofline of k_nearest: algorithmic bytes per launch from the device counters
     D = sc["dim"]
     per_launch = {k: v / args.steps for k, v in cnt.items()}
     alg_bytes = (per_launch["points_evaluated"] * (4 * D + 4) + per_launch["internal_visited"] * (16 + 8 * D)
-                 + per_launch["leaves_visited"] * 16 + per_launch["reranked"] * 8 * D + BATCH * (8 * D + 12))
+                 + per_launch["leaves_visited"] * 16 + per_launch["reranked"] * 8 * D + nqb * (8 * D + 12))
     avg_s = total_ms / 1000.0 / args.steps
     peak, peak_kind = _peaks()
     achieved = alg_bytes / avg_s / 1e9
+    if args.nn_only:
+        if rank == 0:
+            print(json.dumps({"metric": "NN queries/s (profiling case)", "value": value, "unit": "queries/s",
+                              "queries_per_step": nqb, "steps": args.steps, "ms_per_step": total_ms / args.steps,
+                              "alg_bytes_per_launch": alg_bytes, "achieved_gbs": achieved,
+                              "counters_per_launch": per_launch, "gpu_launches": launches}))
+        return
 
     # end to end through the C ABI with pinned host buffers
     hq_pinned = [torch.from_numpy(x).pin_memory() for x in hq]
-    hi = torch.empty(BATCH, dtype=torch.int32).pin_memory()
-    hd = torch.empty(BATCH, dtype=torch.float64).pin_memory()
+    hi = torch.empty(nqb, dtype=torch.int32).pin_memory()
+    hd = torch.empty(nqb, dtype=torch.float64).pin_memory()
     qn = [x.numpy() for x in hq_pinned]
     for i in range(3):
-        ctx.lib.mptg_nearest(tree.h, qn[i % nbuf].ctypes.data, BATCH, hi.data_ptr(), hd.data_ptr(), None)
+        ctx.lib.mptg_nearest(tree.h, qn[i % nbuf].ctypes.data, nqb, hi.data_ptr(), hd.data_ptr(), None)
     torch.cuda.synchronize()
     e2e_t = []
     for s in range(args.steps):
         flush.fill_(s & 0xff)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        st = ctx.lib.mptg_nearest(tree.h, qn[s % nbuf].ctypes.data, BATCH, hi.data_ptr(), hd.data_ptr(), None)
+        st = ctx.lib.mptg_nearest(tree.h, qn[s % nbuf].ctypes.data, nqb, hi.data_ptr(), hd.data_ptr(), None)
         e2e_t.append(time.perf_counter() - t0)
         assert st == 0
     e2e_total = sum(e2e_t)
@@ -240,7 +248,7 @@ def run_gpu(args):
         t = torch.tensor([e2e_total], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_total = float(t.item())
-    e2e_val = ws * BATCH * args.steps / e2e_total
+    e2e_val = ws * nqb * args.steps / e2e_total
     # results of the host path equal the device path
     assert np.array_equal(hi.numpy(), tree.nearest(hq[(args.steps - 1) % nbuf])[0])
 
@@ -287,10 +295,10 @@ def run_gpu(args):
                 "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
                 "data": "synthetic (seeded uniform SO(2)^10 states)",
-                "config": {"workload": "nn_so2x10_1M", "tree_nodes": N_TREE, "queries_per_step": BATCH,
+                "config": {"workload": "nn_so2x10_1M", "tree_nodes": N_TREE, "queries_per_step": nqb,
                            "l2": "flushed (256 MiB write) between steps", "parallelism": "replicas"},
-                "e2e": {"value": e2e_val, "unit": "queries/s", "h2d_bytes_per_step": BATCH * D * 8,
-                        "d2h_bytes_per_step": BATCH * 12},
+                "e2e": {"value": e2e_val, "unit": "queries/s", "h2d_bytes_per_step": nqb * D * 8,
+                        "d2h_bytes_per_step": nqb * 12},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
                              "kernel": "k_nearest<SO2,16>", "alg_bytes_per_launch": alg_bytes,
@@ -311,6 +319,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--queries", type=int, default=BATCH, help="queries per step (profiling: a smaller case)")
+    ap.add_argument("--nn-only", action="store_true", help="time the NN kernel only (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
