@@ -94,6 +94,29 @@ mptg_status mptg_nearest_k(mptg_tree* tree, const double* queries, size_t nq, in
 mptg_status mptg_nearest_linear(mptg_tree* tree, const double* queries, size_t nq, int32_t* idx_out,
                                 double* dist_out, void* stream);
 
+/* Exact 1-NN among n caller-owned points that allocates no device memory.
+ * It has no counterpart in the reference.  It is for callers that cannot
+ * allocate GPU memory while they run: a real-time control loop that must not
+ * call cudaMalloc after start-up (the call can block and synchronise the
+ * device), or a plugin inside a framework that owns all device memory through
+ * its own allocator.  Same results as mptg_nearest_linear on a tree holding
+ * the same points (ids are row indices; lowest id on ties; -1 and +inf when
+ * n == 0).  points, queries, idx_out and dist_out must be device memory of
+ * the context's GPU; weights may be NULL (1, 1) or host memory.
+ * Working memory is one static device array built into the library
+ * (4 MiB + 256 bytes on every GPU that loads the library, kept until the
+ * process exits), so n is at most 65,536 points of at most 16 dimensions;
+ * a larger n returns MPTG_ERR_INVALID_ARG.  A device's first call looks up
+ * the array's device address with cudaGetSymbolAddress and caches it: make
+ * that first call before any stream capture.  All calls share the array and
+ * it keeps the last call's contents (each call clears what must start at
+ * zero), so calls whose work overlaps on the GPU race: order them on one
+ * stream.  Invalid points (NaN, SO2 angles outside [-pi, pi], non-unit
+ * quaternions) give id -1 and NaN for every query of that call. */
+mptg_status mptg_nearest_linear_noalloc(mptg_ctx* ctx, mptg_metric metric, int dim, const double* weights,
+                                        const double* points, size_t n, const double* queries, size_t nq,
+                                        int32_t* idx_out, double* dist_out, void* stream);
+
 /* Per-tree search counters accumulated since the last reset:
  * [0] queries, [1] internal nodes visited, [2] leaves visited,
  * [3] points evaluated in FP32, [4] candidates re-ranked in FP64. */
