@@ -165,11 +165,64 @@ mptg_status mptg_valid_states(mptg_scene* scene, const double* states, size_t n,
  * valid, where steps = ceil(m(a_i, b_i) / step).  resolution 0: m is the
  * space metric (the reference DMV); resolution 1: m is the largest wrapped
  * joint difference (planar-arm edges at a maximum joint step).  a_i is
- * assumed valid, as the reference asserts (:73).  samples_out (may be NULL)
- * receives the number of states checked per edge when every sample is
- * evaluated. */
+ * assumed valid, as the reference asserts (:73).  Edges that would need
+ * more than 2^22 samples are reported invalid. */
 mptg_status mptg_valid_edges(mptg_scene* scene, const double* a, const double* b, size_t n,
                              double step, int resolution, uint8_t* out, void* stream);
+
+/* ---- wavefront planner ---------------------------------------------
+ * PRRT's worker loop (src/mpt/impl/prrt/prrt.hpp:358-452) as wavefronts of
+ * `wavefront` samples: sample (goal with probability goal_bias until the
+ * first solution) -> nearest -> skip if d == 0 -> steer to `range` ->
+ * valid + link (DMV at edge_step) -> goal test -> insert.  Samples come from
+ * a Philox4x32-10 stream keyed by `seed`; a wavefront sees the tree as it
+ * stood before it, and accepted samples join in sample order, so a run is
+ * reproducible from the seed. */
+typedef struct mptg_planner mptg_planner;
+typedef struct {
+    double range;        /* PRRT::setRange (prrt.hpp:168-171); <= 0 means unlimited */
+    double goal_bias;    /* PRRT::setGoalBias (prrt.hpp:159-162), reference default 0.01 */
+    double goal_radius;  /* GoalState radius (goal_state.hpp:64-69); set by set_goal */
+    double edge_step;    /* DiscreteMotionValidator step size */
+    int resolution;      /* 0: space metric, 1: max wrapped joint difference */
+    int wavefront;       /* samples per wavefront, 1 .. 2^20 */
+    uint64_t seed;
+    size_t max_nodes;    /* node budget (tree capacity) */
+} mptg_plan_params;
+
+/* Planner<Scenario, PRRT<...>>(scenario, seed) (prrt.hpp:149-157); lo/hi are
+ * the sampling bounds (Scenario::bounds, src/mpt/impl/scenario_bounds.hpp);
+ * NULL uses [-pi, pi] per joint for SO2 and [0, 1] otherwise (quaternion
+ * dimensions of SE3 are always sampled uniformly on SO(3)). */
+mptg_status mptg_planner_create(mptg_ctx* ctx, mptg_scene* scene, const mptg_plan_params* params,
+                                const double* lo, const double* hi, mptg_planner** planner);
+mptg_status mptg_planner_destroy(mptg_planner* planner);
+/* PRRT::addStart (prrt.hpp:181-187); the start is not checked for validity, as in the reference */
+mptg_status mptg_planner_add_start(mptg_planner* planner, const double* q);
+/* GoalState(radius, q) as the Scenario's goal (src/mpt/goal_state.hpp:43-90) */
+mptg_status mptg_planner_set_goal(mptg_planner* planner, const double* q, double radius);
+/* PRRT::solve (prrt.hpp:194-201) driven by the host between wavefronts: runs
+ * up to max_wavefronts (<= 0: no limit) or time_limit_s (<= 0: none), and
+ * stops after the first solution when stop_when_solved.  No start ->
+ * MPTG_ERR_NO_START (the reference throws "there are no valid initial
+ * states"); a second concurrent call -> MPTG_ERR_ALREADY_SOLVING. */
+mptg_status mptg_planner_run(mptg_planner* planner, int max_wavefronts, double time_limit_s,
+                             int stop_when_solved, int* solved);
+mptg_status mptg_planner_size(mptg_planner* planner, size_t* n);
+/* number of goal nodes found (PRRT::solved() is goals > 0) */
+mptg_status mptg_planner_goals(mptg_planner* planner, size_t* n);
+/* PRRT::solution() (prrt.hpp:263-274): the best goal's path, start first,
+ * len states of dim doubles, and its cost (prrt.hpp:208-234).  path may be
+ * NULL to query len and cost. */
+mptg_status mptg_planner_solution(mptg_planner* planner, double* path, size_t cap, size_t* len,
+                                  double* cost);
+/* PRRT::visitGraph (prrt.hpp:300-316): all states and parent ids (-1 for starts). */
+mptg_status mptg_planner_graph(mptg_planner* planner, double* states, int32_t* parents, size_t cap,
+                               size_t* n);
+/* WorkerStats (prrt.hpp:63-101): [0] wavefronts, [1] samples, [2] nodes
+ * added, [3] tree size, [4] goals, [5] states checked by link, [6] seconds in
+ * run, [7] wavefront counter. */
+mptg_status mptg_planner_stats(mptg_planner* planner, double out[8]);
 
 #ifdef __cplusplus
 }

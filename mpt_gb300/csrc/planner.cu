@@ -1,0 +1,520 @@
+// planner.cu - the PRRT worker loop as GPU wavefronts.
+//
+// Replaces Worker::solve / addSample of src/mpt/impl/prrt/prrt.hpp:358-452
+// (and the WorkerPool of src/mpt/impl/worker_pool_openmp.hpp:101-129).  One
+// wavefront draws W samples at once and runs, batched on the device:
+//   sample (uniform box / SO(2) / Shoemake SO(3); goal with probability
+//     goalBias until the first solution, prrt.hpp:363-389)
+//   -> nearest over the tree as it stood before the wavefront (prrt.hpp:416)
+//   -> skip if d == 0 (:425); steer to `range` with interpolate (:430-434)
+//   -> valid(new) and link(near, new) through the DMV (:439-442)
+//   -> goal test GoalState(radius) (:443-445) -> insert with parent (:447)
+// Accepted samples are compacted in sample order, so a wavefront is a pure
+// function of (seed, wavefront index, tree): the CPU checker replays it
+// exactly.  Unlike the reference's concurrent workers, samples of one
+// wavefront do not see each other's new nodes.
+#include "metrics.cuh"
+#include "scene.cuh"
+#include "tree.cuh"
+#include "philox.cuh"
+#include <chrono>
+
+#define PLAN_SCAN_BLOCK 1024
+
+struct PlanView {
+    int D, metric;
+    double w0, w1;
+    const double* lo;
+    const double* hi;
+    const double* goal;
+    int has_goal;
+    double goal_bias, range, goal_radius;
+    uint64_t seed;
+};
+
+struct mptg_planner {
+    mptg_ctx* ctx = nullptr;
+    mptg_scene* scene = nullptr;
+    mptg_tree* tree = nullptr;
+    mptg_plan_params prm{};
+    int D = 0, metric = 0;
+    double w0 = 1, w1 = 1;
+    double* lo = nullptr;
+    double* hi = nullptr;
+    double* goal = nullptr;
+    int has_goal = 0;
+    std::vector<double> goal_host;
+    int* parent = nullptr;
+    // wavefront buffers
+    double* samp = nullptr;
+    int* nidx = nullptr;
+    double* ndist = nullptr;
+    double* nearst = nullptr;
+    double* newst = nullptr;
+    uint8_t* skip = nullptr;
+    uint8_t* ok = nullptr;
+    int* scan = nullptr;      // per-sample exclusive offsets
+    int* bsum = nullptr;      // per-block sums, then offsets; [nblk] = total
+    double* acc_states = nullptr;
+    int* acc_parent = nullptr;
+    uint8_t* acc_goal = nullptr;
+    int* hbuf = nullptr;      // pinned
+    uint8_t* hgoal = nullptr; // pinned
+    unsigned long long* nsamp = nullptr;
+    uint32_t wave = 0;
+    std::vector<int> goals;   // node ids of goal nodes, in discovery order
+    uint64_t stat_samples = 0, stat_goal_samples = 0, stat_accepted = 0, stat_wavefronts = 0;
+    uint64_t stat_skipped = 0;
+    double stat_seconds = 0;
+    bool solving = false;
+};
+
+// ------------------------------------------------------------------ kernels
+
+__global__ void k_plan_sample(PlanView p, int W, uint32_t wave, int bias_on, double* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W) return;
+    double* q = out + (size_t)i * p.D;
+    bool goal = false;
+    if (p.has_goal && bias_on && p.goal_bias > 0) goal = phx_uniform(p.seed, (uint32_t)i, wave, 16) < p.goal_bias;
+    if (goal) {
+        for (int d = 0; d < p.D; ++d) q[d] = p.goal[d];
+        return;
+    }
+    if (p.metric == MPTG_METRIC_SO3 || p.metric == MPTG_METRIC_SE3) {
+        // Shoemake's uniform rotation (src/mpt/impl/uniform_sampler_so3.hpp:55-68)
+        double a = phx_uniform(p.seed, (uint32_t)i, wave, 0);
+        double b = __dmul_rn(MPTG_TWO_PI, phx_uniform(p.seed, (uint32_t)i, wave, 1));
+        double c = __dmul_rn(MPTG_TWO_PI, phx_uniform(p.seed, (uint32_t)i, wave, 2));
+        double s1 = __dsqrt_rn(__dsub_rn(1.0, a)), s2 = __dsqrt_rn(a);
+        double sb, cb, sc, cc;
+        mptg_sincos(b, &sb, &cb);
+        mptg_sincos(c, &sc, &cc);
+        q[0] = __dmul_rn(s1, sb); q[1] = __dmul_rn(s1, cb); q[2] = __dmul_rn(s2, sc); q[3] = __dmul_rn(s2, cc);
+        for (int d = 4; d < p.D; ++d) {
+            double u = phx_uniform(p.seed, (uint32_t)i, wave, (uint32_t)(d - 1));
+            q[d] = __dadd_rn(p.lo[d], __dmul_rn(__dsub_rn(p.hi[d], p.lo[d]), u));
+        }
+    } else if (p.metric == MPTG_METRIC_SO2) {
+        // U[-pi, pi) per joint (src/mpt/impl/uniform_sampler_so2.hpp:57-64)
+        for (int d = 0; d < p.D; ++d)
+            q[d] = __dadd_rn(-MPTG_PI, __dmul_rn(MPTG_TWO_PI, phx_uniform(p.seed, (uint32_t)i, wave, (uint32_t)d)));
+    } else {
+        // uniform box (src/mpt/uniform_box_sampler.hpp:60-68)
+        for (int d = 0; d < p.D; ++d) {
+            double u = phx_uniform(p.seed, (uint32_t)i, wave, (uint32_t)d);
+            q[d] = __dadd_rn(p.lo[d], __dmul_rn(__dsub_rn(p.hi[d], p.lo[d]), u));
+        }
+    }
+}
+
+__global__ void k_plan_steer(PlanView p, int W, const double* __restrict__ samp, const int* __restrict__ nidx,
+                             const double* __restrict__ ndist, const double* __restrict__ states64,
+                             double* __restrict__ nearst, double* __restrict__ newst, uint8_t* __restrict__ skip) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W) return;
+    const int D = p.D;
+    const double* s = samp + (size_t)i * D;
+    double* nr = nearst + (size_t)i * D;
+    double* nw = newst + (size_t)i * D;
+    int id = nidx[i];
+    double d = ndist[i];
+    if (id < 0 || d == 0.0 || !(d == d)) {  // prrt.hpp:425: avoid adding the same state twice
+        skip[i] = 1;
+        for (int k = 0; k < D; ++k) { nr[k] = s[k]; nw[k] = s[k]; }
+        return;
+    }
+    skip[i] = 0;
+    const double* ns = states64 + (size_t)id * D;
+    double a[MPTG_MAX_DIM], b[MPTG_MAX_DIM];
+    for (int k = 0; k < D; ++k) { a[k] = ns[k]; b[k] = s[k]; nr[k] = a[k]; }
+    if (d > p.range) {
+        double q[MPTG_MAX_DIM];
+        interp64(p.metric, D, a, b, __ddiv_rn(p.range, d), q);
+        for (int k = 0; k < D; ++k) nw[k] = q[k];
+    } else {
+        for (int k = 0; k < D; ++k) nw[k] = b[k];
+    }
+}
+
+// block-local exclusive scan of the acceptance flags
+__global__ void __launch_bounds__(PLAN_SCAN_BLOCK) k_plan_scan(int W, const uint8_t* __restrict__ ok,
+                                                               const uint8_t* __restrict__ skip,
+                                                               int* __restrict__ scan, int* __restrict__ bsum) {
+    __shared__ int wsum[32];
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int f = (i < W && ok[i] && !skip[i]) ? 1 : 0;
+    unsigned m = __ballot_sync(0xffffffffu, f);
+    int pre = __popc(m & ((1u << lane) - 1u));
+    if (lane == 0) wsum[w] = __popc(m);
+    __syncthreads();
+    if (w == 0) {
+        int v = wsum[lane];
+        int x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        wsum[lane] = x - v;
+        if (lane == 31) bsum[blockIdx.x] = x;
+    }
+    __syncthreads();
+    if (i < W) scan[i] = f ? wsum[w] + pre : -1;
+}
+
+// exclusive scan over the (<= 1024) block sums; total at bsum[nblk]
+__global__ void k_plan_scan_top(int nblk, int* __restrict__ bsum) {
+    __shared__ int s[1024];
+    int t = threadIdx.x;
+    s[t] = t < nblk ? bsum[t] : 0;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        int v = t >= o ? s[t - o] : 0;
+        __syncthreads();
+        s[t] += v;
+        __syncthreads();
+    }
+    if (t < nblk) bsum[t] = t == 0 ? 0 : s[t - 1];
+    if (t == 0) bsum[nblk] = s[1023];
+}
+
+__global__ void k_plan_scatter(PlanView p, int W, const int* __restrict__ scan, const int* __restrict__ bsum,
+                               const double* __restrict__ newst, const int* __restrict__ nidx,
+                               double* __restrict__ acc_states, int* __restrict__ acc_parent,
+                               uint8_t* __restrict__ acc_goal) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W) return;
+    int l = scan[i];
+    if (l < 0) return;
+    int pos = bsum[i / PLAN_SCAN_BLOCK] + l;
+    const double* s = newst + (size_t)i * p.D;
+    double* o = acc_states + (size_t)pos * p.D;
+    for (int k = 0; k < p.D; ++k) o[k] = s[k];
+    acc_parent[pos] = nidx[i];
+    uint8_t g = 0;
+    if (p.has_goal) {
+        // GoalState::operator() (src/mpt/goal_state.hpp:64-69): d <= radius
+        double d = dist64(p.metric, p.D, p.w0, p.w1, s, p.goal);
+        g = d <= p.goal_radius ? 1 : 0;
+    }
+    acc_goal[pos] = g;
+}
+
+// walk a goal's parent chain: path ids (start first) and the summed cost
+// (PRRT::pathCost, src/mpt/impl/prrt/prrt.hpp:208-234)
+__global__ void k_plan_path(int goal, const int* __restrict__ parent, const double* __restrict__ states64, int D,
+                            int metric, double w0, double w1, int cap, int* __restrict__ ids, double* __restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int len = 1;
+    double cost = 0.0;
+    int n = goal;
+    for (int guard = 0; guard < (1 << 30); ++guard) {
+        int pnt = parent[n];
+        if (pnt < 0) break;
+        cost = __dadd_rn(cost, dist64(metric, D, w0, w1, states64 + (size_t)n * D, states64 + (size_t)pnt * D));
+        n = pnt;
+        ++len;
+    }
+    out[0] = cost;
+    out[1] = (double)len;
+    if (len <= cap) {
+        n = goal;
+        for (int k = len - 1; k >= 0; --k) {
+            ids[k] = n;
+            n = parent[n];
+        }
+    }
+}
+
+// ------------------------------------------------------------------ host
+
+static PlanView plan_view(const mptg_planner* p) {
+    PlanView v;
+    v.D = p->D; v.metric = p->metric; v.w0 = p->w0; v.w1 = p->w1;
+    v.lo = p->lo; v.hi = p->hi; v.goal = p->goal; v.has_goal = p->has_goal;
+    v.goal_bias = p->prm.goal_bias;
+    v.range = p->prm.range > 0 ? p->prm.range : INFINITY;
+    v.goal_radius = p->prm.goal_radius;
+    v.seed = p->prm.seed;
+    return v;
+}
+
+static void planner_free(mptg_planner* p) {
+    void* ptrs[] = {p->lo, p->hi, p->goal, p->parent, p->samp, p->nidx, p->ndist, p->nearst, p->newst, p->skip,
+                    p->ok, p->scan, p->bsum, p->acc_states, p->acc_parent, p->acc_goal, p->nsamp};
+    for (void* x : ptrs)
+        if (x) cudaFree(x);
+    if (p->hbuf) cudaFreeHost(p->hbuf);
+    if (p->hgoal) cudaFreeHost(p->hgoal);
+    if (p->tree) mptg_tree_destroy(p->tree);
+    delete p;
+}
+
+// one wavefront; returns the number of nodes added
+static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
+    mptg_ctx* ctx = p->ctx;
+    const int W = p->prm.wavefront;
+    *added = 0;
+    size_t n0 = 0;
+    mptg_tree_size(p->tree, &n0);
+    if (n0 >= p->prm.max_nodes) return MPTG_OK;
+    PlanView v = plan_view(p);
+    int bias_on = p->goals.empty() ? 1 : 0;
+    k_plan_sample<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->wave, bias_on, p->samp);
+    mptg_status st = mptg_tree_nearest_dev(p->tree, p->samp, W, p->nidx, p->ndist, s, false);
+    if (st) return st;
+    k_plan_steer<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->samp, p->nidx, p->ndist, mptg_tree_states_dev(p->tree),
+                                                     p->nearst, p->newst, p->skip);
+    ctx->launches += 2;
+    st = scene_edges_dev(p->scene, p->nearst, p->newst, W, p->prm.edge_step, p->prm.resolution, p->ok, s, p->nsamp);
+    if (st) return st;
+    int nblk = (W + PLAN_SCAN_BLOCK - 1) / PLAN_SCAN_BLOCK;
+    k_plan_scan<<<nblk, PLAN_SCAN_BLOCK, 0, s>>>(W, p->ok, p->skip, p->scan, p->bsum);
+    k_plan_scan_top<<<1, 1024, 0, s>>>(nblk, p->bsum);
+    k_plan_scatter<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->scan, p->bsum, p->newst, p->nidx, p->acc_states,
+                                                       p->acc_parent, p->acc_goal);
+    ctx->launches += 3;
+    MPTG_CUDA_TRY(ctx, cudaGetLastError());
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->hbuf, p->bsum + nblk, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    int nacc = p->hbuf[0];
+    size_t room = p->prm.max_nodes - n0;
+    if ((size_t)nacc > room) nacc = (int)room;  // node budget: keep the first accepted samples
+    p->stat_samples += W;
+    p->stat_accepted += nacc;
+    p->stat_wavefronts += 1;
+    p->wave += 1;
+    if (nacc > 0) {
+        st = mptg_tree_insert(p->tree, p->acc_states, nacc, s);
+        if (st) return st;
+        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->parent + n0, p->acc_parent, nacc * sizeof(int), cudaMemcpyDeviceToDevice, s));
+        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->hgoal, p->acc_goal, nacc, cudaMemcpyDeviceToHost, s));
+        MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        for (int k = 0; k < nacc; ++k)
+            if (p->hgoal[k]) p->goals.push_back((int)(n0 + k));
+    }
+    *added = nacc;
+    return MPTG_OK;
+}
+
+extern "C" {
+
+mptg_status mptg_planner_create(mptg_ctx* ctx, mptg_scene* scene, const mptg_plan_params* prm, const double* lo,
+                                const double* hi, mptg_planner** out) {
+    if (!ctx || !scene || !prm || !out) return MPTG_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (prm->wavefront < 1 || prm->wavefront > (1 << 20))
+        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "wavefront must be in [1, 2^20]");
+    if (prm->max_nodes < 1) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "max_nodes must be positive");
+    if (!(prm->edge_step > 0)) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "edge_step must be positive");
+    if (!(prm->goal_bias >= 0 && prm->goal_bias <= 1))
+        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "goal_bias must be in [0, 1]");
+    if (prm->resolution == 1 && scene->metric != MPTG_METRIC_SO2)
+        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "joint-step resolution needs an SO2 scene");
+    MPTG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    mptg_planner* p = new mptg_planner();
+    p->ctx = ctx;
+    p->scene = scene;
+    p->prm = *prm;
+    p->D = scene->D;
+    p->metric = scene->metric;
+    p->w0 = scene->w0;
+    p->w1 = scene->w1;
+    double w[2] = {p->w0, p->w1};
+    mptg_status st = mptg_tree_create(ctx, (mptg_metric)p->metric, p->D, w, prm->max_nodes, &p->tree);
+    if (st) { delete p; return st; }
+    const size_t W = prm->wavefront, D = p->D, N = prm->max_nodes;
+    int nblk = (int)((W + PLAN_SCAN_BLOCK - 1) / PLAN_SCAN_BLOCK);
+    if (nblk > 1024) { planner_free(p); return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "wavefront too large"); }
+    cudaError_t e = cudaSuccess;
+#define ALLOC(ptr, bytes) if (e == cudaSuccess) e = cudaMalloc((void**)&(ptr), (bytes))
+    ALLOC(p->lo, D * sizeof(double));
+    ALLOC(p->hi, D * sizeof(double));
+    ALLOC(p->goal, D * sizeof(double));
+    ALLOC(p->parent, N * sizeof(int));
+    ALLOC(p->samp, W * D * sizeof(double));
+    ALLOC(p->nidx, W * sizeof(int));
+    ALLOC(p->ndist, W * sizeof(double));
+    ALLOC(p->nearst, W * D * sizeof(double));
+    ALLOC(p->newst, W * D * sizeof(double));
+    ALLOC(p->skip, W);
+    ALLOC(p->ok, W);
+    ALLOC(p->scan, W * sizeof(int));
+    ALLOC(p->bsum, (nblk + 1) * sizeof(int));
+    ALLOC(p->acc_states, W * D * sizeof(double));
+    ALLOC(p->acc_parent, W * sizeof(int));
+    ALLOC(p->acc_goal, W);
+    ALLOC(p->nsamp, sizeof(unsigned long long));
+#undef ALLOC
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&p->hbuf, 16 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&p->hgoal, W);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        planner_free(p);
+        return mptg_fail(ctx, MPTG_ERR_OOM, "planner allocation failed: %s", cudaGetErrorString(e));
+    }
+    // sampling bounds: given, else the metric's domain
+    std::vector<double> l(D), h(D);
+    for (size_t d = 0; d < D; ++d) {
+        l[d] = lo ? lo[d] : (p->metric == MPTG_METRIC_SO2 ? -MPTG_PI : 0.0);
+        h[d] = hi ? hi[d] : (p->metric == MPTG_METRIC_SO2 ? MPTG_PI : 1.0);
+    }
+    e = cudaMemcpy(p->lo, l.data(), D * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p->hi, h.data(), D * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(p->nsamp, 0, sizeof(unsigned long long));
+    if (e != cudaSuccess) {
+        planner_free(p);
+        return mptg_fail(ctx, MPTG_ERR_CUDA, "planner init failed: %s", cudaGetErrorString(e));
+    }
+    *out = p;
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_destroy(mptg_planner* p) {
+    if (!p) return MPTG_ERR_INVALID_ARG;
+    cudaDeviceSynchronize();
+    planner_free(p);
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_add_start(mptg_planner* p, const double* q) {
+    if (!p || !q) return MPTG_ERR_INVALID_ARG;
+    size_t n = 0;
+    mptg_tree_size(p->tree, &n);
+    if (n >= p->prm.max_nodes) return mptg_fail(p->ctx, MPTG_ERR_CAPACITY, "node budget reached");
+    mptg_status st = mptg_tree_insert(p->tree, q, 1, nullptr);
+    if (st) return st;
+    int minus1 = -1;
+    MPTG_CUDA_TRY(p->ctx, cudaMemcpy(p->parent + n, &minus1, sizeof(int), cudaMemcpyHostToDevice));
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_set_goal(mptg_planner* p, const double* q, double radius) {
+    if (!p || !q) return MPTG_ERR_INVALID_ARG;
+    if (!(radius >= 0)) return mptg_fail(p->ctx, MPTG_ERR_INVALID_ARG, "goal radius must be >= 0");
+    MPTG_CUDA_TRY(p->ctx, cudaMemcpy(p->goal, q, p->D * sizeof(double), cudaMemcpyHostToDevice));
+    p->goal_host.assign(q, q + p->D);
+    p->has_goal = 1;
+    p->prm.goal_radius = radius;
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_run(mptg_planner* p, int max_wavefronts, double time_limit_s, int stop_when_solved,
+                             int* solved) {
+    if (!p) return MPTG_ERR_INVALID_ARG;
+    mptg_ctx* ctx = p->ctx;
+    size_t n = 0;
+    mptg_tree_size(p->tree, &n);
+    if (n == 0) return mptg_fail(ctx, MPTG_ERR_NO_START, "there are no valid initial states");
+    if (p->solving) return mptg_fail(ctx, MPTG_ERR_ALREADY_SOLVING, "already solving");
+    p->solving = true;
+    MPTG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    auto t0 = std::chrono::steady_clock::now();
+    mptg_status st = MPTG_OK;
+    for (int it = 0; max_wavefronts <= 0 || it < max_wavefronts; ++it) {
+        if (stop_when_solved && !p->goals.empty()) break;
+        mptg_tree_size(p->tree, &n);
+        if (n >= p->prm.max_nodes) break;
+        double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (time_limit_s > 0 && el >= time_limit_s) break;
+        int added = 0;
+        st = plan_wavefront(p, nullptr, &added);
+        if (st) break;
+    }
+    p->stat_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    p->solving = false;
+    if (solved) *solved = p->goals.empty() ? 0 : 1;
+    return st;
+}
+
+mptg_status mptg_planner_size(mptg_planner* p, size_t* n) {
+    if (!p || !n) return MPTG_ERR_INVALID_ARG;
+    return mptg_tree_size(p->tree, n);
+}
+
+mptg_status mptg_planner_goals(mptg_planner* p, size_t* n) {
+    if (!p || !n) return MPTG_ERR_INVALID_ARG;
+    *n = p->goals.size();
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_solution(mptg_planner* p, double* path, size_t cap, size_t* len, double* cost) {
+    if (!p || !len) return MPTG_ERR_INVALID_ARG;
+    mptg_ctx* ctx = p->ctx;
+    *len = 0;
+    if (cost) *cost = INFINITY;
+    if (p->goals.empty()) return MPTG_OK;
+    int* dids = nullptr;
+    double* dout = nullptr;
+    MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&dout, 2 * sizeof(double)));
+    // best goal by path cost; goals are visited newest first with strict <,
+    // as PRRT::bestSolution walks its push_front list (prrt.hpp:219-234)
+    double best = INFINITY;
+    int bestg = -1, bestlen = 0;
+    for (size_t k = p->goals.size(); k-- > 0;) {
+        k_plan_path<<<1, 1>>>(p->goals[k], p->parent, mptg_tree_states_dev(p->tree), p->D, p->metric, p->w0, p->w1, 0,
+                              nullptr, dout);
+        MPTG_LAUNCHED(ctx);
+        double h[2];
+        cudaError_t e = cudaMemcpy(h, dout, sizeof(h), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) { cudaFree(dout); return mptg_fail(ctx, MPTG_ERR_CUDA, "%s", cudaGetErrorString(e)); }
+        if (h[0] < best || bestg < 0) { best = h[0]; bestg = p->goals[k]; bestlen = (int)h[1]; }
+    }
+    *len = (size_t)bestlen;
+    if (cost) *cost = best;
+    if (!path) { cudaFree(dout); return MPTG_OK; }
+    if ((size_t)bestlen > cap) {
+        cudaFree(dout);
+        return mptg_fail(ctx, MPTG_ERR_CAPACITY, "path of %d states does not fit %zu", bestlen, cap);
+    }
+    cudaError_t e = cudaMalloc((void**)&dids, bestlen * sizeof(int));
+    if (e != cudaSuccess) { cudaFree(dout); return mptg_fail(ctx, MPTG_ERR_OOM, "%s", cudaGetErrorString(e)); }
+    k_plan_path<<<1, 1>>>(bestg, p->parent, mptg_tree_states_dev(p->tree), p->D, p->metric, p->w0, p->w1, bestlen,
+                          dids, dout);
+    MPTG_LAUNCHED(ctx);
+    std::vector<int> ids(bestlen);
+    e = cudaMemcpy(ids.data(), dids, bestlen * sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(dids);
+    cudaFree(dout);
+    if (e != cudaSuccess) return mptg_fail(ctx, MPTG_ERR_CUDA, "%s", cudaGetErrorString(e));
+    for (int k = 0; k < bestlen; ++k) {
+        mptg_status st = mptg_tree_states(p->tree, ids[k], 1, path + (size_t)k * p->D, nullptr);
+        if (st) return st;
+    }
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_graph(mptg_planner* p, double* states, int32_t* parents, size_t cap, size_t* n) {
+    if (!p || !n) return MPTG_ERR_INVALID_ARG;
+    size_t sz = 0;
+    mptg_tree_size(p->tree, &sz);
+    *n = sz;
+    if (!states && !parents) return MPTG_OK;
+    if (sz > cap) return mptg_fail(p->ctx, MPTG_ERR_CAPACITY, "graph of %zu nodes does not fit %zu", sz, cap);
+    if (states) {
+        mptg_status st = mptg_tree_states(p->tree, 0, sz, states, nullptr);
+        if (st) return st;
+    }
+    if (parents) MPTG_CUDA_TRY(p->ctx, cudaMemcpy(parents, p->parent, sz * sizeof(int), cudaMemcpyDeviceToHost));
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_stats(mptg_planner* p, double out[8]) {
+    if (!p || !out) return MPTG_ERR_INVALID_ARG;
+    unsigned long long ns = 0;
+    MPTG_CUDA_TRY(p->ctx, cudaMemcpy(&ns, p->nsamp, sizeof(ns), cudaMemcpyDeviceToHost));
+    size_t n = 0;
+    mptg_tree_size(p->tree, &n);
+    out[0] = (double)p->stat_wavefronts;
+    out[1] = (double)p->stat_samples;
+    out[2] = (double)p->stat_accepted;
+    out[3] = (double)n;
+    out[4] = (double)p->goals.size();
+    out[5] = (double)ns;
+    out[6] = p->stat_seconds;
+    out[7] = (double)p->wave;
+    return MPTG_OK;
+}
+
+}  // extern "C"

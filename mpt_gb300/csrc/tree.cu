@@ -967,6 +967,8 @@ mptg_status mptg_tree_counters(mptg_tree* t, uint64_t out[5], int reset) {
     return MPTG_OK;
 }
 
+const double* mptg_tree_states_dev(const mptg_tree* t) { return t->states64; }
+
 // internal: launch the 1-NN search on device buffers (used by the planner too)
 mptg_status mptg_tree_nearest_dev(mptg_tree* t, const double* dq, int nq, int* didx, double* dd, cudaStream_t s,
                                   bool count) {

@@ -1,0 +1,12 @@
+// tree.cuh - internal (non-ABI) entry points of the device kd-tree for the
+// planner unit.
+#pragma once
+#include "common.cuh"
+
+extern "C" {
+// 1-NN of nq device queries into device outputs, asynchronous on s
+mptg_status mptg_tree_nearest_dev(mptg_tree* t, const double* dq, int nq, int* didx, double* dd, cudaStream_t s,
+                                  bool count);
+// device pointer to the FP64 master states [capacity][dim]
+const double* mptg_tree_states_dev(const mptg_tree* t);
+}

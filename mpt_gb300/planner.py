@@ -1,0 +1,316 @@
+"""Planner<Scenario, PRRT<options...>> mirror over the wavefront planner.
+
+Mirrors the reference's planner interface (src/mpt/planner.hpp:46-47,
+src/mpt/prrt.hpp:56-82, src/mpt/impl/prrt/prrt.hpp:149-316,
+src/mpt/impl/planner_base.hpp:58-80): ``add_start`` / ``addStart``,
+``solve(done_fn)``, ``solve_for`` / ``solveFor``, ``solve_until`` /
+``solveUntil``, ``solved``, ``size``, ``set_range`` / ``get_range``,
+``set_goal_bias`` / ``get_goal_bias``, ``solution()`` / ``solution(fn)``,
+``print_stats`` / ``printStats`` and ``visit_graph`` / ``visitGraph``.
+
+Scenarios follow the reference contract (space, bounds, valid, link, goal)
+through a GPU description of their collision world: ``Scenario(scene_dict)``
+for the grid, planar-arm and rigid-mesh scene kinds of mpt_gb300.scenes.
+
+Option tags: ``gpu_wavefront(W)`` (samples per wavefront), ``report_stats(b)``;
+the thread-count tags of planner_tags.hpp (``max_threads``,
+``single_threaded``, ``hardware_concurrency``) are accepted and have no effect
+because wavefronts replace the worker pool.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import time
+
+import numpy as np
+
+from . import Context, MptgError, Scene, _check, load
+
+
+# ------------------------------------------------------------------ option tags
+class gpu_wavefront:  # noqa: N801 (reference tag naming)
+    def __init__(self, n: int):
+        self.n = int(n)
+
+
+class report_stats:  # noqa: N801
+    def __init__(self, enabled: bool = True):
+        self.enabled = bool(enabled)
+
+
+class max_threads:  # noqa: N801
+    def __init__(self, n: int):
+        self.n = int(n)
+
+
+single_threaded = max_threads(1)
+hardware_concurrency = max_threads(0)
+
+
+class PRRT:
+    """Option pack (src/mpt/prrt.hpp:56-71); order of options does not matter."""
+
+    def __init__(self, *options):
+        self.wavefront = 4096
+        self.report_stats = False
+        for o in options:
+            if isinstance(o, gpu_wavefront):
+                self.wavefront = o.n
+            elif isinstance(o, report_stats):
+                self.report_stats = o.enabled
+            elif isinstance(o, max_threads):
+                pass
+            else:
+                raise TypeError("unknown PRRT option %r" % (o,))
+
+    def __eq__(self, other):
+        return isinstance(other, PRRT) and (self.wavefront, self.report_stats) == (other.wavefront,
+                                                                                   other.report_stats)
+
+
+class GoalState:
+    """GoalState(radius, state) (src/mpt/goal_state.hpp:43-90)."""
+
+    def __init__(self, radius: float, state):
+        self.radius = float(radius)
+        self.state = np.asarray(state, dtype=np.float64)
+
+
+class Scenario:
+    """A scenario described for the GPU: scene dict + goal + bounds + link resolution."""
+
+    def __init__(self, desc: dict, goal: GoalState | None = None):
+        self.desc = desc
+        self.goal = goal if goal is not None else GoalState(desc.get("goal_radius", 1e-6), desc["goal"])
+        self.lo = np.asarray(desc["lo"], dtype=np.float64)
+        self.hi = np.asarray(desc["hi"], dtype=np.float64)
+        self.edge_step = float(desc["edge_step"])
+        self.resolution = int(desc.get("resolution", 0))
+        self.default_range = float(desc.get("range", math.inf))
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("range", ctypes.c_double), ("goal_bias", ctypes.c_double), ("goal_radius", ctypes.c_double),
+                ("edge_step", ctypes.c_double), ("resolution", ctypes.c_int), ("wavefront", ctypes.c_int),
+                ("seed", ctypes.c_uint64), ("max_nodes", ctypes.c_size_t)]
+
+
+def _sig(L):
+    if getattr(L, "_planner_sig", False):
+        return
+    P, S = ctypes.c_void_p, ctypes.c_size_t
+    for name, res, args in [
+        ("mptg_planner_create", ctypes.c_int, [P, P, P, P, P, ctypes.POINTER(P)]),
+        ("mptg_planner_destroy", ctypes.c_int, [P]),
+        ("mptg_planner_add_start", ctypes.c_int, [P, P]),
+        ("mptg_planner_set_goal", ctypes.c_int, [P, P, ctypes.c_double]),
+        ("mptg_planner_run", ctypes.c_int, [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+        ("mptg_planner_size", ctypes.c_int, [P, ctypes.POINTER(S)]),
+        ("mptg_planner_goals", ctypes.c_int, [P, ctypes.POINTER(S)]),
+        ("mptg_planner_solution", ctypes.c_int, [P, P, S, ctypes.POINTER(S), ctypes.POINTER(ctypes.c_double)]),
+        ("mptg_planner_graph", ctypes.c_int, [P, P, P, S, ctypes.POINTER(S)]),
+        ("mptg_planner_stats", ctypes.c_int, [P, P]),
+    ]:
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    L._planner_sig = True
+
+
+class Planner:
+    """Planner<Scenario, PRRT<...>>(scenario, seed) on one GPU."""
+
+    def __init__(self, scenario: Scenario, algorithm: PRRT | None = None, seed: int | None = None,
+                 ctx: Context | None = None, max_nodes: int = 1 << 20):
+        self.lib = load()
+        _sig(self.lib)
+        self.ctx = ctx or Context(0)
+        self.scenario = scenario
+        self.algorithm = algorithm or PRRT()
+        if seed is None:  # RandomDeviceSeed: fresh entropy (src/mpt/random_device_seed.hpp:62-88)
+            seed = int.from_bytes(np.random.default_rng().bytes(8), "little")
+        self.seed = int(seed) & ((1 << 64) - 1)
+        self.max_nodes = int(max_nodes)
+        self._range = scenario.default_range
+        self._goal_bias = 0.01
+        self._starts = []
+        self.scene = Scene(self.ctx, scenario.desc)
+        self.h = None
+
+    # -- configuration (prrt.hpp:159-175)
+    def set_range(self, r: float):
+        assert r > 0
+        self._range = float(r)
+        self._require_fresh("set_range")
+
+    def get_range(self) -> float:
+        return self._range
+
+    def set_goal_bias(self, b: float):
+        assert 0 <= b <= 1
+        self._goal_bias = float(b)
+        self._require_fresh("set_goal_bias")
+
+    def get_goal_bias(self) -> float:
+        return self._goal_bias
+
+    def _require_fresh(self, what):
+        if self.h is not None:
+            raise RuntimeError("%s must be called before the first solve" % what)
+
+    # -- tree
+    def add_start(self, q):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        if self.h is None:
+            self._starts.append(q)
+        else:
+            _check(self.ctx.h, self.lib.mptg_planner_add_start(self.h, q.ctypes.data))
+
+    def _create(self):
+        if self.h is not None:
+            return
+        sc = self.scenario
+        prm = _Params()
+        prm.range = self._range if math.isfinite(self._range) else 0.0
+        prm.goal_bias = self._goal_bias
+        prm.goal_radius = sc.goal.radius
+        prm.edge_step = sc.edge_step
+        prm.resolution = sc.resolution
+        prm.wavefront = self.algorithm.wavefront
+        prm.seed = self.seed
+        prm.max_nodes = self.max_nodes
+        h = ctypes.c_void_p()
+        _check(self.ctx.h, self.lib.mptg_planner_create(self.ctx.h, self.scene.h, ctypes.byref(prm),
+                                                        sc.lo.ctypes.data, sc.hi.ctypes.data, ctypes.byref(h)))
+        self.h = h
+        g = np.ascontiguousarray(sc.goal.state, dtype=np.float64)
+        _check(self.ctx.h, self.lib.mptg_planner_set_goal(h, g.ctypes.data, sc.goal.radius))
+        for q in self._starts:
+            _check(self.ctx.h, self.lib.mptg_planner_add_start(h, q.ctypes.data))
+        self._starts = []
+
+    # -- solving (planner_base.hpp:58-80, prrt.hpp:194-201)
+    def run(self, max_wavefronts: int = 1, time_limit: float = 0.0, stop_when_solved: bool = False) -> bool:
+        self._create()
+        solved = ctypes.c_int(0)
+        _check(self.ctx.h, self.lib.mptg_planner_run(self.h, int(max_wavefronts), float(time_limit),
+                                                     int(stop_when_solved), ctypes.byref(solved)))
+        return bool(solved.value)
+
+    def solve(self, done_fn):
+        """Runs wavefronts until done_fn() is true (polled between wavefronts)."""
+        self._create()
+        if self.size() == 0:
+            raise RuntimeError("there are no valid initial states")
+        while not done_fn():
+            before = self.stats()["wavefront_counter"]
+            self.run(1)
+            if self.stats()["wavefront_counter"] == before:  # node budget exhausted
+                break
+
+    def solve_for(self, seconds: float, done_fn=None):
+        deadline = time.monotonic() + seconds
+        self.solve_until(deadline, done_fn)
+
+    def solve_until(self, deadline: float, done_fn=None):
+        if done_fn is None:
+            self.solve(lambda: time.monotonic() >= deadline)
+        else:
+            self.solve(lambda: time.monotonic() >= deadline or done_fn())
+
+    def solved(self) -> bool:
+        if self.h is None:
+            return False
+        n = ctypes.c_size_t()
+        _check(self.ctx.h, self.lib.mptg_planner_goals(self.h, ctypes.byref(n)))
+        return n.value > 0
+
+    def size(self) -> int:
+        if self.h is None:
+            return len(self._starts)
+        n = ctypes.c_size_t()
+        _check(self.ctx.h, self.lib.mptg_planner_size(self.h, ctypes.byref(n)))
+        return n.value
+
+    # -- results (prrt.hpp:208-316)
+    def solution(self, fn=None):
+        if self.h is None:
+            return []
+        n = ctypes.c_size_t()
+        cost = ctypes.c_double()
+        _check(self.ctx.h, self.lib.mptg_planner_solution(self.h, None, 0, ctypes.byref(n), ctypes.byref(cost)))
+        D = self.scene.dim
+        path = np.empty((n.value, D), dtype=np.float64)
+        if n.value:
+            _check(self.ctx.h, self.lib.mptg_planner_solution(self.h, path.ctypes.data, n.value, ctypes.byref(n),
+                                                              ctypes.byref(cost)))
+        self.last_cost = cost.value
+        if fn is None:
+            return [p for p in path]
+        for p in path:
+            fn(p)
+        return None
+
+    def solution_cost(self) -> float:
+        self.solution()
+        return self.last_cost
+
+    def graph(self):
+        n = ctypes.c_size_t()
+        _check(self.ctx.h, self.lib.mptg_planner_graph(self.h, None, None, 0, ctypes.byref(n)))
+        states = np.empty((n.value, self.scene.dim), dtype=np.float64)
+        parents = np.empty(n.value, dtype=np.int32)
+        _check(self.ctx.h, self.lib.mptg_planner_graph(self.h, states.ctypes.data, parents.ctypes.data, n.value,
+                                                       ctypes.byref(n)))
+        return states, parents
+
+    def visit_graph(self, visitor):
+        states, parents = self.graph()
+        for i in range(len(states)):
+            visitor.vertex(states[i])
+            if parents[i] >= 0:
+                visitor.edge(states[parents[i]])
+
+    def stats(self) -> dict:
+        out = (ctypes.c_double * 8)()
+        _check(self.ctx.h, self.lib.mptg_planner_stats(self.h, out))
+        keys = ["wavefronts", "samples", "nodes_added", "tree_size", "goals", "link_states_checked", "seconds",
+                "wavefront_counter"]
+        return dict(zip(keys, [float(v) for v in out]))
+
+    def print_stats(self):
+        s = self.stats() if self.h is not None else {}
+        print("nodes in graph: %d" % self.size())
+        if self.solved():
+            self.solution()
+            print("solutions: %d, best cost=%g" % (s.get("goals", 0), self.last_cost))
+        if self.algorithm.report_stats:
+            for k, v in s.items():
+                print("%s: %g" % (k, v))
+
+    def close(self):
+        if self.h is not None:
+            self.lib.mptg_planner_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # reference spellings
+    addStart = add_start
+    solveFor = solve_for
+    solveUntil = solve_until
+    setRange = set_range
+    getRange = get_range
+    setGoalBias = set_goal_bias
+    getGoalBias = get_goal_bias
+    printStats = print_stats
+    visitGraph = visit_graph
+
+
+__all__ = ["Planner", "PRRT", "Scenario", "GoalState", "gpu_wavefront", "report_stats", "max_threads",
+           "single_threaded", "hardware_concurrency", "MptgError"]

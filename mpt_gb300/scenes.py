@@ -60,24 +60,36 @@ def _arm_clearance(q: np.ndarray, link_len: np.ndarray, discs: np.ndarray) -> np
     ang = np.cumsum(q, axis=1)
     px = np.concatenate([np.zeros((q.shape[0], 1)), np.cumsum(link_len * np.cos(ang), axis=1)], axis=1)
     py = np.concatenate([np.zeros((q.shape[0], 1)), np.cumsum(link_len * np.sin(ang), axis=1)], axis=1)
+    def pt_seg(qx, qy, ax, ay, bx, by):
+        vx, vy = bx - ax, by - ay
+        c2 = vx * vx + vy * vy
+        t = np.clip(((qx - ax) * vx + (qy - ay) * vy) / np.maximum(c2, 1e-300), 0.0, 1.0)
+        dx, dy = ax + t * vx - qx, ay + t * vy - qy
+        return np.sqrt(dx * dx + dy * dy)
+
     best = np.full(q.shape[0], np.inf)
     for i in range(q.shape[1]):
         ax, ay, bx, by = px[:, i:i + 1], py[:, i:i + 1], px[:, i + 1:i + 2], py[:, i + 1:i + 2]
-        vx, vy = bx - ax, by - ay
-        wx, wy = discs[None, :, 0] - ax, discs[None, :, 1] - ay
-        c2 = vx * vx + vy * vy
-        t = np.clip((vx * wx + vy * wy) / np.maximum(c2, 1e-300), 0.0, 1.0)
-        dx, dy = ax + t * vx - discs[None, :, 0], ay + t * vy - discs[None, :, 1]
-        d = np.sqrt(dx * dx + dy * dy) - discs[None, :, 2]
+        d = pt_seg(discs[None, :, 0], discs[None, :, 1], ax, ay, bx, by) - discs[None, :, 2]
         best = np.minimum(best, d.min(axis=1))
-    # self-intersection margin: distance between non-adjacent link midpoints is a
-    # weak proxy; states whose links come within 0.02 of each other are rejected
+    # non-adjacent links: distance between the segments (the minimum of the four
+    # endpoint-to-segment distances, valid when they do not cross; crossing
+    # segments have an endpoint distance that the orientation test catches below)
     for i in range(q.shape[1]):
         for j in range(i + 2, q.shape[1]):
-            mx = 0.5 * (px[:, i] + px[:, i + 1]) - 0.5 * (px[:, j] + px[:, j + 1])
-            my = 0.5 * (py[:, i] + py[:, i + 1]) - 0.5 * (py[:, j] + py[:, j + 1])
-            dd = np.sqrt(mx * mx + my * my) - 0.5 * (link_len[i] + link_len[j]) - 0.02
-            best = np.minimum(best, dd + 1.0)  # only a coarse filter
+            a = (px[:, i], py[:, i], px[:, i + 1], py[:, i + 1])
+            b = (px[:, j], py[:, j], px[:, j + 1], py[:, j + 1])
+            d = np.minimum.reduce([pt_seg(a[0], a[1], *b), pt_seg(a[2], a[3], *b), pt_seg(b[0], b[1], *a),
+                                   pt_seg(b[2], b[3], *a)])
+
+            def orient(p, r, s):
+                return (r[0] - p[0]) * (s[1] - p[1]) - (r[1] - p[1]) * (s[0] - p[0])
+            o1 = orient((a[0], a[1]), (a[2], a[3]), (b[0], b[1]))
+            o2 = orient((a[0], a[1]), (a[2], a[3]), (b[2], b[3]))
+            o3 = orient((b[0], b[1]), (b[2], b[3]), (a[0], a[1]))
+            o4 = orient((b[0], b[1]), (b[2], b[3]), (a[2], a[3]))
+            cross = (o1 * o2 <= 0) & (o3 * o4 <= 0)
+            best = np.minimum(best, np.where(cross, -1.0, d))
     return best
 
 
@@ -105,7 +117,7 @@ def arm_scene(seed: int = 20261205, nlinks: int = 10, link: float = 0.1, ndiscs:
         "kind": "arm", "link_len": link_len, "discs": discs, "robot_radius": 0.0, "self_collision": 1,
         "metric": SO2, "dim": nlinks, "weights": (1.0, 1.0),
         "lo": np.full(nlinks, -math.pi), "hi": np.full(nlinks, math.pi),
-        "start": pts[0], "goal": pts[1], "goal_radius": 1e-6, "range": 2.0,
+        "start": pts[0], "goal": pts[1], "goal_radius": 1e-6, "range": 1.0,
         "edge_step": 0.01, "resolution": 1,
     }
 

@@ -225,6 +225,55 @@ def valid_edges(desc: dict, space: Space, a: np.ndarray, b: np.ndarray, step: fl
     return out, ns.value
 
 
+class PlanParams(ctypes.Structure):
+    _fields_ = [("range", ctypes.c_double), ("goal_bias", ctypes.c_double), ("goal_radius", ctypes.c_double),
+                ("edge_step", ctypes.c_double), ("resolution", ctypes.c_int), ("wavefront", ctypes.c_int),
+                ("seed", ctypes.c_uint64), ("max_nodes", ctypes.c_int64)]
+
+
+def plan(desc: dict, space: Space, params: dict, lo, hi, start, goal, max_waves: int, stop_when_solved: bool,
+         nthreads: int = 0):
+    """Replay of the wavefront planner: (states, parents, goal ids)."""
+    L = lib()
+    if not getattr(L, "_plan_sig", False):
+        P = ctypes.c_void_p
+        L.orc_plan.restype = ctypes.c_int64
+        L.orc_plan.argtypes = [P, P, P, P, P, P, P, ctypes.c_int, ctypes.c_int, P, P, P, P, ctypes.c_int]
+        L.orc_uniform.restype = ctypes.c_double
+        L.orc_uniform.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]
+        L._plan_sig = True
+    sc, keep = make_scene(desc)
+    pp = PlanParams()
+    for k in ("range", "goal_bias", "goal_radius", "edge_step"):
+        setattr(pp, k, float(params[k]))
+    pp.resolution = int(params["resolution"])
+    pp.wavefront = int(params["wavefront"])
+    pp.seed = int(params["seed"])
+    pp.max_nodes = int(params["max_nodes"])
+    D = space.dim
+    lo = np.ascontiguousarray(lo, dtype=np.float64)
+    hi = np.ascontiguousarray(hi, dtype=np.float64)
+    start = np.ascontiguousarray(start, dtype=np.float64)
+    g = None if goal is None else np.ascontiguousarray(goal, dtype=np.float64)
+    states = np.empty((pp.max_nodes, D), dtype=np.float64)
+    parents = np.empty(pp.max_nodes, dtype=np.int32)
+    goals = np.empty(pp.max_nodes, dtype=np.int32)
+    ng = ctypes.c_int64(0)
+    n = L.orc_plan(ctypes.byref(sc), ctypes.byref(space), ctypes.byref(pp), _ptr(lo), _ptr(hi), _ptr(start),
+                   None if g is None else _ptr(g), int(max_waves), int(stop_when_solved), _ptr(states), _ptr(parents),
+                   _ptr(goals), ctypes.byref(ng), nthreads or os.cpu_count())
+    return states[:n].copy(), parents[:n].copy(), goals[:ng.value].copy()
+
+
+def uniform(seed: int, i: int, w: int, j: int) -> float:
+    lib()
+    if not getattr(_lib, "_plan_sig", False):
+        plan  # signatures are set on first plan(); set the one needed here
+        _lib.orc_uniform.restype = ctypes.c_double
+        _lib.orc_uniform.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]
+    return _lib.orc_uniform(seed, i, w, j)
+
+
 def tri_tri(t1, t2) -> bool:
     t1 = np.ascontiguousarray(t1, dtype=np.float64).reshape(9)
     t2 = np.ascontiguousarray(t2, dtype=np.float64).reshape(9)

@@ -745,3 +745,111 @@ void orc_valid_edges(const orc_scene* sc, const orc_space* sp, const double* a, 
     }
     if (samples) *samples = total;
 }
+
+/* ------------------------------------------------------------------ */
+/* Wavefront planner, restated for the checker.
+ *
+ * The reference's worker loop (src/mpt/impl/prrt/prrt.hpp:358-452) run as the
+ * GPU planner runs it: wavefronts of W samples drawn from Philox4x32-10
+ * (Salmon, Moraes, Dror, Shaw, SC'11: round function and constants as
+ * published) addressed by (sample, wavefront, block); every sample of a
+ * wavefront sees the tree as it stood before the wavefront; accepted samples
+ * are appended in sample order.  Per sample: goal with probability goal_bias
+ * until the first solution (:363-389), nearest (exact, lowest id), skip when
+ * d == 0 (:425), steer to range (:430-434), valid + link through the DMV
+ * (:439-442), GoalState test (:443-445), insert with parent (:447). */
+static void orc_philox10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0;
+        uint32_t n1 = (uint32_t)p1;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+        uint32_t n3 = (uint32_t)p0;
+        c[0] = n0; c[1] = n1; c[2] = n2; c[3] = n3;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+double orc_uniform(uint64_t seed, uint32_t i, uint32_t w, uint32_t j) {
+    uint32_t c[4] = {i, w, j >> 1, 0x6d707467u};
+    orc_philox10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    uint32_t a = (j & 1) ? c[2] : c[0], b = (j & 1) ? c[3] : c[1];
+    uint64_t m = ((uint64_t)(a >> 5) << 26) | (uint64_t)(b >> 6);
+    return (double)m * (1.0 / 9007199254740992.0);
+}
+
+static void plan_sample(const orc_space* sp, const orc_plan_params* pp, const double* lo, const double* hi,
+                        const double* goal, int bias_on, uint32_t i, uint32_t w, double* q) {
+    int D = sp->dim;
+    if (goal && bias_on && pp->goal_bias > 0 && orc_uniform(pp->seed, i, w, 16) < pp->goal_bias) {
+        for (int d = 0; d < D; ++d) q[d] = goal[d];
+        return;
+    }
+    if (sp->metric == ORC_SO3 || sp->metric == ORC_SE3) {
+        /* Shoemake uniform rotation (src/mpt/impl/uniform_sampler_so3.hpp:55-68) */
+        double a = orc_uniform(pp->seed, i, w, 0);
+        double b = TWO_PI * orc_uniform(pp->seed, i, w, 1);
+        double c = TWO_PI * orc_uniform(pp->seed, i, w, 2);
+        double s1 = sqrt(1.0 - a), s2 = sqrt(a), sb, cb, sc, cc;
+        mptg_sincos(b, &sb, &cb);
+        mptg_sincos(c, &sc, &cc);
+        q[0] = s1 * sb; q[1] = s1 * cb; q[2] = s2 * sc; q[3] = s2 * cc;
+        for (int d = 4; d < D; ++d) q[d] = lo[d] + (hi[d] - lo[d]) * orc_uniform(pp->seed, i, w, (uint32_t)(d - 1));
+    } else if (sp->metric == ORC_SO2) {
+        for (int d = 0; d < D; ++d) q[d] = -PI + TWO_PI * orc_uniform(pp->seed, i, w, (uint32_t)d);
+    } else {
+        for (int d = 0; d < D; ++d) q[d] = lo[d] + (hi[d] - lo[d]) * orc_uniform(pp->seed, i, w, (uint32_t)d);
+    }
+}
+
+int64_t orc_plan(const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp, const double* lo,
+                 const double* hi, const double* start, const double* goal, int max_waves, int stop_when_solved,
+                 double* states, int32_t* parents, int32_t* goals, int64_t* ngoals, int nthreads) {
+    int D = sp->dim;
+    int W = pp->wavefront;
+    double range = pp->range > 0 ? pp->range : INFINITY;
+    double inv = 1.0 / pp->edge_step;
+    int64_t n = 1, ng = 0;
+    for (int d = 0; d < D; ++d) states[d] = start[d];
+    parents[0] = -1;
+    if (sc->kind == 2) get_env_bvh(sc);
+    double* nw = (double*)malloc((size_t)W * D * sizeof(double));
+    int32_t* par = (int32_t*)malloc((size_t)W * sizeof(int32_t));
+    uint8_t* ok = (uint8_t*)malloc((size_t)W);
+    for (int w = 0; w < max_waves; ++w) {
+        if (stop_when_solved && ng > 0) break;
+        if (n >= pp->max_nodes) break;
+        int bias_on = ng == 0;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads_or_default(nthreads))
+        for (int i = 0; i < W; ++i) {
+            double s[16], a[16];
+            plan_sample(sp, pp, lo, hi, goal, bias_on, (uint32_t)i, (uint32_t)w, s);
+            double best = INFINITY;
+            int32_t bi = -1;
+            for (int64_t j = 0; j < n; ++j) {
+                double dj = orc_distance(sp, s, states + j * D);
+                if (dj < best || (bi < 0 && dj == best)) { best = dj; bi = (int32_t)j; }
+            }
+            ok[i] = 0;
+            if (bi < 0 || best == 0.0 || best != best) continue;
+            for (int d = 0; d < D; ++d) a[d] = states[(int64_t)bi * D + d];
+            double* q = nw + (size_t)i * D;
+            if (best > range) orc_interpolate(sp, a, s, range / best, q);
+            else for (int d = 0; d < D; ++d) q[d] = s[d];
+            par[i] = bi;
+            ok[i] = (uint8_t)dmv_edge(sc, sp, a, q, inv, pp->resolution, NULL);
+        }
+        for (int i = 0; i < W && n < pp->max_nodes; ++i) {
+            if (!ok[i]) continue;
+            for (int d = 0; d < D; ++d) states[n * D + d] = nw[(size_t)i * D + d];
+            parents[n] = par[i];
+            if (goal && orc_distance(sp, nw + (size_t)i * D, goal) <= pp->goal_radius) goals[ng++] = (int32_t)n;
+            ++n;
+        }
+    }
+    free(nw); free(par); free(ok);
+    *ngoals = ng;
+    return n;
+}

@@ -58,6 +58,18 @@ void orc_valid_edges(const orc_scene* sc, const orc_space* sp, const double* a, 
                      int64_t n, double step, int resolution, uint8_t* out, int64_t* samples,
                      int nthreads);
 
+/* Wavefront planner replay (see oracle.c). */
+typedef struct {
+    double range, goal_bias, goal_radius, edge_step;
+    int resolution, wavefront;
+    uint64_t seed;
+    int64_t max_nodes;
+} orc_plan_params;
+double orc_uniform(uint64_t seed, uint32_t i, uint32_t w, uint32_t j);
+int64_t orc_plan(const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp, const double* lo,
+                 const double* hi, const double* start, const double* goal, int max_waves, int stop_when_solved,
+                 double* states, int32_t* parents, int32_t* goals, int64_t* ngoals, int nthreads);
+
 /* Triangle-triangle intersection (FP64 orientation predicates). */
 int orc_tri_tri(const double* t1, const double* t2);
 
