@@ -71,12 +71,22 @@ struct mptg_planner {
 
 // ------------------------------------------------------------------ kernels
 
-__global__ void k_plan_sample(PlanView p, int W, uint32_t wave, int bias_on, double* __restrict__ out) {
+// At most one goal sample per wavefront: the lowest-index sample whose bias
+// draw hits.  Identical goal samples would all steer from the same nearest
+// node to the same new state; the reference draws goal samples on one worker
+// and its d == 0 test rejects repeats (prrt.hpp:363-389,425).
+__global__ void k_plan_goalpick(PlanView p, int W, uint32_t wave, int* __restrict__ first) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W) return;
+    if (phx_uniform(p.seed, (uint32_t)i, wave, 16) < p.goal_bias) atomicMin(first, i);
+}
+
+__global__ void k_plan_sample(PlanView p, int W, uint32_t wave, const int* __restrict__ goal_index,
+                              double* __restrict__ out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= W) return;
     double* q = out + (size_t)i * p.D;
-    bool goal = false;
-    if (p.has_goal && bias_on && p.goal_bias > 0) goal = phx_uniform(p.seed, (uint32_t)i, wave, 16) < p.goal_bias;
+    bool goal = goal_index != nullptr && i == *goal_index;
     if (goal) {
         for (int d = 0; d < p.D; ++d) q[d] = p.goal[d];
         return;
@@ -260,8 +270,15 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
     mptg_tree_size(p->tree, &n0);
     if (n0 >= p->prm.max_nodes) return MPTG_OK;
     PlanView v = plan_view(p);
-    int bias_on = p->goals.empty() ? 1 : 0;
-    k_plan_sample<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->wave, bias_on, p->samp);
+    bool bias_on = p->goals.empty() && p->has_goal && p->prm.goal_bias > 0;
+    int* gidx = nullptr;
+    if (bias_on) {
+        gidx = p->bsum + 1024 + 1;  // scratch word after the scan block sums
+        MPTG_CUDA_TRY(ctx, cudaMemsetAsync(gidx, 0x7f, sizeof(int), s));
+        k_plan_goalpick<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->wave, gidx);
+        MPTG_LAUNCHED(ctx);
+    }
+    k_plan_sample<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->wave, gidx, p->samp);
     mptg_status st = mptg_tree_nearest_dev(p->tree, p->samp, W, p->nidx, p->ndist, s, false);
     if (st) return st;
     k_plan_steer<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->samp, p->nidx, p->ndist, mptg_tree_states_dev(p->tree),
@@ -341,7 +358,7 @@ mptg_status mptg_planner_create(mptg_ctx* ctx, mptg_scene* scene, const mptg_pla
     ALLOC(p->skip, W);
     ALLOC(p->ok, W);
     ALLOC(p->scan, W * sizeof(int));
-    ALLOC(p->bsum, (nblk + 1) * sizeof(int));
+    ALLOC(p->bsum, (1024 + 2) * sizeof(int));
     ALLOC(p->acc_states, W * D * sizeof(double));
     ALLOC(p->acc_parent, W * sizeof(int));
     ALLOC(p->acc_goal, W);

@@ -24,7 +24,10 @@
 namespace {
 
 enum { CNT_NODES = 0, CNT_BUCKETS = 1, CNT_NSEG_NEXT = 2, CNT_ERR = 3, CNT_OVF = 4, CNT_NREG = 5,
-       CNT_PERM = 6, CNT_MAXABS = 7, CNT_N = 8 };
+       CNT_PERM = 6, CNT_MAXABS = 7, CNT_MAXDEPTH = 8, CNT_N = 9 };
+
+// a leaf deeper than this triggers a rebuild of the whole tree
+#define MPTG_REBUILD_DEPTH 40
 
 enum { SEG_SPLIT = 0, SEG_LEAF = 1 };
 
@@ -60,6 +63,7 @@ struct mptg_tree {
     int* leaf_of = nullptr; int* ovf_pts = nullptr; int* ovf_leaf = nullptr; int* leaf_reg = nullptr;
     int* seg_cursor = nullptr;
     int* hcnt = nullptr;  // pinned
+    uint64_t rebuilds = 0;
 };
 
 struct TreeView {
@@ -308,6 +312,7 @@ __global__ void k_seg_c(SegState* __restrict__ cur, int nseg, SegState* __restri
         return;
     }
     nodes[S.node] = make_int4(dim, c, __float_as_int(split), 0);
+    atomicMax(&dcnt[CNT_MAXDEPTH], S.depth + 1);
     node_depth[c] = S.depth + 1;
     node_depth[c + 1] = S.depth + 1;
     for (int d = 0; d < D; ++d) {
@@ -823,7 +828,7 @@ mptg_status mptg_tree_create(mptg_ctx* ctx, mptg_metric metric, int dim, const d
         return mptg_fail(ctx, MPTG_ERR_OOM, "tree allocation failed: %s", cudaGetErrorString(e));
     }
     // root = empty leaf on bucket 0; root cell = the metric's domain
-    int hc[CNT_N] = {1, 1, 0, 0, 0, 0, 0, 0};
+    int hc[CNT_N] = {1, 1, 0, 0, 0, 0, 0, 0, 0};
     int4 root = make_int4(-1, 0, 0, 0);
     std::vector<float> lo(D), hi(D);
     for (size_t d = 0; d < D; ++d) {
@@ -870,6 +875,69 @@ static mptg_status read_counters(mptg_tree* t, cudaStream_t s) {
     return MPTG_OK;
 }
 
+// level-synchronous build of the `nseg` segments in segA over positions
+// [0, total) of perm/pseg
+static mptg_status build_levels(mptg_tree* t, cudaStream_t s, int nseg, int total) {
+    mptg_ctx* ctx = t->ctx;
+    const int D = t->D;
+    SegState* cur = t->segA;
+    SegState* prev = t->segB;
+    int* perm = t->perm; int* perm2 = t->perm2; int* pseg = t->pseg; int* pseg2 = t->pseg2;
+    const unsigned tb = 256;
+    mptg_status st;
+    for (int level = 0; nseg > 0 && level < 4 * MPTG_MAX_DEPTH; ++level) {
+        MPTG_CUDA_TRY(ctx, cudaMemsetAsync(t->dcnt + CNT_NSEG_NEXT, 0, sizeof(int), s));
+        k_seg_a<<<mptg_blocks(nseg, 128), 128, 0, s>>>(cur, nseg, prev, t->nodes, t->dcnt, t->bucket_cap,
+                                                       t->seg_box, D);
+        k_seg_b<<<mptg_blocks(total, tb), tb, 0, s>>>(cur, perm, pseg, pseg2, total, t->pts32, D, t->bpts,
+                                                      t->bids, t->seg_box);
+        k_seg_c<<<mptg_blocks(nseg, 128), 128, 0, s>>>(cur, nseg, prev, t->nodes, t->cell_lo, t->cell_hi,
+                                                       t->node_depth, t->dcnt, t->node_cap, t->seg_cap,
+                                                       t->seg_box, D, t->metric, (float)t->w0, (float)t->w1);
+        k_seg_d<<<mptg_blocks(total, tb), tb, 0, s>>>(cur, perm, pseg, perm2, pseg2, total, t->pts32, D);
+        ctx->launches += 4;
+        st = read_counters(t, s);
+        if (st) return st;
+        nseg = t->hcnt[CNT_NSEG_NEXT];
+        if (nseg > t->seg_cap || (t->hcnt[CNT_ERR] & MPTG_DEVERR_CAPACITY))
+            return mptg_fail(ctx, MPTG_ERR_CAPACITY, "kd-tree build ran out of node/segment capacity");
+        // next level: the children just written to `prev` become current
+        SegState* tmp = cur; cur = prev; prev = tmp;
+        int* tp = perm; perm = perm2; perm2 = tp;
+        tp = pseg; pseg = pseg2; pseg2 = tp;
+    }
+    if (nseg > 0) return mptg_fail(ctx, MPTG_ERR_CAPACITY, "kd-tree build did not converge");
+    return MPTG_OK;
+}
+
+__global__ void k_rebuild_init(int n, int* __restrict__ perm, int* __restrict__ pseg) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    perm[i] = i;
+    pseg[i] = 0;
+}
+
+// drop every node and bucket and build the tree again from all t->n points
+static mptg_status rebuild_all(mptg_tree* t, cudaStream_t s) {
+    mptg_ctx* ctx = t->ctx;
+    int n = (int)t->n;
+    // node 0 stays the root (its cell is the metric's domain); buckets restart at 0
+    int hc[3] = {1, 0, 0};
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(t->dcnt + CNT_NODES, hc, 2 * sizeof(int), cudaMemcpyHostToDevice, s));
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(t->dcnt + CNT_MAXDEPTH, hc + 2, sizeof(int), cudaMemcpyHostToDevice, s));
+    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(t->dcnt + CNT_ERR, 0, sizeof(int), s));
+    k_rebuild_init<<<mptg_blocks(n, 256), 256, 0, s>>>(n, t->perm, t->pseg);
+    MPTG_LAUNCHED(ctx);
+    SegState root;
+    memset(&root, 0, sizeof(root));
+    root.node = 0; root.start = 0; root.count = n; root.depth = 0; root.parent = -1;
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(t->segA, &root, sizeof(root), cudaMemcpyHostToDevice, s));
+    mptg_status st = build_levels(t, s, 1, n);
+    if (st) return st;
+    t->rebuilds += 1;
+    return read_counters(t, s);
+}
+
 mptg_status mptg_tree_insert(mptg_tree* t, const double* states, size_t n, void* stream) {
     if (!t) return MPTG_ERR_INVALID_ARG;
     mptg_ctx* ctx = t->ctx;
@@ -908,40 +976,22 @@ mptg_status mptg_tree_insert(mptg_tree* t, const double* states, size_t n, void*
         k_ovf_scatter<<<mptg_blocks(novf, 256), 256, 0, s>>>(novf, first, t->ovf_pts, t->leaf_of, t->leaf_reg,
                                                              t->segA, t->seg_cursor, t->perm, t->pseg);
         ctx->launches += 2;
-        int total = MPTG_BUCKET * nreg + novf;
-        int nseg = nreg;
-        SegState* cur = t->segA;
-        SegState* prev = t->segB;
-        int* perm = t->perm; int* perm2 = t->perm2; int* pseg = t->pseg; int* pseg2 = t->pseg2;
-        const unsigned tb = 256;
-        for (int level = 0; nseg > 0 && level < 4 * MPTG_MAX_DEPTH; ++level) {
-            MPTG_CUDA_TRY(ctx, cudaMemsetAsync(t->dcnt + CNT_NSEG_NEXT, 0, sizeof(int), s));
-            k_seg_a<<<mptg_blocks(nseg, 128), 128, 0, s>>>(cur, nseg, prev, t->nodes, t->dcnt, t->bucket_cap,
-                                                           t->seg_box, D);
-            k_seg_b<<<mptg_blocks(total, tb), tb, 0, s>>>(cur, perm, pseg, pseg2, total, t->pts32, D, t->bpts,
-                                                          t->bids, t->seg_box);
-            k_seg_c<<<mptg_blocks(nseg, 128), 128, 0, s>>>(cur, nseg, prev, t->nodes, t->cell_lo, t->cell_hi,
-                                                           t->node_depth, t->dcnt, t->node_cap, t->seg_cap,
-                                                           t->seg_box, D, t->metric, (float)t->w0, (float)t->w1);
-            k_seg_d<<<mptg_blocks(total, tb), tb, 0, s>>>(cur, perm, pseg, perm2, pseg2, total, t->pts32, D);
-            ctx->launches += 4;
-            st = read_counters(t, s);
-            if (st) return st;
-            nseg = t->hcnt[CNT_NSEG_NEXT];
-            if (nseg > t->seg_cap || (t->hcnt[CNT_ERR] & MPTG_DEVERR_CAPACITY))
-                return mptg_fail(ctx, MPTG_ERR_CAPACITY, "kd-tree build ran out of node/segment capacity");
-            // next level: the children just written to `prev` become current
-            SegState* tmp = cur; cur = prev; prev = tmp;
-            int* tp = perm; perm = perm2; perm2 = tp;
-            tp = pseg; pseg = pseg2; pseg2 = tp;
-        }
-        if (nseg > 0) return mptg_fail(ctx, MPTG_ERR_CAPACITY, "kd-tree build did not converge");
+        st = build_levels(t, s, nreg, MPTG_BUCKET * nreg + novf);
+        if (st) return st;
     }
     MPTG_CUDA_TRY(ctx, cudaGetLastError());
     st = read_counters(t, s);
     if (st) return st;
+    t->n += n;
+    // Leaf splits only see the points of one leaf, so a tree that keeps
+    // growing at one frontier (a planner extending a corridor) degenerates
+    // into a chain.  When any leaf gets deeper than MPTG_REBUILD_DEPTH (or hit
+    // the depth limit) the whole tree is rebuilt from all its points.
+    if (t->hcnt[CNT_MAXDEPTH] > MPTG_REBUILD_DEPTH || (t->hcnt[CNT_ERR] & MPTG_DEVERR_DEPTH)) {
+        st = rebuild_all(t, s);
+        if (st) return st;
+    }
     int err = t->hcnt[CNT_ERR];
-    t->n += n;  // points are stored even when the tree reports a structural error
     if (err & MPTG_DEVERR_CAPACITY) return mptg_fail(ctx, MPTG_ERR_CAPACITY, "kd-tree node/bucket capacity exceeded");
     if (err & MPTG_DEVERR_DEPTH) return mptg_fail(ctx, MPTG_ERR_CAPACITY, "kd-tree depth limit reached");
     return MPTG_OK;

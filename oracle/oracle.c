@@ -780,10 +780,12 @@ double orc_uniform(uint64_t seed, uint32_t i, uint32_t w, uint32_t j) {
     return (double)m * (1.0 / 9007199254740992.0);
 }
 
+/* goal_index: the one sample of this wavefront that is the goal (the lowest
+ * index whose bias draw hits), or -1 */
 static void plan_sample(const orc_space* sp, const orc_plan_params* pp, const double* lo, const double* hi,
-                        const double* goal, int bias_on, uint32_t i, uint32_t w, double* q) {
+                        const double* goal, int goal_index, uint32_t i, uint32_t w, double* q) {
     int D = sp->dim;
-    if (goal && bias_on && pp->goal_bias > 0 && orc_uniform(pp->seed, i, w, 16) < pp->goal_bias) {
+    if (goal && (int)i == goal_index) {
         for (int d = 0; d < D; ++d) q[d] = goal[d];
         return;
     }
@@ -821,11 +823,16 @@ int64_t orc_plan(const orc_scene* sc, const orc_space* sp, const orc_plan_params
     for (int w = 0; w < max_waves; ++w) {
         if (stop_when_solved && ng > 0) break;
         if (n >= pp->max_nodes) break;
-        int bias_on = ng == 0;
+        /* at most one goal sample per wavefront: the lowest index whose bias
+         * draw hits (the reference draws goal samples on one worker only) */
+        int goal_index = -1;
+        if (goal && ng == 0 && pp->goal_bias > 0)
+            for (int i = 0; i < W; ++i)
+                if (orc_uniform(pp->seed, (uint32_t)i, (uint32_t)w, 16) < pp->goal_bias) { goal_index = i; break; }
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads_or_default(nthreads))
         for (int i = 0; i < W; ++i) {
             double s[16], a[16];
-            plan_sample(sp, pp, lo, hi, goal, bias_on, (uint32_t)i, (uint32_t)w, s);
+            plan_sample(sp, pp, lo, hi, goal, goal_index, (uint32_t)i, (uint32_t)w, s);
             double best = INFINITY;
             int32_t bi = -1;
             for (int64_t j = 0; j < n; ++j) {

@@ -70,6 +70,23 @@ def test_nearest_ties_and_duplicates(ctx, orc):
     assert gi[1] == 0  # lowest id among 100 identical points at distance 0
 
 
+def test_frontier_growth_rebuilds_and_stays_exact(ctx, orc):
+    """A tree grown at one frontier (points along a line, in small batches)
+    degenerates under leaf splits; the depth-triggered rebuild keeps it
+    searchable and exact."""
+    import mpt_gb300 as m
+    rng = np.random.default_rng(3)
+    t = np.linspace(0, 1000, 20000)
+    pts = np.stack([t, 0.001 * np.sin(t)], 1) + rng.normal(0, 1e-3, (20000, 2))
+    tree = m.Tree(ctx, 0, 2, len(pts))
+    for lo in range(0, len(pts), 100):
+        tree.insert(pts[lo:lo + 100])
+    q = np.stack([rng.uniform(-10, 1010, 3000), rng.uniform(-5, 5, 3000)], 1)
+    oi, od = orc.nn_brute(orc.make_space(0, 2), pts, q)
+    gi, gd = tree.nearest(q)
+    assert np.array_equal(gi, oi) and np.array_equal(gd, od)
+
+
 def test_empty_and_single(ctx):
     import mpt_gb300 as m
     tree = m.Tree(ctx, 1, 3, 10)

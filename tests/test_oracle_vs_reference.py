@@ -64,11 +64,11 @@ def test_dmv_bit_exact_with_sample_counts(orc, mk):
     step = 1.0 if sc["kind"] == "grid" else 0.02
     a, b = scenes.steered_edges(sc, 400, 77)
     if sc["kind"] == "arm":
-        # long edges too: more than 256 interior samples exercise the queue's
-        # switch to sequential scanning
-        a2 = scenes.uniform_states(sc, 100, 78)
-        b2 = scenes.uniform_states(sc, 100, 79)
-        a, b = np.concatenate([a, a2]), np.concatenate([b, b2])
+        # long edges in an obstacle-free arm scene: more than 256 interior
+        # samples, all valid, exercise the queue's switch to sequential scanning
+        sc = dict(sc, discs=np.zeros((0, 3)), self_collision=0)
+        a = scenes.uniform_states(sc, 100, 78)
+        b = scenes.uniform_states(sc, 100, 79)
         step = 0.005
     csc, keep = orc.make_scene(sc)
     n = len(a)
