@@ -200,9 +200,9 @@ class Planner:
 
     def solve(self, done_fn):
         """Runs wavefronts until done_fn() is true (polled between wavefronts)."""
-        self._create()
         if self.size() == 0:
             raise RuntimeError("there are no valid initial states")
+        self._create()
         while not done_fn():
             before = self.stats()["wavefront_counter"]
             self.run(1)
