@@ -64,6 +64,11 @@ struct mptg_tree {
     int* seg_cursor = nullptr;
     int* hcnt = nullptr;  // pinned
     uint64_t rebuilds = 0;
+    // query ordering scratch (grown on demand)
+    int* qkey = nullptr;
+    int* qorder = nullptr;
+    int* qhist = nullptr;
+    size_t qcap = 0;
 };
 
 struct TreeView {
@@ -489,12 +494,16 @@ __device__ __forceinline__ void load_query(const double* __restrict__ qd, int D,
         if (lane == d) myq = q[d];
 }
 
+// order (may be null): warp w answers query order[w], so that neighbouring
+// warps, sorted by tree region, reuse each other's nodes in L1
 template <int MK, int DMAX>
-__global__ void __launch_bounds__(256) k_nearest(TreeView t, const double* __restrict__ q64, int nq,
-                                                 int* __restrict__ out_idx, double* __restrict__ out_d) {
+__global__ void __launch_bounds__(256, 5) k_nearest(TreeView t, const double* __restrict__ q64, int nq,
+                                                 const int* __restrict__ order, int* __restrict__ out_idx,
+                                                 double* __restrict__ out_d) {
     const int lane = threadIdx.x & 31;
-    const int qi = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-    if (qi >= nq) return;
+    const int wi = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    if (wi >= nq) return;
+    const int qi = order ? __ldg(&order[wi]) : wi;
     const int D = t.D;
     const double* qd = q64 + (size_t)qi * D;
     float q[DMAX];
@@ -730,28 +739,89 @@ __global__ void __launch_bounds__(256) k_nearest_k(TreeView t, const double* __r
     if (lane + 32 < k) { bool v = lane + 32 < cnt; oi[lane + 32] = v ? li1 : -1; od[lane + 32] = v ? ld1 : INFINITY; }
 }
 
+// ------------------------------------------------------------------ query order
+// Queries are answered in the order of the tree region they fall in: the key
+// is the first MPTG_QSORT_BITS left/right decisions of the query's descent,
+// and a counting sort over 2^16 bins groups queries of the same subtree, so
+// the warps of a block share the nodes and buckets they visit.
+#define MPTG_QSORT_BITS 16
+#define MPTG_QSORT_BINS (1 << MPTG_QSORT_BITS)
+#define MPTG_QSORT_MIN 2048  // smaller batches are answered in input order
+
+__global__ void k_qkey(TreeView t, const double* __restrict__ q64, int nq, int* __restrict__ key,
+                       int* __restrict__ hist) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    const double* qd = q64 + (size_t)i * t.D;
+    int node = 0;
+    unsigned k = 0;
+    int lev = 0;
+    for (; lev < MPTG_QSORT_BITS; ++lev) {
+        int4 nd = __ldg(&t.nodes[node]);
+        if (nd.x < 0) break;
+        int right = !(__double2float_rn(qd[nd.x]) < __int_as_float(nd.z));
+        k = (k << 1) | (unsigned)right;
+        node = nd.y + right;
+    }
+    k <<= (MPTG_QSORT_BITS - lev);
+    key[i] = (int)k;
+    atomicAdd(&hist[k], 1);
+}
+
+// in-place exclusive scan of the 2^16-bin histogram: one block, 64 bins per thread
+__global__ void __launch_bounds__(1024) k_qscan(int* __restrict__ hist) {
+    __shared__ int s[1024];
+    const int t = threadIdx.x;
+    const int base = t * (MPTG_QSORT_BINS / 1024);
+    int sum = 0;
+    for (int j = 0; j < MPTG_QSORT_BINS / 1024; ++j) sum += hist[base + j];
+    s[t] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        int v = t >= o ? s[t - o] : 0;
+        __syncthreads();
+        s[t] += v;
+        __syncthreads();
+    }
+    int run = t ? s[t - 1] : 0;
+    for (int j = 0; j < MPTG_QSORT_BINS / 1024; ++j) {
+        int c = hist[base + j];
+        hist[base + j] = run;
+        run += c;
+    }
+}
+
+__global__ void k_qscatter(int nq, const int* __restrict__ key, int* __restrict__ hist, int* __restrict__ order) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    order[atomicAdd(&hist[key[i]], 1)] = i;
+}
+
 // ------------------------------------------------------------------ host side
+
+// exact-size register arrays for the common dimensions keep register use
+// (and so occupancy) proportional to D
+#define DISPATCH_DIMS(MK, D, KERNEL, grid, block, stream, ...)                                          \
+    if (D <= 2) KERNEL<MK, 2><<<grid, block, 0, stream>>>(__VA_ARGS__);                                 \
+    else if (D <= 3) KERNEL<MK, 3><<<grid, block, 0, stream>>>(__VA_ARGS__);                            \
+    else if (D <= 4) KERNEL<MK, 4><<<grid, block, 0, stream>>>(__VA_ARGS__);                            \
+    else if (D <= 6) KERNEL<MK, 6><<<grid, block, 0, stream>>>(__VA_ARGS__);                            \
+    else if (D <= 8) KERNEL<MK, 8><<<grid, block, 0, stream>>>(__VA_ARGS__);                            \
+    else if (D <= 10) KERNEL<MK, 10><<<grid, block, 0, stream>>>(__VA_ARGS__);                          \
+    else if (D <= 12) KERNEL<MK, 12><<<grid, block, 0, stream>>>(__VA_ARGS__);                          \
+    else KERNEL<MK, 16><<<grid, block, 0, stream>>>(__VA_ARGS__);
 
 #define DISPATCH_METRIC(metric, D, KERNEL, grid, block, stream, ...)                                      \
     do {                                                                                                \
         switch (metric) {                                                                               \
         case MPTG_METRIC_L2:                                                                            \
-            if (D <= 2) KERNEL<MPTG_METRIC_L2, 2><<<grid, block, 0, stream>>>(__VA_ARGS__);             \
-            else if (D <= 4) KERNEL<MPTG_METRIC_L2, 4><<<grid, block, 0, stream>>>(__VA_ARGS__);        \
-            else if (D <= 8) KERNEL<MPTG_METRIC_L2, 8><<<grid, block, 0, stream>>>(__VA_ARGS__);        \
-            else KERNEL<MPTG_METRIC_L2, 16><<<grid, block, 0, stream>>>(__VA_ARGS__);                   \
+            DISPATCH_DIMS(MPTG_METRIC_L2, D, KERNEL, grid, block, stream, __VA_ARGS__)                  \
             break;                                                                                      \
         case MPTG_METRIC_L1:                                                                            \
-            if (D <= 2) KERNEL<MPTG_METRIC_L1, 2><<<grid, block, 0, stream>>>(__VA_ARGS__);             \
-            else if (D <= 4) KERNEL<MPTG_METRIC_L1, 4><<<grid, block, 0, stream>>>(__VA_ARGS__);        \
-            else if (D <= 8) KERNEL<MPTG_METRIC_L1, 8><<<grid, block, 0, stream>>>(__VA_ARGS__);        \
-            else KERNEL<MPTG_METRIC_L1, 16><<<grid, block, 0, stream>>>(__VA_ARGS__);                   \
+            DISPATCH_DIMS(MPTG_METRIC_L1, D, KERNEL, grid, block, stream, __VA_ARGS__)                  \
             break;                                                                                      \
         case MPTG_METRIC_SO2:                                                                           \
-            if (D <= 2) KERNEL<MPTG_METRIC_SO2, 2><<<grid, block, 0, stream>>>(__VA_ARGS__);            \
-            else if (D <= 4) KERNEL<MPTG_METRIC_SO2, 4><<<grid, block, 0, stream>>>(__VA_ARGS__);       \
-            else if (D <= 8) KERNEL<MPTG_METRIC_SO2, 8><<<grid, block, 0, stream>>>(__VA_ARGS__);       \
-            else KERNEL<MPTG_METRIC_SO2, 16><<<grid, block, 0, stream>>>(__VA_ARGS__);                  \
+            DISPATCH_DIMS(MPTG_METRIC_SO2, D, KERNEL, grid, block, stream, __VA_ARGS__)                 \
             break;                                                                                      \
         case MPTG_METRIC_SO3: KERNEL<MPTG_METRIC_SO3, 4><<<grid, block, 0, stream>>>(__VA_ARGS__); break; \
         case MPTG_METRIC_SE3: KERNEL<MPTG_METRIC_SE3, 8><<<grid, block, 0, stream>>>(__VA_ARGS__); break; \
@@ -761,7 +831,8 @@ __global__ void __launch_bounds__(256) k_nearest_k(TreeView t, const double* __r
 static void tree_free(mptg_tree* t) {
     void* ptrs[] = {t->states64, t->pts32, t->nodes, t->cell_lo, t->cell_hi, t->node_depth, t->bpts, t->bids,
                     t->dcnt, t->dstats, t->perm, t->perm2, t->pseg, t->pseg2, t->segA, t->segB, t->seg_box,
-                    t->leaf_of, t->ovf_pts, t->ovf_leaf, t->leaf_reg, t->seg_cursor};
+                    t->leaf_of, t->ovf_pts, t->ovf_leaf, t->leaf_reg, t->seg_cursor, t->qkey, t->qorder,
+                    t->qhist};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (t->hcnt) cudaFreeHost(t->hcnt);
@@ -1023,11 +1094,32 @@ const double* mptg_tree_states_dev(const mptg_tree* t) { return t->states64; }
 mptg_status mptg_tree_nearest_dev(mptg_tree* t, const double* dq, int nq, int* didx, double* dd, cudaStream_t s,
                                   bool count) {
     if (nq <= 0) return MPTG_OK;
+    mptg_ctx* ctx = t->ctx;
     TreeView v = view_of(t);
     if (!count) v.stats = nullptr;
+    const int* order = nullptr;
+    if (nq >= MPTG_QSORT_MIN && t->n > 4 * MPTG_BUCKET) {
+        if ((size_t)nq > t->qcap) {
+            cudaStreamSynchronize(s);
+            cudaFree(t->qkey);
+            cudaFree(t->qorder);
+            t->qkey = t->qorder = nullptr;
+            t->qcap = 0;
+            if (!t->qhist) MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&t->qhist, MPTG_QSORT_BINS * sizeof(int)));
+            MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&t->qkey, (size_t)nq * sizeof(int)));
+            MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&t->qorder, (size_t)nq * sizeof(int)));
+            t->qcap = (size_t)nq;
+        }
+        MPTG_CUDA_TRY(ctx, cudaMemsetAsync(t->qhist, 0, MPTG_QSORT_BINS * sizeof(int), s));
+        k_qkey<<<mptg_blocks(nq, 256), 256, 0, s>>>(v, dq, nq, t->qkey, t->qhist);
+        k_qscan<<<1, 1024, 0, s>>>(t->qhist);
+        k_qscatter<<<mptg_blocks(nq, 256), 256, 0, s>>>(nq, t->qkey, t->qhist, t->qorder);
+        ctx->launches += 3;
+        order = t->qorder;
+    }
     unsigned grid = mptg_blocks((size_t)nq * 32, 256);
-    DISPATCH_METRIC(t->metric, t->D, k_nearest, grid, 256, s, v, dq, nq, didx, dd);
-    MPTG_LAUNCHED(t->ctx);
+    DISPATCH_METRIC(t->metric, t->D, k_nearest, grid, 256, s, v, dq, nq, order, didx, dd);
+    MPTG_LAUNCHED(ctx);
     return MPTG_OK;
 }
 
