@@ -584,6 +584,183 @@ __global__ void __launch_bounds__(256, 5) k_nearest(TreeView t, const double* __
     }
 }
 
+// ------------------------------------------------------------------ packets
+// Packet traversal for large, spatially ordered batches: one warp answers 32
+// neighbouring queries (one per lane) and walks the union of their search
+// trees once.  Every node and bucket it touches is loaded by all lanes from
+// the same address (one L1 transaction, shared by 32 queries), instead of
+// each query following its own dependent chain through L2.  Pruning is per
+// lane; a node is entered when any lane's bound admits it (ballot).
+
+// lower bound of the distance from this lane's query to node c's cell
+template <int MK, int DMAX>
+__device__ __forceinline__ float lane_cell_lb(const TreeView& t, int c, const float (&q)[DMAX], float w0,
+                                              float w1) {
+    const float* lo = t.cell_lo + (size_t)c * t.D;
+    const float* hi = t.cell_hi + (size_t)c * t.D;
+    if constexpr (MK == MPTG_METRIC_L2 || MK == MPTG_METRIC_L1) {
+        float s = 0.f;
+#pragma unroll
+        for (int d = 0; d < DMAX; ++d) {
+            if (d < t.D) {
+                float o = fmaxf(fmaxf(__ldg(&lo[d]) - q[d], q[d] - __ldg(&hi[d])), 0.f);
+                if constexpr (MK == MPTG_METRIC_L2) s = fmaf(o, o, s);
+                else s += o;
+            }
+        }
+        if constexpr (MK == MPTG_METRIC_L2) return sqrtf(s);
+        else return s;
+    } else if constexpr (MK == MPTG_METRIC_SO2) {
+        float s = 0.f;
+#pragma unroll
+        for (int d = 0; d < DMAX; ++d) {
+            if (d < t.D) {
+                float l = __ldg(&lo[d]), h = __ldg(&hi[d]);
+                if (q[d] < l || q[d] > h) s += fminf(so2_w32(q[d] - l), so2_w32(q[d] - h));
+            }
+        }
+        return s;
+    } else {
+        float cp = 0.f, cm = 0.f;
+#pragma unroll
+        for (int d = 0; d < 4; ++d) {
+            float l = __ldg(&lo[d]), h = __ldg(&hi[d]);
+            float o = fmaxf(fmaxf(l - q[d], q[d] - h), 0.f);
+            float om = fmaxf(fmaxf(l + q[d], -q[d] - h), 0.f);
+            cp = fmaf(o, o, cp);
+            cm = fmaf(om, om, cm);
+        }
+        float rot = 2.f * asinf(fminf(1.f, 0.5f * sqrtf(fminf(cp, cm))));
+        if constexpr (MK == MPTG_METRIC_SO3) {
+            return rot;
+        } else {
+            float s = 0.f;
+#pragma unroll
+            for (int d = 4; d < 7; ++d) {
+                float o = fmaxf(fmaxf(__ldg(&lo[d]) - q[d], q[d] - __ldg(&hi[d])), 0.f);
+                s = fmaf(o, o, s);
+            }
+            return w0 * rot + w1 * sqrtf(s);
+        }
+    }
+}
+
+template <int MK, int DMAX>
+__global__ void __launch_bounds__(256, 4) k_nearest_packet(TreeView t, const double* __restrict__ q64, int nq,
+                                                           const int* __restrict__ order, int* __restrict__ out_idx,
+                                                           double* __restrict__ out_d) {
+    const int lane = threadIdx.x & 31;
+    const int base = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5) * 32;
+    if (base >= nq) return;
+    const int D = t.D;
+    const int slot = base + lane;
+    const bool act = slot < nq;
+    const int qi = act ? __ldg(&order[slot]) : 0;
+    const double* qd = q64 + (size_t)qi * D;
+    float q[DMAX];
+    float M = __int_as_float(t.dcnt[CNT_MAXABS]);
+#pragma unroll
+    for (int d = 0; d < DMAX; ++d) {
+        float v = 0.f;
+        if (act && d < D) v = __double2float_rn(qd[d]);
+        q[d] = v;
+        bool lp = MK == MPTG_METRIC_L2 || MK == MPTG_METRIC_L1 || (MK == MPTG_METRIC_SE3 && d >= 4 && d < 7);
+        if (lp && act && d < D) M = fmaxf(M, __double2float_ru(fabs(qd[d])));
+    }
+    const float E = err32<MK>(D, M, t.w0f, t.w1f);
+    const float E2 = __fmul_ru(2.f, E);
+    double best = INFINITY;
+    int bidx = INT_MAX;
+    float bestf_up = act ? INFINITY : -INFINITY;  // inactive lanes never admit a node
+    float run32 = INFINITY;
+    unsigned long long n_int = 0, n_leaf = 0, n_pts = 0, n_rr = 0;
+
+    int sp = 0;
+    int s0n = 0, s1n = 0;
+    int node = 0;
+    while (true) {
+        int4 nd = __ldg(&t.nodes[node]);
+        if (nd.x >= 0) {
+            ++n_int;
+            int c = nd.y;
+            float lbL = lane_cell_lb<MK, DMAX>(t, c, q, t.w0f, t.w1f);
+            float lbR = lane_cell_lb<MK, DMAX>(t, c + 1, q, t.w0f, t.w1f);
+            bool nL = __fsub_rd(lbL, E) <= bestf_up;
+            bool nR = __fsub_rd(lbR, E) <= bestf_up;
+            unsigned bL = __ballot_sync(0xffffffffu, nL), bR = __ballot_sync(0xffffffffu, nR);
+            if (bL && bR) {
+                // enter the child most lanes are closer to; keep the other
+                unsigned pl = __ballot_sync(0xffffffffu, nL && (!nR || lbL <= lbR));
+                unsigned pr = __ballot_sync(0xffffffffu, nR && (!nL || lbR < lbL));
+                int first = __popc(pl) >= __popc(pr) ? c : c + 1;
+                int second = 2 * c + 1 - first;
+                if (sp < 64) {
+                    if (sp < 32) { if (lane == sp) s0n = second; }
+                    else if (lane == sp - 32) s1n = second;
+                    ++sp;
+                }
+                node = first;
+                continue;
+            } else if (bL || bR) {
+                node = bL ? c : c + 1;
+                continue;
+            }
+        } else {
+            ++n_leaf;
+            int cnt = nd.w < MPTG_BUCKET ? nd.w : MPTG_BUCKET;
+            n_pts += cnt;
+            const size_t b = (size_t)nd.y;
+            const float* bp = t.bpts + b * D * MPTG_BUCKET;
+            for (int j = 0; j < cnt; ++j) {
+                float p[DMAX];
+#pragma unroll
+                for (int d = 0; d < DMAX; ++d) p[d] = d < D ? __ldg(&bp[d * MPTG_BUCKET + j]) : 0.f;
+                float d32 = dist32<MK, DMAX>(q, p, t.w0f, t.w1f);
+                if (!(d32 == d32)) continue;
+                run32 = fminf(run32, d32);
+                // a point that could beat or tie this lane's best in exact arithmetic
+                if (act && __fsub_rd(d32, E) <= bestf_up && d32 <= __fadd_ru(run32, E2)) {
+                    int pid = __ldg(&t.bids[b * MPTG_BUCKET + j]);
+                    double dd = dist64(t.metric, D, t.w0, t.w1, qd, t.states64 + (size_t)pid * D);
+                    ++n_rr;
+                    if (dd < best || (dd == best && pid < bidx)) {
+                        best = dd;
+                        bidx = pid;
+                        bestf_up = __double2float_ru(best);
+                    }
+                }
+            }
+        }
+        // pop until a node some lane still needs
+        bool found = false;
+        while (sp > 0) {
+            --sp;
+            int src = sp & 31;
+            int nn = sp < 32 ? __shfl_sync(0xffffffffu, s0n, src) : __shfl_sync(0xffffffffu, s1n, src);
+            float lb = lane_cell_lb<MK, DMAX>(t, nn, q, t.w0f, t.w1f);
+            if (__any_sync(0xffffffffu, __fsub_rd(lb, E) <= bestf_up)) { node = nn; found = true; break; }
+        }
+        if (!found) break;
+    }
+    if (act) {
+        out_idx[qi] = bidx == INT_MAX ? -1 : bidx;
+        out_d[qi] = best;
+    }
+    if (t.stats) {
+        // per-query accounting: every lane paid for the whole packet walk
+        unsigned na = __popc(__ballot_sync(0xffffffffu, act));
+        unsigned long long rr = n_rr;
+        for (int o = 16; o > 0; o >>= 1) rr += __shfl_xor_sync(0xffffffffu, rr, o);
+        if (lane == 0) {
+            atomicAdd(&t.stats[0], (unsigned long long)na);
+            atomicAdd(&t.stats[1], n_int * na);
+            atomicAdd(&t.stats[2], n_leaf * na);
+            atomicAdd(&t.stats[3], n_pts * na);
+            atomicAdd(&t.stats[4], rr);
+        }
+    }
+}
+
 // exhaustive scan (nigh::Linear): warp per query, 32 points per step
 template <int MK, int DMAX>
 __global__ void __launch_bounds__(256) k_nearest_linear(TreeView t, const double* __restrict__ q64, int nq,
@@ -1117,8 +1294,14 @@ mptg_status mptg_tree_nearest_dev(mptg_tree* t, const double* dq, int nq, int* d
         ctx->launches += 3;
         order = t->qorder;
     }
-    unsigned grid = mptg_blocks((size_t)nq * 32, 256);
-    DISPATCH_METRIC(t->metric, t->D, k_nearest, grid, 256, s, v, dq, nq, order, didx, dd);
+    if (order) {
+        // 32 sorted queries per warp
+        unsigned grid = mptg_blocks((size_t)nq, 256);
+        DISPATCH_METRIC(t->metric, t->D, k_nearest_packet, grid, 256, s, v, dq, nq, order, didx, dd);
+    } else {
+        unsigned grid = mptg_blocks((size_t)nq * 32, 256);
+        DISPATCH_METRIC(t->metric, t->D, k_nearest, grid, 256, s, v, dq, nq, order, didx, dd);
+    }
     MPTG_LAUNCHED(ctx);
     return MPTG_OK;
 }

@@ -43,11 +43,17 @@ def test_nearest_matches_oracle(ctx, orc, name):
     assert len(tree) == n
     sp = orc.make_space(sc["metric"], sc["dim"], sc["weights"])
     oi, od = orc.nn_brute(sp, pts, q)
-    gi, gd = tree.nearest(q)
+    gi, gd = tree.nearest(q)  # < 2048 queries: warp-per-query search
     assert np.array_equal(gi, oi), np.nonzero(gi != oi)[0][:10]
     assert np.array_equal(gd.view(np.int64), od.view(np.int64))
     li, ld = tree.nearest(q, linear=True)
     assert np.array_equal(li, oi) and np.array_equal(ld.view(np.int64), od.view(np.int64))
+    # >= 2048 queries: spatially ordered packet search (32 queries per warp)
+    q2 = np.concatenate([q, scenes.uniform_states(sc, 3001, 103)])
+    oi2, od2 = orc.nn_brute(sp, pts, q2)
+    gi2, gd2 = tree.nearest(q2)
+    assert np.array_equal(gi2, oi2), np.nonzero(gi2 != oi2)[0][:10]
+    assert np.array_equal(gd2.view(np.int64), od2.view(np.int64))
     # stored states come back unchanged
     assert np.array_equal(tree.states(), pts)
 
