@@ -403,15 +403,11 @@ __device__ __forceinline__ float so2_w32(float x) {
     return fminf(x, TWO_PI_F - x);
 }
 
-// lower bound of the distance from the query to node `c`'s cell
+// lower bound of the distance from the query to a cell whose interval on
+// dimension d is [lo, hi] in lane d (lanes >= D ignored)
 template <int MK>
-__device__ __forceinline__ float cell_lb(const TreeView& t, int c, float myq, int lane) {
+__device__ __forceinline__ float cell_lb_vals(const TreeView& t, float myq, float lo, float hi, int lane) {
     const int D = t.D;
-    float lo = 0.f, hi = 0.f;
-    if (lane < D) {
-        lo = __ldg(&t.cell_lo[(size_t)c * D + lane]);
-        hi = __ldg(&t.cell_hi[(size_t)c * D + lane]);
-    }
     if constexpr (MK == MPTG_METRIC_L2 || MK == MPTG_METRIC_L1) {
         float o = lane < D ? fmaxf(fmaxf(lo - myq, myq - hi), 0.f) : 0.f;
         if constexpr (MK == MPTG_METRIC_L2) return sqrtf(warp_sum16(o * o));
@@ -440,6 +436,18 @@ __device__ __forceinline__ float cell_lb(const TreeView& t, int c, float myq, in
             return t.w0f * rot + t.w1f * sqrtf(tt);
         }
     }
+}
+
+// lower bound of the distance from the query to node `c`'s stored cell
+template <int MK>
+__device__ __forceinline__ float cell_lb(const TreeView& t, int c, float myq, int lane) {
+    const int D = t.D;
+    float lo = 0.f, hi = 0.f;
+    if (lane < D) {
+        lo = __ldg(&t.cell_lo[(size_t)c * D + lane]);
+        hi = __ldg(&t.cell_hi[(size_t)c * D + lane]);
+    }
+    return cell_lb_vals<MK>(t, myq, lo, hi, lane);
 }
 
 // Candidate step shared by the tree and the linear scan: each lane holds one
@@ -520,15 +528,29 @@ __global__ void __launch_bounds__(256, 5) k_nearest(TreeView t, const double* __
     int s0n = 0, s1n = 0;
     float s0l = 0.f, s1l = 0.f;
     int node = 0;
+    // The current node's record and cell live in registers: lane d < D holds
+    // the cell's interval on dimension d.  A child's cell is its parent's with
+    // one bound replaced by the split (as k_seg_c builds them), so descending
+    // needs no cell load; only a pop reloads a cell.  Both children's records
+    // arrive with one load (lanes 0/1), so each level costs one round trip.
+    int4 nd = __ldg(&t.nodes[0]);
+    float clo = 0.f, chi = 0.f;
+    if (lane < D) { clo = __ldg(&t.cell_lo[lane]); chi = __ldg(&t.cell_hi[lane]); }
     while (true) {
-        int4 nd = __ldg(&t.nodes[node]);
         if (nd.x >= 0) {
             ++n_int;
-            float qv = __shfl_sync(0xffffffffu, myq, nd.x);
-            float split = __int_as_float(nd.z);
-            int nearc = qv < split ? nd.y : nd.y + 1;
-            int farc = 2 * nd.y + 1 - nearc;
-            float lb = cell_lb<MK>(t, farc, myq, lane);
+            const int c = nd.y, s = nd.x;
+            const int4 ch = __ldg(&t.nodes[c + (lane & 1)]);
+            const float split = __int_as_float(nd.z);
+            const float qv = __shfl_sync(0xffffffffu, myq, s);
+            const bool goLeft = qv < split;
+            float flo = clo, fhi = chi;
+            if (lane == s) {
+                if (goLeft) flo = split;
+                else fhi = split;
+            }
+            float lb = cell_lb_vals<MK>(t, myq, flo, fhi, lane);
+            const int farc = goLeft ? c + 1 : c;
             // the builder keeps depth <= MPTG_MAX_DEPTH < 64, so the stack never fills
             if (__fsub_rd(lb, E) <= bestf_up && sp < 64) {
                 if (sp < 32) {
@@ -538,7 +560,16 @@ __global__ void __launch_bounds__(256, 5) k_nearest(TreeView t, const double* __
                 }
                 ++sp;
             }
-            node = nearc;
+            if (lane == s) {
+                if (goLeft) chi = split;
+                else clo = split;
+            }
+            const int src = goLeft ? 0 : 1;
+            nd.x = __shfl_sync(0xffffffffu, ch.x, src);
+            nd.y = __shfl_sync(0xffffffffu, ch.y, src);
+            nd.z = __shfl_sync(0xffffffffu, ch.z, src);
+            nd.w = __shfl_sync(0xffffffffu, ch.w, src);
+            node = goLeft ? c : c + 1;
             continue;
         }
         // leaf
@@ -570,6 +601,11 @@ __global__ void __launch_bounds__(256, 5) k_nearest(TreeView t, const double* __
             if (__fsub_rd(lb, E) <= bestf_up) { node = nn; found = true; break; }
         }
         if (!found) break;
+        nd = __ldg(&t.nodes[node]);
+        if (lane < D) {
+            clo = __ldg(&t.cell_lo[(size_t)node * D + lane]);
+            chi = __ldg(&t.cell_hi[(size_t)node * D + lane]);
+        }
     }
     if (lane == 0) {
         out_idx[qi] = bidx == INT_MAX ? -1 : bidx;
@@ -1294,7 +1330,10 @@ mptg_status mptg_tree_nearest_dev(mptg_tree* t, const double* dq, int nq, int* d
         ctx->launches += 3;
         order = t->qorder;
     }
-    if (order) {
+    // Packets pay off where neighbouring queries' search balls overlap (low
+    // dimension); in SO(2)^10 the union of 32 balls is ~6x one ball, so
+    // higher dimensions keep one query per warp (still in sorted order).
+    if (order && t->D <= 3) {
         // 32 sorted queries per warp
         unsigned grid = mptg_blocks((size_t)nq, 256);
         DISPATCH_METRIC(t->metric, t->D, k_nearest_packet, grid, 256, s, v, dq, nq, order, didx, dd);
