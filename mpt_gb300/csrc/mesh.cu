@@ -1,27 +1,597 @@
 // mesh.cu - rigid-body (SE(3)) mesh-vs-mesh validity.
+//
+// Replaces fcl::collide(robot BVHModel<OBBRSS>, T(q), environment, I) in
+// demo/se3_rigid_body_scenario.hpp:282-312: a state is valid iff no triangle
+// of the robot placed at T(q) = Translation(p) * Rotation(quaternion)
+// intersects an environment triangle.
+//
+// Exactness: the result is the OR, over all (robot, environment) triangle
+// pairs, of an FP64 triangle-triangle test (T. Moller, "A Fast
+// Triangle-Triangle Intersection Test", JGT 1997, no epsilon snapping) on
+// robot vertices transformed in FP64 in a fixed operation order.  Every cull
+// in front of it is conservative (FP32 boxes rounded outward and grown by a
+// margin far above FP32 rounding), so it can only skip pairs that cannot
+// intersect, and the boolean equals the CPU checker's.
+//
+// Per batch of states:
+//  k_mesh_sphere  (thread per state) robot bounding sphere at p vs the
+//                 environment AABB tree: no box within reach -> valid
+//  k_mesh_detail  (block per remaining state, thread per robot leaf) the
+//                 robot leaf's world AABB (its robot-frame box rotated by
+//                 |R|) against the environment tree; triangle pairs of
+//                 overlapping leaves go to the FP64 test; the block stops
+//                 at the first intersection
+// Both trees are built once per scene on the host (top-down median split on
+// the longest axis, leaves of <= 8 triangles).
+#include <algorithm>
+#include <numeric>
+
 #include "metrics.cuh"
 #include "scene.cuh"
 
-struct MeshData {
-    int placeholder;
+#define MESH_LEAF 8
+#define MESH_MARGIN 1e-3f  // box growth, >> FP32 rounding of scene coordinates (|x| <= 1e3)
+#define MESH_STACK 64
+
+struct BvhNode {  // 32 bytes
+    float lo[3];
+    int a;        // internal: left child; leaf: first triangle
+    float hi[3];
+    int b;        // internal: right child; leaf: -(count)
 };
 
-mptg_status mesh_scene_create(mptg_ctx* ctx, const mptg_scene_desc*, mptg_scene*) {
-    return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "rigid mesh scenes are not available in this build");
+struct MeshData {
+    // environment (world frame), triangles in leaf order
+    double* env_tris = nullptr;   // [nenv][9]
+    BvhNode* env_nodes = nullptr;
+    int nenv = 0, nenv_nodes = 0;
+    // robot (robot frame), triangles in leaf order
+    double* robot_tris = nullptr;  // [nrobot][9]
+    BvhNode* robot_leaves = nullptr;  // robot leaves only (AABBs in the robot frame)
+    int nrobot = 0, nrleaves = 0;
+    double robot_radius = 0.0;     // max |vertex| in the robot frame
+    // batch scratch (grown on demand)
+    int* work = nullptr;
+    int* nwork = nullptr;
+    size_t work_cap = 0;
+    double* samples = nullptr;
+    int* sample_edge = nullptr;
+    uint8_t* sample_ok = nullptr;
+    size_t sample_cap = 0;
+    int* counts = nullptr;
+    int* offs = nullptr;
+    size_t edge_cap = 0;
+    int* hbuf = nullptr;  // pinned
+};
+
+// ------------------------------------------------------------------ host BVH build
+
+namespace {
+
+struct Box { double lo[3], hi[3]; };
+
+Box tri_box(const double* t) {
+    Box b;
+    for (int d = 0; d < 3; ++d) {
+        b.lo[d] = std::min(std::min(t[d], t[3 + d]), t[6 + d]);
+        b.hi[d] = std::max(std::max(t[d], t[3 + d]), t[6 + d]);
+    }
+    return b;
+}
+
+// outward FP32 rounding plus a margin
+void store_box(BvhNode& n, const Box& b) {
+    for (int d = 0; d < 3; ++d) {
+        n.lo[d] = std::nextafter((float)b.lo[d], -INFINITY) - MESH_MARGIN;
+        n.hi[d] = std::nextafter((float)b.hi[d], INFINITY) + MESH_MARGIN;
+    }
+}
+
+int build_rec(const std::vector<double>& tris, std::vector<int>& idx, int start, int count,
+              std::vector<BvhNode>& nodes, std::vector<int>* leaves) {
+    int id = (int)nodes.size();
+    nodes.push_back(BvhNode());
+    Box b;
+    for (int d = 0; d < 3; ++d) { b.lo[d] = INFINITY; b.hi[d] = -INFINITY; }
+    for (int i = 0; i < count; ++i) {
+        Box t = tri_box(&tris[9 * (size_t)idx[start + i]]);
+        for (int d = 0; d < 3; ++d) { b.lo[d] = std::min(b.lo[d], t.lo[d]); b.hi[d] = std::max(b.hi[d], t.hi[d]); }
+    }
+    store_box(nodes[id], b);
+    if (count <= MESH_LEAF) {
+        nodes[id].a = start;
+        nodes[id].b = -count;
+        if (leaves) leaves->push_back(id);
+        return id;
+    }
+    int ax = 0;
+    for (int d = 1; d < 3; ++d)
+        if (b.hi[d] - b.lo[d] > b.hi[ax] - b.lo[ax]) ax = d;
+    auto cen = [&](int t) { const double* p = &tris[9 * (size_t)t]; return p[ax] + p[3 + ax] + p[6 + ax]; };
+    int mid = count / 2;
+    std::nth_element(idx.begin() + start, idx.begin() + start + mid, idx.begin() + start + count,
+                     [&](int x, int y) { double cx = cen(x), cy = cen(y); return cx < cy || (cx == cy && x < y); });
+    int l = build_rec(tris, idx, start, mid, nodes, leaves);
+    int r = build_rec(tris, idx, start + mid, count - mid, nodes, leaves);
+    nodes[id].a = l;
+    nodes[id].b = r;
+    return id;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ device helpers
+
+__device__ __forceinline__ void quat_mat64(const double* q, double* R) {
+    // same expression order as the CPU checker (oracle.c quat_to_mat)
+    double x = q[0], y = q[1], z = q[2], w = q[3];
+    double tx = __dmul_rn(2.0, x), ty = __dmul_rn(2.0, y), tz = __dmul_rn(2.0, z);
+    double twx = __dmul_rn(tx, w), twy = __dmul_rn(ty, w), twz = __dmul_rn(tz, w);
+    double txx = __dmul_rn(tx, x), txy = __dmul_rn(ty, x), txz = __dmul_rn(tz, x);
+    double tyy = __dmul_rn(ty, y), tyz = __dmul_rn(tz, y), tzz = __dmul_rn(tz, z);
+    R[0] = __dsub_rn(1.0, __dadd_rn(tyy, tzz)); R[1] = __dsub_rn(txy, twz); R[2] = __dadd_rn(txz, twy);
+    R[3] = __dadd_rn(txy, twz); R[4] = __dsub_rn(1.0, __dadd_rn(txx, tzz)); R[5] = __dsub_rn(tyz, twx);
+    R[6] = __dsub_rn(txz, twy); R[7] = __dadd_rn(tyz, twx); R[8] = __dsub_rn(1.0, __dadd_rn(txx, tyy));
+}
+
+__device__ __forceinline__ void xform64(const double* R, const double* p, const double* v, double* o) {
+    o[0] = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(R[0], v[0]), __dmul_rn(R[1], v[1])), __dmul_rn(R[2], v[2])), p[0]);
+    o[1] = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(R[3], v[0]), __dmul_rn(R[4], v[1])), __dmul_rn(R[5], v[2])), p[1]);
+    o[2] = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(R[6], v[0]), __dmul_rn(R[7], v[1])), __dmul_rn(R[8], v[2])), p[2]);
+}
+
+__device__ __forceinline__ void sub3d(const double* a, const double* b, double* c) {
+    c[0] = __dsub_rn(a[0], b[0]); c[1] = __dsub_rn(a[1], b[1]); c[2] = __dsub_rn(a[2], b[2]);
+}
+__device__ __forceinline__ void cross3d(const double* a, const double* b, double* c) {
+    c[0] = __dsub_rn(__dmul_rn(a[1], b[2]), __dmul_rn(a[2], b[1]));
+    c[1] = __dsub_rn(__dmul_rn(a[2], b[0]), __dmul_rn(a[0], b[2]));
+    c[2] = __dsub_rn(__dmul_rn(a[0], b[1]), __dmul_rn(a[1], b[0]));
+}
+__device__ __forceinline__ double dot3d(const double* a, const double* b) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(a[0], b[0]), __dmul_rn(a[1], b[1])), __dmul_rn(a[2], b[2]));
+}
+__device__ __forceinline__ double orient2d_m(double ax, double ay, double bx, double by, double cx, double cy) {
+    return __dsub_rn(__dmul_rn(__dsub_rn(bx, ax), __dsub_rn(cy, ay)), __dmul_rn(__dsub_rn(by, ay), __dsub_rn(cx, ax)));
+}
+__device__ __forceinline__ bool on_box2(double ax, double ay, double bx, double by, double px, double py) {
+    return fmin(ax, bx) <= px && px <= fmax(ax, bx) && fmin(ay, by) <= py && py <= fmax(ay, by);
+}
+__device__ bool seg2_intersect(double ax, double ay, double bx, double by, double cx, double cy, double dx, double dy) {
+    double o1 = orient2d_m(ax, ay, bx, by, cx, cy), o2 = orient2d_m(ax, ay, bx, by, dx, dy);
+    double o3 = orient2d_m(cx, cy, dx, dy, ax, ay), o4 = orient2d_m(cx, cy, dx, dy, bx, by);
+    if (((o1 > 0 && o2 < 0) || (o1 < 0 && o2 > 0)) && ((o3 > 0 && o4 < 0) || (o3 < 0 && o4 > 0))) return true;
+    if (o1 == 0 && on_box2(ax, ay, bx, by, cx, cy)) return true;
+    if (o2 == 0 && on_box2(ax, ay, bx, by, dx, dy)) return true;
+    if (o3 == 0 && on_box2(cx, cy, dx, dy, ax, ay)) return true;
+    if (o4 == 0 && on_box2(cx, cy, dx, dy, bx, by)) return true;
+    return false;
+}
+__device__ bool point_in_tri2(double px, double py, const double* t) {
+    double d1 = orient2d_m(t[0], t[1], t[2], t[3], px, py);
+    double d2 = orient2d_m(t[2], t[3], t[4], t[5], px, py);
+    double d3 = orient2d_m(t[4], t[5], t[0], t[1], px, py);
+    bool neg = d1 < 0 || d2 < 0 || d3 < 0, pos = d1 > 0 || d2 > 0 || d3 > 0;
+    return !(neg && pos);
+}
+__device__ bool coplanar_tt(const double* n, const double* V0, const double* V1, const double* V2, const double* U0,
+                            const double* U1, const double* U2) {
+    double a0 = fabs(n[0]), a1 = fabs(n[1]), a2 = fabs(n[2]);
+    int i0, i1;
+    if (a0 > a1) { if (a0 > a2) { i0 = 1; i1 = 2; } else { i0 = 0; i1 = 1; } }
+    else { if (a2 > a1) { i0 = 0; i1 = 1; } else { i0 = 0; i1 = 2; } }
+    double v[6] = {V0[i0], V0[i1], V1[i0], V1[i1], V2[i0], V2[i1]};
+    double u[6] = {U0[i0], U0[i1], U1[i0], U1[i1], U2[i0], U2[i1]};
+    for (int e = 0; e < 3; ++e) {
+        int e1 = (e + 1) % 3;
+        for (int f = 0; f < 3; ++f) {
+            int f1 = (f + 1) % 3;
+            if (seg2_intersect(v[2 * e], v[2 * e + 1], v[2 * e1], v[2 * e1 + 1], u[2 * f], u[2 * f + 1], u[2 * f1],
+                               u[2 * f1 + 1]))
+                return true;
+        }
+    }
+    if (point_in_tri2(v[0], v[1], u)) return true;
+    if (point_in_tri2(u[0], u[1], v)) return true;
+    return false;
+}
+__device__ __forceinline__ double lerp_isect(double VVa, double VVb, double Da, double Db) {
+    // VVa + (VVb - VVa) * Da / (Da - Db), evaluated left to right as the checker does
+    return __dadd_rn(VVa, __ddiv_rn(__dmul_rn(__dsub_rn(VVb, VVa), Da), __dsub_rn(Da, Db)));
+}
+__device__ bool tri_interval(double VV0, double VV1, double VV2, double D0, double D1, double D2, double D0D1,
+                             double D0D2, double* i0, double* i1) {
+    if (D0D1 > 0) { *i0 = lerp_isect(VV2, VV0, D2, D0); *i1 = lerp_isect(VV2, VV1, D2, D1); }
+    else if (D0D2 > 0) { *i0 = lerp_isect(VV1, VV0, D1, D0); *i1 = lerp_isect(VV1, VV2, D1, D2); }
+    else if (__dmul_rn(D1, D2) > 0 || D0 != 0) { *i0 = lerp_isect(VV0, VV1, D0, D1); *i1 = lerp_isect(VV0, VV2, D0, D2); }
+    else if (D1 != 0) { *i0 = lerp_isect(VV1, VV0, D1, D0); *i1 = lerp_isect(VV1, VV2, D1, D2); }
+    else if (D2 != 0) { *i0 = lerp_isect(VV2, VV0, D2, D0); *i1 = lerp_isect(VV2, VV1, D2, D1); }
+    else return true;
+    return false;
+}
+
+// Moller's test in FP64 (same expressions as the CPU checker)
+__device__ bool tri_tri64(const double* t1, const double* t2) {
+    const double *V0 = t1, *V1 = t1 + 3, *V2 = t1 + 6;
+    const double *U0 = t2, *U1 = t2 + 3, *U2 = t2 + 6;
+    double E1[3], E2[3], N1[3], N2[3], Dv[3];
+    sub3d(V1, V0, E1); sub3d(V2, V0, E2); cross3d(E1, E2, N1);
+    double d1 = -dot3d(N1, V0);
+    double du0 = __dadd_rn(dot3d(N1, U0), d1), du1 = __dadd_rn(dot3d(N1, U1), d1), du2 = __dadd_rn(dot3d(N1, U2), d1);
+    double du0du1 = __dmul_rn(du0, du1), du0du2 = __dmul_rn(du0, du2);
+    if (du0du1 > 0 && du0du2 > 0) return false;
+    sub3d(U1, U0, E1); sub3d(U2, U0, E2); cross3d(E1, E2, N2);
+    double d2 = -dot3d(N2, U0);
+    double dv0 = __dadd_rn(dot3d(N2, V0), d2), dv1 = __dadd_rn(dot3d(N2, V1), d2), dv2 = __dadd_rn(dot3d(N2, V2), d2);
+    double dv0dv1 = __dmul_rn(dv0, dv1), dv0dv2 = __dmul_rn(dv0, dv2);
+    if (dv0dv1 > 0 && dv0dv2 > 0) return false;
+    cross3d(N1, N2, Dv);
+    double mx = fabs(Dv[0]);
+    int index = 0;
+    double bb = fabs(Dv[1]), cc = fabs(Dv[2]);
+    if (bb > mx) { mx = bb; index = 1; }
+    if (cc > mx) index = 2;
+    double a0, a1, b0, b1;
+    if (tri_interval(V0[index], V1[index], V2[index], dv0, dv1, dv2, dv0dv1, dv0dv2, &a0, &a1))
+        return coplanar_tt(N1, V0, V1, V2, U0, U1, U2);
+    if (tri_interval(U0[index], U1[index], U2[index], du0, du1, du2, du0du1, du0du2, &b0, &b1))
+        return coplanar_tt(N1, V0, V1, V2, U0, U1, U2);
+    if (a0 > a1) { double t = a0; a0 = a1; a1 = t; }
+    if (b0 > b1) { double t = b0; b0 = b1; b1 = t; }
+    return !(a1 < b0 || b1 < a0);
+}
+
+__device__ __forceinline__ bool box_overlap(const float* lo, const float* hi, const BvhNode& n) {
+    return !(n.lo[0] > hi[0] || n.hi[0] < lo[0] || n.lo[1] > hi[1] || n.hi[1] < lo[1] || n.lo[2] > hi[2] ||
+             n.hi[2] < lo[2]);
+}
+
+struct MeshView {
+    const double* env_tris;
+    const BvhNode* env_nodes;
+    const double* robot_tris;
+    const BvhNode* robot_leaves;
+    int nenv, nrleaves;
+    float reach;  // robot bounding radius + margin
+};
+
+// robot bounding sphere (center p, radius reach) against the environment tree
+__global__ void k_mesh_sphere(MeshView m, const double* __restrict__ q, int n, int D, uint8_t* __restrict__ out,
+                              int* __restrict__ work, int* __restrict__ nwork) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* s = q + (size_t)i * D;
+    float p[3] = {(float)s[4], (float)s[5], (float)s[6]};
+    bool bad = !(s[4] == s[4] && s[5] == s[5] && s[6] == s[6] && s[0] == s[0] && s[1] == s[1] && s[2] == s[2] &&
+                 s[3] == s[3]);
+    float r = m.reach + 1e-3f * (1.f + fabsf(p[0]) + fabsf(p[1]) + fabsf(p[2]));
+    float lo[3] = {p[0] - r, p[1] - r, p[2] - r}, hi[3] = {p[0] + r, p[1] + r, p[2] + r};
+    bool near = false;
+    if (!bad && m.nenv > 0) {
+        int stack[MESH_STACK];
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp && !near) {
+            BvhNode nd = m.env_nodes[stack[--sp]];
+            if (!box_overlap(lo, hi, nd)) continue;
+            // sphere-box distance (the box test above is the sphere's bounding cube)
+            float d2 = 0.f;
+            for (int d = 0; d < 3; ++d) {
+                float o = fmaxf(fmaxf(nd.lo[d] - p[d], p[d] - nd.hi[d]), 0.f);
+                d2 = fmaf(o, o, d2);
+            }
+            if (d2 > r * r) continue;
+            if (nd.b < 0) { near = true; break; }
+            if (sp + 2 <= MESH_STACK) { stack[sp++] = nd.a; stack[sp++] = nd.b; }
+            else near = true;  // cannot happen for trees of depth < 62; stay conservative
+        }
+    }
+    if (bad) {
+        out[i] = 0;
+    } else if (!near) {
+        out[i] = 1;
+    } else {
+        out[i] = 0;  // decided by k_mesh_detail
+        work[atomicAdd(nwork, 1)] = i;
+    }
+}
+
+// block per state, thread per robot leaf
+__global__ void __launch_bounds__(256) k_mesh_detail(MeshView m, const double* __restrict__ q, int D,
+                                                     const int* __restrict__ work, const int* __restrict__ nwork,
+                                                     uint8_t* __restrict__ out) {
+    __shared__ double R[9];
+    __shared__ double P[3];
+    __shared__ volatile int hit;
+    const int w = blockIdx.x;
+    if (w >= *nwork) return;
+    const int i = work[w];
+    const double* s = q + (size_t)i * D;
+    if (threadIdx.x == 0) {
+        quat_mat64(s, R);
+        P[0] = s[4]; P[1] = s[5]; P[2] = s[6];
+        hit = 0;
+    }
+    __syncthreads();
+    for (int leaf = threadIdx.x; leaf < m.nrleaves && !hit; leaf += blockDim.x) {
+        const BvhNode rl = m.robot_leaves[leaf];
+        // world AABB of the rotated robot-frame box: center R c + p, half |R| h
+        float c[3], h[3], lo[3], hi[3];
+        for (int d = 0; d < 3; ++d) { c[d] = 0.5f * (rl.lo[d] + rl.hi[d]); h[d] = 0.5f * (rl.hi[d] - rl.lo[d]); }
+        for (int r = 0; r < 3; ++r) {
+            float cw = (float)P[r], hw = 0.f;
+            for (int k = 0; k < 3; ++k) {
+                float rv = (float)R[3 * r + k];
+                cw = fmaf(rv, c[k], cw);
+                hw = fmaf(fabsf(rv), h[k], hw);
+            }
+            float mg = MESH_MARGIN * (1.f + fabsf(cw) + hw);
+            lo[r] = cw - hw - mg;
+            hi[r] = cw + hw + mg;
+        }
+        int stack[MESH_STACK];
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp) {
+            if (hit) break;
+            BvhNode nd = m.env_nodes[stack[--sp]];
+            if (!box_overlap(lo, hi, nd)) continue;
+            if (nd.b >= 0) {
+                if (sp + 2 <= MESH_STACK) { stack[sp++] = nd.a; stack[sp++] = nd.b; }
+                continue;
+            }
+            // environment leaf: exact tests of its triangles against this robot leaf's
+            int rcount = -rl.b;
+            for (int e = nd.a; e < nd.a - nd.b && !hit; ++e) {
+                const double* et = m.env_tris + 9 * (size_t)e;
+                for (int rt = 0; rt < rcount; ++rt) {
+                    const double* lt = m.robot_tris + 9 * (size_t)(rl.a + rt);
+                    double wt[9];
+                    xform64(R, P, lt, wt);
+                    xform64(R, P, lt + 3, wt + 3);
+                    xform64(R, P, lt + 6, wt + 6);
+                    if (tri_tri64(wt, et)) { hit = 1; break; }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) out[i] = hit ? 0 : 1;
+}
+
+// ------------------------------------------------------------------ edges
+__global__ void k_mesh_edge_counts(int metric, int D, double w0, double w1, const double* __restrict__ a,
+                                   const double* __restrict__ b, int n, double inv, int* __restrict__ counts) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    double m = dist64(metric, D, w0, w1, a + (size_t)e * D, b + (size_t)e * D);
+    double sd = ceil(__dmul_rn(m, inv));
+    int c;
+    if (!(sd >= 0.0) || sd > (double)MPTG_MAX_EDGE_SAMPLES) c = -1;  // invalid edge, no samples
+    else c = sd < 2.0 ? 1 : (int)sd;
+    counts[e] = c;
+}
+
+// exclusive scan of counts (negative = 0) over n <= 2^20 edges: 1024 threads,
+// each scans a contiguous chunk
+__global__ void __launch_bounds__(1024) k_mesh_scan(const int* __restrict__ counts, int n, int* __restrict__ offs,
+                                                    int* __restrict__ total) {
+    __shared__ long long s[1024];
+    int t = threadIdx.x;
+    int chunk = (n + 1023) / 1024;
+    int lo = t * chunk, hi = min(n, lo + chunk);
+    long long sum = 0;
+    for (int e = lo; e < hi; ++e) sum += counts[e] > 0 ? counts[e] : 0;
+    s[t] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        long long v = t >= o ? s[t - o] : 0;
+        __syncthreads();
+        s[t] += v;
+        __syncthreads();
+    }
+    long long run = t ? s[t - 1] : 0;
+    for (int e = lo; e < hi; ++e) {
+        offs[e] = (int)run;
+        run += counts[e] > 0 ? counts[e] : 0;
+    }
+    if (t == 1023) *total = (int)s[1023];
+}
+
+__global__ void k_mesh_edge_samples(int metric, int D, const double* __restrict__ a, const double* __restrict__ b,
+                                    int n, const int* __restrict__ counts, const int* __restrict__ offs,
+                                    double* __restrict__ samples, int* __restrict__ sample_edge) {
+    int e = blockIdx.x;
+    if (e >= n) return;
+    int c = counts[e];
+    if (c <= 0) return;
+    const double* A = a + (size_t)e * D;
+    const double* B = b + (size_t)e * D;
+    double delta = c >= 2 ? __ddiv_rn(1.0, (double)c) : 0.0;
+    for (int k = threadIdx.x; k < c; k += blockDim.x) {
+        double* o = samples + (size_t)(offs[e] + k) * D;
+        if (k == 0) {
+            for (int d = 0; d < D; ++d) o[d] = B[d];
+        } else {
+            double A2[MPTG_MAX_DIM], B2[MPTG_MAX_DIM], qv[MPTG_MAX_DIM];
+            for (int d = 0; d < D; ++d) { A2[d] = A[d]; B2[d] = B[d]; }
+            interp64(metric, D, A2, B2, __dmul_rn((double)k, delta), qv);
+            for (int d = 0; d < D; ++d) o[d] = qv[d];
+        }
+        sample_edge[offs[e] + k] = e;
+    }
+}
+
+__global__ void k_mesh_edge_init(const int* __restrict__ counts, int n, uint8_t* __restrict__ out) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n) out[e] = counts[e] > 0 ? 1 : 0;
+}
+
+__global__ void k_mesh_add_count(unsigned long long* __restrict__ c, unsigned long long v) { *c += v; }
+
+__global__ void k_mesh_edge_reduce(const uint8_t* __restrict__ ok, const int* __restrict__ sample_edge, int total,
+                                   uint8_t* __restrict__ out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < total && !ok[k]) out[sample_edge[k]] = 0;
+}
+
+// ------------------------------------------------------------------ host
+
+static MeshView mesh_view(const MeshData* md) {
+    MeshView v;
+    v.env_tris = md->env_tris; v.env_nodes = md->env_nodes;
+    v.robot_tris = md->robot_tris; v.robot_leaves = md->robot_leaves;
+    v.nenv = md->nenv; v.nrleaves = md->nrleaves;
+    v.reach = (float)md->robot_radius * (1.f + 1e-5f) + MESH_MARGIN;
+    return v;
+}
+
+mptg_status mesh_scene_create(mptg_ctx* ctx, const mptg_scene_desc* d, mptg_scene* s) {
+    if (d->nrobot < 1 || !d->robot_tris || d->nenv < 0 || (d->nenv && !d->env_tris) || d->nenv > (1 << 28) ||
+        d->nrobot > (1 << 24))
+        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "rigid mesh scene needs robot triangles and an environment");
+    MeshData* md = new MeshData();
+    s->mesh = md;
+    // environment tree
+    std::vector<double> env(d->env_tris, d->env_tris + 9 * (size_t)d->nenv);
+    std::vector<int> eidx(d->nenv);
+    std::iota(eidx.begin(), eidx.end(), 0);
+    std::vector<BvhNode> enodes;
+    if (d->nenv) build_rec(env, eidx, 0, (int)d->nenv, enodes, nullptr);
+    std::vector<double> env_sorted(env.size());
+    for (size_t i = 0; i < eidx.size(); ++i)
+        std::copy(&env[9 * (size_t)eidx[i]], &env[9 * (size_t)eidx[i]] + 9, &env_sorted[9 * i]);
+    // robot tree (only its leaves are used on the device)
+    std::vector<double> rob(d->robot_tris, d->robot_tris + 9 * (size_t)d->nrobot);
+    std::vector<int> ridx(d->nrobot);
+    std::iota(ridx.begin(), ridx.end(), 0);
+    std::vector<BvhNode> rnodes;
+    std::vector<int> rleaf_ids;
+    build_rec(rob, ridx, 0, (int)d->nrobot, rnodes, &rleaf_ids);
+    std::vector<double> rob_sorted(rob.size());
+    for (size_t i = 0; i < ridx.size(); ++i)
+        std::copy(&rob[9 * (size_t)ridx[i]], &rob[9 * (size_t)ridx[i]] + 9, &rob_sorted[9 * i]);
+    std::vector<BvhNode> rleaves;
+    for (int id : rleaf_ids) rleaves.push_back(rnodes[id]);
+    double rad = 0.0;
+    for (size_t v = 0; v < rob.size() / 3; ++v) {
+        double x = rob[3 * v], y = rob[3 * v + 1], z = rob[3 * v + 2];
+        rad = std::max(rad, std::sqrt(x * x + y * y + z * z));
+    }
+    md->robot_radius = rad;
+    md->nenv = (int)d->nenv;
+    md->nenv_nodes = (int)enodes.size();
+    md->nrobot = (int)d->nrobot;
+    md->nrleaves = (int)rleaves.size();
+    cudaError_t e = cudaSuccess;
+    auto up = [&](void** dst, const void* src, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(dst, bytes ? bytes : 16);
+        if (e == cudaSuccess && bytes) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+    };
+    up((void**)&md->env_tris, env_sorted.data(), env_sorted.size() * sizeof(double));
+    up((void**)&md->env_nodes, enodes.data(), enodes.size() * sizeof(BvhNode));
+    up((void**)&md->robot_tris, rob_sorted.data(), rob_sorted.size() * sizeof(double));
+    up((void**)&md->robot_leaves, rleaves.data(), rleaves.size() * sizeof(BvhNode));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&md->nwork, sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&md->hbuf, 4 * sizeof(int));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return mptg_fail(ctx, MPTG_ERR_OOM, "mesh scene allocation failed: %s", cudaGetErrorString(e));
+    }
+    return MPTG_OK;
 }
 
 void mesh_scene_free(mptg_scene* s) {
-    delete s->mesh;
+    MeshData* md = s->mesh;
+    if (!md) return;
+    void* ptrs[] = {md->env_tris, md->env_nodes, md->robot_tris, md->robot_leaves, md->work, md->nwork,
+                    md->samples, md->sample_edge, md->sample_ok, md->counts, md->offs};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (md->hbuf) cudaFreeHost(md->hbuf);
+    delete md;
     s->mesh = nullptr;
 }
 
 void mesh_fill_view(const mptg_scene*, SceneView*) {}
 
-mptg_status mesh_edges_dev(mptg_scene* sc, const double*, const double*, int, double, int, uint8_t*, cudaStream_t,
-                           unsigned long long*) {
-    return mptg_fail(sc->ctx, MPTG_ERR_INVALID_ARG, "rigid mesh scenes are not available in this build");
+static mptg_status grow(mptg_ctx* ctx, void** p, size_t* cap, size_t need, size_t elem, cudaStream_t s) {
+    if (need <= *cap) return MPTG_OK;
+    MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    size_t n = need + need / 2 + 1024;
+    MPTG_CUDA_TRY(ctx, cudaMalloc(p, n * elem));
+    *cap = n;
+    return MPTG_OK;
 }
 
-mptg_status mesh_states_dev(mptg_scene* sc, const double*, int, uint8_t*, cudaStream_t) {
-    return mptg_fail(sc->ctx, MPTG_ERR_INVALID_ARG, "rigid mesh scenes are not available in this build");
+mptg_status mesh_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* dout, cudaStream_t s) {
+    mptg_ctx* ctx = sc->ctx;
+    MeshData* md = sc->mesh;
+    if (n <= 0) return MPTG_OK;
+    size_t cap = md->work_cap;
+    mptg_status st = grow(ctx, (void**)&md->work, &cap, (size_t)n, sizeof(int), s);
+    if (st) return st;
+    md->work_cap = cap;
+    MeshView v = mesh_view(md);
+    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(md->nwork, 0, sizeof(int), s));
+    k_mesh_sphere<<<mptg_blocks(n, 128), 128, 0, s>>>(v, dq, n, sc->D, dout, md->work, md->nwork);
+    MPTG_LAUNCHED(ctx);
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(md->hbuf, md->nwork, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    int nw = md->hbuf[0];
+    if (nw > 0) {
+        // one block per state that the sphere test could not clear
+        k_mesh_detail<<<nw, 256, 0, s>>>(v, dq, sc->D, md->work, md->nwork, dout);
+        MPTG_LAUNCHED(ctx);
+    }
+    MPTG_CUDA_TRY(ctx, cudaGetLastError());
+    return MPTG_OK;
+}
+
+mptg_status mesh_edges_dev(mptg_scene* sc, const double* da, const double* db, int n, double step, int resolution,
+                           uint8_t* dout, cudaStream_t s, unsigned long long* nsamp) {
+    mptg_ctx* ctx = sc->ctx;
+    MeshData* md = sc->mesh;
+    if (n <= 0) return MPTG_OK;
+    if (resolution != 0) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "rigid mesh edges use the space metric");
+    if (n > (1 << 20)) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "at most 2^20 mesh edges per call");
+    size_t cap = md->edge_cap;
+    mptg_status st = grow(ctx, (void**)&md->counts, &cap, (size_t)n + 1, sizeof(int), s);
+    if (st) return st;
+    cap = md->edge_cap;
+    st = grow(ctx, (void**)&md->offs, &cap, (size_t)n + 1, sizeof(int), s);
+    if (st) return st;
+    md->edge_cap = cap;
+    k_mesh_edge_counts<<<mptg_blocks(n, 128), 128, 0, s>>>(sc->metric, sc->D, sc->w0, sc->w1, da, db, n, 1.0 / step,
+                                                           md->counts);
+    k_mesh_scan<<<1, 1024, 0, s>>>(md->counts, n, md->offs, md->offs + n);
+    ctx->launches += 2;
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(md->hbuf, md->offs + n, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    int total = md->hbuf[0];
+    k_mesh_edge_init<<<mptg_blocks(n, 256), 256, 0, s>>>(md->counts, n, dout);
+    MPTG_LAUNCHED(ctx);
+    if (total > 0) {
+        cap = md->sample_cap;
+        size_t cap2 = md->sample_cap, cap3 = md->sample_cap;
+        if ((st = grow(ctx, (void**)&md->samples, &cap, (size_t)total, sc->D * sizeof(double), s))) return st;
+        if ((st = grow(ctx, (void**)&md->sample_edge, &cap2, (size_t)total, sizeof(int), s))) return st;
+        if ((st = grow(ctx, (void**)&md->sample_ok, &cap3, (size_t)total, 1, s))) return st;
+        md->sample_cap = std::min(cap, std::min(cap2, cap3));
+        k_mesh_edge_samples<<<n, 64, 0, s>>>(sc->metric, sc->D, da, db, n, md->counts, md->offs, md->samples,
+                                             md->sample_edge);
+        MPTG_LAUNCHED(ctx);
+        st = mesh_states_dev(sc, md->samples, total, md->sample_ok, s);
+        if (st) return st;
+        k_mesh_edge_reduce<<<mptg_blocks(total, 256), 256, 0, s>>>(md->sample_ok, md->sample_edge, total, dout);
+        MPTG_LAUNCHED(ctx);
+        if (nsamp) {
+            k_mesh_add_count<<<1, 1, 0, s>>>(nsamp, (unsigned long long)total);
+            MPTG_LAUNCHED(ctx);
+        }
+    }
+    MPTG_CUDA_TRY(ctx, cudaGetLastError());
+    return MPTG_OK;
 }

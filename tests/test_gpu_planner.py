@@ -33,7 +33,8 @@ def _oracle_plan(orc, sc, wavefront, seed, max_nodes, waves, stop, goal_bias=0.0
     return orc.plan(sc, sp, params, sc["lo"], sc["hi"], sc["start"], sc["goal"], waves, stop)
 
 
-@pytest.mark.parametrize("mk,wavefront,waves", [(scenes.grid_scene, 512, 8), (scenes.arm_scene, 256, 4)])
+@pytest.mark.parametrize("mk,wavefront,waves", [(scenes.grid_scene, 512, 8), (scenes.arm_scene, 256, 4),
+                                                (scenes.mesh_scene, 256, 4)])
 def test_wavefronts_replay_oracle_bit_exact(ctx, orc, mk, wavefront, waves):
     sc = mk()
     pl = _planner(ctx, sc, wavefront, 1234, 50000)

@@ -44,6 +44,46 @@ def test_edges_match_oracle(ctx, orc, mk):
     assert 0.01 < want.mean() < 0.99
 
 
+def _near_contact_states(sc, n, seed):
+    """SE(3) states whose robot sits within about one bounding radius of a box face."""
+    rng = np.random.default_rng(seed)
+    boxes = sc["boxes"]
+    out = scenes.uniform_states(sc, n, seed + 1)
+    for i in range(n):
+        lo, hi = boxes[rng.integers(len(boxes))]
+        p = rng.uniform(lo, hi)
+        ax = rng.integers(3)
+        side = rng.integers(2)
+        p[ax] = (hi if side else lo)[ax] + (1 if side else -1) * rng.uniform(0.3, 1.2) * sc["robot_bound"]
+        out[i, 4:] = p
+    return out
+
+
+def test_mesh_states_match_oracle(ctx, orc):
+    sc = scenes.mesh_scene()
+    q = np.concatenate([scenes.uniform_states(sc, 3000, 501), _near_contact_states(sc, 3000, 502)])
+    g = _scene(ctx, sc)
+    sp = orc.make_space(3, 7, sc["weights"])
+    want = orc.valid_states(sc, sp, q)
+    got = g.valid(q)
+    assert np.array_equal(got, want), np.nonzero(got != want)[0][:10]
+    assert 0.05 < want.mean() < 0.95
+
+
+def test_mesh_edges_match_oracle(ctx, orc):
+    sc = scenes.mesh_scene()
+    a, b = scenes.steered_edges(sc, 1500, 503)
+    near = _near_contact_states(sc, 500, 504)
+    a = np.concatenate([a, near])
+    b = np.concatenate([b, near + np.concatenate([np.zeros((500, 4)), np.full((500, 3), 0.4)], 1)])
+    g = _scene(ctx, sc)
+    sp = orc.make_space(3, 7, sc["weights"])
+    want, _ = orc.valid_edges(sc, sp, a, b, sc["edge_step"], 0)
+    got = g.link(a, b, sc["edge_step"], 0)
+    assert np.array_equal(got, want), np.nonzero(got != want)[0][:10]
+    assert 0.05 < want.mean() < 0.95
+
+
 def test_edges_degenerate(ctx, orc):
     sc = scenes.grid_scene()
     g = _scene(ctx, sc)
