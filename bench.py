@@ -119,6 +119,61 @@ def _queries(sc, nbatches, seed):
     return [scenes.uniform_states(sc, BATCH, seed + i) for i in range(nbatches)]
 
 
+def edge_rates(ctx, m, stream, torch):
+    """Edge checks/s through the batched DMV for the three scenes (device buffers)."""
+    from mpt_gb300 import scenes
+    out = {}
+    for name, mk, n in [("grid_1024", scenes.grid_scene, 65536), ("arm_10link", scenes.arm_scene, 65536),
+                        ("se3_mesh", scenes.mesh_scene, 16384)]:
+        sc = mk()
+        scene = m.Scene(ctx, sc)
+        ea, eb = scenes.steered_edges(sc, 4096, 555)
+        reps = n // len(ea)
+        da = torch.from_numpy(np.tile(ea, (reps, 1))).cuda()
+        db = torch.from_numpy(np.tile(eb, (reps, 1))).cuda()
+        eo = torch.empty(len(da), dtype=torch.uint8, device="cuda")
+        for _ in range(2):
+            scene.link(da, db, sc["edge_step"], sc["resolution"], out=eo, stream=stream)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            scene.link(da, db, sc["edge_step"], sc["resolution"], out=eo, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = {"edges_per_s": len(da) * 3 / (e0.elapsed_time(e1) / 1000.0), "edges_per_launch": len(da),
+                     "valid_fraction": float(eo.float().mean().item())}
+        scene.close()
+    return out
+
+
+def solve_times(ctx, seeds=5, cap_s=20.0):
+    """Wall time to the first solution of the plain wavefront planner per scene (p50 over seeds)."""
+    from mpt_gb300 import planner as P
+    from mpt_gb300 import scenes
+    res = {}
+    for name, mk, W in [("grid_1024", scenes.grid_scene, 2048), ("arm_10link", scenes.arm_scene, 4096),
+                        ("se3_mesh", scenes.mesh_scene, 4096)]:
+        sc = mk()
+        times, solved, nodes = [], 0, []
+        for s in range(seeds):
+            pl = P.Planner(P.Scenario(sc), P.PRRT(P.gpu_wavefront(W)), seed=1000 + s, ctx=ctx, max_nodes=1 << 21)
+            pl.add_start(sc["start"])
+            t0 = time.perf_counter()
+            pl.solve_for(cap_s, lambda: pl.solved())
+            dt = time.perf_counter() - t0
+            if pl.solved():
+                solved += 1
+                times.append(dt)
+            nodes.append(pl.size())
+            pl.close()
+        res[name] = {"p50_s": statistics.median(times) if times else None,
+                     "p99_s": max(times) if times else None, "solved": solved, "seeds": seeds,
+                     "cap_s": cap_s, "median_nodes": statistics.median(nodes)}
+    return res
+
+
 def run_reference(args):
     """CPU kd-tree (oracle port) on all host cores, bounded sample per step."""
     ws, rank, _ = _dist_env()
@@ -252,31 +307,25 @@ def run_gpu(args):
     # results of the host path equal the device path
     assert np.array_equal(hi.numpy(), tree.nearest(hq[(args.steps - 1) % nbuf])[0])
 
-    # secondary: edge checks/s on the arm scene (DMV at 0.01 rad joint steps)
-    from mpt_gb300 import scenes
-    scene = m.Scene(ctx, sc)
-    ea, eb = scenes.steered_edges(sc, 8192, 555)
-    reps = N_EDGES // len(ea)
-    da = torch.from_numpy(np.tile(ea, (reps, 1))).cuda()
-    db = torch.from_numpy(np.tile(eb, (reps, 1))).cuda()
-    eo = torch.empty(N_EDGES, dtype=torch.uint8, device="cuda")
-    for _ in range(2):
-        scene.link(da, db, sc["edge_step"], sc["resolution"], out=eo, stream=stream)
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    esteps = 3
-    for _ in range(esteps):
-        scene.link(da, db, sc["edge_step"], sc["resolution"], out=eo, stream=stream)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    edge_rate = N_EDGES * esteps / (e0.elapsed_time(e1) / 1000.0)
+    # secondary figures: edge checks/s (three scenes) and time to solve
+    edges = edge_rates(ctx, m, stream, torch)
+    solves = solve_times(ctx) if not args.no_solve else None
 
-    # CPU baseline: oracle kd-tree on the host cores, bounded sample
+    # CPU baselines: oracle kd-tree and DMV on the host cores, bounded samples
     cpu = None
     if rank == 0:
         import oracle
+        from mpt_gb300 import scenes
+        for name, mk in [("grid_1024", scenes.grid_scene), ("arm_10link", scenes.arm_scene),
+                         ("se3_mesh", scenes.mesh_scene)]:
+            scx = mk()
+            ea, eb = scenes.steered_edges(scx, 4096, 555)
+            osp = oracle.make_space(scx["metric"], scx["dim"], scx["weights"])
+            oracle.valid_edges(scx, osp, ea[:64], eb[:64], scx["edge_step"], scx["resolution"])
+            t0 = time.perf_counter()
+            oracle.valid_edges(scx, osp, ea, eb, scx["edge_step"], scx["resolution"])
+            edges[name]["cpu_edges_per_s"] = len(ea) / (time.perf_counter() - t0)
+            edges[name]["cpu_cores"] = os.cpu_count()
         osp = oracle.make_space(sc["metric"], sc["dim"])
         ot = oracle.KDTree(osp, pts, 8)
         sample = 2048
@@ -304,8 +353,9 @@ def run_gpu(args):
                              "kernel": "k_nearest<SO2,16>", "alg_bytes_per_launch": alg_bytes,
                              "counters_per_launch": per_launch},
                 "cpu_baseline": cpu,
-                "edge_checks": {"value": edge_rate, "unit": "edges/s", "workload": "arm DMV, 0.01 rad joint step",
-                                "edges_per_launch": N_EDGES},
+                "edge_checks": {"unit": "edges/s", "per_scene": edges,
+                                "cpu_kind": "port (oracle DMV + exact validity, all host cores)"},
+                "time_to_solve": {"unit": "s", "planner": "plain wavefront PRRT (GPU)", "per_scene": solves},
                 "clocks": clk.summary(), "gpu_launches": launches, "tree_build_s": build_s,
                 "wall_s_timed": wall}
         print(json.dumps(line))
@@ -321,6 +371,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--queries", type=int, default=BATCH, help="queries per step (profiling: a smaller case)")
     ap.add_argument("--nn-only", action="store_true", help="time the NN kernel only (profiling)")
+    ap.add_argument("--no-solve", action="store_true", help="skip the time-to-solve runs")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
