@@ -219,6 +219,31 @@ mptg_status mptg_planner_solution(mptg_planner* planner, double* path, size_t ca
 /* PRRT::visitGraph (prrt.hpp:300-316): all states and parent ids (-1 for starts). */
 mptg_status mptg_planner_graph(mptg_planner* planner, double* states, int32_t* parents, size_t cap,
                                size_t* n);
+/* ---- learned collision surrogate ------------------------------------
+ * No counterpart in the reference.  An MLP in -> 256 -> 256 -> 256 -> 256 -> 1
+ * (SiLU, BF16 weights/activations, FP32 accumulation) predicting the logit
+ * that a state is in collision, trained on states labelled by the exact
+ * checker.  It only orders and culls candidate edges; edges enter the tree
+ * only after the exact check.  Inputs are (state - shift) * scale. */
+typedef struct mptg_surrogate mptg_surrogate;
+mptg_status mptg_surrogate_create(mptg_ctx* ctx, int in_dim, const double* scale, const double* shift,
+                                  uint64_t seed, mptg_surrogate** surrogate);
+mptg_status mptg_surrogate_destroy(mptg_surrogate* surrogate);
+mptg_status mptg_surrogate_num_params(mptg_surrogate* surrogate, size_t* n);
+/* which 0: parameters, 1: gradients of the last train step (FP32, host buffer of n) */
+mptg_status mptg_surrogate_get(mptg_surrogate* surrogate, int which, float* out, size_t n);
+mptg_status mptg_surrogate_set(mptg_surrogate* surrogate, const float* params, size_t n);
+/* One Adam step (lr <= 0: gradients only) of BCE-with-logits on n states
+ * (n a multiple of 128), labels 1 = in collision; the batch loss goes to loss. */
+mptg_status mptg_surrogate_train_step(mptg_surrogate* surrogate, const double* states, const uint8_t* labels,
+                                      size_t n, double lr, float* loss, void* stream);
+/* collision logits of n states */
+mptg_status mptg_surrogate_score(mptg_surrogate* surrogate, const double* states, size_t n, float* logits,
+                                 void* stream);
+/* Cull edges whose new state's collision logit exceeds `threshold` before the
+ * exact check (they count as rejected); NULL removes the surrogate. */
+mptg_status mptg_planner_set_surrogate(mptg_planner* planner, mptg_surrogate* surrogate, double threshold);
+
 /* WorkerStats (prrt.hpp:63-101): [0] wavefronts, [1] samples, [2] nodes
  * added, [3] tree size, [4] goals, [5] states checked by link, [6] seconds in
  * run, [7] wavefront counter. */

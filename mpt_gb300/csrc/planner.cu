@@ -67,7 +67,20 @@ struct mptg_planner {
     uint64_t stat_skipped = 0;
     double stat_seconds = 0;
     bool solving = false;
+    // learned surrogate: cull edges whose new state is predicted in collision
+    mptg_surrogate* sg = nullptr;
+    float sg_thr = 0.f;
+    float* logits = nullptr;
+    double* near_c = nullptr;
+    double* new_c = nullptr;
+    int* cmap = nullptr;
+    uint8_t* ok_c = nullptr;
+    uint8_t* keep = nullptr;
+    uint64_t stat_culled = 0;
 };
+
+extern "C" mptg_status mptg_surrogate_score_dev(mptg_surrogate* s, const double* dstates, int n, float* dlogits,
+                                                cudaStream_t st);
 
 // ------------------------------------------------------------------ kernels
 
@@ -211,6 +224,36 @@ __global__ void k_plan_scatter(PlanView p, int W, const int* __restrict__ scan, 
     acc_goal[pos] = g;
 }
 
+// surrogate culling: flag the edges that go to the exact check
+__global__ void k_plan_keep(int W, const uint8_t* __restrict__ skip, const float* __restrict__ logit, float thr,
+                            uint8_t* __restrict__ keep, uint8_t* __restrict__ ok) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W) return;
+    keep[i] = (!skip[i] && !(logit[i] > thr)) ? 1 : 0;
+    ok[i] = 0;
+}
+
+__global__ void k_plan_cgather(PlanView p, int W, const int* __restrict__ scan, const int* __restrict__ bsum,
+                               const double* __restrict__ nearst, const double* __restrict__ newst,
+                               double* __restrict__ near_c, double* __restrict__ new_c, int* __restrict__ cmap) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W) return;
+    int l = scan[i];
+    if (l < 0) return;
+    int pos = bsum[i / PLAN_SCAN_BLOCK] + l;
+    for (int k = 0; k < p.D; ++k) {
+        near_c[(size_t)pos * p.D + k] = nearst[(size_t)i * p.D + k];
+        new_c[(size_t)pos * p.D + k] = newst[(size_t)i * p.D + k];
+    }
+    cmap[pos] = i;
+}
+
+__global__ void k_plan_cscatter(int n, const int* __restrict__ cmap, const uint8_t* __restrict__ ok_c,
+                                uint8_t* __restrict__ ok) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) ok[cmap[j]] = ok_c[j];
+}
+
 // walk a goal's parent chain: path ids (start first) and the summed cost
 // (PRRT::pathCost, src/mpt/impl/prrt/prrt.hpp:208-234)
 __global__ void k_plan_path(int goal, const int* __restrict__ parent, const double* __restrict__ states64, int D,
@@ -252,7 +295,8 @@ static PlanView plan_view(const mptg_planner* p) {
 
 static void planner_free(mptg_planner* p) {
     void* ptrs[] = {p->lo, p->hi, p->goal, p->parent, p->samp, p->nidx, p->ndist, p->nearst, p->newst, p->skip,
-                    p->ok, p->scan, p->bsum, p->acc_states, p->acc_parent, p->acc_goal, p->nsamp};
+                    p->ok, p->scan, p->bsum, p->acc_states, p->acc_parent, p->acc_goal, p->nsamp, p->logits,
+                    p->near_c, p->new_c, p->cmap, p->ok_c, p->keep};
     for (void* x : ptrs)
         if (x) cudaFree(x);
     if (p->hbuf) cudaFreeHost(p->hbuf);
@@ -284,9 +328,32 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
     k_plan_steer<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->samp, p->nidx, p->ndist, mptg_tree_states_dev(p->tree),
                                                      p->nearst, p->newst, p->skip);
     ctx->launches += 2;
-    st = scene_edges_dev(p->scene, p->nearst, p->newst, W, p->prm.edge_step, p->prm.resolution, p->ok, s, p->nsamp);
-    if (st) return st;
     int nblk = (W + PLAN_SCAN_BLOCK - 1) / PLAN_SCAN_BLOCK;
+    if (p->sg) {
+        // score the new states; only edges the surrogate does not reject go to the exact check
+        if ((st = mptg_surrogate_score_dev(p->sg, p->newst, W, p->logits, s))) return st;
+        k_plan_keep<<<mptg_blocks(W, 256), 256, 0, s>>>(W, p->skip, p->logits, p->sg_thr, p->keep, p->ok);
+        k_plan_scan<<<nblk, PLAN_SCAN_BLOCK, 0, s>>>(W, p->keep, p->skip, p->scan, p->bsum);
+        k_plan_scan_top<<<1, 1024, 0, s>>>(nblk, p->bsum);
+        k_plan_cgather<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->scan, p->bsum, p->nearst, p->newst, p->near_c,
+                                                           p->new_c, p->cmap);
+        ctx->launches += 4;
+        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->hbuf + 1, p->bsum + nblk, sizeof(int), cudaMemcpyDeviceToHost, s));
+        MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        int nk = p->hbuf[1];
+        p->stat_culled += (uint64_t)(W - nk);
+        if (nk > 0) {
+            st = scene_edges_dev(p->scene, p->near_c, p->new_c, nk, p->prm.edge_step, p->prm.resolution, p->ok_c, s,
+                                 p->nsamp);
+            if (st) return st;
+            k_plan_cscatter<<<mptg_blocks(nk, 256), 256, 0, s>>>(nk, p->cmap, p->ok_c, p->ok);
+            MPTG_LAUNCHED(ctx);
+        }
+    } else {
+        st = scene_edges_dev(p->scene, p->nearst, p->newst, W, p->prm.edge_step, p->prm.resolution, p->ok, s,
+                             p->nsamp);
+        if (st) return st;
+    }
     k_plan_scan<<<nblk, PLAN_SCAN_BLOCK, 0, s>>>(W, p->ok, p->skip, p->scan, p->bsum);
     k_plan_scan_top<<<1, 1024, 0, s>>>(nblk, p->bsum);
     k_plan_scatter<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->scan, p->bsum, p->newst, p->nidx, p->acc_states,
@@ -514,6 +581,27 @@ mptg_status mptg_planner_graph(mptg_planner* p, double* states, int32_t* parents
         if (st) return st;
     }
     if (parents) MPTG_CUDA_TRY(p->ctx, cudaMemcpy(parents, p->parent, sz * sizeof(int), cudaMemcpyDeviceToHost));
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_set_surrogate(mptg_planner* p, mptg_surrogate* sg, double threshold) {
+    if (!p) return MPTG_ERR_INVALID_ARG;
+    if (sg && !p->logits) {
+        const size_t W = p->prm.wavefront, D = p->D;
+        cudaError_t e = cudaSuccess;
+        if (e == cudaSuccess) e = cudaMalloc((void**)&p->logits, W * sizeof(float));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&p->near_c, W * D * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&p->new_c, W * D * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&p->cmap, W * sizeof(int));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&p->ok_c, W);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&p->keep, W);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return mptg_fail(p->ctx, MPTG_ERR_OOM, "surrogate buffers: %s", cudaGetErrorString(e));
+        }
+    }
+    p->sg = sg;
+    p->sg_thr = (float)threshold;
     return MPTG_OK;
 }
 

@@ -1,0 +1,593 @@
+// surrogate.cu - learned collision surrogate: an MLP trained on the GPU by
+// this project's own forward/backward kernels.
+//
+// No counterpart in the reference (a GB300 addition): the network only orders
+// and culls candidate edges; an edge still enters the tree only after the
+// exact check (scene.cu / mesh.cu) accepts it.
+//
+// Network: in (<= 16, SE(3) states use 7) -> 256 -> 256 -> 256 -> 256 -> 1,
+// SiLU after each hidden layer, logit out (1 = in collision).  BF16 weights and
+// activations, FP32 accumulation; FP32 master weights, Adam, BCE-with-logits.
+//   layer 0 (in -> 256) and the output layer (256 -> 1): CUDA cores
+//   layers 1-3 (256 -> 256), forward, input-gradient and weight-gradient
+//   products: BF16 tensor-core GEMM (mma.sync m16n8k16, FP32 accumulate),
+//   tiles 128 x 128 x 32, fused epilogues (bias + SiLU; SiLU'; split-K sums)
+// The network is tiny next to the collision checks it screens (0.4 MFLOP per
+// state forward), so the GEMM is sized for correctness and simplicity.
+#include <cuda_bf16.h>
+
+#include "metrics.cuh"
+#include "philox.cuh"
+
+#define SG_W 256
+#define SG_MAXIN 16
+#define SG_TM 128
+#define SG_TN 128
+#define SG_TK 32
+#define SG_PAD 8
+
+typedef __nv_bfloat16 bf16;
+
+struct mptg_surrogate {
+    mptg_ctx* ctx = nullptr;
+    int in = 7;
+    double scale[SG_MAXIN], shift[SG_MAXIN];
+    size_t nparam = 0;
+    float* P = nullptr;   // FP32 master parameters
+    float* G = nullptr;   // gradients
+    float* Mo = nullptr;  // Adam first moment
+    float* Vo = nullptr;  // Adam second moment
+    // BF16 copies of the hidden weights: [l][out][in] and transposed [l][in][out]
+    bf16* Wb = nullptr;
+    bf16* WTb = nullptr;
+    int step = 0;
+    // activations for a batch of capacity cap
+    size_t cap = 0;
+    bf16* X = nullptr;            // [cap][16]
+    float* Z = nullptr;           // [4][cap][256] pre-activations
+    bf16* H = nullptr;            // [4][cap][256]
+    bf16* HT = nullptr;           // [4][256][cap]
+    bf16* dZ = nullptr;           // [cap][256] current layer
+    bf16* dZT = nullptr;          // [256][cap]
+    float* dH = nullptr;          // [cap][256] (output-layer backprop)
+    float* zout = nullptr;        // [cap]
+    float* dzout = nullptr;       // [cap]
+    float* loss = nullptr;        // [1]
+    double* dstates = nullptr;    // staging for host inputs [cap][in]
+    uint8_t* dlabels = nullptr;
+    float* dlogits = nullptr;
+};
+
+// parameter layout (floats)
+struct SgLayout {
+    size_t W0, b0, W[4], b[4], w4, b4, total;
+};
+static SgLayout sg_layout(int in) {
+    SgLayout L;
+    size_t o = 0;
+    L.W0 = o; o += (size_t)SG_W * in;
+    L.b0 = o; o += SG_W;
+    for (int l = 1; l <= 3; ++l) { L.W[l] = o; o += (size_t)SG_W * SG_W; L.b[l] = o; o += SG_W; }
+    L.w4 = o; o += SG_W;
+    L.b4 = o; o += 1;
+    L.total = o;
+    return L;
+}
+
+__device__ __forceinline__ float sg_sigmoid(float z) { return 1.f / (1.f + __expf(-z)); }
+__device__ __forceinline__ float sg_silu(float z) { return z * sg_sigmoid(z); }
+__device__ __forceinline__ float sg_dsilu(float z) {
+    float s = sg_sigmoid(z);
+    return s * (1.f + z * (1.f - s));
+}
+
+// ------------------------------------------------------------------ tensor-core GEMM
+// C[m][n] = sum_k A[m][k] * B[n][k]  (A: [M][lda], B: [N][ldb], K contiguous)
+// blockIdx.z splits K into ranges of kspan.  8 warps: 4 (M) x 2 (N), 32 x 64 each.
+enum { EPI_FWD = 0, EPI_BWD = 1, EPI_GRAD = 2 };
+
+struct EpiArgs {
+    // forward: z = acc + bias; Z[m][n] = z; H[m][n] = silu(z) (bf16), HT[n][m]
+    const float* bias;
+    float* Z;
+    bf16* H;
+    bf16* HT;
+    int ldt;  // leading dimension of the transposed outputs (= M)
+    // backward: dz = acc * silu'(Zin[m][n]); dZ[m][n], dZT[n][m]
+    const float* Zin;
+    bf16* dZ;
+    bf16* dZT;
+    // gradient: G[m][n] += acc * gscale
+    float* G;
+    int ldc;
+};
+
+__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, const uint32_t* b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(256) k_sg_gemm(const bf16* __restrict__ A, int lda, const bf16* __restrict__ B,
+                                                 int ldb, int kspan, EpiArgs ep) {
+    __shared__ __align__(16) bf16 As[SG_TM][SG_TK + SG_PAD];
+    __shared__ __align__(16) bf16 Bs[SG_TN][SG_TK + SG_PAD];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = warp >> 1, wn = warp & 1;
+    const int g = lane >> 2, tg = lane & 3;
+    const int m0 = blockIdx.y * SG_TM, n0 = blockIdx.x * SG_TN;
+    const int k0 = blockIdx.z * kspan;
+    float acc[2][8][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
+
+    for (int kt = k0; kt < k0 + kspan; kt += SG_TK) {
+        // 128 rows x 32 bf16 = 512 x 16-byte vectors per operand: 2 per thread
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+            int idx = tid + v * 256;
+            int r = idx >> 2, c = (idx & 3) * 8;
+            *reinterpret_cast<uint4*>(&As[r][c]) =
+                *reinterpret_cast<const uint4*>(&A[(size_t)(m0 + r) * lda + kt + c]);
+            *reinterpret_cast<uint4*>(&Bs[r][c]) =
+                *reinterpret_cast<const uint4*>(&B[(size_t)(n0 + r) * ldb + kt + c]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < SG_TK; kk += 16) {
+            uint32_t af[2][4], bfr[8][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                int r = wm * 32 + i * 16 + g;
+                af[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][kk + tg * 2]);
+                af[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + tg * 2]);
+                af[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][kk + tg * 2 + 8]);
+                af[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + tg * 2 + 8]);
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                int n = wn * 64 + j * 8 + g;
+                bfr[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[n][kk + tg * 2]);
+                bfr[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[n][kk + tg * 2 + 8]);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
+        }
+        __syncthreads();
+    }
+    // epilogue: acc[i][j] holds rows (g, g+8) x cols (2tg, 2tg+1) of a 16 x 8 tile
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                int m = m0 + wm * 32 + i * 16 + g + (r >= 2 ? 8 : 0);
+                int n = n0 + wn * 64 + j * 8 + tg * 2 + (r & 1);
+                float v = acc[i][j][r];
+                if (EPI == EPI_FWD) {
+                    float z = v + ep.bias[n];
+                    ep.Z[(size_t)m * SG_W + n] = z;
+                    bf16 h = __float2bfloat16_rn(sg_silu(z));
+                    ep.H[(size_t)m * SG_W + n] = h;
+                    ep.HT[(size_t)n * ep.ldt + m] = h;
+                } else if (EPI == EPI_BWD) {
+                    float dz = v * sg_dsilu(ep.Zin[(size_t)m * SG_W + n]);
+                    bf16 h = __float2bfloat16_rn(dz);
+                    ep.dZ[(size_t)m * SG_W + n] = h;
+                    ep.dZT[(size_t)n * ep.ldt + m] = h;
+                } else {
+                    atomicAdd(&ep.G[(size_t)m * ep.ldc + n], v);
+                }
+            }
+}
+
+// ------------------------------------------------------------------ CUDA-core parts
+
+// inputs: FP64 states -> normalised BF16 features, padded to 16
+__global__ void k_sg_inputs(const double* __restrict__ s, int n, int in, const double* __restrict__ scale,
+                            const double* __restrict__ shift, int cap, bf16* __restrict__ X) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap) return;
+    for (int k = 0; k < SG_MAXIN; ++k) {
+        float v = 0.f;
+        if (i < n && k < in) v = (float)((s[(size_t)i * in + k] - shift[k]) * scale[k]);
+        X[(size_t)i * SG_MAXIN + k] = __float2bfloat16_rn(v);
+    }
+}
+
+// layer 0: Z0 = X W0^T + b0 (bf16 operands, fp32 accumulate); thread per (m, n)
+__global__ void k_sg_layer0(const bf16* __restrict__ X, int in, const float* __restrict__ W0,
+                            const float* __restrict__ b0, int M, float* __restrict__ Z, bf16* __restrict__ H,
+                            bf16* __restrict__ HT) {
+    size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (idx >= (size_t)M * SG_W) return;
+    int m = (int)(idx / SG_W), n = (int)(idx % SG_W);
+    float z = b0[n];
+    for (int k = 0; k < in; ++k)
+        z = fmaf(__bfloat162float(X[(size_t)m * SG_MAXIN + k]), __bfloat162float(__float2bfloat16_rn(W0[n * in + k])), z);
+    Z[idx] = z;
+    bf16 h = __float2bfloat16_rn(sg_silu(z));
+    H[idx] = h;
+    HT[(size_t)n * M + m] = h;
+}
+
+// output layer: zout[m] = H3[m] . w4 + b4 (warp per sample)
+__global__ void k_sg_out(const bf16* __restrict__ H3, const float* __restrict__ w4, const float* __restrict__ b4,
+                         int M, float* __restrict__ zout) {
+    int m = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (m >= M) return;
+    float s = 0.f;
+    for (int k = lane; k < SG_W; k += 32)
+        s = fmaf(__bfloat162float(H3[(size_t)m * SG_W + k]), __bfloat162float(__float2bfloat16_rn(w4[k])), s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) zout[m] = s + b4[0];
+}
+
+// BCE-with-logits: loss and dL/dz for the first n (real) rows
+__global__ void k_sg_loss(const float* __restrict__ zout, const uint8_t* __restrict__ y, int n, float inv_n,
+                          float* __restrict__ dz, float* __restrict__ loss) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.f;
+    if (m < n) {
+        float z = zout[m], t = y[m] ? 1.f : 0.f;
+        l = fmaxf(z, 0.f) - z * t + log1pf(__expf(-fabsf(z)));
+        dz[m] = (sg_sigmoid(z) - t) * inv_n;
+    }
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+    if ((threadIdx.x & 31) == 0 && l != 0.f) atomicAdd(loss, l * inv_n);
+}
+
+// backprop through the output layer: dZ3 = (dz w4) * silu'(Z3); grads of w4, b4
+__global__ void k_sg_out_back(const float* __restrict__ dz, const float* __restrict__ w4,
+                              const float* __restrict__ Z3, const bf16* __restrict__ H3, int M, bf16* __restrict__ dZ,
+                              bf16* __restrict__ dZT, float* __restrict__ gw4, float* __restrict__ gb4) {
+    size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (idx >= (size_t)M * SG_W) return;
+    int m = (int)(idx / SG_W), n = (int)(idx % SG_W);
+    float d = dz[m];
+    float dh = d * __bfloat162float(__float2bfloat16_rn(w4[n]));
+    bf16 v = __float2bfloat16_rn(dh * sg_dsilu(Z3[idx]));
+    dZ[idx] = v;
+    dZT[(size_t)n * M + m] = v;
+    if (d != 0.f) {
+        atomicAdd(&gw4[n], d * __bfloat162float(H3[idx]));
+        if (n == 0) atomicAdd(gb4, d);
+    }
+}
+
+// bias gradient: column sums of dZ (block per column)
+__global__ void k_sg_colsum(const bf16* __restrict__ dZT, int M, float* __restrict__ gb) {
+    int n = blockIdx.x;
+    float s = 0.f;
+    for (int m = threadIdx.x; m < M; m += blockDim.x) s += __bfloat162float(dZT[(size_t)n * M + m]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ float ws[32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[w];
+        gb[n] = t;
+    }
+}
+
+// layer-0 weight gradient: G0[n][k] = sum_m dZ0[m][n] X[m][k] (block per n)
+__global__ void k_sg_grad0(const bf16* __restrict__ dZT0, const bf16* __restrict__ X, int M, int in,
+                           float* __restrict__ G0) {
+    int n = blockIdx.x;
+    __shared__ float acc[SG_MAXIN][8];
+    float s[SG_MAXIN];
+    for (int k = 0; k < SG_MAXIN; ++k) s[k] = 0.f;
+    for (int m = threadIdx.x; m < M; m += blockDim.x) {
+        float d = __bfloat162float(dZT0[(size_t)n * M + m]);
+        for (int k = 0; k < in; ++k) s[k] = fmaf(d, __bfloat162float(X[(size_t)m * SG_MAXIN + k]), s[k]);
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int k = 0; k < in; ++k) {
+        float v = s[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) acc[k][w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < in) {
+        float t = 0.f;
+        for (int ww = 0; ww < (int)(blockDim.x >> 5); ++ww) t += acc[threadIdx.x][ww];
+        G0[n * in + threadIdx.x] = t;
+    }
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 masters; refreshes the BF16 weight copies
+__global__ void k_sg_adam(float* __restrict__ P, const float* __restrict__ G, float* __restrict__ Mo,
+                          float* __restrict__ Vo, size_t n, float lr, float b1, float b2, float eps, float c1, float c2) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float g = G[i];
+    float m = b1 * Mo[i] + (1.f - b1) * g;
+    float v = b2 * Vo[i] + (1.f - b2) * g * g;
+    Mo[i] = m;
+    Vo[i] = v;
+    P[i] -= lr * (m / c1) / (sqrtf(v / c2) + eps);
+}
+
+__global__ void k_sg_refresh(const float* __restrict__ P, size_t off1, size_t off2, size_t off3,
+                             bf16* __restrict__ Wb, bf16* __restrict__ WTb) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 3 * SG_W * SG_W) return;
+    int l = idx / (SG_W * SG_W), r = idx % (SG_W * SG_W);
+    int o = r / SG_W, i = r % SG_W;
+    size_t off = l == 0 ? off1 : (l == 1 ? off2 : off3);
+    bf16 w = __float2bfloat16_rn(P[off + r]);
+    Wb[(size_t)l * SG_W * SG_W + (size_t)o * SG_W + i] = w;
+    WTb[(size_t)l * SG_W * SG_W + (size_t)i * SG_W + o] = w;
+}
+
+// deterministic initialisation: uniform(-1/sqrt(fan_in), 1/sqrt(fan_in))
+__global__ void k_sg_init(float* __restrict__ P, size_t n, uint64_t seed, SgLayout L, int in) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int fan = SG_W;
+    if (i < L.b0) fan = in;
+    double u = phx_uniform(seed, (uint32_t)i, 0x5eedu, 0);
+    P[i] = (float)((2.0 * u - 1.0) / sqrt((double)fan));
+}
+
+// ------------------------------------------------------------------ host
+
+static mptg_status sg_reserve(mptg_surrogate* s, size_t cap) {
+    if (cap <= s->cap) return MPTG_OK;
+    mptg_ctx* ctx = s->ctx;
+    MPTG_CUDA_TRY(ctx, cudaDeviceSynchronize());
+    void* ptrs[] = {s->X, s->Z, s->H, s->HT, s->dZ, s->dZT, s->dH, s->zout, s->dzout, s->dstates, s->dlabels,
+                    s->dlogits};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    cap = (cap + SG_TM - 1) / SG_TM * SG_TM;
+    cudaError_t e = cudaSuccess;
+#define A(p, b) if (e == cudaSuccess) e = cudaMalloc((void**)&(p), (b))
+    A(s->X, cap * SG_MAXIN * sizeof(bf16));
+    A(s->Z, 4 * cap * SG_W * sizeof(float));
+    A(s->H, 4 * cap * SG_W * sizeof(bf16));
+    A(s->HT, 4 * cap * SG_W * sizeof(bf16));
+    A(s->dZ, cap * SG_W * sizeof(bf16));
+    A(s->dZT, cap * SG_W * sizeof(bf16));
+    A(s->dH, cap * SG_W * sizeof(float));
+    A(s->zout, cap * sizeof(float));
+    A(s->dzout, cap * sizeof(float));
+    // [0, 16) scale, [16, 32) shift, then up to cap staged states
+    A(s->dstates, (cap * SG_MAXIN + 2 * SG_MAXIN) * sizeof(double));
+    A(s->dlabels, cap);
+    A(s->dlogits, cap * sizeof(float));
+#undef A
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return mptg_fail(ctx, MPTG_ERR_OOM, "surrogate buffers: %s", cudaGetErrorString(e));
+    }
+    s->cap = cap;
+    return MPTG_OK;
+}
+
+// forward over M (multiple of 128) rows already in s->X
+static void sg_forward(mptg_surrogate* s, int M, cudaStream_t st) {
+    SgLayout L = sg_layout(s->in);
+    const size_t MW = (size_t)M * SG_W;
+    k_sg_layer0<<<mptg_blocks(MW, 256), 256, 0, st>>>(s->X, s->in, s->P + L.W0, s->P + L.b0, M, s->Z, s->H, s->HT);
+    for (int l = 1; l <= 3; ++l) {
+        EpiArgs ep{};
+        ep.bias = s->P + L.b[l];
+        ep.Z = s->Z + l * MW;
+        ep.H = s->H + l * MW;
+        ep.HT = s->HT + l * MW;
+        ep.ldt = M;
+        dim3 grid(SG_W / SG_TN, M / SG_TM, 1);
+        k_sg_gemm<EPI_FWD><<<grid, 256, 0, st>>>(s->H + (l - 1) * MW, SG_W, s->Wb + (size_t)(l - 1) * SG_W * SG_W,
+                                                 SG_W, SG_W, ep);
+    }
+    k_sg_out<<<mptg_blocks((size_t)M * 32, 256), 256, 0, st>>>(s->H + 3 * MW, s->P + L.w4, s->P + L.b4, M, s->zout);
+    s->ctx->launches += 5;
+}
+
+extern "C" {
+
+mptg_status mptg_surrogate_create(mptg_ctx* ctx, int in_dim, const double* scale, const double* shift, uint64_t seed,
+                                  mptg_surrogate** out) {
+    if (!ctx || !out) return MPTG_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (in_dim < 1 || in_dim > SG_MAXIN) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "input dimension 1..16");
+    MPTG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    mptg_surrogate* s = new mptg_surrogate();
+    s->ctx = ctx;
+    s->in = in_dim;
+    for (int k = 0; k < SG_MAXIN; ++k) {
+        s->scale[k] = (scale && k < in_dim) ? scale[k] : 1.0;
+        s->shift[k] = (shift && k < in_dim) ? shift[k] : 0.0;
+    }
+    SgLayout L = sg_layout(in_dim);
+    s->nparam = L.total;
+    cudaError_t e = cudaSuccess;
+    size_t pb = L.total * sizeof(float);
+    for (float** p : {&s->P, &s->G, &s->Mo, &s->Vo})
+        if (e == cudaSuccess) e = cudaMalloc((void**)p, pb);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&s->Wb, 3 * SG_W * SG_W * sizeof(bf16));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&s->WTb, 3 * SG_W * SG_W * sizeof(bf16));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&s->loss, sizeof(float));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        delete s;
+        return mptg_fail(ctx, MPTG_ERR_OOM, "surrogate parameters: %s", cudaGetErrorString(e));
+    }
+    cudaMemset(s->Mo, 0, pb);
+    cudaMemset(s->Vo, 0, pb);
+    cudaMemset(s->G, 0, pb);
+    k_sg_init<<<mptg_blocks(L.total, 256), 256>>>(s->P, L.total, seed, L, in_dim);
+    // biases start at zero
+    cudaMemset(s->P + L.b0, 0, SG_W * sizeof(float));
+    for (int l = 1; l <= 3; ++l) cudaMemset(s->P + L.b[l], 0, SG_W * sizeof(float));
+    cudaMemset(s->P + L.b4, 0, sizeof(float));
+    k_sg_refresh<<<mptg_blocks(3 * SG_W * SG_W, 256), 256>>>(s->P, L.W[1], L.W[2], L.W[3], s->Wb, s->WTb);
+    ctx->launches += 2;
+    MPTG_CUDA_TRY(ctx, cudaDeviceSynchronize());
+    *out = s;
+    return MPTG_OK;
+}
+
+mptg_status mptg_surrogate_destroy(mptg_surrogate* s) {
+    if (!s) return MPTG_ERR_INVALID_ARG;
+    cudaDeviceSynchronize();
+    void* ptrs[] = {s->P, s->G, s->Mo, s->Vo, s->Wb, s->WTb, s->X, s->Z, s->H, s->HT, s->dZ, s->dZT, s->dH,
+                    s->zout, s->dzout, s->dstates, s->dlabels, s->dlogits, s->loss};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete s;
+    return MPTG_OK;
+}
+
+mptg_status mptg_surrogate_num_params(mptg_surrogate* s, size_t* n) {
+    if (!s || !n) return MPTG_ERR_INVALID_ARG;
+    *n = s->nparam;
+    return MPTG_OK;
+}
+
+mptg_status mptg_surrogate_get(mptg_surrogate* s, int which, float* out, size_t n) {
+    if (!s || !out || n != s->nparam || which < 0 || which > 1) return MPTG_ERR_INVALID_ARG;
+    MPTG_CUDA_TRY(s->ctx, cudaDeviceSynchronize());
+    MPTG_CUDA_TRY(s->ctx, cudaMemcpy(out, which == 0 ? s->P : s->G, n * sizeof(float), cudaMemcpyDeviceToHost));
+    return MPTG_OK;
+}
+
+mptg_status mptg_surrogate_set(mptg_surrogate* s, const float* in, size_t n) {
+    if (!s || !in || n != s->nparam) return MPTG_ERR_INVALID_ARG;
+    SgLayout L = sg_layout(s->in);
+    MPTG_CUDA_TRY(s->ctx, cudaMemcpy(s->P, in, n * sizeof(float), cudaMemcpyHostToDevice));
+    k_sg_refresh<<<mptg_blocks(3 * SG_W * SG_W, 256), 256>>>(s->P, L.W[1], L.W[2], L.W[3], s->Wb, s->WTb);
+    MPTG_LAUNCHED(s->ctx);
+    MPTG_CUDA_TRY(s->ctx, cudaDeviceSynchronize());
+    return MPTG_OK;
+}
+
+// internal: logits for n device states (used by the planner)
+mptg_status mptg_surrogate_score_dev(mptg_surrogate* s, const double* dstates, int n, float* dlogits, cudaStream_t st) {
+    if (n <= 0) return MPTG_OK;
+    mptg_status r = sg_reserve(s, (size_t)n);
+    if (r) return r;
+    int M = (n + SG_TM - 1) / SG_TM * SG_TM;
+    // scale/shift travel in the first 32 doubles of the staging buffer
+    MPTG_CUDA_TRY(s->ctx, cudaMemcpyAsync(s->dstates, s->scale, sizeof(s->scale), cudaMemcpyHostToDevice, st));
+    MPTG_CUDA_TRY(s->ctx, cudaMemcpyAsync(s->dstates + SG_MAXIN, s->shift, sizeof(s->shift), cudaMemcpyHostToDevice,
+                                          st));
+    k_sg_inputs<<<mptg_blocks(M, 256), 256, 0, st>>>(dstates, n, s->in, s->dstates, s->dstates + SG_MAXIN, M, s->X);
+    MPTG_LAUNCHED(s->ctx);
+    sg_forward(s, M, st);
+    MPTG_CUDA_TRY(s->ctx, cudaMemcpyAsync(dlogits, s->zout, n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    return MPTG_OK;
+}
+
+mptg_status mptg_surrogate_score(mptg_surrogate* s, const double* states, size_t n, float* logits, void* stream) {
+    if (!s || (!states && n) || (!logits && n)) return MPTG_ERR_INVALID_ARG;
+    if (n == 0) return MPTG_OK;
+    if (n > (1u << 26)) return mptg_fail(s->ctx, MPTG_ERR_INVALID_ARG, "too many states");
+    cudaStream_t st = (cudaStream_t)stream;
+    DevBuf bq, bo;
+    mptg_status r;
+    if ((r = mptg_stage_in(s->ctx, states, n * s->in * sizeof(double), st, &bq))) return r;
+    if ((r = mptg_stage_out_alloc(s->ctx, logits, n * sizeof(float), st, &bo))) return r;
+    if ((r = mptg_surrogate_score_dev(s, (const double*)bq.dptr, (int)n, (float*)bo.dptr, st))) return r;
+    MPTG_CUDA_TRY(s->ctx, cudaGetLastError());
+    return mptg_stage_finish(s->ctx, st, &bo, 1, &bq, 1);
+}
+
+// One Adam step on a batch: loss and gradients of BCE-with-logits, labels 1 =
+// in collision.  n must be a multiple of 128.  lr <= 0 computes the loss and
+// the gradients (readable with mptg_surrogate_get(s, 1, ...)) without
+// updating the parameters.
+mptg_status mptg_surrogate_train_step(mptg_surrogate* s, const double* states, const uint8_t* labels, size_t n,
+                                      double lr, float* loss_out, void* stream) {
+    if (!s || !states || !labels || n == 0) return MPTG_ERR_INVALID_ARG;
+    mptg_ctx* ctx = s->ctx;
+    if (n % SG_TM) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "batch must be a multiple of %d", SG_TM);
+    if (n > (1u << 20)) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "batch too large");
+    cudaStream_t st = (cudaStream_t)stream;
+    mptg_status r = sg_reserve(s, n);
+    if (r) return r;
+    const int M = (int)n;
+    const size_t MW = (size_t)M * SG_W;
+    SgLayout L = sg_layout(s->in);
+    // inputs
+    const double* dq = states;
+    if (!mptg_is_device_ptr(states)) {
+        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(s->dstates + 2 * SG_MAXIN, states, n * s->in * sizeof(double),
+                                           cudaMemcpyHostToDevice, st));
+        dq = s->dstates + 2 * SG_MAXIN;
+    }
+    const uint8_t* dy = labels;
+    if (!mptg_is_device_ptr(labels)) {
+        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(s->dlabels, labels, n, cudaMemcpyHostToDevice, st));
+        dy = s->dlabels;
+    }
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(s->dstates, s->scale, sizeof(s->scale), cudaMemcpyHostToDevice, st));
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(s->dstates + SG_MAXIN, s->shift, sizeof(s->shift), cudaMemcpyHostToDevice, st));
+    k_sg_inputs<<<mptg_blocks(M, 256), 256, 0, st>>>(dq, M, s->in, s->dstates, s->dstates + SG_MAXIN, M, s->X);
+    MPTG_LAUNCHED(ctx);
+    sg_forward(s, M, st);
+    // loss and output-layer gradients
+    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(s->G, 0, s->nparam * sizeof(float), st));
+    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(s->loss, 0, sizeof(float), st));
+    k_sg_loss<<<mptg_blocks(M, 256), 256, 0, st>>>(s->zout, dy, M, 1.f / (float)M, s->dzout, s->loss);
+    k_sg_out_back<<<mptg_blocks(MW, 256), 256, 0, st>>>(s->dzout, s->P + L.w4, s->Z + 3 * MW, s->H + 3 * MW, M,
+                                                        s->dZ, s->dZT, s->G + L.w4, s->G + L.b4);
+    ctx->launches += 2;
+    // hidden layers 3, 2, 1: weight and bias gradients, then back through W
+    for (int l = 3; l >= 1; --l) {
+        k_sg_colsum<<<SG_W, 256, 0, st>>>(s->dZT, M, s->G + L.b[l]);
+        EpiArgs eg{};
+        eg.G = s->G + L.W[l];
+        eg.ldc = SG_W;
+        int splits = M / 128;  // K (= batch) split into spans of 128
+        dim3 gg(SG_W / SG_TN, SG_W / SG_TM, splits);
+        // dW[out][in] = sum_m dZ[m][out] H_{l-1}[m][in]: A = dZ^T [out][M], B = H^T [in][M]
+        k_sg_gemm<EPI_GRAD><<<gg, 256, 0, st>>>(s->dZT, M, s->HT + (size_t)(l - 1) * MW, M, 128, eg);
+        // dH_{l-1} = dZ_l W_l, then * silu'(Z_{l-1})
+        EpiArgs eb{};
+        eb.Zin = s->Z + (size_t)(l - 1) * MW;
+        eb.dZ = s->dZ;
+        eb.dZT = s->dZT;
+        eb.ldt = M;
+        dim3 gb(SG_W / SG_TN, M / SG_TM, 1);
+        // the GEMM reads dZ/dZT of layer l while writing layer l-1's into the same
+        // buffers: stage through dH
+        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(s->dH, s->dZ, MW * sizeof(bf16), cudaMemcpyDeviceToDevice, st));
+        k_sg_gemm<EPI_BWD><<<gb, 256, 0, st>>>((const bf16*)s->dH, SG_W, s->WTb + (size_t)(l - 1) * SG_W * SG_W,
+                                               SG_W, SG_W, eb);
+        ctx->launches += 3;
+    }
+    // layer 0
+    k_sg_colsum<<<SG_W, 256, 0, st>>>(s->dZT, M, s->G + L.b0);
+    k_sg_grad0<<<SG_W, 256, 0, st>>>(s->dZT, s->X, M, s->in, s->G + L.W0);
+    ctx->launches += 2;
+    if (lr > 0) {
+        s->step += 1;
+        const float b1 = 0.9f, b2 = 0.999f;
+        float c1 = 1.f - powf(b1, (float)s->step), c2 = 1.f - powf(b2, (float)s->step);
+        k_sg_adam<<<mptg_blocks(s->nparam, 256), 256, 0, st>>>(s->P, s->G, s->Mo, s->Vo, s->nparam, (float)lr, b1, b2,
+                                                                1e-8f, c1, c2);
+        k_sg_refresh<<<mptg_blocks(3 * SG_W * SG_W, 256), 256, 0, st>>>(s->P, L.W[1], L.W[2], L.W[3], s->Wb, s->WTb);
+        ctx->launches += 2;
+    }
+    if (loss_out) {
+        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(loss_out, s->loss, sizeof(float), cudaMemcpyDeviceToHost, st));
+        MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    }
+    MPTG_CUDA_TRY(ctx, cudaGetLastError());
+    return MPTG_OK;
+}
+
+}  // extern "C"

@@ -135,8 +135,22 @@ class Planner:
         self._range = scenario.default_range
         self._goal_bias = 0.01
         self._starts = []
+        self._surrogate = None
         self.scene = Scene(self.ctx, scenario.desc)
         self.h = None
+
+    def set_surrogate(self, surrogate, threshold: float = 0.0):
+        """Cull edges whose new state the surrogate scores above `threshold`
+        (collision logit) before the exact check; None removes it."""
+        self._surrogate = (surrogate, float(threshold)) if surrogate is not None else None
+        if self.h is not None:
+            self._apply_surrogate()
+
+    def _apply_surrogate(self):
+        from . import surrogate as S
+        S._sig(self.lib)
+        sg, thr = self._surrogate if self._surrogate else (None, 0.0)
+        _check(self.ctx.h, self.lib.mptg_planner_set_surrogate(self.h, sg.h if sg else None, thr))
 
     # -- configuration (prrt.hpp:159-175)
     def set_range(self, r: float):
@@ -189,6 +203,8 @@ class Planner:
         for q in self._starts:
             _check(self.ctx.h, self.lib.mptg_planner_add_start(h, q.ctypes.data))
         self._starts = []
+        if self._surrogate:
+            self._apply_surrogate()
 
     # -- solving (planner_base.hpp:58-80, prrt.hpp:194-201)
     def run(self, max_wavefronts: int = 1, time_limit: float = 0.0, stop_when_solved: bool = False) -> bool:

@@ -226,6 +226,23 @@ def mesh_scene(seed: int = 20261206, nboxes: int = 400, cube: float = 20.0, box_
     }
 
 
+def near_contact_states(scene: dict, n: int, seed: int) -> np.ndarray:
+    """SE(3) states whose robot sits within about one bounding radius of a box
+    face (random orientation): the near-contact half of the surrogate's
+    training set."""
+    rng = np.random.default_rng(seed)
+    boxes = scene["boxes"]
+    out = uniform_states(scene, n, seed + 1)
+    for i in range(n):
+        lo, hi = boxes[rng.integers(len(boxes))]
+        p = rng.uniform(lo, hi)
+        ax = rng.integers(3)
+        side = rng.integers(2)
+        p[ax] = (hi if side else lo)[ax] + (1 if side else -1) * rng.uniform(0.3, 1.2) * scene["robot_bound"]
+        out[i, 4:] = p
+    return out
+
+
 # --------------------------------------------------------------------------- samplers
 def uniform_states(scene: dict, n: int, seed: int) -> np.ndarray:
     """Uniform states in the scene's sampling space (box for Lp/SO(2)^n, Shoemake

@@ -1,0 +1,100 @@
+"""GPU: the learned collision surrogate.
+
+* forward logits and backward gradients of the device kernels against the
+  CPU reference MLP (oracle/mlp.py, FP64 with the same BF16 rounding points).
+  Tolerance: relative L2 error of the gradient vector < 3e-2 and cosine
+  > 0.999; logits within 0.02 + 0.02|z| (BF16 operands round at 2^-8
+  relative, and a rounding flip of one activation moves sums at that scale);
+* training on exact-checker labels learns the SE(3) scene (held-out accuracy,
+  false-positive / false-negative rates reported);
+* the surrogate-culled planner returns only exact-validated paths and spends
+  fewer exact checks than the plain planner for the same wavefronts."""
+import numpy as np
+import pytest
+
+from mpt_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _labelled(ctx, sc, n, seed):
+    import mpt_gb300 as m
+    q = np.concatenate([scenes.uniform_states(sc, n // 2, seed), scenes.near_contact_states(sc, n - n // 2, seed + 7)])
+    valid = m.Scene(ctx, sc).valid(q)
+    return q, (1 - valid).astype(np.uint8)  # label 1 = in collision
+
+
+def test_forward_and_gradients_match_reference(ctx):
+    from mpt_gb300.surrogate import Surrogate, se3_normalisation
+    from oracle import mlp
+    sc = scenes.mesh_scene()
+    scale, shift = se3_normalisation(sc["lo"], sc["hi"])
+    sg = Surrogate(ctx, 7, scale, shift, seed=3)
+    rng = np.random.default_rng(0)
+    x = scenes.uniform_states(sc, 512, 11)
+    y = rng.integers(0, 2, 512).astype(np.uint8)
+    feats = (x - shift) * scale
+    p = sg.params().astype(np.float64)
+    z = sg.score(x)
+    zr, _ = mlp.forward(p, feats, 7)
+    assert np.all(np.abs(z - zr) <= 0.02 + 0.02 * np.abs(zr)), np.abs(z - zr).max()
+    loss = sg.train_step(x, y, lr=0.0)
+    g = sg.grads().astype(np.float64)
+    lr_, gr, _ = mlp.loss_and_grad(p, feats, y, 7)
+    assert abs(loss - lr_) < 1e-3 * max(1.0, abs(lr_))
+    rel = np.linalg.norm(g - gr) / np.linalg.norm(gr)
+    cos = float(g @ gr / (np.linalg.norm(g) * np.linalg.norm(gr)))
+    assert rel < 3e-2 and cos > 0.999, (rel, cos)
+    # a step with lr > 0 moves the parameters and leaves them finite
+    sg.train_step(x, y, lr=1e-3)
+    p2 = sg.params()
+    assert np.isfinite(p2).all() and not np.array_equal(p2, p.astype(np.float32))
+
+
+@pytest.fixture(scope="module")
+def trained(ctx):
+    from mpt_gb300.surrogate import Surrogate, se3_normalisation
+    sc = scenes.mesh_scene()
+    scale, shift = se3_normalisation(sc["lo"], sc["hi"])
+    q, y = _labelled(ctx, sc, 262144, 21)
+    sg = Surrogate(ctx, 7, scale, shift, seed=5)
+    hist = sg.fit(q, y, epochs=6, batch=8192, lr=1e-3)
+    return sc, sg, hist
+
+
+def test_training_learns_the_scene(ctx, trained):
+    sc, sg, hist = trained
+    assert hist[-1] < hist[0]
+    qt, yt = _labelled(ctx, sc, 32768, 99)
+    pred = (sg.score(qt) > 0).astype(np.uint8)
+    acc = float((pred == yt).mean())
+    fp = float(((pred == 1) & (yt == 0)).sum() / max(1, (yt == 0).sum()))  # free predicted in collision
+    fn = float(((pred == 0) & (yt == 1)).sum() / max(1, (yt == 1).sum()))  # collision predicted free
+    print("surrogate held-out accuracy %.4f  FP %.4f  FN %.4f  loss %s" % (acc, fp, fn, hist))
+    assert acc > 0.85, (acc, fp, fn)
+
+
+def test_surrogate_planner_exact_paths_and_fewer_checks(ctx, orc, trained):
+    from mpt_gb300 import planner as P
+    sc, sg, _ = trained
+    waves = 6
+    stats = {}
+    for mode in ("plain", "surrogate"):
+        pl = P.Planner(P.Scenario(sc), P.PRRT(P.gpu_wavefront(4096)), seed=17, ctx=ctx, max_nodes=1 << 20)
+        pl.add_start(sc["start"])
+        if mode == "surrogate":
+            pl.set_surrogate(sg, threshold=2.0)
+        pl.run(waves)
+        st = pl.stats()
+        stats[mode] = st
+        # every tree edge passed the exact check
+        states, parents = pl.graph()
+        sel = np.nonzero(parents >= 0)[0][:2000]
+        sp = orc.make_space(3, 7, sc["weights"])
+        ok, _ = orc.valid_edges(sc, sp, states[parents[sel]], states[sel], sc["edge_step"], 0)
+        assert ok.all()
+        pl.close()
+    print("link states checked: plain %d, surrogate %d; nodes: plain %d, surrogate %d" % (
+        stats["plain"]["link_states_checked"], stats["surrogate"]["link_states_checked"],
+        stats["plain"]["tree_size"], stats["surrogate"]["tree_size"]))
+    assert stats["surrogate"]["link_states_checked"] < stats["plain"]["link_states_checked"]
