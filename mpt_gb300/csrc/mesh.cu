@@ -43,6 +43,7 @@ struct BvhNode {  // 32 bytes
 struct MeshData {
     // environment (world frame), triangles in leaf order
     double* env_tris = nullptr;   // [nenv][9]
+    float* env_boxes = nullptr;   // [nenv][6] lo.xyz, hi.xyz, outward-rounded plus margin
     BvhNode* env_nodes = nullptr;
     int nenv = 0, nenv_nodes = 0;
     // robot (robot frame), triangles in leaf order
@@ -60,6 +61,7 @@ struct MeshData {
     size_t sample_cap = 0;
     int* counts = nullptr;
     int* offs = nullptr;
+    uint8_t* okb = nullptr;
     size_t edge_cap = 0;
     int* hbuf = nullptr;  // pinned
 };
@@ -248,6 +250,7 @@ __device__ __forceinline__ bool box_overlap(const float* lo, const float* hi, co
 
 struct MeshView {
     const double* env_tris;
+    const float* env_boxes;
     const BvhNode* env_nodes;
     const double* robot_tris;
     const BvhNode* robot_leaves;
@@ -329,6 +332,28 @@ __global__ void __launch_bounds__(256) k_mesh_detail(MeshView m, const double* _
             lo[r] = cw - hw - mg;
             hi[r] = cw + hw + mg;
         }
+        // world AABBs of this leaf's robot triangles (FP32 transform, grown by a
+        // margin covering the FP32 rotation and rounding): pair prefilter
+        const int rcount = -rl.b;
+        float tb[MESH_LEAF][6];
+        for (int rt = 0; rt < rcount; ++rt) {
+            const double* lt = m.robot_tris + 9 * (size_t)(rl.a + rt);
+            for (int d = 0; d < 3; ++d) { tb[rt][d] = INFINITY; tb[rt][3 + d] = -INFINITY; }
+            for (int vtx = 0; vtx < 3; ++vtx) {
+                float v0 = (float)lt[3 * vtx], v1 = (float)lt[3 * vtx + 1], v2 = (float)lt[3 * vtx + 2];
+                for (int r = 0; r < 3; ++r) {
+                    float w = fmaf((float)R[3 * r], v0, fmaf((float)R[3 * r + 1], v1, fmaf((float)R[3 * r + 2], v2,
+                                                                                           (float)P[r])));
+                    tb[rt][r] = fminf(tb[rt][r], w);
+                    tb[rt][3 + r] = fmaxf(tb[rt][3 + r], w);
+                }
+            }
+            for (int d = 0; d < 3; ++d) {
+                float mg = MESH_MARGIN * (1.f + fabsf(tb[rt][d]) + fabsf(tb[rt][3 + d]));
+                tb[rt][d] -= mg;
+                tb[rt][3 + d] += mg;
+            }
+        }
         int stack[MESH_STACK];
         int sp = 0;
         stack[sp++] = 0;
@@ -340,11 +365,15 @@ __global__ void __launch_bounds__(256) k_mesh_detail(MeshView m, const double* _
                 if (sp + 2 <= MESH_STACK) { stack[sp++] = nd.a; stack[sp++] = nd.b; }
                 continue;
             }
-            // environment leaf: exact tests of its triangles against this robot leaf's
-            int rcount = -rl.b;
+            // environment leaf: exact tests of the pairs whose boxes overlap
             for (int e = nd.a; e < nd.a - nd.b && !hit; ++e) {
+                const float* eb = m.env_boxes + 6 * (size_t)e;
+                float elo[3] = {eb[0], eb[1], eb[2]}, ehi[3] = {eb[3], eb[4], eb[5]};
                 const double* et = m.env_tris + 9 * (size_t)e;
                 for (int rt = 0; rt < rcount; ++rt) {
+                    if (tb[rt][0] > ehi[0] || tb[rt][3] < elo[0] || tb[rt][1] > ehi[1] || tb[rt][4] < elo[1] ||
+                        tb[rt][2] > ehi[2] || tb[rt][5] < elo[2])
+                        continue;
                     const double* lt = m.robot_tris + 9 * (size_t)(rl.a + rt);
                     double wt[9];
                     xform64(R, P, lt, wt);
@@ -360,16 +389,24 @@ __global__ void __launch_bounds__(256) k_mesh_detail(MeshView m, const double* _
 }
 
 // ------------------------------------------------------------------ edges
+// after the end states were checked (okb): the number of interior samples
+// (steps - 1) of every edge whose end state is valid; the edge result starts
+// as the end state's
 __global__ void k_mesh_edge_counts(int metric, int D, double w0, double w1, const double* __restrict__ a,
-                                   const double* __restrict__ b, int n, double inv, int* __restrict__ counts) {
+                                   const double* __restrict__ b, int n, double inv, const uint8_t* __restrict__ okb,
+                                   int* __restrict__ counts, uint8_t* __restrict__ out) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n) return;
-    double m = dist64(metric, D, w0, w1, a + (size_t)e * D, b + (size_t)e * D);
-    double sd = ceil(__dmul_rn(m, inv));
-    int c;
-    if (!(sd >= 0.0) || sd > (double)MPTG_MAX_EDGE_SAMPLES) c = -1;  // invalid edge, no samples
-    else c = sd < 2.0 ? 1 : (int)sd;
+    int c = 0;
+    uint8_t ok = okb[e];
+    if (ok) {
+        double m = dist64(metric, D, w0, w1, a + (size_t)e * D, b + (size_t)e * D);
+        double sd = ceil(__dmul_rn(m, inv));
+        if (!(sd >= 0.0) || sd > (double)MPTG_MAX_EDGE_SAMPLES) ok = 0;  // NaN or absurdly long: invalid
+        else if (sd >= 2.0) c = (int)sd - 1;
+    }
     counts[e] = c;
+    out[e] = ok;
 }
 
 // exclusive scan of counts (negative = 0) over n <= 2^20 edges: 1024 threads,
@@ -403,29 +440,21 @@ __global__ void k_mesh_edge_samples(int metric, int D, const double* __restrict_
                                     double* __restrict__ samples, int* __restrict__ sample_edge) {
     int e = blockIdx.x;
     if (e >= n) return;
-    int c = counts[e];
+    int c = counts[e];  // interior samples i = 1 .. c of steps = c + 1
     if (c <= 0) return;
     const double* A = a + (size_t)e * D;
     const double* B = b + (size_t)e * D;
-    double delta = c >= 2 ? __ddiv_rn(1.0, (double)c) : 0.0;
+    double delta = __ddiv_rn(1.0, (double)(c + 1));
     for (int k = threadIdx.x; k < c; k += blockDim.x) {
         double* o = samples + (size_t)(offs[e] + k) * D;
-        if (k == 0) {
-            for (int d = 0; d < D; ++d) o[d] = B[d];
-        } else {
-            double A2[MPTG_MAX_DIM], B2[MPTG_MAX_DIM], qv[MPTG_MAX_DIM];
-            for (int d = 0; d < D; ++d) { A2[d] = A[d]; B2[d] = B[d]; }
-            interp64(metric, D, A2, B2, __dmul_rn((double)k, delta), qv);
-            for (int d = 0; d < D; ++d) o[d] = qv[d];
-        }
+        double A2[MPTG_MAX_DIM], B2[MPTG_MAX_DIM], qv[MPTG_MAX_DIM];
+        for (int d = 0; d < D; ++d) { A2[d] = A[d]; B2[d] = B[d]; }
+        interp64(metric, D, A2, B2, __dmul_rn((double)(k + 1), delta), qv);
+        for (int d = 0; d < D; ++d) o[d] = qv[d];
         sample_edge[offs[e] + k] = e;
     }
 }
 
-__global__ void k_mesh_edge_init(const int* __restrict__ counts, int n, uint8_t* __restrict__ out) {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < n) out[e] = counts[e] > 0 ? 1 : 0;
-}
 
 __global__ void k_mesh_add_count(unsigned long long* __restrict__ c, unsigned long long v) { *c += v; }
 
@@ -439,7 +468,7 @@ __global__ void k_mesh_edge_reduce(const uint8_t* __restrict__ ok, const int* __
 
 static MeshView mesh_view(const MeshData* md) {
     MeshView v;
-    v.env_tris = md->env_tris; v.env_nodes = md->env_nodes;
+    v.env_tris = md->env_tris; v.env_boxes = md->env_boxes; v.env_nodes = md->env_nodes;
     v.robot_tris = md->robot_tris; v.robot_leaves = md->robot_leaves;
     v.nenv = md->nenv; v.nrleaves = md->nrleaves;
     v.reach = (float)md->robot_radius * (1.f + 1e-5f) + MESH_MARGIN;
@@ -461,6 +490,14 @@ mptg_status mesh_scene_create(mptg_ctx* ctx, const mptg_scene_desc* d, mptg_scen
     std::vector<double> env_sorted(env.size());
     for (size_t i = 0; i < eidx.size(); ++i)
         std::copy(&env[9 * (size_t)eidx[i]], &env[9 * (size_t)eidx[i]] + 9, &env_sorted[9 * i]);
+    std::vector<float> env_boxes(6 * (size_t)d->nenv + 6);
+    for (size_t i = 0; i < (size_t)d->nenv; ++i) {
+        Box b = tri_box(&env_sorted[9 * i]);
+        for (int k = 0; k < 3; ++k) {
+            env_boxes[6 * i + k] = std::nextafter((float)b.lo[k], -INFINITY) - MESH_MARGIN;
+            env_boxes[6 * i + 3 + k] = std::nextafter((float)b.hi[k], INFINITY) + MESH_MARGIN;
+        }
+    }
     // robot tree (only its leaves are used on the device)
     std::vector<double> rob(d->robot_tris, d->robot_tris + 9 * (size_t)d->nrobot);
     std::vector<int> ridx(d->nrobot);
@@ -489,6 +526,7 @@ mptg_status mesh_scene_create(mptg_ctx* ctx, const mptg_scene_desc* d, mptg_scen
         if (e == cudaSuccess && bytes) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
     };
     up((void**)&md->env_tris, env_sorted.data(), env_sorted.size() * sizeof(double));
+    up((void**)&md->env_boxes, env_boxes.data(), env_boxes.size() * sizeof(float));
     up((void**)&md->env_nodes, enodes.data(), enodes.size() * sizeof(BvhNode));
     up((void**)&md->robot_tris, rob_sorted.data(), rob_sorted.size() * sizeof(double));
     up((void**)&md->robot_leaves, rleaves.data(), rleaves.size() * sizeof(BvhNode));
@@ -504,8 +542,8 @@ mptg_status mesh_scene_create(mptg_ctx* ctx, const mptg_scene_desc* d, mptg_scen
 void mesh_scene_free(mptg_scene* s) {
     MeshData* md = s->mesh;
     if (!md) return;
-    void* ptrs[] = {md->env_tris, md->env_nodes, md->robot_tris, md->robot_leaves, md->work, md->nwork,
-                    md->samples, md->sample_edge, md->sample_ok, md->counts, md->offs};
+    void* ptrs[] = {md->env_tris, md->env_boxes, md->env_nodes, md->robot_tris, md->robot_leaves, md->work, md->nwork,
+                    md->samples, md->sample_edge, md->sample_ok, md->counts, md->offs, md->okb};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (md->hbuf) cudaFreeHost(md->hbuf);
@@ -557,22 +595,26 @@ mptg_status mesh_edges_dev(mptg_scene* sc, const double* da, const double* db, i
     if (n <= 0) return MPTG_OK;
     if (resolution != 0) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "rigid mesh edges use the space metric");
     if (n > (1 << 20)) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "at most 2^20 mesh edges per call");
-    size_t cap = md->edge_cap;
+    size_t cap = md->edge_cap, cap2 = md->edge_cap, cap3 = md->edge_cap;
     mptg_status st = grow(ctx, (void**)&md->counts, &cap, (size_t)n + 1, sizeof(int), s);
     if (st) return st;
-    cap = md->edge_cap;
-    st = grow(ctx, (void**)&md->offs, &cap, (size_t)n + 1, sizeof(int), s);
-    if (st) return st;
-    md->edge_cap = cap;
+    if ((st = grow(ctx, (void**)&md->offs, &cap2, (size_t)n + 1, sizeof(int), s))) return st;
+    if ((st = grow(ctx, (void**)&md->okb, &cap3, (size_t)n + 1, 1, s))) return st;
+    md->edge_cap = std::min(cap, std::min(cap2, cap3));
+    // phase A: every edge's end state first (the DMV checks `to` before any
+    // interior sample); only edges whose end state is valid expand further
+    if ((st = mesh_states_dev(sc, db, n, md->okb, s))) return st;
+    if (nsamp) {
+        k_mesh_add_count<<<1, 1, 0, s>>>(nsamp, (unsigned long long)n);
+        MPTG_LAUNCHED(ctx);
+    }
     k_mesh_edge_counts<<<mptg_blocks(n, 128), 128, 0, s>>>(sc->metric, sc->D, sc->w0, sc->w1, da, db, n, 1.0 / step,
-                                                           md->counts);
+                                                           md->okb, md->counts, dout);
     k_mesh_scan<<<1, 1024, 0, s>>>(md->counts, n, md->offs, md->offs + n);
     ctx->launches += 2;
     MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(md->hbuf, md->offs + n, sizeof(int), cudaMemcpyDeviceToHost, s));
     MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     int total = md->hbuf[0];
-    k_mesh_edge_init<<<mptg_blocks(n, 256), 256, 0, s>>>(md->counts, n, dout);
-    MPTG_LAUNCHED(ctx);
     if (total > 0) {
         cap = md->sample_cap;
         size_t cap2 = md->sample_cap, cap3 = md->sample_cap;

@@ -182,10 +182,256 @@ __global__ void __launch_bounds__(256) k_valid_edges(SceneView s, const double* 
     }
 }
 
+// ------------------------------------------------------------------ FP32 filters
+// Each filter returns VF_INVALID or VF_VALID when the FP32 evaluation decides
+// the state with certainty (every FP32 quantity lies farther from its decision
+// boundary than an a-priori bound on its error), else VF_UNSURE, and the
+// caller re-evaluates the state in FP64.
+enum { VF_INVALID = 0, VF_VALID = 1, VF_UNSURE = 2 };
+
+// grid: cell = (int)(x + 0.5) per axis; e bounds |v32 - v64| for v = x + 0.5
+__device__ __forceinline__ int grid_valid32(const SceneView& s, float x, float y, float e) {
+    float vx = x + 0.5f, vy = y + 0.5f;
+    // every decision boundary (integers, -1 and the grid size) must be farther than e
+    float fx = vx - floorf(vx), fy = vy - floorf(vy);
+    if (fx <= e || fx >= 1.f - e || fy <= e || fy >= 1.f - e) return VF_UNSURE;
+    if (!(vx > -1.f && vx < (float)s.width && vy > -1.f && vy < (float)s.height)) return VF_INVALID;
+    int xi = (int)vx, yi = (int)vy;
+    return __ldg(&s.grid[(size_t)s.width * yi + xi]) == 0 ? VF_VALID : VF_INVALID;
+}
+
+__device__ __forceinline__ float dpseg2_32(float px, float py, float ax, float ay, float bx, float by) {
+    float vx = bx - ax, vy = by - ay, wx = px - ax, wy = py - ay;
+    float c1 = vx * wx + vy * wy;
+    if (c1 <= 0.f) return wx * wx + wy * wy;
+    float c2 = vx * vx + vy * vy;
+    if (c2 <= c1) { float ex = px - bx, ey = py - by; return ex * ex + ey * ey; }
+    float f = c1 / c2;
+    float ex = ax - px + vx * f, ey = ay - py + vy * f;
+    return ex * ex + ey * ey;
+}
+
+// planar arm from FP32 joint angles q (each within ea of the exact angle).
+// Positions: the cumulative angle is kept in [-pi, pi] and sincosf is within
+// a few ulp, so every joint position is within
+//   delta = reach * (nlinks * (ea + 16u*pi) + 16u*nlinks)
+// of the FP64 forward kinematics (factor 2 of slack included).
+__device__ int arm_valid32(const SceneView& s, const float* q, float ea) {
+    const int nl = s.nlinks;
+    const float R = s.arm_reach;
+    const float delta = 2.f * R * ((float)nl * (ea + 16.f * U32 * PI_F) + 16.f * U32 * (float)nl) + 1e-30f;
+    float x[MPTG_MAX_DIM + 1], y[MPTG_MAX_DIM + 1];
+    float ang = 0.f;
+    x[0] = 0.f; y[0] = 0.f;
+    bool unsure = false;
+    for (int i = 0; i < nl; ++i) {
+        ang += q[i];
+        if (ang > PI_F) ang -= TWO_PI_F;
+        else if (ang < -PI_F) ang += TWO_PI_F;
+        float sn, cs;
+        sincosf(ang, &sn, &cs);
+        float L = __ldg(&s.link32[i]);
+        x[i + 1] = fmaf(L, cs, x[i]);
+        y[i + 1] = fmaf(L, sn, y[i]);
+        for (int k = 0; k < s.ndiscs; ++k) {
+            float4 d = __ldg(&s.discs32[k]);
+            float d2 = dpseg2_32(d.x, d.y, x[i], y[i], x[i + 1], y[i + 1]);
+            float m = 3.f * sqrtf(fmaxf(d2, d.z)) * delta + delta * delta + 8.f * U32 * (d2 + d.z);
+            if (d2 <= d.z - m) return VF_INVALID;
+            if (!(d2 > d.z + m)) unsure = true;
+        }
+    }
+    if (s.self_collision) {
+        // each coordinate within delta: each product of two differences moves by
+        // <= 8 R delta + 4 delta^2, two products, plus FP32 rounding on |.| <= 4R^2
+        const float mo = 16.f * delta * R + 8.f * delta * delta + 32.f * U32 * R * R + 1e-30f;
+        for (int i = 0; i < nl; ++i)
+            for (int j = i + 2; j < nl; ++j) {
+                float ax = x[i], ay = y[i], bx = x[i + 1], by = y[i + 1];
+                float cx = x[j], cy = y[j], dx = x[j + 1], dy = y[j + 1];
+                float o1 = (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
+                float o2 = (bx - ax) * (dy - ay) - (by - ay) * (dx - ax);
+                float o3 = (dx - cx) * (ay - cy) - (dy - cy) * (ax - cx);
+                float o4 = (dx - cx) * (by - cy) - (dy - cy) * (bx - cx);
+                if (fabsf(o1) <= mo || fabsf(o2) <= mo || fabsf(o3) <= mo || fabsf(o4) <= mo) {
+                    unsure = true;
+                    continue;
+                }
+                if ((o1 > 0) != (o2 > 0) && (o3 > 0) != (o4 > 0)) return VF_INVALID;
+            }
+    }
+    return unsure ? VF_UNSURE : VF_VALID;
+}
+
+// exact decision for a state given in FP64 (FP32 filter first)
+__device__ __forceinline__ bool state_valid_f(const SceneView& s, const double* q) {
+    int r;
+    if (s.kind == MPTG_SCENE_GRID) {
+        float x = __double2float_rn(q[0]), y = __double2float_rn(q[1]);
+        float e = 4.f * U32 * (fabsf(x) + fabsf(y) + 1.f);
+        r = (x == x && y == y && fabsf(x) < 1e7f && fabsf(y) < 1e7f) ? grid_valid32(s, x, y, e) : VF_UNSURE;
+    } else {
+        float qf[MPTG_MAX_DIM];
+        float mx = 0.f;
+        bool fin = true;
+        for (int d = 0; d < s.nlinks; ++d) {
+            qf[d] = __double2float_rn(q[d]);
+            mx = fmaxf(mx, fabsf(qf[d]));
+            fin = fin && (qf[d] == qf[d]) && fabsf(qf[d]) < 1e4f;
+        }
+        r = fin ? arm_valid32(s, qf, 2.f * U32 * mx + U32 * PI_F) : VF_UNSURE;
+    }
+    if (r != VF_UNSURE) return r == VF_VALID;
+    return state_valid64(s, q);
+}
+
+__global__ void __launch_bounds__(256) k_states_f(SceneView s, const double* __restrict__ q, int n,
+                                                  uint8_t* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double st[MPTG_MAX_DIM];
+    for (int d = 0; d < s.D; ++d) st[d] = q[(size_t)i * s.D + d];
+    out[i] = state_valid_f(s, st) ? 1 : 0;
+}
+
+// step count ceil(m(a, b) * inv) with an FP32 filter: FP64 only when the
+// FP32 value lies within its error bound of an integer
+__device__ __forceinline__ long long edge_steps(const SceneView& s, const double* A, const double* B, double inv,
+                                                int resolution) {
+    const int D = s.D;
+    float m32 = 0.f, err = 0.f;
+    bool fast = true;
+    if (resolution == 1) {
+        for (int i = 0; i < D; ++i) {
+            float ai = __double2float_rn(A[i]), bi = __double2float_rn(B[i]);
+            // the FP32 form assumes angles in [-pi, pi] (no fmod reduction)
+            if (!(fabsf(ai) <= PI_F && fabsf(bi) <= PI_F)) fast = false;
+            float d = fabsf(ai - bi);
+            d = fminf(d, TWO_PI_F - d);
+            m32 = fmaxf(m32, d);
+        }
+        err = 16.f * U32 * PI_F;
+    } else if (s.metric == MPTG_METRIC_L2 && D == 2) {
+        float dx = __double2float_rn(A[0]) - __double2float_rn(B[0]);
+        float dy = __double2float_rn(A[1]) - __double2float_rn(B[1]);
+        m32 = sqrtf(dx * dx + dy * dy);
+        float M = fmaxf(fmaxf(fabsf((float)A[0]), fabsf((float)A[1])), fmaxf(fabsf((float)B[0]), fabsf((float)B[1])));
+        err = 16.f * U32 * (M + m32) + 1e-30f;
+    } else {
+        fast = false;
+    }
+    if (fast && m32 == m32) {
+        float x = m32 * (float)inv;
+        float e = err * (float)inv + 4.f * U32 * x;
+        float lo = ceilf(x - e), hi = ceilf(x + e);
+        if (lo == hi && x < 1e7f) return (long long)lo;
+    }
+    double m = resolution == 1 ? linf_so2_64(A, B, D) : dist64(s.metric, D, s.w0, s.w1, A, B);
+    double sd = ceil(__dmul_rn(m, inv));
+    if (!(sd >= 0.0) || sd > (double)MPTG_MAX_EDGE_SAMPLES) return -1;
+    return (long long)sd;
+}
+
+// phase A, thread per edge: the end state (checked first, as the DMV does),
+// then the step count; edges with interior samples go to the work list
+__global__ void __launch_bounds__(256) k_edges_a(SceneView s, const double* __restrict__ a,
+                                                 const double* __restrict__ b, int n, double inv, int resolution,
+                                                 uint8_t* __restrict__ out, int* __restrict__ work,
+                                                 int* __restrict__ wsteps, int* __restrict__ wcount,
+                                                 unsigned long long* __restrict__ nsamp) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const int D = s.D;
+    double A[MPTG_MAX_DIM], B[MPTG_MAX_DIM];
+    for (int d = 0; d < D; ++d) { A[d] = a[(size_t)e * D + d]; B[d] = b[(size_t)e * D + d]; }
+    if (nsamp) atomicAdd(nsamp, 1ull);
+    if (!state_valid_f(s, B)) { out[e] = 0; return; }
+    long long steps = edge_steps(s, A, B, inv, resolution);
+    if (steps < 0) { out[e] = 0; return; }
+    out[e] = 1;
+    if (steps >= 2) {
+        int k = atomicAdd(wcount, 1);
+        work[k] = e;
+        wsteps[k] = (int)steps;
+    }
+}
+
+// phase B, warp per surviving edge: interior samples i*delta, 1 <= i < steps,
+// coarse-to-fine (lane j of round r takes sample 1 + j*R + r), FP32 filter
+// per sample with the exact FP64 sample as fallback; ballot early exit
+__global__ void __launch_bounds__(256) k_edges_b(SceneView s, const double* __restrict__ a,
+                                                 const double* __restrict__ b, const int* __restrict__ work,
+                                                 const int* __restrict__ wsteps, const int* __restrict__ wcount,
+                                                 uint8_t* __restrict__ out, unsigned long long* __restrict__ nsamp) {
+    const int lane = threadIdx.x & 31;
+    const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    if (w >= *wcount) return;
+    const int e = work[w];
+    const int steps = wsteps[w];
+    const int D = s.D;
+    double A[MPTG_MAX_DIM], B[MPTG_MAX_DIM];
+    float a32[MPTG_MAX_DIM], dir32[MPTG_MAX_DIM];
+    for (int d = 0; d < D; ++d) {
+        A[d] = a[(size_t)e * D + d];
+        B[d] = b[(size_t)e * D + d];
+        a32[d] = __double2float_rn(A[d]);
+        if (s.metric == MPTG_METRIC_SO2) {
+            // signed shortest-arc offset of interpolate (src/mpt/so2_space.hpp:44-65);
+            // the wrap of the result is irrelevant to forward kinematics
+            double ccw = so2_ccw64(A[d], B[d]);
+            dir32[d] = __double2float_rn(ccw < MPTG_PI ? ccw : -__dsub_rn(MPTG_TWO_PI, ccw));
+        } else {
+            dir32[d] = __double2float_rn(__dsub_rn(B[d], A[d]));
+        }
+    }
+    const int M = steps - 1;
+    const int R = (M + 31) / 32;
+    const double delta = __ddiv_rn(1.0, (double)steps);
+    bool ok = true;
+    unsigned long long cnt = 0;
+    for (int r = 0; ok && r < R; ++r) {
+        int k = 1 + lane * R + r;
+        bool v = true;
+        if (k <= M) {
+            ++cnt;
+            float t = (float)k / (float)steps;
+            int res;
+            if (s.kind == MPTG_SCENE_GRID) {
+                float x = fmaf(dir32[0], t, a32[0]), y = fmaf(dir32[1], t, a32[1]);
+                float e = 8.f * U32 * (fabsf(a32[0]) + fabsf(a32[1]) + fabsf(dir32[0]) + fabsf(dir32[1]) + 1.f);
+                res = grid_valid32(s, x, y, e);
+            } else {
+                float q[MPTG_MAX_DIM];
+                float ea = 0.f;
+                for (int d = 0; d < D; ++d) {
+                    q[d] = fmaf(dir32[d], t, a32[d]);
+                    ea = fmaxf(ea, 8.f * U32 * (fabsf(a32[d]) + 2.f * fabsf(dir32[d])));
+                }
+                res = arm_valid32(s, q, ea + 2.f * U32 * PI_F);
+            }
+            if (res == VF_UNSURE) {
+                double qs[MPTG_MAX_DIM];
+                interp64(s.metric, D, A, B, __dmul_rn((double)k, delta), qs);
+                v = state_valid64(s, qs);
+            } else {
+                v = res == VF_VALID;
+            }
+        }
+        if (__any_sync(0xffffffffu, !v)) ok = false;
+    }
+    if (nsamp) {
+        for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    }
+    if (lane == 0) {
+        if (!ok) out[e] = 0;
+        if (nsamp) atomicAdd(nsamp, cnt);
+    }
+}
+
 // ------------------------------------------------------------------ host
 
 static void scene_free(mptg_scene* s) {
-    void* ptrs[] = {s->grid, s->link_len64, s->discs64};
+    void* ptrs[] = {s->grid, s->link_len64, s->discs64, s->discs32, s->link32, s->work, s->wsteps, s->wcount};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     mesh_scene_free(s);
@@ -199,8 +445,43 @@ SceneView scene_view(const mptg_scene* s) {
     v.grid = s->grid; v.width = s->width; v.height = s->height;
     v.nlinks = s->nlinks; v.link_len64 = s->link_len64; v.ndiscs = s->ndiscs; v.discs64 = s->discs64;
     v.robot_radius = s->robot_radius; v.self_collision = s->self_collision;
+    v.discs32 = s->discs32; v.link32 = s->link32; v.arm_reach = s->arm_reach;
     mesh_fill_view(s, &v);
     return v;
+}
+
+// FP32 copies for the filters: discs as (cx, cy, (r + robot_radius)^2) with
+// the square taken in FP64 as the exact test does
+static cudaError_t scene_make_f32(mptg_scene* s, const mptg_scene_desc* d) {
+    std::vector<float4> dc(d->ndiscs > 0 ? d->ndiscs : 1);
+    for (int k = 0; k < d->ndiscs; ++k) {
+        double r = d->discs[3 * k + 2] + d->robot_radius;
+        dc[k] = make_float4((float)d->discs[3 * k], (float)d->discs[3 * k + 1], (float)(r * r), 0.f);
+    }
+    std::vector<float> ll(d->nlinks);
+    double reach = 0;
+    for (int i = 0; i < d->nlinks; ++i) { ll[i] = (float)d->link_len[i]; reach += fabs(d->link_len[i]); }
+    s->arm_reach = (float)(reach * (1.0 + 1e-6)) + 1e-6f;
+    cudaError_t e = cudaMalloc((void**)&s->discs32, dc.size() * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMemcpy(s->discs32, dc.data(), dc.size() * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&s->link32, ll.size() * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(s->link32, ll.data(), ll.size() * sizeof(float), cudaMemcpyHostToDevice);
+    return e;
+}
+
+static mptg_status scene_reserve(mptg_scene* sc, size_t n, cudaStream_t s) {
+    if (!sc->wcount) MPTG_CUDA_TRY(sc->ctx, cudaMalloc((void**)&sc->wcount, sizeof(int)));
+    if (n <= sc->work_cap) return MPTG_OK;
+    MPTG_CUDA_TRY(sc->ctx, cudaStreamSynchronize(s));
+    cudaFree(sc->work);
+    cudaFree(sc->wsteps);
+    sc->work = sc->wsteps = nullptr;
+    sc->work_cap = 0;
+    size_t cap = n + n / 2 + 1024;
+    MPTG_CUDA_TRY(sc->ctx, cudaMalloc((void**)&sc->work, cap * sizeof(int)));
+    MPTG_CUDA_TRY(sc->ctx, cudaMalloc((void**)&sc->wsteps, cap * sizeof(int)));
+    sc->work_cap = cap;
+    return MPTG_OK;
 }
 
 mptg_status scene_edges_dev(mptg_scene* sc, const double* da, const double* db, int n, double step, int resolution,
@@ -208,9 +489,16 @@ mptg_status scene_edges_dev(mptg_scene* sc, const double* da, const double* db, 
     if (n <= 0) return MPTG_OK;
     if (sc->kind == MPTG_SCENE_RIGID_MESH)
         return mesh_edges_dev(sc, da, db, n, step, resolution, dout, s, nsamp);
+    mptg_status st = scene_reserve(sc, (size_t)n, s);
+    if (st) return st;
     SceneView v = scene_view(sc);
-    k_valid_edges<<<mptg_blocks((size_t)n * 32, 256), 256, 0, s>>>(v, da, db, n, 1.0 / step, resolution, dout, nsamp);
-    MPTG_LAUNCHED(sc->ctx);
+    MPTG_CUDA_TRY(sc->ctx, cudaMemsetAsync(sc->wcount, 0, sizeof(int), s));
+    k_edges_a<<<mptg_blocks(n, 128), 128, 0, s>>>(v, da, db, n, 1.0 / step, resolution, dout, sc->work, sc->wsteps,
+                                                  sc->wcount, nsamp);
+    // one warp per edge that survived phase A (surplus warps exit at once)
+    k_edges_b<<<mptg_blocks((size_t)n * 32, 256), 256, 0, s>>>(v, da, db, sc->work, sc->wsteps, sc->wcount, dout,
+                                                               nsamp);
+    sc->ctx->launches += 2;
     return MPTG_OK;
 }
 
@@ -218,7 +506,7 @@ mptg_status scene_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* d
     if (n <= 0) return MPTG_OK;
     if (sc->kind == MPTG_SCENE_RIGID_MESH) return mesh_states_dev(sc, dq, n, dout, s);
     SceneView v = scene_view(sc);
-    k_valid_states<<<mptg_blocks(n, 256), 256, 0, s>>>(v, dq, n, dout);
+    k_states_f<<<mptg_blocks(n, 256), 256, 0, s>>>(v, dq, n, dout);
     MPTG_LAUNCHED(sc->ctx);
     return MPTG_OK;
 }
@@ -259,6 +547,7 @@ mptg_status mptg_scene_create(mptg_ctx* ctx, const mptg_scene_desc* d, mptg_scen
         if (e == cudaSuccess) e = cudaMalloc((void**)&s->discs64, (d->ndiscs * 3 + 1) * sizeof(double));
         if (e == cudaSuccess && d->ndiscs)
             e = cudaMemcpy(s->discs64, d->discs, d->ndiscs * 3 * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = scene_make_f32(s, d);
         break;
     }
     case MPTG_SCENE_RIGID_MESH: {

@@ -18,6 +18,15 @@ struct mptg_scene {
     double* discs64 = nullptr;
     // rigid mesh
     MeshData* mesh = nullptr;
+    // FP32 filter data: discs (cx, cy, (r + robot_radius)^2, unused), link lengths
+    float4* discs32 = nullptr;
+    float* link32 = nullptr;
+    float arm_reach = 0.f;
+    // two-phase edge scratch: surviving edges and their step counts
+    int* work = nullptr;
+    int* wsteps = nullptr;
+    int* wcount = nullptr;
+    size_t work_cap = 0;
 };
 
 // POD view passed to kernels by value
@@ -30,6 +39,9 @@ struct SceneView {
     double robot_radius;
     const double* link_len64;
     const double* discs64;
+    const float4* discs32;
+    const float* link32;
+    float arm_reach;
     // rigid mesh (see mesh.cu)
     const double* robot_tris;   // [nrobot][9]
     int nrobot;

@@ -44,6 +44,34 @@ def test_edges_match_oracle(ctx, orc, mk):
     assert 0.01 < want.mean() < 0.99
 
 
+def test_arm_states_on_the_collision_boundary(ctx, orc):
+    """States bisected to within ~1e-10 rad of the collision boundary: the FP32
+    filter must defer them to FP64, and the answers must equal the oracle's."""
+    sc = scenes.arm_scene()
+    sp = orc.make_space(1, 10)
+    rng = np.random.default_rng(5)
+    q = scenes.uniform_states(sc, 4000, 601)
+    v = orc.valid_states(sc, sp, q)
+    good, bad = q[v == 1][:150], q[v == 0][:150]
+    lo, hi = good.copy(), bad.copy()  # lo valid, hi invalid
+    for _ in range(34):
+        mid = lo + 0.5 * (hi - lo)
+        mv = orc.valid_states(sc, sp, mid).astype(bool)
+        lo[mv] = mid[mv]
+        hi[~mv] = mid[~mv]
+    pts = np.concatenate([lo, hi, lo + 1e-12 * rng.normal(size=lo.shape), hi + 1e-12 * rng.normal(size=hi.shape)])
+    pts = np.clip(pts, -np.pi, np.pi)
+    g = _scene(ctx, sc)
+    want = orc.valid_states(sc, sp, pts)
+    got = g.valid(pts)
+    assert np.array_equal(got, want), np.nonzero(got != want)[0][:10]
+    # edges ending on the boundary take the same exact path
+    a = np.repeat(good[:1], len(pts), axis=0)
+    wante, _ = orc.valid_edges(sc, sp, a, pts, 0.01, 1)
+    gote = g.link(a, pts, 0.01, 1)
+    assert np.array_equal(gote, wante)
+
+
 def _near_contact_states(sc, n, seed):
     """SE(3) states whose robot sits within about one bounding radius of a box face."""
     rng = np.random.default_rng(seed)
