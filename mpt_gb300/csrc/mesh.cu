@@ -51,19 +51,6 @@ struct MeshData {
     BvhNode* robot_leaves = nullptr;  // robot leaves only (AABBs in the robot frame)
     int nrobot = 0, nrleaves = 0;
     double robot_radius = 0.0;     // max |vertex| in the robot frame
-    // batch scratch (grown on demand)
-    int* work = nullptr;
-    int* nwork = nullptr;
-    size_t work_cap = 0;
-    double* samples = nullptr;
-    int* sample_edge = nullptr;
-    uint8_t* sample_ok = nullptr;
-    size_t sample_cap = 0;
-    int* counts = nullptr;
-    int* offs = nullptr;
-    uint8_t* okb = nullptr;
-    size_t edge_cap = 0;
-    int* hbuf = nullptr;  // pinned
 };
 
 // ------------------------------------------------------------------ host BVH build
@@ -530,8 +517,6 @@ mptg_status mesh_scene_create(mptg_ctx* ctx, const mptg_scene_desc* d, mptg_scen
     up((void**)&md->env_nodes, enodes.data(), enodes.size() * sizeof(BvhNode));
     up((void**)&md->robot_tris, rob_sorted.data(), rob_sorted.size() * sizeof(double));
     up((void**)&md->robot_leaves, rleaves.data(), rleaves.size() * sizeof(BvhNode));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&md->nwork, sizeof(int));
-    if (e == cudaSuccess) e = cudaMallocHost((void**)&md->hbuf, 4 * sizeof(int));
     if (e != cudaSuccess) {
         cudaGetLastError();
         return mptg_fail(ctx, MPTG_ERR_OOM, "mesh scene allocation failed: %s", cudaGetErrorString(e));
@@ -542,11 +527,9 @@ mptg_status mesh_scene_create(mptg_ctx* ctx, const mptg_scene_desc* d, mptg_scen
 void mesh_scene_free(mptg_scene* s) {
     MeshData* md = s->mesh;
     if (!md) return;
-    void* ptrs[] = {md->env_tris, md->env_boxes, md->env_nodes, md->robot_tris, md->robot_leaves, md->work, md->nwork,
-                    md->samples, md->sample_edge, md->sample_ok, md->counts, md->offs, md->okb};
+    void* ptrs[] = {md->env_tris, md->env_boxes, md->env_nodes, md->robot_tris, md->robot_leaves};
     for (void* p : ptrs)
         if (p) cudaFree(p);
-    if (md->hbuf) cudaFreeHost(md->hbuf);
     delete md;
     s->mesh = nullptr;
 }
@@ -564,24 +547,31 @@ static mptg_status grow(mptg_ctx* ctx, void** p, size_t* cap, size_t need, size_
     return MPTG_OK;
 }
 
-mptg_status mesh_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* dout, cudaStream_t s) {
+static mptg_status mesh_scratch_init(mptg_ctx* ctx, EdgeScratch* x) {
+    if (!x->nwork) MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&x->nwork, sizeof(int)));
+    if (!x->hbuf) MPTG_CUDA_TRY(ctx, cudaMallocHost((void**)&x->hbuf, 4 * sizeof(int)));
+    return MPTG_OK;
+}
+
+mptg_status mesh_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* dout, cudaStream_t s, EdgeScratch* x) {
     mptg_ctx* ctx = sc->ctx;
     MeshData* md = sc->mesh;
     if (n <= 0) return MPTG_OK;
-    size_t cap = md->work_cap;
-    mptg_status st = grow(ctx, (void**)&md->work, &cap, (size_t)n, sizeof(int), s);
+    mptg_status st = mesh_scratch_init(ctx, x);
     if (st) return st;
-    md->work_cap = cap;
+    size_t cap = x->mwork_cap;
+    if ((st = grow(ctx, (void**)&x->mwork, &cap, (size_t)n, sizeof(int), s))) return st;
+    x->mwork_cap = cap;
     MeshView v = mesh_view(md);
-    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(md->nwork, 0, sizeof(int), s));
-    k_mesh_sphere<<<mptg_blocks(n, 128), 128, 0, s>>>(v, dq, n, sc->D, dout, md->work, md->nwork);
+    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(x->nwork, 0, sizeof(int), s));
+    k_mesh_sphere<<<mptg_blocks(n, 128), 128, 0, s>>>(v, dq, n, sc->D, dout, x->mwork, x->nwork);
     MPTG_LAUNCHED(ctx);
-    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(md->hbuf, md->nwork, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(x->hbuf, x->nwork, sizeof(int), cudaMemcpyDeviceToHost, s));
     MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
-    int nw = md->hbuf[0];
+    int nw = x->hbuf[0];
     if (nw > 0) {
         // one block per state that the sphere test could not clear
-        k_mesh_detail<<<nw, 256, 0, s>>>(v, dq, sc->D, md->work, md->nwork, dout);
+        k_mesh_detail<<<nw, 256, 0, s>>>(v, dq, sc->D, x->mwork, x->nwork, dout);
         MPTG_LAUNCHED(ctx);
     }
     MPTG_CUDA_TRY(ctx, cudaGetLastError());
@@ -589,45 +579,46 @@ mptg_status mesh_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* do
 }
 
 mptg_status mesh_edges_dev(mptg_scene* sc, const double* da, const double* db, int n, double step, int resolution,
-                           uint8_t* dout, cudaStream_t s, unsigned long long* nsamp) {
+                           uint8_t* dout, cudaStream_t s, unsigned long long* nsamp, EdgeScratch* x) {
     mptg_ctx* ctx = sc->ctx;
-    MeshData* md = sc->mesh;
     if (n <= 0) return MPTG_OK;
     if (resolution != 0) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "rigid mesh edges use the space metric");
     if (n > (1 << 20)) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "at most 2^20 mesh edges per call");
-    size_t cap = md->edge_cap, cap2 = md->edge_cap, cap3 = md->edge_cap;
-    mptg_status st = grow(ctx, (void**)&md->counts, &cap, (size_t)n + 1, sizeof(int), s);
+    mptg_status st = mesh_scratch_init(ctx, x);
     if (st) return st;
-    if ((st = grow(ctx, (void**)&md->offs, &cap2, (size_t)n + 1, sizeof(int), s))) return st;
-    if ((st = grow(ctx, (void**)&md->okb, &cap3, (size_t)n + 1, 1, s))) return st;
-    md->edge_cap = std::min(cap, std::min(cap2, cap3));
+    size_t cap = x->edge_cap, cap2 = x->edge_cap, cap3 = x->edge_cap;
+    if ((st = grow(ctx, (void**)&x->counts, &cap, (size_t)n + 1, sizeof(int), s))) return st;
+    if ((st = grow(ctx, (void**)&x->offs, &cap2, (size_t)n + 1, sizeof(int), s))) return st;
+    if ((st = grow(ctx, (void**)&x->okb, &cap3, (size_t)n + 1, 1, s))) return st;
+    x->edge_cap = std::min(cap, std::min(cap2, cap3));
     // phase A: every edge's end state first (the DMV checks `to` before any
     // interior sample); only edges whose end state is valid expand further
-    if ((st = mesh_states_dev(sc, db, n, md->okb, s))) return st;
+    if ((st = mesh_states_dev(sc, db, n, x->okb, s, x))) return st;
     if (nsamp) {
         k_mesh_add_count<<<1, 1, 0, s>>>(nsamp, (unsigned long long)n);
         MPTG_LAUNCHED(ctx);
     }
     k_mesh_edge_counts<<<mptg_blocks(n, 128), 128, 0, s>>>(sc->metric, sc->D, sc->w0, sc->w1, da, db, n, 1.0 / step,
-                                                           md->okb, md->counts, dout);
-    k_mesh_scan<<<1, 1024, 0, s>>>(md->counts, n, md->offs, md->offs + n);
+                                                           x->okb, x->counts, dout);
+    k_mesh_scan<<<1, 1024, 0, s>>>(x->counts, n, x->offs, x->offs + n);
     ctx->launches += 2;
-    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(md->hbuf, md->offs + n, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(x->hbuf + 1, x->offs + n, sizeof(int), cudaMemcpyDeviceToHost, s));
     MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
-    int total = md->hbuf[0];
+    int total = x->hbuf[1];
     if (total > 0) {
-        cap = md->sample_cap;
-        size_t cap2 = md->sample_cap, cap3 = md->sample_cap;
-        if ((st = grow(ctx, (void**)&md->samples, &cap, (size_t)total, sc->D * sizeof(double), s))) return st;
-        if ((st = grow(ctx, (void**)&md->sample_edge, &cap2, (size_t)total, sizeof(int), s))) return st;
-        if ((st = grow(ctx, (void**)&md->sample_ok, &cap3, (size_t)total, 1, s))) return st;
-        md->sample_cap = std::min(cap, std::min(cap2, cap3));
-        k_mesh_edge_samples<<<n, 64, 0, s>>>(sc->metric, sc->D, da, db, n, md->counts, md->offs, md->samples,
-                                             md->sample_edge);
+        cap = x->sample_cap;
+        cap2 = x->sample_cap;
+        cap3 = x->sample_cap;
+        if ((st = grow(ctx, (void**)&x->samples, &cap, (size_t)total, sc->D * sizeof(double), s))) return st;
+        if ((st = grow(ctx, (void**)&x->sample_edge, &cap2, (size_t)total, sizeof(int), s))) return st;
+        if ((st = grow(ctx, (void**)&x->sample_ok, &cap3, (size_t)total, 1, s))) return st;
+        x->sample_cap = std::min(cap, std::min(cap2, cap3));
+        k_mesh_edge_samples<<<n, 64, 0, s>>>(sc->metric, sc->D, da, db, n, x->counts, x->offs, x->samples,
+                                             x->sample_edge);
         MPTG_LAUNCHED(ctx);
-        st = mesh_states_dev(sc, md->samples, total, md->sample_ok, s);
+        st = mesh_states_dev(sc, x->samples, total, x->sample_ok, s, x);
         if (st) return st;
-        k_mesh_edge_reduce<<<mptg_blocks(total, 256), 256, 0, s>>>(md->sample_ok, md->sample_edge, total, dout);
+        k_mesh_edge_reduce<<<mptg_blocks(total, 256), 256, 0, s>>>(x->sample_ok, x->sample_edge, total, dout);
         MPTG_LAUNCHED(ctx);
         if (nsamp) {
             k_mesh_add_count<<<1, 1, 0, s>>>(nsamp, (unsigned long long)total);

@@ -430,10 +430,20 @@ __global__ void __launch_bounds__(256) k_edges_b(SceneView s, const double* __re
 
 // ------------------------------------------------------------------ host
 
-static void scene_free(mptg_scene* s) {
-    void* ptrs[] = {s->grid, s->link_len64, s->discs64, s->discs32, s->link32, s->work, s->wsteps, s->wcount};
+void scratch_free(EdgeScratch* s) {
+    void* ptrs[] = {s->work, s->wsteps, s->wcount, s->mwork, s->nwork, s->samples, s->sample_edge, s->sample_ok,
+                    s->counts, s->offs, s->okb};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (s->hbuf) cudaFreeHost(s->hbuf);
+    *s = EdgeScratch();
+}
+
+static void scene_free(mptg_scene* s) {
+    void* ptrs[] = {s->grid, s->link_len64, s->discs64, s->discs32, s->link32};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    scratch_free(&s->scratch);
     mesh_scene_free(s);
     delete s;
 }
@@ -469,42 +479,43 @@ static cudaError_t scene_make_f32(mptg_scene* s, const mptg_scene_desc* d) {
     return e;
 }
 
-static mptg_status scene_reserve(mptg_scene* sc, size_t n, cudaStream_t s) {
-    if (!sc->wcount) MPTG_CUDA_TRY(sc->ctx, cudaMalloc((void**)&sc->wcount, sizeof(int)));
-    if (n <= sc->work_cap) return MPTG_OK;
-    MPTG_CUDA_TRY(sc->ctx, cudaStreamSynchronize(s));
-    cudaFree(sc->work);
-    cudaFree(sc->wsteps);
-    sc->work = sc->wsteps = nullptr;
-    sc->work_cap = 0;
+static mptg_status scene_reserve(mptg_ctx* ctx, EdgeScratch* x, size_t n, cudaStream_t s) {
+    if (!x->wcount) MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&x->wcount, sizeof(int)));
+    if (n <= x->work_cap) return MPTG_OK;
+    MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    cudaFree(x->work);
+    cudaFree(x->wsteps);
+    x->work = x->wsteps = nullptr;
+    x->work_cap = 0;
     size_t cap = n + n / 2 + 1024;
-    MPTG_CUDA_TRY(sc->ctx, cudaMalloc((void**)&sc->work, cap * sizeof(int)));
-    MPTG_CUDA_TRY(sc->ctx, cudaMalloc((void**)&sc->wsteps, cap * sizeof(int)));
-    sc->work_cap = cap;
+    MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&x->work, cap * sizeof(int)));
+    MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&x->wsteps, cap * sizeof(int)));
+    x->work_cap = cap;
     return MPTG_OK;
 }
 
 mptg_status scene_edges_dev(mptg_scene* sc, const double* da, const double* db, int n, double step, int resolution,
-                            uint8_t* dout, cudaStream_t s, unsigned long long* nsamp) {
+                            uint8_t* dout, cudaStream_t s, unsigned long long* nsamp, EdgeScratch* scr) {
     if (n <= 0) return MPTG_OK;
+    EdgeScratch* x = scr ? scr : &sc->scratch;
     if (sc->kind == MPTG_SCENE_RIGID_MESH)
-        return mesh_edges_dev(sc, da, db, n, step, resolution, dout, s, nsamp);
-    mptg_status st = scene_reserve(sc, (size_t)n, s);
+        return mesh_edges_dev(sc, da, db, n, step, resolution, dout, s, nsamp, x);
+    mptg_status st = scene_reserve(sc->ctx, x, (size_t)n, s);
     if (st) return st;
     SceneView v = scene_view(sc);
-    MPTG_CUDA_TRY(sc->ctx, cudaMemsetAsync(sc->wcount, 0, sizeof(int), s));
-    k_edges_a<<<mptg_blocks(n, 128), 128, 0, s>>>(v, da, db, n, 1.0 / step, resolution, dout, sc->work, sc->wsteps,
-                                                  sc->wcount, nsamp);
+    MPTG_CUDA_TRY(sc->ctx, cudaMemsetAsync(x->wcount, 0, sizeof(int), s));
+    k_edges_a<<<mptg_blocks(n, 128), 128, 0, s>>>(v, da, db, n, 1.0 / step, resolution, dout, x->work, x->wsteps,
+                                                  x->wcount, nsamp);
     // one warp per edge that survived phase A (surplus warps exit at once)
-    k_edges_b<<<mptg_blocks((size_t)n * 32, 256), 256, 0, s>>>(v, da, db, sc->work, sc->wsteps, sc->wcount, dout,
-                                                               nsamp);
+    k_edges_b<<<mptg_blocks((size_t)n * 32, 256), 256, 0, s>>>(v, da, db, x->work, x->wsteps, x->wcount, dout, nsamp);
     sc->ctx->launches += 2;
     return MPTG_OK;
 }
 
-mptg_status scene_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* dout, cudaStream_t s) {
+mptg_status scene_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* dout, cudaStream_t s,
+                             EdgeScratch* scr) {
     if (n <= 0) return MPTG_OK;
-    if (sc->kind == MPTG_SCENE_RIGID_MESH) return mesh_states_dev(sc, dq, n, dout, s);
+    if (sc->kind == MPTG_SCENE_RIGID_MESH) return mesh_states_dev(sc, dq, n, dout, s, scr ? scr : &sc->scratch);
     SceneView v = scene_view(sc);
     k_states_f<<<mptg_blocks(n, 256), 256, 0, s>>>(v, dq, n, dout);
     MPTG_LAUNCHED(sc->ctx);

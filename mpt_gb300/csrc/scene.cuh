@@ -4,6 +4,31 @@
 
 struct MeshData;  // rigid-mesh BVHs (mesh.cu)
 
+// Working memory of one batched validity call.  A scene owns one for the
+// C-ABI calls; every planner owns its own, so planners sharing a scene can run
+// concurrently on their own streams.
+struct EdgeScratch {
+    // grid / planar-arm two-phase edges
+    int* work = nullptr;
+    int* wsteps = nullptr;
+    int* wcount = nullptr;
+    size_t work_cap = 0;
+    // rigid mesh
+    int* mwork = nullptr;
+    int* nwork = nullptr;
+    size_t mwork_cap = 0;
+    double* samples = nullptr;
+    int* sample_edge = nullptr;
+    uint8_t* sample_ok = nullptr;
+    size_t sample_cap = 0;
+    int* counts = nullptr;
+    int* offs = nullptr;
+    uint8_t* okb = nullptr;
+    size_t edge_cap = 0;
+    int* hbuf = nullptr;  // pinned, 4 ints
+};
+void scratch_free(EdgeScratch* s);
+
 struct mptg_scene {
     mptg_ctx* ctx = nullptr;
     int kind = 0, metric = 0, D = 0;
@@ -22,11 +47,8 @@ struct mptg_scene {
     float4* discs32 = nullptr;
     float* link32 = nullptr;
     float arm_reach = 0.f;
-    // two-phase edge scratch: surviving edges and their step counts
-    int* work = nullptr;
-    int* wsteps = nullptr;
-    int* wcount = nullptr;
-    size_t work_cap = 0;
+    // scratch of the C-ABI validity calls on this scene
+    EdgeScratch scratch;
 };
 
 // POD view passed to kernels by value
@@ -51,14 +73,17 @@ struct SceneView {
 };
 
 SceneView scene_view(const mptg_scene* s);
+// scr == nullptr uses the scene's own scratch
 mptg_status scene_edges_dev(mptg_scene* sc, const double* da, const double* db, int n, double step, int resolution,
-                            uint8_t* dout, cudaStream_t s, unsigned long long* nsamp);
-mptg_status scene_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* dout, cudaStream_t s);
+                            uint8_t* dout, cudaStream_t s, unsigned long long* nsamp, EdgeScratch* scr = nullptr);
+mptg_status scene_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* dout, cudaStream_t s,
+                             EdgeScratch* scr = nullptr);
 
 // rigid-mesh hooks (mesh.cu)
 mptg_status mesh_scene_create(mptg_ctx* ctx, const mptg_scene_desc* d, mptg_scene* s);
 void mesh_scene_free(mptg_scene* s);
 void mesh_fill_view(const mptg_scene* s, SceneView* v);
 mptg_status mesh_edges_dev(mptg_scene* sc, const double* da, const double* db, int n, double step, int resolution,
-                           uint8_t* dout, cudaStream_t s, unsigned long long* nsamp);
-mptg_status mesh_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* dout, cudaStream_t s);
+                           uint8_t* dout, cudaStream_t s, unsigned long long* nsamp, EdgeScratch* scr);
+mptg_status mesh_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* dout, cudaStream_t s,
+                            EdgeScratch* scr);
