@@ -75,6 +75,9 @@ mptg_status mptg_tree_destroy(mptg_tree* tree);
  * (row-major n x dim doubles); their ids are size()..size()+n-1. */
 mptg_status mptg_tree_insert(mptg_tree* tree, const double* states, size_t n, void* stream);
 mptg_status mptg_tree_size(mptg_tree* tree, size_t* n);
+/* Remove every state, keeping the tree's allocations (no reference
+ * counterpart: a reference planner is rebuilt for each query). */
+mptg_status mptg_tree_clear(mptg_tree* tree, void* stream);
 /* Copy states [first, first+n) out of the tree (row-major doubles). */
 mptg_status mptg_tree_states(mptg_tree* tree, size_t first, size_t n, double* out, void* stream);
 /* nigh nearest(q) (src/mpt/impl/prrt/prrt.hpp:406-409): for each of nq
@@ -248,6 +251,51 @@ mptg_status mptg_planner_set_surrogate(mptg_planner* planner, mptg_surrogate* su
  * added, [3] tree size, [4] goals, [5] states checked by link, [6] seconds in
  * run, [7] wavefront counter. */
 mptg_status mptg_planner_stats(mptg_planner* planner, double out[8]);
+
+/* Start over as a new Planner(scenario, seed) on the same scene, keeping the
+ * allocations: tree, goal, solutions and statistics are cleared.  params NULL
+ * keeps the current ones; otherwise wavefront and max_nodes may not exceed
+ * those the planner was created with (MPTG_ERR_CAPACITY). */
+mptg_status mptg_planner_reset(mptg_planner* planner, const mptg_plan_params* params);
+
+/* ---- batched multi-query serving -------------------------------------
+ * Many independent planning queries (one start, one GoalState each) over
+ * shared scenes.  `concurrency` host workers (<= 0: 8) each own one CUDA
+ * stream and reuse one planner per scene between queries, so the wavefronts
+ * of different queries overlap on the GPU.  A query's planner behaves exactly
+ * as mptg_planner_create + add_start + set_goal + run(stop_when_solved)
+ * with the same parameters: the same seed gives the same tree and path. */
+typedef struct {
+    mptg_scene* scene;
+    const double* start;        /* [dim], host */
+    const double* goal;         /* [dim], host */
+    double goal_radius;
+    mptg_plan_params params;    /* params.max_nodes is the query's node budget */
+    const double* lo;           /* sampling bounds or NULL, as mptg_planner_create */
+    const double* hi;
+    double time_limit_s;        /* <= 0: none */
+    mptg_surrogate* surrogate;  /* NULL: plain planner */
+    double surrogate_threshold;
+    double* path;               /* optional host buffer of path_cap states */
+    size_t path_cap;
+} mptg_query;
+
+typedef struct {
+    mptg_status status;
+    int solved;
+    size_t nodes;               /* tree size at the end */
+    size_t wavefronts;
+    double solve_s;             /* from the query's first wavefront to its end */
+    double finish_s;            /* from the batch's start to the query's end */
+    double cost;                /* best path cost, +inf when unsolved */
+    size_t path_len;            /* states of the best path (0 if unsolved); written to
+                                   query.path only when it fits path_cap */
+} mptg_result;
+
+/* Runs queries [0, n) and fills out[0, n).  Returns MPTG_OK when every query
+ * ran (per-query failures are in out[i].status), else the first error. */
+mptg_status mptg_plan_batch(mptg_ctx* ctx, const mptg_query* queries, size_t n, int concurrency,
+                            mptg_result* out);
 
 #ifdef __cplusplus
 }

@@ -3,10 +3,14 @@
 
 mptg_status mptg_fail(mptg_ctx* ctx, mptg_status st, const char* fmt, ...) {
     if (ctx) {
+        char msg[sizeof(ctx->err)];
         va_list ap;
         va_start(ap, fmt);
-        vsnprintf(ctx->err, sizeof(ctx->err), fmt, ap);
+        vsnprintf(msg, sizeof(msg), fmt, ap);
         va_end(ap);
+        // batch workers may fail concurrently on one context
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        memcpy(ctx->err, msg, sizeof(msg));
     }
     return st;
 }

@@ -17,7 +17,11 @@
 #include "scene.cuh"
 #include "tree.cuh"
 #include "philox.cuh"
+#include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <map>
+#include <thread>
 
 #define PLAN_SCAN_BLOCK 1024
 
@@ -77,10 +81,19 @@ struct mptg_planner {
     uint8_t* ok_c = nullptr;
     uint8_t* keep = nullptr;
     uint64_t stat_culled = 0;
+    // every call of this planner runs on its own non-blocking stream, with its
+    // own validity scratch, so planners on one scene can run concurrently
+    cudaStream_t stream = nullptr;
+    EdgeScratch scratch;
+    size_t cap_nodes = 0;     // tree capacity and parent array length
+    int cap_wave = 0;         // wavefront buffers
+    int* path_ids = nullptr;  // [cap_nodes]
+    double* path_out = nullptr;  // [2]
 };
 
 extern "C" mptg_status mptg_surrogate_score_dev(mptg_surrogate* s, const double* dstates, int n, float* dlogits,
                                                 cudaStream_t st);
+std::mutex* mptg_surrogate_mutex(mptg_surrogate* s);
 
 // ------------------------------------------------------------------ kernels
 
@@ -280,6 +293,15 @@ __global__ void k_plan_path(int goal, const int* __restrict__ parent, const doub
     }
 }
 
+// out[k] = states64[ids[k]] for k < n (one double per thread)
+__global__ void k_plan_gather(const int* __restrict__ ids, int n, const double* __restrict__ states64, int D,
+                              double* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * D) return;
+    int k = i / D, d = i - k * D;
+    out[i] = states64[(size_t)ids[k] * D + d];
+}
+
 // ------------------------------------------------------------------ host
 
 static PlanView plan_view(const mptg_planner* p) {
@@ -296,13 +318,71 @@ static PlanView plan_view(const mptg_planner* p) {
 static void planner_free(mptg_planner* p) {
     void* ptrs[] = {p->lo, p->hi, p->goal, p->parent, p->samp, p->nidx, p->ndist, p->nearst, p->newst, p->skip,
                     p->ok, p->scan, p->bsum, p->acc_states, p->acc_parent, p->acc_goal, p->nsamp, p->logits,
-                    p->near_c, p->new_c, p->cmap, p->ok_c, p->keep};
+                    p->near_c, p->new_c, p->cmap, p->ok_c, p->keep, p->path_ids, p->path_out};
+    if (p->stream) cudaStreamSynchronize(p->stream);
     for (void* x : ptrs)
         if (x) cudaFree(x);
     if (p->hbuf) cudaFreeHost(p->hbuf);
     if (p->hgoal) cudaFreeHost(p->hgoal);
+    scratch_free(&p->scratch);
     if (p->tree) mptg_tree_destroy(p->tree);
+    if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
+}
+
+static mptg_status check_params(mptg_ctx* ctx, const mptg_scene* scene, const mptg_plan_params* prm) {
+    if (prm->wavefront < 1 || prm->wavefront > (1 << 20))
+        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "wavefront must be in [1, 2^20]");
+    if (prm->max_nodes < 1) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "max_nodes must be positive");
+    if (!(prm->edge_step > 0)) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "edge_step must be positive");
+    if (!(prm->goal_bias >= 0 && prm->goal_bias <= 1))
+        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "goal_bias must be in [0, 1]");
+    if (prm->resolution == 1 && scene->metric != MPTG_METRIC_SO2)
+        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "joint-step resolution needs an SO2 scene");
+    return MPTG_OK;
+}
+
+// sampling bounds: given, else the metric's domain
+static mptg_status set_bounds(mptg_planner* p, const double* lo, const double* hi) {
+    const int D = p->D;
+    double l[MPTG_MAX_DIM], h[MPTG_MAX_DIM];
+    for (int d = 0; d < D; ++d) {
+        l[d] = lo ? lo[d] : (p->metric == MPTG_METRIC_SO2 ? -MPTG_PI : 0.0);
+        h[d] = hi ? hi[d] : (p->metric == MPTG_METRIC_SO2 ? MPTG_PI : 1.0);
+    }
+    MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(p->lo, l, D * sizeof(double), cudaMemcpyHostToDevice, p->stream));
+    MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(p->hi, h, D * sizeof(double), cudaMemcpyHostToDevice, p->stream));
+    MPTG_CUDA_TRY(p->ctx, cudaStreamSynchronize(p->stream));
+    return MPTG_OK;
+}
+
+// a fresh Planner(scenario, seed) on the same allocations
+static mptg_status planner_reset(mptg_planner* p, const mptg_plan_params* prm, bool bounds, const double* lo,
+                                 const double* hi) {
+    mptg_ctx* ctx = p->ctx;
+    if (p->solving) return mptg_fail(ctx, MPTG_ERR_ALREADY_SOLVING, "already solving");
+    if (prm) {
+        mptg_status st = check_params(ctx, p->scene, prm);
+        if (st) return st;
+        if (prm->wavefront > p->cap_wave || prm->max_nodes > p->cap_nodes)
+            return mptg_fail(ctx, MPTG_ERR_CAPACITY, "reset needs wavefront <= %d and max_nodes <= %zu", p->cap_wave,
+                             p->cap_nodes);
+        p->prm = *prm;
+    }
+    MPTG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    mptg_status st = mptg_tree_clear(p->tree, p->stream);
+    if (st) return st;
+    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->nsamp, 0, sizeof(unsigned long long), p->stream));
+    if (bounds && (st = set_bounds(p, lo, hi))) return st;
+    MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(p->stream));
+    p->has_goal = 0;
+    p->goal_host.clear();
+    p->goals.clear();
+    p->wave = 0;
+    p->stat_samples = p->stat_goal_samples = p->stat_accepted = p->stat_wavefronts = 0;
+    p->stat_skipped = p->stat_culled = 0;
+    p->stat_seconds = 0;
+    return MPTG_OK;
 }
 
 // one wavefront; returns the number of nodes added
@@ -331,27 +411,33 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
     int nblk = (W + PLAN_SCAN_BLOCK - 1) / PLAN_SCAN_BLOCK;
     if (p->sg) {
         // score the new states; only edges the surrogate does not reject go to the exact check
-        if ((st = mptg_surrogate_score_dev(p->sg, p->newst, W, p->logits, s))) return st;
-        k_plan_keep<<<mptg_blocks(W, 256), 256, 0, s>>>(W, p->skip, p->logits, p->sg_thr, p->keep, p->ok);
-        k_plan_scan<<<nblk, PLAN_SCAN_BLOCK, 0, s>>>(W, p->keep, p->skip, p->scan, p->bsum);
-        k_plan_scan_top<<<1, 1024, 0, s>>>(nblk, p->bsum);
-        k_plan_cgather<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->scan, p->bsum, p->nearst, p->newst, p->near_c,
-                                                           p->new_c, p->cmap);
-        ctx->launches += 4;
-        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->hbuf + 1, p->bsum + nblk, sizeof(int), cudaMemcpyDeviceToHost, s));
-        MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
-        int nk = p->hbuf[1];
+        int nk = 0;
+        {
+            // the surrogate's activation buffers are shared between planners:
+            // hold it until this stream has consumed its logits
+            std::lock_guard<std::mutex> lock(*mptg_surrogate_mutex(p->sg));
+            if ((st = mptg_surrogate_score_dev(p->sg, p->newst, W, p->logits, s))) return st;
+            k_plan_keep<<<mptg_blocks(W, 256), 256, 0, s>>>(W, p->skip, p->logits, p->sg_thr, p->keep, p->ok);
+            k_plan_scan<<<nblk, PLAN_SCAN_BLOCK, 0, s>>>(W, p->keep, p->skip, p->scan, p->bsum);
+            k_plan_scan_top<<<1, 1024, 0, s>>>(nblk, p->bsum);
+            k_plan_cgather<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->scan, p->bsum, p->nearst, p->newst,
+                                                               p->near_c, p->new_c, p->cmap);
+            ctx->launches += 4;
+            MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->hbuf + 1, p->bsum + nblk, sizeof(int), cudaMemcpyDeviceToHost, s));
+            MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+            nk = p->hbuf[1];
+        }
         p->stat_culled += (uint64_t)(W - nk);
         if (nk > 0) {
             st = scene_edges_dev(p->scene, p->near_c, p->new_c, nk, p->prm.edge_step, p->prm.resolution, p->ok_c, s,
-                                 p->nsamp);
+                                 p->nsamp, &p->scratch);
             if (st) return st;
             k_plan_cscatter<<<mptg_blocks(nk, 256), 256, 0, s>>>(nk, p->cmap, p->ok_c, p->ok);
             MPTG_LAUNCHED(ctx);
         }
     } else {
         st = scene_edges_dev(p->scene, p->nearst, p->newst, W, p->prm.edge_step, p->prm.resolution, p->ok, s,
-                             p->nsamp);
+                             p->nsamp, &p->scratch);
         if (st) return st;
     }
     k_plan_scan<<<nblk, PLAN_SCAN_BLOCK, 0, s>>>(W, p->ok, p->skip, p->scan, p->bsum);
@@ -388,14 +474,8 @@ mptg_status mptg_planner_create(mptg_ctx* ctx, mptg_scene* scene, const mptg_pla
                                 const double* hi, mptg_planner** out) {
     if (!ctx || !scene || !prm || !out) return MPTG_ERR_INVALID_ARG;
     *out = nullptr;
-    if (prm->wavefront < 1 || prm->wavefront > (1 << 20))
-        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "wavefront must be in [1, 2^20]");
-    if (prm->max_nodes < 1) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "max_nodes must be positive");
-    if (!(prm->edge_step > 0)) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "edge_step must be positive");
-    if (!(prm->goal_bias >= 0 && prm->goal_bias <= 1))
-        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "goal_bias must be in [0, 1]");
-    if (prm->resolution == 1 && scene->metric != MPTG_METRIC_SO2)
-        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "joint-step resolution needs an SO2 scene");
+    mptg_status st = check_params(ctx, scene, prm);
+    if (st) return st;
     MPTG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     mptg_planner* p = new mptg_planner();
     p->ctx = ctx;
@@ -405,13 +485,19 @@ mptg_status mptg_planner_create(mptg_ctx* ctx, mptg_scene* scene, const mptg_pla
     p->metric = scene->metric;
     p->w0 = scene->w0;
     p->w1 = scene->w1;
+    p->cap_nodes = prm->max_nodes;
+    p->cap_wave = prm->wavefront;
+    cudaError_t e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete p;
+        return mptg_fail(ctx, MPTG_ERR_CUDA, "planner stream: %s", cudaGetErrorString(e));
+    }
     double w[2] = {p->w0, p->w1};
-    mptg_status st = mptg_tree_create(ctx, (mptg_metric)p->metric, p->D, w, prm->max_nodes, &p->tree);
-    if (st) { delete p; return st; }
+    if ((st = mptg_tree_create(ctx, (mptg_metric)p->metric, p->D, w, prm->max_nodes, &p->tree))) {
+        planner_free(p);
+        return st;
+    }
     const size_t W = prm->wavefront, D = p->D, N = prm->max_nodes;
-    int nblk = (int)((W + PLAN_SCAN_BLOCK - 1) / PLAN_SCAN_BLOCK);
-    if (nblk > 1024) { planner_free(p); return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "wavefront too large"); }
-    cudaError_t e = cudaSuccess;
 #define ALLOC(ptr, bytes) if (e == cudaSuccess) e = cudaMalloc((void**)&(ptr), (bytes))
     ALLOC(p->lo, D * sizeof(double));
     ALLOC(p->hi, D * sizeof(double));
@@ -430,6 +516,8 @@ mptg_status mptg_planner_create(mptg_ctx* ctx, mptg_scene* scene, const mptg_pla
     ALLOC(p->acc_parent, W * sizeof(int));
     ALLOC(p->acc_goal, W);
     ALLOC(p->nsamp, sizeof(unsigned long long));
+    ALLOC(p->path_ids, N * sizeof(int));
+    ALLOC(p->path_out, 2 * sizeof(double));
 #undef ALLOC
     if (e == cudaSuccess) e = cudaMallocHost((void**)&p->hbuf, 16 * sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost((void**)&p->hgoal, W);
@@ -438,15 +526,9 @@ mptg_status mptg_planner_create(mptg_ctx* ctx, mptg_scene* scene, const mptg_pla
         planner_free(p);
         return mptg_fail(ctx, MPTG_ERR_OOM, "planner allocation failed: %s", cudaGetErrorString(e));
     }
-    // sampling bounds: given, else the metric's domain
-    std::vector<double> l(D), h(D);
-    for (size_t d = 0; d < D; ++d) {
-        l[d] = lo ? lo[d] : (p->metric == MPTG_METRIC_SO2 ? -MPTG_PI : 0.0);
-        h[d] = hi ? hi[d] : (p->metric == MPTG_METRIC_SO2 ? MPTG_PI : 1.0);
-    }
-    e = cudaMemcpy(p->lo, l.data(), D * sizeof(double), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(p->hi, h.data(), D * sizeof(double), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(p->nsamp, 0, sizeof(unsigned long long));
+    if ((st = set_bounds(p, lo, hi))) { planner_free(p); return st; }
+    e = cudaMemsetAsync(p->nsamp, 0, sizeof(unsigned long long), p->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
     if (e != cudaSuccess) {
         planner_free(p);
         return mptg_fail(ctx, MPTG_ERR_CUDA, "planner init failed: %s", cudaGetErrorString(e));
@@ -457,9 +539,13 @@ mptg_status mptg_planner_create(mptg_ctx* ctx, mptg_scene* scene, const mptg_pla
 
 mptg_status mptg_planner_destroy(mptg_planner* p) {
     if (!p) return MPTG_ERR_INVALID_ARG;
-    cudaDeviceSynchronize();
     planner_free(p);
     return MPTG_OK;
+}
+
+mptg_status mptg_planner_reset(mptg_planner* p, const mptg_plan_params* params) {
+    if (!p) return MPTG_ERR_INVALID_ARG;
+    return planner_reset(p, params, false, nullptr, nullptr);
 }
 
 mptg_status mptg_planner_add_start(mptg_planner* p, const double* q) {
@@ -467,17 +553,19 @@ mptg_status mptg_planner_add_start(mptg_planner* p, const double* q) {
     size_t n = 0;
     mptg_tree_size(p->tree, &n);
     if (n >= p->prm.max_nodes) return mptg_fail(p->ctx, MPTG_ERR_CAPACITY, "node budget reached");
-    mptg_status st = mptg_tree_insert(p->tree, q, 1, nullptr);
+    mptg_status st = mptg_tree_insert(p->tree, q, 1, p->stream);
     if (st) return st;
-    int minus1 = -1;
-    MPTG_CUDA_TRY(p->ctx, cudaMemcpy(p->parent + n, &minus1, sizeof(int), cudaMemcpyHostToDevice));
+    const int minus1 = -1;
+    MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(p->parent + n, &minus1, sizeof(int), cudaMemcpyHostToDevice, p->stream));
+    MPTG_CUDA_TRY(p->ctx, cudaStreamSynchronize(p->stream));
     return MPTG_OK;
 }
 
 mptg_status mptg_planner_set_goal(mptg_planner* p, const double* q, double radius) {
     if (!p || !q) return MPTG_ERR_INVALID_ARG;
     if (!(radius >= 0)) return mptg_fail(p->ctx, MPTG_ERR_INVALID_ARG, "goal radius must be >= 0");
-    MPTG_CUDA_TRY(p->ctx, cudaMemcpy(p->goal, q, p->D * sizeof(double), cudaMemcpyHostToDevice));
+    MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(p->goal, q, p->D * sizeof(double), cudaMemcpyDefault, p->stream));
+    MPTG_CUDA_TRY(p->ctx, cudaStreamSynchronize(p->stream));
     p->goal_host.assign(q, q + p->D);
     p->has_goal = 1;
     p->prm.goal_radius = radius;
@@ -503,7 +591,7 @@ mptg_status mptg_planner_run(mptg_planner* p, int max_wavefronts, double time_li
         double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (time_limit_s > 0 && el >= time_limit_s) break;
         int added = 0;
-        st = plan_wavefront(p, nullptr, &added);
+        st = plan_wavefront(p, p->stream, &added);
         if (st) break;
     }
     p->stat_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -523,50 +611,54 @@ mptg_status mptg_planner_goals(mptg_planner* p, size_t* n) {
     return MPTG_OK;
 }
 
-mptg_status mptg_planner_solution(mptg_planner* p, double* path, size_t cap, size_t* len, double* cost) {
-    if (!p || !len) return MPTG_ERR_INVALID_ARG;
+// PRRT::bestSolution + solution() (prrt.hpp:219-274) on the planner's stream
+static mptg_status planner_solution(mptg_planner* p, double* path, size_t cap, size_t* len, double* cost,
+                                    bool path_must_fit) {
     mptg_ctx* ctx = p->ctx;
+    cudaStream_t s = p->stream;
     *len = 0;
     if (cost) *cost = INFINITY;
     if (p->goals.empty()) return MPTG_OK;
-    int* dids = nullptr;
-    double* dout = nullptr;
-    MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&dout, 2 * sizeof(double)));
+    MPTG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    double* hd = reinterpret_cast<double*>(p->hbuf + 8);  // 2 doubles of the pinned words
+    const double* states = mptg_tree_states_dev(p->tree);
     // best goal by path cost; goals are visited newest first with strict <,
     // as PRRT::bestSolution walks its push_front list (prrt.hpp:219-234)
     double best = INFINITY;
     int bestg = -1, bestlen = 0;
     for (size_t k = p->goals.size(); k-- > 0;) {
-        k_plan_path<<<1, 1>>>(p->goals[k], p->parent, mptg_tree_states_dev(p->tree), p->D, p->metric, p->w0, p->w1, 0,
-                              nullptr, dout);
+        k_plan_path<<<1, 1, 0, s>>>(p->goals[k], p->parent, states, p->D, p->metric, p->w0, p->w1, 0, nullptr,
+                                    p->path_out);
         MPTG_LAUNCHED(ctx);
-        double h[2];
-        cudaError_t e = cudaMemcpy(h, dout, sizeof(h), cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) { cudaFree(dout); return mptg_fail(ctx, MPTG_ERR_CUDA, "%s", cudaGetErrorString(e)); }
-        if (h[0] < best || bestg < 0) { best = h[0]; bestg = p->goals[k]; bestlen = (int)h[1]; }
+        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(hd, p->path_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        if (hd[0] < best || bestg < 0) { best = hd[0]; bestg = p->goals[k]; bestlen = (int)hd[1]; }
     }
     *len = (size_t)bestlen;
     if (cost) *cost = best;
-    if (!path) { cudaFree(dout); return MPTG_OK; }
+    if (!path) return MPTG_OK;
     if ((size_t)bestlen > cap) {
-        cudaFree(dout);
+        if (!path_must_fit) return MPTG_OK;
         return mptg_fail(ctx, MPTG_ERR_CAPACITY, "path of %d states does not fit %zu", bestlen, cap);
     }
-    cudaError_t e = cudaMalloc((void**)&dids, bestlen * sizeof(int));
-    if (e != cudaSuccess) { cudaFree(dout); return mptg_fail(ctx, MPTG_ERR_OOM, "%s", cudaGetErrorString(e)); }
-    k_plan_path<<<1, 1>>>(bestg, p->parent, mptg_tree_states_dev(p->tree), p->D, p->metric, p->w0, p->w1, bestlen,
-                          dids, dout);
+    k_plan_path<<<1, 1, 0, s>>>(bestg, p->parent, states, p->D, p->metric, p->w0, p->w1, bestlen, p->path_ids,
+                                p->path_out);
     MPTG_LAUNCHED(ctx);
-    std::vector<int> ids(bestlen);
-    e = cudaMemcpy(ids.data(), dids, bestlen * sizeof(int), cudaMemcpyDeviceToHost);
-    cudaFree(dids);
-    cudaFree(dout);
-    if (e != cudaSuccess) return mptg_fail(ctx, MPTG_ERR_CUDA, "%s", cudaGetErrorString(e));
-    for (int k = 0; k < bestlen; ++k) {
-        mptg_status st = mptg_tree_states(p->tree, ids[k], 1, path + (size_t)k * p->D, nullptr);
-        if (st) return st;
+    // gather the waypoints through the wavefront state buffer, cap_wave states at a time
+    for (int c = 0; c < bestlen; c += p->cap_wave) {
+        int m = std::min(p->cap_wave, bestlen - c);
+        k_plan_gather<<<mptg_blocks(m * p->D, 256), 256, 0, s>>>(p->path_ids + c, m, states, p->D, p->acc_states);
+        MPTG_LAUNCHED(ctx);
+        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(path + (size_t)c * p->D, p->acc_states, (size_t)m * p->D * sizeof(double),
+                                           cudaMemcpyDefault, s));
     }
+    MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     return MPTG_OK;
+}
+
+mptg_status mptg_planner_solution(mptg_planner* p, double* path, size_t cap, size_t* len, double* cost) {
+    if (!p || !len) return MPTG_ERR_INVALID_ARG;
+    return planner_solution(p, path, cap, len, cost, true);
 }
 
 mptg_status mptg_planner_graph(mptg_planner* p, double* states, int32_t* parents, size_t cap, size_t* n) {
@@ -577,17 +669,19 @@ mptg_status mptg_planner_graph(mptg_planner* p, double* states, int32_t* parents
     if (!states && !parents) return MPTG_OK;
     if (sz > cap) return mptg_fail(p->ctx, MPTG_ERR_CAPACITY, "graph of %zu nodes does not fit %zu", sz, cap);
     if (states) {
-        mptg_status st = mptg_tree_states(p->tree, 0, sz, states, nullptr);
+        mptg_status st = mptg_tree_states(p->tree, 0, sz, states, p->stream);
         if (st) return st;
     }
-    if (parents) MPTG_CUDA_TRY(p->ctx, cudaMemcpy(parents, p->parent, sz * sizeof(int), cudaMemcpyDeviceToHost));
+    if (parents)
+        MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(parents, p->parent, sz * sizeof(int), cudaMemcpyDefault, p->stream));
+    MPTG_CUDA_TRY(p->ctx, cudaStreamSynchronize(p->stream));
     return MPTG_OK;
 }
 
 mptg_status mptg_planner_set_surrogate(mptg_planner* p, mptg_surrogate* sg, double threshold) {
     if (!p) return MPTG_ERR_INVALID_ARG;
     if (sg && !p->logits) {
-        const size_t W = p->prm.wavefront, D = p->D;
+        const size_t W = p->cap_wave, D = p->D;
         cudaError_t e = cudaSuccess;
         if (e == cudaSuccess) e = cudaMalloc((void**)&p->logits, W * sizeof(float));
         if (e == cudaSuccess) e = cudaMalloc((void**)&p->near_c, W * D * sizeof(double));
@@ -608,7 +702,8 @@ mptg_status mptg_planner_set_surrogate(mptg_planner* p, mptg_surrogate* sg, doub
 mptg_status mptg_planner_stats(mptg_planner* p, double out[8]) {
     if (!p || !out) return MPTG_ERR_INVALID_ARG;
     unsigned long long ns = 0;
-    MPTG_CUDA_TRY(p->ctx, cudaMemcpy(&ns, p->nsamp, sizeof(ns), cudaMemcpyDeviceToHost));
+    MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(&ns, p->nsamp, sizeof(ns), cudaMemcpyDeviceToHost, p->stream));
+    MPTG_CUDA_TRY(p->ctx, cudaStreamSynchronize(p->stream));
     size_t n = 0;
     mptg_tree_size(p->tree, &n);
     out[0] = (double)p->stat_wavefronts;
@@ -620,6 +715,91 @@ mptg_status mptg_planner_stats(mptg_planner* p, double out[8]) {
     out[6] = p->stat_seconds;
     out[7] = (double)p->wave;
     return MPTG_OK;
+}
+
+// ------------------------------------------------------------- batch serving
+
+using BatchCaps = std::map<mptg_scene*, std::pair<size_t, int>>;  // scene -> (max budget, max wavefront)
+
+static double seconds_since(std::chrono::steady_clock::time_point t) {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t).count();
+}
+
+// one query on this worker's planner for its scene (created on first use with
+// the batch's largest budget and wavefront for that scene)
+static mptg_status batch_query(mptg_ctx* ctx, const mptg_query& q, const BatchCaps& caps,
+                               std::map<mptg_scene*, mptg_planner*>& mine, mptg_result& r) {
+    mptg_planner*& p = mine[q.scene];
+    mptg_status st;
+    if (!p) {
+        mptg_plan_params c = q.params;
+        const auto& cap = caps.at(q.scene);
+        c.max_nodes = cap.first;
+        c.wavefront = cap.second;
+        if ((st = mptg_planner_create(ctx, q.scene, &c, q.lo, q.hi, &p))) return st;
+    }
+    if ((st = planner_reset(p, &q.params, true, q.lo, q.hi))) return st;
+    if ((st = mptg_planner_set_surrogate(p, q.surrogate, q.surrogate_threshold))) return st;
+    if ((st = mptg_planner_add_start(p, q.start))) return st;
+    if ((st = mptg_planner_set_goal(p, q.goal, q.goal_radius))) return st;
+    const auto t = std::chrono::steady_clock::now();
+    int solved = 0;
+    st = mptg_planner_run(p, 0, q.time_limit_s, 1, &solved);
+    r.solve_s = seconds_since(t);
+    r.solved = solved;
+    mptg_tree_size(p->tree, &r.nodes);
+    r.wavefronts = (size_t)p->stat_wavefronts;
+    if (st) return st;
+    return planner_solution(p, q.path, q.path_cap, &r.path_len, &r.cost, false);
+}
+
+mptg_status mptg_plan_batch(mptg_ctx* ctx, const mptg_query* qs, size_t n, int concurrency, mptg_result* out) {
+    if (!ctx) return MPTG_ERR_INVALID_ARG;
+    if (n == 0) return MPTG_OK;
+    if (!qs || !out) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "null queries or results");
+    BatchCaps caps;
+    for (size_t i = 0; i < n; ++i) {
+        const mptg_query& q = qs[i];
+        if (!q.scene || !q.start || !q.goal)
+            return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "query %zu: null scene, start or goal", i);
+        if (q.scene->ctx != ctx) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "query %zu: scene of another context", i);
+        if (!(q.goal_radius >= 0)) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "query %zu: goal radius < 0", i);
+        mptg_status st = check_params(ctx, q.scene, &q.params);
+        if (st) return st;
+        auto& c = caps[q.scene];
+        c.first = std::max(c.first, q.params.max_nodes);
+        c.second = std::max(c.second, q.params.wavefront);
+    }
+    size_t workers = concurrency > 0 ? (size_t)concurrency : 8;
+    workers = std::min(workers, n);
+    std::atomic<size_t> next{0};
+    std::mutex mu;
+    mptg_status first = MPTG_OK;
+    const auto t0 = std::chrono::steady_clock::now();
+    auto work = [&]() {
+        std::map<mptg_scene*, mptg_planner*> mine;
+        const bool dev_ok = cudaSetDevice(ctx->device) == cudaSuccess;
+        for (size_t i; (i = next.fetch_add(1)) < n;) {
+            mptg_result& r = out[i];
+            r = mptg_result{};
+            r.cost = INFINITY;
+            mptg_status st = dev_ok ? batch_query(ctx, qs[i], caps, mine, r)
+                                    : mptg_fail(ctx, MPTG_ERR_CUDA, "cudaSetDevice failed in a batch worker");
+            r.status = st;
+            r.finish_s = seconds_since(t0);
+            if (st) {
+                std::lock_guard<std::mutex> lock(mu);
+                if (first == MPTG_OK) first = st;
+            }
+        }
+        for (auto& kv : mine)
+            if (kv.second) planner_free(kv.second);
+    };
+    std::vector<std::thread> pool;
+    for (size_t k = 1; k < workers; ++k) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    return first;
 }
 
 }  // extern "C"

@@ -56,7 +56,12 @@ struct mptg_surrogate {
     double* dstates = nullptr;    // staging for host inputs [cap][in]
     uint8_t* dlabels = nullptr;
     float* dlogits = nullptr;
+    // held by a planner from scoring until its stream has consumed the logits,
+    // since the activation buffers above are shared
+    std::mutex mu;
 };
+
+std::mutex* mptg_surrogate_mutex(mptg_surrogate* s) { return &s->mu; }
 
 // parameter layout (floats)
 struct SgLayout {

@@ -1152,6 +1152,25 @@ mptg_status mptg_tree_size(mptg_tree* t, size_t* n) {
     return MPTG_OK;
 }
 
+// Back to the empty tree of mptg_tree_create, keeping every allocation: the
+// root becomes an empty leaf on bucket 0 again.  The root cell (the metric's
+// domain) is never written by inserts or rebuilds, so it stays as created.
+mptg_status mptg_tree_clear(mptg_tree* t, void* stream) {
+    if (!t) return MPTG_ERR_INVALID_ARG;
+    mptg_ctx* ctx = t->ctx;
+    cudaStream_t s = (cudaStream_t)stream;
+    MPTG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const int hc[CNT_N] = {1, 1, 0, 0, 0, 0, 0, 0, 0};
+    const int4 root = make_int4(-1, 0, 0, 0);
+    const int zero = 0;
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(t->dcnt, hc, sizeof(hc), cudaMemcpyHostToDevice, s));
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(t->nodes, &root, sizeof(root), cudaMemcpyHostToDevice, s));
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(t->node_depth, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
+    MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    t->n = 0;
+    return MPTG_OK;
+}
+
 static mptg_status read_counters(mptg_tree* t, cudaStream_t s) {
     mptg_ctx* ctx = t->ctx;
     MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(t->hcnt, t->dcnt, CNT_N * sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -56,9 +56,9 @@ def trained(ctx):
     from mpt_gb300.surrogate import Surrogate, se3_normalisation
     sc = scenes.mesh_scene()
     scale, shift = se3_normalisation(sc["lo"], sc["hi"])
-    q, y = _labelled(ctx, sc, 262144, 21)
+    q, y = _labelled(ctx, sc, 1 << 20, 21)
     sg = Surrogate(ctx, 7, scale, shift, seed=5)
-    hist = sg.fit(q, y, epochs=6, batch=8192, lr=1e-3)
+    hist = sg.fit(q, y, epochs=10, batch=8192, lr=1e-3)
     return sc, sg, hist
 
 
