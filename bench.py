@@ -174,6 +174,148 @@ def solve_times(ctx, seeds=5, cap_s=20.0):
     return res
 
 
+def _labelled_mesh_states(m, ctx, sc, n, seed):
+    """SE(3) states, half uniform and half near contact, labelled 1 = in collision by the exact checker."""
+    from mpt_gb300 import scenes
+    q = np.concatenate([scenes.uniform_states(sc, n // 2, seed), scenes.near_contact_states(sc, n - n // 2, seed + 7)])
+    scene = m.Scene(ctx, sc)
+    y = (1 - scene.valid(q)).astype(np.uint8)
+    scene.close()
+    return q, y
+
+
+def learned_vs_plain(ctx, m, torch, seeds=5, cap_s=20.0, n_train=1 << 22, epochs=10):
+    """Learned collision surrogate on the SE(3) scene: training throughput, held-out
+    FP/FN rates, scoring throughput against the bf16 tensor peak, and time to
+    solve with the surrogate culling edges versus the plain planner (same seeds)."""
+    from mpt_gb300 import planner as P
+    from mpt_gb300 import scenes
+    from mpt_gb300.surrogate import Surrogate, se3_normalisation
+    sc = scenes.mesh_scene()
+    t0 = time.perf_counter()
+    q, y = _labelled_mesh_states(m, ctx, sc, n_train, 21)
+    label_s = time.perf_counter() - t0
+    qt, yt = _labelled_mesh_states(m, ctx, sc, 65536, 99)
+    scale, shift = se3_normalisation(sc["lo"], sc["hi"], 20.0)
+    sg = Surrogate(ctx, 7, scale, shift, seed=5)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist = sg.fit(q, y, epochs=epochs, batch=8192, lr=2e-3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    z = sg.score(qt)
+    pred = (z > 0).astype(np.uint8)
+    fp = float(((pred == 1) & (yt == 0)).sum() / max(1, (yt == 0).sum()))
+    fn = float(((pred == 0) & (yt == 1)).sum() / max(1, (yt == 1).sum()))
+    # scoring throughput: 65,536 device-resident states per launch
+    dq = torch.from_numpy(np.ascontiguousarray(qt)).cuda()
+    dz = torch.empty(len(qt), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        sg.lib.mptg_surrogate_score(sg.h, dq.data_ptr(), len(qt), dz.data_ptr(), stream.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(10):
+        sg.lib.mptg_surrogate_score(sg.h, dq.data_ptr(), len(qt), dz.data_ptr(), stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    score_s = e0.elapsed_time(e1) / 1000.0 / 10
+    flops_fwd = 2.0 * (7 * 256 + 3 * 256 * 256 + 256)
+    res = {"train_states": int(n_train), "label_s": label_s, "epochs": epochs, "train_s": train_s,
+           "train_samples_per_s": n_train * epochs / train_s, "final_loss": hist[-1],
+           "heldout_accuracy": float((pred == yt).mean()), "fp_rate": fp, "fn_rate": fn,
+           "score_states_per_s": len(qt) / score_s,
+           "score_tflops": flops_fwd * len(qt) / score_s / 1e12,
+           "train_tflops": 3 * flops_fwd * n_train * epochs / train_s / 1e12}
+    for mode in ("plain", "learned"):
+        times, solved, checked = [], 0, []
+        for s in range(seeds):
+            pl = P.Planner(P.Scenario(sc), P.PRRT(P.gpu_wavefront(4096)), seed=1000 + s, ctx=ctx, max_nodes=1 << 21)
+            if mode == "learned":
+                pl.set_surrogate(sg, threshold=2.0)
+            pl.add_start(sc["start"])
+            t0 = time.perf_counter()
+            pl.solve_for(cap_s, lambda: pl.solved())
+            dt = time.perf_counter() - t0
+            if pl.solved():
+                solved += 1
+                times.append(dt)
+            checked.append(pl.stats()["link_states_checked"])
+            pl.close()
+        res[mode] = {"p50_s": statistics.median(times) if times else None, "p99_s": max(times) if times else None,
+                     "solved": solved, "seeds": seeds, "median_link_states_checked": statistics.median(checked)}
+    return res
+
+
+def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0):
+    """Config of the serving benchmark: n queries uniform over the three scenes,
+    start and goal rejection-sampled valid, node budgets log-uniform in
+    [1k, 200k], wavefront budget/16 clipped to [256, 4096]."""
+    from mpt_gb300 import planner as P
+    from mpt_gb300 import scenes
+    from mpt_gb300.batch import Query
+    rng = np.random.default_rng(seed)
+    descs = [scenes.grid_scene(), scenes.arm_scene(), scenes.mesh_scene()]
+    kinds = rng.integers(0, 3, n)
+    pools = []
+    for k, d in enumerate(descs):
+        need = 2 * int((kinds == k).sum())
+        scene = m.Scene(ctx, d)
+        got = []
+        s = 0
+        while sum(len(g) for g in got) < need:
+            c = scenes.uniform_states(d, 8 * need + 64, seed + 17 * k + s)
+            got.append(c[scene.valid(c) == 1])
+            s += 1
+        scene.close()
+        pools.append(np.concatenate(got)[:need])
+    used = [0, 0, 0]
+    qs = []
+    for i in range(n):
+        k = int(kinds[i])
+        d = descs[k]
+        a, b = pools[k][used[k]], pools[k][used[k] + 1]
+        used[k] += 2
+        budget = int(round(math.exp(rng.uniform(math.log(1000), math.log(200000)))))
+        W = int(min(4096, max(256, budget // 16)))
+        sc = P.Scenario(d, P.GoalState(d["goal_radius"], b))
+        qs.append(Query(sc, a, seed=seed + i, max_nodes=budget, wavefront=W, time_limit=time_limit))
+    return qs
+
+
+def batch_serving(m, ctx, n=512, concurrency=8, seq_sample=64):
+    """Batched multi-query serving: queries/s and time to solution over n queries
+    with `concurrency` concurrent planners, against the same planner running the
+    queries one after another (on the first seq_sample queries)."""
+    from mpt_gb300.batch import plan_batch
+    qs = batch_queries(m, ctx, n)
+    plan_batch(ctx, qs[:8], concurrency=concurrency)  # warm-up: planners, kernels
+    t0 = time.perf_counter()
+    r = plan_batch(ctx, qs, concurrency=concurrency)
+    wall = time.perf_counter() - t0
+    sol = sorted(x["solve_s"] for x in r if x["solved"])
+    kinds = [q.scenario.desc["kind"] for q in qs]
+    per = {}
+    for k in ("grid", "arm", "mesh"):
+        idx = [i for i in range(n) if kinds[i] == k]
+        sk = sorted(r[i]["solve_s"] for i in idx if r[i]["solved"])
+        per[k] = {"queries": len(idx), "solved": len(sk), "p50_s": sk[len(sk) // 2] if sk else None}
+    t0 = time.perf_counter()
+    rs = plan_batch(ctx, qs[:seq_sample], concurrency=1)
+    seq_wall = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    plan_batch(ctx, qs[:seq_sample], concurrency=concurrency)
+    conc_wall = time.perf_counter() - t0
+    same = all(a["solved"] == b["solved"] and a["nodes"] == b["nodes"] for a, b in zip(r[:seq_sample], rs))
+    return {"queries": n, "concurrency": concurrency, "wall_s": wall, "queries_per_s": n / wall,
+            "solved": len(sol), "p50_solve_s": sol[len(sol) // 2] if sol else None,
+            "p99_solve_s": sol[min(len(sol) - 1, int(0.99 * len(sol)))] if sol else None,
+            "per_scene": per, "time_limit_s": qs[0].time_limit,
+            "sequential_sample": {"queries": seq_sample, "sequential_queries_per_s": seq_sample / seq_wall,
+                                  "concurrent_queries_per_s": seq_sample / conc_wall,
+                                  "results_identical": bool(same)}}
+
+
 def run_reference(args):
     """CPU kd-tree (oracle port) on all host cores, bounded sample per step."""
     ws, rank, _ = _dist_env()
@@ -310,6 +452,8 @@ def run_gpu(args):
     # secondary figures: edge checks/s (three scenes) and time to solve
     edges = edge_rates(ctx, m, stream, torch)
     solves = solve_times(ctx) if not args.no_solve else None
+    learned = learned_vs_plain(ctx, m, torch) if not (args.no_solve or args.no_learned) else None
+    serving = batch_serving(m, ctx) if not (args.no_solve or args.no_batch) else None
 
     # CPU baselines: oracle kd-tree and DMV on the host cores, bounded samples
     cpu = None
@@ -356,6 +500,8 @@ def run_gpu(args):
                 "edge_checks": {"unit": "edges/s", "per_scene": edges,
                                 "cpu_kind": "port (oracle DMV + exact validity, all host cores)"},
                 "time_to_solve": {"unit": "s", "planner": "plain wavefront PRRT (GPU)", "per_scene": solves},
+                "learned_surrogate_se3": learned,
+                "batch_serving": serving,
                 "clocks": clk.summary(), "gpu_launches": launches, "tree_build_s": build_s,
                 "wall_s_timed": wall}
         print(json.dumps(line))
@@ -371,7 +517,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--queries", type=int, default=BATCH, help="queries per step (profiling: a smaller case)")
     ap.add_argument("--nn-only", action="store_true", help="time the NN kernel only (profiling)")
-    ap.add_argument("--no-solve", action="store_true", help="skip the time-to-solve runs")
+    ap.add_argument("--no-solve", action="store_true", help="skip the time-to-solve, surrogate and serving runs")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-surrogate comparison")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched serving run")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -8,18 +8,20 @@
 //   Scenario::link(a, b) through DiscreteMotionValidator
 //     src/mpt/discrete_motion_validator.hpp:71-130
 //
-// Edge kernel: one warp per edge.  The DMV result is the AND of valid() over
-// the fixed sample set {b} U {interpolate(a, b, i/steps) : 1 <= i < steps},
-// so evaluation order does not change it; the warp takes 32 samples per round
-// in a coarse-to-fine spread (lane j of round r tests sample j*R + r) and
-// leaves as soon as a ballot sees an invalid sample.
+// The DMV result is the AND of valid() over the fixed sample set
+// {b} U {interpolate(a, b, i/steps) : 1 <= i < steps}, so evaluation order
+// does not change it.  Grid edges: a thread per edge checks b and the step
+// count, then a warp per surviving edge takes 32 samples per round in a
+// coarse-to-fine spread (lane j of round r tests sample j*R + r).  Planar-arm
+// edges: a warp per edge decides one sample at a time with the lanes split
+// over the (link, obstacle) pairs, so it leaves at the first colliding link
+// of the first colliding sample.
 //
-// Exactness: every boolean equals the FP64 definition.  States are first
-// decided in FP32 with an a-priori error margin; a state whose FP32 result
-// lies inside the margin of a decision boundary is recomputed in FP64 with
-// explicit round-to-nearest intrinsics (no FMA contraction) and the
-// deterministic sin/cos of mptg_detmath.h, the same expressions the CPU
-// checker evaluates.
+// Exactness: every boolean equals the FP64 definition.  Values are first
+// computed in FP32 with an a-priori error margin; a decision whose FP32 value
+// lies inside the margin of its boundary is recomputed in FP64 with explicit
+// round-to-nearest intrinsics (no FMA contraction) and the deterministic
+// sin/cos of mptg_detmath.h, the same expressions the CPU checker evaluates.
 #include "metrics.cuh"
 #include "scene.cuh"
 
@@ -107,81 +109,6 @@ __device__ bool arm_valid64(const SceneView& s, const double* q) {
     return true;
 }
 
-__device__ __forceinline__ bool state_valid64(const SceneView& s, const double* q) {
-    switch (s.kind) {
-    case MPTG_SCENE_GRID: return grid_valid64(s, q);
-    case MPTG_SCENE_PLANAR_ARM: return arm_valid64(s, q);
-    default: return false;
-    }
-}
-
-// ------------------------------------------------------------------ kernels
-
-__global__ void __launch_bounds__(256) k_valid_states(SceneView s, const double* __restrict__ q, int n,
-                                                      uint8_t* __restrict__ out) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double st[MPTG_MAX_DIM];
-    for (int d = 0; d < s.D; ++d) st[d] = q[(size_t)i * s.D + d];
-    out[i] = state_valid64(s, st) ? 1 : 0;
-}
-
-// largest wrapped joint difference (planar-arm edge resolution)
-__device__ __forceinline__ double linf_so2_64(const double* a, const double* b, int D) {
-    double m = 0.0;
-    for (int i = 0; i < D; ++i) {
-        double d = so2_dist1_64(a[i], b[i]);
-        if (d > m) m = d;
-    }
-    return m;
-}
-
-__global__ void __launch_bounds__(256) k_valid_edges(SceneView s, const double* __restrict__ a,
-                                                     const double* __restrict__ b, int n, double inv, int resolution,
-                                                     uint8_t* __restrict__ out, unsigned long long* __restrict__ nsamp) {
-    const int lane = threadIdx.x & 31;
-    const int e = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-    if (e >= n) return;
-    const int D = s.D;
-    double A[MPTG_MAX_DIM], B[MPTG_MAX_DIM];
-    for (int d = 0; d < D; ++d) { A[d] = a[(size_t)e * D + d]; B[d] = b[(size_t)e * D + d]; }
-    double m = resolution == 1 ? linf_so2_64(A, B, D) : dist64(s.metric, D, s.w0, s.w1, A, B);
-    double sd = ceil(__dmul_rn(m, inv));
-    // steps as the reference's size_t; NaN distances make the edge invalid, and
-    // so do edges needing more than MPTG_MAX_EDGE_SAMPLES samples (a bounded
-    // kernel instead of the reference's unbounded loop)
-    bool ok = true;
-    long long steps = 0;
-    if (!(sd >= 0.0) || sd > (double)MPTG_MAX_EDGE_SAMPLES) ok = false;
-    else steps = (long long)sd;
-    long long M = steps < 2 ? 1 : steps;  // sample 0 = b, samples 1..steps-1 interior
-    double delta = steps >= 2 ? __ddiv_rn(1.0, (double)steps) : 0.0;
-    long long R = (M + 31) / 32;
-    unsigned long long cnt = 0;
-    for (long long r = 0; ok && r < R; ++r) {
-        long long k = (long long)lane * R + r;
-        bool v = true;
-        if (k < M) {
-            ++cnt;
-            if (k == 0) {
-                v = state_valid64(s, B);
-            } else {
-                double qs[MPTG_MAX_DIM];
-                interp64(s.metric, D, A, B, __dmul_rn((double)k, delta), qs);
-                v = state_valid64(s, qs);
-            }
-        }
-        if (__any_sync(0xffffffffu, !v)) ok = false;
-    }
-    if (nsamp) {
-        for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    }
-    if (lane == 0) {
-        out[e] = ok ? 1 : 0;
-        if (nsamp) atomicAdd(nsamp, cnt);
-    }
-}
-
 // ------------------------------------------------------------------ FP32 filters
 // Each filter returns VF_INVALID or VF_VALID when the FP32 evaluation decides
 // the state with certainty (every FP32 quantity lies farther from its decision
@@ -211,142 +138,58 @@ __device__ __forceinline__ float dpseg2_32(float px, float py, float ax, float a
     return ex * ex + ey * ey;
 }
 
-// planar arm from FP32 joint angles q (each within ea of the exact angle).
-// Positions: the cumulative angle is kept in [-pi, pi] and sincosf is within
-// a few ulp, so every joint position is within
-//   delta = reach * (nlinks * (ea + 16u*pi) + 16u*nlinks)
-// of the FP64 forward kinematics (factor 2 of slack included).
-__device__ int arm_valid32(const SceneView& s, const float* q, float ea) {
-    const int nl = s.nlinks;
-    const float R = s.arm_reach;
-    const float delta = 2.f * R * ((float)nl * (ea + 16.f * U32 * PI_F) + 16.f * U32 * (float)nl) + 1e-30f;
-    float x[MPTG_MAX_DIM + 1], y[MPTG_MAX_DIM + 1];
-    float ang = 0.f;
-    x[0] = 0.f; y[0] = 0.f;
-    bool unsure = false;
-    for (int i = 0; i < nl; ++i) {
-        ang += q[i];
-        if (ang > PI_F) ang -= TWO_PI_F;
-        else if (ang < -PI_F) ang += TWO_PI_F;
-        float sn, cs;
-        sincosf(ang, &sn, &cs);
-        float L = __ldg(&s.link32[i]);
-        x[i + 1] = fmaf(L, cs, x[i]);
-        y[i + 1] = fmaf(L, sn, y[i]);
-        for (int k = 0; k < s.ndiscs; ++k) {
-            float4 d = __ldg(&s.discs32[k]);
-            float d2 = dpseg2_32(d.x, d.y, x[i], y[i], x[i + 1], y[i + 1]);
-            float m = 3.f * sqrtf(fmaxf(d2, d.z)) * delta + delta * delta + 8.f * U32 * (d2 + d.z);
-            if (d2 <= d.z - m) return VF_INVALID;
-            if (!(d2 > d.z + m)) unsure = true;
-        }
-    }
-    if (s.self_collision) {
-        // each coordinate within delta: each product of two differences moves by
-        // <= 8 R delta + 4 delta^2, two products, plus FP32 rounding on |.| <= 4R^2
-        const float mo = 16.f * delta * R + 8.f * delta * delta + 32.f * U32 * R * R + 1e-30f;
-        for (int i = 0; i < nl; ++i)
-            for (int j = i + 2; j < nl; ++j) {
-                float ax = x[i], ay = y[i], bx = x[i + 1], by = y[i + 1];
-                float cx = x[j], cy = y[j], dx = x[j + 1], dy = y[j + 1];
-                float o1 = (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
-                float o2 = (bx - ax) * (dy - ay) - (by - ay) * (dx - ax);
-                float o3 = (dx - cx) * (ay - cy) - (dy - cy) * (ax - cx);
-                float o4 = (dx - cx) * (by - cy) - (dy - cy) * (bx - cx);
-                if (fabsf(o1) <= mo || fabsf(o2) <= mo || fabsf(o3) <= mo || fabsf(o4) <= mo) {
-                    unsure = true;
-                    continue;
-                }
-                if ((o1 > 0) != (o2 > 0) && (o3 > 0) != (o4 > 0)) return VF_INVALID;
-            }
-    }
-    return unsure ? VF_UNSURE : VF_VALID;
-}
-
-// exact decision for a state given in FP64 (FP32 filter first)
-__device__ __forceinline__ bool state_valid_f(const SceneView& s, const double* q) {
-    int r;
-    if (s.kind == MPTG_SCENE_GRID) {
-        float x = __double2float_rn(q[0]), y = __double2float_rn(q[1]);
-        float e = 4.f * U32 * (fabsf(x) + fabsf(y) + 1.f);
-        r = (x == x && y == y && fabsf(x) < 1e7f && fabsf(y) < 1e7f) ? grid_valid32(s, x, y, e) : VF_UNSURE;
-    } else {
-        float qf[MPTG_MAX_DIM];
-        float mx = 0.f;
-        bool fin = true;
-        for (int d = 0; d < s.nlinks; ++d) {
-            qf[d] = __double2float_rn(q[d]);
-            mx = fmaxf(mx, fabsf(qf[d]));
-            fin = fin && (qf[d] == qf[d]) && fabsf(qf[d]) < 1e4f;
-        }
-        r = fin ? arm_valid32(s, qf, 2.f * U32 * mx + U32 * PI_F) : VF_UNSURE;
-    }
+// exact decision for a grid state given in FP64 (FP32 filter first)
+__device__ __forceinline__ bool grid_valid_f(const SceneView& s, const double* q) {
+    float x = __double2float_rn(q[0]), y = __double2float_rn(q[1]);
+    float e = 4.f * U32 * (fabsf(x) + fabsf(y) + 1.f);
+    int r = (x == x && y == y && fabsf(x) < 1e7f && fabsf(y) < 1e7f) ? grid_valid32(s, x, y, e) : VF_UNSURE;
     if (r != VF_UNSURE) return r == VF_VALID;
-    return state_valid64(s, q);
+    return grid_valid64(s, q);
 }
 
-__global__ void __launch_bounds__(256) k_states_f(SceneView s, const double* __restrict__ q, int n,
-                                                  uint8_t* __restrict__ out) {
+// Scenario::valid for grid states, thread per state
+__global__ void __launch_bounds__(256) k_grid_states(SceneView s, const double* __restrict__ q, int n,
+                                                     uint8_t* __restrict__ out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double st[MPTG_MAX_DIM];
-    for (int d = 0; d < s.D; ++d) st[d] = q[(size_t)i * s.D + d];
-    out[i] = state_valid_f(s, st) ? 1 : 0;
+    const double st[2] = {q[(size_t)i * 2], q[(size_t)i * 2 + 1]};
+    out[i] = grid_valid_f(s, st) ? 1 : 0;
 }
 
-// step count ceil(m(a, b) * inv) with an FP32 filter: FP64 only when the
-// FP32 value lies within its error bound of an integer
-__device__ __forceinline__ long long edge_steps(const SceneView& s, const double* A, const double* B, double inv,
-                                                int resolution) {
-    const int D = s.D;
-    float m32 = 0.f, err = 0.f;
-    bool fast = true;
-    if (resolution == 1) {
-        for (int i = 0; i < D; ++i) {
-            float ai = __double2float_rn(A[i]), bi = __double2float_rn(B[i]);
-            // the FP32 form assumes angles in [-pi, pi] (no fmod reduction)
-            if (!(fabsf(ai) <= PI_F && fabsf(bi) <= PI_F)) fast = false;
-            float d = fabsf(ai - bi);
-            d = fminf(d, TWO_PI_F - d);
-            m32 = fmaxf(m32, d);
-        }
-        err = 16.f * U32 * PI_F;
-    } else if (s.metric == MPTG_METRIC_L2 && D == 2) {
-        float dx = __double2float_rn(A[0]) - __double2float_rn(B[0]);
-        float dy = __double2float_rn(A[1]) - __double2float_rn(B[1]);
-        m32 = sqrtf(dx * dx + dy * dy);
-        float M = fmaxf(fmaxf(fabsf((float)A[0]), fabsf((float)A[1])), fmaxf(fabsf((float)B[0]), fabsf((float)B[1])));
-        err = 16.f * U32 * (M + m32) + 1e-30f;
-    } else {
-        fast = false;
-    }
-    if (fast && m32 == m32) {
+// grid edge step count ceil(|a - b| * inv) (the L2 metric, dist64) with an
+// FP32 filter: FP64 only when the FP32 value lies within its error bound of
+// an integer
+__device__ __forceinline__ long long grid_edge_steps(const double* A, const double* B, double inv) {
+    float dx = __double2float_rn(A[0]) - __double2float_rn(B[0]);
+    float dy = __double2float_rn(A[1]) - __double2float_rn(B[1]);
+    float m32 = sqrtf(dx * dx + dy * dy);
+    float M = fmaxf(fmaxf(fabsf((float)A[0]), fabsf((float)A[1])), fmaxf(fabsf((float)B[0]), fabsf((float)B[1])));
+    float err = 16.f * U32 * (M + m32) + 1e-30f;
+    if (m32 == m32) {
         float x = m32 * (float)inv;
         float e = err * (float)inv + 4.f * U32 * x;
         float lo = ceilf(x - e), hi = ceilf(x + e);
         if (lo == hi && x < 1e7f) return (long long)lo;
     }
-    double m = resolution == 1 ? linf_so2_64(A, B, D) : dist64(s.metric, D, s.w0, s.w1, A, B);
-    double sd = ceil(__dmul_rn(m, inv));
+    double sd = ceil(__dmul_rn(l2_dist64(A, B, 2), inv));
     if (!(sd >= 0.0) || sd > (double)MPTG_MAX_EDGE_SAMPLES) return -1;
     return (long long)sd;
 }
 
-// phase A, thread per edge: the end state (checked first, as the DMV does),
-// then the step count; edges with interior samples go to the work list
-__global__ void __launch_bounds__(256) k_edges_a(SceneView s, const double* __restrict__ a,
-                                                 const double* __restrict__ b, int n, double inv, int resolution,
-                                                 uint8_t* __restrict__ out, int* __restrict__ work,
-                                                 int* __restrict__ wsteps, int* __restrict__ wcount,
-                                                 unsigned long long* __restrict__ nsamp) {
+// grid phase A, thread per edge: the end state (checked first, as the DMV
+// does), then the step count; edges with interior samples go to the work list
+__global__ void __launch_bounds__(256) k_grid_edges_a(SceneView s, const double* __restrict__ a,
+                                                      const double* __restrict__ b, int n, double inv,
+                                                      uint8_t* __restrict__ out, int* __restrict__ work,
+                                                      int* __restrict__ wsteps, int* __restrict__ wcount,
+                                                      unsigned long long* __restrict__ nsamp) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n) return;
-    const int D = s.D;
-    double A[MPTG_MAX_DIM], B[MPTG_MAX_DIM];
-    for (int d = 0; d < D; ++d) { A[d] = a[(size_t)e * D + d]; B[d] = b[(size_t)e * D + d]; }
+    const double A[2] = {a[(size_t)e * 2], a[(size_t)e * 2 + 1]};
+    const double B[2] = {b[(size_t)e * 2], b[(size_t)e * 2 + 1]};
     if (nsamp) atomicAdd(nsamp, 1ull);
-    if (!state_valid_f(s, B)) { out[e] = 0; return; }
-    long long steps = edge_steps(s, A, B, inv, resolution);
+    if (!grid_valid_f(s, B)) { out[e] = 0; return; }
+    long long steps = grid_edge_steps(A, B, inv);
     if (steps < 0) { out[e] = 0; return; }
     out[e] = 1;
     if (steps >= 2) {
@@ -356,34 +199,26 @@ __global__ void __launch_bounds__(256) k_edges_a(SceneView s, const double* __re
     }
 }
 
-// phase B, warp per surviving edge: interior samples i*delta, 1 <= i < steps,
-// coarse-to-fine (lane j of round r takes sample 1 + j*R + r), FP32 filter
-// per sample with the exact FP64 sample as fallback; ballot early exit
-__global__ void __launch_bounds__(256) k_edges_b(SceneView s, const double* __restrict__ a,
-                                                 const double* __restrict__ b, const int* __restrict__ work,
-                                                 const int* __restrict__ wsteps, const int* __restrict__ wcount,
-                                                 uint8_t* __restrict__ out, unsigned long long* __restrict__ nsamp) {
+// grid phase B, warp per surviving edge: interior samples i*delta,
+// 1 <= i < steps, coarse-to-fine (lane j of round r takes sample 1 + j*R + r),
+// FP32 filter per sample with the exact FP64 sample as fallback; ballot early exit
+__global__ void __launch_bounds__(256) k_grid_edges_b(SceneView s, const double* __restrict__ a,
+                                                      const double* __restrict__ b, const int* __restrict__ work,
+                                                      const int* __restrict__ wsteps, const int* __restrict__ wcount,
+                                                      uint8_t* __restrict__ out, unsigned long long* __restrict__ nsamp) {
     const int lane = threadIdx.x & 31;
     const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     if (w >= *wcount) return;
     const int e = work[w];
     const int steps = wsteps[w];
-    const int D = s.D;
-    double A[MPTG_MAX_DIM], B[MPTG_MAX_DIM];
-    float a32[MPTG_MAX_DIM], dir32[MPTG_MAX_DIM];
-    for (int d = 0; d < D; ++d) {
-        A[d] = a[(size_t)e * D + d];
-        B[d] = b[(size_t)e * D + d];
+    const double A[2] = {a[(size_t)e * 2], a[(size_t)e * 2 + 1]};
+    const double B[2] = {b[(size_t)e * 2], b[(size_t)e * 2 + 1]};
+    float a32[2], dir32[2];
+    for (int d = 0; d < 2; ++d) {
         a32[d] = __double2float_rn(A[d]);
-        if (s.metric == MPTG_METRIC_SO2) {
-            // signed shortest-arc offset of interpolate (src/mpt/so2_space.hpp:44-65);
-            // the wrap of the result is irrelevant to forward kinematics
-            double ccw = so2_ccw64(A[d], B[d]);
-            dir32[d] = __double2float_rn(ccw < MPTG_PI ? ccw : -__dsub_rn(MPTG_TWO_PI, ccw));
-        } else {
-            dir32[d] = __double2float_rn(__dsub_rn(B[d], A[d]));
-        }
+        dir32[d] = __double2float_rn(__dsub_rn(B[d], A[d]));
     }
+    const float eps = 8.f * U32 * (fabsf(a32[0]) + fabsf(a32[1]) + fabsf(dir32[0]) + fabsf(dir32[1]) + 1.f);
     const int M = steps - 1;
     const int R = (M + 31) / 32;
     const double delta = __ddiv_rn(1.0, (double)steps);
@@ -395,24 +230,11 @@ __global__ void __launch_bounds__(256) k_edges_b(SceneView s, const double* __re
         if (k <= M) {
             ++cnt;
             float t = (float)k / (float)steps;
-            int res;
-            if (s.kind == MPTG_SCENE_GRID) {
-                float x = fmaf(dir32[0], t, a32[0]), y = fmaf(dir32[1], t, a32[1]);
-                float e = 8.f * U32 * (fabsf(a32[0]) + fabsf(a32[1]) + fabsf(dir32[0]) + fabsf(dir32[1]) + 1.f);
-                res = grid_valid32(s, x, y, e);
-            } else {
-                float q[MPTG_MAX_DIM];
-                float ea = 0.f;
-                for (int d = 0; d < D; ++d) {
-                    q[d] = fmaf(dir32[d], t, a32[d]);
-                    ea = fmaxf(ea, 8.f * U32 * (fabsf(a32[d]) + 2.f * fabsf(dir32[d])));
-                }
-                res = arm_valid32(s, q, ea + 2.f * U32 * PI_F);
-            }
+            int res = grid_valid32(s, fmaf(dir32[0], t, a32[0]), fmaf(dir32[1], t, a32[1]), eps);
             if (res == VF_UNSURE) {
-                double qs[MPTG_MAX_DIM];
-                interp64(s.metric, D, A, B, __dmul_rn((double)k, delta), qs);
-                v = state_valid64(s, qs);
+                double qs[2];
+                interp64(MPTG_METRIC_L2, 2, A, B, __dmul_rn((double)k, delta), qs);
+                v = grid_valid64(s, qs);
             } else {
                 v = res == VF_VALID;
             }
@@ -424,6 +246,285 @@ __global__ void __launch_bounds__(256) k_edges_b(SceneView s, const double* __re
     }
     if (lane == 0) {
         if (!ok) out[e] = 0;
+        if (nsamp) atomicAdd(nsamp, cnt);
+    }
+}
+
+// ------------------------------------------------------------------ planar arm, warp per state
+// One warp decides one arm state at a time.  Lane j < nlinks owns joint j
+// (its cumulative angle and sincos); every lane then runs the same FMA chain
+// over the shuffled sines and cosines, and lane m keeps joint position m.
+// The (link, disc) pairs are split over the lanes link by link (lane l takes
+// discs l, l+32, ...), the self pairs (i, j >= i+2) likewise, and the warp
+// stops at the first link with a certain collision.  Pairs the FP32 filter
+// cannot decide are re-tested in FP64 on a warp-parallel forward kinematics
+// that reproduces arm_fk64 operation for operation, so the result is exactly
+// arm_valid64's: the state is invalid iff some pair collides in FP64.
+
+#define FULL_MASK 0xffffffffu
+#define ARM_SELF_SLOTS 4  // (16-2)(16-1)/2 = 105 self pairs at most: 4 per lane
+
+struct ArmLane {
+    float L32;       // link length of joint `lane`
+    double L64;
+    float4 d0, d1;   // discs lane and lane + 32 (cx, cy, (r + robot_radius)^2)
+    int si[ARM_SELF_SLOTS], sj[ARM_SELF_SLOTS];  // self pairs lane + 32 c
+    int nself;
+};
+
+__device__ __forceinline__ ArmLane arm_lane(const SceneView& s, int lane) {
+    ArmLane al;
+    al.L32 = lane < s.nlinks ? __ldg(&s.link32[lane]) : 0.f;
+    al.L64 = lane < s.nlinks ? __ldg(&s.link_len64[lane]) : 0.0;
+    al.d0 = lane < s.ndiscs ? __ldg(&s.discs32[lane]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    al.d1 = lane + 32 < s.ndiscs ? __ldg(&s.discs32[lane + 32]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int nl = s.nlinks;
+    al.nself = nl >= 3 ? (nl - 2) * (nl - 1) / 2 : 0;
+#pragma unroll
+    for (int c = 0; c < ARM_SELF_SLOTS; ++c) {
+        int p = lane + 32 * c, i = 0, j = 2;
+        if (p < al.nself) {
+            for (i = 0; i < nl; ++i) {
+                int cnt = nl - 2 - i;
+                if (p < cnt) { j = i + 2 + p; break; }
+                p -= cnt;
+            }
+        } else {
+            i = 0;
+            j = 2;
+        }
+        al.si[c] = i;
+        al.sj[c] = j;
+    }
+    return al;
+}
+
+__device__ __forceinline__ float warp_max_f(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(FULL_MASK, v, o));
+    return v;
+}
+
+// arm_fk64 across the warp: lane m receives joint position m (x64, y64); q64
+// holds joint `lane`'s angle on lanes < nlinks
+__device__ __noinline__ void arm_fk64_warp(const SceneView& s, const ArmLane& al, int lane, double q64,
+                                              double& x64, double& y64) {
+    const int nl = s.nlinks;
+    double angle = 0.0;
+    for (int i = 0; i < nl; ++i) {
+        double qi = __shfl_sync(FULL_MASK, q64, i);
+        if (i <= lane) angle = __dadd_rn(angle, qi);
+    }
+    double sn = 0.0, cs = 0.0;
+    if (lane < nl) mptg_sincos(angle, &sn, &cs);
+    double fx = 0.0, fy = 0.0;
+    x64 = 0.0;
+    y64 = 0.0;
+    for (int i = 0; i < nl; ++i) {
+        double Li = __shfl_sync(FULL_MASK, al.L64, i);
+        fx = __dadd_rn(fx, __dmul_rn(Li, __shfl_sync(FULL_MASK, cs, i)));
+        fy = __dadd_rn(fy, __dmul_rn(Li, __shfl_sync(FULL_MASK, sn, i)));
+        if (lane == i + 1) { x64 = fx; y64 = fy; }
+    }
+}
+
+// One arm state, warp-uniform result.  q32: joint `lane`'s FP32 angle, within
+// ea of the exact one; q64of(): joint `lane`'s exact FP64 angle (evaluated by
+// lanes < nlinks only when some pair needs FP64).  force64 sends every pair
+// to FP64 (inputs outside the range of the FP32 error bound).
+template <class Q64>
+__device__ __forceinline__ bool arm_state_warp(const SceneView& s, const ArmLane& al, int lane, float q32, float ea,
+                                               bool force64, const Q64& q64of) {
+    const int nl = s.nlinks;
+    // FP32 forward kinematics.  The cumulative angle is kept in [-pi, pi] and
+    // sincosf is within a few ulp, so every joint position is within
+    //   delta = reach * (nlinks * (ea + 16u*pi) + 16u*nlinks)
+    // of the FP64 forward kinematics (a factor 2 of slack included).
+    float ang = 0.f;
+    for (int i = 0; i < nl; ++i) {
+        float qi = __shfl_sync(FULL_MASK, q32, i);
+        if (i <= lane) {
+            ang += qi;
+            if (ang > PI_F) ang -= TWO_PI_F;
+            else if (ang < -PI_F) ang += TWO_PI_F;
+        }
+    }
+    float sn, cs;
+    sincosf(ang, &sn, &cs);
+    float xm = 0.f, ym = 0.f;
+    {
+        float x = 0.f, y = 0.f;
+        for (int i = 0; i < nl; ++i) {
+            float Li = __shfl_sync(FULL_MASK, al.L32, i);
+            x = fmaf(Li, __shfl_sync(FULL_MASK, cs, i), x);
+            y = fmaf(Li, __shfl_sync(FULL_MASK, sn, i), y);
+            if (lane == i + 1) { xm = x; ym = y; }
+        }
+    }
+    const float R = s.arm_reach;
+    const float delta = 2.f * R * ((float)nl * (ea + 16.f * U32 * PI_F) + 16.f * U32 * (float)nl) + 1e-30f;
+    bool have64 = false;
+    double x64 = 0.0, y64 = 0.0;
+    const int C = (s.ndiscs + 31) >> 5;
+    for (int i = 0; i < nl; ++i) {
+        const float ax = __shfl_sync(FULL_MASK, xm, i), ay = __shfl_sync(FULL_MASK, ym, i);
+        const float bx = __shfl_sync(FULL_MASK, xm, i + 1), by = __shfl_sync(FULL_MASK, ym, i + 1);
+        for (int c = 0; c < C; ++c) {
+            const int k = lane + 32 * c;
+            int r = VF_VALID;
+            if (k < s.ndiscs) {
+                if (force64) {
+                    r = VF_UNSURE;
+                } else {
+                    float4 d = c == 0 ? al.d0 : (c == 1 ? al.d1 : __ldg(&s.discs32[k]));
+                    float d2 = dpseg2_32(d.x, d.y, ax, ay, bx, by);
+                    float m = 3.f * sqrtf(fmaxf(d2, d.z)) * delta + delta * delta + 8.f * U32 * (d2 + d.z);
+                    r = d2 <= d.z - m ? VF_INVALID : (d2 > d.z + m ? VF_VALID : VF_UNSURE);
+                }
+            }
+            if (__any_sync(FULL_MASK, r == VF_INVALID)) return false;
+            if (__any_sync(FULL_MASK, r == VF_UNSURE)) {
+                if (!have64) {
+                    double q64 = lane < nl ? q64of() : 0.0;
+                    arm_fk64_warp(s, al, lane, q64, x64, y64);
+                    have64 = true;
+                }
+                const double pax = __shfl_sync(FULL_MASK, x64, i), pay = __shfl_sync(FULL_MASK, y64, i);
+                const double pbx = __shfl_sync(FULL_MASK, x64, i + 1), pby = __shfl_sync(FULL_MASK, y64, i + 1);
+                bool hit = false;
+                if (r == VF_UNSURE) {
+                    const double* dk = s.discs64 + 3 * k;
+                    double rr = __dmul_rn(__dadd_rn(dk[2], s.robot_radius), __dadd_rn(dk[2], s.robot_radius));
+                    hit = !(dist_point_segment_sq64(dk[0], dk[1], pax, pay, pbx, pby) > rr);
+                }
+                if (__any_sync(FULL_MASK, hit)) return false;
+            }
+        }
+    }
+    if (s.self_collision && al.nself > 0) {
+        const float mo = 16.f * delta * R + 8.f * delta * delta + 32.f * U32 * R * R + 1e-30f;
+#pragma unroll
+        for (int c = 0; c < ARM_SELF_SLOTS; ++c) {
+            if (32 * c >= al.nself) break;
+            const int i = al.si[c], j = al.sj[c];
+            const float ax = __shfl_sync(FULL_MASK, xm, i), ay = __shfl_sync(FULL_MASK, ym, i);
+            const float bx = __shfl_sync(FULL_MASK, xm, i + 1), by = __shfl_sync(FULL_MASK, ym, i + 1);
+            const float cx = __shfl_sync(FULL_MASK, xm, j), cy = __shfl_sync(FULL_MASK, ym, j);
+            const float dx = __shfl_sync(FULL_MASK, xm, j + 1), dy = __shfl_sync(FULL_MASK, ym, j + 1);
+            int r = VF_VALID;
+            if (lane + 32 * c < al.nself) {
+                if (force64) {
+                    r = VF_UNSURE;
+                } else {
+                    float o1 = (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
+                    float o2 = (bx - ax) * (dy - ay) - (by - ay) * (dx - ax);
+                    float o3 = (dx - cx) * (ay - cy) - (dy - cy) * (ax - cx);
+                    float o4 = (dx - cx) * (by - cy) - (dy - cy) * (bx - cx);
+                    if (fabsf(o1) <= mo || fabsf(o2) <= mo || fabsf(o3) <= mo || fabsf(o4) <= mo) r = VF_UNSURE;
+                    else if ((o1 > 0) != (o2 > 0) && (o3 > 0) != (o4 > 0)) r = VF_INVALID;
+                }
+            }
+            if (__any_sync(FULL_MASK, r == VF_INVALID)) return false;
+            if (__any_sync(FULL_MASK, r == VF_UNSURE)) {
+                if (!have64) {
+                    double q64 = lane < nl ? q64of() : 0.0;
+                    arm_fk64_warp(s, al, lane, q64, x64, y64);
+                    have64 = true;
+                }
+                const double pax = __shfl_sync(FULL_MASK, x64, i), pay = __shfl_sync(FULL_MASK, y64, i);
+                const double pbx = __shfl_sync(FULL_MASK, x64, i + 1), pby = __shfl_sync(FULL_MASK, y64, i + 1);
+                const double pcx = __shfl_sync(FULL_MASK, x64, j), pcy = __shfl_sync(FULL_MASK, y64, j);
+                const double pdx = __shfl_sync(FULL_MASK, x64, j + 1), pdy = __shfl_sync(FULL_MASK, y64, j + 1);
+                bool hit = r == VF_UNSURE && segs_intersect64(pax, pay, pbx, pby, pcx, pcy, pdx, pdy);
+                if (__any_sync(FULL_MASK, hit)) return false;
+            }
+        }
+    }
+    return true;
+}
+
+// a state given in FP64, joint `lane` in qd; the FP32 angles are within
+// 2u|q| + u*pi of it (rounding, plus the wrap); non-finite or huge angles go
+// to FP64 pair by pair
+__device__ __forceinline__ bool arm_state_exact(const SceneView& s, const ArmLane& al, int lane, double qd) {
+    const float q32 = __double2float_rn(qd);
+    const bool fin = lane >= s.nlinks || (q32 == q32 && fabsf(q32) < 1e4f);
+    const float mx = warp_max_f(lane < s.nlinks && fin ? fabsf(q32) : 0.f);
+    const bool force64 = !__all_sync(FULL_MASK, fin);
+    return arm_state_warp(s, al, lane, q32, 2.f * U32 * mx + U32 * PI_F, force64, [&]() { return qd; });
+}
+
+// Scenario::valid for planar-arm states, warp per state
+__global__ void __launch_bounds__(256) k_arm_states(SceneView s, const double* __restrict__ q, int n,
+                                                    uint8_t* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int e = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    if (e >= n) return;
+    const ArmLane al = arm_lane(s, lane);
+    const double qd = lane < s.D ? q[(size_t)e * s.D + lane] : 0.0;
+    const bool ok = arm_state_exact(s, al, lane, qd);
+    if (lane == 0) out[e] = ok ? 1 : 0;
+}
+
+// DMV link for planar-arm edges, warp per edge: the end state first, then the
+// step count (edge_steps' FP64 value, lane per joint), then the interior
+// samples i*delta one at a time in the coarse-to-fine order of k_grid_edges_b
+__global__ void __launch_bounds__(256) k_arm_edges(SceneView s, const double* __restrict__ a,
+                                                   const double* __restrict__ b, int n, double inv, int resolution,
+                                                   uint8_t* __restrict__ out, unsigned long long* __restrict__ nsamp) {
+    const int lane = threadIdx.x & 31;
+    const int e = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    if (e >= n) return;
+    const int D = s.D;
+    const ArmLane al = arm_lane(s, lane);
+    const double Ad = lane < D ? a[(size_t)e * D + lane] : 0.0;
+    const double Bd = lane < D ? b[(size_t)e * D + lane] : 0.0;
+    unsigned long long cnt = 1;
+    bool ok = arm_state_exact(s, al, lane, Bd);
+    long long steps = 0;
+    if (ok) {
+        // ceil(m(a, b) * inv): m = max wrapped joint difference (resolution 1)
+        // or the SO(2)^n distance, summed in joint order as dist64 does
+        const double dd = lane < D ? so2_dist1_64(Ad, Bd) : 0.0;
+        double m = 0.0;
+        if (resolution == 1) {
+            m = dd;
+            for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(FULL_MASK, m, o));
+        } else {
+            for (int i = 0; i < D; ++i) m = __dadd_rn(m, __shfl_sync(FULL_MASK, dd, i));
+        }
+        const double sd = ceil(__dmul_rn(m, inv));
+        if (!(sd >= 0.0) || sd > (double)MPTG_MAX_EDGE_SAMPLES) ok = false;
+        else steps = (long long)sd;
+    }
+    if (ok && steps >= 2) {
+        const float a32 = __double2float_rn(Ad);
+        float dir32 = 0.f;
+        if (lane < D) {
+            // signed shortest-arc offset of interpolate (src/mpt/so2_space.hpp:44-65)
+            double ccw = so2_ccw64(Ad, Bd);
+            dir32 = __double2float_rn(ccw < MPTG_PI ? ccw : -__dsub_rn(MPTG_TWO_PI, ccw));
+        }
+        const bool fin = lane >= D || (a32 == a32 && dir32 == dir32 && fabsf(a32) < 1e4f && fabsf(dir32) < 1e4f);
+        const bool force64 = !__all_sync(FULL_MASK, fin);
+        const float ea = warp_max_f(lane < D && fin ? 8.f * U32 * (fabsf(a32) + 2.f * fabsf(dir32)) : 0.f) +
+                         2.f * U32 * PI_F;
+        const int M = (int)steps - 1;
+        const int R = (M + 31) / 32;
+        const double delta = __ddiv_rn(1.0, (double)steps);
+        for (int r = 0; ok && r < R; ++r) {
+            for (int j = 0; ok && j < 32; ++j) {
+                const int k = 1 + j * R + r;
+                if (k > M) continue;
+                ++cnt;
+                const float t = (float)k / (float)steps;
+                const float q32 = fmaf(dir32, t, a32);
+                ok = arm_state_warp(s, al, lane, q32, ea, force64,
+                                    [&]() { return so2_interp64(Ad, Bd, __dmul_rn((double)k, delta)); });
+            }
+        }
+    }
+    if (lane == 0) {
+        out[e] = ok ? 1 : 0;
         if (nsamp) atomicAdd(nsamp, cnt);
     }
 }
@@ -500,14 +601,21 @@ mptg_status scene_edges_dev(mptg_scene* sc, const double* da, const double* db, 
     EdgeScratch* x = scr ? scr : &sc->scratch;
     if (sc->kind == MPTG_SCENE_RIGID_MESH)
         return mesh_edges_dev(sc, da, db, n, step, resolution, dout, s, nsamp, x);
+    if (sc->kind == MPTG_SCENE_PLANAR_ARM) {
+        k_arm_edges<<<mptg_blocks((size_t)n * 32, 256), 256, 0, s>>>(scene_view(sc), da, db, n, 1.0 / step,
+                                                                     resolution, dout, nsamp);
+        MPTG_LAUNCHED(sc->ctx);
+        return MPTG_OK;
+    }
     mptg_status st = scene_reserve(sc->ctx, x, (size_t)n, s);
     if (st) return st;
     SceneView v = scene_view(sc);
     MPTG_CUDA_TRY(sc->ctx, cudaMemsetAsync(x->wcount, 0, sizeof(int), s));
-    k_edges_a<<<mptg_blocks(n, 128), 128, 0, s>>>(v, da, db, n, 1.0 / step, resolution, dout, x->work, x->wsteps,
-                                                  x->wcount, nsamp);
+    k_grid_edges_a<<<mptg_blocks(n, 128), 128, 0, s>>>(v, da, db, n, 1.0 / step, dout, x->work, x->wsteps,
+                                                       x->wcount, nsamp);
     // one warp per edge that survived phase A (surplus warps exit at once)
-    k_edges_b<<<mptg_blocks((size_t)n * 32, 256), 256, 0, s>>>(v, da, db, x->work, x->wsteps, x->wcount, dout, nsamp);
+    k_grid_edges_b<<<mptg_blocks((size_t)n * 32, 256), 256, 0, s>>>(v, da, db, x->work, x->wsteps, x->wcount, dout,
+                                                                    nsamp);
     sc->ctx->launches += 2;
     return MPTG_OK;
 }
@@ -517,7 +625,10 @@ mptg_status scene_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* d
     if (n <= 0) return MPTG_OK;
     if (sc->kind == MPTG_SCENE_RIGID_MESH) return mesh_states_dev(sc, dq, n, dout, s, scr ? scr : &sc->scratch);
     SceneView v = scene_view(sc);
-    k_states_f<<<mptg_blocks(n, 256), 256, 0, s>>>(v, dq, n, dout);
+    if (sc->kind == MPTG_SCENE_PLANAR_ARM)
+        k_arm_states<<<mptg_blocks((size_t)n * 32, 256), 256, 0, s>>>(v, dq, n, dout);
+    else
+        k_grid_states<<<mptg_blocks(n, 256), 256, 0, s>>>(v, dq, n, dout);
     MPTG_LAUNCHED(sc->ctx);
     return MPTG_OK;
 }
