@@ -34,6 +34,9 @@ sys.path.insert(0, ROOT)
 N_TREE = 1 << 20
 BATCH = 65536
 N_EDGES = 65536
+# DRAM bytes (read + write) per query of k_nearest on the 1M-node tree, from one
+# ncu capture of a 32,768-query launch: 9.344 GB + 48.7 MB
+NN_DRAM_BYTES_PER_QUERY = (9.344e9 + 48.7e6) / 32768
 
 
 def _peaks():
@@ -227,12 +230,12 @@ def learned_vs_plain(ctx, m, torch, seeds=5, cap_s=20.0, n_train=1 << 22, epochs
            "score_states_per_s": len(qt) / score_s,
            "score_tflops": flops_fwd * len(qt) / score_s / 1e12,
            "train_tflops": 3 * flops_fwd * n_train * epochs / train_s / 1e12}
-    for mode in ("plain", "learned"):
+    for mode, points in (("plain", 0), ("learned_new_state", 1), ("learned_edge_4pts", 4)):
         times, solved, checked = [], 0, []
         for s in range(seeds):
             pl = P.Planner(P.Scenario(sc), P.PRRT(P.gpu_wavefront(4096)), seed=1000 + s, ctx=ctx, max_nodes=1 << 21)
-            if mode == "learned":
-                pl.set_surrogate(sg, threshold=2.0)
+            if points:
+                pl.set_surrogate(sg, threshold=2.0, points=points)
             pl.add_start(sc["start"])
             t0 = time.perf_counter()
             pl.solve_for(cap_s, lambda: pl.solved())
@@ -359,6 +362,16 @@ def run_gpu(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     ctx = m.Context(local)
+    if args.edges_only or args.solve_only:
+        # profiling modes: one secondary section alone
+        if args.edges_only:
+            out = {"edge_checks": edge_rates(ctx, m, torch.cuda.current_stream(), torch)}
+        else:
+            out = {"time_to_solve": solve_times(ctx, seeds=args.solve_seeds)}
+        out["gpu_launches"] = ctx.kernel_launches()
+        if rank == 0:
+            print(json.dumps(out))
+        return
     sc, pts = _workload()
     tree = m.Tree(ctx, sc["metric"], sc["dim"], N_TREE)
     t0 = time.perf_counter()
@@ -493,7 +506,10 @@ def run_gpu(args):
                 "e2e": {"value": e2e_val, "unit": "queries/s", "h2d_bytes_per_step": nqb * D * 8,
                         "d2h_bytes_per_step": nqb * 12},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                             "frac": achieved / peak, "traffic": NN_DRAM_BYTES_PER_QUERY * nqb,
+                             "traffic_source": "ncu dram__bytes_read+write of a 32,768-query launch, scaled by "
+                                               "queries (profiles/k_nearest_so2x10_1M.md)",
+                             "peak_source": peak_kind,
                              "kernel": "k_nearest<SO2,16>", "alg_bytes_per_launch": alg_bytes,
                              "counters_per_launch": per_launch},
                 "cpu_baseline": cpu,
@@ -520,6 +536,9 @@ def main():
     ap.add_argument("--no-solve", action="store_true", help="skip the time-to-solve, surrogate and serving runs")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-surrogate comparison")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched serving run")
+    ap.add_argument("--edges-only", action="store_true", help="edge checks/s of the three scenes only (profiling)")
+    ap.add_argument("--solve-only", action="store_true", help="time to solve of the three scenes only (profiling)")
+    ap.add_argument("--solve-seeds", type=int, default=5)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -246,6 +246,10 @@ mptg_status mptg_surrogate_score(mptg_surrogate* surrogate, const double* states
 /* Cull edges whose new state's collision logit exceeds `threshold` before the
  * exact check (they count as rejected); NULL removes the surrogate. */
 mptg_status mptg_planner_set_surrogate(mptg_planner* planner, mptg_surrogate* surrogate, double threshold);
+/* Score `points` states per candidate edge (1 .. 8, default 1): the new state
+ * and interpolate(near, new, j/points) for 1 <= j < points; the edge is culled
+ * when any of them exceeds the threshold. */
+mptg_status mptg_planner_set_surrogate_points(mptg_planner* planner, int points);
 
 /* WorkerStats (prrt.hpp:63-101): [0] wavefronts, [1] samples, [2] nodes
  * added, [3] tree size, [4] goals, [5] states checked by link, [6] seconds in
@@ -276,6 +280,7 @@ typedef struct {
     double time_limit_s;        /* <= 0: none */
     mptg_surrogate* surrogate;  /* NULL: plain planner */
     double surrogate_threshold;
+    int surrogate_points;       /* as mptg_planner_set_surrogate_points (<= 1: the new state only) */
     double* path;               /* optional host buffer of path_cap states */
     size_t path_cap;
 } mptg_query;

@@ -24,7 +24,8 @@ class _Query(ctypes.Structure):
     _fields_ = [("scene", ctypes.c_void_p), ("start", ctypes.c_void_p), ("goal", ctypes.c_void_p),
                 ("goal_radius", ctypes.c_double), ("params", _Params), ("lo", ctypes.c_void_p),
                 ("hi", ctypes.c_void_p), ("time_limit_s", ctypes.c_double), ("surrogate", ctypes.c_void_p),
-                ("surrogate_threshold", ctypes.c_double), ("path", ctypes.c_void_p), ("path_cap", ctypes.c_size_t)]
+                ("surrogate_threshold", ctypes.c_double), ("surrogate_points", ctypes.c_int),
+                ("path", ctypes.c_void_p), ("path_cap", ctypes.c_size_t)]
 
 
 class _Result(ctypes.Structure):
@@ -60,6 +61,7 @@ class Query:
     time_limit: float = 0.0           # seconds, <= 0: none
     surrogate: object | None = None   # mpt_gb300.surrogate.Surrogate
     threshold: float = 0.0
+    surrogate_points: int = 1         # states scored per candidate edge
     path_cap: int = 4096
 
 
@@ -106,6 +108,7 @@ def plan_batch(ctx: Context, queries: list[Query], concurrency: int = 8) -> list
             h = q.surrogate.h
             p.surrogate = h.value if isinstance(h, ctypes.c_void_p) else h
             p.surrogate_threshold = float(q.threshold)
+            p.surrogate_points = int(q.surrogate_points)
         p.path, p.path_cap = path.ctypes.data, q.path_cap
     out = (_Result * len(queries))()
     _check(ctx.h, L.mptg_plan_batch(ctx.h, qs, len(queries), int(concurrency), out))

@@ -51,6 +51,11 @@ struct MeshData {
     BvhNode* robot_leaves = nullptr;  // robot leaves only (AABBs in the robot frame)
     int nrobot = 0, nrleaves = 0;
     double robot_radius = 0.0;     // max |vertex| in the robot frame
+    // FP32 copies for the certified pre-tests (round to nearest of the FP64 data)
+    float* env_tris32 = nullptr;    // [nenv][9]
+    float* robot_tris32 = nullptr;  // [nrobot][9]
+    float env_max = 0.f;            // >= max |coordinate| of the environment
+    float robot_l1 = 0.f;           // >= max |x|+|y|+|z| of a robot vertex
 };
 
 // ------------------------------------------------------------------ host BVH build
@@ -241,8 +246,11 @@ struct MeshView {
     const BvhNode* env_nodes;
     const double* robot_tris;
     const BvhNode* robot_leaves;
+    const float* env_tris32;
+    const float* robot_tris32;
     int nenv, nrleaves;
     float reach;  // robot bounding radius + margin
+    float env_max, robot_l1;
 };
 
 // robot bounding sphere (center p, radius reach) against the environment tree
@@ -287,58 +295,122 @@ __global__ void k_mesh_sphere(MeshView m, const double* __restrict__ q, int n, i
 }
 
 // block per state, thread per robot leaf
-__global__ void __launch_bounds__(256) k_mesh_detail(MeshView m, const double* __restrict__ q, int D,
-                                                     const int* __restrict__ work, const int* __restrict__ nwork,
-                                                     uint8_t* __restrict__ out) {
+// The FP64 decision of one (robot, environment) triangle pair: the robot
+// triangle transformed by (R, P) in the CPU checker's operation order, then
+// Moller's test.  Kept out of line: it is the rare path.
+__device__ __noinline__ bool pair_hits64(const double* R, const double* P, const double* lt, const double* et) {
+    double wt[9];
+    xform64(R, P, lt, wt);
+    xform64(R, P, lt + 3, wt + 3);
+    xform64(R, P, lt + 6, wt + 6);
+    return tri_tri64(wt, et);
+}
+
+// True when the plane of triangle U certainly separates the points V0..V2:
+// every d_i = n.(V_i - U0), n = (U1 - U0) x (U2 - U0), lies beyond its error
+// bound with one sign.  The FP32 coordinates are within eps (per coordinate)
+// of the FP64 coordinates tri_tri64 uses, and X bounds every |coordinate|.
+// Bound (2-norms bounded by the computed L1 norms): the differences move by
+// a = 4 eps + u|.| (perturbation plus rounding), the normal by
+// nu = |e1| a2 + |e2| a1 + a1 a2 + 4u|e1||e2| (perturbation plus the cross
+// product's rounding), each d by |n| w + |w| nu + 2 nu w + 3u|n||w| (the dot
+// product's rounding), plus the FP64 test's own rounding (far below
+// 1e-13 (|e1||e2| + |n|)(X + 1)).  Then every FP64 distance in tri_tri64 has
+// the FP32 sign and none is 0, so the test returns false at this plane.
+__device__ __forceinline__ bool plane_separates32(const float* U, const float* V, float eps, float X) {
+    const float e1x = U[3] - U[0], e1y = U[4] - U[1], e1z = U[5] - U[2];
+    const float e2x = U[6] - U[0], e2y = U[7] - U[1], e2z = U[8] - U[2];
+    const float nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+    const float l1 = fabsf(e1x) + fabsf(e1y) + fabsf(e1z), l2 = fabsf(e2x) + fabsf(e2y) + fabsf(e2z);
+    const float ln = fabsf(nx) + fabsf(ny) + fabsf(nz);
+    const float a1 = 4.f * eps + U32 * l1, a2 = 4.f * eps + U32 * l2;
+    const float nu = l1 * a2 + l2 * a1 + a1 * a2 + 4.f * U32 * l1 * l2;
+    float dmin = INFINITY, dmax = -INFINITY, lw = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float wx = V[3 * i] - U[0], wy = V[3 * i + 1] - U[1], wz = V[3 * i + 2] - U[2];
+        const float d = fmaf(nx, wx, fmaf(ny, wy, nz * wz));
+        dmin = fminf(dmin, d);
+        dmax = fmaxf(dmax, d);
+        lw = fmaxf(lw, fabsf(wx) + fabsf(wy) + fabsf(wz));
+    }
+    const float w = 4.f * eps + U32 * lw;
+    const float E = ((ln + nu) * w + (lw + w) * nu + nu * w + 3.f * U32 * ln * lw +
+                     1e-13f * (l1 * l2 + ln) * (X + 1.f)) * 1.01f + 1e-30f;
+    return dmin > E || dmax < -E;
+}
+
+#define MESH_DETAIL_THREADS 128
+
+// Block per state that the sphere test could not clear, thread per robot
+// leaf (two per thread).  Each thread tests its leaf's world AABB against the
+// environment tree; in an environment leaf each (robot, environment) pair
+// whose boxes overlap is first tried with the certified FP32 separating-plane
+// test (both triangles' planes), and only the pairs it cannot separate run
+// the FP64 test.  The block stops at the first intersection.
+__global__ void __launch_bounds__(MESH_DETAIL_THREADS, 8) k_mesh_detail(MeshView m, const double* __restrict__ q, int D,
+                                                                      const int* __restrict__ work,
+                                                                      const int* __restrict__ nwork,
+                                                                      uint8_t* __restrict__ out) {
     __shared__ double R[9];
     __shared__ double P[3];
+    __shared__ float R32[9], P32[3];
+    __shared__ float eps_s, X_s;
+    __shared__ float tbs[MESH_LEAF][6][MESH_DETAIL_THREADS];  // robot triangle world boxes per thread
     __shared__ volatile int hit;
     const int w = blockIdx.x;
     if (w >= *nwork) return;
     const int i = work[w];
+    const int tid = threadIdx.x;
     const double* s = q + (size_t)i * D;
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
         quat_mat64(s, R);
         P[0] = s[4]; P[1] = s[5]; P[2] = s[6];
+        for (int k = 0; k < 9; ++k) R32[k] = (float)R[k];
+        float pm = 0.f;
+        for (int k = 0; k < 3; ++k) { P32[k] = (float)P[k]; pm = fmaxf(pm, fabsf(P32[k])); }
+        pm = pm * (1.f + 2.f * U32);
+        // FP32 world vertex fma(R, v, P) against xform64: <= u(5|v|_1 + 4|P|);
+        // FP32 environment coordinates: <= u |x|
+        eps_s = fmaxf(6.f * U32 * (m.robot_l1 + pm), U32 * m.env_max) * 1.01f;
+        X_s = fmaxf(m.env_max, m.robot_l1 + pm);
         hit = 0;
     }
     __syncthreads();
-    for (int leaf = threadIdx.x; leaf < m.nrleaves && !hit; leaf += blockDim.x) {
+    const float eps = eps_s, X = X_s;
+    for (int leaf = tid; leaf < m.nrleaves && !hit; leaf += MESH_DETAIL_THREADS) {
         const BvhNode rl = m.robot_leaves[leaf];
         // world AABB of the rotated robot-frame box: center R c + p, half |R| h
-        float c[3], h[3], lo[3], hi[3];
-        for (int d = 0; d < 3; ++d) { c[d] = 0.5f * (rl.lo[d] + rl.hi[d]); h[d] = 0.5f * (rl.hi[d] - rl.lo[d]); }
+        float lo[3], hi[3];
         for (int r = 0; r < 3; ++r) {
-            float cw = (float)P[r], hw = 0.f;
+            float cw = P32[r], hw = 0.f;
             for (int k = 0; k < 3; ++k) {
-                float rv = (float)R[3 * r + k];
-                cw = fmaf(rv, c[k], cw);
-                hw = fmaf(fabsf(rv), h[k], hw);
+                float rv = R32[3 * r + k];
+                cw = fmaf(rv, 0.5f * (rl.lo[k] + rl.hi[k]), cw);
+                hw = fmaf(fabsf(rv), 0.5f * (rl.hi[k] - rl.lo[k]), hw);
             }
             float mg = MESH_MARGIN * (1.f + fabsf(cw) + hw);
             lo[r] = cw - hw - mg;
             hi[r] = cw + hw + mg;
         }
-        // world AABBs of this leaf's robot triangles (FP32 transform, grown by a
-        // margin covering the FP32 rotation and rounding): pair prefilter
+        // world AABBs of this leaf's robot triangles (grown by a margin far
+        // above the FP32 transform's error): the pair prefilter
         const int rcount = -rl.b;
-        float tb[MESH_LEAF][6];
         for (int rt = 0; rt < rcount; ++rt) {
-            const double* lt = m.robot_tris + 9 * (size_t)(rl.a + rt);
-            for (int d = 0; d < 3; ++d) { tb[rt][d] = INFINITY; tb[rt][3 + d] = -INFINITY; }
+            const float* lt = m.robot_tris32 + 9 * (size_t)(rl.a + rt);
+            float bl[3] = {INFINITY, INFINITY, INFINITY}, bh[3] = {-INFINITY, -INFINITY, -INFINITY};
             for (int vtx = 0; vtx < 3; ++vtx) {
-                float v0 = (float)lt[3 * vtx], v1 = (float)lt[3 * vtx + 1], v2 = (float)lt[3 * vtx + 2];
                 for (int r = 0; r < 3; ++r) {
-                    float w = fmaf((float)R[3 * r], v0, fmaf((float)R[3 * r + 1], v1, fmaf((float)R[3 * r + 2], v2,
-                                                                                           (float)P[r])));
-                    tb[rt][r] = fminf(tb[rt][r], w);
-                    tb[rt][3 + r] = fmaxf(tb[rt][3 + r], w);
+                    float wv = fmaf(R32[3 * r], lt[3 * vtx],
+                                    fmaf(R32[3 * r + 1], lt[3 * vtx + 1], fmaf(R32[3 * r + 2], lt[3 * vtx + 2], P32[r])));
+                    bl[r] = fminf(bl[r], wv);
+                    bh[r] = fmaxf(bh[r], wv);
                 }
             }
             for (int d = 0; d < 3; ++d) {
-                float mg = MESH_MARGIN * (1.f + fabsf(tb[rt][d]) + fabsf(tb[rt][3 + d]));
-                tb[rt][d] -= mg;
-                tb[rt][3 + d] += mg;
+                float mg = MESH_MARGIN * (1.f + fabsf(bl[d]) + fabsf(bh[d]));
+                tbs[rt][d][tid] = bl[d] - mg;
+                tbs[rt][3 + d][tid] = bh[d] + mg;
             }
         }
         int stack[MESH_STACK];
@@ -352,27 +424,37 @@ __global__ void __launch_bounds__(256) k_mesh_detail(MeshView m, const double* _
                 if (sp + 2 <= MESH_STACK) { stack[sp++] = nd.a; stack[sp++] = nd.b; }
                 continue;
             }
-            // environment leaf: exact tests of the pairs whose boxes overlap
+            // environment leaf
             for (int e = nd.a; e < nd.a - nd.b && !hit; ++e) {
                 const float* eb = m.env_boxes + 6 * (size_t)e;
-                float elo[3] = {eb[0], eb[1], eb[2]}, ehi[3] = {eb[3], eb[4], eb[5]};
-                const double* et = m.env_tris + 9 * (size_t)e;
+                const float elx = eb[0], ely = eb[1], elz = eb[2], ehx = eb[3], ehy = eb[4], ehz = eb[5];
                 for (int rt = 0; rt < rcount; ++rt) {
-                    if (tb[rt][0] > ehi[0] || tb[rt][3] < elo[0] || tb[rt][1] > ehi[1] || tb[rt][4] < elo[1] ||
-                        tb[rt][2] > ehi[2] || tb[rt][5] < elo[2])
+                    if (tbs[rt][0][tid] > ehx || tbs[rt][3][tid] < elx || tbs[rt][1][tid] > ehy ||
+                        tbs[rt][4][tid] < ely || tbs[rt][2][tid] > ehz || tbs[rt][5][tid] < elz)
                         continue;
-                    const double* lt = m.robot_tris + 9 * (size_t)(rl.a + rt);
-                    double wt[9];
-                    xform64(R, P, lt, wt);
-                    xform64(R, P, lt + 3, wt + 3);
-                    xform64(R, P, lt + 6, wt + 6);
-                    if (tri_tri64(wt, et)) { hit = 1; break; }
+                    float U[9], V[9];
+                    const float* et32 = m.env_tris32 + 9 * (size_t)e;
+                    const float* lt = m.robot_tris32 + 9 * (size_t)(rl.a + rt);
+#pragma unroll
+                    for (int k = 0; k < 9; ++k) U[k] = et32[k];
+#pragma unroll
+                    for (int vtx = 0; vtx < 3; ++vtx)
+#pragma unroll
+                        for (int r = 0; r < 3; ++r)
+                            V[3 * vtx + r] = fmaf(R32[3 * r], lt[3 * vtx],
+                                                  fmaf(R32[3 * r + 1], lt[3 * vtx + 1],
+                                                       fmaf(R32[3 * r + 2], lt[3 * vtx + 2], P32[r])));
+                    if (plane_separates32(V, U, eps, X) || plane_separates32(U, V, eps, X)) continue;
+                    if (pair_hits64(R, P, m.robot_tris + 9 * (size_t)(rl.a + rt), m.env_tris + 9 * (size_t)e)) {
+                        hit = 1;
+                        break;
+                    }
                 }
             }
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0) out[i] = hit ? 0 : 1;
+    if (tid == 0) out[i] = hit ? 0 : 1;
 }
 
 // ------------------------------------------------------------------ edges
@@ -457,8 +539,10 @@ static MeshView mesh_view(const MeshData* md) {
     MeshView v;
     v.env_tris = md->env_tris; v.env_boxes = md->env_boxes; v.env_nodes = md->env_nodes;
     v.robot_tris = md->robot_tris; v.robot_leaves = md->robot_leaves;
+    v.env_tris32 = md->env_tris32; v.robot_tris32 = md->robot_tris32;
     v.nenv = md->nenv; v.nrleaves = md->nrleaves;
     v.reach = (float)md->robot_radius * (1.f + 1e-5f) + MESH_MARGIN;
+    v.env_max = md->env_max; v.robot_l1 = md->robot_l1;
     return v;
 }
 
@@ -503,6 +587,18 @@ mptg_status mesh_scene_create(mptg_ctx* ctx, const mptg_scene_desc* d, mptg_scen
         rad = std::max(rad, std::sqrt(x * x + y * y + z * z));
     }
     md->robot_radius = rad;
+    std::vector<float> env32(env_sorted.size()), rob32(rob_sorted.size());
+    double emax = 0.0, rl1 = 0.0;
+    for (size_t i = 0; i < env_sorted.size(); ++i) {
+        env32[i] = (float)env_sorted[i];
+        emax = std::max(emax, std::fabs(env_sorted[i]));
+    }
+    for (size_t i = 0; i < rob_sorted.size(); ++i) rob32[i] = (float)rob_sorted[i];
+    for (size_t v = 0; v < rob_sorted.size() / 3; ++v)
+        rl1 = std::max(rl1, std::fabs(rob_sorted[3 * v]) + std::fabs(rob_sorted[3 * v + 1]) +
+                                std::fabs(rob_sorted[3 * v + 2]));
+    md->env_max = (float)(emax * (1.0 + 1e-6)) + 1e-6f;
+    md->robot_l1 = (float)(rl1 * (1.0 + 1e-6)) + 1e-6f;
     md->nenv = (int)d->nenv;
     md->nenv_nodes = (int)enodes.size();
     md->nrobot = (int)d->nrobot;
@@ -517,6 +613,8 @@ mptg_status mesh_scene_create(mptg_ctx* ctx, const mptg_scene_desc* d, mptg_scen
     up((void**)&md->env_nodes, enodes.data(), enodes.size() * sizeof(BvhNode));
     up((void**)&md->robot_tris, rob_sorted.data(), rob_sorted.size() * sizeof(double));
     up((void**)&md->robot_leaves, rleaves.data(), rleaves.size() * sizeof(BvhNode));
+    up((void**)&md->env_tris32, env32.data(), env32.size() * sizeof(float));
+    up((void**)&md->robot_tris32, rob32.data(), rob32.size() * sizeof(float));
     if (e != cudaSuccess) {
         cudaGetLastError();
         return mptg_fail(ctx, MPTG_ERR_OOM, "mesh scene allocation failed: %s", cudaGetErrorString(e));
@@ -527,7 +625,8 @@ mptg_status mesh_scene_create(mptg_ctx* ctx, const mptg_scene_desc* d, mptg_scen
 void mesh_scene_free(mptg_scene* s) {
     MeshData* md = s->mesh;
     if (!md) return;
-    void* ptrs[] = {md->env_tris, md->env_boxes, md->env_nodes, md->robot_tris, md->robot_leaves};
+    void* ptrs[] = {md->env_tris, md->env_boxes, md->env_nodes, md->robot_tris, md->robot_leaves, md->env_tris32,
+                    md->robot_tris32};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete md;
@@ -571,7 +670,7 @@ mptg_status mesh_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* do
     int nw = x->hbuf[0];
     if (nw > 0) {
         // one block per state that the sphere test could not clear
-        k_mesh_detail<<<nw, 256, 0, s>>>(v, dq, sc->D, x->mwork, x->nwork, dout);
+        k_mesh_detail<<<nw, MESH_DETAIL_THREADS, 0, s>>>(v, dq, sc->D, x->mwork, x->nwork, dout);
         MPTG_LAUNCHED(ctx);
     }
     MPTG_CUDA_TRY(ctx, cudaGetLastError());

@@ -81,6 +81,9 @@ struct mptg_planner {
     uint8_t* ok_c = nullptr;
     uint8_t* keep = nullptr;
     uint64_t stat_culled = 0;
+    int sg_points = 1;          // states scored per candidate edge
+    double* sg_pts = nullptr;   // [sg_points][cap_wave][D] when sg_points > 1
+    int sg_pts_cap = 1;         // sg_points the logits/sg_pts buffers hold
     // every call of this planner runs on its own non-blocking stream, with its
     // own validity scratch, so planners on one scene can run concurrently
     cudaStream_t stream = nullptr;
@@ -238,11 +241,31 @@ __global__ void k_plan_scatter(PlanView p, int W, const int* __restrict__ scan, 
 }
 
 // surrogate culling: flag the edges that go to the exact check
-__global__ void k_plan_keep(int W, const uint8_t* __restrict__ skip, const float* __restrict__ logit, float thr,
+// the states the surrogate scores for each candidate edge (near -> new): the
+// new state first, then interpolate(near, new, j/P) for 1 <= j < P; layout
+// [j][W][D] so that pts[0] is the new-state block
+__global__ void k_plan_edge_points(PlanView p, int W, int P, const double* __restrict__ nearst,
+                                   const double* __restrict__ newst, double* __restrict__ pts) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W * (P - 1)) return;
+    const int e = i % W, j = 1 + i / W;
+    const int D = p.D;
+    double a[MPTG_MAX_DIM], b[MPTG_MAX_DIM], q[MPTG_MAX_DIM];
+    for (int k = 0; k < D; ++k) { a[k] = nearst[(size_t)e * D + k]; b[k] = newst[(size_t)e * D + k]; }
+    interp64(p.metric, D, a, b, __ddiv_rn((double)j, (double)P), q);
+    double* out = pts + ((size_t)j * W + e) * D;
+    for (int k = 0; k < D; ++k) out[k] = q[k];
+}
+
+// an edge goes to the exact check unless skipped or some scored point's
+// collision logit exceeds thr (logits [P][W])
+__global__ void k_plan_keep(int W, int P, const uint8_t* __restrict__ skip, const float* __restrict__ logit, float thr,
                             uint8_t* __restrict__ keep, uint8_t* __restrict__ ok) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= W) return;
-    keep[i] = (!skip[i] && !(logit[i] > thr)) ? 1 : 0;
+    bool cull = false;
+    for (int j = 0; j < P; ++j) cull = cull || logit[(size_t)j * W + i] > thr;
+    keep[i] = (!skip[i] && !cull) ? 1 : 0;
     ok[i] = 0;
 }
 
@@ -318,7 +341,7 @@ static PlanView plan_view(const mptg_planner* p) {
 static void planner_free(mptg_planner* p) {
     void* ptrs[] = {p->lo, p->hi, p->goal, p->parent, p->samp, p->nidx, p->ndist, p->nearst, p->newst, p->skip,
                     p->ok, p->scan, p->bsum, p->acc_states, p->acc_parent, p->acc_goal, p->nsamp, p->logits,
-                    p->near_c, p->new_c, p->cmap, p->ok_c, p->keep, p->path_ids, p->path_out};
+                    p->near_c, p->new_c, p->cmap, p->ok_c, p->keep, p->path_ids, p->path_out, p->sg_pts};
     if (p->stream) cudaStreamSynchronize(p->stream);
     for (void* x : ptrs)
         if (x) cudaFree(x);
@@ -415,9 +438,17 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
         {
             // the surrogate's activation buffers are shared between planners:
             // hold it until this stream has consumed its logits
+            const int P = p->sg_points;
+            if (P > 1) {
+                MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->sg_pts, p->newst, (size_t)W * p->D * sizeof(double),
+                                                   cudaMemcpyDeviceToDevice, s));
+                k_plan_edge_points<<<mptg_blocks((size_t)W * (P - 1), 128), 128, 0, s>>>(v, W, P, p->nearst, p->newst,
+                                                                                         p->sg_pts);
+                MPTG_LAUNCHED(ctx);
+            }
             std::lock_guard<std::mutex> lock(*mptg_surrogate_mutex(p->sg));
-            if ((st = mptg_surrogate_score_dev(p->sg, p->newst, W, p->logits, s))) return st;
-            k_plan_keep<<<mptg_blocks(W, 256), 256, 0, s>>>(W, p->skip, p->logits, p->sg_thr, p->keep, p->ok);
+            if ((st = mptg_surrogate_score_dev(p->sg, P > 1 ? p->sg_pts : p->newst, W * P, p->logits, s))) return st;
+            k_plan_keep<<<mptg_blocks(W, 256), 256, 0, s>>>(W, P, p->skip, p->logits, p->sg_thr, p->keep, p->ok);
             k_plan_scan<<<nblk, PLAN_SCAN_BLOCK, 0, s>>>(W, p->keep, p->skip, p->scan, p->bsum);
             k_plan_scan_top<<<1, 1024, 0, s>>>(nblk, p->bsum);
             k_plan_cgather<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->scan, p->bsum, p->nearst, p->newst,
@@ -680,15 +711,17 @@ mptg_status mptg_planner_graph(mptg_planner* p, double* states, int32_t* parents
 
 mptg_status mptg_planner_set_surrogate(mptg_planner* p, mptg_surrogate* sg, double threshold) {
     if (!p) return MPTG_ERR_INVALID_ARG;
-    if (sg && !p->logits) {
+    if (sg && (!p->logits || !p->near_c)) {
         const size_t W = p->cap_wave, D = p->D;
         cudaError_t e = cudaSuccess;
-        if (e == cudaSuccess) e = cudaMalloc((void**)&p->logits, W * sizeof(float));
-        if (e == cudaSuccess) e = cudaMalloc((void**)&p->near_c, W * D * sizeof(double));
-        if (e == cudaSuccess) e = cudaMalloc((void**)&p->new_c, W * D * sizeof(double));
-        if (e == cudaSuccess) e = cudaMalloc((void**)&p->cmap, W * sizeof(int));
-        if (e == cudaSuccess) e = cudaMalloc((void**)&p->ok_c, W);
-        if (e == cudaSuccess) e = cudaMalloc((void**)&p->keep, W);
+        if (!p->logits) e = cudaMalloc((void**)&p->logits, W * p->sg_pts_cap * sizeof(float));
+        if (!p->near_c) {
+            if (e == cudaSuccess) e = cudaMalloc((void**)&p->near_c, W * D * sizeof(double));
+            if (e == cudaSuccess) e = cudaMalloc((void**)&p->new_c, W * D * sizeof(double));
+            if (e == cudaSuccess) e = cudaMalloc((void**)&p->cmap, W * sizeof(int));
+            if (e == cudaSuccess) e = cudaMalloc((void**)&p->ok_c, W);
+            if (e == cudaSuccess) e = cudaMalloc((void**)&p->keep, W);
+        }
         if (e != cudaSuccess) {
             cudaGetLastError();
             return mptg_fail(p->ctx, MPTG_ERR_OOM, "surrogate buffers: %s", cudaGetErrorString(e));
@@ -696,6 +729,29 @@ mptg_status mptg_planner_set_surrogate(mptg_planner* p, mptg_surrogate* sg, doub
     }
     p->sg = sg;
     p->sg_thr = (float)threshold;
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_set_surrogate_points(mptg_planner* p, int points) {
+    if (!p) return MPTG_ERR_INVALID_ARG;
+    if (points < 1 || points > 8) return mptg_fail(p->ctx, MPTG_ERR_INVALID_ARG, "surrogate points must be in [1, 8]");
+    if (points > p->sg_pts_cap) {
+        const size_t W = p->cap_wave, D = p->D;
+        MPTG_CUDA_TRY(p->ctx, cudaStreamSynchronize(p->stream));
+        cudaFree(p->logits);
+        cudaFree(p->sg_pts);
+        p->logits = nullptr;
+        p->sg_pts = nullptr;
+        p->sg_pts_cap = 0;
+        cudaError_t e = cudaMalloc((void**)&p->logits, W * points * sizeof(float));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&p->sg_pts, W * points * D * sizeof(double));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return mptg_fail(p->ctx, MPTG_ERR_OOM, "surrogate point buffers: %s", cudaGetErrorString(e));
+        }
+        p->sg_pts_cap = points;
+    }
+    p->sg_points = points;
     return MPTG_OK;
 }
 
@@ -740,6 +796,7 @@ static mptg_status batch_query(mptg_ctx* ctx, const mptg_query& q, const BatchCa
     }
     if ((st = planner_reset(p, &q.params, true, q.lo, q.hi))) return st;
     if ((st = mptg_planner_set_surrogate(p, q.surrogate, q.surrogate_threshold))) return st;
+    if ((st = mptg_planner_set_surrogate_points(p, q.surrogate ? std::max(1, q.surrogate_points) : 1))) return st;
     if ((st = mptg_planner_add_start(p, q.start))) return st;
     if ((st = mptg_planner_set_goal(p, q.goal, q.goal_radius))) return st;
     const auto t = std::chrono::steady_clock::now();

@@ -24,6 +24,8 @@
 // sin/cos of mptg_detmath.h, the same expressions the CPU checker evaluates.
 #include "metrics.cuh"
 #include "scene.cuh"
+#include <algorithm>
+#include <vector>
 
 // ------------------------------------------------------------------ grid
 __device__ __forceinline__ bool grid_valid64(const SceneView& s, const double* q) {
@@ -335,10 +337,18 @@ template <class Q64>
 __device__ __forceinline__ bool arm_state_warp(const SceneView& s, const ArmLane& al, int lane, float q32, float ea,
                                                bool force64, const Q64& q64of) {
     const int nl = s.nlinks;
-    // FP32 forward kinematics.  The cumulative angle is kept in [-pi, pi] and
-    // sincosf is within a few ulp, so every joint position is within
-    //   delta = reach * (nlinks * (ea + 16u*pi) + 16u*nlinks)
-    // of the FP64 forward kinematics (a factor 2 of slack included).
+    // FP32 forward kinematics.  Error bound against the FP64 kinematics
+    // (arm_fk64 on the exact angles), with u = 2^-24 and joint angles within
+    // ea of the exact ones, |q32| <= 2pi (the callers send larger inputs to
+    // FP64):
+    //  * cumulative angle: |ang| <= pi before each add, so |ang + q| <= 3pi and
+    //    the add rounds by <= 3u*pi; the wrap subtracts TWO_PI_F exactly
+    //    (Sterbenz) and TWO_PI_F is within u*pi of 2pi; after i joints the
+    //    angle is within i*(ea + 4u*pi) of the exact one (mod 2pi);
+    //  * sincosf is within 2 ulp (<= 4u) of sin/cos of its argument;
+    //  * each FMA position step adds <= u*reach (rounding) + u*L (FP32 link).
+    // So every joint position is within
+    //   R*(nlinks*(ea + 5u*pi) + 5u) + nlinks*u*R  <=  delta / 2.
     float ang = 0.f;
     for (int i = 0; i < nl; ++i) {
         float qi = __shfl_sync(FULL_MASK, q32, i);
@@ -361,7 +371,10 @@ __device__ __forceinline__ bool arm_state_warp(const SceneView& s, const ArmLane
         }
     }
     const float R = s.arm_reach;
-    const float delta = 2.f * R * ((float)nl * (ea + 16.f * U32 * PI_F) + 16.f * U32 * (float)nl) + 1e-30f;
+    const float delta = 2.f * R * ((float)nl * (ea + 5.f * U32 * PI_F) + (float)(nl + 5) * U32) + 1e-30f;
+    // the disc test's FP32 evaluation (coordinates of magnitude <= arm_span)
+    // rounds like a further perturbation of the points by <= 8u*arm_span
+    const float dd = delta + 8.f * U32 * s.arm_span;
     bool have64 = false;
     double x64 = 0.0, y64 = 0.0;
     const int C = (s.ndiscs + 31) >> 5;
@@ -377,7 +390,8 @@ __device__ __forceinline__ bool arm_state_warp(const SceneView& s, const ArmLane
                 } else {
                     float4 d = c == 0 ? al.d0 : (c == 1 ? al.d1 : __ldg(&s.discs32[k]));
                     float d2 = dpseg2_32(d.x, d.y, ax, ay, bx, by);
-                    float m = 3.f * sqrtf(fmaxf(d2, d.z)) * delta + delta * delta + 8.f * U32 * (d2 + d.z);
+                    // the distance moves by <= dd, so d^2 by <= 2*d*dd + dd^2
+                    float m = 3.f * sqrtf(fmaxf(d2, d.z)) * dd + dd * dd + 8.f * U32 * (d2 + d.z);
                     r = d2 <= d.z - m ? VF_INVALID : (d2 > d.z + m ? VF_VALID : VF_UNSURE);
                 }
             }
@@ -419,8 +433,21 @@ __device__ __forceinline__ bool arm_state_warp(const SceneView& s, const ArmLane
                     float o2 = (bx - ax) * (dy - ay) - (by - ay) * (dx - ax);
                     float o3 = (dx - cx) * (ay - cy) - (dy - cy) * (ax - cx);
                     float o4 = (dx - cx) * (by - cy) - (dy - cy) * (bx - cx);
-                    if (fabsf(o1) <= mo || fabsf(o2) <= mo || fabsf(o3) <= mo || fabsf(o4) <= mo) r = VF_UNSURE;
-                    else if ((o1 > 0) != (o2 > 0) && (o3 > 0) != (o4 > 0)) r = VF_INVALID;
+                    const bool c12 = fabsf(o1) > mo && fabsf(o2) > mo, c34 = fabsf(o3) > mo && fabsf(o4) > mo;
+                    if (c12 && c34) {
+                        // every FP64 orientation has the FP32 sign and none is 0
+                        r = ((o1 > 0) != (o2 > 0) && (o3 > 0) != (o4 > 0)) ? VF_INVALID : VF_VALID;
+                    } else {
+                        // Bounding boxes apart by more than 2*delta stay apart in
+                        // FP64, so none of segs_intersect64's collinear cases can
+                        // fire; then one certain same-sign pair of orientations
+                        // rules out its proper crossing.
+                        const float g = 2.f * delta;
+                        const bool apart = fmaxf(ax, bx) + g < fminf(cx, dx) || fmaxf(cx, dx) + g < fminf(ax, bx) ||
+                                           fmaxf(ay, by) + g < fminf(cy, dy) || fmaxf(cy, dy) + g < fminf(ay, by);
+                        r = (apart && ((c12 && (o1 > 0) == (o2 > 0)) || (c34 && (o3 > 0) == (o4 > 0)))) ? VF_VALID
+                                                                                                       : VF_UNSURE;
+                    }
                 }
             }
             if (__any_sync(FULL_MASK, r == VF_INVALID)) return false;
@@ -447,7 +474,7 @@ __device__ __forceinline__ bool arm_state_warp(const SceneView& s, const ArmLane
 // to FP64 pair by pair
 __device__ __forceinline__ bool arm_state_exact(const SceneView& s, const ArmLane& al, int lane, double qd) {
     const float q32 = __double2float_rn(qd);
-    const bool fin = lane >= s.nlinks || (q32 == q32 && fabsf(q32) < 1e4f);
+    const bool fin = lane >= s.nlinks || fabsf(q32) <= 4.f;  // false for NaN
     const float mx = warp_max_f(lane < s.nlinks && fin ? fabsf(q32) : 0.f);
     const bool force64 = !__all_sync(FULL_MASK, fin);
     return arm_state_warp(s, al, lane, q32, 2.f * U32 * mx + U32 * PI_F, force64, [&]() { return qd; });
@@ -504,10 +531,11 @@ __global__ void __launch_bounds__(256) k_arm_edges(SceneView s, const double* __
             double ccw = so2_ccw64(Ad, Bd);
             dir32 = __double2float_rn(ccw < MPTG_PI ? ccw : -__dsub_rn(MPTG_TWO_PI, ccw));
         }
-        const bool fin = lane >= D || (a32 == a32 && dir32 == dir32 && fabsf(a32) < 1e4f && fabsf(dir32) < 1e4f);
+        // q32 = fma(dir32, t, a32) is within u(|a| + 2|dir| + |q|) <= u(2|a| + 3|dir|)
+        // of the exact sample (FP32 rounding of a, dir and t, then the FMA)
+        const bool fin = lane >= D || (fabsf(a32) <= 3.1416f && fabsf(dir32) <= 3.1416f);
         const bool force64 = !__all_sync(FULL_MASK, fin);
-        const float ea = warp_max_f(lane < D && fin ? 8.f * U32 * (fabsf(a32) + 2.f * fabsf(dir32)) : 0.f) +
-                         2.f * U32 * PI_F;
+        const float ea = warp_max_f(lane < D && fin ? 4.f * U32 * (fabsf(a32) + fabsf(dir32)) : 0.f);
         const int M = (int)steps - 1;
         const int R = (M + 31) / 32;
         const double delta = __ddiv_rn(1.0, (double)steps);
@@ -556,7 +584,7 @@ SceneView scene_view(const mptg_scene* s) {
     v.grid = s->grid; v.width = s->width; v.height = s->height;
     v.nlinks = s->nlinks; v.link_len64 = s->link_len64; v.ndiscs = s->ndiscs; v.discs64 = s->discs64;
     v.robot_radius = s->robot_radius; v.self_collision = s->self_collision;
-    v.discs32 = s->discs32; v.link32 = s->link32; v.arm_reach = s->arm_reach;
+    v.discs32 = s->discs32; v.link32 = s->link32; v.arm_reach = s->arm_reach; v.arm_span = s->arm_span;
     mesh_fill_view(s, &v);
     return v;
 }
@@ -573,6 +601,9 @@ static cudaError_t scene_make_f32(mptg_scene* s, const mptg_scene_desc* d) {
     double reach = 0;
     for (int i = 0; i < d->nlinks; ++i) { ll[i] = (float)d->link_len[i]; reach += fabs(d->link_len[i]); }
     s->arm_reach = (float)(reach * (1.0 + 1e-6)) + 1e-6f;
+    double cmax = 0;
+    for (int k = 0; k < d->ndiscs; ++k) cmax = std::max(cmax, fabs(d->discs[3 * k]) + fabs(d->discs[3 * k + 1]));
+    s->arm_span = (float)((2.0 * reach + cmax) * (1.0 + 1e-6)) + 1e-6f;
     cudaError_t e = cudaMalloc((void**)&s->discs32, dc.size() * sizeof(float4));
     if (e == cudaSuccess) e = cudaMemcpy(s->discs32, dc.data(), dc.size() * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc((void**)&s->link32, ll.size() * sizeof(float));

@@ -47,6 +47,7 @@ struct mptg_scene {
     float4* discs32 = nullptr;
     float* link32 = nullptr;
     float arm_reach = 0.f;
+    float arm_span = 0.f;  // bound on |x| + |y| of joint positions and disc centres
     // scratch of the C-ABI validity calls on this scene
     EdgeScratch scratch;
 };
@@ -64,6 +65,7 @@ struct SceneView {
     const float4* discs32;
     const float* link32;
     float arm_reach;
+    float arm_span;
     // rigid mesh (see mesh.cu)
     const double* robot_tris;   // [nrobot][9]
     int nrobot;

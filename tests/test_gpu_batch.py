@@ -26,7 +26,7 @@ def _single(ctx, q):
     pl = P.Planner(q.scenario, P.PRRT(P.gpu_wavefront(q.wavefront)), seed=q.seed, ctx=ctx, max_nodes=q.max_nodes)
     pl.set_goal_bias(q.goal_bias)
     if q.surrogate is not None:
-        pl.set_surrogate(q.surrogate, q.threshold)
+        pl.set_surrogate(q.surrogate, q.threshold, q.surrogate_points)
     pl.add_start(q.start)
     pl.run(0, 0.0, True)
     st = pl.stats()
@@ -38,7 +38,7 @@ def _single(ctx, q):
     return out
 
 
-def _queries(three, n, seed0, surrogate=None):
+def _queries(three, n, seed0, surrogate=None, points=1):
     from mpt_gb300 import planner as P
     from mpt_gb300.batch import Query
     sc = {k: P.Scenario(v) for k, v in three.items()}
@@ -50,7 +50,7 @@ def _queries(three, n, seed0, surrogate=None):
         k = kinds[i % 3]
         qs.append(Query(sc[k], three[k]["start"], seed=seed0 + i, max_nodes=budgets[k][(i // 3) % 2],
                         wavefront=waves[k], goal_bias=0.05, surrogate=surrogate if k == "mesh" else None,
-                        threshold=0.0))
+                        threshold=0.0, surrogate_points=points))
     return qs
 
 
@@ -80,10 +80,11 @@ def test_batch_with_surrogate_equals_single(ctx, three):
     from mpt_gb300.surrogate import Surrogate, se3_normalisation
     scale, shift = se3_normalisation(three["mesh"]["lo"], three["mesh"]["hi"])
     sg = Surrogate(ctx, 7, scale, shift, seed=3)
-    qs = _queries(three, 9, 500, surrogate=sg)
-    res = plan_batch(ctx, qs, concurrency=6)
-    for q, r in zip(qs, res):
-        _same(r, _single(ctx, q))
+    for points in (1, 3):
+        qs = _queries(three, 9, 500, surrogate=sg, points=points)
+        res = plan_batch(ctx, qs, concurrency=6)
+        for q, r in zip(qs, res):
+            _same(r, _single(ctx, q))
 
 
 def test_batch_path_is_a_chain_of_the_oracle_tree(ctx, orc, three):
