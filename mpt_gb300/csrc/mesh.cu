@@ -341,13 +341,81 @@ __device__ __forceinline__ bool plane_separates32(const float* U, const float* V
 }
 
 #define MESH_DETAIL_THREADS 128
+#define MESH_CAND 512   // environment leaves within the robot's bounding sphere
+#define MESH_FRONT 512  // breadth-first frontier of that sweep
+#define MESH_QUEUE 512  // (robot leaf, environment leaf) pairs per round
+static_assert(MESH_LEAF == 8, "k_mesh_detail spreads 8 x 8 triangle pairs per leaf pair");
 
-// Block per state that the sphere test could not clear, thread per robot
-// leaf (two per thread).  Each thread tests its leaf's world AABB against the
-// environment tree; in an environment leaf each (robot, environment) pair
-// whose boxes overlap is first tried with the certified FP32 separating-plane
-// test (both triangles' planes), and only the pairs it cannot separate run
-// the FP64 test.  The block stops at the first intersection.
+// The robot triangle `lt` (robot frame, FP32) placed at (R32, P32) in FP32.
+__device__ __forceinline__ void robot_tri32(const float* R32, const float* P32, const float* lt, float* V) {
+#pragma unroll
+    for (int vtx = 0; vtx < 3; ++vtx)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+            V[3 * vtx + r] = fmaf(R32[3 * r], lt[3 * vtx],
+                                  fmaf(R32[3 * r + 1], lt[3 * vtx + 1], fmaf(R32[3 * r + 2], lt[3 * vtx + 2], P32[r])));
+}
+
+// One (robot triangle ri, environment triangle ei) pair: the world box of the
+// FP32 robot triangle (grown by a margin far above the transform's error)
+// against the environment triangle's box, then the certified FP32
+// separating-plane tests, and only then the FP64 test.
+__device__ __forceinline__ bool pair_hits(const MeshView& m, const double* R, const double* P, const float* R32,
+                                          const float* P32, float eps, float X, int ri, int ei) {
+    float V[9];
+    robot_tri32(R32, P32, m.robot_tris32 + 9 * (size_t)ri, V);
+    const float* eb = m.env_boxes + 6 * (size_t)ei;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        float lo = fminf(V[d], fminf(V[3 + d], V[6 + d])), hi = fmaxf(V[d], fmaxf(V[3 + d], V[6 + d]));
+        float mg = MESH_MARGIN * (1.f + fabsf(lo) + fabsf(hi));
+        if (lo - mg > eb[3 + d] || hi + mg < eb[d]) return false;
+    }
+    float U[9];
+    const float* et = m.env_tris32 + 9 * (size_t)ei;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) U[k] = et[k];
+    if (plane_separates32(V, U, eps, X) || plane_separates32(U, V, eps, X)) return false;
+    return pair_hits64(R, P, m.robot_tris + 9 * (size_t)ri, m.env_tris + 9 * (size_t)ei);
+}
+
+__device__ __forceinline__ bool sphere_box(const float* p, float r, const BvhNode& nd) {
+    float d2 = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        float o = fmaxf(fmaxf(nd.lo[d] - p[d], p[d] - nd.hi[d]), 0.f);
+        d2 = fmaf(o, o, d2);
+    }
+    return d2 <= r * r;
+}
+
+// world AABB of robot leaf rl at (R32, P32): center R c + p, half |R| h, grown
+__device__ __forceinline__ void robot_leaf_box(const BvhNode& rl, const float* R32, const float* P32, float* lo,
+                                               float* hi) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        float cw = P32[r], hw = 0.f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            float rv = R32[3 * r + k];
+            cw = fmaf(rv, 0.5f * (rl.lo[k] + rl.hi[k]), cw);
+            hw = fmaf(fabsf(rv), 0.5f * (rl.hi[k] - rl.lo[k]), hw);
+        }
+        float mg = MESH_MARGIN * (1.f + fabsf(cw) + hw);
+        lo[r] = cw - hw - mg;
+        hi[r] = cw + hw + mg;
+    }
+}
+
+// Block per state that the sphere test could not clear.
+//  1. The block sweeps the environment tree breadth first for the leaves whose
+//     boxes meet the robot's bounding sphere (candidates, in shared memory).
+//  2. Thread t takes robot leaf t (of each chunk of 128) and queues the
+//     (robot leaf, candidate) pairs whose boxes overlap.
+//  3. The 64 triangle pairs of every queued leaf pair are spread over the
+//     whole block: triangle box test, certified FP32 separating planes, FP64.
+// The block stops at the first intersection.  More candidates than fit
+// (MESH_CAND / MESH_FRONT) fall back to a per-thread depth-first walk.
 __global__ void __launch_bounds__(MESH_DETAIL_THREADS, 8) k_mesh_detail(MeshView m, const double* __restrict__ q, int D,
                                                                       const int* __restrict__ work,
                                                                       const int* __restrict__ nwork,
@@ -356,7 +424,12 @@ __global__ void __launch_bounds__(MESH_DETAIL_THREADS, 8) k_mesh_detail(MeshView
     __shared__ double P[3];
     __shared__ float R32[9], P32[3];
     __shared__ float eps_s, X_s;
-    __shared__ float tbs[MESH_LEAF][6][MESH_DETAIL_THREADS];  // robot triangle world boxes per thread
+    __shared__ int front[2][MESH_FRONT];
+    __shared__ int nfront[2];
+    __shared__ int cand[MESH_CAND];
+    __shared__ float cbox[6][MESH_CAND];
+    __shared__ int ncand, overflow, nq;
+    __shared__ int qra[MESH_QUEUE], qrc[MESH_QUEUE], qea[MESH_QUEUE], qec[MESH_QUEUE];
     __shared__ volatile int hit;
     const int w = blockIdx.x;
     if (w >= *nwork) return;
@@ -374,83 +447,117 @@ __global__ void __launch_bounds__(MESH_DETAIL_THREADS, 8) k_mesh_detail(MeshView
         // FP32 environment coordinates: <= u |x|
         eps_s = fmaxf(6.f * U32 * (m.robot_l1 + pm), U32 * m.env_max) * 1.01f;
         X_s = fmaxf(m.env_max, m.robot_l1 + pm);
+        front[0][0] = 0;
+        nfront[0] = m.nenv > 0 ? 1 : 0;
+        nfront[1] = 0;
+        ncand = 0;
+        overflow = 0;
+        nq = 0;
         hit = 0;
     }
     __syncthreads();
     const float eps = eps_s, X = X_s;
-    for (int leaf = tid; leaf < m.nrleaves && !hit; leaf += MESH_DETAIL_THREADS) {
-        const BvhNode rl = m.robot_leaves[leaf];
-        // world AABB of the rotated robot-frame box: center R c + p, half |R| h
-        float lo[3], hi[3];
-        for (int r = 0; r < 3; ++r) {
-            float cw = P32[r], hw = 0.f;
-            for (int k = 0; k < 3; ++k) {
-                float rv = R32[3 * r + k];
-                cw = fmaf(rv, 0.5f * (rl.lo[k] + rl.hi[k]), cw);
-                hw = fmaf(fabsf(rv), 0.5f * (rl.hi[k] - rl.lo[k]), hw);
-            }
-            float mg = MESH_MARGIN * (1.f + fabsf(cw) + hw);
-            lo[r] = cw - hw - mg;
-            hi[r] = cw + hw + mg;
-        }
-        // world AABBs of this leaf's robot triangles (grown by a margin far
-        // above the FP32 transform's error): the pair prefilter
-        const int rcount = -rl.b;
-        for (int rt = 0; rt < rcount; ++rt) {
-            const float* lt = m.robot_tris32 + 9 * (size_t)(rl.a + rt);
-            float bl[3] = {INFINITY, INFINITY, INFINITY}, bh[3] = {-INFINITY, -INFINITY, -INFINITY};
-            for (int vtx = 0; vtx < 3; ++vtx) {
-                for (int r = 0; r < 3; ++r) {
-                    float wv = fmaf(R32[3 * r], lt[3 * vtx],
-                                    fmaf(R32[3 * r + 1], lt[3 * vtx + 1], fmaf(R32[3 * r + 2], lt[3 * vtx + 2], P32[r])));
-                    bl[r] = fminf(bl[r], wv);
-                    bh[r] = fmaxf(bh[r], wv);
-                }
-            }
-            for (int d = 0; d < 3; ++d) {
-                float mg = MESH_MARGIN * (1.f + fabsf(bl[d]) + fabsf(bh[d]));
-                tbs[rt][d][tid] = bl[d] - mg;
-                tbs[rt][3 + d][tid] = bh[d] + mg;
-            }
-        }
-        int stack[MESH_STACK];
-        int sp = 0;
-        stack[sp++] = 0;
-        while (sp) {
-            if (hit) break;
-            BvhNode nd = m.env_nodes[stack[--sp]];
-            if (!box_overlap(lo, hi, nd)) continue;
-            if (nd.b >= 0) {
-                if (sp + 2 <= MESH_STACK) { stack[sp++] = nd.a; stack[sp++] = nd.b; }
-                continue;
-            }
-            // environment leaf
-            for (int e = nd.a; e < nd.a - nd.b && !hit; ++e) {
-                const float* eb = m.env_boxes + 6 * (size_t)e;
-                const float elx = eb[0], ely = eb[1], elz = eb[2], ehx = eb[3], ehy = eb[4], ehz = eb[5];
-                for (int rt = 0; rt < rcount; ++rt) {
-                    if (tbs[rt][0][tid] > ehx || tbs[rt][3][tid] < elx || tbs[rt][1][tid] > ehy ||
-                        tbs[rt][4][tid] < ely || tbs[rt][2][tid] > ehz || tbs[rt][5][tid] < elz)
-                        continue;
-                    float U[9], V[9];
-                    const float* et32 = m.env_tris32 + 9 * (size_t)e;
-                    const float* lt = m.robot_tris32 + 9 * (size_t)(rl.a + rt);
-#pragma unroll
-                    for (int k = 0; k < 9; ++k) U[k] = et32[k];
-#pragma unroll
-                    for (int vtx = 0; vtx < 3; ++vtx)
-#pragma unroll
-                        for (int r = 0; r < 3; ++r)
-                            V[3 * vtx + r] = fmaf(R32[3 * r], lt[3 * vtx],
-                                                  fmaf(R32[3 * r + 1], lt[3 * vtx + 1],
-                                                       fmaf(R32[3 * r + 2], lt[3 * vtx + 2], P32[r])));
-                    if (plane_separates32(V, U, eps, X) || plane_separates32(U, V, eps, X)) continue;
-                    if (pair_hits64(R, P, m.robot_tris + 9 * (size_t)(rl.a + rt), m.env_tris + 9 * (size_t)e)) {
-                        hit = 1;
-                        break;
+    // 1. candidates: environment leaves within the bounding sphere (center p,
+    //    radius reach plus a margin far above FP32 rounding)
+    {
+        const float pc[3] = {P32[0], P32[1], P32[2]};
+        const float rad = m.reach + 1e-3f * (1.f + fabsf(pc[0]) + fabsf(pc[1]) + fabsf(pc[2]));
+        int cur = 0;
+        for (int level = 0; level < 2 * MESH_STACK; ++level) {
+            const int nf = min(nfront[cur], MESH_FRONT);
+            if (nf == 0) break;
+            for (int k = tid; k < nf; k += MESH_DETAIL_THREADS) {
+                const int node = front[cur][k];
+                const BvhNode nd = m.env_nodes[node];
+                if (!sphere_box(pc, rad, nd)) continue;
+                if (nd.b < 0) {
+                    const int c = atomicAdd(&ncand, 1);
+                    if (c < MESH_CAND) {
+                        cand[c] = node;
+                        cbox[0][c] = nd.lo[0]; cbox[1][c] = nd.lo[1]; cbox[2][c] = nd.lo[2];
+                        cbox[3][c] = nd.hi[0]; cbox[4][c] = nd.hi[1]; cbox[5][c] = nd.hi[2];
+                    } else {
+                        overflow = 1;
                     }
+                } else {
+                    const int f = atomicAdd(&nfront[cur ^ 1], 2);
+                    if (f + 2 <= MESH_FRONT) { front[cur ^ 1][f] = nd.a; front[cur ^ 1][f + 1] = nd.b; }
+                    else overflow = 1;
                 }
             }
+            __syncthreads();
+            if (tid == 0) nfront[cur] = 0;
+            cur ^= 1;
+            __syncthreads();
+        }
+        if (tid == 0 && nfront[cur] != 0) overflow = 1;
+        __syncthreads();
+    }
+    if (overflow) {
+        // per-thread depth-first walk with each robot leaf's world box
+        for (int leaf = tid; leaf < m.nrleaves && !hit; leaf += MESH_DETAIL_THREADS) {
+            const BvhNode rl = m.robot_leaves[leaf];
+            float lo[3], hi[3];
+            robot_leaf_box(rl, R32, P32, lo, hi);
+            int stack[MESH_STACK];
+            int sp = 0;
+            stack[sp++] = 0;
+            while (sp && !hit) {
+                BvhNode nd = m.env_nodes[stack[--sp]];
+                if (!box_overlap(lo, hi, nd)) continue;
+                if (nd.b >= 0) {
+                    if (sp + 2 <= MESH_STACK) { stack[sp++] = nd.a; stack[sp++] = nd.b; }
+                    continue;
+                }
+                for (int e = nd.a; e < nd.a - nd.b && !hit; ++e)
+                    for (int rt = 0; rt < -rl.b; ++rt)
+                        if (pair_hits(m, R, P, R32, P32, eps, X, rl.a + rt, e)) { hit = 1; break; }
+            }
+        }
+        __syncthreads();
+        if (tid == 0) out[i] = hit ? 0 : 1;
+        return;
+    }
+    const int nc = min(ncand, MESH_CAND);
+    for (int base = 0; base < m.nrleaves && !hit; base += MESH_DETAIL_THREADS) {
+        // 2. this thread's robot leaf against the candidates
+        const int leaf = base + tid;
+        float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f};
+        int ra = 0, rc = 0, c_next = nc;
+        if (leaf < m.nrleaves) {
+            const BvhNode rl = m.robot_leaves[leaf];
+            robot_leaf_box(rl, R32, P32, lo, hi);
+            ra = rl.a;
+            rc = -rl.b;
+            c_next = 0;
+        }
+        for (;;) {
+            while (c_next < nc) {
+                const bool ov = !(cbox[0][c_next] > hi[0] || cbox[3][c_next] < lo[0] || cbox[1][c_next] > hi[1] ||
+                                  cbox[4][c_next] < lo[1] || cbox[2][c_next] > hi[2] || cbox[5][c_next] < lo[2]);
+                if (ov) {
+                    const int slot = atomicAdd(&nq, 1);
+                    if (slot >= MESH_QUEUE) break;  // queue full: retry this candidate next round
+                    const BvhNode el = m.env_nodes[cand[c_next]];
+                    qra[slot] = ra;
+                    qrc[slot] = rc;
+                    qea[slot] = el.a;
+                    qec[slot] = -el.b;
+                }
+                ++c_next;
+            }
+            const bool more = c_next < nc;
+            __syncthreads();
+            // 3. triangle pairs of the queued leaf pairs, spread over the block
+            const int npairs = min(nq, MESH_QUEUE);
+            for (int j = tid; j < npairs * 64 && !hit; j += MESH_DETAIL_THREADS) {
+                const int e = j >> 6, rt = (j >> 3) & 7, et = j & 7;
+                if (rt >= qrc[e] || et >= qec[e]) continue;
+                if (pair_hits(m, R, P, R32, P32, eps, X, qra[e] + rt, qea[e] + et)) hit = 1;
+            }
+            __syncthreads();
+            if (tid == 0) nq = 0;
+            if (!__syncthreads_or(more) || hit) break;
         }
     }
     __syncthreads();

@@ -20,6 +20,8 @@
 // midpoint split on the widest axis of the points), so the tree is exact and
 // complete after every insert.
 #include "metrics.cuh"
+#include <algorithm>
+#include <vector>
 
 namespace {
 
@@ -954,14 +956,21 @@ __global__ void __launch_bounds__(256) k_nearest_k(TreeView t, const double* __r
 
 // ------------------------------------------------------------------ query order
 // Queries are answered in the order of the tree region they fall in: the key
-// is the first MPTG_QSORT_BITS left/right decisions of the query's descent,
-// and a counting sort over 2^16 bins groups queries of the same subtree, so
-// the warps of a block share the nodes and buckets they visit.
+// is the first `bits` left/right decisions of the query's descent (10 to 16,
+// about twice as many bins as queries), and a counting sort groups queries of
+// the same subtree, so the warps of a block share the nodes and buckets they
+// visit.
 #define MPTG_QSORT_BITS 16
 #define MPTG_QSORT_BINS (1 << MPTG_QSORT_BITS)
 #define MPTG_QSORT_MIN 2048  // smaller batches are answered in input order
 
-__global__ void k_qkey(TreeView t, const double* __restrict__ q64, int nq, int* __restrict__ key,
+static int qsort_bits(int nq) {
+    int b = 1;
+    while ((1 << b) < nq && b < MPTG_QSORT_BITS) ++b;
+    return std::min(MPTG_QSORT_BITS, std::max(10, b + 1));
+}
+
+__global__ void k_qkey(TreeView t, const double* __restrict__ q64, int nq, int bits, int* __restrict__ key,
                        int* __restrict__ hist) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nq) return;
@@ -969,25 +978,26 @@ __global__ void k_qkey(TreeView t, const double* __restrict__ q64, int nq, int* 
     int node = 0;
     unsigned k = 0;
     int lev = 0;
-    for (; lev < MPTG_QSORT_BITS; ++lev) {
+    for (; lev < bits; ++lev) {
         int4 nd = __ldg(&t.nodes[node]);
         if (nd.x < 0) break;
         int right = !(__double2float_rn(qd[nd.x]) < __int_as_float(nd.z));
         k = (k << 1) | (unsigned)right;
         node = nd.y + right;
     }
-    k <<= (MPTG_QSORT_BITS - lev);
+    k <<= (bits - lev);
     key[i] = (int)k;
     atomicAdd(&hist[k], 1);
 }
 
-// in-place exclusive scan of the 2^16-bin histogram: one block, 64 bins per thread
-__global__ void __launch_bounds__(1024) k_qscan(int* __restrict__ hist) {
+// in-place exclusive scan of the 2^bits-bin histogram: one block, bins/1024 per thread
+__global__ void __launch_bounds__(1024) k_qscan(int* __restrict__ hist, int bins) {
     __shared__ int s[1024];
     const int t = threadIdx.x;
-    const int base = t * (MPTG_QSORT_BINS / 1024);
+    const int per = bins / 1024;
+    const int base = t * per;
     int sum = 0;
-    for (int j = 0; j < MPTG_QSORT_BINS / 1024; ++j) sum += hist[base + j];
+    for (int j = 0; j < per; ++j) sum += hist[base + j];
     s[t] = sum;
     __syncthreads();
     for (int o = 1; o < 1024; o <<= 1) {
@@ -997,7 +1007,7 @@ __global__ void __launch_bounds__(1024) k_qscan(int* __restrict__ hist) {
         __syncthreads();
     }
     int run = t ? s[t - 1] : 0;
-    for (int j = 0; j < MPTG_QSORT_BINS / 1024; ++j) {
+    for (int j = 0; j < per; ++j) {
         int c = hist[base + j];
         hist[base + j] = run;
         run += c;
@@ -1342,9 +1352,10 @@ mptg_status mptg_tree_nearest_dev(mptg_tree* t, const double* dq, int nq, int* d
             MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&t->qorder, (size_t)nq * sizeof(int)));
             t->qcap = (size_t)nq;
         }
-        MPTG_CUDA_TRY(ctx, cudaMemsetAsync(t->qhist, 0, MPTG_QSORT_BINS * sizeof(int), s));
-        k_qkey<<<mptg_blocks(nq, 256), 256, 0, s>>>(v, dq, nq, t->qkey, t->qhist);
-        k_qscan<<<1, 1024, 0, s>>>(t->qhist);
+        const int bits = qsort_bits(nq);
+        MPTG_CUDA_TRY(ctx, cudaMemsetAsync(t->qhist, 0, ((size_t)1 << bits) * sizeof(int), s));
+        k_qkey<<<mptg_blocks(nq, 256), 256, 0, s>>>(v, dq, nq, bits, t->qkey, t->qhist);
+        k_qscan<<<1, 1024, 0, s>>>(t->qhist, 1 << bits);
         k_qscatter<<<mptg_blocks(nq, 256), 256, 0, s>>>(nq, t->qkey, t->qhist, t->qorder);
         ctx->launches += 3;
         order = t->qorder;
@@ -1352,7 +1363,8 @@ mptg_status mptg_tree_nearest_dev(mptg_tree* t, const double* dq, int nq, int* d
     // Packets pay off where neighbouring queries' search balls overlap (low
     // dimension); in SO(2)^10 the union of 32 balls is ~6x one ball, so
     // higher dimensions keep one query per warp (still in sorted order).
-    if (order && t->D <= 3) {
+    // Below 32k queries a packet launch has too few warps to fill the GPU.
+    if (order && t->D <= 3 && nq >= 32768) {
         // 32 sorted queries per warp
         unsigned grid = mptg_blocks((size_t)nq, 256);
         DISPATCH_METRIC(t->metric, t->D, k_nearest_packet, grid, 256, s, v, dq, nq, order, didx, dd);
