@@ -151,29 +151,50 @@ def edge_rates(ctx, m, stream, torch):
     return out
 
 
-def solve_times(ctx, seeds=5, cap_s=20.0):
-    """Wall time to the first solution of the plain wavefront planner per scene (p50 over seeds)."""
+def _solve_stats(ctx, sc, W, seeds, cap_s, surrogate=None, points=1):
+    """p50/p99 wall time to the first solution over seeds 1000.., with the phase timers."""
+    from mpt_gb300 import planner as P
+    times, solved, nodes, checked, timers = [], 0, [], [], []
+    for s in range(seeds):
+        pl = P.Planner(P.Scenario(sc), P.PRRT(P.gpu_wavefront(W)), seed=1000 + s, ctx=ctx, max_nodes=1 << 21)
+        if surrogate is not None:
+            pl.set_surrogate(surrogate, threshold=2.0, points=points)
+        pl.add_start(sc["start"])
+        t0 = time.perf_counter()
+        pl.solve_for(cap_s, lambda: pl.solved())
+        dt = time.perf_counter() - t0
+        if pl.solved():
+            solved += 1
+            times.append(dt)
+        nodes.append(pl.size())
+        checked.append(pl.stats()["link_states_checked"])
+        timers.append(pl.timers())
+        pl.close()
+    med_t = {k: statistics.median(t[k] for t in timers) for k in timers[0]}
+    return {"wavefront": W, "p50_s": statistics.median(times) if times else None,
+            "p99_s": max(times) if times else None, "solved": solved, "seeds": seeds, "cap_s": cap_s,
+            "median_nodes": statistics.median(nodes), "median_link_states_checked": statistics.median(checked),
+            "median_phase_s": med_t}
+
+
+def solve_times(ctx, seeds=5, cap_s=20.0, tune=True):
+    """Wall time to the first solution of the plain wavefront planner per scene
+    (p50 over seeds), at the default wavefront and at the one the native
+    autotuner picks (tuned on seeds 500.. of the same query)."""
     from mpt_gb300 import planner as P
     from mpt_gb300 import scenes
     res = {}
     for name, mk, W in [("grid_1024", scenes.grid_scene, 2048), ("arm_10link", scenes.arm_scene, 4096),
                         ("se3_mesh", scenes.mesh_scene, 4096)]:
         sc = mk()
-        times, solved, nodes = [], 0, []
-        for s in range(seeds):
-            pl = P.Planner(P.Scenario(sc), P.PRRT(P.gpu_wavefront(W)), seed=1000 + s, ctx=ctx, max_nodes=1 << 21)
-            pl.add_start(sc["start"])
+        r = {"default": _solve_stats(ctx, sc, W, seeds, cap_s)}
+        if tune:
             t0 = time.perf_counter()
-            pl.solve_for(cap_s, lambda: pl.solved())
-            dt = time.perf_counter() - t0
-            if pl.solved():
-                solved += 1
-                times.append(dt)
-            nodes.append(pl.size())
-            pl.close()
-        res[name] = {"p50_s": statistics.median(times) if times else None,
-                     "p99_s": max(times) if times else None, "solved": solved, "seeds": seeds,
-                     "cap_s": cap_s, "median_nodes": statistics.median(nodes)}
+            best, med = P.autotune_wavefront(ctx, P.Scenario(sc), sc["start"], trials=5, time_limit=1.0, seed=500)
+            r["autotune"] = {"best": best, "median_s": {str(k): v for k, v in med.items()},
+                             "tuning_s": time.perf_counter() - t0}
+            r["tuned"] = _solve_stats(ctx, sc, best, seeds, cap_s)
+        res[name] = r
     return res
 
 
@@ -187,7 +208,7 @@ def _labelled_mesh_states(m, ctx, sc, n, seed):
     return q, y
 
 
-def learned_vs_plain(ctx, m, torch, seeds=5, cap_s=20.0, n_train=1 << 22, epochs=10):
+def learned_vs_plain(ctx, m, torch, seeds=5, cap_s=20.0, n_train=1 << 22, epochs=10, wavefront_tuned=None):
     """Learned collision surrogate on the SE(3) scene: training throughput, held-out
     FP/FN rates, scoring throughput against the bf16 tensor peak, and time to
     solve with the surrogate culling edges versus the plain planner (same seeds)."""
@@ -230,30 +251,20 @@ def learned_vs_plain(ctx, m, torch, seeds=5, cap_s=20.0, n_train=1 << 22, epochs
            "score_states_per_s": len(qt) / score_s,
            "score_tflops": flops_fwd * len(qt) / score_s / 1e12,
            "train_tflops": 3 * flops_fwd * n_train * epochs / train_s / 1e12}
-    for mode, points in (("plain", 0), ("learned_new_state", 1), ("learned_edge_4pts", 4)):
-        times, solved, checked = [], 0, []
-        for s in range(seeds):
-            pl = P.Planner(P.Scenario(sc), P.PRRT(P.gpu_wavefront(4096)), seed=1000 + s, ctx=ctx, max_nodes=1 << 21)
-            if points:
-                pl.set_surrogate(sg, threshold=2.0, points=points)
-            pl.add_start(sc["start"])
-            t0 = time.perf_counter()
-            pl.solve_for(cap_s, lambda: pl.solved())
-            dt = time.perf_counter() - t0
-            if pl.solved():
-                solved += 1
-                times.append(dt)
-            checked.append(pl.stats()["link_states_checked"])
-            pl.close()
-        res[mode] = {"p50_s": statistics.median(times) if times else None, "p99_s": max(times) if times else None,
-                     "solved": solved, "seeds": seeds, "median_link_states_checked": statistics.median(checked)}
+    # plain versus learned at the configured wavefront (4096) and at the
+    # autotuned one for this scene, same seeds
+    Ws = sorted({4096, int(wavefront_tuned or 4096)})
+    for W in Ws:
+        for mode, points in (("plain", 0), ("learned_new_state", 1), ("learned_edge_4pts", 4)):
+            res["%s_w%d" % (mode, W)] = _solve_stats(ctx, sc, W, seeds, cap_s, sg if points else None, points)
     return res
 
 
-def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0):
+def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0, wave_for=None):
     """Config of the serving benchmark: n queries uniform over the three scenes,
     start and goal rejection-sampled valid, node budgets log-uniform in
-    [1k, 200k], wavefront budget/16 clipped to [256, 4096]."""
+    [1k, 200k]; wavefront = the scene's autotuned size (wave_for[kind]) when
+    given, else budget/16, clipped to [256, 4096] and to the budget/4."""
     from mpt_gb300 import planner as P
     from mpt_gb300 import scenes
     from mpt_gb300.batch import Query
@@ -280,18 +291,19 @@ def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0):
         a, b = pools[k][used[k]], pools[k][used[k] + 1]
         used[k] += 2
         budget = int(round(math.exp(rng.uniform(math.log(1000), math.log(200000)))))
-        W = int(min(4096, max(256, budget // 16)))
+        W = wave_for[d["kind"]] if wave_for else budget // 16
+        W = int(min(4096, budget // 4, max(256, W)))
         sc = P.Scenario(d, P.GoalState(d["goal_radius"], b))
         qs.append(Query(sc, a, seed=seed + i, max_nodes=budget, wavefront=W, time_limit=time_limit))
     return qs
 
 
-def batch_serving(m, ctx, n=512, concurrency=8, seq_sample=64):
+def batch_serving(m, ctx, n=512, concurrency=8, seq_sample=64, wave_for=None):
     """Batched multi-query serving: queries/s and time to solution over n queries
     with `concurrency` concurrent planners, against the same planner running the
     queries one after another (on the first seq_sample queries)."""
     from mpt_gb300.batch import plan_batch
-    qs = batch_queries(m, ctx, n)
+    qs = batch_queries(m, ctx, n, wave_for=wave_for)
     plan_batch(ctx, qs[:8], concurrency=concurrency)  # warm-up: planners, kernels
     t0 = time.perf_counter()
     r = plan_batch(ctx, qs, concurrency=concurrency)
@@ -465,8 +477,14 @@ def run_gpu(args):
     # secondary figures: edge checks/s (three scenes) and time to solve
     edges = edge_rates(ctx, m, stream, torch)
     solves = solve_times(ctx) if not args.no_solve else None
-    learned = learned_vs_plain(ctx, m, torch) if not (args.no_solve or args.no_learned) else None
-    serving = batch_serving(m, ctx) if not (args.no_solve or args.no_batch) else None
+    w_se3 = solves["se3_mesh"]["autotune"]["best"] if solves and "autotune" in solves["se3_mesh"] else None
+    learned = (learned_vs_plain(ctx, m, torch, wavefront_tuned=w_se3)
+               if not (args.no_solve or args.no_learned) else None)
+    wave_for = None
+    if solves and all("autotune" in solves[k] for k in solves):
+        wave_for = {"grid": solves["grid_1024"]["autotune"]["best"], "arm": solves["arm_10link"]["autotune"]["best"],
+                    "mesh": solves["se3_mesh"]["autotune"]["best"]}
+    serving = batch_serving(m, ctx, wave_for=wave_for) if not (args.no_solve or args.no_batch) else None
 
     # CPU baselines: oracle kd-tree and DMV on the host cores, bounded samples
     cpu = None

@@ -75,6 +75,15 @@ mptg_status mptg_tree_destroy(mptg_tree* tree);
  * (row-major n x dim doubles); their ids are size()..size()+n-1. */
 mptg_status mptg_tree_insert(mptg_tree* tree, const double* states, size_t n, void* stream);
 mptg_status mptg_tree_size(mptg_tree* tree, size_t* n);
+/* Search strategy, as the reference picks a nigh strategy per planner
+ * (src/mpt/impl/nearest_strategy.hpp:44-72; auto = nigh::auto_strategy_t).
+ * KDTREE: the bucketed kd-tree walk.  EXHAUSTIVE: every stored point, staged
+ * through shared memory 256 queries at a time (nigh::Linear's answer).  AUTO
+ * uses EXHAUSTIVE for six or more dimensions or a rotation metric up to
+ * 131,072 points, where the tree must visit a large share of them.  Every
+ * strategy returns the same exact ids and distances. */
+typedef enum { MPTG_NN_AUTO = 0, MPTG_NN_KDTREE = 1, MPTG_NN_EXHAUSTIVE = 2 } mptg_nn_strategy;
+mptg_status mptg_tree_set_strategy(mptg_tree* tree, int strategy);
 /* Remove every state, keeping the tree's allocations (no reference
  * counterpart: a reference planner is rebuilt for each query). */
 mptg_status mptg_tree_clear(mptg_tree* tree, void* stream);
@@ -255,6 +264,10 @@ mptg_status mptg_planner_set_surrogate_points(mptg_planner* planner, int points)
  * added, [3] tree size, [4] goals, [5] states checked by link, [6] seconds in
  * run, [7] wavefront counter. */
 mptg_status mptg_planner_stats(mptg_planner* planner, double out[8]);
+/* WorkerStats' timers (prrt.hpp:72-101) on the GPU timeline, seconds summed
+ * over wavefronts: [0] sample + nearest + steer, [1] surrogate scoring,
+ * [2] valid motion (state + DMV link checks), [3] compaction + insert. */
+mptg_status mptg_planner_timers(mptg_planner* planner, double out[4]);
 
 /* Start over as a new Planner(scenario, seed) on the same scene, keeping the
  * allocations: tree, goal, solutions and statistics are cleared.  params NULL
@@ -296,6 +309,18 @@ typedef struct {
     size_t path_len;            /* states of the best path (0 if unsolved); written to
                                    query.path only when it fits path_cap */
 } mptg_result;
+
+/* Project-written autotuner for the wavefront size of one scene and query:
+ * plans `trials` seeds (params->seed, +1, ...) from start to the goal for each
+ * candidate size (stop at the first solution, time_limit_s each; unsolved
+ * counts as the limit) and returns in *best the size with the lowest median
+ * time to solution; median_s (ncand entries, may be NULL) receives the
+ * medians.  The time to solution is governed by tree depth (wavefronts
+ * needed) times per-wavefront latency, so the best size is scene-dependent. */
+mptg_status mptg_autotune_wavefront(mptg_ctx* ctx, mptg_scene* scene, const mptg_plan_params* params,
+                                    const double* lo, const double* hi, const double* start, const double* goal,
+                                    double goal_radius, const int* candidates, int ncand, int trials,
+                                    double time_limit_s, int* best, double* median_s);
 
 /* Runs queries [0, n) and fills out[0, n).  Returns MPTG_OK when every query
  * ran (per-query failures are in out[i].status), else the first error. */

@@ -81,6 +81,12 @@ class Tree:
         _check(ctx.h, self.lib.mptg_tree_create(ctx.h, metric, dim, w.ctypes.data, capacity, ctypes.byref(h)))
         self.h = h
 
+    # nearest-neighbour strategies (mptg_nn_strategy)
+    AUTO, KDTREE, EXHAUSTIVE = 0, 1, 2
+
+    def set_strategy(self, strategy: int):
+        _check(self.ctx.h, self.lib.mptg_tree_set_strategy(self.h, int(strategy)))
+
     def __len__(self):
         n = ctypes.c_size_t()
         _check(self.ctx.h, self.lib.mptg_tree_size(self.h, ctypes.byref(n)))

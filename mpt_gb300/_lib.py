@@ -63,6 +63,7 @@ def load(build_if_missing: bool = True):
         "mptg_tree_destroy": (St, [P]),
         "mptg_tree_insert": (St, [P, P, S, P]),
         "mptg_tree_size": (St, [P, ctypes.POINTER(S)]),
+        "mptg_tree_set_strategy": (St, [P, I]),
         "mptg_tree_states": (St, [P, S, S, P, P]),
         "mptg_nearest": (St, [P, P, S, P, P, P]),
         "mptg_nearest_k": (St, [P, P, S, I, D, P, P, P]),

@@ -84,13 +84,16 @@ __device__ __forceinline__ double dist64(int metric, int D, double w0, double w1
 }
 
 // ---- interpolation (exact FP64, mirrors the reference expressions) ----
+// fmod(x, 2pi) is x itself when |x| < 2pi (fmod is exact), which skips the
+// library's reduction loop in the common case
+__device__ __forceinline__ double fmod_2pi(double x) { return fabs(x) < MPTG_TWO_PI ? x : fmod(x, MPTG_TWO_PI); }
 __device__ __forceinline__ double so2_ccw64(double a, double b) {
-    double d = fmod(__dsub_rn(b, a), MPTG_TWO_PI);
+    double d = fmod_2pi(__dsub_rn(b, a));
     if (d < 0) d = __dadd_rn(d, MPTG_TWO_PI);
     return d;
 }
 __device__ __forceinline__ double so2_bound64(double v) {
-    v = fmod(v, MPTG_TWO_PI);
+    v = fmod_2pi(v);
     if (v < -MPTG_PI) v = __dadd_rn(v, MPTG_TWO_PI);
     else if (v >= MPTG_PI) v = __dsub_rn(v, MPTG_TWO_PI);
     return v;

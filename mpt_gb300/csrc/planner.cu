@@ -92,6 +92,10 @@ struct mptg_planner {
     int cap_wave = 0;         // wavefront buffers
     int* path_ids = nullptr;  // [cap_nodes]
     double* path_out = nullptr;  // [2]
+    // phase timing on the stream's timeline (WorkerStats' nearest_ and
+    // validMotion_ timers, prrt.hpp:72-101): events at the phase boundaries
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    double t_phase[4] = {0, 0, 0, 0};  // nearest, surrogate, valid motion, insert (seconds)
 };
 
 extern "C" mptg_status mptg_surrogate_score_dev(mptg_surrogate* s, const double* dstates, int n, float* dlogits,
@@ -348,6 +352,8 @@ static void planner_free(mptg_planner* p) {
     if (p->hbuf) cudaFreeHost(p->hbuf);
     if (p->hgoal) cudaFreeHost(p->hgoal);
     scratch_free(&p->scratch);
+    for (cudaEvent_t e : p->ev)
+        if (e) cudaEventDestroy(e);
     if (p->tree) mptg_tree_destroy(p->tree);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
@@ -405,6 +411,7 @@ static mptg_status planner_reset(mptg_planner* p, const mptg_plan_params* prm, b
     p->stat_samples = p->stat_goal_samples = p->stat_accepted = p->stat_wavefronts = 0;
     p->stat_skipped = p->stat_culled = 0;
     p->stat_seconds = 0;
+    for (double& t : p->t_phase) t = 0;
     return MPTG_OK;
 }
 
@@ -417,6 +424,7 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
     mptg_tree_size(p->tree, &n0);
     if (n0 >= p->prm.max_nodes) return MPTG_OK;
     PlanView v = plan_view(p);
+    MPTG_CUDA_TRY(ctx, cudaEventRecord(p->ev[0], s));
     bool bias_on = p->goals.empty() && p->has_goal && p->prm.goal_bias > 0;
     int* gidx = nullptr;
     if (bias_on) {
@@ -431,6 +439,7 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
     k_plan_steer<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->samp, p->nidx, p->ndist, mptg_tree_states_dev(p->tree),
                                                      p->nearst, p->newst, p->skip);
     ctx->launches += 2;
+    MPTG_CUDA_TRY(ctx, cudaEventRecord(p->ev[1], s));
     int nblk = (W + PLAN_SCAN_BLOCK - 1) / PLAN_SCAN_BLOCK;
     if (p->sg) {
         // score the new states; only edges the surrogate does not reject go to the exact check
@@ -459,6 +468,7 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
             nk = p->hbuf[1];
         }
         p->stat_culled += (uint64_t)(W - nk);
+        MPTG_CUDA_TRY(ctx, cudaEventRecord(p->ev[2], s));
         if (nk > 0) {
             st = scene_edges_dev(p->scene, p->near_c, p->new_c, nk, p->prm.edge_step, p->prm.resolution, p->ok_c, s,
                                  p->nsamp, &p->scratch);
@@ -467,10 +477,12 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
             MPTG_LAUNCHED(ctx);
         }
     } else {
+        MPTG_CUDA_TRY(ctx, cudaEventRecord(p->ev[2], s));
         st = scene_edges_dev(p->scene, p->nearst, p->newst, W, p->prm.edge_step, p->prm.resolution, p->ok, s,
                              p->nsamp, &p->scratch);
         if (st) return st;
     }
+    MPTG_CUDA_TRY(ctx, cudaEventRecord(p->ev[3], s));
     k_plan_scan<<<nblk, PLAN_SCAN_BLOCK, 0, s>>>(W, p->ok, p->skip, p->scan, p->bsum);
     k_plan_scan_top<<<1, 1024, 0, s>>>(nblk, p->bsum);
     k_plan_scatter<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->scan, p->bsum, p->newst, p->nidx, p->acc_states,
@@ -494,6 +506,13 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
         MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
         for (int k = 0; k < nacc; ++k)
             if (p->hgoal[k]) p->goals.push_back((int)(n0 + k));
+    }
+    MPTG_CUDA_TRY(ctx, cudaEventRecord(p->ev[4], s));
+    MPTG_CUDA_TRY(ctx, cudaEventSynchronize(p->ev[4]));
+    for (int k = 0; k < 4; ++k) {
+        float ms = 0.f;
+        MPTG_CUDA_TRY(ctx, cudaEventElapsedTime(&ms, p->ev[k], p->ev[k + 1]));
+        p->t_phase[k] += 1e-3 * ms;
     }
     *added = nacc;
     return MPTG_OK;
@@ -522,6 +541,12 @@ mptg_status mptg_planner_create(mptg_ctx* ctx, mptg_scene* scene, const mptg_pla
     if (e != cudaSuccess) {
         delete p;
         return mptg_fail(ctx, MPTG_ERR_CUDA, "planner stream: %s", cudaGetErrorString(e));
+    }
+    for (cudaEvent_t& ev : p->ev)
+        if (e == cudaSuccess) e = cudaEventCreate(&ev);
+    if (e != cudaSuccess) {
+        planner_free(p);
+        return mptg_fail(ctx, MPTG_ERR_CUDA, "planner events: %s", cudaGetErrorString(e));
     }
     double w[2] = {p->w0, p->w1};
     if ((st = mptg_tree_create(ctx, (mptg_metric)p->metric, p->D, w, prm->max_nodes, &p->tree))) {
@@ -755,6 +780,12 @@ mptg_status mptg_planner_set_surrogate_points(mptg_planner* p, int points) {
     return MPTG_OK;
 }
 
+mptg_status mptg_planner_timers(mptg_planner* p, double out[4]) {
+    if (!p || !out) return MPTG_ERR_INVALID_ARG;
+    for (int k = 0; k < 4; ++k) out[k] = p->t_phase[k];
+    return MPTG_OK;
+}
+
 mptg_status mptg_planner_stats(mptg_planner* p, double out[8]) {
     if (!p || !out) return MPTG_ERR_INVALID_ARG;
     unsigned long long ns = 0;
@@ -857,6 +888,52 @@ mptg_status mptg_plan_batch(mptg_ctx* ctx, const mptg_query* qs, size_t n, int c
     work();
     for (auto& th : pool) th.join();
     return first;
+}
+
+// ------------------------------------------------------------- wavefront autotuner
+
+mptg_status mptg_autotune_wavefront(mptg_ctx* ctx, mptg_scene* scene, const mptg_plan_params* params,
+                                    const double* lo, const double* hi, const double* start, const double* goal,
+                                    double goal_radius, const int* candidates, int ncand, int trials,
+                                    double time_limit_s, int* best, double* median_s) {
+    if (!ctx || !scene || !params || !start || !goal || !candidates || ncand < 1 || trials < 1 || !best)
+        return MPTG_ERR_INVALID_ARG;
+    int wmax = 0;
+    for (int c = 0; c < ncand; ++c) {
+        if (candidates[c] < 1 || candidates[c] > (1 << 20))
+            return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "wavefront candidate %d out of [1, 2^20]", candidates[c]);
+        wmax = std::max(wmax, candidates[c]);
+    }
+    mptg_plan_params cp = *params;
+    cp.wavefront = wmax;
+    mptg_planner* p = nullptr;
+    mptg_status st = mptg_planner_create(ctx, scene, &cp, lo, hi, &p);
+    if (st) return st;
+    double best_t = INFINITY;
+    *best = candidates[0];
+    for (int c = 0; c < ncand && !st; ++c) {
+        std::vector<double> ts;
+        for (int t = 0; t < trials && !st; ++t) {
+            mptg_plan_params q = *params;
+            q.wavefront = candidates[c];
+            q.seed = params->seed + (uint64_t)t;
+            if ((st = planner_reset(p, &q, false, nullptr, nullptr))) break;
+            if ((st = mptg_planner_set_goal(p, goal, goal_radius))) break;
+            if ((st = mptg_planner_add_start(p, start))) break;
+            int solved = 0;
+            const auto t0 = std::chrono::steady_clock::now();
+            if ((st = mptg_planner_run(p, 0, time_limit_s, 1, &solved))) break;
+            const double dt = seconds_since(t0);
+            ts.push_back(solved ? dt : std::max(dt, time_limit_s));
+        }
+        if (st) break;
+        std::sort(ts.begin(), ts.end());
+        const double med = ts[ts.size() / 2];
+        if (median_s) median_s[c] = med;
+        if (med < best_t) { best_t = med; *best = candidates[c]; }
+    }
+    planner_free(p);
+    return st;
 }
 
 }  // extern "C"

@@ -269,8 +269,7 @@ __global__ void __launch_bounds__(256) k_grid_edges_b(SceneView s, const double*
 struct ArmLane {
     float L32;       // link length of joint `lane`
     double L64;
-    float4 d0, d1;   // discs lane and lane + 32 (cx, cy, (r + robot_radius)^2)
-    int si[ARM_SELF_SLOTS], sj[ARM_SELF_SLOTS];  // self pairs lane + 32 c
+    int sij[ARM_SELF_SLOTS];  // self pairs lane + 32 c: i | j << 8
     int nself;
 };
 
@@ -278,8 +277,6 @@ __device__ __forceinline__ ArmLane arm_lane(const SceneView& s, int lane) {
     ArmLane al;
     al.L32 = lane < s.nlinks ? __ldg(&s.link32[lane]) : 0.f;
     al.L64 = lane < s.nlinks ? __ldg(&s.link_len64[lane]) : 0.0;
-    al.d0 = lane < s.ndiscs ? __ldg(&s.discs32[lane]) : make_float4(0.f, 0.f, 0.f, 0.f);
-    al.d1 = lane + 32 < s.ndiscs ? __ldg(&s.discs32[lane + 32]) : make_float4(0.f, 0.f, 0.f, 0.f);
     const int nl = s.nlinks;
     al.nself = nl >= 3 ? (nl - 2) * (nl - 1) / 2 : 0;
 #pragma unroll
@@ -295,8 +292,7 @@ __device__ __forceinline__ ArmLane arm_lane(const SceneView& s, int lane) {
             i = 0;
             j = 2;
         }
-        al.si[c] = i;
-        al.sj[c] = j;
+        al.sij[c] = i | (j << 8);
     }
     return al;
 }
@@ -305,6 +301,12 @@ __device__ __forceinline__ float warp_max_f(float v) {
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(FULL_MASK, v, o));
     return v;
 }
+
+// The exact FP64 joint angle of lane `lane` for one sample: b itself (t < 0)
+// or so2 interpolate(a, b, t), the DMV's sample expression.
+struct ArmSample {
+    double a, b, t;
+};
 
 // arm_fk64 across the warp: lane m receives joint position m (x64, y64); q64
 // holds joint `lane`'s angle on lanes < nlinks
@@ -329,13 +331,20 @@ __device__ __noinline__ void arm_fk64_warp(const SceneView& s, const ArmLane& al
     }
 }
 
+// FP64 joint positions of a sample (the rare path, out of line)
+__device__ __noinline__ void arm_sample_fk64(const SceneView& s, const ArmLane& al, int lane, const ArmSample& smp,
+                                             double& x64, double& y64) {
+    double q64 = 0.0;
+    if (lane < s.nlinks) q64 = smp.t < 0.0 ? smp.b : so2_interp64(smp.a, smp.b, smp.t);
+    arm_fk64_warp(s, al, lane, q64, x64, y64);
+}
+
 // One arm state, warp-uniform result.  q32: joint `lane`'s FP32 angle, within
-// ea of the exact one; q64of(): joint `lane`'s exact FP64 angle (evaluated by
-// lanes < nlinks only when some pair needs FP64).  force64 sends every pair
-// to FP64 (inputs outside the range of the FP32 error bound).
-template <class Q64>
+// ea of the exact one; smp: how to get joint `lane`'s exact FP64 angle (only
+// when some pair needs FP64).  force64 sends every pair to FP64 (inputs
+// outside the range of the FP32 error bound).
 __device__ __forceinline__ bool arm_state_warp(const SceneView& s, const ArmLane& al, int lane, float q32, float ea,
-                                               bool force64, const Q64& q64of) {
+                                               bool force64, const ArmSample& smp) {
     const int nl = s.nlinks;
     // FP32 forward kinematics.  Error bound against the FP64 kinematics
     // (arm_fk64 on the exact angles), with u = 2^-24 and joint angles within
@@ -388,7 +397,7 @@ __device__ __forceinline__ bool arm_state_warp(const SceneView& s, const ArmLane
                 if (force64) {
                     r = VF_UNSURE;
                 } else {
-                    float4 d = c == 0 ? al.d0 : (c == 1 ? al.d1 : __ldg(&s.discs32[k]));
+                    const float4 d = __ldg(&s.discs32[k]);  // 1 KB per scene: L1-resident
                     float d2 = dpseg2_32(d.x, d.y, ax, ay, bx, by);
                     // the distance moves by <= dd, so d^2 by <= 2*d*dd + dd^2
                     float m = 3.f * sqrtf(fmaxf(d2, d.z)) * dd + dd * dd + 8.f * U32 * (d2 + d.z);
@@ -398,8 +407,7 @@ __device__ __forceinline__ bool arm_state_warp(const SceneView& s, const ArmLane
             if (__any_sync(FULL_MASK, r == VF_INVALID)) return false;
             if (__any_sync(FULL_MASK, r == VF_UNSURE)) {
                 if (!have64) {
-                    double q64 = lane < nl ? q64of() : 0.0;
-                    arm_fk64_warp(s, al, lane, q64, x64, y64);
+                    arm_sample_fk64(s, al, lane, smp, x64, y64);
                     have64 = true;
                 }
                 const double pax = __shfl_sync(FULL_MASK, x64, i), pay = __shfl_sync(FULL_MASK, y64, i);
@@ -419,7 +427,7 @@ __device__ __forceinline__ bool arm_state_warp(const SceneView& s, const ArmLane
 #pragma unroll
         for (int c = 0; c < ARM_SELF_SLOTS; ++c) {
             if (32 * c >= al.nself) break;
-            const int i = al.si[c], j = al.sj[c];
+            const int i = al.sij[c] & 0xff, j = al.sij[c] >> 8;
             const float ax = __shfl_sync(FULL_MASK, xm, i), ay = __shfl_sync(FULL_MASK, ym, i);
             const float bx = __shfl_sync(FULL_MASK, xm, i + 1), by = __shfl_sync(FULL_MASK, ym, i + 1);
             const float cx = __shfl_sync(FULL_MASK, xm, j), cy = __shfl_sync(FULL_MASK, ym, j);
@@ -453,8 +461,7 @@ __device__ __forceinline__ bool arm_state_warp(const SceneView& s, const ArmLane
             if (__any_sync(FULL_MASK, r == VF_INVALID)) return false;
             if (__any_sync(FULL_MASK, r == VF_UNSURE)) {
                 if (!have64) {
-                    double q64 = lane < nl ? q64of() : 0.0;
-                    arm_fk64_warp(s, al, lane, q64, x64, y64);
+                    arm_sample_fk64(s, al, lane, smp, x64, y64);
                     have64 = true;
                 }
                 const double pax = __shfl_sync(FULL_MASK, x64, i), pay = __shfl_sync(FULL_MASK, y64, i);
@@ -477,7 +484,7 @@ __device__ __forceinline__ bool arm_state_exact(const SceneView& s, const ArmLan
     const bool fin = lane >= s.nlinks || fabsf(q32) <= 4.f;  // false for NaN
     const float mx = warp_max_f(lane < s.nlinks && fin ? fabsf(q32) : 0.f);
     const bool force64 = !__all_sync(FULL_MASK, fin);
-    return arm_state_warp(s, al, lane, q32, 2.f * U32 * mx + U32 * PI_F, force64, [&]() { return qd; });
+    return arm_state_warp(s, al, lane, q32, 2.f * U32 * mx + U32 * PI_F, force64, ArmSample{0.0, qd, -1.0});
 }
 
 // Scenario::valid for planar-arm states, warp per state
@@ -546,8 +553,7 @@ __global__ void __launch_bounds__(256) k_arm_edges(SceneView s, const double* __
                 ++cnt;
                 const float t = (float)k / (float)steps;
                 const float q32 = fmaf(dir32, t, a32);
-                ok = arm_state_warp(s, al, lane, q32, ea, force64,
-                                    [&]() { return so2_interp64(Ad, Bd, __dmul_rn((double)k, delta)); });
+                ok = arm_state_warp(s, al, lane, q32, ea, force64, ArmSample{Ad, Bd, __dmul_rn((double)k, delta)});
             }
         }
     }

@@ -66,6 +66,11 @@ struct mptg_tree {
     int* seg_cursor = nullptr;
     int* hcnt = nullptr;  // pinned
     uint64_t rebuilds = 0;
+    int strategy = MPTG_NN_AUTO;  // mptg_nn_strategy
+    // exhaustive sweep scratch: [split][BRUTE_K][queries] candidates
+    float* bcd = nullptr;
+    int* bci = nullptr;
+    size_t bcap = 0;
     // query ordering scratch (grown on demand)
     int* qkey = nullptr;
     int* qorder = nullptr;
@@ -835,6 +840,141 @@ __global__ void __launch_bounds__(256) k_nearest_linear(TreeView t, const double
     }
 }
 
+// ------------------------------------------------------------------ tiled exhaustive 1-NN
+// For trees in high dimension the kd-tree visits a large share of the points
+// at a high cost per point (dependent node loads, divergent lanes).  This
+// sweep is thread per query and runs in two passes.
+//  Pass 1 (k_nearest_tiled): block (query tile, point split) stages its split
+//   of the FP32 points through shared memory, BRUTE_TILE at a time, so each
+//   point is read once per 256 queries, and every thread keeps the BRUTE_K
+//   smallest FP32 distances (distance, id) of the split in registers.
+//   Splitting the points keeps the GPU full when there are few queries.
+//  Pass 2 (k_nearest_tiled_merge): the exact argmin p* satisfies
+//   d32(p*) <= d64(p*) + E <= d64(argmin32) + E <= min32 + 2E
+//   (|d32 - d64| <= E for every point), and so does every point tied with it.
+//   When every split's K-th kept distance exceeds min32 + 2E, each such point
+//   is in some list and the FP64 re-rank runs on the lists alone; otherwise
+//   (more than K points within 2E in a split, e.g. duplicates) the thread
+//   sweeps all points again and re-ranks every one within min32 + 2E.
+// Ties go to the lowest id, as in k_nearest.
+#define BRUTE_K 8
+#define BRUTE_TILE 256
+
+template <int MK, int DMAX>
+__device__ __forceinline__ float load_query32(const TreeView& t, const double* __restrict__ qd, bool active,
+                                              float (&q)[DMAX]) {
+    float M = __int_as_float(t.dcnt[CNT_MAXABS]);
+#pragma unroll
+    for (int d = 0; d < DMAX; ++d) {
+        float v = 0.f;
+        if (d < t.D && active) v = __double2float_rn(qd[d]);
+        q[d] = v;
+        bool lp = MK == MPTG_METRIC_L2 || MK == MPTG_METRIC_L1 || (MK == MPTG_METRIC_SE3 && d >= 4 && d < 7);
+        if (lp && d < t.D && active) M = fmaxf(M, __double2float_ru(fabs(qd[d])));
+    }
+    return err32<MK>(t.D, M, t.w0f, t.w1f);
+}
+
+// cd / ci: [split][BRUTE_K][nq]
+template <int MK, int DMAX>
+__global__ void __launch_bounds__(BRUTE_TILE) k_nearest_tiled(TreeView t, const double* __restrict__ q64, int nq,
+                                                              int chunk, float* __restrict__ cd,
+                                                              int* __restrict__ ci) {
+    __shared__ float tile[DMAX][BRUTE_TILE];
+    const int qi = blockIdx.x * BRUTE_TILE + threadIdx.x;
+    const int split = blockIdx.y;
+    const bool active = qi < nq;
+    const int D = t.D;
+    float q[DMAX];
+    load_query32<MK, DMAX>(t, q64 + (size_t)(active ? qi : 0) * D, active, q);
+    float kd[BRUTE_K];
+    int ki[BRUTE_K];
+#pragma unroll
+    for (int s = 0; s < BRUTE_K; ++s) { kd[s] = INFINITY; ki[s] = -1; }
+    const int lo = split * chunk, hi = min(t.n, lo + chunk);
+    for (int base = lo; base < hi; base += BRUTE_TILE) {
+        __syncthreads();
+        const int j = base + threadIdx.x;
+#pragma unroll
+        for (int d = 0; d < DMAX; ++d) tile[d][threadIdx.x] = (j < hi && d < D) ? t.pts32[(size_t)j * D + d] : 0.f;
+        __syncthreads();
+        if (!active) continue;
+        const int cnt = min(BRUTE_TILE, hi - base);
+        for (int k = 0; k < cnt; ++k) {
+            float p[DMAX];
+#pragma unroll
+            for (int d = 0; d < DMAX; ++d) p[d] = tile[d][k];
+            float d32 = dist32<MK, DMAX>(q, p, t.w0f, t.w1f);
+            if (d32 < kd[BRUTE_K - 1]) {  // false for NaN
+                float xd = d32;
+                int xi = base + k;
+#pragma unroll
+                for (int s = 0; s < BRUTE_K; ++s) {
+                    if (xd < kd[s]) {
+                        float td = kd[s]; kd[s] = xd; xd = td;
+                        int ti = ki[s]; ki[s] = xi; xi = ti;
+                    }
+                }
+            }
+        }
+    }
+    if (!active) return;
+#pragma unroll
+    for (int s = 0; s < BRUTE_K; ++s) {
+        cd[((size_t)split * BRUTE_K + s) * nq + qi] = kd[s];
+        ci[((size_t)split * BRUTE_K + s) * nq + qi] = ki[s];
+    }
+}
+
+template <int MK, int DMAX>
+__global__ void __launch_bounds__(256) k_nearest_tiled_merge(TreeView t, const double* __restrict__ q64, int nq,
+                                                             int nsplit, const float* __restrict__ cd,
+                                                             const int* __restrict__ ci, int* __restrict__ out_idx,
+                                                             double* __restrict__ out_d) {
+    const int qi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= nq) return;
+    const int D = t.D;
+    const double* qd = q64 + (size_t)qi * D;
+    float q[DMAX];
+    const float E = load_query32<MK, DMAX>(t, qd, true, q);
+    float m = INFINITY;
+    for (int sp = 0; sp < nsplit; ++sp) m = fminf(m, cd[((size_t)sp * BRUTE_K) * nq + qi]);
+    double best = INFINITY;
+    int bidx = INT_MAX;
+    unsigned long long nrr = 0;
+    if (m < INFINITY) {
+        const float thr = __fadd_ru(m, __fmul_ru(2.f, E));
+        bool complete = true;
+        for (int sp = 0; sp < nsplit; ++sp) complete = complete && cd[((size_t)sp * BRUTE_K + BRUTE_K - 1) * nq + qi] > thr;
+        auto consider = [&](int id) {
+            ++nrr;
+            double dd = dist64(t.metric, D, t.w0, t.w1, qd, t.states64 + (size_t)id * D);
+            if (dd == dd && (dd < best || (dd == best && id < bidx))) { best = dd; bidx = id; }
+        };
+        if (complete) {
+            for (int sp = 0; sp < nsplit; ++sp)
+                for (int s = 0; s < BRUTE_K; ++s) {
+                    const size_t o = ((size_t)sp * BRUTE_K + s) * nq + qi;
+                    if (ci[o] >= 0 && cd[o] <= thr) consider(ci[o]);
+                }
+        } else {
+            for (int j = 0; j < t.n; ++j) {
+                float p[DMAX];
+#pragma unroll
+                for (int d = 0; d < DMAX; ++d) p[d] = d < D ? t.pts32[(size_t)j * D + d] : 0.f;
+                if (dist32<MK, DMAX>(q, p, t.w0f, t.w1f) <= thr) consider(j);
+            }
+        }
+    }
+    out_idx[qi] = bidx == INT_MAX ? -1 : bidx;
+    out_d[qi] = best;
+    if (t.stats) {
+        atomicAdd(&t.stats[0], 1ull);
+        atomicAdd(&t.stats[3], (unsigned long long)t.n);
+        atomicAdd(&t.stats[4], nrr);
+    }
+}
+
 // ------------------------------------------------------------------ k-NN
 
 // Exact k nearest (k <= 64) sorted by (distance, id), warp per query.  The
@@ -1055,7 +1195,7 @@ static void tree_free(mptg_tree* t) {
     void* ptrs[] = {t->states64, t->pts32, t->nodes, t->cell_lo, t->cell_hi, t->node_depth, t->bpts, t->bids,
                     t->dcnt, t->dstats, t->perm, t->perm2, t->pseg, t->pseg2, t->segA, t->segB, t->seg_box,
                     t->leaf_of, t->ovf_pts, t->ovf_leaf, t->leaf_reg, t->seg_cursor, t->qkey, t->qorder,
-                    t->qhist};
+                    t->qhist, t->bcd, t->bci};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (t->hcnt) cudaFreeHost(t->hcnt);
@@ -1159,6 +1299,14 @@ mptg_status mptg_tree_destroy(mptg_tree* t) {
 mptg_status mptg_tree_size(mptg_tree* t, size_t* n) {
     if (!t || !n) return MPTG_ERR_INVALID_ARG;
     *n = t->n;
+    return MPTG_OK;
+}
+
+mptg_status mptg_tree_set_strategy(mptg_tree* t, int strategy) {
+    if (!t) return MPTG_ERR_INVALID_ARG;
+    if (strategy < MPTG_NN_AUTO || strategy > MPTG_NN_EXHAUSTIVE)
+        return mptg_fail(t->ctx, MPTG_ERR_INVALID_ARG, "unknown nearest-neighbour strategy %d", strategy);
+    t->strategy = strategy;
     return MPTG_OK;
 }
 
@@ -1332,6 +1480,20 @@ mptg_status mptg_tree_counters(mptg_tree* t, uint64_t out[5], int reset) {
 
 const double* mptg_tree_states_dev(const mptg_tree* t) { return t->states64; }
 
+// The tiled exhaustive sweep beats the kd-tree where the tree must visit a
+// large share of its points: Lp / SO(2)^n spaces of six or more dimensions.
+// Measured on SO(2)^10 (GB300): the sweep evaluates ~4.3e11 (query, point)
+// pairs/s, the tree ~0.1-2 us per query; the sweep is chosen while
+// points x queries x dimensions stays below MPTG_TILED_MAX_WORK.  Rotation
+// metrics keep the tree (it prunes well there).
+#define MPTG_TILED_MAX_WORK 2.5e11
+static bool tree_use_tiled(const mptg_tree* t, int nq) {
+    if (t->strategy == MPTG_NN_KDTREE || t->n == 0) return false;
+    if (t->strategy == MPTG_NN_EXHAUSTIVE) return true;
+    const bool lp = t->metric == MPTG_METRIC_L2 || t->metric == MPTG_METRIC_L1 || t->metric == MPTG_METRIC_SO2;
+    return lp && t->D >= 6 && (double)t->n * nq * t->D <= MPTG_TILED_MAX_WORK;
+}
+
 // internal: launch the 1-NN search on device buffers (used by the planner too)
 mptg_status mptg_tree_nearest_dev(mptg_tree* t, const double* dq, int nq, int* didx, double* dd, cudaStream_t s,
                                   bool count) {
@@ -1339,6 +1501,32 @@ mptg_status mptg_tree_nearest_dev(mptg_tree* t, const double* dq, int nq, int* d
     mptg_ctx* ctx = t->ctx;
     TreeView v = view_of(t);
     if (!count) v.stats = nullptr;
+    if (tree_use_tiled(t, nq)) {
+        // enough (query tile, point split) blocks to fill the GPU four times over
+        const int qblocks = (int)mptg_blocks((size_t)nq, BRUTE_TILE);
+        const int maxsplit = std::max(1, (int)((t->n + BRUTE_TILE - 1) / BRUTE_TILE));
+        const int nsplit = std::min(maxsplit, std::max(1, (4 * 152 + qblocks - 1) / qblocks));
+        const int chunk = (int)((t->n + nsplit - 1) / nsplit);
+        const size_t need = (size_t)nsplit * BRUTE_K * nq;
+        if (need > t->bcap) {
+            MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+            cudaFree(t->bcd);
+            cudaFree(t->bci);
+            t->bcd = nullptr;
+            t->bci = nullptr;
+            t->bcap = 0;
+            const size_t cap = need + need / 2;
+            MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&t->bcd, cap * sizeof(float)));
+            MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&t->bci, cap * sizeof(int)));
+            t->bcap = cap;
+        }
+        dim3 grid(qblocks, nsplit);
+        DISPATCH_METRIC(t->metric, t->D, k_nearest_tiled, grid, BRUTE_TILE, s, v, dq, nq, chunk, t->bcd, t->bci);
+        DISPATCH_METRIC(t->metric, t->D, k_nearest_tiled_merge, mptg_blocks((size_t)nq, 256), 256, s, v, dq, nq, nsplit,
+                        t->bcd, t->bci, didx, dd);
+        ctx->launches += 2;
+        return MPTG_OK;
+    }
     const int* order = nullptr;
     if (nq >= MPTG_QSORT_MIN && t->n > 4 * MPTG_BUCKET) {
         if ((size_t)nq > t->qcap) {

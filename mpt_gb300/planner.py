@@ -111,6 +111,9 @@ def _sig(L):
         ("mptg_planner_solution", ctypes.c_int, [P, P, S, ctypes.POINTER(S), ctypes.POINTER(ctypes.c_double)]),
         ("mptg_planner_graph", ctypes.c_int, [P, P, P, S, ctypes.POINTER(S)]),
         ("mptg_planner_stats", ctypes.c_int, [P, P]),
+        ("mptg_planner_timers", ctypes.c_int, [P, P]),
+        ("mptg_autotune_wavefront", ctypes.c_int, [P, P, P, P, P, P, P, ctypes.c_double, P, ctypes.c_int,
+                                                   ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_int), P]),
     ]:
         f = getattr(L, name)
         f.restype = res
@@ -297,6 +300,13 @@ class Planner:
                 "wavefront_counter"]
         return dict(zip(keys, [float(v) for v in out]))
 
+    def timers(self) -> dict:
+        """Seconds per phase on the GPU timeline (WorkerStats' nearest / validMotion
+        timers, src/mpt/impl/prrt/prrt.hpp:72-101)."""
+        out = (ctypes.c_double * 4)()
+        _check(self.ctx.h, self.lib.mptg_planner_timers(self.h, out))
+        return dict(zip(["nearest", "surrogate", "valid_motion", "insert"], [float(v) for v in out]))
+
     def print_stats(self):
         s = self.stats() if self.h is not None else {}
         print("nodes in graph: %d" % self.size())
@@ -306,6 +316,9 @@ class Planner:
         if self.algorithm.report_stats:
             for k, v in s.items():
                 print("%s: %g" % (k, v))
+            if self.h is not None:
+                for k, v in self.timers().items():
+                    print("%s: %.6f s" % (k, v))
 
     def close(self):
         if self.h is not None:
@@ -330,5 +343,37 @@ class Planner:
     visitGraph = visit_graph
 
 
-__all__ = ["Planner", "PRRT", "Scenario", "GoalState", "gpu_wavefront", "report_stats", "max_threads",
+def autotune_wavefront(ctx: Context, scenario: Scenario, start, candidates=(256, 512, 1024, 2048, 4096, 8192),
+                       trials: int = 3, time_limit: float = 2.0, seed: int = 1, max_nodes: int = 1 << 21,
+                       goal_bias: float = 0.01, range_: float | None = None):
+    """Native wavefront-size autotuner (mptg_autotune_wavefront): the size with
+    the lowest median time to the first solution over `trials` seeds.
+    Returns (best size, {size: median seconds})."""
+    lib = load()
+    _sig(lib)
+    scene = Scene(ctx, scenario.desc)
+    prm = _Params()
+    rng = scenario.default_range if range_ is None else float(range_)
+    prm.range = rng if math.isfinite(rng) else 0.0
+    prm.goal_bias = goal_bias
+    prm.goal_radius = scenario.goal.radius
+    prm.edge_step = scenario.edge_step
+    prm.resolution = scenario.resolution
+    prm.wavefront = max(candidates)
+    prm.seed = int(seed) & ((1 << 64) - 1)
+    prm.max_nodes = int(max_nodes)
+    cand = (ctypes.c_int * len(candidates))(*candidates)
+    med = (ctypes.c_double * len(candidates))()
+    best = ctypes.c_int()
+    q0 = np.ascontiguousarray(start, dtype=np.float64)
+    g = np.ascontiguousarray(scenario.goal.state, dtype=np.float64)
+    _check(ctx.h, lib.mptg_autotune_wavefront(ctx.h, scene.h, ctypes.byref(prm), scenario.lo.ctypes.data,
+                                              scenario.hi.ctypes.data, q0.ctypes.data, g.ctypes.data,
+                                              scenario.goal.radius, cand, len(candidates), int(trials),
+                                              float(time_limit), ctypes.byref(best), med))
+    scene.close()
+    return best.value, {c: med[i] for i, c in enumerate(candidates)}
+
+
+__all__ = ["Planner", "autotune_wavefront", "PRRT", "Scenario", "GoalState", "gpu_wavefront", "report_stats", "max_threads",
            "single_threaded", "hardware_concurrency", "MptgError"]

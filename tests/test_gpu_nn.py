@@ -43,17 +43,19 @@ def test_nearest_matches_oracle(ctx, orc, name):
     assert len(tree) == n
     sp = orc.make_space(sc["metric"], sc["dim"], sc["weights"])
     oi, od = orc.nn_brute(sp, pts, q)
-    gi, gd = tree.nearest(q)  # < 2048 queries: warp-per-query search
-    assert np.array_equal(gi, oi), np.nonzero(gi != oi)[0][:10]
-    assert np.array_equal(gd.view(np.int64), od.view(np.int64))
-    li, ld = tree.nearest(q, linear=True)
-    assert np.array_equal(li, oi) and np.array_equal(ld.view(np.int64), od.view(np.int64))
-    # >= 2048 queries: spatially ordered packet search (32 queries per warp)
     q2 = np.concatenate([q, scenes.uniform_states(sc, 3001, 103)])
     oi2, od2 = orc.nn_brute(sp, pts, q2)
-    gi2, gd2 = tree.nearest(q2)
-    assert np.array_equal(gi2, oi2), np.nonzero(gi2 != oi2)[0][:10]
-    assert np.array_equal(gd2.view(np.int64), od2.view(np.int64))
+    for strategy in (tree.KDTREE, tree.EXHAUSTIVE, tree.AUTO):
+        tree.set_strategy(strategy)
+        gi, gd = tree.nearest(q)  # < 2048 queries: input order
+        assert np.array_equal(gi, oi), (strategy, np.nonzero(gi != oi)[0][:10])
+        assert np.array_equal(gd.view(np.int64), od.view(np.int64))
+        # >= 2048 queries: spatially ordered search
+        gi2, gd2 = tree.nearest(q2)
+        assert np.array_equal(gi2, oi2), (strategy, np.nonzero(gi2 != oi2)[0][:10])
+        assert np.array_equal(gd2.view(np.int64), od2.view(np.int64))
+    li, ld = tree.nearest(q, linear=True)
+    assert np.array_equal(li, oi) and np.array_equal(ld.view(np.int64), od.view(np.int64))
     # stored states come back unchanged
     assert np.array_equal(tree.states(), pts)
 
@@ -71,9 +73,24 @@ def test_nearest_ties_and_duplicates(ctx, orc):
     q = np.array([[2.0, 1.0], [1.0, 1.0], [0.5, 0.5], [4.5, 4.5], [9.0, 9.0], [100.0, -3.0]])
     sp = orc.make_space(0, 2)
     oi, od = orc.nn_brute(sp, pts, q)
-    gi, gd = tree.nearest(q)
-    assert np.array_equal(gi, oi) and np.array_equal(gd, od)
-    assert gi[1] == 0  # lowest id among 100 identical points at distance 0
+    for strategy in (tree.KDTREE, tree.EXHAUSTIVE):
+        tree.set_strategy(strategy)
+        gi, gd = tree.nearest(q)
+        assert np.array_equal(gi, oi) and np.array_equal(gd, od)
+        assert gi[1] == 0  # lowest id among 100 identical points at distance 0
+    # more than 8 points within the FP32 band of the minimum: the exhaustive
+    # sweep's second pass
+    pts8 = np.concatenate([np.repeat(np.array([[0.25] * 8]), 20, axis=0),
+                           scenes.uniform_states({"metric": 0, "dim": 8, "lo": np.zeros(8), "hi": np.ones(8)}, 500, 7)])
+    t8 = m.Tree(ctx, 0, 8, len(pts8))
+    t8.insert(pts8)
+    q8 = np.concatenate([np.full((3, 8), 0.25), np.full((2, 8), 0.2500001), np.random.default_rng(1).random((50, 8))])
+    oi8, od8 = orc.nn_brute(orc.make_space(0, 8), pts8, q8)
+    for strategy in (t8.KDTREE, t8.EXHAUSTIVE):
+        t8.set_strategy(strategy)
+        gi8, gd8 = t8.nearest(q8)
+        assert np.array_equal(gi8, oi8) and np.array_equal(gd8.view(np.int64), od8.view(np.int64))
+        assert (gi8[:5] == 0).all()
 
 
 def test_frontier_growth_rebuilds_and_stays_exact(ctx, orc):

@@ -135,3 +135,22 @@ def test_same_seed_same_tree(ctx):
     c.run(3)
     sc_, _ = c.graph()
     assert len(sc_) != len(sa) or not np.array_equal(sc_, sa)
+
+
+def test_phase_timers_and_wavefront_autotuner(ctx):
+    from mpt_gb300 import planner as P
+    sc = scenes.grid_scene()
+    pl = _planner(ctx, sc, 512, 3, 200000)
+    pl.solve_for(20.0, lambda: pl.solved())
+    t = pl.timers()
+    st = pl.stats()
+    assert set(t) == {"nearest", "surrogate", "valid_motion", "insert"}
+    # phases are stream-timeline spans; without a surrogate its span is only
+    # the gap between two event records
+    assert all(v >= 0 for v in t.values()) and t["surrogate"] <= 0.05 * sum(t.values()) + 1e-3
+    assert 0 < sum(t.values()) <= st["seconds"] * 1.05 + 1e-3
+    pl.close()
+    best, med = P.autotune_wavefront(ctx, P.Scenario(sc), sc["start"], candidates=(256, 2048), trials=1,
+                                     time_limit=5.0, seed=9)
+    assert best in (256, 2048) and set(med) == {256, 2048}
+    assert med[best] == min(med.values()) and med[best] < 5.0
