@@ -772,6 +772,14 @@ mptg_status mesh_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* do
     MPTG_CUDA_TRY(ctx, cudaMemsetAsync(x->nwork, 0, sizeof(int), s));
     k_mesh_sphere<<<mptg_blocks(n, 128), 128, 0, s>>>(v, dq, n, sc->D, dout, x->mwork, x->nwork);
     MPTG_LAUNCHED(ctx);
+    if (n <= 16384) {
+        // small batches: one block per state, the blocks past the device-side
+        // count leave at once, and no host round trip is needed
+        k_mesh_detail<<<n, MESH_DETAIL_THREADS, 0, s>>>(v, dq, sc->D, x->mwork, x->nwork, dout);
+        MPTG_LAUNCHED(ctx);
+        MPTG_CUDA_TRY(ctx, cudaGetLastError());
+        return MPTG_OK;
+    }
     MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(x->hbuf, x->nwork, sizeof(int), cudaMemcpyDeviceToHost, s));
     MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     int nw = x->hbuf[0];

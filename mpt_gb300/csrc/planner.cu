@@ -499,11 +499,12 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
     p->stat_wavefronts += 1;
     p->wave += 1;
     if (nacc > 0) {
-        st = mptg_tree_insert(p->tree, p->acc_states, nacc, s);
-        if (st) return st;
+        // enqueued ahead of the insert, whose counter read-back synchronises
+        // the stream, so the goal flags are on the host when it returns
         MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->parent + n0, p->acc_parent, nacc * sizeof(int), cudaMemcpyDeviceToDevice, s));
         MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->hgoal, p->acc_goal, nacc, cudaMemcpyDeviceToHost, s));
-        MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        st = mptg_tree_insert(p->tree, p->acc_states, nacc, s);
+        if (st) return st;
         for (int k = 0; k < nacc; ++k)
             if (p->hgoal[k]) p->goals.push_back((int)(n0 + k));
     }

@@ -152,6 +152,8 @@ __global__ void k_append(int4* __restrict__ nodes, const float* __restrict__ pts
                          int* __restrict__ leaf_reg) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    // k_convert rejected a state of this batch: leave the tree untouched
+    if (dcnt[CNT_ERR] & MPTG_DEVERR_BAD_STATE) return;
     int L = leaf_of[i];
     int slot = atomicAdd(&nodes[L].w, 1);
     if (slot < MPTG_BUCKET) {
@@ -1417,17 +1419,17 @@ mptg_status mptg_tree_insert(mptg_tree* t, const double* states, size_t n, void*
     k_convert<<<mptg_blocks(n, 256), 256, 0, s>>>(t->states64 + (size_t)first * D, t->pts32 + (size_t)first * D, nn,
                                                   D, t->metric, t->dcnt);
     MPTG_LAUNCHED(ctx);
+    // one host round trip: k_append does nothing when k_convert flagged a bad
+    // state, and the flag is read together with the overflow counts
+    k_locate<<<mptg_blocks(n, 256), 256, 0, s>>>(t->nodes, t->pts32, first, nn, D, t->leaf_of);
+    k_append<<<mptg_blocks(n, 256), 256, 0, s>>>(t->nodes, t->pts32, t->bpts, t->bids, first, nn, D, t->leaf_of,
+                                                 t->dcnt, t->ovf_pts, t->ovf_leaf, t->leaf_reg);
+    ctx->launches += 2;
     mptg_status st = read_counters(t, s);
     if (st) return st;
     if (t->hcnt[CNT_ERR] & MPTG_DEVERR_BAD_STATE)
         return mptg_fail(ctx, MPTG_ERR_INVALID_ARG,
                          "invalid state (NaN/inf, SO2 angle outside [-pi,pi], or non-unit quaternion)");
-    k_locate<<<mptg_blocks(n, 256), 256, 0, s>>>(t->nodes, t->pts32, first, nn, D, t->leaf_of);
-    k_append<<<mptg_blocks(n, 256), 256, 0, s>>>(t->nodes, t->pts32, t->bpts, t->bids, first, nn, D, t->leaf_of,
-                                                 t->dcnt, t->ovf_pts, t->ovf_leaf, t->leaf_reg);
-    ctx->launches += 2;
-    st = read_counters(t, s);
-    if (st) return st;
     int nreg = t->hcnt[CNT_NREG];
     int novf = t->hcnt[CNT_OVF];
     if (nreg > 0) {
@@ -1441,8 +1443,7 @@ mptg_status mptg_tree_insert(mptg_tree* t, const double* states, size_t n, void*
         if (st) return st;
     }
     MPTG_CUDA_TRY(ctx, cudaGetLastError());
-    st = read_counters(t, s);
-    if (st) return st;
+    // hcnt is current: read after k_append, or after the builder's last level
     t->n += n;
     // Leaf splits only see the points of one leaf, so a tree that keeps
     // growing at one frontier (a planner extending a corridor) degenerates
