@@ -264,6 +264,25 @@ mptg_status mptg_planner_set_surrogate_points(mptg_planner* planner, int points)
  * added, [3] tree size, [4] goals, [5] states checked by link, [6] seconds in
  * run, [7] wavefront counter. */
 mptg_status mptg_planner_stats(mptg_planner* planner, double out[8]);
+/* Planner<Scenario, PRRTStar<...>> (src/mpt/prrt_star.hpp:56-95): wavefronts
+ * with k-nearest rewiring (rewire_k_nearest, the reference default):
+ * k = ceil(rewire_factor * e * (1 + 1/dim) * ln(n + 1)), at most 64
+ * (src/mpt/impl/rrg_rewire_neighbors.hpp:47-66), rewire_factor default 1.1
+ * (PRRTStar::setRewireFactor, src/mpt/impl/prrt_star/prrt_star.hpp:234-240).
+ * Per wavefront, against the tree before it: choose-parent among the
+ * accepted state's k nearest in (cost + d, d, id) order with batched link
+ * checks; rewiring of the neighbours the choose step did not reach when
+ * cost(new) + d < cost(neighbour) and link(new, neighbour) holds (each
+ * neighbour takes the proposal with the smallest (cost, new id)); every cost
+ * is then recomputed from the edge lengths by pointer jumping.  Call before
+ * the first wavefront; enabled = 0 returns to plain PRRT. */
+mptg_status mptg_planner_set_rewire(mptg_planner* planner, int enabled, double rewire_factor);
+/* Each node's cost (Edge::cost, prrt_star.hpp) with rewiring on; out NULL
+ * queries n only. */
+mptg_status mptg_planner_costs(mptg_planner* planner, double* out, size_t cap, size_t* n);
+/* PRRT*'s Stats (prrt_star.hpp:121-152): [0] rewires applied, [1] links checked
+ * for choose-parent and rewiring */
+mptg_status mptg_planner_rewire_stats(mptg_planner* planner, double out[2]);
 /* WorkerStats' timers (prrt.hpp:72-101) on the GPU timeline, seconds summed
  * over wavefronts: [0] sample + nearest + steer, [1] surrogate scoring,
  * [2] valid motion (state + DMV link checks), [3] compaction + insert. */

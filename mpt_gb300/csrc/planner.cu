@@ -96,6 +96,31 @@ struct mptg_planner {
     // validMotion_ timers, prrt.hpp:72-101): events at the phase boundaries
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     double t_phase[4] = {0, 0, 0, 0};  // nearest, surrogate, valid motion, insert (seconds)
+    // PRRT* (mptg_planner_set_rewire)
+    int star = 0;
+    double rewire_factor = 1.1;
+    double* cost = nullptr;             // [cap_nodes]
+    double* elen = nullptr;             // [cap_nodes] length of the edge to the parent
+    double* pj_s = nullptr;             // [cap_nodes] pointer-jumping buffers
+    int* pj_a = nullptr;
+    int* pj_a2 = nullptr;
+    unsigned long long* bbits = nullptr;  // [cap_nodes] best rewire proposal per node
+    int* bid = nullptr;
+    int* knn_i = nullptr;               // [cap_wave][64]
+    double* knn_d = nullptr;
+    uint8_t* pv = nullptr;
+    int* s_pair = nullptr;
+    double* s_rcost = nullptr;
+    uint8_t* s_ok = nullptr;
+    double* s_ea = nullptr;             // [cap_wave * 64][D]
+    double* s_eb = nullptr;
+    double* dnear = nullptr;            // [cap_wave]
+    int* cpar = nullptr;
+    double* ccost = nullptr;
+    double* celen = nullptr;
+    int* s_cnt = nullptr;               // [2]
+    unsigned long long* nrw = nullptr;  // rewires applied
+    uint64_t stat_rewire_tests = 0;
 };
 
 extern "C" mptg_status mptg_surrogate_score_dev(mptg_surrogate* s, const double* dstates, int n, float* dlogits,
@@ -329,6 +354,167 @@ __global__ void k_plan_gather(const int* __restrict__ ids, int n, const double* 
     out[i] = states64[(size_t)ids[k] * D + d];
 }
 
+// ------------------------------------------------------------------ PRRT* (rewiring)
+// The worker's addSample of src/mpt/impl/prrt_star/prrt_star.hpp:505-657 as
+// wavefront steps (the CPU checker's orc_plan_star is the same algorithm):
+// k-nearest choose-parent in (cost + d, d, id) key order, rewiring of the
+// neighbours the choose loop did not reach, and costs recomputed by pointer
+// jumping over the edge lengths.
+
+__device__ __forceinline__ bool star_less(double c1, double d1, int i1, double c2, double d2, int i2) {
+    if (c1 != c2) return c1 < c2;
+    if (d1 != d2) return d1 < d2;
+    return i1 < i2;
+}
+
+// d(near, new) of every accepted new state
+__global__ void k_star_near(PlanView p, int A, const double* __restrict__ acc, const int* __restrict__ near,
+                            const double* __restrict__ states64, double* __restrict__ dnear) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A) return;
+    dnear[a] = dist64(p.metric, p.D, p.w0, p.w1, states64 + (size_t)near[a] * p.D, acc + (size_t)a * p.D);
+}
+
+__device__ __forceinline__ void copy_state(double* __restrict__ dst, const double* __restrict__ src, int D) {
+    for (int d = 0; d < D; ++d) dst[d] = src[d];
+}
+
+// choose-parent candidates: neighbour j of new state a whose key is below
+// near's; their links neighbour -> new are gathered (in any order) for one
+// batched DMV call
+__global__ void k_star_pc(PlanView p, int A, int k, const int* __restrict__ ki, const double* __restrict__ kd,
+                          const int* __restrict__ near, const double* __restrict__ dnear,
+                          const double* __restrict__ cost, const double* __restrict__ states64,
+                          const double* __restrict__ acc, int* __restrict__ cnt, int* __restrict__ pair_of,
+                          double* __restrict__ ea, double* __restrict__ eb) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A * k) return;
+    const int a = t / k, nb = ki[t], nr = near[a];
+    if (nb < 0 || nb == nr) return;
+    const double dj = kd[t], cj = __dadd_rn(cost[nb], dj);
+    const double dn = dnear[a], cn = __dadd_rn(cost[nr], dn);
+    if (!star_less(cj, dj, nb, cn, dn, nr)) return;
+    const int slot = atomicAdd(cnt, 1);  // < A * k
+    pair_of[slot] = t;
+    copy_state(ea + (size_t)slot * p.D, states64 + (size_t)nb * p.D, p.D);
+    copy_state(eb + (size_t)slot * p.D, acc + (size_t)a * p.D, p.D);
+}
+
+__global__ void k_star_scatter(int m, const int* __restrict__ pair_of, const uint8_t* __restrict__ ok,
+                               uint8_t* __restrict__ pv) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < m) pv[pair_of[s]] = ok[s];
+}
+
+// the parent: the smallest key among near and the valid candidates
+__global__ void k_star_choose(int A, int k, const int* __restrict__ ki, const double* __restrict__ kd,
+                              const int* __restrict__ near, const double* __restrict__ dnear,
+                              const double* __restrict__ cost, const uint8_t* __restrict__ pv, int* __restrict__ cpar,
+                              double* __restrict__ ccost, double* __restrict__ celen) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A) return;
+    int bp = near[a];
+    double bd = dnear[a], bc = __dadd_rn(cost[bp], bd);
+    for (int j = 0; j < k; ++j) {
+        const int t = a * k + j;
+        if (!pv[t]) continue;
+        const int nb = ki[t];
+        const double dj = kd[t], cj = __dadd_rn(cost[nb], dj);
+        if (star_less(cj, dj, nb, bc, bd, bp)) { bp = nb; bc = cj; bd = dj; }
+    }
+    cpar[a] = bp;
+    ccost[a] = bc;
+    celen[a] = bd;
+}
+
+// rewire candidates: neighbours past the chosen parent in key order with
+// cost(new) + d < cost(neighbour); links new -> neighbour gathered
+__global__ void k_star_rw(PlanView p, int A, int k, const int* __restrict__ ki, const double* __restrict__ kd,
+                          const double* __restrict__ cost, const int* __restrict__ cpar,
+                          const double* __restrict__ ccost, const double* __restrict__ celen,
+                          const double* __restrict__ states64, const double* __restrict__ acc, int* __restrict__ cnt,
+                          int* __restrict__ pair_of, double* __restrict__ rcost, double* __restrict__ ea,
+                          double* __restrict__ eb) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A * k) return;
+    const int a = t / k, nb = ki[t];
+    if (nb < 0) return;
+    const double dj = kd[t], cj = __dadd_rn(cost[nb], dj);
+    if (!star_less(ccost[a], celen[a], cpar[a], cj, dj, nb)) return;  // reached by the choose loop
+    const double nc = __dadd_rn(ccost[a], dj);
+    if (!(nc < cost[nb])) return;
+    const int slot = atomicAdd(cnt, 1);
+    pair_of[slot] = t;
+    rcost[slot] = nc;
+    copy_state(ea + (size_t)slot * p.D, acc + (size_t)a * p.D, p.D);
+    copy_state(eb + (size_t)slot * p.D, states64 + (size_t)nb * p.D, p.D);
+}
+
+// each neighbour takes the valid proposal with the smallest (cost, new id):
+// costs are >= 0, so their bit patterns order as unsigned integers
+__global__ void k_star_rw_min(int m, const int* __restrict__ pair_of, const double* __restrict__ rcost,
+                              const uint8_t* __restrict__ ok, const int* __restrict__ ki,
+                              unsigned long long* __restrict__ bbits) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= m || !ok[s]) return;
+    atomicMin(&bbits[ki[pair_of[s]]], (unsigned long long)__double_as_longlong(rcost[s]));
+}
+
+__global__ void k_star_rw_id(int m, int k, const int* __restrict__ pair_of, const double* __restrict__ rcost,
+                             const uint8_t* __restrict__ ok, const int* __restrict__ ki,
+                             const unsigned long long* __restrict__ bbits, int* __restrict__ bid) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= m || !ok[s]) return;
+    const int nb = ki[pair_of[s]];
+    if ((unsigned long long)__double_as_longlong(rcost[s]) == bbits[nb]) atomicMin(&bid[nb], pair_of[s] / k);
+}
+
+__global__ void k_star_rw_apply(int m, int k, int n0, const int* __restrict__ pair_of, const double* __restrict__ rcost,
+                                const uint8_t* __restrict__ ok, const int* __restrict__ ki,
+                                const double* __restrict__ kd, const unsigned long long* __restrict__ bbits,
+                                const int* __restrict__ bid, int* __restrict__ parent, double* __restrict__ elen,
+                                unsigned long long* __restrict__ nrw) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= m || !ok[s]) return;
+    const int t = pair_of[s], nb = ki[t], a = t / k;
+    if ((unsigned long long)__double_as_longlong(rcost[s]) != bbits[nb] || bid[nb] != a) return;
+    parent[nb] = n0 + a;
+    elen[nb] = kd[t];
+    atomicAdd(nrw, 1ull);
+}
+
+__global__ void k_star_rw_reset(int m, const int* __restrict__ pair_of, const int* __restrict__ ki,
+                                unsigned long long* __restrict__ bbits, int* __restrict__ bid) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= m) return;
+    const int nb = ki[pair_of[s]];
+    bbits[nb] = ~0ull;
+    bid[nb] = INT_MAX;
+}
+
+__global__ void k_star_insert(int A, int n0, const int* __restrict__ cpar, const double* __restrict__ celen,
+                              int* __restrict__ parent, double* __restrict__ elen) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A) return;
+    parent[n0 + a] = cpar[a];
+    elen[n0 + a] = celen[a];
+}
+
+// one pointer-jumping round: s[x] += s[a[x]], a[x] = a[a[x]]
+__global__ void k_star_pj(int n, const double* __restrict__ s_in, const int* __restrict__ a_in,
+                          double* __restrict__ s_out, int* __restrict__ a_out) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    const int a = a_in[x];
+    if (a >= 0) {
+        s_out[x] = __dadd_rn(s_in[x], s_in[a]);
+        a_out[x] = a_in[a];
+    } else {
+        s_out[x] = s_in[x];
+        a_out[x] = -1;
+    }
+}
+
 // ------------------------------------------------------------------ host
 
 static PlanView plan_view(const mptg_planner* p) {
@@ -345,7 +531,10 @@ static PlanView plan_view(const mptg_planner* p) {
 static void planner_free(mptg_planner* p) {
     void* ptrs[] = {p->lo, p->hi, p->goal, p->parent, p->samp, p->nidx, p->ndist, p->nearst, p->newst, p->skip,
                     p->ok, p->scan, p->bsum, p->acc_states, p->acc_parent, p->acc_goal, p->nsamp, p->logits,
-                    p->near_c, p->new_c, p->cmap, p->ok_c, p->keep, p->path_ids, p->path_out, p->sg_pts};
+                    p->near_c, p->new_c, p->cmap, p->ok_c, p->keep, p->path_ids, p->path_out, p->sg_pts,
+                    p->cost, p->elen, p->pj_s, p->pj_a, p->pj_a2, p->bbits, p->bid, p->knn_i, p->knn_d, p->pv,
+                    p->s_pair, p->s_rcost, p->s_ok, p->s_ea, p->s_eb, p->dnear, p->cpar, p->ccost, p->celen,
+                    p->s_cnt, p->nrw};
     if (p->stream) cudaStreamSynchronize(p->stream);
     for (void* x : ptrs)
         if (x) cudaFree(x);
@@ -412,6 +601,87 @@ static mptg_status planner_reset(mptg_planner* p, const mptg_plan_params* prm, b
     p->stat_skipped = p->stat_culled = 0;
     p->stat_seconds = 0;
     for (double& t : p->t_phase) t = 0;
+    p->stat_rewire_tests = 0;
+    if (p->nrw) MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->nrw, 0, sizeof(unsigned long long), p->stream));
+    return MPTG_OK;
+}
+
+// PRRT* steps of one wavefront on the A accepted new states (acc_states,
+// nearest node acc_parent), against the tree of n0 nodes as it stood before
+// the wavefront: choose-parent (cpar / ccost / celen) and rewiring of old
+// nodes (parent / elen).  The new nodes are inserted by the caller.
+static mptg_status star_wave(mptg_planner* p, cudaStream_t s, int A, size_t n0) {
+    mptg_ctx* ctx = p->ctx;
+    const PlanView v = plan_view(p);
+    const double* st64 = mptg_tree_states_dev(p->tree);
+    int k = (int)ceil(p->rewire_factor * 2.718281828459045 * (1.0 + 1.0 / p->D) * log((double)n0 + 1.0));
+    k = std::max(1, std::min(k, std::min(64, (int)n0)));
+    const int pairs = A * k;
+    mptg_status st;
+    k_star_near<<<mptg_blocks(A, 128), 128, 0, s>>>(v, A, p->acc_states, p->acc_parent, st64, p->dnear);
+    MPTG_LAUNCHED(ctx);
+    if ((st = mptg_tree_nearest_k_dev(p->tree, p->acc_states, A, k, p->knn_i, p->knn_d, s))) return st;
+    // choose parent
+    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->s_cnt, 0, 2 * sizeof(int), s));
+    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->pv, 0, pairs, s));
+    k_star_pc<<<mptg_blocks(pairs, 128), 128, 0, s>>>(v, A, k, p->knn_i, p->knn_d, p->acc_parent, p->dnear, p->cost,
+                                                     st64, p->acc_states, p->s_cnt, p->s_pair, p->s_ea, p->s_eb);
+    MPTG_LAUNCHED(ctx);
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->hbuf + 2, p->s_cnt, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    const int npc = p->hbuf[2];
+    if (npc > 0) {
+        if ((st = scene_edges_dev(p->scene, p->s_ea, p->s_eb, npc, p->prm.edge_step, p->prm.resolution, p->s_ok, s,
+                                  p->nsamp, &p->scratch)))
+            return st;
+        k_star_scatter<<<mptg_blocks(npc, 256), 256, 0, s>>>(npc, p->s_pair, p->s_ok, p->pv);
+        MPTG_LAUNCHED(ctx);
+    }
+    k_star_choose<<<mptg_blocks(A, 128), 128, 0, s>>>(A, k, p->knn_i, p->knn_d, p->acc_parent, p->dnear, p->cost,
+                                                      p->pv, p->cpar, p->ccost, p->celen);
+    // rewire
+    k_star_rw<<<mptg_blocks(pairs, 128), 128, 0, s>>>(v, A, k, p->knn_i, p->knn_d, p->cost, p->cpar, p->ccost,
+                                                     p->celen, st64, p->acc_states, p->s_cnt + 1, p->s_pair,
+                                                     p->s_rcost, p->s_ea, p->s_eb);
+    ctx->launches += 2;
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->hbuf + 3, p->s_cnt + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    const int nrc = p->hbuf[3];
+    p->stat_rewire_tests += (uint64_t)(npc + nrc);
+    if (nrc > 0) {
+        if ((st = scene_edges_dev(p->scene, p->s_ea, p->s_eb, nrc, p->prm.edge_step, p->prm.resolution, p->s_ok, s,
+                                  p->nsamp, &p->scratch)))
+            return st;
+        const unsigned g = mptg_blocks(nrc, 256);
+        k_star_rw_min<<<g, 256, 0, s>>>(nrc, p->s_pair, p->s_rcost, p->s_ok, p->knn_i, p->bbits);
+        k_star_rw_id<<<g, 256, 0, s>>>(nrc, k, p->s_pair, p->s_rcost, p->s_ok, p->knn_i, p->bbits, p->bid);
+        k_star_rw_apply<<<g, 256, 0, s>>>(nrc, k, (int)n0, p->s_pair, p->s_rcost, p->s_ok, p->knn_i, p->knn_d,
+                                          p->bbits, p->bid, p->parent, p->elen, p->nrw);
+        k_star_rw_reset<<<g, 256, 0, s>>>(nrc, p->s_pair, p->knn_i, p->bbits, p->bid);
+        ctx->launches += 4;
+    }
+    return MPTG_OK;
+}
+
+// every node's cost from the edge lengths by pointer jumping,
+// ceil(log2(n + 1)) rounds (the depth is below n)
+static mptg_status star_costs(mptg_planner* p, cudaStream_t s, size_t n) {
+    mptg_ctx* ctx = p->ctx;
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->pj_s, p->elen, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->pj_a, p->parent, n * sizeof(int), cudaMemcpyDeviceToDevice, s));
+    int rounds = 0;
+    while (((size_t)1 << rounds) < n + 1) ++rounds;
+    double* sa = p->pj_s;
+    double* sb = p->cost;
+    int* aa = p->pj_a;
+    int* ab = p->pj_a2;
+    for (int r = 0; r < rounds; ++r) {
+        k_star_pj<<<mptg_blocks(n, 256), 256, 0, s>>>((int)n, sa, aa, sb, ab);
+        std::swap(sa, sb);
+        std::swap(aa, ab);
+    }
+    ctx->launches += rounds;
+    if (sa != p->cost) MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->cost, sa, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
     return MPTG_OK;
 }
 
@@ -499,12 +769,21 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
     p->stat_wavefronts += 1;
     p->wave += 1;
     if (nacc > 0) {
+        if (p->star) {
+            // choose-parent and rewiring against the tree before the insert
+            if ((st = star_wave(p, s, nacc, n0))) return st;
+            k_star_insert<<<mptg_blocks(nacc, 128), 128, 0, s>>>(nacc, (int)n0, p->cpar, p->celen, p->parent, p->elen);
+            MPTG_LAUNCHED(ctx);
+        } else {
+            MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->parent + n0, p->acc_parent, nacc * sizeof(int),
+                                               cudaMemcpyDeviceToDevice, s));
+        }
         // enqueued ahead of the insert, whose counter read-back synchronises
         // the stream, so the goal flags are on the host when it returns
-        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->parent + n0, p->acc_parent, nacc * sizeof(int), cudaMemcpyDeviceToDevice, s));
         MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->hgoal, p->acc_goal, nacc, cudaMemcpyDeviceToHost, s));
         st = mptg_tree_insert(p->tree, p->acc_states, nacc, s);
         if (st) return st;
+        if (p->star && (st = star_costs(p, s, n0 + nacc))) return st;
         for (int k = 0; k < nacc; ++k)
             if (p->hgoal[k]) p->goals.push_back((int)(n0 + k));
     }
@@ -614,6 +893,10 @@ mptg_status mptg_planner_add_start(mptg_planner* p, const double* q) {
     if (st) return st;
     const int minus1 = -1;
     MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(p->parent + n, &minus1, sizeof(int), cudaMemcpyHostToDevice, p->stream));
+    if (p->star) {
+        MPTG_CUDA_TRY(p->ctx, cudaMemsetAsync(p->cost + n, 0, sizeof(double), p->stream));
+        MPTG_CUDA_TRY(p->ctx, cudaMemsetAsync(p->elen + n, 0, sizeof(double), p->stream));
+    }
     MPTG_CUDA_TRY(p->ctx, cudaStreamSynchronize(p->stream));
     return MPTG_OK;
 }
@@ -778,6 +1061,83 @@ mptg_status mptg_planner_set_surrogate_points(mptg_planner* p, int points) {
         p->sg_pts_cap = points;
     }
     p->sg_points = points;
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_set_rewire(mptg_planner* p, int enabled, double rewire_factor) {
+    if (!p) return MPTG_ERR_INVALID_ARG;
+    mptg_ctx* ctx = p->ctx;
+    if (!(rewire_factor > 0) || !std::isfinite(rewire_factor))
+        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "rewire factor must be positive");
+    if (p->stat_wavefronts > 0)
+        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "rewiring must be chosen before the first wavefront");
+    p->rewire_factor = rewire_factor;
+    if (!enabled) { p->star = 0; return MPTG_OK; }
+    if (!p->cost) {
+        const size_t N = p->cap_nodes, W = p->cap_wave, D = p->D, P = W * 64;
+        cudaError_t e = cudaSuccess;
+#define ALLOC(ptr, bytes) if (e == cudaSuccess) e = cudaMalloc((void**)&(ptr), (bytes))
+        ALLOC(p->cost, N * sizeof(double));
+        ALLOC(p->elen, N * sizeof(double));
+        ALLOC(p->pj_s, N * sizeof(double));
+        ALLOC(p->pj_a, N * sizeof(int));
+        ALLOC(p->pj_a2, N * sizeof(int));
+        ALLOC(p->bbits, N * sizeof(unsigned long long));
+        ALLOC(p->bid, N * sizeof(int));
+        ALLOC(p->knn_i, P * sizeof(int));
+        ALLOC(p->knn_d, P * sizeof(double));
+        ALLOC(p->pv, P);
+        ALLOC(p->s_pair, P * sizeof(int));
+        ALLOC(p->s_rcost, P * sizeof(double));
+        ALLOC(p->s_ok, P);
+        ALLOC(p->s_ea, P * D * sizeof(double));
+        ALLOC(p->s_eb, P * D * sizeof(double));
+        ALLOC(p->dnear, W * sizeof(double));
+        ALLOC(p->cpar, W * sizeof(int));
+        ALLOC(p->ccost, W * sizeof(double));
+        ALLOC(p->celen, W * sizeof(double));
+        ALLOC(p->s_cnt, 2 * sizeof(int));
+        ALLOC(p->nrw, sizeof(unsigned long long));
+#undef ALLOC
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return mptg_fail(ctx, MPTG_ERR_OOM, "rewiring buffers: %s", cudaGetErrorString(e));
+        }
+        MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->bbits, 0xff, N * sizeof(unsigned long long), p->stream));
+        MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->bid, 0x7f, N * sizeof(int), p->stream));
+    }
+    // every node so far is a start: no parent, cost 0
+    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->cost, 0, p->cap_nodes * sizeof(double), p->stream));
+    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->elen, 0, p->cap_nodes * sizeof(double), p->stream));
+    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->nrw, 0, sizeof(unsigned long long), p->stream));
+    MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(p->stream));
+    p->star = 1;
+    p->stat_rewire_tests = 0;
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_costs(mptg_planner* p, double* out, size_t cap, size_t* n) {
+    if (!p || !n) return MPTG_ERR_INVALID_ARG;
+    size_t sz = 0;
+    mptg_tree_size(p->tree, &sz);
+    *n = sz;
+    if (!out) return MPTG_OK;
+    if (!p->star) return mptg_fail(p->ctx, MPTG_ERR_INVALID_ARG, "node costs are kept with rewiring only");
+    if (sz > cap) return mptg_fail(p->ctx, MPTG_ERR_CAPACITY, "%zu costs do not fit %zu", sz, cap);
+    MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(out, p->cost, sz * sizeof(double), cudaMemcpyDefault, p->stream));
+    MPTG_CUDA_TRY(p->ctx, cudaStreamSynchronize(p->stream));
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_rewire_stats(mptg_planner* p, double out[2]) {
+    if (!p || !out) return MPTG_ERR_INVALID_ARG;
+    unsigned long long n = 0;
+    if (p->nrw) {
+        MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(&n, p->nrw, sizeof(n), cudaMemcpyDeviceToHost, p->stream));
+        MPTG_CUDA_TRY(p->ctx, cudaStreamSynchronize(p->stream));
+    }
+    out[0] = (double)n;
+    out[1] = (double)p->stat_rewire_tests;
     return MPTG_OK;
 }
 

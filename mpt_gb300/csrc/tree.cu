@@ -1605,6 +1605,18 @@ mptg_status mptg_nearest_linear(mptg_tree* t, const double* q, size_t nq, int32_
     return mptg_stage_finish(ctx, s, outs, 2, &bq, 1);
 }
 
+mptg_status mptg_tree_nearest_k_dev(mptg_tree* t, const double* dq, int nq, int k, int* didx, double* dd,
+                                    cudaStream_t s) {
+    if (nq <= 0) return MPTG_OK;
+    if (k < 1 || k > 64) return mptg_fail(t->ctx, MPTG_ERR_INVALID_ARG, "k=%d outside [1,64]", k);
+    TreeView v = view_of(t);
+    v.stats = nullptr;
+    unsigned grid = mptg_blocks((size_t)nq * 32, 256);
+    DISPATCH_METRIC(t->metric, t->D, k_nearest_k, grid, 256, s, v, dq, nq, k, (double)INFINITY, didx, dd);
+    MPTG_LAUNCHED(t->ctx);
+    return MPTG_OK;
+}
+
 mptg_status mptg_nearest_k(mptg_tree* t, const double* q, size_t nq, int k, double r, int32_t* idx, double* dist,
                            void* stream) {
     if (!t) return MPTG_ERR_INVALID_ARG;

@@ -51,6 +51,8 @@ hardware_concurrency = max_threads(0)
 class PRRT:
     """Option pack (src/mpt/prrt.hpp:56-71); order of options does not matter."""
 
+    rewire = False
+
     def __init__(self, *options):
         self.wavefront = 4096
         self.report_stats = False
@@ -67,6 +69,13 @@ class PRRT:
     def __eq__(self, other):
         return isinstance(other, PRRT) and (self.wavefront, self.report_stats) == (other.wavefront,
                                                                                    other.report_stats)
+
+
+class PRRTStar(PRRT):
+    """Option pack of PRRTStar (src/mpt/prrt_star.hpp:56-95): the wavefront
+    planner with k-nearest rewiring (rewire_k_nearest, the reference default)."""
+
+    rewire = True
 
 
 class GoalState:
@@ -112,6 +121,9 @@ def _sig(L):
         ("mptg_planner_graph", ctypes.c_int, [P, P, P, S, ctypes.POINTER(S)]),
         ("mptg_planner_stats", ctypes.c_int, [P, P]),
         ("mptg_planner_timers", ctypes.c_int, [P, P]),
+        ("mptg_planner_set_rewire", ctypes.c_int, [P, ctypes.c_int, ctypes.c_double]),
+        ("mptg_planner_rewire_stats", ctypes.c_int, [P, P]),
+        ("mptg_planner_costs", ctypes.c_int, [P, P, S, ctypes.POINTER(S)]),
         ("mptg_autotune_wavefront", ctypes.c_int, [P, P, P, P, P, P, P, ctypes.c_double, P, ctypes.c_int,
                                                    ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_int), P]),
     ]:
@@ -137,6 +149,7 @@ class Planner:
         self.max_nodes = int(max_nodes)
         self._range = scenario.default_range
         self._goal_bias = 0.01
+        self._rewire_factor = 1.1
         self._starts = []
         self._surrogate = None
         self.scene = Scene(self.ctx, scenario.desc)
@@ -170,6 +183,15 @@ class Planner:
         assert 0 <= b <= 1
         self._goal_bias = float(b)
         self._require_fresh("set_goal_bias")
+
+    def set_rewire_factor(self, f: float):
+        """PRRTStar::setRewireFactor (src/mpt/impl/prrt_star/prrt_star.hpp:234-240)."""
+        assert f > 0
+        self._rewire_factor = float(f)
+        self._require_fresh("set_rewire_factor")
+
+    def get_rewire_factor(self) -> float:
+        return self._rewire_factor
 
     def get_goal_bias(self) -> float:
         return self._goal_bias
@@ -205,6 +227,8 @@ class Planner:
         self.h = h
         g = np.ascontiguousarray(sc.goal.state, dtype=np.float64)
         _check(self.ctx.h, self.lib.mptg_planner_set_goal(h, g.ctypes.data, sc.goal.radius))
+        if self.algorithm.rewire:
+            _check(self.ctx.h, self.lib.mptg_planner_set_rewire(h, 1, self._rewire_factor))
         for q in self._starts:
             _check(self.ctx.h, self.lib.mptg_planner_add_start(h, q.ctypes.data))
         self._starts = []
@@ -300,6 +324,19 @@ class Planner:
                 "wavefront_counter"]
         return dict(zip(keys, [float(v) for v in out]))
 
+    def costs(self) -> np.ndarray:
+        """Each node's cost (PRRTStar only)."""
+        n = ctypes.c_size_t()
+        _check(self.ctx.h, self.lib.mptg_planner_costs(self.h, None, 0, ctypes.byref(n)))
+        out = np.empty(n.value, dtype=np.float64)
+        _check(self.ctx.h, self.lib.mptg_planner_costs(self.h, out.ctypes.data, n.value, ctypes.byref(n)))
+        return out
+
+    def rewire_stats(self) -> dict:
+        out = (ctypes.c_double * 2)()
+        _check(self.ctx.h, self.lib.mptg_planner_rewire_stats(self.h, out))
+        return {"rewires": int(out[0]), "rewire_tests": int(out[1])}
+
     def timers(self) -> dict:
         """Seconds per phase on the GPU timeline (WorkerStats' nearest / validMotion
         timers, src/mpt/impl/prrt/prrt.hpp:72-101)."""
@@ -339,6 +376,8 @@ class Planner:
     getRange = get_range
     setGoalBias = set_goal_bias
     getGoalBias = get_goal_bias
+    setRewireFactor = set_rewire_factor
+    getRewireFactor = get_rewire_factor
     printStats = print_stats
     visitGraph = visit_graph
 
@@ -375,5 +414,5 @@ def autotune_wavefront(ctx: Context, scenario: Scenario, start, candidates=(256,
     return best.value, {c: med[i] for i, c in enumerate(candidates)}
 
 
-__all__ = ["Planner", "autotune_wavefront", "PRRT", "Scenario", "GoalState", "gpu_wavefront", "report_stats", "max_threads",
+__all__ = ["Planner", "PRRTStar", "autotune_wavefront", "PRRT", "Scenario", "GoalState", "gpu_wavefront", "report_stats", "max_threads",
            "single_threaded", "hardware_concurrency", "MptgError"]

@@ -265,6 +265,43 @@ def plan(desc: dict, space: Space, params: dict, lo, hi, start, goal, max_waves:
     return states[:n].copy(), parents[:n].copy(), goals[:ng.value].copy()
 
 
+def plan_star(desc: dict, space: Space, params: dict, lo, hi, start, goal, max_waves: int, rewire_factor: float = 1.1,
+              nthreads: int = 0):
+    """Replay of the wavefront PRRT* planner: (states, parents, costs, goal ids, rewires)."""
+    L = lib()
+    if not getattr(L, "_plan_star_sig", False):
+        P = ctypes.c_void_p
+        L.orc_plan_star.restype = ctypes.c_int64
+        L.orc_plan_star.argtypes = [P, P, P, P, P, P, P, ctypes.c_int, ctypes.c_double, P, P, P, P, P, P,
+                                    ctypes.c_int]
+        L._plan_star_sig = True
+    sc, keep = make_scene(desc)
+    pp = PlanParams()
+    for k in ("range", "goal_bias", "goal_radius", "edge_step"):
+        setattr(pp, k, float(params[k]))
+    pp.resolution = int(params["resolution"])
+    pp.wavefront = int(params["wavefront"])
+    pp.seed = int(params["seed"])
+    pp.max_nodes = int(params["max_nodes"])
+    D = space.dim
+    lo = np.ascontiguousarray(lo, dtype=np.float64)
+    hi = np.ascontiguousarray(hi, dtype=np.float64)
+    start = np.ascontiguousarray(start, dtype=np.float64)
+    g = None if goal is None else np.ascontiguousarray(goal, dtype=np.float64)
+    states = np.empty((pp.max_nodes, D), dtype=np.float64)
+    parents = np.empty(pp.max_nodes, dtype=np.int32)
+    costs = np.empty(pp.max_nodes, dtype=np.float64)
+    goals = np.empty(pp.max_nodes, dtype=np.int32)
+    ng = ctypes.c_int64(0)
+    nrw = ctypes.c_int64(0)
+    n = L.orc_plan_star(ctypes.byref(sc), ctypes.byref(space), ctypes.byref(pp), _ptr(lo), _ptr(hi), _ptr(start),
+                        None if g is None else _ptr(g), int(max_waves), float(rewire_factor), _ptr(states),
+                        _ptr(parents), _ptr(costs), _ptr(goals), ctypes.byref(ng), ctypes.byref(nrw),
+                        nthreads or os.cpu_count())
+    del keep
+    return states[:n].copy(), parents[:n].copy(), costs[:n].copy(), goals[:ng.value].copy(), nrw.value
+
+
 def uniform(seed: int, i: int, w: int, j: int) -> float:
     lib()
     if not getattr(_lib, "_plan_sig", False):

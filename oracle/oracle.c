@@ -806,6 +806,35 @@ static void plan_sample(const orc_space* sp, const orc_plan_params* pp, const do
     }
 }
 
+/* One wavefront's candidates (prrt.hpp:411-442): sample i, its nearest tree
+ * node par[i] among the first n states, the steered new state nw[i] and
+ * ok[i] = valid(new) && link(near, new), all against the tree as it stood
+ * before the wavefront. */
+static void plan_wave(const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp, const double* lo,
+                      const double* hi, const double* goal, int goal_index, int w, double range, double inv,
+                      const double* states, int64_t n, double* nw, int32_t* par, uint8_t* ok, int nthreads) {
+    const int D = sp->dim, W = pp->wavefront;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads_or_default(nthreads))
+    for (int i = 0; i < W; ++i) {
+        double s[16], a[16];
+        plan_sample(sp, pp, lo, hi, goal, goal_index, (uint32_t)i, (uint32_t)w, s);
+        double best = INFINITY;
+        int32_t bi = -1;
+        for (int64_t j = 0; j < n; ++j) {
+            double dj = orc_distance(sp, s, states + j * D);
+            if (dj < best || (bi < 0 && dj == best)) { best = dj; bi = (int32_t)j; }
+        }
+        ok[i] = 0;
+        if (bi < 0 || best == 0.0 || best != best) continue;
+        for (int d = 0; d < D; ++d) a[d] = states[(int64_t)bi * D + d];
+        double* q = nw + (size_t)i * D;
+        if (best > range) orc_interpolate(sp, a, s, range / best, q);
+        else for (int d = 0; d < D; ++d) q[d] = s[d];
+        par[i] = bi;
+        ok[i] = (uint8_t)dmv_edge(sc, sp, a, q, inv, pp->resolution, NULL);
+    }
+}
+
 int64_t orc_plan(const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp, const double* lo,
                  const double* hi, const double* start, const double* goal, int max_waves, int stop_when_solved,
                  double* states, int32_t* parents, int32_t* goals, int64_t* ngoals, int nthreads) {
@@ -829,25 +858,7 @@ int64_t orc_plan(const orc_scene* sc, const orc_space* sp, const orc_plan_params
         if (goal && ng == 0 && pp->goal_bias > 0)
             for (int i = 0; i < W; ++i)
                 if (orc_uniform(pp->seed, (uint32_t)i, (uint32_t)w, 16) < pp->goal_bias) { goal_index = i; break; }
-#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads_or_default(nthreads))
-        for (int i = 0; i < W; ++i) {
-            double s[16], a[16];
-            plan_sample(sp, pp, lo, hi, goal, goal_index, (uint32_t)i, (uint32_t)w, s);
-            double best = INFINITY;
-            int32_t bi = -1;
-            for (int64_t j = 0; j < n; ++j) {
-                double dj = orc_distance(sp, s, states + j * D);
-                if (dj < best || (bi < 0 && dj == best)) { best = dj; bi = (int32_t)j; }
-            }
-            ok[i] = 0;
-            if (bi < 0 || best == 0.0 || best != best) continue;
-            for (int d = 0; d < D; ++d) a[d] = states[(int64_t)bi * D + d];
-            double* q = nw + (size_t)i * D;
-            if (best > range) orc_interpolate(sp, a, s, range / best, q);
-            else for (int d = 0; d < D; ++d) q[d] = s[d];
-            par[i] = bi;
-            ok[i] = (uint8_t)dmv_edge(sc, sp, a, q, inv, pp->resolution, NULL);
-        }
+        plan_wave(sc, sp, pp, lo, hi, goal, goal_index, w, range, inv, states, n, nw, par, ok, nthreads);
         for (int i = 0; i < W && n < pp->max_nodes; ++i) {
             if (!ok[i]) continue;
             for (int d = 0; d < D; ++d) states[n * D + d] = nw[(size_t)i * D + d];
@@ -858,5 +869,174 @@ int64_t orc_plan(const orc_scene* sc, const orc_space* sp, const orc_plan_params
     }
     free(nw); free(par); free(ok);
     *ngoals = ng;
+    return n;
+}
+
+/* ------------------------------------------------------------------ */
+/* Wavefront PRRT*: the worker's addSample of
+ * src/mpt/impl/prrt_star/prrt_star.hpp:505-657 with the neighbourhood of
+ * src/mpt/impl/rrg_rewire_neighbors.hpp:47-66, restated for wavefronts.
+ * Per wavefront, against the tree as it stood before it:
+ *  1. the PRRT candidates (plan_wave), accepted in sample order up to the
+ *     node budget;
+ *  2. k = ceil(f e (1 + 1/dim) ln(n0 + 1)) (at most 64 and n0) nearest old
+ *     nodes of each new state, sorted by (distance, id);
+ *  3. choose parent: the key of a neighbour is (cost + d, d, id); near keeps
+ *     (cost[near] + d(near, new), d(near, new), near); the parent is the
+ *     smallest key among near and the neighbours whose key is below near's
+ *     and whose link(neighbour, new) is valid;
+ *  4. insert the new nodes (ids n0 + a in acceptance order) with that parent;
+ *  5. rewire: every neighbour whose key is above the chosen parent's (the
+ *     ones the reference's sorted loop did not reach) with
+ *     cost(new) + d < cost(neighbour) and a valid link(new, neighbour)
+ *     proposes the new node as its parent; each neighbour takes the proposal
+ *     with the smallest (cost, new id);
+ *  6. every cost is recomputed from the edge lengths by pointer jumping:
+ *     s <- elen, a <- parent; ceil(log2(n + 1)) rounds of
+ *     s[x] <- s[x] + s[a[x]], a[x] <- a[a[x]] (for a[x] >= 0).
+ * Costs are therefore sums in pointer-jumping order, the definition the GPU
+ * planner computes bit for bit. */
+static int star_key_less(double c1, double d1, int32_t i1, double c2, double d2, int32_t i2) {
+    if (c1 != c2) return c1 < c2;
+    if (d1 != d2) return d1 < d2;
+    return i1 < i2;
+}
+
+static void star_costs(const int32_t* parents, const double* elen, int64_t n, double* costs) {
+    double* s = (double*)malloc((size_t)n * sizeof(double));
+    double* s2 = (double*)malloc((size_t)n * sizeof(double));
+    int32_t* a = (int32_t*)malloc((size_t)n * sizeof(int32_t));
+    int32_t* a2 = (int32_t*)malloc((size_t)n * sizeof(int32_t));
+    for (int64_t x = 0; x < n; ++x) { s[x] = elen[x]; a[x] = parents[x]; }
+    int rounds = 0;
+    while (((int64_t)1 << rounds) < n + 1) ++rounds;
+    for (int r = 0; r < rounds; ++r) {
+        for (int64_t x = 0; x < n; ++x) {
+            if (a[x] >= 0) { s2[x] = s[x] + s[a[x]]; a2[x] = a[a[x]]; }
+            else { s2[x] = s[x]; a2[x] = -1; }
+        }
+        double* ts = s; s = s2; s2 = ts;
+        int32_t* ta = a; a = a2; a2 = ta;
+    }
+    for (int64_t x = 0; x < n; ++x) costs[x] = s[x];
+    free(s); free(s2); free(a); free(a2);
+}
+
+int64_t orc_plan_star(const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp, const double* lo,
+                      const double* hi, const double* start, const double* goal, int max_waves,
+                      double rewire_factor, double* states, int32_t* parents, double* costs, int32_t* goals,
+                      int64_t* ngoals, int64_t* rewires, int nthreads) {
+    const int D = sp->dim, W = pp->wavefront;
+    const double range = pp->range > 0 ? pp->range : INFINITY;
+    const double inv = 1.0 / pp->edge_step;
+    int64_t n = 1, ng = 0, nrw = 0;
+    for (int d = 0; d < D; ++d) states[d] = start[d];
+    parents[0] = -1;
+    costs[0] = 0.0;
+    if (sc->kind == 2) get_env_bvh(sc);
+    double* elen = (double*)malloc((size_t)pp->max_nodes * sizeof(double));
+    elen[0] = 0.0;
+    double* nw = (double*)malloc((size_t)W * D * sizeof(double));
+    int32_t* par = (int32_t*)malloc((size_t)W * sizeof(int32_t));
+    uint8_t* ok = (uint8_t*)malloc((size_t)W);
+    int32_t* acc = (int32_t*)malloc((size_t)W * sizeof(int32_t));
+    double* qa = (double*)malloc((size_t)W * D * sizeof(double));
+    int32_t* ki = (int32_t*)malloc((size_t)W * 64 * sizeof(int32_t));
+    double* kd = (double*)malloc((size_t)W * 64 * sizeof(double));
+    int32_t* cpar = (int32_t*)malloc((size_t)W * sizeof(int32_t));
+    double* ccost = (double*)malloc((size_t)W * sizeof(double));
+    double* celen = (double*)malloc((size_t)W * sizeof(double));
+    uint8_t* rok = (uint8_t*)malloc((size_t)W * 64);
+    double* bestc = (double*)malloc((size_t)pp->max_nodes * sizeof(double));
+    int32_t* besta = (int32_t*)malloc((size_t)pp->max_nodes * sizeof(int32_t));
+    for (int w = 0; w < max_waves; ++w) {
+        if (n >= pp->max_nodes) break;
+        int goal_index = -1;
+        if (goal && ng == 0 && pp->goal_bias > 0)
+            for (int i = 0; i < W; ++i)
+                if (orc_uniform(pp->seed, (uint32_t)i, (uint32_t)w, 16) < pp->goal_bias) { goal_index = i; break; }
+        plan_wave(sc, sp, pp, lo, hi, goal, goal_index, w, range, inv, states, n, nw, par, ok, nthreads);
+        int A = 0;
+        for (int i = 0; i < W && n + A < pp->max_nodes; ++i)
+            if (ok[i]) acc[A++] = i;
+        if (A == 0) continue;
+        const int64_t n0 = n;
+        int k = (int)ceil(rewire_factor * 2.718281828459045 * (1.0 + 1.0 / D) * log((double)n0 + 1.0));
+        if (k > 64) k = 64;
+        if (k > n0) k = (int)n0;
+        if (k < 1) k = 1;
+        for (int a = 0; a < A; ++a)
+            for (int d = 0; d < D; ++d) qa[(size_t)a * D + d] = nw[(size_t)acc[a] * D + d];
+        orc_knn_brute(sp, states, n0, qa, A, k, ki, kd, nthreads);
+        /* 3. choose parent */
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads_or_default(nthreads))
+        for (int a = 0; a < A; ++a) {
+            const double* q = qa + (size_t)a * D;
+            const int32_t near = par[acc[a]];
+            const double dn = orc_distance(sp, states + (int64_t)near * D, q);
+            const double cn = costs[near] + dn;
+            int32_t bp = near;
+            double bc = cn, bd = dn;
+            for (int j = 0; j < k; ++j) {
+                const int32_t nb = ki[a * k + j];
+                if (nb < 0 || nb == near) continue;
+                const double dj = kd[a * k + j], cj = costs[nb] + dj;
+                if (!star_key_less(cj, dj, nb, cn, dn, near)) continue;
+                if (!star_key_less(cj, dj, nb, bc, bd, bp)) continue;
+                if (dmv_edge(sc, sp, states + (int64_t)nb * D, q, inv, pp->resolution, NULL)) {
+                    bp = nb; bc = cj; bd = dj;
+                }
+            }
+            cpar[a] = bp; ccost[a] = bc; celen[a] = bd;
+        }
+        /* 4. insert */
+        for (int a = 0; a < A; ++a) {
+            for (int d = 0; d < D; ++d) states[(n0 + a) * D + d] = qa[(size_t)a * D + d];
+            parents[n0 + a] = cpar[a];
+            elen[n0 + a] = celen[a];
+            if (goal && orc_distance(sp, qa + (size_t)a * D, goal) <= pp->goal_radius) goals[ng++] = (int32_t)(n0 + a);
+        }
+        n = n0 + A;
+        /* 5. rewire proposals (old costs), then the best proposal per neighbour */
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads_or_default(nthreads))
+        for (int a = 0; a < A; ++a) {
+            const double* q = qa + (size_t)a * D;
+            for (int j = 0; j < k; ++j) {
+                const int32_t nb = ki[a * k + j];
+                rok[a * k + j] = 0;
+                if (nb < 0) continue;
+                const double dj = kd[a * k + j], cj = costs[nb] + dj;
+                if (!star_key_less(ccost[a], celen[a], cpar[a], cj, dj, nb)) continue;  /* reached by step 3 */
+                const double nc = ccost[a] + dj;
+                if (!(nc < costs[nb])) continue;
+                rok[a * k + j] = (uint8_t)dmv_edge(sc, sp, q, states + (int64_t)nb * D, inv, pp->resolution, NULL);
+            }
+        }
+        for (int a = 0; a < A; ++a)
+            for (int j = 0; j < k; ++j)
+                if (rok[a * k + j]) { bestc[ki[a * k + j]] = INFINITY; besta[ki[a * k + j]] = -1; }
+        for (int a = 0; a < A; ++a)
+            for (int j = 0; j < k; ++j) {
+                if (!rok[a * k + j]) continue;
+                const int32_t nb = ki[a * k + j];
+                const double nc = ccost[a] + kd[a * k + j];
+                if (besta[nb] < 0 || nc < bestc[nb] || (nc == bestc[nb] && a < besta[nb])) { bestc[nb] = nc; besta[nb] = a; }
+            }
+        for (int a = 0; a < A; ++a)
+            for (int j = 0; j < k; ++j) {
+                const int32_t nb = ki[a * k + j];
+                if (!rok[a * k + j] || besta[nb] != a) continue;
+                parents[nb] = (int32_t)(n0 + a);
+                elen[nb] = kd[a * k + j];
+                besta[nb] = -2;  /* applied */
+                ++nrw;
+            }
+        /* 6. costs */
+        star_costs(parents, elen, n, costs);
+    }
+    free(elen); free(nw); free(par); free(ok); free(acc); free(qa); free(ki); free(kd);
+    free(cpar); free(ccost); free(celen); free(rok); free(bestc); free(besta);
+    *ngoals = ng;
+    *rewires = nrw;
     return n;
 }

@@ -70,6 +70,14 @@ int64_t orc_plan(const orc_scene* sc, const orc_space* sp, const orc_plan_params
                  const double* hi, const double* start, const double* goal, int max_waves, int stop_when_solved,
                  double* states, int32_t* parents, int32_t* goals, int64_t* ngoals, int nthreads);
 
+/* Replay of the wavefront PRRT* (rewiring) planner: as orc_plan, then per
+ * wavefront k-nearest choose-parent, rewiring and pointer-jumping costs
+ * (see orc_plan_star in oracle.c).  costs receives each node's cost. */
+int64_t orc_plan_star(const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp, const double* lo,
+                      const double* hi, const double* start, const double* goal, int max_waves,
+                      double rewire_factor, double* states, int32_t* parents, double* costs, int32_t* goals,
+                      int64_t* ngoals, int64_t* rewires, int nthreads);
+
 /* Triangle-triangle intersection (FP64 orientation predicates). */
 int orc_tri_tri(const double* t1, const double* t2);
 
