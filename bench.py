@@ -260,6 +260,45 @@ def learned_vs_plain(ctx, m, torch, seeds=5, cap_s=20.0, n_train=1 << 22, epochs
     return res
 
 
+def prrt_star_section(ctx, wave_for=None, refine_s=1.0, seeds=3):
+    """PRRT* (k-nearest rewiring) against PRRT on the same seeds: time to the
+    first solution, and the best path cost after refining for refine_s more."""
+    from mpt_gb300 import planner as P
+    from mpt_gb300 import scenes
+    out = {}
+    for name, mk, kind in [("grid_1024", scenes.grid_scene, "grid"), ("arm_10link", scenes.arm_scene, "arm"),
+                           ("se3_mesh", scenes.mesh_scene, "mesh")]:
+        sc = mk()
+        W = (wave_for or {}).get(kind, 1024)
+        res = {"wavefront": W}
+        for label, algo in (("prrt", P.PRRT), ("prrt_star", P.PRRTStar)):
+            first_t, first_c, final_c, rewires = [], [], [], []
+            for s in range(seeds):
+                pl = P.Planner(P.Scenario(sc), algo(P.gpu_wavefront(W)), seed=2000 + s, ctx=ctx, max_nodes=1 << 21)
+                pl.add_start(sc["start"])
+                t0 = time.perf_counter()
+                pl.solve_for(20.0, lambda: pl.solved())
+                if not pl.solved():
+                    pl.close()
+                    continue
+                first_t.append(time.perf_counter() - t0)
+                first_c.append(pl.solution_cost())
+                pl.solve_for(refine_s)
+                final_c.append(pl.solution_cost())
+                if algo is P.PRRTStar:
+                    rewires.append(pl.rewire_stats()["rewires"])
+                pl.close()
+            res[label] = {"solved": len(first_t), "seeds": seeds,
+                          "p50_first_solution_s": statistics.median(first_t) if first_t else None,
+                          "median_first_cost": statistics.median(first_c) if first_c else None,
+                          "median_cost_after_refine": statistics.median(final_c) if final_c else None,
+                          "refine_s": refine_s}
+            if rewires:
+                res[label]["median_rewires"] = statistics.median(rewires)
+        out[name] = res
+    return out
+
+
 def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0, wave_for=None):
     """Config of the serving benchmark: n queries uniform over the three scenes,
     start and goal rejection-sampled valid, node budgets log-uniform in
@@ -374,10 +413,12 @@ def run_gpu(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     ctx = m.Context(local)
-    if args.edges_only or args.solve_only:
+    if args.edges_only or args.solve_only or args.star_only:
         # profiling modes: one secondary section alone
         if args.edges_only:
             out = {"edge_checks": edge_rates(ctx, m, torch.cuda.current_stream(), torch)}
+        elif args.star_only:
+            out = {"prrt_star": prrt_star_section(ctx)}
         else:
             out = {"time_to_solve": solve_times(ctx, seeds=args.solve_seeds)}
         out["gpu_launches"] = ctx.kernel_launches()
@@ -485,6 +526,7 @@ def run_gpu(args):
         wave_for = {"grid": solves["grid_1024"]["autotune"]["best"], "arm": solves["arm_10link"]["autotune"]["best"],
                     "mesh": solves["se3_mesh"]["autotune"]["best"]}
     serving = batch_serving(m, ctx, wave_for=wave_for) if not (args.no_solve or args.no_batch) else None
+    star = prrt_star_section(ctx, wave_for) if not (args.no_solve or args.no_star) else None
 
     # CPU baselines: oracle kd-tree and DMV on the host cores, bounded samples
     cpu = None
@@ -536,6 +578,7 @@ def run_gpu(args):
                 "time_to_solve": {"unit": "s", "planner": "plain wavefront PRRT (GPU)", "per_scene": solves},
                 "learned_surrogate_se3": learned,
                 "batch_serving": serving,
+                "prrt_star": star,
                 "clocks": clk.summary(), "gpu_launches": launches, "tree_build_s": build_s,
                 "wall_s_timed": wall}
         print(json.dumps(line))
@@ -554,6 +597,8 @@ def main():
     ap.add_argument("--no-solve", action="store_true", help="skip the time-to-solve, surrogate and serving runs")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-surrogate comparison")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched serving run")
+    ap.add_argument("--no-star", action="store_true", help="skip the PRRT* comparison")
+    ap.add_argument("--star-only", action="store_true", help="the PRRT* comparison only (profiling)")
     ap.add_argument("--edges-only", action="store_true", help="edge checks/s of the three scenes only (profiling)")
     ap.add_argument("--solve-only", action="store_true", help="time to solve of the three scenes only (profiling)")
     ap.add_argument("--solve-seeds", type=int, default=5)

@@ -143,11 +143,13 @@ class Planner<Scenario, PRRT<Options...>> {
 public:
     using State = typename Scenario::State;
 
-private:
+protected:
     Scenario scenario_;
     uint64_t seed_;
     double range_ = -1.0;
     double goalBias_ = 0.01;
+    bool rewire_ = false;       // PRRTStar
+    double rewireFactor_ = 1.1;
     size_t maxNodes_;
     mptg_ctx* ctx_ = nullptr;
     mptg_scene* scene_ = nullptr;
@@ -179,6 +181,7 @@ private:
         }
         impl::check(ctx_, mptg_planner_create(ctx_, scene_, &p, lo, hi, &planner_));
         impl::check(ctx_, mptg_planner_set_goal(planner_, impl::data(goal.state), goal.radius));
+        if (rewire_) impl::check(ctx_, mptg_planner_set_rewire(planner_, 1, rewireFactor_));
         for (const State& q : starts_) impl::check(ctx_, mptg_planner_add_start(planner_, impl::data(q)));
         starts_.clear();
     }
@@ -323,8 +326,36 @@ public:
             impl::check(ctx_, mptg_planner_stats(planner_, st));
             std::printf("wavefronts: %.0f\nsamples: %.0f\nnodes added: %.0f\nlink states checked: %.0f\n", st[0],
                         st[1], st[2], st[5]);
+            if (rewire_) {
+                double rw[2];
+                impl::check(ctx_, mptg_planner_rewire_stats(planner_, rw));
+                std::printf("rewire count: %.0f of %.0f\n", rw[0], rw[1]);
+            }
         }
     }
+};
+
+// Planner<Scenario, PRRTStar<Options...>> (src/mpt/prrt_star.hpp:56-95): the
+// same wavefront planner with k-nearest rewiring (rewire_k_nearest)
+template <class... Options> struct PRRTStar : PRRT<Options...> {};
+
+template <class Scenario, class... Options>
+class Planner<Scenario, PRRTStar<Options...>> : public Planner<Scenario, PRRT<Options...>> {
+    using Base = Planner<Scenario, PRRT<Options...>>;
+
+public:
+    explicit Planner(const Scenario& scenario = Scenario(), uint64_t seed = std::random_device{}(),
+                     size_t maxNodes = size_t(1) << 21, int device = 0)
+        : Base(scenario, seed, maxNodes, device) {
+        this->rewire_ = true;
+    }
+    // PRRTStar::setRewireFactor (src/mpt/impl/prrt_star/prrt_star.hpp:234-240)
+    void setRewireFactor(double f) {
+        if (!(f > 0)) throw std::invalid_argument("rewire factor must be positive");
+        if (this->planner_) throw std::logic_error("setRewireFactor must precede the first solve");
+        this->rewireFactor_ = f;
+    }
+    double getRewireFactor() const { return this->rewireFactor_; }
 };
 
 }  // namespace unc::robotics::mpt_gb300

@@ -79,6 +79,27 @@ int main() {
     planner.visitGraph(cnt);
     CHECK(cnt.v == planner.size());
     CHECK(cnt.e == planner.size() - 1);
-    std::printf("C++ Planner OK: %zu waypoints, %zu nodes\n", path.size(), planner.size());
+
+    // Planner<Scenario, PRRTStar<...>>: the same contract, rewiring on
+    Planner<WallScenario, PRRTStar<gpu_wavefront<1024>, report_stats<true>>> star(sc, 42);
+    star.setRange(32.0);
+    star.setGoalBias(0.05);
+    star.setRewireFactor(1.2);
+    CHECK(star.getRewireFactor() == 1.2);
+    star.addStart(WallScenario::startState());
+    star.solveFor([&] { return star.solved(); }, std::chrono::seconds(10));
+    CHECK(star.solved());
+    auto spath = star.solution();
+    CHECK(spath.size() > 2 && spath.front() == WallScenario::startState() && spath.back() == sc.goal().state);
+    bool threw2 = false;
+    try {
+        star.setRewireFactor(1.5);
+    } catch (const std::logic_error&) {
+        threw2 = true;
+    }
+    CHECK(threw2);
+    star.printStats();
+    std::printf("C++ Planner OK: %zu waypoints, %zu nodes; PRRTStar %zu waypoints\n", path.size(), planner.size(),
+                spath.size());
     return 0;
 }
