@@ -281,8 +281,9 @@ mptg_status mptg_planner_set_rewire(mptg_planner* planner, int enabled, double r
  * queries n only. */
 mptg_status mptg_planner_costs(mptg_planner* planner, double* out, size_t cap, size_t* n);
 /* PRRT*'s Stats (prrt_star.hpp:121-152): [0] rewires applied, [1] links checked
- * for choose-parent and rewiring */
-mptg_status mptg_planner_rewire_stats(mptg_planner* planner, double out[2]);
+ * for choose-parent and rewiring; seconds on the GPU timeline in [2] k-NN,
+ * [3] choose parent, [4] rewire, [5] cost recomputation */
+mptg_status mptg_planner_rewire_stats(mptg_planner* planner, double out[6]);
 /* WorkerStats' timers (prrt.hpp:72-101) on the GPU timeline, seconds summed
  * over wavefronts: [0] sample + nearest + steer, [1] surrogate scoring,
  * [2] valid motion (state + DMV link checks), [3] compaction + insert. */

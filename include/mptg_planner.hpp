@@ -327,7 +327,7 @@ public:
             std::printf("wavefronts: %.0f\nsamples: %.0f\nnodes added: %.0f\nlink states checked: %.0f\n", st[0],
                         st[1], st[2], st[5]);
             if (rewire_) {
-                double rw[2];
+                double rw[6];
                 impl::check(ctx_, mptg_planner_rewire_stats(planner_, rw));
                 std::printf("rewire count: %.0f of %.0f\n", rw[0], rw[1]);
             }

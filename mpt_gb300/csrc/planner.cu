@@ -119,8 +119,13 @@ struct mptg_planner {
     double* ccost = nullptr;
     double* celen = nullptr;
     int* s_cnt = nullptr;               // [2]
+    int* rank = nullptr;                // [cap_wave][64] choose-parent rank (-1: no candidate)
+    uint8_t* decided = nullptr;         // [cap_wave]
     unsigned long long* nrw = nullptr;  // rewires applied
     uint64_t stat_rewire_tests = 0;
+    cudaEvent_t sev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    double t_star[4] = {0, 0, 0, 0};    // k-NN, choose parent, rewire, costs (seconds)
+    bool star_timed = false;            // sev recorded in the current wavefront
 };
 
 extern "C" mptg_status mptg_surrogate_score_dev(mptg_surrogate* s, const double* dstates, int n, float* dlogits,
@@ -380,24 +385,52 @@ __device__ __forceinline__ void copy_state(double* __restrict__ dst, const doubl
 }
 
 // choose-parent candidates: neighbour j of new state a whose key is below
-// near's; their links neighbour -> new are gathered (in any order) for one
-// batched DMV call
-__global__ void k_star_pc(PlanView p, int A, int k, const int* __restrict__ ki, const double* __restrict__ kd,
-                          const int* __restrict__ near, const double* __restrict__ dnear,
-                          const double* __restrict__ cost, const double* __restrict__ states64,
-                          const double* __restrict__ acc, int* __restrict__ cnt, int* __restrict__ pair_of,
-                          double* __restrict__ ea, double* __restrict__ eb) {
+// near's, ranked by key among the state's candidates (rank -1: not one)
+__global__ void k_star_rank(int A, int k, const int* __restrict__ ki, const double* __restrict__ kd,
+                            const int* __restrict__ near, const double* __restrict__ dnear,
+                            const double* __restrict__ cost, int* __restrict__ rank) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= A * k) return;
     const int a = t / k, nb = ki[t], nr = near[a];
+    rank[t] = -1;
     if (nb < 0 || nb == nr) return;
     const double dj = kd[t], cj = __dadd_rn(cost[nb], dj);
     const double dn = dnear[a], cn = __dadd_rn(cost[nr], dn);
     if (!star_less(cj, dj, nb, cn, dn, nr)) return;
+    int r = 0;
+    for (int j = 0; j < k; ++j) {
+        const int o = ki[a * k + j];
+        if (o < 0 || o == nr || o == nb) continue;
+        const double dd = kd[a * k + j], cc = __dadd_rn(cost[o], dd);
+        if (star_less(cc, dd, o, cn, dn, nr) && star_less(cc, dd, o, cj, dj, nb)) ++r;
+    }
+    rank[t] = r;
+}
+
+// one round of choose-parent checks: the candidates of rank [lo, hi) of the
+// states that have no valid candidate yet; their links neighbour -> new are
+// gathered (in any order) for one batched DMV call.  A state stops at the
+// first round with a valid candidate: every lower-ranked candidate was
+// checked and failed, so the smallest valid key is the reference's choice.
+__global__ void k_star_pc(PlanView p, int A, int k, int lo, int hi, const int* __restrict__ ki,
+                          const int* __restrict__ rank, const uint8_t* __restrict__ decided,
+                          const double* __restrict__ states64, const double* __restrict__ acc, int* __restrict__ cnt,
+                          int* __restrict__ pair_of, double* __restrict__ ea, double* __restrict__ eb) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A * k) return;
+    const int a = t / k, r = rank[t];
+    if (r < lo || r >= hi || decided[a]) return;
     const int slot = atomicAdd(cnt, 1);  // < A * k
     pair_of[slot] = t;
-    copy_state(ea + (size_t)slot * p.D, states64 + (size_t)nb * p.D, p.D);
+    copy_state(ea + (size_t)slot * p.D, states64 + (size_t)ki[t] * p.D, p.D);
     copy_state(eb + (size_t)slot * p.D, acc + (size_t)a * p.D, p.D);
+}
+
+// states with a valid candidate among this round's are decided
+__global__ void k_star_decide(int m, int k, const int* __restrict__ pair_of, const uint8_t* __restrict__ ok,
+                              uint8_t* __restrict__ decided) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < m && ok[s]) decided[pair_of[s] / k] = 1;
 }
 
 __global__ void k_star_scatter(int m, const int* __restrict__ pair_of, const uint8_t* __restrict__ ok,
@@ -534,7 +567,7 @@ static void planner_free(mptg_planner* p) {
                     p->near_c, p->new_c, p->cmap, p->ok_c, p->keep, p->path_ids, p->path_out, p->sg_pts,
                     p->cost, p->elen, p->pj_s, p->pj_a, p->pj_a2, p->bbits, p->bid, p->knn_i, p->knn_d, p->pv,
                     p->s_pair, p->s_rcost, p->s_ok, p->s_ea, p->s_eb, p->dnear, p->cpar, p->ccost, p->celen,
-                    p->s_cnt, p->nrw};
+                    p->s_cnt, p->nrw, p->rank, p->decided};
     if (p->stream) cudaStreamSynchronize(p->stream);
     for (void* x : ptrs)
         if (x) cudaFree(x);
@@ -542,6 +575,8 @@ static void planner_free(mptg_planner* p) {
     if (p->hgoal) cudaFreeHost(p->hgoal);
     scratch_free(&p->scratch);
     for (cudaEvent_t e : p->ev)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : p->sev)
         if (e) cudaEventDestroy(e);
     if (p->tree) mptg_tree_destroy(p->tree);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -602,6 +637,7 @@ static mptg_status planner_reset(mptg_planner* p, const mptg_plan_params* prm, b
     p->stat_seconds = 0;
     for (double& t : p->t_phase) t = 0;
     p->stat_rewire_tests = 0;
+    for (double& t : p->t_star) t = 0;
     if (p->nrw) MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->nrw, 0, sizeof(unsigned long long), p->stream));
     return MPTG_OK;
 }
@@ -618,27 +654,41 @@ static mptg_status star_wave(mptg_planner* p, cudaStream_t s, int A, size_t n0) 
     k = std::max(1, std::min(k, std::min(64, (int)n0)));
     const int pairs = A * k;
     mptg_status st;
+    MPTG_CUDA_TRY(ctx, cudaEventRecord(p->sev[0], s));
     k_star_near<<<mptg_blocks(A, 128), 128, 0, s>>>(v, A, p->acc_states, p->acc_parent, st64, p->dnear);
     MPTG_LAUNCHED(ctx);
     if ((st = mptg_tree_nearest_k_dev(p->tree, p->acc_states, A, k, p->knn_i, p->knn_d, s))) return st;
-    // choose parent
-    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->s_cnt, 0, 2 * sizeof(int), s));
+    MPTG_CUDA_TRY(ctx, cudaEventRecord(p->sev[1], s));
+    // choose parent: candidates in key order, in rounds of rank [0,1), [1,5), [5,k)
     MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->pv, 0, pairs, s));
-    k_star_pc<<<mptg_blocks(pairs, 128), 128, 0, s>>>(v, A, k, p->knn_i, p->knn_d, p->acc_parent, p->dnear, p->cost,
-                                                     st64, p->acc_states, p->s_cnt, p->s_pair, p->s_ea, p->s_eb);
+    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->decided, 0, A, s));
+    k_star_rank<<<mptg_blocks(pairs, 128), 128, 0, s>>>(A, k, p->knn_i, p->knn_d, p->acc_parent, p->dnear, p->cost,
+                                                       p->rank);
     MPTG_LAUNCHED(ctx);
-    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->hbuf + 2, p->s_cnt, sizeof(int), cudaMemcpyDeviceToHost, s));
-    MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
-    const int npc = p->hbuf[2];
-    if (npc > 0) {
-        if ((st = scene_edges_dev(p->scene, p->s_ea, p->s_eb, npc, p->prm.edge_step, p->prm.resolution, p->s_ok, s,
+    int npc = 0;
+    const int bounds[4] = {0, 1, 5, 64};
+    for (int r = 0; r < 3; ++r) {
+        MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->s_cnt, 0, sizeof(int), s));
+        k_star_pc<<<mptg_blocks(pairs, 128), 128, 0, s>>>(v, A, k, bounds[r], bounds[r + 1], p->knn_i, p->rank,
+                                                         p->decided, st64, p->acc_states, p->s_cnt, p->s_pair,
+                                                         p->s_ea, p->s_eb);
+        MPTG_LAUNCHED(ctx);
+        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->hbuf + 2, p->s_cnt, sizeof(int), cudaMemcpyDeviceToHost, s));
+        MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        const int m = p->hbuf[2];
+        if (m == 0) continue;
+        npc += m;
+        if ((st = scene_edges_dev(p->scene, p->s_ea, p->s_eb, m, p->prm.edge_step, p->prm.resolution, p->s_ok, s,
                                   p->nsamp, &p->scratch)))
             return st;
-        k_star_scatter<<<mptg_blocks(npc, 256), 256, 0, s>>>(npc, p->s_pair, p->s_ok, p->pv);
-        MPTG_LAUNCHED(ctx);
+        k_star_scatter<<<mptg_blocks(m, 256), 256, 0, s>>>(m, p->s_pair, p->s_ok, p->pv);
+        k_star_decide<<<mptg_blocks(m, 256), 256, 0, s>>>(m, k, p->s_pair, p->s_ok, p->decided);
+        ctx->launches += 2;
     }
+    MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->s_cnt + 1, 0, sizeof(int), s));
     k_star_choose<<<mptg_blocks(A, 128), 128, 0, s>>>(A, k, p->knn_i, p->knn_d, p->acc_parent, p->dnear, p->cost,
                                                       p->pv, p->cpar, p->ccost, p->celen);
+    MPTG_CUDA_TRY(ctx, cudaEventRecord(p->sev[2], s));
     // rewire
     k_star_rw<<<mptg_blocks(pairs, 128), 128, 0, s>>>(v, A, k, p->knn_i, p->knn_d, p->cost, p->cpar, p->ccost,
                                                      p->celen, st64, p->acc_states, p->s_cnt + 1, p->s_pair,
@@ -660,6 +710,8 @@ static mptg_status star_wave(mptg_planner* p, cudaStream_t s, int A, size_t n0) 
         k_star_rw_reset<<<g, 256, 0, s>>>(nrc, p->s_pair, p->knn_i, p->bbits, p->bid);
         ctx->launches += 4;
     }
+    MPTG_CUDA_TRY(ctx, cudaEventRecord(p->sev[3], s));
+    p->star_timed = true;
     return MPTG_OK;
 }
 
@@ -667,6 +719,7 @@ static mptg_status star_wave(mptg_planner* p, cudaStream_t s, int A, size_t n0) 
 // ceil(log2(n + 1)) rounds (the depth is below n)
 static mptg_status star_costs(mptg_planner* p, cudaStream_t s, size_t n) {
     mptg_ctx* ctx = p->ctx;
+    MPTG_CUDA_TRY(ctx, cudaEventRecord(p->sev[4], s));
     MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->pj_s, p->elen, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
     MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->pj_a, p->parent, n * sizeof(int), cudaMemcpyDeviceToDevice, s));
     int rounds = 0;
@@ -682,6 +735,7 @@ static mptg_status star_costs(mptg_planner* p, cudaStream_t s, size_t n) {
     }
     ctx->launches += rounds;
     if (sa != p->cost) MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->cost, sa, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    MPTG_CUDA_TRY(ctx, cudaEventRecord(p->sev[5], s));
     return MPTG_OK;
 }
 
@@ -793,6 +847,15 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
         float ms = 0.f;
         MPTG_CUDA_TRY(ctx, cudaEventElapsedTime(&ms, p->ev[k], p->ev[k + 1]));
         p->t_phase[k] += 1e-3 * ms;
+    }
+    if (p->star_timed) {
+        const int pairs[4][2] = {{0, 1}, {1, 2}, {2, 3}, {4, 5}};
+        for (int k = 0; k < 4; ++k) {
+            float ms = 0.f;
+            MPTG_CUDA_TRY(ctx, cudaEventElapsedTime(&ms, p->sev[pairs[k][0]], p->sev[pairs[k][1]]));
+            p->t_star[k] += 1e-3 * ms;
+        }
+        p->star_timed = false;
     }
     *added = nacc;
     return MPTG_OK;
@@ -1098,6 +1161,8 @@ mptg_status mptg_planner_set_rewire(mptg_planner* p, int enabled, double rewire_
         ALLOC(p->celen, W * sizeof(double));
         ALLOC(p->s_cnt, 2 * sizeof(int));
         ALLOC(p->nrw, sizeof(unsigned long long));
+        ALLOC(p->rank, P * sizeof(int));
+        ALLOC(p->decided, W);
 #undef ALLOC
         if (e != cudaSuccess) {
             cudaGetLastError();
@@ -1105,6 +1170,7 @@ mptg_status mptg_planner_set_rewire(mptg_planner* p, int enabled, double rewire_
         }
         MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->bbits, 0xff, N * sizeof(unsigned long long), p->stream));
         MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->bid, 0x7f, N * sizeof(int), p->stream));
+        for (cudaEvent_t& ev : p->sev) MPTG_CUDA_TRY(ctx, cudaEventCreate(&ev));
     }
     // every node so far is a start: no parent, cost 0
     MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->cost, 0, p->cap_nodes * sizeof(double), p->stream));
@@ -1129,7 +1195,7 @@ mptg_status mptg_planner_costs(mptg_planner* p, double* out, size_t cap, size_t*
     return MPTG_OK;
 }
 
-mptg_status mptg_planner_rewire_stats(mptg_planner* p, double out[2]) {
+mptg_status mptg_planner_rewire_stats(mptg_planner* p, double out[6]) {
     if (!p || !out) return MPTG_ERR_INVALID_ARG;
     unsigned long long n = 0;
     if (p->nrw) {
@@ -1138,6 +1204,7 @@ mptg_status mptg_planner_rewire_stats(mptg_planner* p, double out[2]) {
     }
     out[0] = (double)n;
     out[1] = (double)p->stat_rewire_tests;
+    for (int k = 0; k < 4; ++k) out[2 + k] = p->t_star[k];
     return MPTG_OK;
 }
 

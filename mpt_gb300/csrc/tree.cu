@@ -979,6 +979,115 @@ __global__ void __launch_bounds__(256) k_nearest_tiled_merge(TreeView t, const d
 
 // ------------------------------------------------------------------ k-NN
 
+// One batch of up to 32 candidate points (lane: have, pid, d32) against the
+// warp's sorted k-NN list: every point whose FP32 distance is within E of the
+// bound tau gets its FP64 distance, and those within tau join the list in
+// (distance, id) order, one at a time (the list lives two entries per lane).
+__device__ __forceinline__ void knn_consider(const TreeView& t, const double* __restrict__ qd, int lane, int k,
+                                             double radius, bool have, int pid, float d32, float E, double& ld0,
+                                             double& ld1, int& li0, int& li1, int& cnt, double& tau, float& tauf) {
+    bool cand = have && __fsub_rd(d32, E) <= tauf;
+    double dd = INFINITY;
+    if (cand) {
+        dd = dist64(t.metric, t.D, t.w0, t.w1, qd, t.states64 + (size_t)pid * t.D);
+        cand = dd <= tau;
+    }
+    unsigned cmask = __ballot_sync(0xffffffffu, cand);
+    while (cmask) {
+        int src = __ffs(cmask) - 1;
+        cmask &= cmask - 1;
+        double cd = __shfl_sync(0xffffffffu, dd, src);
+        int ci = __shfl_sync(0xffffffffu, pid, src);
+        // insert (cd, ci) into the sorted list if it ranks among the k best
+        if (cnt == k) {
+            double kd = (k - 1) < 32 ? __shfl_sync(0xffffffffu, ld0, k - 1) : __shfl_sync(0xffffffffu, ld1, k - 33);
+            int ki = (k - 1) < 32 ? __shfl_sync(0xffffffffu, li0, k - 1) : __shfl_sync(0xffffffffu, li1, k - 33);
+            if (!(cd < kd || (cd == kd && ci < ki))) continue;
+        }
+        // rank position = number of entries strictly ahead of (cd, ci)
+        bool ahead0 = lane < cnt && (ld0 < cd || (ld0 == cd && li0 < ci));
+        bool ahead1 = lane + 32 < cnt && (ld1 < cd || (ld1 == cd && li1 < ci));
+        int pos = __popc(__ballot_sync(0xffffffffu, ahead0)) + __popc(__ballot_sync(0xffffffffu, ahead1));
+        // shift entries at >= pos one place back
+        double p0d = __shfl_up_sync(0xffffffffu, ld0, 1);
+        int p0i = __shfl_up_sync(0xffffffffu, li0, 1);
+        double p1d = __shfl_up_sync(0xffffffffu, ld1, 1);
+        int p1i = __shfl_up_sync(0xffffffffu, li1, 1);
+        double last0d = __shfl_sync(0xffffffffu, ld0, 31);
+        int last0i = __shfl_sync(0xffffffffu, li0, 31);
+        if (lane == 0) { p1d = last0d; p1i = last0i; }
+        // slot 0 entries (index = lane)
+        if (lane > pos) { ld0 = p0d; li0 = p0i; }
+        else if (lane == pos) { ld0 = cd; li0 = ci; }
+        int j1 = lane + 32;
+        if (j1 > pos) { ld1 = p1d; li1 = p1i; }
+        else if (j1 == pos) { ld1 = cd; li1 = ci; }
+        if (cnt < k) ++cnt;
+        if (cnt == k) {
+            double kd = (k - 1) < 32 ? __shfl_sync(0xffffffffu, ld0, k - 1) : __shfl_sync(0xffffffffu, ld1, k - 33);
+            tau = fmin(kd, radius);
+            tauf = __double2float_ru(tau);
+        }
+    }
+}
+
+// Exhaustive k nearest for high-dimensional trees (the strategy rule of the
+// 1-NN sweep): a block of 8 warps (8 queries) stages the FP32 points through
+// shared memory, 256 at a time, and each warp runs every 32-point slice
+// through knn_consider, the list logic of the tree walk.  The list is the
+// exact (distance, id)-ordered top k whatever order the points arrive in, so
+// the answers equal k_nearest_k's.
+template <int MK, int DMAX>
+__global__ void __launch_bounds__(256) k_nearest_k_tiled(TreeView t, const double* __restrict__ q64, int nq, int k,
+                                                         double radius, int* __restrict__ out_idx,
+                                                         double* __restrict__ out_d) {
+    __shared__ float tile[DMAX][256];
+    const int lane = threadIdx.x & 31;
+    const int qi = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const bool active = qi < nq;  // warp-uniform
+    const int D = t.D;
+    const double* qd = q64 + (size_t)(active ? qi : 0) * D;
+    float q[DMAX];
+    float myq, M;
+    load_query<MK, DMAX>(qd, D, lane, q, myq, M, t);
+    const float E = err32<MK>(D, M, t.w0f, t.w1f);
+    double ld0 = INFINITY, ld1 = INFINITY;
+    int li0 = INT_MAX, li1 = INT_MAX;
+    int cnt = 0;
+    double tau = radius;
+    float tauf = __double2float_ru(tau);
+    const int n = t.n;
+    for (int base = 0; base < n; base += 256) {
+        __syncthreads();
+        const int j = base + threadIdx.x;
+#pragma unroll
+        for (int d = 0; d < DMAX; ++d) tile[d][threadIdx.x] = (j < n && d < D) ? t.pts32[(size_t)j * D + d] : 0.f;
+        __syncthreads();
+        if (!active) continue;
+        const int cntp = min(256, n - base);
+        for (int sub = 0; sub < cntp; sub += 32) {
+            const int off = sub + lane;
+            const bool have = off < cntp;
+            float d32 = INFINITY;
+            int pid = -1;
+            if (have) {
+                float p[DMAX];
+#pragma unroll
+                for (int d = 0; d < DMAX; ++d) p[d] = tile[d][off];
+                d32 = dist32<MK, DMAX>(q, p, t.w0f, t.w1f);
+                if (!(d32 == d32)) d32 = INFINITY;
+                pid = base + off;
+            }
+            knn_consider(t, qd, lane, k, radius, have, pid, d32, E, ld0, ld1, li0, li1, cnt, tau, tauf);
+        }
+    }
+    if (!active) return;
+    int* oi = out_idx + (size_t)qi * k;
+    double* od = out_d + (size_t)qi * k;
+    if (lane < k) { bool v = lane < cnt; oi[lane] = v ? li0 : -1; od[lane] = v ? ld0 : INFINITY; }
+    if (lane + 32 < k) { bool v = lane + 32 < cnt; oi[lane + 32] = v ? li1 : -1; od[lane + 32] = v ? ld1 : INFINITY; }
+}
+
 // Exact k nearest (k <= 64) sorted by (distance, id), warp per query.  The
 // running list lives in registers: entry j in lane j (j < 32) / lane j-32 of
 // the second slot.  tau = the k-th best exact distance (or the radius).
@@ -1035,49 +1144,7 @@ __global__ void __launch_bounds__(256) k_nearest_k(TreeView t, const double* __r
             d32 = dist32<MK, DMAX>(q, p, t.w0f, t.w1f);
             if (!(d32 == d32)) d32 = INFINITY;
         }
-        bool cand = have && __fsub_rd(d32, E) <= tauf;
-        double dd = INFINITY;
-        if (cand) {
-            dd = dist64(t.metric, D, t.w0, t.w1, qd, t.states64 + (size_t)pid * D);
-            cand = dd <= tau;
-        }
-        unsigned cmask = __ballot_sync(0xffffffffu, cand);
-        while (cmask) {
-            int src = __ffs(cmask) - 1;
-            cmask &= cmask - 1;
-            double cd = __shfl_sync(0xffffffffu, dd, src);
-            int ci = __shfl_sync(0xffffffffu, pid, src);
-            // insert (cd, ci) into the sorted list if it ranks among the k best
-            if (cnt == k) {
-                double kd = (k - 1) < 32 ? __shfl_sync(0xffffffffu, ld0, k - 1) : __shfl_sync(0xffffffffu, ld1, k - 33);
-                int ki = (k - 1) < 32 ? __shfl_sync(0xffffffffu, li0, k - 1) : __shfl_sync(0xffffffffu, li1, k - 33);
-                if (!(cd < kd || (cd == kd && ci < ki))) continue;
-            }
-            // rank position = number of entries strictly ahead of (cd, ci)
-            bool ahead0 = lane < cnt && (ld0 < cd || (ld0 == cd && li0 < ci));
-            bool ahead1 = lane + 32 < cnt && (ld1 < cd || (ld1 == cd && li1 < ci));
-            int pos = __popc(__ballot_sync(0xffffffffu, ahead0)) + __popc(__ballot_sync(0xffffffffu, ahead1));
-            // shift entries at >= pos one place back
-            double p0d = __shfl_up_sync(0xffffffffu, ld0, 1);
-            int p0i = __shfl_up_sync(0xffffffffu, li0, 1);
-            double p1d = __shfl_up_sync(0xffffffffu, ld1, 1);
-            int p1i = __shfl_up_sync(0xffffffffu, li1, 1);
-            double last0d = __shfl_sync(0xffffffffu, ld0, 31);
-            int last0i = __shfl_sync(0xffffffffu, li0, 31);
-            if (lane == 0) { p1d = last0d; p1i = last0i; }
-            // slot 0 entries (index = lane)
-            if (lane > pos) { ld0 = p0d; li0 = p0i; }
-            else if (lane == pos) { ld0 = cd; li0 = ci; }
-            int j1 = lane + 32;
-            if (j1 > pos) { ld1 = p1d; li1 = p1i; }
-            else if (j1 == pos) { ld1 = cd; li1 = ci; }
-            if (cnt < k) ++cnt;
-            if (cnt == k) {
-                double kd = (k - 1) < 32 ? __shfl_sync(0xffffffffu, ld0, k - 1) : __shfl_sync(0xffffffffu, ld1, k - 33);
-                tau = fmin(kd, radius);
-                tauf = __double2float_ru(tau);
-            }
-        }
+        knn_consider(t, qd, lane, k, radius, have, pid, d32, E, ld0, ld1, li0, li1, cnt, tau, tauf);
         bool found = false;
         while (sp > 0) {
             --sp;
@@ -1611,8 +1678,13 @@ mptg_status mptg_tree_nearest_k_dev(mptg_tree* t, const double* dq, int nq, int 
     if (k < 1 || k > 64) return mptg_fail(t->ctx, MPTG_ERR_INVALID_ARG, "k=%d outside [1,64]", k);
     TreeView v = view_of(t);
     v.stats = nullptr;
-    unsigned grid = mptg_blocks((size_t)nq * 32, 256);
-    DISPATCH_METRIC(t->metric, t->D, k_nearest_k, grid, 256, s, v, dq, nq, k, (double)INFINITY, didx, dd);
+    if (tree_use_tiled(t, nq)) {
+        DISPATCH_METRIC(t->metric, t->D, k_nearest_k_tiled, mptg_blocks((size_t)nq, 8), 256, s, v, dq, nq, k,
+                        (double)INFINITY, didx, dd);
+    } else {
+        unsigned grid = mptg_blocks((size_t)nq * 32, 256);
+        DISPATCH_METRIC(t->metric, t->D, k_nearest_k, grid, 256, s, v, dq, nq, k, (double)INFINITY, didx, dd);
+    }
     MPTG_LAUNCHED(t->ctx);
     return MPTG_OK;
 }
@@ -1632,9 +1704,14 @@ mptg_status mptg_nearest_k(mptg_tree* t, const double* q, size_t nq, int k, doub
     if ((st = mptg_stage_out_alloc(ctx, idx, nq * k * sizeof(int32_t), s, &bi))) return st;
     if ((st = mptg_stage_out_alloc(ctx, dist, nq * k * sizeof(double), s, &bd))) return st;
     TreeView v = view_of(t);
-    unsigned grid = mptg_blocks(nq * 32, 256);
-    DISPATCH_METRIC(t->metric, t->D, k_nearest_k, grid, 256, s, v, (const double*)bq.dptr, (int)nq, k, r,
-                    (int*)bi.dptr, (double*)bd.dptr);
+    if (tree_use_tiled(t, (int)nq)) {
+        DISPATCH_METRIC(t->metric, t->D, k_nearest_k_tiled, mptg_blocks(nq, 8), 256, s, v, (const double*)bq.dptr,
+                        (int)nq, k, r, (int*)bi.dptr, (double*)bd.dptr);
+    } else {
+        unsigned grid = mptg_blocks(nq * 32, 256);
+        DISPATCH_METRIC(t->metric, t->D, k_nearest_k, grid, 256, s, v, (const double*)bq.dptr, (int)nq, k, r,
+                        (int*)bi.dptr, (double*)bd.dptr);
+    }
     MPTG_LAUNCHED(ctx);
     MPTG_CUDA_TRY(ctx, cudaGetLastError());
     DevBuf outs[2] = {bi, bd};

@@ -333,9 +333,10 @@ class Planner:
         return out
 
     def rewire_stats(self) -> dict:
-        out = (ctypes.c_double * 2)()
+        out = (ctypes.c_double * 6)()
         _check(self.ctx.h, self.lib.mptg_planner_rewire_stats(self.h, out))
-        return {"rewires": int(out[0]), "rewire_tests": int(out[1])}
+        return {"rewires": int(out[0]), "rewire_tests": int(out[1]), "knn_s": out[2], "choose_s": out[3],
+                "rewire_s": out[4], "costs_s": out[5]}
 
     def timers(self) -> dict:
         """Seconds per phase on the GPU timeline (WorkerStats' nearest / validMotion

@@ -153,9 +153,11 @@ def test_nearest_k_matches_oracle(ctx, orc, name, k, radius):
         far = od > radius
         oi[far] = -1
         od[far] = np.inf
-    gi, gd = tree.nearest_k(q, k, radius)
-    assert np.array_equal(gi, oi)
-    assert np.array_equal(gd, od)
+    for strategy in (tree.KDTREE, tree.EXHAUSTIVE, tree.AUTO):
+        tree.set_strategy(strategy)
+        gi, gd = tree.nearest_k(q, k, radius)
+        assert np.array_equal(gi, oi), strategy
+        assert np.array_equal(gd, od)
 
 
 def test_device_buffers_async(ctx, orc):
