@@ -302,6 +302,53 @@ __device__ __forceinline__ float warp_max_f(float v) {
     return v;
 }
 
+// FP32 test of link [a,b] against disc k, every point within dd of its FP64
+// position (per coordinate)
+__device__ __forceinline__ int arm_disc32(const SceneView& s, int k, float ax, float ay, float bx, float by,
+                                          float dd) {
+    const float4 d = __ldg(&s.discs32[k]);  // 1 KB per scene: L1-resident
+    float d2 = dpseg2_32(d.x, d.y, ax, ay, bx, by);
+    // the distance moves by <= dd, so d^2 by <= 2*d*dd + dd^2
+    float m = 3.f * sqrtf(fmaxf(d2, d.z)) * dd + dd * dd + 8.f * U32 * (d2 + d.z);
+    return d2 <= d.z - m ? VF_INVALID : (d2 > d.z + m ? VF_VALID : VF_UNSURE);
+}
+
+// Margin of one FP32 orientation v x w (v, w differences of joint positions,
+// nv, nw their FP32 L1 norms).  Each coordinate of a joint position is within
+// delta/2 of the FP64 one, so each coordinate of v and w is within delta, and
+//   |V x W - v x w| <= delta*(|v|_1 + |w|_1) + 2*delta^2;
+// the FP32 evaluation (two differences, two products, a difference) and the
+// FP64 one round by less than 8u(|v|_1 + 2delta)(|w|_1 + 2delta).  The margin
+// doubles both, which also covers the rounding of the norms and of itself.
+__device__ __forceinline__ float orient_margin32(float nv, float nw, float delta) {
+    return 2.f * delta * (nv + nw) + 4.f * delta * delta + 16.f * U32 * (nv + 2.f * delta) * (nw + 2.f * delta) +
+           1e-30f;
+}
+
+// FP32 test of links [a,b] and [c,d] (segs_intersect64 in FP64)
+__device__ __forceinline__ int arm_self32(float ax, float ay, float bx, float by, float cx, float cy, float dx,
+                                          float dy, float delta) {
+    const float nab = fabsf(bx - ax) + fabsf(by - ay), ncd = fabsf(dx - cx) + fabsf(dy - cy);
+    const float nac = fabsf(cx - ax) + fabsf(cy - ay), nad = fabsf(dx - ax) + fabsf(dy - ay);
+    const float nbc = fabsf(bx - cx) + fabsf(by - cy);
+    const float o1 = (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
+    const float o2 = (bx - ax) * (dy - ay) - (by - ay) * (dx - ax);
+    const float o3 = (dx - cx) * (ay - cy) - (dy - cy) * (ax - cx);
+    const float o4 = (dx - cx) * (by - cy) - (dy - cy) * (bx - cx);
+    const bool s1 = fabsf(o1) > orient_margin32(nab, nac, delta), s2 = fabsf(o2) > orient_margin32(nab, nad, delta);
+    const bool s3 = fabsf(o3) > orient_margin32(ncd, nac, delta), s4 = fabsf(o4) > orient_margin32(ncd, nbc, delta);
+    const bool c12 = s1 && s2, c34 = s3 && s4;
+    // every FP64 orientation has the FP32 sign and none is 0
+    if (c12 && c34) return ((o1 > 0) != (o2 > 0) && (o3 > 0) != (o4 > 0)) ? VF_INVALID : VF_VALID;
+    // Bounding boxes apart by more than 2*delta stay apart in FP64, so none of
+    // segs_intersect64's collinear cases can fire; then one certain same-sign
+    // pair of orientations rules out its proper crossing.
+    const float g = 2.f * delta;
+    const bool apart = fmaxf(ax, bx) + g < fminf(cx, dx) || fmaxf(cx, dx) + g < fminf(ax, bx) ||
+                       fmaxf(ay, by) + g < fminf(cy, dy) || fmaxf(cy, dy) + g < fminf(ay, by);
+    return (apart && ((c12 && (o1 > 0) == (o2 > 0)) || (c34 && (o3 > 0) == (o4 > 0)))) ? VF_VALID : VF_UNSURE;
+}
+
 // The exact FP64 joint angle of lane `lane` for one sample: b itself (t < 0)
 // or so2 interpolate(a, b, t), the DMV's sample expression.
 struct ArmSample {
@@ -384,46 +431,68 @@ __device__ __forceinline__ bool arm_state_warp(const SceneView& s, const ArmLane
     // the disc test's FP32 evaluation (coordinates of magnitude <= arm_span)
     // rounds like a further perturbation of the points by <= 8u*arm_span
     const float dd = delta + 8.f * U32 * s.arm_span;
-    bool have64 = false;
-    double x64 = 0.0, y64 = 0.0;
     const int C = (s.ndiscs + 31) >> 5;
-    for (int i = 0; i < nl; ++i) {
-        const float ax = __shfl_sync(FULL_MASK, xm, i), ay = __shfl_sync(FULL_MASK, ym, i);
-        const float bx = __shfl_sync(FULL_MASK, xm, i + 1), by = __shfl_sync(FULL_MASK, ym, i + 1);
-        for (int c = 0; c < C; ++c) {
-            const int k = lane + 32 * c;
-            int r = VF_VALID;
-            if (k < s.ndiscs) {
-                if (force64) {
-                    r = VF_UNSURE;
-                } else {
-                    const float4 d = __ldg(&s.discs32[k]);  // 1 KB per scene: L1-resident
-                    float d2 = dpseg2_32(d.x, d.y, ax, ay, bx, by);
-                    // the distance moves by <= dd, so d^2 by <= 2*d*dd + dd^2
-                    float m = 3.f * sqrtf(fmaxf(d2, d.z)) * dd + dd * dd + 8.f * U32 * (d2 + d.z);
-                    r = d2 <= d.z - m ? VF_INVALID : (d2 > d.z + m ? VF_VALID : VF_UNSURE);
+    const bool self = s.self_collision && al.nself > 0;
+    // The FP32 tests of all pairs first, with a vote on certain collisions
+    // every second link and one on undecided pairs at the end: the tests are
+    // independent, so the scheduler overlaps them, and the result does not
+    // depend on the order (the state is invalid iff some pair collides in
+    // FP64; an FP32 INVALID is a certain FP64 collision).
+    bool inv = false, uns = force64 && (lane < s.ndiscs || (self && lane < al.nself));
+    if (!force64) {
+#pragma unroll 2
+        for (int i = 0; i < nl; ++i) {
+            const float ax = __shfl_sync(FULL_MASK, xm, i), ay = __shfl_sync(FULL_MASK, ym, i);
+            const float bx = __shfl_sync(FULL_MASK, xm, i + 1), by = __shfl_sync(FULL_MASK, ym, i + 1);
+            for (int c = 0; c < C; ++c) {
+                const int k = lane + 32 * c;
+                if (k < s.ndiscs) {
+                    const int r = arm_disc32(s, k, ax, ay, bx, by, dd);
+                    inv |= r == VF_INVALID;
+                    uns |= r == VF_UNSURE;
                 }
             }
-            if (__any_sync(FULL_MASK, r == VF_INVALID)) return false;
-            if (__any_sync(FULL_MASK, r == VF_UNSURE)) {
-                if (!have64) {
-                    arm_sample_fk64(s, al, lane, smp, x64, y64);
-                    have64 = true;
+            // colliding states leave early, every second link
+            if ((i & 1) && __any_sync(FULL_MASK, inv)) return false;
+        }
+        if (self) {
+#pragma unroll
+            for (int c = 0; c < ARM_SELF_SLOTS; ++c) {
+                if (32 * c >= al.nself) break;
+                const int i = al.sij[c] & 0xff, j = al.sij[c] >> 8;
+                const float ax = __shfl_sync(FULL_MASK, xm, i), ay = __shfl_sync(FULL_MASK, ym, i);
+                const float bx = __shfl_sync(FULL_MASK, xm, i + 1), by = __shfl_sync(FULL_MASK, ym, i + 1);
+                const float cx = __shfl_sync(FULL_MASK, xm, j), cy = __shfl_sync(FULL_MASK, ym, j);
+                const float dx = __shfl_sync(FULL_MASK, xm, j + 1), dy = __shfl_sync(FULL_MASK, ym, j + 1);
+                if (lane + 32 * c < al.nself) {
+                    const int r = arm_self32(ax, ay, bx, by, cx, cy, dx, dy, delta);
+                    inv |= r == VF_INVALID;
+                    uns |= r == VF_UNSURE;
                 }
-                const double pax = __shfl_sync(FULL_MASK, x64, i), pay = __shfl_sync(FULL_MASK, y64, i);
-                const double pbx = __shfl_sync(FULL_MASK, x64, i + 1), pby = __shfl_sync(FULL_MASK, y64, i + 1);
-                bool hit = false;
-                if (r == VF_UNSURE) {
-                    const double* dk = s.discs64 + 3 * k;
-                    double rr = __dmul_rn(__dadd_rn(dk[2], s.robot_radius), __dadd_rn(dk[2], s.robot_radius));
-                    hit = !(dist_point_segment_sq64(dk[0], dk[1], pax, pay, pbx, pby) > rr);
-                }
-                if (__any_sync(FULL_MASK, hit)) return false;
             }
         }
     }
-    if (s.self_collision && al.nself > 0) {
-        const float mo = 16.f * delta * R + 8.f * delta * delta + 32.f * U32 * R * R + 1e-30f;
+    if (__any_sync(FULL_MASK, inv)) return false;
+    if (!__any_sync(FULL_MASK, uns)) return true;
+    // the rare path: FP64 kinematics once, then the undecided pairs in FP64
+    double x64 = 0.0, y64 = 0.0;
+    arm_sample_fk64(s, al, lane, smp, x64, y64);
+    bool hit = false;
+    for (int i = 0; i < nl; ++i) {
+        const float ax = __shfl_sync(FULL_MASK, xm, i), ay = __shfl_sync(FULL_MASK, ym, i);
+        const float bx = __shfl_sync(FULL_MASK, xm, i + 1), by = __shfl_sync(FULL_MASK, ym, i + 1);
+        const double pax = __shfl_sync(FULL_MASK, x64, i), pay = __shfl_sync(FULL_MASK, y64, i);
+        const double pbx = __shfl_sync(FULL_MASK, x64, i + 1), pby = __shfl_sync(FULL_MASK, y64, i + 1);
+        for (int c = 0; c < C; ++c) {
+            const int k = lane + 32 * c;
+            if (k < s.ndiscs && (force64 || arm_disc32(s, k, ax, ay, bx, by, dd) == VF_UNSURE)) {
+                const double* dk = s.discs64 + 3 * k;
+                double rr = __dmul_rn(__dadd_rn(dk[2], s.robot_radius), __dadd_rn(dk[2], s.robot_radius));
+                hit |= !(dist_point_segment_sq64(dk[0], dk[1], pax, pay, pbx, pby) > rr);
+            }
+        }
+    }
+    if (self) {
 #pragma unroll
         for (int c = 0; c < ARM_SELF_SLOTS; ++c) {
             if (32 * c >= al.nself) break;
@@ -432,48 +501,16 @@ __device__ __forceinline__ bool arm_state_warp(const SceneView& s, const ArmLane
             const float bx = __shfl_sync(FULL_MASK, xm, i + 1), by = __shfl_sync(FULL_MASK, ym, i + 1);
             const float cx = __shfl_sync(FULL_MASK, xm, j), cy = __shfl_sync(FULL_MASK, ym, j);
             const float dx = __shfl_sync(FULL_MASK, xm, j + 1), dy = __shfl_sync(FULL_MASK, ym, j + 1);
-            int r = VF_VALID;
-            if (lane + 32 * c < al.nself) {
-                if (force64) {
-                    r = VF_UNSURE;
-                } else {
-                    float o1 = (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
-                    float o2 = (bx - ax) * (dy - ay) - (by - ay) * (dx - ax);
-                    float o3 = (dx - cx) * (ay - cy) - (dy - cy) * (ax - cx);
-                    float o4 = (dx - cx) * (by - cy) - (dy - cy) * (bx - cx);
-                    const bool c12 = fabsf(o1) > mo && fabsf(o2) > mo, c34 = fabsf(o3) > mo && fabsf(o4) > mo;
-                    if (c12 && c34) {
-                        // every FP64 orientation has the FP32 sign and none is 0
-                        r = ((o1 > 0) != (o2 > 0) && (o3 > 0) != (o4 > 0)) ? VF_INVALID : VF_VALID;
-                    } else {
-                        // Bounding boxes apart by more than 2*delta stay apart in
-                        // FP64, so none of segs_intersect64's collinear cases can
-                        // fire; then one certain same-sign pair of orientations
-                        // rules out its proper crossing.
-                        const float g = 2.f * delta;
-                        const bool apart = fmaxf(ax, bx) + g < fminf(cx, dx) || fmaxf(cx, dx) + g < fminf(ax, bx) ||
-                                           fmaxf(ay, by) + g < fminf(cy, dy) || fmaxf(cy, dy) + g < fminf(ay, by);
-                        r = (apart && ((c12 && (o1 > 0) == (o2 > 0)) || (c34 && (o3 > 0) == (o4 > 0)))) ? VF_VALID
-                                                                                                       : VF_UNSURE;
-                    }
-                }
-            }
-            if (__any_sync(FULL_MASK, r == VF_INVALID)) return false;
-            if (__any_sync(FULL_MASK, r == VF_UNSURE)) {
-                if (!have64) {
-                    arm_sample_fk64(s, al, lane, smp, x64, y64);
-                    have64 = true;
-                }
-                const double pax = __shfl_sync(FULL_MASK, x64, i), pay = __shfl_sync(FULL_MASK, y64, i);
-                const double pbx = __shfl_sync(FULL_MASK, x64, i + 1), pby = __shfl_sync(FULL_MASK, y64, i + 1);
-                const double pcx = __shfl_sync(FULL_MASK, x64, j), pcy = __shfl_sync(FULL_MASK, y64, j);
-                const double pdx = __shfl_sync(FULL_MASK, x64, j + 1), pdy = __shfl_sync(FULL_MASK, y64, j + 1);
-                bool hit = r == VF_UNSURE && segs_intersect64(pax, pay, pbx, pby, pcx, pcy, pdx, pdy);
-                if (__any_sync(FULL_MASK, hit)) return false;
-            }
+            const double pax = __shfl_sync(FULL_MASK, x64, i), pay = __shfl_sync(FULL_MASK, y64, i);
+            const double pbx = __shfl_sync(FULL_MASK, x64, i + 1), pby = __shfl_sync(FULL_MASK, y64, i + 1);
+            const double pcx = __shfl_sync(FULL_MASK, x64, j), pcy = __shfl_sync(FULL_MASK, y64, j);
+            const double pdx = __shfl_sync(FULL_MASK, x64, j + 1), pdy = __shfl_sync(FULL_MASK, y64, j + 1);
+            if (lane + 32 * c < al.nself &&
+                (force64 || arm_self32(ax, ay, bx, by, cx, cy, dx, dy, delta) == VF_UNSURE))
+                hit |= segs_intersect64(pax, pay, pbx, pby, pcx, pcy, pdx, pdy);
         }
     }
-    return true;
+    return !__any_sync(FULL_MASK, hit);
 }
 
 // a state given in FP64, joint `lane` in qd; the FP32 angles are within
