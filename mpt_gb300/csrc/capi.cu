@@ -89,6 +89,7 @@ mptg_status mptg_create(mptg_ctx** out, int device) {
     if (cudaSetDevice(device) != cudaSuccess) return MPTG_ERR_CUDA;
     mptg_ctx* c = new mptg_ctx();
     c->device = device;
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
     *out = c;
     return MPTG_OK;
 }

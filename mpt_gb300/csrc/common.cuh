@@ -26,6 +26,7 @@
 
 struct mptg_ctx {
     int device = 0;
+    int sms = 152;  // multiprocessors of the device
     char err[512] = {0};
     std::atomic<uint64_t> launches{0};
     std::mutex mu;

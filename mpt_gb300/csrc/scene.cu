@@ -536,21 +536,20 @@ __global__ void __launch_bounds__(256) k_arm_states(SceneView s, const double* _
     if (lane == 0) out[e] = ok ? 1 : 0;
 }
 
-// DMV link for planar-arm edges, warp per edge: the end state first, then the
-// step count (edge_steps' FP64 value, lane per joint), then the interior
-// samples i*delta one at a time in the coarse-to-fine order of k_grid_edges_b
-__global__ void __launch_bounds__(256) k_arm_edges(SceneView s, const double* __restrict__ a,
-                                                   const double* __restrict__ b, int n, double inv, int resolution,
-                                                   uint8_t* __restrict__ out, unsigned long long* __restrict__ nsamp) {
-    const int lane = threadIdx.x & 31;
-    const int e = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-    if (e >= n) return;
+// one warp's share of edge e (see k_arm_edges); false iff it met an invalid
+// sample or the step count is out of range
+__device__ __forceinline__ bool arm_edge_warp(const SceneView& s, const double* __restrict__ a,
+                                              const double* __restrict__ b, int e, double inv, int resolution,
+                                              int lane, int g, int G, volatile int* dead, unsigned long long& cnt) {
     const int D = s.D;
     const ArmLane al = arm_lane(s, lane);
     const double Ad = lane < D ? a[(size_t)e * D + lane] : 0.0;
     const double Bd = lane < D ? b[(size_t)e * D + lane] : 0.0;
-    unsigned long long cnt = 1;
-    bool ok = arm_state_exact(s, al, lane, Bd);
+    bool ok = true;
+    if (g == 0) {
+        cnt = 1;
+        ok = arm_state_exact(s, al, lane, Bd);
+    }
     long long steps = 0;
     if (ok) {
         // ceil(m(a, b) * inv): m = max wrapped joint difference (resolution 1)
@@ -584,9 +583,11 @@ __global__ void __launch_bounds__(256) k_arm_edges(SceneView s, const double* __
         const int R = (M + 31) / 32;
         const double delta = __ddiv_rn(1.0, (double)steps);
         for (int r = 0; ok && r < R; ++r) {
-            for (int j = 0; ok && j < 32; ++j) {
+            for (int j = g; ok && j < 32; j += G) {
                 const int k = 1 + j * R + r;
                 if (k > M) continue;
+                // another warp of the edge met an invalid sample (lane 0's read, warp-uniform)
+                if (dead && __shfl_sync(FULL_MASK, *dead, 0)) return true;
                 ++cnt;
                 const float t = (float)k / (float)steps;
                 const float q32 = fmaf(dir32, t, a32);
@@ -594,8 +595,40 @@ __global__ void __launch_bounds__(256) k_arm_edges(SceneView s, const double* __
             }
         }
     }
-    if (lane == 0) {
-        out[e] = ok ? 1 : 0;
+    return ok;
+}
+
+// DMV link for planar-arm edges, 2^lg warps per edge (lg <= 3; 1 for large
+// batches, more when the batch is too small to fill the GPU): the end state
+// (warp 0), then the step count (edge_steps' FP64 value, lane per joint), then
+// the interior samples i*delta in the coarse-to-fine order of k_grid_edges_b,
+// dealt round-robin to the edge's warps.  The edge is valid iff no warp finds
+// an invalid sample, whatever the order; a warp that finds one raises the
+// edge's shared flag and the others stop at their next sample.
+__global__ void __launch_bounds__(256) k_arm_edges(SceneView s, const double* __restrict__ a,
+                                                   const double* __restrict__ b, int n, double inv, int resolution,
+                                                   uint8_t* __restrict__ out, unsigned long long* __restrict__ nsamp,
+                                                   int lg) {
+    __shared__ int dead[8];  // per edge of the block
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lg > 0) {
+        if (threadIdx.x < 8) dead[threadIdx.x] = 0;
+        __syncthreads();
+    }
+    const int G = 1 << lg, g = w & (G - 1), slot = w >> lg;
+    const int e = (int)(((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5) >> lg);
+    bool ok = true;
+    unsigned long long cnt = 0;
+    if (e < n) {
+        ok = arm_edge_warp(s, a, b, e, inv, resolution, lane, g, G, lg > 0 ? &dead[slot] : nullptr, cnt);
+        if (!ok && lg > 0 && lane == 0) atomicExch(&dead[slot], 1);
+    }
+    if (lg > 0) {
+        __syncthreads();
+        ok = dead[slot] == 0;
+    }
+    if (e < n && lane == 0) {
+        if (g == 0) out[e] = ok ? 1 : 0;
         if (nsamp) atomicAdd(nsamp, cnt);
     }
 }
@@ -676,8 +709,11 @@ mptg_status scene_edges_dev(mptg_scene* sc, const double* da, const double* db, 
     if (sc->kind == MPTG_SCENE_RIGID_MESH)
         return mesh_edges_dev(sc, da, db, n, step, resolution, dout, s, nsamp, x);
     if (sc->kind == MPTG_SCENE_PLANAR_ARM) {
-        k_arm_edges<<<mptg_blocks((size_t)n * 32, 256), 256, 0, s>>>(scene_view(sc), da, db, n, 1.0 / step,
-                                                                     resolution, dout, nsamp);
+        // up to 8 warps per edge while the batch has fewer than 16 warps per SM
+        int lg = 0;
+        while (lg < 3 && ((size_t)n << lg) < (size_t)sc->ctx->sms * 16) ++lg;
+        k_arm_edges<<<mptg_blocks(((size_t)n * 32) << lg, 256), 256, 0, s>>>(scene_view(sc), da, db, n, 1.0 / step,
+                                                                            resolution, dout, nsamp, lg);
         MPTG_LAUNCHED(sc->ctx);
         return MPTG_OK;
     }

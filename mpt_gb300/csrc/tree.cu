@@ -71,6 +71,10 @@ struct mptg_tree {
     float* bcd = nullptr;
     int* bci = nullptr;
     size_t bcap = 0;
+    // split k-NN scratch: [split][queries][k] lists
+    double* kcd = nullptr;
+    int* kci = nullptr;
+    size_t kcap = 0;
     // query ordering scratch (grown on demand)
     int* qkey = nullptr;
     int* qorder = nullptr;
@@ -928,39 +932,51 @@ __global__ void __launch_bounds__(BRUTE_TILE) k_nearest_tiled(TreeView t, const 
     }
 }
 
+// Warp per query: the lanes take the splits round-robin.  Each split's list is
+// sorted, so a split whose first entry exceeds min32 + 2E holds no candidate
+// and is complete, and the common case reads one value per split.
 template <int MK, int DMAX>
 __global__ void __launch_bounds__(256) k_nearest_tiled_merge(TreeView t, const double* __restrict__ q64, int nq,
                                                              int nsplit, const float* __restrict__ cd,
                                                              const int* __restrict__ ci, int* __restrict__ out_idx,
                                                              double* __restrict__ out_d) {
-    const int qi = blockIdx.x * blockDim.x + threadIdx.x;
-    if (qi >= nq) return;
+    const int lane = threadIdx.x & 31;
+    const int qi = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    if (qi >= nq) return;  // warp-uniform
     const int D = t.D;
     const double* qd = q64 + (size_t)qi * D;
     float q[DMAX];
     const float E = load_query32<MK, DMAX>(t, qd, true, q);
     float m = INFINITY;
-    for (int sp = 0; sp < nsplit; ++sp) m = fminf(m, cd[((size_t)sp * BRUTE_K) * nq + qi]);
+    for (int sp = lane; sp < nsplit; sp += 32) m = fminf(m, cd[((size_t)sp * BRUTE_K) * nq + qi]);
+    for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
     double best = INFINITY;
     int bidx = INT_MAX;
     unsigned long long nrr = 0;
     if (m < INFINITY) {
         const float thr = __fadd_ru(m, __fmul_ru(2.f, E));
-        bool complete = true;
-        for (int sp = 0; sp < nsplit; ++sp) complete = complete && cd[((size_t)sp * BRUTE_K + BRUTE_K - 1) * nq + qi] > thr;
         auto consider = [&](int id) {
             ++nrr;
             double dd = dist64(t.metric, D, t.w0, t.w1, qd, t.states64 + (size_t)id * D);
             if (dd == dd && (dd < best || (dd == best && id < bidx))) { best = dd; bidx = id; }
         };
-        if (complete) {
-            for (int sp = 0; sp < nsplit; ++sp)
-                for (int s = 0; s < BRUTE_K; ++s) {
-                    const size_t o = ((size_t)sp * BRUTE_K + s) * nq + qi;
-                    if (ci[o] >= 0 && cd[o] <= thr) consider(ci[o]);
-                }
-        } else {
-            for (int j = 0; j < t.n; ++j) {
+        bool complete = true;
+        for (int sp = lane; sp < nsplit; sp += 32) {
+            const size_t o0 = ((size_t)sp * BRUTE_K) * nq + qi;
+            if (!(cd[o0] <= thr)) continue;
+            complete = complete && cd[o0 + (size_t)(BRUTE_K - 1) * nq] > thr;
+            for (int s = 0; s < BRUTE_K; ++s) {
+                const size_t o = o0 + (size_t)s * nq;
+                if (!(cd[o] <= thr)) break;
+                if (ci[o] >= 0) consider(ci[o]);
+            }
+        }
+        if (!__all_sync(0xffffffffu, complete)) {
+            // more than BRUTE_K points within 2E in some split: every point
+            // again, lanes round-robin
+            best = INFINITY;
+            bidx = INT_MAX;
+            for (int j = lane; j < t.n; j += 32) {
                 float p[DMAX];
 #pragma unroll
                 for (int d = 0; d < DMAX; ++d) p[d] = d < D ? t.pts32[(size_t)j * D + d] : 0.f;
@@ -968,12 +984,21 @@ __global__ void __launch_bounds__(256) k_nearest_tiled_merge(TreeView t, const d
             }
         }
     }
-    out_idx[qi] = bidx == INT_MAX ? -1 : bidx;
-    out_d[qi] = best;
-    if (t.stats) {
-        atomicAdd(&t.stats[0], 1ull);
-        atomicAdd(&t.stats[3], (unsigned long long)t.n);
-        atomicAdd(&t.stats[4], nrr);
+    // (distance, id) minimum over the lanes
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+        if (ob < best || (ob == best && oi < bidx)) { best = ob; bidx = oi; }
+    }
+    for (int o = 16; o > 0; o >>= 1) nrr += __shfl_xor_sync(0xffffffffu, nrr, o);
+    if (lane == 0) {
+        out_idx[qi] = bidx == INT_MAX ? -1 : bidx;
+        out_d[qi] = best;
+        if (t.stats) {
+            atomicAdd(&t.stats[0], 1ull);
+            atomicAdd(&t.stats[3], (unsigned long long)t.n);
+            atomicAdd(&t.stats[4], nrr);
+        }
     }
 }
 
@@ -983,6 +1008,9 @@ __global__ void __launch_bounds__(256) k_nearest_tiled_merge(TreeView t, const d
 // warp's sorted k-NN list: every point whose FP32 distance is within E of the
 // bound tau gets its FP64 distance, and those within tau join the list in
 // (distance, id) order, one at a time (the list lives two entries per lane).
+__device__ __forceinline__ void knn_insert(int lane, int k, double radius, bool cand, double dd, int pid, double& ld0,
+                                           double& ld1, int& li0, int& li1, int& cnt, double& tau, float& tauf);
+
 __device__ __forceinline__ void knn_consider(const TreeView& t, const double* __restrict__ qd, int lane, int k,
                                              double radius, bool have, int pid, float d32, float E, double& ld0,
                                              double& ld1, int& li0, int& li1, int& cnt, double& tau, float& tauf) {
@@ -992,6 +1020,12 @@ __device__ __forceinline__ void knn_consider(const TreeView& t, const double* __
         dd = dist64(t.metric, t.D, t.w0, t.w1, qd, t.states64 + (size_t)pid * t.D);
         cand = dd <= tau;
     }
+    knn_insert(lane, k, radius, cand, dd, pid, ld0, ld1, li0, li1, cnt, tau, tauf);
+}
+
+// the lanes with cand set offer (dd, pid) to the list, lowest lane first
+__device__ __forceinline__ void knn_insert(int lane, int k, double radius, bool cand, double dd, int pid, double& ld0,
+                                           double& ld1, int& li0, int& li1, int& cnt, double& tau, float& tauf) {
     unsigned cmask = __ballot_sync(0xffffffffu, cand);
     while (cmask) {
         int src = __ffs(cmask) - 1;
@@ -1031,19 +1065,64 @@ __device__ __forceinline__ void knn_consider(const TreeView& t, const double* __
     }
 }
 
+// FP32 twin of knn_insert for k_nearest_k_tiled's running list: the 64 best
+// (d32, id) pairs, entry j in lane j (fd0/fi0) or lane j - 32 (fd1/fi1)
+__device__ __forceinline__ void fknn_insert(int lane, bool cand, float d32, int pid, float& fd0, float& fd1, int& fi0,
+                                            int& fi1, int& fcnt, float& ftau) {
+    unsigned cmask = __ballot_sync(0xffffffffu, cand);
+    while (cmask) {
+        const int src = __ffs(cmask) - 1;
+        cmask &= cmask - 1;
+        const float cd = __shfl_sync(0xffffffffu, d32, src);
+        const int ci = __shfl_sync(0xffffffffu, pid, src);
+        if (fcnt == 64) {
+            const float kd = __shfl_sync(0xffffffffu, fd1, 31);
+            const int ki = __shfl_sync(0xffffffffu, fi1, 31);
+            if (!(cd < kd || (cd == kd && ci < ki))) continue;
+        }
+        const bool ahead0 = lane < fcnt && (fd0 < cd || (fd0 == cd && fi0 < ci));
+        const bool ahead1 = lane + 32 < fcnt && (fd1 < cd || (fd1 == cd && fi1 < ci));
+        const int pos = __popc(__ballot_sync(0xffffffffu, ahead0)) + __popc(__ballot_sync(0xffffffffu, ahead1));
+        const float p0d = __shfl_up_sync(0xffffffffu, fd0, 1), p1d = __shfl_up_sync(0xffffffffu, fd1, 1);
+        const int p0i = __shfl_up_sync(0xffffffffu, fi0, 1), p1i = __shfl_up_sync(0xffffffffu, fi1, 1);
+        const float l0d = __shfl_sync(0xffffffffu, fd0, 31);
+        const int l0i = __shfl_sync(0xffffffffu, fi0, 31);
+        if (lane > pos) { fd0 = p0d; fi0 = p0i; }
+        else if (lane == pos) { fd0 = cd; fi0 = ci; }
+        const int j1 = lane + 32;
+        if (j1 > pos) { fd1 = lane == 0 ? l0d : p1d; fi1 = lane == 0 ? l0i : p1i; }
+        else if (j1 == pos) { fd1 = cd; fi1 = ci; }
+        if (fcnt < 64) ++fcnt;
+        if (fcnt == 64) ftau = __shfl_sync(0xffffffffu, fd1, 31);
+    }
+}
+
 // Exhaustive k nearest for high-dimensional trees (the strategy rule of the
-// 1-NN sweep): a block of 8 warps (8 queries) stages the FP32 points through
-// shared memory, 256 at a time, and each warp runs every 32-point slice
-// through knn_consider, the list logic of the tree walk.  The list is the
-// exact (distance, id)-ordered top k whatever order the points arrive in, so
-// the answers equal k_nearest_k's.
+// 1-NN sweep), warp per (query, point split): a block of 8 queries stages the
+// split's FP32 points through shared memory, 256 at a time, and each warp
+// keeps the 64 best FP32 (distance, id) pairs, FP32 work only.  With
+// dk = the k-th kept FP32 distance, every member p of the exact top k has
+//   d32(p) <= d64(p) + E <= dk + 2E
+// (the k FP32-best points lie within dk + E in FP64, or one of them lies
+// beyond the radius, which then is below dk + E), so when the list holds the
+// whole split or its 64th entry exceeds dk + 2E, the exact top k is the
+// knn_insert ranking of the kept entries within dk + 2E by their FP64
+// distances.  Otherwise (more than 64 - k points within 2E of dk, e.g.
+// duplicates) the warp sweeps the split again through knn_consider, the list
+// logic of the tree walk.  Either way the list is the exact (distance,
+// id)-ordered top k of the split.  With one split it is the answer (equal to
+// k_nearest_k's); with several, each split's list goes to out + split * nq * k
+// and k_nearest_k_merge keeps the top k of their union, which holds the
+// global top k.  The list's slack is 64 - k entries, so with k near 64 the
+// second sweep runs more often.
 template <int MK, int DMAX>
 __global__ void __launch_bounds__(256) k_nearest_k_tiled(TreeView t, const double* __restrict__ q64, int nq, int k,
-                                                         double radius, int* __restrict__ out_idx,
+                                                         double radius, int chunk, int* __restrict__ out_idx,
                                                          double* __restrict__ out_d) {
     __shared__ float tile[DMAX][256];
     const int lane = threadIdx.x & 31;
     const int qi = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int split = blockIdx.y;
     const bool active = qi < nq;  // warp-uniform
     const int D = t.D;
     const double* qd = q64 + (size_t)(active ? qi : 0) * D;
@@ -1051,13 +1130,10 @@ __global__ void __launch_bounds__(256) k_nearest_k_tiled(TreeView t, const doubl
     float myq, M;
     load_query<MK, DMAX>(qd, D, lane, q, myq, M, t);
     const float E = err32<MK>(D, M, t.w0f, t.w1f);
-    double ld0 = INFINITY, ld1 = INFINITY;
-    int li0 = INT_MAX, li1 = INT_MAX;
-    int cnt = 0;
-    double tau = radius;
-    float tauf = __double2float_ru(tau);
-    const int n = t.n;
-    for (int base = 0; base < n; base += 256) {
+    float fd0 = INFINITY, fd1 = INFINITY, ftau = INFINITY;
+    int fi0 = INT_MAX, fi1 = INT_MAX, fcnt = 0;
+    const int lo = split * chunk, n = min(t.n, lo + chunk);
+    for (int base = lo; base < n; base += 256) {
         __syncthreads();
         const int j = base + threadIdx.x;
 #pragma unroll
@@ -1069,19 +1145,82 @@ __global__ void __launch_bounds__(256) k_nearest_k_tiled(TreeView t, const doubl
             const int off = sub + lane;
             const bool have = off < cntp;
             float d32 = INFINITY;
-            int pid = -1;
             if (have) {
                 float p[DMAX];
 #pragma unroll
                 for (int d = 0; d < DMAX; ++d) p[d] = tile[d][off];
                 d32 = dist32<MK, DMAX>(q, p, t.w0f, t.w1f);
                 if (!(d32 == d32)) d32 = INFINITY;
-                pid = base + off;
             }
-            knn_consider(t, qd, lane, k, radius, have, pid, d32, E, ld0, ld1, li0, li1, cnt, tau, tauf);
+            fknn_insert(lane, have && d32 <= ftau, d32, base + off, fd0, fd1, fi0, fi1, fcnt, ftau);
         }
     }
     if (!active) return;
+    double ld0 = INFINITY, ld1 = INFINITY;
+    int li0 = INT_MAX, li1 = INT_MAX;
+    int cnt = 0;
+    double tau = radius;
+    float tauf = __double2float_ru(tau);
+    const float dk = __shfl_sync(0xffffffffu, k - 1 < 32 ? fd0 : fd1, (k - 1) & 31);
+    const float thr = __fadd_ru(dk, __fmul_ru(2.f, E));
+    const bool whole = fcnt < 64;
+    if (whole || (thr < INFINITY && __shfl_sync(0xffffffffu, fd1, 31) > thr)) {
+        // exact re-rank of the kept entries within thr (all of them for a whole split)
+        for (int slot = 0; slot < 2; ++slot) {
+            const int e = lane + 32 * slot;
+            const float fd = slot ? fd1 : fd0;
+            const int fi = slot ? fi1 : fi0;
+            bool cand = e < fcnt && (whole || fd <= thr);
+            double dd = INFINITY;
+            if (cand) {
+                dd = dist64(t.metric, D, t.w0, t.w1, qd, t.states64 + (size_t)fi * D);
+                cand = dd <= tau;
+            }
+            knn_insert(lane, k, radius, cand, dd, fi, ld0, ld1, li0, li1, cnt, tau, tauf);
+        }
+    } else {
+        for (int base = lo; base < n; base += 32) {
+            const int j = base + lane;
+            const bool have = j < n;
+            float d32 = INFINITY;
+            if (have) {
+                float p[DMAX];
+#pragma unroll
+                for (int d = 0; d < DMAX; ++d) p[d] = d < D ? t.pts32[(size_t)j * D + d] : 0.f;
+                d32 = dist32<MK, DMAX>(q, p, t.w0f, t.w1f);
+                if (!(d32 == d32)) d32 = INFINITY;
+            }
+            knn_consider(t, qd, lane, k, radius, have, j, d32, E, ld0, ld1, li0, li1, cnt, tau, tauf);
+        }
+    }
+    int* oi = out_idx + ((size_t)split * nq + qi) * k;
+    double* od = out_d + ((size_t)split * nq + qi) * k;
+    if (lane < k) { bool v = lane < cnt; oi[lane] = v ? li0 : -1; od[lane] = v ? ld0 : INFINITY; }
+    if (lane + 32 < k) { bool v = lane + 32 < cnt; oi[lane + 32] = v ? li1 : -1; od[lane + 32] = v ? ld1 : INFINITY; }
+}
+
+// Top k of the per-split lists of k_nearest_k_tiled (cd / ci: [split][nq][k],
+// FP64 distances), warp per query, through the same insertion logic.
+__global__ void __launch_bounds__(256) k_nearest_k_merge(int nq, int k, double radius, int nsplit,
+                                                         const double* __restrict__ cd, const int* __restrict__ ci,
+                                                         int* __restrict__ out_idx, double* __restrict__ out_d) {
+    const int lane = threadIdx.x & 31;
+    const int qi = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    if (qi >= nq) return;  // warp-uniform
+    double ld0 = INFINITY, ld1 = INFINITY;
+    int li0 = INT_MAX, li1 = INT_MAX;
+    int cnt = 0;
+    double tau = radius;
+    float tauf = __double2float_ru(tau);
+    const int total = nsplit * k;
+    for (int c0 = 0; c0 < total; c0 += 32) {
+        const int c = c0 + lane;
+        const int sp = c / k, j = c - sp * k;
+        const size_t o = ((size_t)sp * nq + qi) * k + j;
+        const int pid = c < total ? ci[o] : -1;
+        const double dd = pid >= 0 ? cd[o] : INFINITY;
+        knn_insert(lane, k, radius, pid >= 0 && dd <= tau, dd, pid, ld0, ld1, li0, li1, cnt, tau, tauf);
+    }
     int* oi = out_idx + (size_t)qi * k;
     double* od = out_d + (size_t)qi * k;
     if (lane < k) { bool v = lane < cnt; oi[lane] = v ? li0 : -1; od[lane] = v ? ld0 : INFINITY; }
@@ -1264,7 +1403,7 @@ static void tree_free(mptg_tree* t) {
     void* ptrs[] = {t->states64, t->pts32, t->nodes, t->cell_lo, t->cell_hi, t->node_depth, t->bpts, t->bids,
                     t->dcnt, t->dstats, t->perm, t->perm2, t->pseg, t->pseg2, t->segA, t->segB, t->seg_box,
                     t->leaf_of, t->ovf_pts, t->ovf_leaf, t->leaf_reg, t->seg_cursor, t->qkey, t->qorder,
-                    t->qhist, t->bcd, t->bci};
+                    t->qhist, t->bcd, t->bci, t->kcd, t->kci};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (t->hcnt) cudaFreeHost(t->hcnt);
@@ -1590,8 +1729,8 @@ mptg_status mptg_tree_nearest_dev(mptg_tree* t, const double* dq, int nq, int* d
         }
         dim3 grid(qblocks, nsplit);
         DISPATCH_METRIC(t->metric, t->D, k_nearest_tiled, grid, BRUTE_TILE, s, v, dq, nq, chunk, t->bcd, t->bci);
-        DISPATCH_METRIC(t->metric, t->D, k_nearest_tiled_merge, mptg_blocks((size_t)nq, 256), 256, s, v, dq, nq, nsplit,
-                        t->bcd, t->bci, didx, dd);
+        DISPATCH_METRIC(t->metric, t->D, k_nearest_tiled_merge, mptg_blocks((size_t)nq * 32, 256), 256, s, v, dq, nq,
+                        nsplit, t->bcd, t->bci, didx, dd);
         ctx->launches += 2;
         return MPTG_OK;
     }
@@ -1672,21 +1811,56 @@ mptg_status mptg_nearest_linear(mptg_tree* t, const double* q, size_t nq, int32_
     return mptg_stage_finish(ctx, s, outs, 2, &bq, 1);
 }
 
+// k nearest on device buffers: the tree walk, or the exhaustive sweep with
+// the points split over blocks while the queries alone give fewer than two
+// blocks per SM (at least 2048 points per split), then the merge of the lists
+static mptg_status knn_launch(mptg_tree* t, const TreeView& v, const double* dq, int nq, int k, double radius,
+                              int* didx, double* dd, cudaStream_t s) {
+    mptg_ctx* ctx = t->ctx;
+    if (!tree_use_tiled(t, nq)) {
+        unsigned grid = mptg_blocks((size_t)nq * 32, 256);
+        DISPATCH_METRIC(t->metric, t->D, k_nearest_k, grid, 256, s, v, dq, nq, k, radius, didx, dd);
+        MPTG_LAUNCHED(ctx);
+        return MPTG_OK;
+    }
+    const int qblocks = (int)mptg_blocks((size_t)nq, 8);
+    const int maxsplit = std::max(1, (int)(t->n / 2048));
+    const int nsplit = std::min(maxsplit, std::max(1, (2 * ctx->sms + qblocks - 1) / qblocks));
+    const int chunk = (int)((t->n + nsplit - 1) / nsplit);
+    if (nsplit == 1) {
+        DISPATCH_METRIC(t->metric, t->D, k_nearest_k_tiled, dim3(qblocks, 1), 256, s, v, dq, nq, k, radius, chunk,
+                        didx, dd);
+        MPTG_LAUNCHED(ctx);
+        return MPTG_OK;
+    }
+    const size_t need = (size_t)nsplit * nq * k;
+    if (need > t->kcap) {
+        MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        cudaFree(t->kcd);
+        cudaFree(t->kci);
+        t->kcd = nullptr;
+        t->kci = nullptr;
+        t->kcap = 0;
+        const size_t cap = need + need / 2;
+        MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&t->kcd, cap * sizeof(double)));
+        MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&t->kci, cap * sizeof(int)));
+        t->kcap = cap;
+    }
+    DISPATCH_METRIC(t->metric, t->D, k_nearest_k_tiled, dim3(qblocks, nsplit), 256, s, v, dq, nq, k, radius, chunk,
+                    t->kci, t->kcd);
+    k_nearest_k_merge<<<mptg_blocks((size_t)nq * 32, 256), 256, 0, s>>>(nq, k, radius, nsplit, t->kcd, t->kci, didx,
+                                                                         dd);
+    ctx->launches += 2;
+    return MPTG_OK;
+}
+
 mptg_status mptg_tree_nearest_k_dev(mptg_tree* t, const double* dq, int nq, int k, int* didx, double* dd,
                                     cudaStream_t s) {
     if (nq <= 0) return MPTG_OK;
     if (k < 1 || k > 64) return mptg_fail(t->ctx, MPTG_ERR_INVALID_ARG, "k=%d outside [1,64]", k);
     TreeView v = view_of(t);
     v.stats = nullptr;
-    if (tree_use_tiled(t, nq)) {
-        DISPATCH_METRIC(t->metric, t->D, k_nearest_k_tiled, mptg_blocks((size_t)nq, 8), 256, s, v, dq, nq, k,
-                        (double)INFINITY, didx, dd);
-    } else {
-        unsigned grid = mptg_blocks((size_t)nq * 32, 256);
-        DISPATCH_METRIC(t->metric, t->D, k_nearest_k, grid, 256, s, v, dq, nq, k, (double)INFINITY, didx, dd);
-    }
-    MPTG_LAUNCHED(t->ctx);
-    return MPTG_OK;
+    return knn_launch(t, v, dq, nq, k, (double)INFINITY, didx, dd, s);
 }
 
 mptg_status mptg_nearest_k(mptg_tree* t, const double* q, size_t nq, int k, double r, int32_t* idx, double* dist,
@@ -1704,15 +1878,8 @@ mptg_status mptg_nearest_k(mptg_tree* t, const double* q, size_t nq, int k, doub
     if ((st = mptg_stage_out_alloc(ctx, idx, nq * k * sizeof(int32_t), s, &bi))) return st;
     if ((st = mptg_stage_out_alloc(ctx, dist, nq * k * sizeof(double), s, &bd))) return st;
     TreeView v = view_of(t);
-    if (tree_use_tiled(t, (int)nq)) {
-        DISPATCH_METRIC(t->metric, t->D, k_nearest_k_tiled, mptg_blocks(nq, 8), 256, s, v, (const double*)bq.dptr,
-                        (int)nq, k, r, (int*)bi.dptr, (double*)bd.dptr);
-    } else {
-        unsigned grid = mptg_blocks(nq * 32, 256);
-        DISPATCH_METRIC(t->metric, t->D, k_nearest_k, grid, 256, s, v, (const double*)bq.dptr, (int)nq, k, r,
-                        (int*)bi.dptr, (double*)bd.dptr);
-    }
-    MPTG_LAUNCHED(ctx);
+    if ((st = knn_launch(t, v, (const double*)bq.dptr, (int)nq, k, r, (int*)bi.dptr, (double*)bd.dptr, s)))
+        return st;
     MPTG_CUDA_TRY(ctx, cudaGetLastError());
     DevBuf outs[2] = {bi, bd};
     return mptg_stage_finish(ctx, s, outs, 2, &bq, 1);

@@ -160,6 +160,26 @@ def test_nearest_k_matches_oracle(ctx, orc, name, k, radius):
         assert np.array_equal(gd, od)
 
 
+@pytest.mark.parametrize("n,reps,k", [(40, 1, 32), (12000, 6, 32), (12000, 40, 20), (9000, 1, 48)])
+def test_nearest_k_exhaustive_ties(ctx, orc, n, reps, k):
+    """The exhaustive k-NN's FP32 selection: splits smaller than its 64-entry
+    list, runs of duplicates longer than the list's slack (the exact second
+    sweep) and k near the slack, against the oracle's (distance, id) order."""
+    sc = SPACES["arm_so2x10"]()
+    base = scenes.uniform_states(sc, max(1, n // reps), 211)
+    pts = np.repeat(base, reps, axis=0)[:n]
+    q = np.concatenate([scenes.uniform_states(sc, 300, 212), base[:20]])
+    tree = _make(ctx, sc, n)
+    tree.insert(pts)
+    sp = orc.make_space(sc["metric"], sc["dim"], sc["weights"])
+    oi, od = orc.knn_brute(sp, pts, q, k)
+    for strategy in (tree.EXHAUSTIVE, tree.KDTREE):
+        tree.set_strategy(strategy)
+        gi, gd = tree.nearest_k(q, k)
+        assert np.array_equal(gi, oi), strategy
+        assert np.array_equal(gd, od)
+
+
 def test_device_buffers_async(ctx, orc):
     torch = pytest.importorskip("torch")
     import mpt_gb300 as m
