@@ -347,6 +347,48 @@ mptg_status mptg_autotune_wavefront(mptg_ctx* ctx, mptg_scene* scene, const mptg
 mptg_status mptg_plan_batch(mptg_ctx* ctx, const mptg_query* queries, size_t n, int concurrency,
                             mptg_result* out);
 
+/* ---- PPRM: parallel k-nearest probabilistic roadmap ------------------
+ * PPRM's Worker::addSample (src/mpt/impl/pprm/pprm.hpp:293-340) over
+ * wavefronts of `wavefront` uniform samples (the Philox stream of the PRRT
+ * planner, without goal samples).  Each valid sample q joins the roadmap in
+ * sample order: k = ceil((e + e/dim) ln(n + 1)) (at most 64) nearest of the n
+ * nodes before it, sorted by (distance, id); skipped when the nearest is
+ * closer than DBL_EPSILON; a goal node when within goal_radius of the goal;
+ * an edge (q, nbr, distance) for every neighbour with a valid link(q, nbr).
+ * Within a wavefront a sample's neighbours include the wavefront's earlier
+ * samples, so the roadmap equals the one-at-a-time roadmap of the same sample
+ * sequence.  Components are a union-find; solved when a start and a goal
+ * node share one.  Uses mptg_plan_params' goal_radius, edge_step,
+ * resolution, wavefront, seed and max_nodes. */
+typedef struct mptg_prm mptg_prm;
+/* Planner<Scenario, PPRM<...>>(scenario, seed) (pprm.hpp:141-149); lo/hi as mptg_planner_create */
+mptg_status mptg_prm_create(mptg_ctx* ctx, mptg_scene* scene, const mptg_plan_params* params, const double* lo,
+                            const double* hi, const double* goal, mptg_prm** prm);
+mptg_status mptg_prm_destroy(mptg_prm* prm);
+/* PPRM::addStart / addGoal (pprm.hpp:155-170): addSample with the start or
+ * goal flag; *id = the node id, or -1 when the state is invalid or a
+ * duplicate (the reference returns nullptr) */
+mptg_status mptg_prm_add_start(mptg_prm* prm, const double* q, int32_t* id);
+mptg_status mptg_prm_add_goal(mptg_prm* prm, const double* q, int32_t* id);
+/* PPRM::solve (pprm.hpp:173-183): wavefronts until max_wavefronts (<= 0: no
+ * limit), time_limit_s (<= 0: none), the node budget, or the first solution
+ * when stop_when_solved.  No start or no goal -> MPTG_ERR_NO_START (the
+ * reference throws "PPRM requires both start and goal configurations"). */
+mptg_status mptg_prm_run(mptg_prm* prm, int max_wavefronts, double time_limit_s, int stop_when_solved,
+                         int* solved);
+mptg_status mptg_prm_size(mptg_prm* prm, size_t* nodes, size_t* edges);
+/* states [n][dim] (may be NULL), and the undirected edges (from, to,
+ * distance), from > to, sorted by (from, to) (any may be NULL) */
+mptg_status mptg_prm_graph(mptg_prm* prm, double* states, size_t cap_nodes, int32_t* from, int32_t* to,
+                           double* dist, size_t cap_edges, size_t* n, size_t* ne);
+/* PPRM::solution() (pprm.hpp:232-243): Dijkstra from the start nodes to the
+ * nearest goal node over the edge distances; len states, start first (path
+ * may be NULL to query len and cost; cost = +inf and len = 0 when unsolved) */
+mptg_status mptg_prm_solution(mptg_prm* prm, double* path, size_t cap, size_t* len, double* cost);
+/* counters: [0] wavefronts, [1] samples, [2] valid samples, [3] duplicates
+ * skipped, [4] links checked, [5] edges, [6] goal nodes, [7] solved */
+mptg_status mptg_prm_stats(mptg_prm* prm, uint64_t out[8]);
+
 #ifdef __cplusplus
 }
 #endif

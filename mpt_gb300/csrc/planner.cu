@@ -16,7 +16,7 @@
 #include "metrics.cuh"
 #include "scene.cuh"
 #include "tree.cuh"
-#include "philox.cuh"
+#include "sampler.cuh"
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -154,31 +154,7 @@ __global__ void k_plan_sample(PlanView p, int W, uint32_t wave, const int* __res
         for (int d = 0; d < p.D; ++d) q[d] = p.goal[d];
         return;
     }
-    if (p.metric == MPTG_METRIC_SO3 || p.metric == MPTG_METRIC_SE3) {
-        // Shoemake's uniform rotation (src/mpt/impl/uniform_sampler_so3.hpp:55-68)
-        double a = phx_uniform(p.seed, (uint32_t)i, wave, 0);
-        double b = __dmul_rn(MPTG_TWO_PI, phx_uniform(p.seed, (uint32_t)i, wave, 1));
-        double c = __dmul_rn(MPTG_TWO_PI, phx_uniform(p.seed, (uint32_t)i, wave, 2));
-        double s1 = __dsqrt_rn(__dsub_rn(1.0, a)), s2 = __dsqrt_rn(a);
-        double sb, cb, sc, cc;
-        mptg_sincos(b, &sb, &cb);
-        mptg_sincos(c, &sc, &cc);
-        q[0] = __dmul_rn(s1, sb); q[1] = __dmul_rn(s1, cb); q[2] = __dmul_rn(s2, sc); q[3] = __dmul_rn(s2, cc);
-        for (int d = 4; d < p.D; ++d) {
-            double u = phx_uniform(p.seed, (uint32_t)i, wave, (uint32_t)(d - 1));
-            q[d] = __dadd_rn(p.lo[d], __dmul_rn(__dsub_rn(p.hi[d], p.lo[d]), u));
-        }
-    } else if (p.metric == MPTG_METRIC_SO2) {
-        // U[-pi, pi) per joint (src/mpt/impl/uniform_sampler_so2.hpp:57-64)
-        for (int d = 0; d < p.D; ++d)
-            q[d] = __dadd_rn(-MPTG_PI, __dmul_rn(MPTG_TWO_PI, phx_uniform(p.seed, (uint32_t)i, wave, (uint32_t)d)));
-    } else {
-        // uniform box (src/mpt/uniform_box_sampler.hpp:60-68)
-        for (int d = 0; d < p.D; ++d) {
-            double u = phx_uniform(p.seed, (uint32_t)i, wave, (uint32_t)d);
-            q[d] = __dadd_rn(p.lo[d], __dmul_rn(__dsub_rn(p.hi[d], p.lo[d]), u));
-        }
-    }
+    sample_uniform_state(p.metric, p.D, p.seed, (uint32_t)i, wave, p.lo, p.hi, q);
 }
 
 __global__ void k_plan_steer(PlanView p, int W, const double* __restrict__ samp, const int* __restrict__ nidx,

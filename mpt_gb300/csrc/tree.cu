@@ -20,6 +20,7 @@
 // midpoint split on the widest axis of the points), so the tree is exact and
 // complete after every insert.
 #include "metrics.cuh"
+#include "knn.cuh"
 #include <algorithm>
 #include <vector>
 
@@ -1008,9 +1009,6 @@ __global__ void __launch_bounds__(256) k_nearest_tiled_merge(TreeView t, const d
 // warp's sorted k-NN list: every point whose FP32 distance is within E of the
 // bound tau gets its FP64 distance, and those within tau join the list in
 // (distance, id) order, one at a time (the list lives two entries per lane).
-__device__ __forceinline__ void knn_insert(int lane, int k, double radius, bool cand, double dd, int pid, double& ld0,
-                                           double& ld1, int& li0, int& li1, int& cnt, double& tau, float& tauf);
-
 __device__ __forceinline__ void knn_consider(const TreeView& t, const double* __restrict__ qd, int lane, int k,
                                              double radius, bool have, int pid, float d32, float E, double& ld0,
                                              double& ld1, int& li0, int& li1, int& cnt, double& tau, float& tauf) {
@@ -1021,48 +1019,6 @@ __device__ __forceinline__ void knn_consider(const TreeView& t, const double* __
         cand = dd <= tau;
     }
     knn_insert(lane, k, radius, cand, dd, pid, ld0, ld1, li0, li1, cnt, tau, tauf);
-}
-
-// the lanes with cand set offer (dd, pid) to the list, lowest lane first
-__device__ __forceinline__ void knn_insert(int lane, int k, double radius, bool cand, double dd, int pid, double& ld0,
-                                           double& ld1, int& li0, int& li1, int& cnt, double& tau, float& tauf) {
-    unsigned cmask = __ballot_sync(0xffffffffu, cand);
-    while (cmask) {
-        int src = __ffs(cmask) - 1;
-        cmask &= cmask - 1;
-        double cd = __shfl_sync(0xffffffffu, dd, src);
-        int ci = __shfl_sync(0xffffffffu, pid, src);
-        // insert (cd, ci) into the sorted list if it ranks among the k best
-        if (cnt == k) {
-            double kd = (k - 1) < 32 ? __shfl_sync(0xffffffffu, ld0, k - 1) : __shfl_sync(0xffffffffu, ld1, k - 33);
-            int ki = (k - 1) < 32 ? __shfl_sync(0xffffffffu, li0, k - 1) : __shfl_sync(0xffffffffu, li1, k - 33);
-            if (!(cd < kd || (cd == kd && ci < ki))) continue;
-        }
-        // rank position = number of entries strictly ahead of (cd, ci)
-        bool ahead0 = lane < cnt && (ld0 < cd || (ld0 == cd && li0 < ci));
-        bool ahead1 = lane + 32 < cnt && (ld1 < cd || (ld1 == cd && li1 < ci));
-        int pos = __popc(__ballot_sync(0xffffffffu, ahead0)) + __popc(__ballot_sync(0xffffffffu, ahead1));
-        // shift entries at >= pos one place back
-        double p0d = __shfl_up_sync(0xffffffffu, ld0, 1);
-        int p0i = __shfl_up_sync(0xffffffffu, li0, 1);
-        double p1d = __shfl_up_sync(0xffffffffu, ld1, 1);
-        int p1i = __shfl_up_sync(0xffffffffu, li1, 1);
-        double last0d = __shfl_sync(0xffffffffu, ld0, 31);
-        int last0i = __shfl_sync(0xffffffffu, li0, 31);
-        if (lane == 0) { p1d = last0d; p1i = last0i; }
-        // slot 0 entries (index = lane)
-        if (lane > pos) { ld0 = p0d; li0 = p0i; }
-        else if (lane == pos) { ld0 = cd; li0 = ci; }
-        int j1 = lane + 32;
-        if (j1 > pos) { ld1 = p1d; li1 = p1i; }
-        else if (j1 == pos) { ld1 = cd; li1 = ci; }
-        if (cnt < k) ++cnt;
-        if (cnt == k) {
-            double kd = (k - 1) < 32 ? __shfl_sync(0xffffffffu, ld0, k - 1) : __shfl_sync(0xffffffffu, ld1, k - 33);
-            tau = fmin(kd, radius);
-            tauf = __double2float_ru(tau);
-        }
-    }
 }
 
 // FP32 twin of knn_insert for k_nearest_k_tiled's running list: the 64 best

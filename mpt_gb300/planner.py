@@ -78,6 +78,11 @@ class PRRTStar(PRRT):
     rewire = True
 
 
+class PPRM(PRRT):
+    """Option pack of PPRM (src/mpt/pprm.hpp:56-84): the parallel k-nearest
+    probabilistic roadmap (Planner(scenario, PPRM(...)) builds a PPRMPlanner)."""
+
+
 class GoalState:
     """GoalState(radius, state) (src/mpt/goal_state.hpp:43-90)."""
 
@@ -126,6 +131,15 @@ def _sig(L):
         ("mptg_planner_costs", ctypes.c_int, [P, P, S, ctypes.POINTER(S)]),
         ("mptg_autotune_wavefront", ctypes.c_int, [P, P, P, P, P, P, P, ctypes.c_double, P, ctypes.c_int,
                                                    ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_int), P]),
+        ("mptg_prm_create", ctypes.c_int, [P, P, P, P, P, P, ctypes.POINTER(P)]),
+        ("mptg_prm_destroy", ctypes.c_int, [P]),
+        ("mptg_prm_add_start", ctypes.c_int, [P, P, ctypes.POINTER(ctypes.c_int32)]),
+        ("mptg_prm_add_goal", ctypes.c_int, [P, P, ctypes.POINTER(ctypes.c_int32)]),
+        ("mptg_prm_run", ctypes.c_int, [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+        ("mptg_prm_size", ctypes.c_int, [P, ctypes.POINTER(S), ctypes.POINTER(S)]),
+        ("mptg_prm_graph", ctypes.c_int, [P, P, S, P, P, P, S, ctypes.POINTER(S), ctypes.POINTER(S)]),
+        ("mptg_prm_solution", ctypes.c_int, [P, P, S, ctypes.POINTER(S), ctypes.POINTER(ctypes.c_double)]),
+        ("mptg_prm_stats", ctypes.c_int, [P, P]),
     ]:
         f = getattr(L, name)
         f.restype = res
@@ -134,7 +148,13 @@ def _sig(L):
 
 
 class Planner:
-    """Planner<Scenario, PRRT<...>>(scenario, seed) on one GPU."""
+    """Planner<Scenario, PRRT<...>>(scenario, seed) on one GPU; with a PPRM
+    option pack the planner is a PPRMPlanner."""
+
+    def __new__(cls, scenario=None, algorithm=None, *args, **kwargs):
+        if cls is Planner and isinstance(algorithm, PPRM):
+            return super().__new__(PPRMPlanner)
+        return super().__new__(cls)
 
     def __init__(self, scenario: Scenario, algorithm: PRRT | None = None, seed: int | None = None,
                  ctx: Context | None = None, max_nodes: int = 1 << 20):
@@ -379,6 +399,145 @@ class Planner:
     getGoalBias = get_goal_bias
     setRewireFactor = set_rewire_factor
     getRewireFactor = get_rewire_factor
+    printStats = print_stats
+    visitGraph = visit_graph
+
+
+class PPRMPlanner(Planner):
+    """Planner<Scenario, PPRM<...>>(scenario, seed) (src/mpt/impl/pprm/pprm.hpp:141-250):
+    add_start / addStart, add_goal / addGoal, solve(done_fn), solve_for,
+    solve_until, solved, size, solution() (Dijkstra's shortest roadmap path,
+    pprm.hpp:230-240), print_stats and visit_graph (every node, then the far
+    end of each of its edges, pprm.hpp:381-388)."""
+
+    def __init__(self, scenario: Scenario, algorithm: PPRM | None = None, seed: int | None = None,
+                 ctx: Context | None = None, max_nodes: int = 1 << 20):
+        self.lib = load()
+        _sig(self.lib)
+        self.ctx = ctx or Context(0)
+        self.scenario = scenario
+        self.algorithm = algorithm or PPRM()
+        if seed is None:
+            seed = int.from_bytes(np.random.default_rng().bytes(8), "little")
+        self.seed = int(seed) & ((1 << 64) - 1)
+        self.max_nodes = int(max_nodes)
+        self.scene = Scene(self.ctx, scenario.desc)
+        prm = _Params()
+        prm.range = 0.0
+        prm.goal_bias = 0.0
+        prm.goal_radius = scenario.goal.radius
+        prm.edge_step = scenario.edge_step
+        prm.resolution = scenario.resolution
+        prm.wavefront = self.algorithm.wavefront
+        prm.seed = self.seed
+        prm.max_nodes = self.max_nodes
+        g = np.ascontiguousarray(scenario.goal.state, dtype=np.float64)
+        h = ctypes.c_void_p()
+        _check(self.ctx.h, self.lib.mptg_prm_create(self.ctx.h, self.scene.h, ctypes.byref(prm),
+                                                    scenario.lo.ctypes.data, scenario.hi.ctypes.data, g.ctypes.data,
+                                                    ctypes.byref(h)))
+        self.h = h
+        self.last_cost = math.inf
+
+    def add_start(self, q) -> int:
+        """addSample with the start flag: the node id, or -1 (invalid or duplicate)."""
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        i = ctypes.c_int32(-1)
+        _check(self.ctx.h, self.lib.mptg_prm_add_start(self.h, q.ctypes.data, ctypes.byref(i)))
+        return i.value
+
+    def add_goal(self, q) -> int:
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        i = ctypes.c_int32(-1)
+        _check(self.ctx.h, self.lib.mptg_prm_add_goal(self.h, q.ctypes.data, ctypes.byref(i)))
+        return i.value
+
+    def run(self, max_wavefronts: int = 1, time_limit: float = 0.0, stop_when_solved: bool = False) -> bool:
+        solved = ctypes.c_int(0)
+        _check(self.ctx.h, self.lib.mptg_prm_run(self.h, int(max_wavefronts), float(time_limit),
+                                                 int(stop_when_solved), ctypes.byref(solved)))
+        return bool(solved.value)
+
+    def solve(self, done_fn):
+        """Runs wavefronts until done_fn() is true (polled between wavefronts)."""
+        while not done_fn():
+            before = self.stats()["wavefronts"]
+            self.run(1)
+            if self.stats()["wavefronts"] == before:  # node budget exhausted
+                break
+
+    def solved(self) -> bool:
+        return bool(self.stats()["solved"])
+
+    def size(self) -> int:
+        n = ctypes.c_size_t()
+        _check(self.ctx.h, self.lib.mptg_prm_size(self.h, ctypes.byref(n), None))
+        return n.value
+
+    def edges(self) -> int:
+        e = ctypes.c_size_t()
+        _check(self.ctx.h, self.lib.mptg_prm_size(self.h, None, ctypes.byref(e)))
+        return e.value
+
+    def solution(self, fn=None):
+        n = ctypes.c_size_t()
+        cost = ctypes.c_double()
+        _check(self.ctx.h, self.lib.mptg_prm_solution(self.h, None, 0, ctypes.byref(n), ctypes.byref(cost)))
+        path = np.empty((n.value, self.scene.dim), dtype=np.float64)
+        if n.value:
+            _check(self.ctx.h, self.lib.mptg_prm_solution(self.h, path.ctypes.data, n.value, ctypes.byref(n),
+                                                          ctypes.byref(cost)))
+        self.last_cost = cost.value
+        if fn is None:
+            return [p for p in path]
+        for p in path:
+            fn(p)
+        return None
+
+    def graph(self):
+        """(states [n][dim], (from, to, distance)) with from > to, sorted by (from, to)."""
+        n, ne = ctypes.c_size_t(), ctypes.c_size_t()
+        _check(self.ctx.h, self.lib.mptg_prm_size(self.h, ctypes.byref(n), ctypes.byref(ne)))
+        states = np.empty((n.value, self.scene.dim), dtype=np.float64)
+        ef = np.empty(ne.value, dtype=np.int32)
+        et = np.empty(ne.value, dtype=np.int32)
+        ed = np.empty(ne.value, dtype=np.float64)
+        _check(self.ctx.h, self.lib.mptg_prm_graph(self.h, states.ctypes.data, n.value, ef.ctypes.data,
+                                                   et.ctypes.data, ed.ctypes.data, ne.value, ctypes.byref(n),
+                                                   ctypes.byref(ne)))
+        return states, (ef, et, ed)
+
+    def visit_graph(self, visitor):
+        states, (ef, et, _) = self.graph()
+        adj = [[] for _ in range(len(states))]
+        for a, b in zip(ef.tolist(), et.tolist()):
+            adj[a].append(b)
+            adj[b].append(a)
+        for i in range(len(states)):
+            visitor.vertex(states[i])
+            for j in adj[i]:
+                visitor.edge(states[j])
+
+    def stats(self) -> dict:
+        out = (ctypes.c_uint64 * 8)()
+        _check(self.ctx.h, self.lib.mptg_prm_stats(self.h, out))
+        keys = ["wavefronts", "samples", "valid_samples", "duplicates", "links_checked", "edges", "goal_nodes",
+                "solved"]
+        return dict(zip(keys, [int(v) for v in out]))
+
+    def print_stats(self):
+        print("nodes in graph: %d" % self.size())
+        if self.algorithm.report_stats:
+            for k, v in self.stats().items():
+                print("%s: %d" % (k, v))
+
+    def close(self):
+        if self.h is not None:
+            self.lib.mptg_prm_destroy(self.h)
+            self.h = None
+
+    addStart = add_start
+    addGoal = add_goal
     printStats = print_stats
     visitGraph = visit_graph
 

@@ -302,6 +302,68 @@ def plan_star(desc: dict, space: Space, params: dict, lo, hi, start, goal, max_w
     return states[:n].copy(), parents[:n].copy(), costs[:n].copy(), goals[:ng.value].copy(), nrw.value
 
 
+def prm(desc: dict, space: Space, params: dict, lo, hi, goal, starts, goals, max_waves: int,
+        stop_when_solved: bool = False, edge_cap: int = 1 << 22):
+    """Replay of the wavefront PPRM roadmap: dict(states, flags, edges (from, to,
+    dist) sorted by (from, to), stats[8], path node ids, cost)."""
+    L = lib()
+    if not getattr(L, "_prm_sig", False):
+        P = ctypes.c_void_p
+        L.orc_prm.restype = ctypes.c_int64
+        L.orc_prm.argtypes = [P, P, P, P, P, P, P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P,
+                              P, P, P, P, ctypes.c_int64, P]
+        L.orc_prm_dijkstra.restype = ctypes.c_int64
+        L.orc_prm_dijkstra.argtypes = [ctypes.c_int64, P, ctypes.c_int64, P, P, P, P, P]
+        L.orc_prm_k.restype = ctypes.c_int
+        L.orc_prm_k.argtypes = [ctypes.c_int64, ctypes.c_int]
+        L._prm_sig = True
+    sc, keep = make_scene(desc)
+    pp = PlanParams()
+    pp.range = 0.0
+    pp.goal_bias = 0.0
+    pp.goal_radius = float(params["goal_radius"])
+    pp.edge_step = float(params["edge_step"])
+    pp.resolution = int(params["resolution"])
+    pp.wavefront = int(params["wavefront"])
+    pp.seed = int(params["seed"])
+    pp.max_nodes = int(params["max_nodes"])
+    D = space.dim
+    f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    lo, hi = f64(lo), f64(hi)
+    g = None if goal is None else f64(goal)
+    S = f64(starts).reshape(-1, D)
+    G = f64(goals).reshape(-1, D)
+    states = np.empty((pp.max_nodes, D), dtype=np.float64)
+    flags = np.empty(pp.max_nodes, dtype=np.uint8)
+    ef = np.empty(edge_cap, dtype=np.int32)
+    et = np.empty(edge_cap, dtype=np.int32)
+    ed = np.empty(edge_cap, dtype=np.float64)
+    ne = ctypes.c_int64(0)
+    stats = np.zeros(8, dtype=np.int64)
+    n = L.orc_prm(ctypes.byref(sc), ctypes.byref(space), ctypes.byref(pp), _ptr(lo), _ptr(hi),
+                  None if g is None else _ptr(g), _ptr(S), len(S), _ptr(G), len(G), int(max_waves),
+                  int(stop_when_solved), _ptr(states), _ptr(flags), ctypes.byref(ne), _ptr(ef), _ptr(et), _ptr(ed),
+                  edge_cap, _ptr(stats))
+    del keep
+    m = ne.value
+    assert m <= edge_cap, "edge_cap too small"
+    order = np.lexsort((et[:m], ef[:m]))
+    ef, et, ed = ef[:m][order].copy(), et[:m][order].copy(), ed[:m][order].copy()
+    path = np.empty(max(n, 1), dtype=np.int32)
+    cost = ctypes.c_double(0.0)
+    plen = L.orc_prm_dijkstra(n, _ptr(flags), m, _ptr(ef), _ptr(et), _ptr(ed), _ptr(path), ctypes.byref(cost))
+    return {"states": states[:n].copy(), "flags": flags[:n].copy(), "edges": (ef, et, ed), "stats": stats,
+            "path": path[:plen].copy(), "cost": cost.value}
+
+
+def prm_k(n: int, dim: int) -> int:
+    """k of the PPRM neighbourhood for a roadmap of n nodes."""
+    L = lib()
+    L.orc_prm_k.restype = ctypes.c_int
+    L.orc_prm_k.argtypes = [ctypes.c_int64, ctypes.c_int]
+    return int(L.orc_prm_k(int(n), int(dim)))
+
+
 def uniform(seed: int, i: int, w: int, j: int) -> float:
     lib()
     if not getattr(_lib, "_plan_sig", False):

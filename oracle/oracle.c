@@ -1040,3 +1040,206 @@ int64_t orc_plan_star(const orc_scene* sc, const orc_space* sp, const orc_plan_p
     *rewires = nrw;
     return n;
 }
+
+/* ------------------------------------------------------------------ */
+/* PPRM roadmap: the worker's addSample of src/mpt/impl/pprm/pprm.hpp:298-339
+ * applied one sample at a time, in the sample order of the wavefront
+ * planner's stream (no goal samples):
+ *   valid(q) (:299-300); k = ceil((e + e/dim) ln(n + 1)) (:302-303, kRRG_ of
+ *   :145; at most 64 and n) nearest of the n nodes by (distance, id); skip
+ *   when the nearest is closer than DBL_EPSILON (:306-308); goal flag from the
+ *   caller or GoalState(radius) (:312-316); for each neighbour in order, an
+ *   edge (q, nbr, d) when link(q, nbr) is valid (:325-334) and a union of the
+ *   components (:341-363, whose flags OR together); solved once a union
+ *   leaves a component holding a start and a goal (:332-333, component.hpp
+ *   isSolution).  The roadmap is then a pure function of the sample
+ *   sequence, which is what the wavefront GPU planner reproduces. */
+static int32_t uf_root(int32_t* uf, int32_t x) {
+    while (uf[x] != x) { uf[x] = uf[uf[x]]; x = uf[x]; }
+    return x;
+}
+
+int orc_prm_k(int64_t n, int dim) {
+    if (n <= 0) return 0;
+    const double e = 2.718281828459045, kRRG = e + e / dim;
+    double kd = ceil(kRRG * log((double)n + 1.0));
+    int k = kd > 64.0 ? 64 : (int)kd;
+    if (k > n) k = (int)n;
+    return k < 1 ? 1 : k;
+}
+
+typedef struct {
+    const orc_scene* sc; const orc_space* sp; const orc_plan_params* pp; const double* goal;
+    double* states; uint8_t* flags; int32_t* uf; uint8_t* cflag; int64_t n;
+    int32_t* efrom; int32_t* eto; double* edist; int64_t ne, ecap;
+    int64_t* stats; double* kd; int32_t* ki;
+} prm_state;
+
+static int32_t prm_add(prm_state* P, const double* q, int flag) {
+    const int D = P->sp->dim;
+    P->stats[1]++;
+    if (!state_valid(P->sc, q)) return -1;
+    P->stats[2]++;
+    const int64_t n = P->n;
+    const int k = orc_prm_k(n, D);
+    int cnt = 0;
+    for (int64_t j = 0; j < n; ++j) {
+        double dj = orc_distance(P->sp, q, P->states + j * D);
+        if (!(dj == dj)) continue;
+        if (cnt == k) {
+            if (!(dj < P->kd[k - 1])) continue; /* ids ascend: a tie keeps the earlier id */
+            cnt--;
+        }
+        int pos = cnt;
+        while (pos > 0 && P->kd[pos - 1] > dj) { P->kd[pos] = P->kd[pos - 1]; P->ki[pos] = P->ki[pos - 1]; --pos; }
+        P->kd[pos] = dj;
+        P->ki[pos] = (int32_t)j;
+        cnt++;
+    }
+    if (cnt > 0 && P->kd[0] < DBL_EPSILON) { P->stats[3]++; return -1; }
+    if (n >= P->pp->max_nodes) return -1;
+    int isgoal = (flag & 2) || (P->goal && orc_distance(P->sp, q, P->goal) <= P->pp->goal_radius);
+    uint8_t f = (uint8_t)(flag | (isgoal ? 2 : 0));
+    for (int d = 0; d < D; ++d) P->states[n * D + d] = q[d];
+    P->flags[n] = f;
+    P->uf[n] = (int32_t)n;
+    P->cflag[n] = f;
+    P->n = n + 1;
+    if (isgoal) P->stats[6]++;
+    const double inv = 1.0 / P->pp->edge_step;
+    for (int t = 0; t < cnt; ++t) {
+        const int32_t nb = P->ki[t];
+        P->stats[4]++;
+        if (!dmv_edge(P->sc, P->sp, q, P->states + (int64_t)nb * D, inv, P->pp->resolution, NULL)) continue;
+        if (P->ne < P->ecap) {
+            P->efrom[P->ne] = (int32_t)n; P->eto[P->ne] = nb; P->edist[P->ne] = P->kd[t];
+        }
+        P->ne++;
+        int32_t a = uf_root(P->uf, (int32_t)n), b = uf_root(P->uf, nb);
+        if (a != b) {
+            if (a > b) { int32_t x = a; a = b; b = x; }
+            P->uf[b] = a;
+            P->cflag[a] |= P->cflag[b];
+        }
+        if (P->cflag[a] == 3) P->stats[7] = 1;
+    }
+    return (int32_t)n;
+}
+
+static int edge_cmp(const void* x, const void* y) {
+    const int64_t* a = (const int64_t*)x; const int64_t* b = (const int64_t*)y;
+    return a[0] < b[0] ? -1 : (a[0] > b[0] ? 1 : 0);
+}
+
+/* Dijkstra from the start nodes (distance 0, in id order) to the first goal
+ * node settled; heap order (distance, id); adjacency in (from, to) edge order,
+ * each edge listed at both ends; a node's predecessor changes only on a strict
+ * improvement.  Returns the path length (0 when no goal is reachable). */
+int64_t orc_prm_dijkstra(int64_t n, const uint8_t* flags, int64_t ne, const int32_t* efrom, const int32_t* eto,
+                         const double* edist, int32_t* path, double* cost) {
+    int64_t* key = (int64_t*)malloc((size_t)(ne > 0 ? ne : 1) * 2 * sizeof(int64_t));
+    for (int64_t e = 0; e < ne; ++e) { key[2 * e] = ((int64_t)efrom[e] << 32) | (uint32_t)eto[e]; key[2 * e + 1] = e; }
+    qsort(key, (size_t)ne, 2 * sizeof(int64_t), edge_cmp);
+    int64_t* deg = (int64_t*)calloc((size_t)n + 1, sizeof(int64_t));
+    for (int64_t e = 0; e < ne; ++e) { deg[efrom[e] + 1]++; deg[eto[e] + 1]++; }
+    for (int64_t v = 0; v < n; ++v) deg[v + 1] += deg[v];
+    int64_t* fill = (int64_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
+    memcpy(fill, deg, (size_t)n * sizeof(int64_t));
+    int32_t* adj = (int32_t*)malloc((size_t)(2 * ne > 0 ? 2 * ne : 1) * sizeof(int32_t));
+    double* adjw = (double*)malloc((size_t)(2 * ne > 0 ? 2 * ne : 1) * sizeof(double));
+    for (int64_t s = 0; s < ne; ++s) {
+        int64_t e = key[2 * s + 1];
+        int32_t a = efrom[e], b = eto[e];
+        adj[fill[a]] = b; adjw[fill[a]++] = edist[e];
+        adj[fill[b]] = a; adjw[fill[b]++] = edist[e];
+    }
+    double* dist = (double*)malloc((size_t)(n > 0 ? n : 1) * sizeof(double));
+    int32_t* pred = (int32_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int32_t));
+    uint8_t* done = (uint8_t*)calloc((size_t)n + 1, 1);
+    /* binary heap of (dist, id), lazy deletion */
+    int64_t hcap = 2 * ne + n + 1, hn = 0;
+    double* hd = (double*)malloc((size_t)hcap * sizeof(double));
+    int32_t* hi = (int32_t*)malloc((size_t)hcap * sizeof(int32_t));
+#define HLESS(i, j) (hd[i] < hd[j] || (hd[i] == hd[j] && hi[i] < hi[j]))
+#define HSWAP(i, j) do { double td = hd[i]; hd[i] = hd[j]; hd[j] = td; int32_t ti = hi[i]; hi[i] = hi[j]; hi[j] = ti; } while (0)
+    for (int64_t v = 0; v < n; ++v) { dist[v] = INFINITY; pred[v] = -1; }
+    for (int64_t v = 0; v < n; ++v)
+        if (flags[v] & 1) {
+            dist[v] = 0.0;
+            int64_t c = hn++; hd[c] = 0.0; hi[c] = (int32_t)v;
+            while (c > 0 && HLESS(c, (c - 1) / 2)) { HSWAP(c, (c - 1) / 2); c = (c - 1) / 2; }
+        }
+    int32_t found = -1;
+    while (hn > 0) {
+        double du = hd[0]; int32_t u = hi[0];
+        hn--; hd[0] = hd[hn]; hi[0] = hi[hn];
+        for (int64_t c = 0;;) {
+            int64_t l = 2 * c + 1, r = l + 1, m = c;
+            if (l < hn && HLESS(l, m)) m = l;
+            if (r < hn && HLESS(r, m)) m = r;
+            if (m == c) break;
+            HSWAP(c, m); c = m;
+        }
+        if (done[u] || du != dist[u]) continue;
+        done[u] = 1;
+        if (flags[u] & 2) { found = u; break; }
+        for (int64_t t = deg[u]; t < deg[u + 1]; ++t) {
+            int32_t v = adj[t];
+            double nd = du + adjw[t];
+            if (nd < dist[v]) {
+                dist[v] = nd; pred[v] = u;
+                int64_t c = hn++; hd[c] = nd; hi[c] = v;
+                while (c > 0 && HLESS(c, (c - 1) / 2)) { HSWAP(c, (c - 1) / 2); c = (c - 1) / 2; }
+            }
+        }
+    }
+#undef HLESS
+#undef HSWAP
+    int64_t len = 0;
+    *cost = INFINITY;
+    if (found >= 0) {
+        *cost = dist[found];
+        for (int32_t v = found; v >= 0; v = pred[v]) len++;
+        if (path) {
+            int64_t i = len;
+            for (int32_t v = found; v >= 0; v = pred[v]) path[--i] = v;
+        }
+    }
+    free(key); free(deg); free(fill); free(adj); free(adjw); free(dist); free(pred); free(done); free(hd); free(hi);
+    return len;
+}
+
+int64_t orc_prm(const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp, const double* lo,
+                const double* hi, const double* goal, const double* starts, int nstarts, const double* goals,
+                int ngoals, int max_waves, int stop_when_solved, double* states, uint8_t* flags, int64_t* ne,
+                int32_t* efrom, int32_t* eto, double* edist, int64_t ecap, int64_t* stats) {
+    const int D = sp->dim, W = pp->wavefront;
+    if (sc->kind == 2) get_env_bvh(sc);
+    prm_state P;
+    memset(&P, 0, sizeof(P));
+    P.sc = sc; P.sp = sp; P.pp = pp; P.goal = goal;
+    P.states = states; P.flags = flags;
+    P.uf = (int32_t*)malloc((size_t)pp->max_nodes * sizeof(int32_t));
+    P.cflag = (uint8_t*)malloc((size_t)pp->max_nodes);
+    P.efrom = efrom; P.eto = eto; P.edist = edist; P.ecap = ecap;
+    P.stats = stats;
+    P.kd = (double*)malloc(64 * sizeof(double));
+    P.ki = (int32_t*)malloc(64 * sizeof(int32_t));
+    for (int i = 0; i < 8; ++i) stats[i] = 0;
+    for (int i = 0; i < nstarts; ++i) prm_add(&P, starts + (size_t)i * D, 1);
+    for (int i = 0; i < ngoals; ++i) prm_add(&P, goals + (size_t)i * D, 2);
+    double* q = (double*)malloc((size_t)D * sizeof(double));
+    for (int w = 0; w < max_waves; ++w) {
+        if (stop_when_solved && stats[7]) break;
+        if (P.n >= pp->max_nodes) break;
+        for (int i = 0; i < W; ++i) {
+            plan_sample(sp, pp, lo, hi, NULL, -1, (uint32_t)i, (uint32_t)w, q);
+            prm_add(&P, q, 0);
+        }
+        stats[0]++;
+    }
+    stats[5] = P.ne;
+    *ne = P.ne;
+    free(q); free(P.uf); free(P.cflag); free(P.kd); free(P.ki);
+    return P.n;
+}

@@ -78,6 +78,19 @@ int64_t orc_plan_star(const orc_scene* sc, const orc_space* sp, const orc_plan_p
                       double rewire_factor, double* states, int32_t* parents, double* costs, int32_t* goals,
                       int64_t* ngoals, int64_t* rewires, int nthreads);
 
+/* Replay of the wavefront PPRM roadmap (see orc_prm in oracle.c): starts,
+ * then goals, then max_waves wavefronts of the sample stream, one sample at a
+ * time.  Returns the node count; edges (from = new node > to) in insertion
+ * order up to ecap (*ne = all); stats as mptg_prm_stats. */
+int orc_prm_k(int64_t n, int dim);
+int64_t orc_prm(const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp, const double* lo,
+                const double* hi, const double* goal, const double* starts, int nstarts, const double* goals,
+                int ngoals, int max_waves, int stop_when_solved, double* states, uint8_t* flags, int64_t* ne,
+                int32_t* efrom, int32_t* eto, double* edist, int64_t ecap, int64_t* stats);
+/* Dijkstra over a roadmap (start flag 1, goal flag 2); path = node ids */
+int64_t orc_prm_dijkstra(int64_t n, const uint8_t* flags, int64_t ne, const int32_t* efrom, const int32_t* eto,
+                         const double* edist, int32_t* path, double* cost);
+
 /* Triangle-triangle intersection (FP64 orientation predicates). */
 int orc_tri_tri(const double* t1, const double* t2);
 
