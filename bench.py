@@ -299,6 +299,70 @@ def prrt_star_section(ctx, wave_for=None, refine_s=1.0, seeds=3):
     return out
 
 
+def prm_section(ctx, seeds=3, cap_s=20.0):
+    """PPRM (k-nearest roadmap) per scene: p50 time to the first solution and
+    the path cost, and the roadmap build rate against the oracle's
+    one-sample-at-a-time replay (one core) on the same sample stream, with the
+    two roadmaps compared edge for edge."""
+    import oracle
+    from mpt_gb300 import planner as P
+    from mpt_gb300 import scenes
+    out = {}
+    for name, mk, W, cmp_waves in [("grid_1024", scenes.grid_scene, 1024, 8), ("arm_10link", scenes.arm_scene, 4096, 2),
+                                   ("se3_mesh", scenes.mesh_scene, 1024, 2)]:
+        sc = mk()
+        times, costs, nodes, edges, links = [], [], [], [], []
+        for s in range(seeds):
+            pl = P.Planner(P.Scenario(sc), P.PPRM(P.gpu_wavefront(W)), seed=3000 + s, ctx=ctx, max_nodes=1 << 21)
+            t0 = time.perf_counter()
+            pl.add_start(sc["start"])
+            pl.add_goal(sc["goal"])
+            pl.solve_for(cap_s, lambda: pl.solved())
+            dt = time.perf_counter() - t0
+            if pl.solved():
+                times.append(dt)
+                pl.solution()
+                costs.append(pl.last_cost)
+            st = pl.stats()
+            nodes.append(pl.size())
+            edges.append(st["edges"])
+            links.append(st["links_checked"] / dt)
+            pl.close()
+        # build rate on the same sample prefix: GPU planner vs oracle replay
+        pl = P.Planner(P.Scenario(sc), P.PPRM(P.gpu_wavefront(W)), seed=76, ctx=ctx, max_nodes=1 << 21)
+        pl.add_start(sc["start"])
+        pl.add_goal(sc["goal"])
+        pl.run(1)  # warm-up
+        pl.close()
+        pl = P.Planner(P.Scenario(sc), P.PPRM(P.gpu_wavefront(W)), seed=77, ctx=ctx, max_nodes=1 << 21)
+        t0 = time.perf_counter()
+        pl.add_start(sc["start"])
+        pl.add_goal(sc["goal"])
+        pl.run(cmp_waves)
+        gpu_s = time.perf_counter() - t0
+        _, (gf, gt, gd) = pl.graph()
+        n_gpu = pl.size()
+        pl.close()
+        sp = oracle.make_space(sc["metric"], sc["dim"], sc["weights"])
+        params = {"goal_radius": sc["goal_radius"], "edge_step": sc["edge_step"], "resolution": sc["resolution"],
+                  "wavefront": W, "seed": 77, "max_nodes": 1 << 21}
+        oracle.prm(sc, sp, params, sc["lo"], sc["hi"], sc["goal"], sc["start"], sc["goal"], 1)
+        t0 = time.perf_counter()
+        ref = oracle.prm(sc, sp, params, sc["lo"], sc["hi"], sc["goal"], sc["start"], sc["goal"], cmp_waves)
+        cpu_s = time.perf_counter() - t0
+        rf, rt, rd = ref["edges"]
+        out[name] = {"wavefront": W, "solved": len(times), "seeds": seeds,
+                     "p50_first_solution_s": statistics.median(times) if times else None,
+                     "median_path_cost": statistics.median(costs) if costs else None,
+                     "median_nodes": statistics.median(nodes), "median_edges": statistics.median(edges),
+                     "median_links_checked_per_s": statistics.median(links),
+                     "build": {"samples": cmp_waves * W, "gpu_samples_per_s": cmp_waves * W / gpu_s,
+                               "cpu_oracle_samples_per_s": cmp_waves * W / cpu_s, "cpu_cores": 1,
+                               "roadmap_equal": bool(n_gpu == len(ref["states"]) and np.array_equal(gf, rf)
+                                                     and np.array_equal(gt, rt) and np.array_equal(gd, rd))}}
+    return out
+
+
 def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0, wave_for=None):
     """Config of the serving benchmark: n queries uniform over the three scenes,
     start and goal rejection-sampled valid, node budgets log-uniform in
@@ -413,12 +477,14 @@ def run_gpu(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     ctx = m.Context(local)
-    if args.edges_only or args.solve_only or args.star_only:
+    if args.edges_only or args.solve_only or args.star_only or args.prm_only:
         # profiling modes: one secondary section alone
         if args.edges_only:
             out = {"edge_checks": edge_rates(ctx, m, torch.cuda.current_stream(), torch)}
         elif args.star_only:
             out = {"prrt_star": prrt_star_section(ctx)}
+        elif args.prm_only:
+            out = {"pprm": prm_section(ctx)}
         else:
             out = {"time_to_solve": solve_times(ctx, seeds=args.solve_seeds)}
         out["gpu_launches"] = ctx.kernel_launches()
@@ -527,6 +593,7 @@ def run_gpu(args):
                     "mesh": solves["se3_mesh"]["autotune"]["best"]}
     serving = batch_serving(m, ctx, wave_for=wave_for) if not (args.no_solve or args.no_batch) else None
     star = prrt_star_section(ctx, wave_for) if not (args.no_solve or args.no_star) else None
+    prm = prm_section(ctx) if not (args.no_solve or args.no_prm) else None
 
     # CPU baselines: oracle kd-tree and DMV on the host cores, bounded samples
     cpu = None
@@ -579,6 +646,7 @@ def run_gpu(args):
                 "learned_surrogate_se3": learned,
                 "batch_serving": serving,
                 "prrt_star": star,
+                "pprm": prm,
                 "clocks": clk.summary(), "gpu_launches": launches, "tree_build_s": build_s,
                 "wall_s_timed": wall}
         print(json.dumps(line))
@@ -599,6 +667,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched serving run")
     ap.add_argument("--no-star", action="store_true", help="skip the PRRT* comparison")
     ap.add_argument("--star-only", action="store_true", help="the PRRT* comparison only (profiling)")
+    ap.add_argument("--no-prm", action="store_true", help="skip the PPRM roadmap run")
+    ap.add_argument("--prm-only", action="store_true", help="the PPRM roadmap run only (profiling)")
     ap.add_argument("--edges-only", action="store_true", help="edge checks/s of the three scenes only (profiling)")
     ap.add_argument("--solve-only", action="store_true", help="time to solve of the three scenes only (profiling)")
     ap.add_argument("--solve-seeds", type=int, default=5)

@@ -358,4 +358,170 @@ public:
     double getRewireFactor() const { return this->rewireFactor_; }
 };
 
+// Planner<Scenario, PPRM<Options...>> (src/mpt/pprm.hpp:56-84,
+// src/mpt/impl/pprm/pprm.hpp:141-250): the k-nearest roadmap over wavefronts.
+// addStart / addGoal run addSample at once (invalid or duplicate states are
+// dropped, as the reference's nullptr); solve needs both.
+template <class... Options> struct PPRM : PRRT<Options...> {};
+
+template <class Scenario, class... Options>
+class Planner<Scenario, PPRM<Options...>> {
+    static_assert(impl::has_gpu_scene<Scenario>::value,
+                  "the Scenario must describe its collision world with gpu_scene() "
+                  "(GridScene, PlanarArmScene or RigidMeshScene): no CPU fallback exists");
+    using Algo = PPRM<Options...>;
+
+public:
+    using State = typename Scenario::State;
+
+private:
+    Scenario scenario_;
+    mptg_ctx* ctx_ = nullptr;
+    mptg_scene* scene_ = nullptr;
+    mptg_prm* prm_ = nullptr;
+    int dim_ = 0;
+
+    uint64_t stat(int i) const {
+        uint64_t st[8];
+        impl::check(ctx_, mptg_prm_stats(prm_, st));
+        return st[i];
+    }
+
+public:
+    explicit Planner(const Scenario& scenario = Scenario(), uint64_t seed = std::random_device{}(),
+                     size_t maxNodes = size_t(1) << 21, int device = 0)
+        : scenario_(scenario) {
+        if (mptg_create(&ctx_, device) != MPTG_OK) throw std::runtime_error("mptg: no usable GPU");
+        auto d = impl::desc_of(scenario_.gpu_scene());
+        impl::check(ctx_, mptg_scene_create(ctx_, &d, &scene_));
+        double w[2];
+        impl::check(ctx_, mptg_scene_space(scene_, &dim_, nullptr, w));
+        mptg_plan_params p{};
+        auto goal = scenario_.goal();
+        p.goal_radius = goal.radius;
+        p.edge_step = 1.0;
+        if constexpr (impl::has_link_step<Scenario>::value) p.edge_step = scenario_.link_step();
+        p.resolution = 0;
+        if constexpr (impl::has_link_resolution<Scenario>::value) p.resolution = scenario_.link_resolution();
+        p.wavefront = Algo::wavefront;
+        p.seed = seed;
+        p.max_nodes = maxNodes;
+        const double* lo = nullptr;
+        const double* hi = nullptr;
+        std::pair<State, State> b;
+        if constexpr (impl::has_bounds<Scenario>::value) {
+            b = scenario_.bounds();
+            lo = impl::data(b.first);
+            hi = impl::data(b.second);
+        }
+        impl::check(ctx_, mptg_prm_create(ctx_, scene_, &p, lo, hi, impl::data(goal.state), &prm_));
+    }
+    Planner(const Planner&) = delete;
+    Planner& operator=(const Planner&) = delete;
+    ~Planner() {
+        if (prm_) mptg_prm_destroy(prm_);
+        if (scene_) mptg_scene_destroy(scene_);
+        if (ctx_) mptg_destroy(ctx_);
+    }
+
+    void addStart(const State& q) {  // pprm.hpp:157-165
+        int32_t id;
+        impl::check(ctx_, mptg_prm_add_start(prm_, impl::data(q), &id));
+    }
+    void addGoal(const State& q) {  // pprm.hpp:167-170
+        int32_t id;
+        impl::check(ctx_, mptg_prm_add_goal(prm_, impl::data(q), &id));
+    }
+
+    std::size_t size() const {
+        size_t n = 0;
+        impl::check(ctx_, mptg_prm_size(prm_, &n, nullptr));
+        return n;
+    }
+    bool solved() const { return stat(7) != 0; }
+
+    // pprm.hpp:173-183: doneFn is polled between wavefronts
+    template <class DoneFn>
+    void solve(DoneFn done) {
+        while (!done()) {
+            const uint64_t before = stat(0);
+            int s = 0;
+            impl::check(ctx_, mptg_prm_run(prm_, 1, 0.0, 0, &s));
+            if (stat(0) == before) break;  // node budget reached
+        }
+    }
+    template <class Rep, class Period>
+    void solveFor(const std::chrono::duration<Rep, Period>& d) {
+        auto end = std::chrono::steady_clock::now() + d;
+        solve([&] { return std::chrono::steady_clock::now() >= end; });
+    }
+    template <class DoneFn, class Rep, class Period>
+    void solveFor(DoneFn done, const std::chrono::duration<Rep, Period>& d) {
+        auto end = std::chrono::steady_clock::now() + d;
+        solve([&] { return std::chrono::steady_clock::now() >= end || done(); });
+    }
+    template <class Clock, class Duration>
+    void solveUntil(const std::chrono::time_point<Clock, Duration>& t) {
+        solve([&] { return Clock::now() >= t; });
+    }
+    template <class DoneFn, class Clock, class Duration>
+    void solveUntil(DoneFn done, const std::chrono::time_point<Clock, Duration>& t) {
+        solve([&] { return Clock::now() >= t || done(); });
+    }
+
+    // pprm.hpp:230-240: the shortest roadmap path from a start to a goal node
+    std::vector<State> solution() const {
+        std::vector<State> path;
+        size_t len = 0;
+        double cost = 0;
+        impl::check(ctx_, mptg_prm_solution(prm_, nullptr, 0, &len, &cost));
+        if (!len) return path;
+        std::vector<double> buf(len * dim_);
+        impl::check(ctx_, mptg_prm_solution(prm_, buf.data(), len, &len, &cost));
+        path.resize(len);
+        for (size_t i = 0; i < len; ++i)
+            for (int d = 0; d < dim_; ++d) path[i][d] = buf[i * dim_ + d];
+        return path;
+    }
+    template <class Fn>
+    void solution(Fn fn) const {
+        for (const State& q : solution()) fn(q);
+    }
+
+    // pprm.hpp:381-388: every node, then the far end of each of its edges
+    template <class Visitor>
+    void visitGraph(Visitor&& visitor) const {
+        size_t n = 0, ne = 0;
+        impl::check(ctx_, mptg_prm_size(prm_, &n, &ne));
+        std::vector<double> st(n * dim_);
+        std::vector<int32_t> ef(ne), et(ne);
+        impl::check(ctx_, mptg_prm_graph(prm_, st.data(), n, ef.data(), et.data(), nullptr, ne, &n, &ne));
+        std::vector<std::vector<int32_t>> adj(n);
+        for (size_t e = 0; e < ne; ++e) {
+            adj[ef[e]].push_back(et[e]);
+            adj[et[e]].push_back(ef[e]);
+        }
+        State q, p;
+        for (size_t i = 0; i < n; ++i) {
+            for (int d = 0; d < dim_; ++d) q[d] = st[i * dim_ + d];
+            visitor.vertex(q);
+            for (int32_t j : adj[i]) {
+                for (int d = 0; d < dim_; ++d) p[d] = st[(size_t)j * dim_ + d];
+                visitor.edge(p);
+            }
+        }
+    }
+
+    void printStats() const {  // pprm.hpp:242-245
+        std::printf("nodes in graph: %zu\n", size());
+        if constexpr (Algo::stats) {
+            uint64_t st[8];
+            impl::check(ctx_, mptg_prm_stats(prm_, st));
+            std::printf("wavefronts: %llu\nsamples: %llu\nedges: %llu\nlinks checked: %llu\n",
+                        (unsigned long long)st[0], (unsigned long long)st[1], (unsigned long long)st[5],
+                        (unsigned long long)st[4]);
+        }
+    }
+};
+
 }  // namespace unc::robotics::mpt_gb300

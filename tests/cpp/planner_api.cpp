@@ -99,7 +99,28 @@ int main() {
     }
     CHECK(threw2);
     star.printStats();
-    std::printf("C++ Planner OK: %zu waypoints, %zu nodes; PRRTStar %zu waypoints\n", path.size(), planner.size(),
-                spath.size());
+
+    // Planner<Scenario, PPRM<...>>: roadmap with explicit start and goal
+    Planner<WallScenario, PPRM<gpu_wavefront<2048>, report_stats<true>>> prm(sc, 7);
+    bool threw3 = false;
+    try {
+        prm.solveFor(std::chrono::seconds(1));  // "PPRM requires both start and goal configurations"
+    } catch (const std::runtime_error&) {
+        threw3 = true;
+    }
+    CHECK(threw3);
+    prm.addStart(WallScenario::startState());
+    prm.addGoal(sc.goal().state);
+    CHECK(prm.size() == 2);
+    prm.solveFor([&] { return prm.solved(); }, std::chrono::seconds(10));
+    CHECK(prm.solved());
+    auto ppath = prm.solution();
+    CHECK(ppath.size() >= 2 && ppath.front() == WallScenario::startState() && ppath.back() == sc.goal().state);
+    Counter pc;
+    prm.visitGraph(pc);
+    CHECK(pc.v == prm.size() && pc.e > pc.v && pc.e % 2 == 0);
+    prm.printStats();
+    std::printf("C++ Planner OK: %zu waypoints, %zu nodes; PRRTStar %zu waypoints; PPRM %zu waypoints\n",
+                path.size(), planner.size(), spath.size(), ppath.size());
     return 0;
 }
