@@ -389,6 +389,14 @@ mptg_status mptg_prm_solution(mptg_prm* prm, double* path, size_t cap, size_t* l
  * skipped, [4] links checked, [5] edges, [6] goal nodes, [7] solved */
 mptg_status mptg_prm_stats(mptg_prm* prm, uint64_t out[8]);
 
+/* ---- scene ingestion helpers (host only) -------------------------------
+ * PNG scanline reconstruction for the image reader of mpt_gb300.ingest (the
+ * row filters libpng undoes for demo/png_2d_scenario.hpp:198-240): raw holds
+ * height rows of (filter byte + stride bytes), out receives height * stride
+ * bytes; bpp = bytes per complete pixel (at least 1).  An unknown filter type
+ * returns MPTG_ERR_INVALID_ARG. */
+mptg_status mptg_png_unfilter(const uint8_t* raw, int height, int stride, int bpp, uint8_t* out);
+
 #ifdef __cplusplus
 }
 #endif
