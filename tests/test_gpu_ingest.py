@@ -61,3 +61,31 @@ def test_loaded_png_grid_solves(ctx, orc, tmp_path):
     ok, _ = orc.valid_edges(sc, sp, path[:-1], path[1:], sc["edge_step"], sc["resolution"])
     assert ok.all()
     pl.close()
+
+
+def test_export_real_runs(ctx, tmp_path):
+    """The writers on real planners: the PPRM roadmap of the grid (each
+    undirected edge visited from both ends) and a PRRT arm solution."""
+    import xml.etree.ElementTree as ET
+    import json
+    from mpt_gb300 import export
+    from mpt_gb300 import planner as P
+    sc = scenes.grid_scene()
+    pl = P.Planner(P.Scenario(sc), P.PPRM(P.gpu_wavefront(1024)), seed=9, ctx=ctx, max_nodes=1 << 18)
+    pl.add_start(sc["start"])
+    pl.add_goal(sc["goal"])
+    pl.solve_for(20.0, lambda: pl.solved())
+    n = export.svg_2d(str(tmp_path / "prm.svg"), pl, sc)
+    assert n == 2 * pl.edges() and n > 0
+    root = ET.parse(str(tmp_path / "prm.svg")).getroot()
+    assert len(root.findall("{http://www.w3.org/2000/svg}line")) == n + len(pl.solution()) - 1
+    pl.close()
+    arm = scenes.arm_scene()
+    pa = P.Planner(P.Scenario(arm), P.PRRT(P.gpu_wavefront(4096)), seed=1000, ctx=ctx, max_nodes=1 << 21)
+    pa.add_start(arm["start"])
+    pa.solve_for(20.0, lambda: pa.solved())
+    assert pa.solved()
+    k = export.arm_solution_js(str(tmp_path / "solution.js"), pa, arm)
+    d = json.loads(open(str(tmp_path / "solution.js")).read()[len("data = "):])
+    assert k == len(d["solution"]) >= 2 and d["solution"][0] == [float(v) for v in arm["start"]]
+    pa.close()
