@@ -416,10 +416,22 @@ __device__ __forceinline__ void robot_leaf_box(const BvhNode& rl, const float* R
 //     whole block: triangle box test, certified FP32 separating planes, FP64.
 // The block stops at the first intersection.  More candidates than fit
 // (MESH_CAND / MESH_FRONT) fall back to a per-thread depth-first walk.
+//
+// For the interior samples of a batch of edges (sample_edge != nullptr), a
+// block first reads its edge's result in edge_out and skips the sample when
+// another sample has already made the edge invalid (the edge result is the
+// AND of its samples, so the skipped sample's own result cannot matter), and
+// a colliding sample clears edge_out at once.  Blocks take the work items in
+// the scattered order w * MESH_PERM mod nwork, so the samples of one edge are
+// spread over the launch and most samples after an edge's first collision
+// are skipped.
+#define MESH_PERM 1000003ull  // prime; the identity order when it divides nwork
 __global__ void __launch_bounds__(MESH_DETAIL_THREADS, 8) k_mesh_detail(MeshView m, const double* __restrict__ q, int D,
                                                                       const int* __restrict__ work,
                                                                       const int* __restrict__ nwork,
-                                                                      uint8_t* __restrict__ out) {
+                                                                      uint8_t* __restrict__ out,
+                                                                      const int* __restrict__ sample_edge,
+                                                                      uint8_t* __restrict__ edge_out) {
     __shared__ double R[9];
     __shared__ double P[3];
     __shared__ float R32[9], P32[3];
@@ -432,9 +444,14 @@ __global__ void __launch_bounds__(MESH_DETAIL_THREADS, 8) k_mesh_detail(MeshView
     __shared__ int qra[MESH_QUEUE], qrc[MESH_QUEUE], qea[MESH_QUEUE], qec[MESH_QUEUE];
     __shared__ volatile int hit;
     const int w = blockIdx.x;
-    if (w >= *nwork) return;
-    const int i = work[w];
+    const int nw = *nwork;
+    if (w >= nw) return;
+    const int i = work[(unsigned long long)nw % MESH_PERM ? (int)(((unsigned long long)w * MESH_PERM) % nw) : w];
     const int tid = threadIdx.x;
+    if (sample_edge && __ldcg(&edge_out[sample_edge[i]]) == 0) {  // block-uniform
+        if (tid == 0) out[i] = 0;
+        return;
+    }
     const double* s = q + (size_t)i * D;
     if (tid == 0) {
         quat_mat64(s, R);
@@ -561,7 +578,10 @@ __global__ void __launch_bounds__(MESH_DETAIL_THREADS, 8) k_mesh_detail(MeshView
         }
     }
     __syncthreads();
-    if (tid == 0) out[i] = hit ? 0 : 1;
+    if (tid == 0) {
+        out[i] = hit ? 0 : 1;
+        if (hit && sample_edge) edge_out[sample_edge[i]] = 0;
+    }
 }
 
 // ------------------------------------------------------------------ edges
@@ -759,7 +779,8 @@ static mptg_status mesh_scratch_init(mptg_ctx* ctx, EdgeScratch* x) {
     return MPTG_OK;
 }
 
-mptg_status mesh_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* dout, cudaStream_t s, EdgeScratch* x) {
+mptg_status mesh_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* dout, cudaStream_t s, EdgeScratch* x,
+                            const int* sample_edge, uint8_t* edge_out) {
     mptg_ctx* ctx = sc->ctx;
     MeshData* md = sc->mesh;
     if (n <= 0) return MPTG_OK;
@@ -775,7 +796,8 @@ mptg_status mesh_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* do
     if (n <= 16384) {
         // small batches: one block per state, the blocks past the device-side
         // count leave at once, and no host round trip is needed
-        k_mesh_detail<<<n, MESH_DETAIL_THREADS, 0, s>>>(v, dq, sc->D, x->mwork, x->nwork, dout);
+        k_mesh_detail<<<n, MESH_DETAIL_THREADS, 0, s>>>(v, dq, sc->D, x->mwork, x->nwork, dout, sample_edge,
+                                                        edge_out);
         MPTG_LAUNCHED(ctx);
         MPTG_CUDA_TRY(ctx, cudaGetLastError());
         return MPTG_OK;
@@ -785,7 +807,8 @@ mptg_status mesh_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* do
     int nw = x->hbuf[0];
     if (nw > 0) {
         // one block per state that the sphere test could not clear
-        k_mesh_detail<<<nw, MESH_DETAIL_THREADS, 0, s>>>(v, dq, sc->D, x->mwork, x->nwork, dout);
+        k_mesh_detail<<<nw, MESH_DETAIL_THREADS, 0, s>>>(v, dq, sc->D, x->mwork, x->nwork, dout, sample_edge,
+                                                         edge_out);
         MPTG_LAUNCHED(ctx);
     }
     MPTG_CUDA_TRY(ctx, cudaGetLastError());
@@ -830,7 +853,7 @@ mptg_status mesh_edges_dev(mptg_scene* sc, const double* da, const double* db, i
         k_mesh_edge_samples<<<n, 64, 0, s>>>(sc->metric, sc->D, da, db, n, x->counts, x->offs, x->samples,
                                              x->sample_edge);
         MPTG_LAUNCHED(ctx);
-        st = mesh_states_dev(sc, x->samples, total, x->sample_ok, s, x);
+        st = mesh_states_dev(sc, x->samples, total, x->sample_ok, s, x, x->sample_edge, dout);
         if (st) return st;
         k_mesh_edge_reduce<<<mptg_blocks(total, 256), 256, 0, s>>>(x->sample_ok, x->sample_edge, total, dout);
         MPTG_LAUNCHED(ctx);

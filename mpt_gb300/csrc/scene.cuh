@@ -87,5 +87,6 @@ void mesh_scene_free(mptg_scene* s);
 void mesh_fill_view(const mptg_scene* s, SceneView* v);
 mptg_status mesh_edges_dev(mptg_scene* sc, const double* da, const double* db, int n, double step, int resolution,
                            uint8_t* dout, cudaStream_t s, unsigned long long* nsamp, EdgeScratch* scr);
+// sample_edge / edge_out: the interior samples of a batch of edges (see k_mesh_detail)
 mptg_status mesh_states_dev(mptg_scene* sc, const double* dq, int n, uint8_t* dout, cudaStream_t s,
-                            EdgeScratch* scr);
+                            EdgeScratch* scr, const int* sample_edge = nullptr, uint8_t* edge_out = nullptr);
