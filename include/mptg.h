@@ -78,10 +78,10 @@ mptg_status mptg_tree_size(mptg_tree* tree, size_t* n);
 /* Search strategy, as the reference picks a nigh strategy per planner
  * (src/mpt/impl/nearest_strategy.hpp:44-72; auto = nigh::auto_strategy_t).
  * KDTREE: the bucketed kd-tree walk.  EXHAUSTIVE: every stored point, staged
- * through shared memory 256 queries at a time (nigh::Linear's answer).  AUTO
- * uses EXHAUSTIVE for six or more dimensions or a rotation metric up to
- * 131,072 points, where the tree must visit a large share of them.  Every
- * strategy returns the same exact ids and distances. */
+ * through shared memory (nigh::Linear's answer).  AUTO uses EXHAUSTIVE for
+ * L2, L1 and SO2 spaces of six or more dimensions while points x queries x
+ * dim <= 2.5e11, where the tree must visit a large share of the points.
+ * Every strategy returns the same exact ids and distances. */
 typedef enum { MPTG_NN_AUTO = 0, MPTG_NN_KDTREE = 1, MPTG_NN_EXHAUSTIVE = 2 } mptg_nn_strategy;
 mptg_status mptg_tree_set_strategy(mptg_tree* tree, int strategy);
 /* Remove every state, keeping the tree's allocations (no reference
