@@ -448,12 +448,12 @@ __global__ void __launch_bounds__(MESH_DETAIL_THREADS, 8) k_mesh_detail(MeshView
     if (w >= nw) return;
     const int i = work[(unsigned long long)nw % MESH_PERM ? (int)(((unsigned long long)w * MESH_PERM) % nw) : w];
     const int tid = threadIdx.x;
-    if (sample_edge && __ldcg(&edge_out[sample_edge[i]]) == 0) {  // block-uniform
-        if (tid == 0) out[i] = 0;
-        return;
-    }
+    __shared__ int dead;
     const double* s = q + (size_t)i * D;
     if (tid == 0) {
+        // one read of the edge's result for the whole block (other blocks may
+        // clear it at any time, so per-thread reads could disagree)
+        dead = sample_edge && __ldcg(&edge_out[sample_edge[i]]) == 0;
         quat_mat64(s, R);
         P[0] = s[4]; P[1] = s[5]; P[2] = s[6];
         for (int k = 0; k < 9; ++k) R32[k] = (float)R[k];
@@ -473,6 +473,10 @@ __global__ void __launch_bounds__(MESH_DETAIL_THREADS, 8) k_mesh_detail(MeshView
         hit = 0;
     }
     __syncthreads();
+    if (dead) {  // block-uniform
+        if (tid == 0) out[i] = 0;
+        return;
+    }
     const float eps = eps_s, X = X_s;
     // 1. candidates: environment leaves within the bounding sphere (center p,
     //    radius reach plus a margin far above FP32 rounding)
