@@ -154,7 +154,7 @@ def edge_rates(ctx, m, stream, torch):
 def _solve_stats(ctx, sc, W, seeds, cap_s, surrogate=None, points=1):
     """p50/p99 wall time to the first solution over seeds 1000.., with the phase timers."""
     from mpt_gb300 import planner as P
-    times, solved, nodes, checked, timers = [], 0, [], [], []
+    times, solved, nodes, checked, timers, seed_times = [], 0, [], [], [], []
     for s in range(seeds):
         pl = P.Planner(P.Scenario(sc), P.PRRT(P.gpu_wavefront(W)), seed=1000 + s, ctx=ctx, max_nodes=1 << 21)
         if surrogate is not None:
@@ -166,18 +166,19 @@ def _solve_stats(ctx, sc, W, seeds, cap_s, surrogate=None, points=1):
         if pl.solved():
             solved += 1
             times.append(dt)
+        seed_times.append(dt if pl.solved() else None)
         nodes.append(pl.size())
         checked.append(pl.stats()["link_states_checked"])
         timers.append(pl.timers())
         pl.close()
     med_t = {k: statistics.median(t[k] for t in timers) for k in timers[0]}
-    return {"wavefront": W, "p50_s": statistics.median(times) if times else None,
+    return {"wavefront": W, "seed_times_s": seed_times, "p50_s": statistics.median(times) if times else None,
             "p99_s": max(times) if times else None, "solved": solved, "seeds": seeds, "cap_s": cap_s,
             "median_nodes": statistics.median(nodes), "median_link_states_checked": statistics.median(checked),
             "median_phase_s": med_t}
 
 
-def solve_times(ctx, seeds=5, cap_s=20.0, tune=True):
+def solve_times(ctx, seeds=5, cap_s=20.0, tune=True, cpu=True):
     """Wall time to the first solution of the plain wavefront planner per scene
     (p50 over seeds), at the default wavefront and at the one the native
     autotuner picks (tuned on seeds 500.. of the same query)."""
@@ -188,9 +189,25 @@ def solve_times(ctx, seeds=5, cap_s=20.0, tune=True):
                         ("se3_mesh", scenes.mesh_scene, 4096)]:
         sc = mk()
         r = {"default": _solve_stats(ctx, sc, W, seeds, cap_s)}
+        if cpu:
+            # the oracle's replay of the same wavefront planner (identical tree, brute-force
+            # NN, all host cores) on the first seed: a CPU port of the same run
+            import oracle
+            sp = oracle.make_space(sc["metric"], sc["dim"], sc["weights"])
+            prm = {"range": sc["range"], "goal_bias": 0.01, "goal_radius": sc["goal_radius"],
+                   "edge_step": sc["edge_step"], "resolution": sc["resolution"], "wavefront": W, "seed": 1000,
+                   "max_nodes": 1 << 21}
+            t0 = time.perf_counter()
+            st, _, g = oracle.plan(sc, sp, prm, sc["lo"], sc["hi"], sc["start"], sc["goal"], 400, True)
+            cpu_s = time.perf_counter() - t0
+            gpu_first = r["default"]["seed_times_s"][0]
+            r["cpu_port_seed1000"] = {"kind": "port (oracle replay of the same wavefront planner, brute-force NN)",
+                                      "cores": os.cpu_count(), "wavefront": W, "s": cpu_s, "solved": len(g) > 0,
+                                      "nodes": len(st), "gpu_same_seed_s": gpu_first,
+                                      "ratio": cpu_s / gpu_first if gpu_first else None}
         if tune:
             t0 = time.perf_counter()
-            best, med = P.autotune_wavefront(ctx, P.Scenario(sc), sc["start"], trials=5, time_limit=1.0, seed=500)
+            best, med = P.autotune_wavefront(ctx, P.Scenario(sc), sc["start"], trials=7, time_limit=1.0, seed=500)
             r["autotune"] = {"best": best, "median_s": {str(k): v for k, v in med.items()},
                              "tuning_s": time.perf_counter() - t0}
             r["tuned"] = _solve_stats(ctx, sc, best, seeds, cap_s)
