@@ -635,15 +635,15 @@ static mptg_status star_wave(mptg_planner* p, cudaStream_t s, int A, size_t n0) 
     MPTG_LAUNCHED(ctx);
     if ((st = mptg_tree_nearest_k_dev(p->tree, p->acc_states, A, k, p->knn_i, p->knn_d, s))) return st;
     MPTG_CUDA_TRY(ctx, cudaEventRecord(p->sev[1], s));
-    // choose parent: candidates in key order, in rounds of rank [0,1), [1,5), [5,k)
+    // choose parent: candidates in key order, in rounds of rank [0,1) and [1,k)
     MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->pv, 0, pairs, s));
     MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->decided, 0, A, s));
     k_star_rank<<<mptg_blocks(pairs, 128), 128, 0, s>>>(A, k, p->knn_i, p->knn_d, p->acc_parent, p->dnear, p->cost,
                                                        p->rank);
     MPTG_LAUNCHED(ctx);
     int npc = 0;
-    const int bounds[4] = {0, 1, 5, 64};
-    for (int r = 0; r < 3; ++r) {
+    const int bounds[3] = {0, 1, 64};
+    for (int r = 0; r < 2; ++r) {
         MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->s_cnt, 0, sizeof(int), s));
         k_star_pc<<<mptg_blocks(pairs, 128), 128, 0, s>>>(v, A, k, bounds[r], bounds[r + 1], p->knn_i, p->rank,
                                                          p->decided, st64, p->acc_states, p->s_cnt, p->s_pair,
