@@ -13,9 +13,9 @@
 // does not change it.  Grid edges: a thread per edge checks b and the step
 // count, then a warp per surviving edge takes 32 samples per round in a
 // coarse-to-fine spread (lane j of round r tests sample j*R + r).  Planar-arm
-// edges: a warp per edge decides one sample at a time with the lanes split
-// over the (link, obstacle) pairs, so it leaves at the first colliding link
-// of the first colliding sample.
+// edges: a warp (up to 8 warps for small batches) per edge decides one sample
+// at a time with the lanes split over the (link, obstacle) pairs, so it leaves
+// soon after the first colliding link of the first colliding sample.
 //
 // Exactness: every boolean equals the FP64 definition.  Values are first
 // computed in FP32 with an a-priori error margin; a decision whose FP32 value
@@ -605,7 +605,7 @@ __device__ __forceinline__ bool arm_edge_warp(const SceneView& s, const double* 
 // dealt round-robin to the edge's warps.  The edge is valid iff no warp finds
 // an invalid sample, whatever the order; a warp that finds one raises the
 // edge's shared flag and the others stop at their next sample.
-__global__ void __launch_bounds__(256) k_arm_edges(SceneView s, const double* __restrict__ a,
+__global__ void __launch_bounds__(256, 4) k_arm_edges(SceneView s, const double* __restrict__ a,
                                                    const double* __restrict__ b, int n, double inv, int resolution,
                                                    uint8_t* __restrict__ out, unsigned long long* __restrict__ nsamp,
                                                    int lg) {
