@@ -519,7 +519,7 @@ __device__ __forceinline__ void load_query(const double* __restrict__ qd, int D,
 // order (may be null): warp w answers query order[w], so that neighbouring
 // warps, sorted by tree region, reuse each other's nodes in L1
 template <int MK, int DMAX>
-__global__ void __launch_bounds__(256, 5) k_nearest(TreeView t, const double* __restrict__ q64, int nq,
+__global__ void __launch_bounds__(256, 4) k_nearest(TreeView t, const double* __restrict__ q64, int nq,
                                                  const int* __restrict__ order, int* __restrict__ out_idx,
                                                  double* __restrict__ out_d) {
     const int lane = threadIdx.x & 31;
