@@ -151,10 +151,13 @@ def edge_rates(ctx, m, stream, torch):
     return out
 
 
-def _solve_stats(ctx, sc, W, seeds, cap_s, surrogate=None, points=1):
+def _solve_stats(ctx, sc, W, seeds, cap_s, surrogate=None, points=1, want_path=False):
     """p50/p99 wall time to the first solution over seeds 1000.., with the phase timers."""
     from mpt_gb300 import planner as P
+    import oracle
+    osp = oracle.make_space(sc["metric"], sc["dim"], sc["weights"])
     times, solved, nodes, checked, timers, seed_times = [], 0, [], [], [], []
+    validated, costs, first_path = 0, [], None
     for s in range(seeds):
         pl = P.Planner(P.Scenario(sc), P.PRRT(P.gpu_wavefront(W)), seed=1000 + s, ctx=ctx, max_nodes=1 << 21)
         if surrogate is not None:
@@ -166,16 +169,25 @@ def _solve_stats(ctx, sc, W, seeds, cap_s, surrogate=None, points=1):
         if pl.solved():
             solved += 1
             times.append(dt)
+            # every path re-validated by the CPU checker (outside the timed region)
+            path = np.array(pl.solution())
+            ok, _ = oracle.valid_edges(sc, osp, path[:-1], path[1:], sc["edge_step"], sc["resolution"])
+            validated += int(ok.all())
+            costs.append(pl.last_cost)
+            if s == 0:
+                first_path = (path, pl.last_cost)
         seed_times.append(dt if pl.solved() else None)
         nodes.append(pl.size())
         checked.append(pl.stats()["link_states_checked"])
         timers.append(pl.timers())
         pl.close()
     med_t = {k: statistics.median(t[k] for t in timers) for k in timers[0]}
-    return {"wavefront": W, "seed_times_s": seed_times, "p50_s": statistics.median(times) if times else None,
+    res = {"wavefront": W, "seed_times_s": seed_times, "paths_validated_by_checker": validated, "median_path_cost": statistics.median(costs) if costs else None,
+            "p50_s": statistics.median(times) if times else None,
             "p99_s": max(times) if times else None, "solved": solved, "seeds": seeds, "cap_s": cap_s,
             "median_nodes": statistics.median(nodes), "median_link_states_checked": statistics.median(checked),
             "median_phase_s": med_t}
+    return (res, first_path) if want_path else res
 
 
 def solve_times(ctx, seeds=5, cap_s=20.0, tune=True, cpu=True):
@@ -188,7 +200,8 @@ def solve_times(ctx, seeds=5, cap_s=20.0, tune=True, cpu=True):
     for name, mk, W in [("grid_1024", scenes.grid_scene, 2048), ("arm_10link", scenes.arm_scene, 4096),
                         ("se3_mesh", scenes.mesh_scene, 4096)]:
         sc = mk()
-        r = {"default": _solve_stats(ctx, sc, W, seeds, cap_s)}
+        dflt, fp = _solve_stats(ctx, sc, W, seeds, cap_s, want_path=True)
+        r = {"default": dflt}
         if cpu:
             # the oracle's replay of the same wavefront planner (identical tree, brute-force
             # NN, all host cores) on the first seed: a CPU port of the same run
@@ -198,13 +211,30 @@ def solve_times(ctx, seeds=5, cap_s=20.0, tune=True, cpu=True):
                    "edge_step": sc["edge_step"], "resolution": sc["resolution"], "wavefront": W, "seed": 1000,
                    "max_nodes": 1 << 21}
             t0 = time.perf_counter()
-            st, _, g = oracle.plan(sc, sp, prm, sc["lo"], sc["hi"], sc["start"], sc["goal"], 400, True)
+            st, par, g = oracle.plan(sc, sp, prm, sc["lo"], sc["hi"], sc["start"], sc["goal"], 400, True)
             cpu_s = time.perf_counter() - t0
             gpu_first = r["default"]["seed_times_s"][0]
+            # the replay's best goal path (lowest cost, summed from the start) against the GPU's
+            same_path = None
+            if len(g) and fp is not None:
+                best = None
+                for gi in g:
+                    chain = [int(gi)]
+                    while par[chain[-1]] >= 0:
+                        chain.append(int(par[chain[-1]]))
+                    chain.reverse()
+                    c = 0.0
+                    for a, b in zip(chain[:-1], chain[1:]):
+                        c += oracle.distance(sp, st[a], st[b])
+                    if best is None or c < best[0]:
+                        best = (c, chain)
+                same_path = bool(len(best[1]) == len(fp[0]) and np.array_equal(st[best[1]], fp[0]) and
+                                 abs(best[0] - fp[1]) <= 1e-12 * max(1.0, best[0]))
             r["cpu_port_seed1000"] = {"kind": "port (oracle replay of the same wavefront planner, brute-force NN)",
                                       "cores": os.cpu_count(), "wavefront": W, "s": cpu_s, "solved": len(g) > 0,
                                       "nodes": len(st), "gpu_same_seed_s": gpu_first,
-                                      "ratio": cpu_s / gpu_first if gpu_first else None}
+                                      "ratio": cpu_s / gpu_first if gpu_first else None,
+                                      "same_path_and_cost_as_gpu": same_path}
         if tune:
             t0 = time.perf_counter()
             best, med = P.autotune_wavefront(ctx, P.Scenario(sc), sc["start"], trials=7, time_limit=1.0, seed=500)
@@ -633,12 +663,13 @@ def run_gpu(args):
         cores = os.cpu_count()
         ot.nearest(hq[0][:256], cores)
         t0 = time.perf_counter()
-        ci, _ = ot.nearest(hq[0][:sample], cores)
+        ci, cd = ot.nearest(hq[0][:sample], cores)
         cpu_s = time.perf_counter() - t0
-        gi, _ = tree.nearest(hq[0][:sample])
+        gi, gd = tree.nearest(hq[0][:sample])
         cpu = {"value": sample / cpu_s, "unit": "queries/s", "cores": cores, "kind": "port",
                "sample": "%d queries against the full 1,048,576-node tree" % sample,
-               "ids_equal_gpu": bool(np.array_equal(ci, gi))}
+               "ids_equal_gpu": bool(np.array_equal(ci, gi)),
+               "max_abs_dist_err_vs_fp64_oracle": float(np.max(np.abs(gd - cd)))}
 
     if rank == 0:
         line = {"metric": "NN queries/s @1M nodes (SO(2)^10, 10-link arm)", "value": value, "unit": "queries/s",
