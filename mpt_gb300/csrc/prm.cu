@@ -502,7 +502,23 @@ static mptg_status prm_wave(mptg_prm* p, int W, uint8_t flag, int* first_id) {
 static mptg_status prm_add(mptg_prm* p, const double* q, uint8_t flag, int32_t* id) {
     if (!p || !q) return MPTG_ERR_INVALID_ARG;
     if (p->solving) return mptg_fail(p->ctx, MPTG_ERR_ALREADY_SOLVING, "already solving");
-    MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(p->samp, q, p->D * sizeof(double), cudaMemcpyDefault, p->stream));
+    // a state outside the space (the tree's insert rules) is an error before
+    // anything joins the roadmap, not a dropped sample
+    std::vector<double> h(p->D);
+    MPTG_CUDA_TRY(p->ctx, cudaMemcpy(h.data(), q, p->D * sizeof(double), cudaMemcpyDefault));
+    bool bad = false;
+    for (int d = 0; d < p->D; ++d) {
+        bad = bad || !std::isfinite(h[d]);
+        if (p->metric == MPTG_METRIC_SO2) bad = bad || !(h[d] >= -MPTG_PI && h[d] <= MPTG_PI);
+    }
+    if (p->metric == MPTG_METRIC_SO3 || p->metric == MPTG_METRIC_SE3) {
+        const double nn = h[0] * h[0] + h[1] * h[1] + h[2] * h[2] + h[3] * h[3];
+        bad = bad || !(std::fabs(nn - 1.0) <= MPTG_QUAT_NORM_TOL);
+    }
+    if (bad)
+        return mptg_fail(p->ctx, MPTG_ERR_INVALID_ARG,
+                         "invalid state (NaN/inf, SO2 angle outside [-pi,pi], or non-unit quaternion)");
+    MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(p->samp, h.data(), p->D * sizeof(double), cudaMemcpyHostToDevice, p->stream));
     int first = -1;
     mptg_status st = prm_wave(p, 1, flag, &first);
     if (id) *id = first;

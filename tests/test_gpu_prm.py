@@ -98,6 +98,9 @@ def test_prm_errors_and_duplicates(ctx):
         pl.run(1)  # no goal
     ys, xs = np.nonzero(sc["grid"])
     assert pl.add_goal(np.array([float(xs[0]), float(ys[0])])) == -1  # invalid state (pprm.hpp:299-300)
+    with pytest.raises(m.MptgError):
+        pl.add_goal(np.array([np.nan, 5.0]))  # outside the space: an error, nothing added
+    assert pl.size() == 1
     assert pl.add_goal(sc["goal"]) == 1
     pl.run(2)
     assert pl.stats()["wavefronts"] == 2
