@@ -110,6 +110,22 @@ def _dist_env():
     return ws, rank, local
 
 
+def _max_over_ranks(x: float, ws: int, device: str = "cuda") -> float:
+    """The largest x over the ranks: the slowest replica sets the job's time."""
+    if ws <= 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _whole_job_rate(ws: int, units_per_rank_step: int, steps: int, max_seconds: float) -> float:
+    """Units of all ranks per second of the slowest rank (weak scaling: every
+    rank processes the same per-step work on its own replica)."""
+    return ws * units_per_rank_step * steps / max_seconds
+
+
 def _workload(seed_base=20261205):
     from mpt_gb300 import scenes
     sc = scenes.arm_scene()
@@ -580,12 +596,9 @@ def run_gpu(args):
     launches = ctx.kernel_launches() - launches0
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     total_ms = sum(step_ms)
-    if ws > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = _max_over_ranks(total_ms, ws)
     cnt = tree.counters(reset=True)
-    value = ws * nqb * args.steps / (total_ms / 1000.0)
+    value = _whole_job_rate(ws, nqb, args.steps, total_ms / 1000.0)
 
     # roofline of k_nearest: algorithmic bytes per launch from the device counters
     D = sc["dim"]
@@ -619,12 +632,8 @@ def run_gpu(args):
         st = ctx.lib.mptg_nearest(tree.h, qn[s % nbuf].ctypes.data, nqb, hi.data_ptr(), hd.data_ptr(), None)
         e2e_t.append(time.perf_counter() - t0)
         assert st == 0
-    e2e_total = sum(e2e_t)
-    if ws > 1:
-        t = torch.tensor([e2e_total], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_val = ws * nqb * args.steps / e2e_total
+    e2e_total = _max_over_ranks(sum(e2e_t), ws)
+    e2e_val = _whole_job_rate(ws, nqb, args.steps, e2e_total)
     # results of the host path equal the device path
     assert np.array_equal(hi.numpy(), tree.nearest(hq[(args.steps - 1) % nbuf])[0])
 

@@ -1,0 +1,69 @@
+"""CPU, two gloo ranks: the host side of `bench.py --gpus N` (replicas only) --
+rank/world parsing, the max-over-ranks timing rule, the whole-job rate, and
+the reference arm's rule that only rank 0 runs and prints."""
+import os
+import socket
+import sys
+
+import pytest
+
+torch = pytest.importorskip("torch")
+import torch.distributed as dist  # noqa: E402
+import torch.multiprocessing as mp  # noqa: E402
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _rank_main(rank, ws, port, out):
+    os.environ.update({"MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port), "WORLD_SIZE": str(ws),
+                       "RANK": str(rank), "LOCAL_RANK": str(rank)})
+    sys.path.insert(0, ROOT)
+    import bench
+    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    try:
+        w, r, local = bench._dist_env()
+        assert (w, r, local) == (ws, rank, rank)
+        # rank r takes 100 + 50 r ms: the job's time is the slowest rank's
+        t = bench._max_over_ranks(100.0 + 50.0 * rank, w, device="cpu")
+        rate = bench._whole_job_rate(w, 65536, 10, t / 1000.0)
+
+        class Args:
+            gpus, steps, warmup = ws, 1, 1
+        printed = None
+        if rank != 0:
+            import io
+            import contextlib
+            buf = io.StringIO()
+            with contextlib.redirect_stdout(buf):
+                bench.run_reference(Args())  # ranks other than 0 exit without work
+            printed = buf.getvalue()
+        out[rank] = (t, rate, printed)
+        dist.barrier()
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_time_and_rate():
+    ws = 2
+    ctx = mp.get_context("spawn")
+    out = ctx.Manager().dict()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_main, args=(r, ws, port, out)) for r in range(ws)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    t0, rate0, _ = out[0]
+    t1, rate1, printed1 = out[1]
+    assert t0 == t1 == 150.0
+    assert rate0 == rate1 == 2 * 65536 * 10 / 0.15
+    assert printed1 == ""
