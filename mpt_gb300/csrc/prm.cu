@@ -339,16 +339,15 @@ static void prm_free(mptg_prm* p) {
     delete p;
 }
 
-// grows a device array (contents kept) to hold at least need elements
+// replaces a device array by one of `need` elements, keeping its first `keep`
 template <typename T>
-static mptg_status grow(mptg_ctx* ctx, cudaStream_t s, T** ptr, size_t have, size_t need, size_t keep) {
+static mptg_status grow(mptg_ctx* ctx, cudaStream_t s, T** ptr, size_t need, size_t keep) {
     T* q = nullptr;
     MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&q, need * sizeof(T)));
     if (*ptr && keep) MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(q, *ptr, keep * sizeof(T), cudaMemcpyDeviceToDevice, s));
     MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     if (*ptr) cudaFree(*ptr);
     *ptr = q;
-    (void)have;
     return MPTG_OK;
 }
 
@@ -358,12 +357,12 @@ static mptg_status prm_reserve_pairs(mptg_prm* p, size_t M) {
     const size_t cap = std::max(M, p->pcap + p->pcap / 2);
     const size_t D = p->D;
     mptg_status st;
-    if ((st = grow(ctx, p->stream, &p->pa, p->pcap, cap, 0))) return st;
-    if ((st = grow(ctx, p->stream, &p->pb, p->pcap, cap, 0))) return st;
-    if ((st = grow(ctx, p->stream, &p->pd, p->pcap, cap, 0))) return st;
-    if ((st = grow(ctx, p->stream, &p->ea, p->pcap * D, cap * D, 0))) return st;
-    if ((st = grow(ctx, p->stream, &p->eb, p->pcap * D, cap * D, 0))) return st;
-    if ((st = grow(ctx, p->stream, &p->eok, p->pcap, cap, 0))) return st;
+    if ((st = grow(ctx, p->stream, &p->pa, cap, 0))) return st;
+    if ((st = grow(ctx, p->stream, &p->pb, cap, 0))) return st;
+    if ((st = grow(ctx, p->stream, &p->pd, cap, 0))) return st;
+    if ((st = grow(ctx, p->stream, &p->ea, cap * D, 0))) return st;
+    if ((st = grow(ctx, p->stream, &p->eb, cap * D, 0))) return st;
+    if ((st = grow(ctx, p->stream, &p->eok, cap, 0))) return st;
     p->pcap = cap;
     return MPTG_OK;
 }
@@ -373,9 +372,9 @@ static mptg_status prm_reserve_edges(mptg_prm* p, size_t need) {
     mptg_ctx* ctx = p->ctx;
     const size_t cap = std::max(need, p->ecap * 2);
     mptg_status st;
-    if ((st = grow(ctx, p->stream, &p->efrom, p->ecap, cap, p->ne))) return st;
-    if ((st = grow(ctx, p->stream, &p->eto, p->ecap, cap, p->ne))) return st;
-    if ((st = grow(ctx, p->stream, &p->edist, p->ecap, cap, p->ne))) return st;
+    if ((st = grow(ctx, p->stream, &p->efrom, cap, p->ne))) return st;
+    if ((st = grow(ctx, p->stream, &p->eto, cap, p->ne))) return st;
+    if ((st = grow(ctx, p->stream, &p->edist, cap, p->ne))) return st;
     p->ecap = cap;
     return MPTG_OK;
 }
