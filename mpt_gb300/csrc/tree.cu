@@ -31,6 +31,8 @@ enum { CNT_NODES = 0, CNT_BUCKETS = 1, CNT_NSEG_NEXT = 2, CNT_ERR = 3, CNT_OVF =
 
 // a leaf deeper than this triggers a rebuild of the whole tree
 #define MPTG_REBUILD_DEPTH 40
+// inserts up to this many states queue the first build level without a round trip
+#define MPTG_INSERT_PENDING_MAX 65536
 
 enum { SEG_SPLIT = 0, SEG_LEAF = 1 };
 
@@ -179,11 +181,29 @@ __global__ void k_append(int4* __restrict__ nodes, const float* __restrict__ pts
 
 // one thread per overflowing leaf: open a build segment holding the leaf's
 // bucket points followed by its overflow points
+// Counts the host has not read yet: the first builder launches of an insert
+// are queued behind k_append without a round trip, with -1 for the count,
+// and read it from the device counters.  More overflowing leaves than build
+// segments make every such launch a no-op (k_ovf_segs flags the capacity
+// error, which the host reads with the next counters).
+__device__ __forceinline__ int pending_nreg(const int* dcnt, int seg_cap) {
+    const int r = dcnt[CNT_NREG];
+    return r <= seg_cap ? r : 0;
+}
+__device__ __forceinline__ int pending_total(const int* dcnt, int seg_cap) {
+    const int r = pending_nreg(dcnt, seg_cap);
+    return r ? MPTG_BUCKET * r + dcnt[CNT_OVF] : 0;
+}
+
 __global__ void k_ovf_segs(const int4* __restrict__ nodes, const int* __restrict__ bids,
                            const int* __restrict__ node_depth, int nreg, const int* __restrict__ ovf_leaf,
                            int* __restrict__ dcnt, SegState* __restrict__ seg, int* __restrict__ perm,
-                           int* __restrict__ pseg, int* __restrict__ seg_cursor) {
+                           int* __restrict__ pseg, int* __restrict__ seg_cursor, int seg_cap) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nreg < 0) {
+        if (dcnt[CNT_NREG] > seg_cap && r == 0) atomicOr((unsigned*)&dcnt[CNT_ERR], MPTG_DEVERR_CAPACITY);
+        nreg = pending_nreg(dcnt, seg_cap);
+    }
     if (r >= nreg) return;
     int L = ovf_leaf[r];
     int4 nd = nodes[L];
@@ -202,8 +222,10 @@ __global__ void k_ovf_segs(const int4* __restrict__ nodes, const int* __restrict
 
 __global__ void k_ovf_scatter(int novf, int first, const int* __restrict__ ovf_pts, const int* __restrict__ leaf_of,
                               const int* __restrict__ leaf_reg, const SegState* __restrict__ seg,
-                              int* __restrict__ seg_cursor, int* __restrict__ perm, int* __restrict__ pseg) {
+                              int* __restrict__ seg_cursor, int* __restrict__ perm, int* __restrict__ pseg,
+                              const int* __restrict__ dcnt, int seg_cap) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (novf < 0) novf = pending_nreg(dcnt, seg_cap) ? dcnt[CNT_OVF] : 0;
     if (k >= novf) return;
     int i = ovf_pts[k];
     int r = leaf_reg[leaf_of[i]];
@@ -216,8 +238,9 @@ __global__ void k_ovf_scatter(int novf, int first, const int* __restrict__ ovf_p
 // decide leaf vs split
 __global__ void k_seg_a(SegState* __restrict__ cur, int nseg, const SegState* __restrict__ prev,
                         int4* __restrict__ nodes, int* __restrict__ dcnt, int bucket_cap, int* __restrict__ box,
-                        int D) {
+                        int D, int seg_cap) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nseg < 0) nseg = pending_nreg(dcnt, seg_cap);
     if (s >= nseg) return;
     SegState S = cur[s];
     if (S.parent >= 0) {
@@ -251,7 +274,9 @@ __global__ void k_seg_a(SegState* __restrict__ cur, int nseg, const SegState* __
 // level step B (per position): fill leaf buckets, accumulate split boxes
 __global__ void k_seg_b(const SegState* __restrict__ cur, const int* __restrict__ perm, const int* __restrict__ pseg,
                         int* __restrict__ pseg2, int total, const float* __restrict__ pts32, int D,
-                        float* __restrict__ bpts, int* __restrict__ bids, int* __restrict__ box) {
+                        float* __restrict__ bpts, int* __restrict__ bids, int* __restrict__ box,
+                        const int* __restrict__ dcnt, int seg_cap) {
+    if (total < 0) total = pending_total(dcnt, seg_cap);
     int pos = blockIdx.x * blockDim.x + threadIdx.x;
     int lane = threadIdx.x & 31;
     int s = pos < total ? pseg[pos] : -1;
@@ -297,6 +322,7 @@ __global__ void k_seg_c(SegState* __restrict__ cur, int nseg, SegState* __restri
                         int* __restrict__ node_depth, int* __restrict__ dcnt, int node_cap, int seg_cap,
                         const int* __restrict__ box, int D, int metric, float w0, float w1) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nseg < 0) nseg = pending_nreg(dcnt, seg_cap);
     if (s >= nseg) return;
     SegState S = cur[s];
     if (S.kind != SEG_SPLIT) return;
@@ -363,7 +389,8 @@ __global__ void k_seg_c(SegState* __restrict__ cur, int nseg, SegState* __restri
 // level step D (per position): partition the points of split segments
 __global__ void k_seg_d(SegState* __restrict__ cur, const int* __restrict__ perm, const int* __restrict__ pseg,
                         int* __restrict__ perm2, int* __restrict__ pseg2, int total, const float* __restrict__ pts32,
-                        int D) {
+                        int D, const int* __restrict__ dcnt, int seg_cap) {
+    if (total < 0) total = pending_total(dcnt, seg_cap);
     int pos = blockIdx.x * blockDim.x + threadIdx.x;
     int lane = threadIdx.x & 31;
     int s = pos < total ? pseg[pos] : -1;
@@ -1501,8 +1528,12 @@ static mptg_status read_counters(mptg_tree* t, cudaStream_t s) {
 }
 
 // level-synchronous build of the `nseg` segments in segA over positions
-// [0, total) of perm/pseg
-static mptg_status build_levels(mptg_tree* t, cudaStream_t s, int nseg, int total) {
+// [0, total) of perm/pseg.  nseg = total = -1: the first level runs on the
+// counts k_append left on the device (the overflowing leaves, see
+// pending_nreg), in grids of bound_seg / bound_total threads, and the host
+// learns the counts with that level's counters.
+static mptg_status build_levels(mptg_tree* t, cudaStream_t s, int nseg, int total, int bound_seg = 0,
+                                int bound_total = 0) {
     mptg_ctx* ctx = t->ctx;
     const int D = t->D;
     SegState* cur = t->segA;
@@ -1510,19 +1541,28 @@ static mptg_status build_levels(mptg_tree* t, cudaStream_t s, int nseg, int tota
     int* perm = t->perm; int* perm2 = t->perm2; int* pseg = t->pseg; int* pseg2 = t->pseg2;
     const unsigned tb = 256;
     mptg_status st;
-    for (int level = 0; nseg > 0 && level < 4 * MPTG_MAX_DEPTH; ++level) {
+    for (int level = 0; nseg != 0 && level < 4 * MPTG_MAX_DEPTH; ++level) {
+        const bool pending = nseg < 0;
+        const int gs = pending ? bound_seg : nseg, gt = pending ? bound_total : total;
         MPTG_CUDA_TRY(ctx, cudaMemsetAsync(t->dcnt + CNT_NSEG_NEXT, 0, sizeof(int), s));
-        k_seg_a<<<mptg_blocks(nseg, 128), 128, 0, s>>>(cur, nseg, prev, t->nodes, t->dcnt, t->bucket_cap,
-                                                       t->seg_box, D);
-        k_seg_b<<<mptg_blocks(total, tb), tb, 0, s>>>(cur, perm, pseg, pseg2, total, t->pts32, D, t->bpts,
-                                                      t->bids, t->seg_box);
-        k_seg_c<<<mptg_blocks(nseg, 128), 128, 0, s>>>(cur, nseg, prev, t->nodes, t->cell_lo, t->cell_hi,
-                                                       t->node_depth, t->dcnt, t->node_cap, t->seg_cap,
-                                                       t->seg_box, D, t->metric, (float)t->w0, (float)t->w1);
-        k_seg_d<<<mptg_blocks(total, tb), tb, 0, s>>>(cur, perm, pseg, perm2, pseg2, total, t->pts32, D);
-        ctx->launches += 4;
+        if (gs > 0) {
+            k_seg_a<<<mptg_blocks(gs, 128), 128, 0, s>>>(cur, nseg, prev, t->nodes, t->dcnt, t->bucket_cap,
+                                                         t->seg_box, D, t->seg_cap);
+            k_seg_b<<<mptg_blocks(gt, tb), tb, 0, s>>>(cur, perm, pseg, pseg2, total, t->pts32, D, t->bpts,
+                                                       t->bids, t->seg_box, t->dcnt, t->seg_cap);
+            k_seg_c<<<mptg_blocks(gs, 128), 128, 0, s>>>(cur, nseg, prev, t->nodes, t->cell_lo, t->cell_hi,
+                                                         t->node_depth, t->dcnt, t->node_cap, t->seg_cap,
+                                                         t->seg_box, D, t->metric, (float)t->w0, (float)t->w1);
+            k_seg_d<<<mptg_blocks(gt, tb), tb, 0, s>>>(cur, perm, pseg, perm2, pseg2, total, t->pts32, D, t->dcnt,
+                                                       t->seg_cap);
+            ctx->launches += 4;
+        }
         st = read_counters(t, s);
         if (st) return st;
+        if (pending) {
+            const int r = t->hcnt[CNT_NREG];
+            total = r <= t->seg_cap && r > 0 ? MPTG_BUCKET * r + t->hcnt[CNT_OVF] : 0;
+        }
         nseg = t->hcnt[CNT_NSEG_NEXT];
         if (nseg > t->seg_cap || (t->hcnt[CNT_ERR] & MPTG_DEVERR_CAPACITY))
             return mptg_fail(ctx, MPTG_ERR_CAPACITY, "kd-tree build ran out of node/segment capacity");
@@ -1587,22 +1627,42 @@ mptg_status mptg_tree_insert(mptg_tree* t, const double* states, size_t n, void*
     k_append<<<mptg_blocks(n, 256), 256, 0, s>>>(t->nodes, t->pts32, t->bpts, t->bids, first, nn, D, t->leaf_of,
                                                  t->dcnt, t->ovf_pts, t->ovf_leaf, t->leaf_reg);
     ctx->launches += 2;
-    mptg_status st = read_counters(t, s);
-    if (st) return st;
-    if (t->hcnt[CNT_ERR] & MPTG_DEVERR_BAD_STATE)
-        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG,
-                         "invalid state (NaN/inf, SO2 angle outside [-pi,pi], or non-unit quaternion)");
-    int nreg = t->hcnt[CNT_NREG];
-    int novf = t->hcnt[CNT_OVF];
-    if (nreg > 0) {
-        if (nreg > t->seg_cap) return mptg_fail(ctx, MPTG_ERR_CAPACITY, "too many overflowing leaves");
-        k_ovf_segs<<<mptg_blocks(nreg, 128), 128, 0, s>>>(t->nodes, t->bids, t->node_depth, nreg, t->ovf_leaf,
-                                                          t->dcnt, t->segA, t->perm, t->pseg, t->seg_cursor);
-        k_ovf_scatter<<<mptg_blocks(novf, 256), 256, 0, s>>>(novf, first, t->ovf_pts, t->leaf_of, t->leaf_reg,
-                                                             t->segA, t->seg_cursor, t->perm, t->pseg);
+    mptg_status st;
+    if (nn <= MPTG_INSERT_PENDING_MAX) {
+        // small batches (a planner's wavefront): the overflow segments and the
+        // first builder level are queued on the counts k_append leaves on the
+        // device, so the first counter read comes after that level
+        const int rb = std::min(nn, t->seg_cap);
+        k_ovf_segs<<<mptg_blocks(rb, 128), 128, 0, s>>>(t->nodes, t->bids, t->node_depth, -1, t->ovf_leaf, t->dcnt,
+                                                        t->segA, t->perm, t->pseg, t->seg_cursor, t->seg_cap);
+        k_ovf_scatter<<<mptg_blocks(nn, 256), 256, 0, s>>>(-1, first, t->ovf_pts, t->leaf_of, t->leaf_reg, t->segA,
+                                                           t->seg_cursor, t->perm, t->pseg, t->dcnt, t->seg_cap);
         ctx->launches += 2;
-        st = build_levels(t, s, nreg, MPTG_BUCKET * nreg + novf);
+        st = build_levels(t, s, -1, -1, rb, MPTG_BUCKET * rb + nn);
         if (st) return st;
+        if (t->hcnt[CNT_ERR] & MPTG_DEVERR_BAD_STATE)
+            return mptg_fail(ctx, MPTG_ERR_INVALID_ARG,
+                             "invalid state (NaN/inf, SO2 angle outside [-pi,pi], or non-unit quaternion)");
+    } else {
+        st = read_counters(t, s);
+        if (st) return st;
+        if (t->hcnt[CNT_ERR] & MPTG_DEVERR_BAD_STATE)
+            return mptg_fail(ctx, MPTG_ERR_INVALID_ARG,
+                             "invalid state (NaN/inf, SO2 angle outside [-pi,pi], or non-unit quaternion)");
+        int nreg = t->hcnt[CNT_NREG];
+        int novf = t->hcnt[CNT_OVF];
+        if (nreg > 0) {
+            if (nreg > t->seg_cap) return mptg_fail(ctx, MPTG_ERR_CAPACITY, "too many overflowing leaves");
+            k_ovf_segs<<<mptg_blocks(nreg, 128), 128, 0, s>>>(t->nodes, t->bids, t->node_depth, nreg, t->ovf_leaf,
+                                                              t->dcnt, t->segA, t->perm, t->pseg, t->seg_cursor,
+                                                              t->seg_cap);
+            k_ovf_scatter<<<mptg_blocks(novf, 256), 256, 0, s>>>(novf, first, t->ovf_pts, t->leaf_of, t->leaf_reg,
+                                                                 t->segA, t->seg_cursor, t->perm, t->pseg, t->dcnt,
+                                                                 t->seg_cap);
+            ctx->launches += 2;
+            st = build_levels(t, s, nreg, MPTG_BUCKET * nreg + novf);
+            if (st) return st;
+        }
     }
     MPTG_CUDA_TRY(ctx, cudaGetLastError());
     // hcnt is current: read after k_append, or after the builder's last level
