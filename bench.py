@@ -271,11 +271,9 @@ def _labelled_mesh_states(m, ctx, sc, n, seed):
     return q, y
 
 
-def learned_vs_plain(ctx, m, torch, seeds=5, cap_s=20.0, n_train=1 << 22, epochs=10, wavefront_tuned=None):
-    """Learned collision surrogate on the SE(3) scene: training throughput, held-out
-    FP/FN rates, scoring throughput against the bf16 tensor peak, and time to
-    solve with the surrogate culling edges versus the plain planner (same seeds)."""
-    from mpt_gb300 import planner as P
+def surrogate_rates(ctx, m, torch, n_train=1 << 22, epochs=10):
+    """Train the SE(3) collision surrogate on n_train labelled states and time
+    training and scoring: (results, trained surrogate, scene)."""
     from mpt_gb300 import scenes
     from mpt_gb300.surrogate import Surrogate, se3_normalisation
     sc = scenes.mesh_scene()
@@ -314,6 +312,14 @@ def learned_vs_plain(ctx, m, torch, seeds=5, cap_s=20.0, n_train=1 << 22, epochs
            "score_states_per_s": len(qt) / score_s,
            "score_tflops": flops_fwd * len(qt) / score_s / 1e12,
            "train_tflops": 3 * flops_fwd * n_train * epochs / train_s / 1e12}
+    return res, sg, sc
+
+
+def learned_vs_plain(ctx, m, torch, seeds=5, cap_s=20.0, n_train=1 << 22, epochs=10, wavefront_tuned=None):
+    """Learned collision surrogate on the SE(3) scene: training throughput, held-out
+    FP/FN rates, scoring throughput against the bf16 tensor peak, and time to
+    solve with the surrogate culling edges versus the plain planner (same seeds)."""
+    res, sg, sc = surrogate_rates(ctx, m, torch, n_train, epochs)
     # plain versus learned at the configured wavefront (4096) and at the
     # autotuned one for this scene, same seeds
     Ws = sorted({4096, int(wavefront_tuned or 4096)})
@@ -540,7 +546,7 @@ def run_gpu(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     ctx = m.Context(local)
-    if args.edges_only or args.solve_only or args.star_only or args.prm_only:
+    if args.edges_only or args.solve_only or args.star_only or args.prm_only or args.sg_only:
         # profiling modes: one secondary section alone
         if args.edges_only:
             out = {"edge_checks": edge_rates(ctx, m, torch.cuda.current_stream(), torch)}
@@ -548,6 +554,8 @@ def run_gpu(args):
             out = {"prrt_star": prrt_star_section(ctx)}
         elif args.prm_only:
             out = {"pprm": prm_section(ctx)}
+        elif args.sg_only:
+            out = {"surrogate": surrogate_rates(ctx, m, torch, n_train=1 << 18, epochs=1)[0]}
         else:
             out = {"time_to_solve": solve_times(ctx, seeds=args.solve_seeds)}
         out["gpu_launches"] = ctx.kernel_launches()
@@ -726,6 +734,8 @@ def main():
     ap.add_argument("--star-only", action="store_true", help="the PRRT* comparison only (profiling)")
     ap.add_argument("--no-prm", action="store_true", help="skip the PPRM roadmap run")
     ap.add_argument("--prm-only", action="store_true", help="the PPRM roadmap run only (profiling)")
+    ap.add_argument("--sg-only", action="store_true",
+                    help="surrogate training (262,144 states, 1 epoch) and scoring rates only (profiling)")
     ap.add_argument("--edges-only", action="store_true", help="edge checks/s of the three scenes only (profiling)")
     ap.add_argument("--solve-only", action="store_true", help="time to solve of the three scenes only (profiling)")
     ap.add_argument("--solve-seeds", type=int, default=5)
