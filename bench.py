@@ -219,16 +219,20 @@ def solve_times(ctx, seeds=5, cap_s=20.0, tune=True, cpu=True):
         dflt, fp = _solve_stats(ctx, sc, W, seeds, cap_s, want_path=True)
         r = {"default": dflt}
         if cpu:
-            # the oracle's replay of the same wavefront planner (identical tree, brute-force
-            # NN, all host cores) on the first seed: a CPU port of the same run
+            # the oracle's replay of the same wavefront planner (identical tree, all host
+            # cores; the exact kd-tree NN where it pays) on the first seed: a CPU port of the same run
             import oracle
             sp = oracle.make_space(sc["metric"], sc["dim"], sc["weights"])
             prm = {"range": sc["range"], "goal_bias": 0.01, "goal_radius": sc["goal_radius"],
                    "edge_step": sc["edge_step"], "resolution": sc["resolution"], "wavefront": W, "seed": 1000,
                    "max_nodes": 1 << 21}
-            t0 = time.perf_counter()
-            st, par, g = oracle.plan(sc, sp, prm, sc["lo"], sc["hi"], sc["start"], sc["goal"], 400, True)
-            cpu_s = time.perf_counter() - t0
+            oracle.set_plan_nn("auto")
+            try:
+                t0 = time.perf_counter()
+                st, par, g = oracle.plan(sc, sp, prm, sc["lo"], sc["hi"], sc["start"], sc["goal"], 400, True)
+                cpu_s = time.perf_counter() - t0
+            finally:
+                oracle.set_plan_nn("brute")
             gpu_first = r["default"]["seed_times_s"][0]
             # the replay's best goal path (lowest cost, summed from the start) against the GPU's
             same_path = None
@@ -246,7 +250,8 @@ def solve_times(ctx, seeds=5, cap_s=20.0, tune=True, cpu=True):
                         best = (c, chain)
                 same_path = bool(len(best[1]) == len(fp[0]) and np.array_equal(st[best[1]], fp[0]) and
                                  abs(best[0] - fp[1]) <= 1e-12 * max(1.0, best[0]))
-            r["cpu_port_seed1000"] = {"kind": "port (oracle replay of the same wavefront planner, brute-force NN)",
+            r["cpu_port_seed1000"] = {"kind": "port (oracle replay of the same wavefront planner; exact CPU "
+                                              "kd-tree NN up to 7 dimensions, brute force above)",
                                       "cores": os.cpu_count(), "wavefront": W, "s": cpu_s, "solved": len(g) > 0,
                                       "nodes": len(st), "gpu_same_seed_s": gpu_first,
                                       "ratio": cpu_s / gpu_first if gpu_first else None,

@@ -265,6 +265,17 @@ def plan(desc: dict, space: Space, params: dict, lo, hi, start, goal, max_waves:
     return states[:n].copy(), parents[:n].copy(), goals[:ng.value].copy()
 
 
+def set_plan_nn(mode):
+    """Nearest-neighbour search of the planner replays: "brute" (or False; the
+    definition, the default), "kdtree" (or True; the exact kd-tree, same
+    answers) or "auto" (the kd-tree up to 7 dimensions), for CPU timing runs."""
+    code = {False: 0, True: 1, "brute": 0, "kdtree": 1, "auto": 2}[mode]
+    L = lib()
+    L.orc_set_plan_nn.restype = None
+    L.orc_set_plan_nn.argtypes = [ctypes.c_int]
+    L.orc_set_plan_nn(code)
+
+
 def plan_star(desc: dict, space: Space, params: dict, lo, hi, start, goal, max_waves: int, rewire_factor: float = 1.1,
               nthreads: int = 0):
     """Replay of the wavefront PRRT* planner: (states, parents, costs, goal ids, rewires)."""

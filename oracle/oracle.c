@@ -810,19 +810,35 @@ static void plan_sample(const orc_space* sp, const orc_plan_params* pp, const do
  * node par[i] among the first n states, the steered new state nw[i] and
  * ok[i] = valid(new) && link(near, new), all against the tree as it stood
  * before the wavefront. */
+/* Nearest-neighbour search of the replays: 0 the brute-force scan (the
+ * definition), 1 the exact kd-tree above built over the tree's states once
+ * per wavefront -- the same (distance, lowest id) answer -- or 2 the kd-tree
+ * up to 7 dimensions and the scan above (where a per-wavefront kd-tree does
+ * not pay), for CPU timing runs of the planner. */
+static int g_plan_kd = 0;
+void orc_set_plan_nn(int mode) { g_plan_kd = mode; }
+
 static void plan_wave(const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp, const double* lo,
                       const double* hi, const double* goal, int goal_index, int w, double range, double inv,
                       const double* states, int64_t n, double* nw, int32_t* par, uint8_t* ok, int nthreads) {
     const int D = sp->dim, W = pp->wavefront;
+    const int use_kd = g_plan_kd == 1 || (g_plan_kd == 2 && D <= 7);
+    kd_tree* kd = (use_kd && n > 0) ? (kd_tree*)orc_kd_build(sp, states, n, 8) : NULL;
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads_or_default(nthreads))
     for (int i = 0; i < W; ++i) {
         double s[16], a[16];
         plan_sample(sp, pp, lo, hi, goal, goal_index, (uint32_t)i, (uint32_t)w, s);
         double best = INFINITY;
         int32_t bi = -1;
-        for (int64_t j = 0; j < n; ++j) {
-            double dj = orc_distance(sp, s, states + j * D);
-            if (dj < best || (bi < 0 && dj == best)) { best = dj; bi = (int32_t)j; }
+        if (kd) {
+            kd_result r = {INFINITY, INT32_MAX, 0};
+            kd_search(kd, 0, s, &r);
+            if (r.idx != INT32_MAX) { best = r.best; bi = r.idx; }
+        } else {
+            for (int64_t j = 0; j < n; ++j) {
+                double dj = orc_distance(sp, s, states + j * D);
+                if (dj < best || (bi < 0 && dj == best)) { best = dj; bi = (int32_t)j; }
+            }
         }
         ok[i] = 0;
         if (bi < 0 || best == 0.0 || best != best) continue;
@@ -833,6 +849,7 @@ static void plan_wave(const orc_scene* sc, const orc_space* sp, const orc_plan_p
         par[i] = bi;
         ok[i] = (uint8_t)dmv_edge(sc, sp, a, q, inv, pp->resolution, NULL);
     }
+    if (kd) orc_kd_free(kd);
 }
 
 int64_t orc_plan(const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp, const double* lo,

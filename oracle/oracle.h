@@ -66,6 +66,10 @@ typedef struct {
     int64_t max_nodes;
 } orc_plan_params;
 double orc_uniform(uint64_t seed, uint32_t i, uint32_t w, uint32_t j);
+/* nearest-neighbour search of the replays: 0 brute force (default), 1 the
+ * exact kd-tree, 2 the kd-tree up to 7 dimensions (same answers; for CPU
+ * timing runs) */
+void orc_set_plan_nn(int mode);
 int64_t orc_plan(const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp, const double* lo,
                  const double* hi, const double* start, const double* goal, int max_waves, int stop_when_solved,
                  double* states, int32_t* parents, int32_t* goals, int64_t* ngoals, int nthreads);

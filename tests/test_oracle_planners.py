@@ -62,3 +62,21 @@ def test_prrt_star_replay_costs_are_path_lengths(orc):
 
     for x in sel[:: max(1, len(sel) // 100)]:
         assert costs[x] <= cost0(x) * (1 + 1e-12)
+
+
+def test_replay_kdtree_nn_equals_brute_force(orc):
+    """The kd-tree option of the replays (used to time the CPU planner) builds
+    the same trees as the brute-force definition."""
+    for mk, W, waves in ((scenes.grid_scene, 512, 8), (scenes.arm_scene, 1024, 3), (scenes.mesh_scene, 128, 3)):
+        sc = mk()
+        sp = orc.make_space(sc["metric"], sc["dim"], sc["weights"])
+        p = _params(sc, W, 5)
+        try:
+            orc.set_plan_nn(True)
+            a = orc.plan(sc, sp, p, sc["lo"], sc["hi"], sc["start"], sc["goal"], waves, False)
+        finally:
+            orc.set_plan_nn(False)
+        b = orc.plan(sc, sp, p, sc["lo"], sc["hi"], sc["start"], sc["goal"], waves, False)
+        assert len(a[0]) == len(b[0]) > 20
+        assert np.array_equal(a[0].view(np.int64), b[0].view(np.int64))
+        assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
