@@ -67,3 +67,26 @@ def test_two_gloo_ranks_time_and_rate():
     assert t0 == t1 == 150.0
     assert rate0 == rate1 == 2 * 65536 * 10 / 0.15
     assert printed1 == ""
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+    """`bench.py --impl reference` on rank 0: one JSON line with the contract's keys,
+    the reference marker, and an e2e without device copies (a smaller tree here)."""
+    import json
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.setattr(bench, "N_TREE", 20000)
+    monkeypatch.setattr(bench, "BATCH", 4096)
+    for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+
+    class Args:
+        gpus, steps, warmup = 1, 2, 1
+    bench.run_reference(Args())
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
