@@ -1,0 +1,25 @@
+"""CPU: the Planner mirror's option packs and dispatch (src/mpt/prrt.hpp:56-82,
+src/mpt/prrt_star.hpp:56-95, src/mpt/pprm.hpp:56-84, src/mpt/planner_tags.hpp):
+options in any order, thread-count tags accepted, unknown options rejected, and
+Planner(scenario, PPRM(...)) building the roadmap planner."""
+import pytest
+
+from mpt_gb300 import planner as P
+
+
+def test_option_order_and_tags():
+    a = P.PRRT(P.gpu_wavefront(1024), P.report_stats(True), P.max_threads(8))
+    b = P.PRRT(P.max_threads(1), P.report_stats(True), P.gpu_wavefront(1024))
+    assert a == b and a.wavefront == 1024 and a.report_stats
+    assert P.PRRT().wavefront == 4096 and not P.PRRT().report_stats
+    assert P.PRRTStar.rewire and not P.PRRT.rewire
+    assert isinstance(P.PPRM(P.gpu_wavefront(512)), P.PRRT) and P.PPRM(P.gpu_wavefront(512)).wavefront == 512
+    with pytest.raises(TypeError):
+        P.PRRT("unknown option")
+
+
+def test_planner_dispatches_pprm():
+    obj = P.Planner.__new__(P.Planner, None, P.PPRM())
+    assert type(obj) is P.PPRMPlanner
+    assert type(P.Planner.__new__(P.Planner, None, P.PRRTStar())) is P.Planner
+    assert type(P.Planner.__new__(P.Planner, None, None)) is P.Planner
