@@ -123,29 +123,37 @@ def load_obj(path: str, shift_to_center: bool = False):
     negative (relative) indices; every object and group of the file is one
     mesh.  The center is the mean of the distinct vertex positions the faces
     use (assimp's JoinIdenticalVertices keeps each position once)."""
-    verts = []
-    faces = []
     with open(path, "r") as f:
-        for line in f:
-            if line.startswith("v "):
-                p = line.split()
-                verts.append((float(p[1]), float(p[2]), float(p[3])))
-            elif line.startswith("f "):
-                idx = []
-                for tok in line.split()[1:]:
-                    i = int(tok.split("/")[0])
-                    idx.append(i - 1 if i > 0 else len(verts) + i)
-                faces.append(idx)
-    if not faces:
+        lines = f.read().splitlines()
+    vlines = [ln[2:] for ln in lines if ln.startswith("v ")]
+    flines = [ln[2:] for ln in lines if ln.startswith("f ")]
+    if not flines:
         raise ValueError("mesh file '%s' does not contain meshes" % path)
-    V = np.asarray(verts, dtype=np.float64).reshape(-1, 3)
-    tri = []
-    for idx in faces:
-        if len(idx) < 3:
-            continue
-        for k in range(1, len(idx) - 1):  # fan around the first vertex
-            tri.append((idx[0], idx[k], idx[k + 1]))
-    T = np.asarray(tri, dtype=np.int64).reshape(-1, 3)
+    # fast paths for the common layout (three coordinates per vertex, triangles
+    # of positive plain indices); anything else goes line by line
+    if all(len(ln.split()) == 3 for ln in vlines):
+        V = np.array(" ".join(vlines).split(), dtype=np.float64).reshape(-1, 3)
+    else:
+        V = np.array([[float(x) for x in ln.split()[:3]] for ln in vlines], dtype=np.float64).reshape(-1, 3)
+    T = None
+    if all(len(ln.split()) == 3 for ln in flines):
+        ft = " ".join(flines).split()
+        if all(c.isdigit() for c in ft):
+            T = np.array(ft, dtype=np.int64).reshape(-1, 3) - 1
+    if T is None:
+        tri = []
+        nv = 0
+        for ln in lines:  # relative indices count the vertices read so far
+            if ln.startswith("v "):
+                nv += 1
+            elif ln.startswith("f "):
+                idx = []
+                for tok in ln.split()[1:]:
+                    i = int(tok.split("/")[0])
+                    idx.append(i - 1 if i > 0 else nv + i)
+                for k in range(1, len(idx) - 1):  # fan around the first vertex; < 3 indices: skipped
+                    tri.append((idx[0], idx[k], idx[k + 1]))
+        T = np.asarray(tri, dtype=np.int64).reshape(-1, 3)
     if T.size and (T.min() < 0 or T.max() >= len(V)):
         raise ValueError("mesh file '%s' has a face index out of range" % path)
     used = np.unique(V[np.unique(T)], axis=0) if T.size else V[:0]
