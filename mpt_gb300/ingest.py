@@ -17,7 +17,7 @@ reference's demos, turned into the scene dictionaries of mpt_gb300.scenes.
   palette expanded to RGB, 16-bit samples reduced to 8, sub-byte depths
   unpacked, alpha dropped; a pixel is an obstacle when some FilterColor
   (r, g, b, tol) holds every channel within tol (:50-69).  PNG is decoded
-  with zlib (non-interlaced images); Netpbm P1-P6 is read directly.
+  with zlib (plain and Adam7-interlaced images); Netpbm P1-P6 is read directly.
 * ``se3_problem`` / ``png_grid_scene``: the scenarios of
   demo/se3_rigid_body_planning.cpp:237-281 and demo/png_2d_planning.cpp:60-90
   as scene dictionaries (see each docstring for the parameters they fix).
@@ -174,6 +174,35 @@ def write_obj(path: str, tris: np.ndarray):
 
 
 # ------------------------------------------------------------------ images
+def _png_samples(raw: np.ndarray, w: int, h: int, depth: int, ctype: int):
+    """8-bit samples [h][w * channels] of one (sub-)image of filtered scanlines
+    at the start of raw, and the number of bytes it took."""
+    chans = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+    bits = depth * chans
+    stride = (w * bits + 7) // 8
+    bpp = max(1, bits // 8)
+    need = h * (stride + 1)
+    if len(raw) < need:
+        raise ValueError("truncated PNG image data")
+    out = np.empty((h, stride), dtype=np.uint8)
+    lib = load()
+    lib.mptg_png_unfilter.restype = ctypes.c_int
+    lib.mptg_png_unfilter.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    rows = np.ascontiguousarray(raw[:need])
+    if lib.mptg_png_unfilter(rows.ctypes.data, h, stride, bpp, out.ctypes.data) != 0:
+        raise ValueError("PNG row with an unknown filter type")
+    if depth == 16:
+        px = out.reshape(h, w * chans, 2)[:, :, 0]  # strip to the high byte
+    elif depth < 8:
+        px = np.unpackbits(out, axis=1).reshape(h, -1, depth)[:, :w * chans]
+        px = (px * (1 << np.arange(depth - 1, -1, -1))).sum(axis=2).astype(np.uint8)
+        if ctype == 0:
+            px = (px * (255 // ((1 << depth) - 1))).astype(np.uint8)
+    else:
+        px = out[:, :w * chans]
+    return px, need
+
+
 def _png_rgb(data: bytes) -> np.ndarray:
     if data[:8] != b"\x89PNG\r\n\x1a\n":
         raise ValueError("not a PNG file")
@@ -193,31 +222,22 @@ def _png_rgb(data: bytes) -> np.ndarray:
     if hdr is None:
         raise ValueError("PNG without IHDR")
     w, h, depth, ctype, _, _, interlace = hdr
-    if interlace:
-        raise ValueError("interlaced PNG is not supported")
     chans = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
-    bits = depth * chans
-    stride = (w * bits + 7) // 8
-    bpp = max(1, bits // 8)
     raw = np.frombuffer(zlib.decompress(b"".join(idat)), dtype=np.uint8)
-    if len(raw) < h * (stride + 1):
-        raise ValueError("truncated PNG image data")
-    out = np.empty((h, stride), dtype=np.uint8)
-    lib = load()
-    lib.mptg_png_unfilter.restype = ctypes.c_int
-    lib.mptg_png_unfilter.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
-    raw = np.ascontiguousarray(raw[:h * (stride + 1)])
-    if lib.mptg_png_unfilter(raw.ctypes.data, h, stride, bpp, out.ctypes.data) != 0:
-        raise ValueError("PNG row with an unknown filter type")
-    if depth == 16:
-        px = out.reshape(h, w * chans, 2)[:, :, 0]  # strip to the high byte
-    elif depth < 8:
-        px = np.unpackbits(out, axis=1).reshape(h, -1, depth)[:, :w * chans]
-        px = (px * (1 << np.arange(depth - 1, -1, -1))).sum(axis=2).astype(np.uint8)
-        if ctype == 0:
-            px = (px * (255 // ((1 << depth) - 1))).astype(np.uint8)
+    if not interlace:
+        px, _ = _png_samples(raw, w, h, depth, ctype)
     else:
-        px = out[:, :w * chans]
+        # Adam7: seven passes of sub-images, each filtered on its own
+        px = np.zeros((h, w, chans), dtype=np.uint8)
+        off = 0
+        for x0, y0, dx, dy in ((0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2),
+                               (0, 1, 1, 2)):
+            pw, ph = (w - x0 + dx - 1) // dx, (h - y0 + dy - 1) // dy
+            if pw <= 0 or ph <= 0:
+                continue
+            sub, used = _png_samples(raw[off:], pw, ph, depth, ctype)
+            px[y0::dy, x0::dx] = sub.reshape(ph, pw, chans)
+            off += used
     px = px.reshape(h, w, chans)
     if ctype == 3:
         return plte[px[:, :, 0]]

@@ -20,10 +20,9 @@ def _paeth(a, b, c):
     return a if pa <= pb and pa <= pc else (b if pb <= pc else c)
 
 
-def _png(path, rows: np.ndarray, ctype: int, depth: int, palette=None, width=None):
-    """rows: [h][stride] packed sample bytes; filter type y % 5 on row y."""
+def _filtered(rows: np.ndarray, bpp: int) -> bytes:
+    """PNG scanlines of rows [h][stride], filter type y % 5 on row y."""
     h, stride = rows.shape
-    bpp = max(1, {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype] * depth // 8)
     raw = bytearray()
     prev = np.zeros(stride, dtype=np.int64)
     for y in range(h):
@@ -39,17 +38,48 @@ def _png(path, rows: np.ndarray, ctype: int, depth: int, palette=None, width=Non
         raw.append(ft)
         raw += bytes(out.astype(np.uint8))
         prev = cur
+    return bytes(raw)
 
+
+def _write_png(path, w, h, ctype, depth, raw: bytes, palette=None, interlace=0):
     def chunk(kind, body):
         return struct.pack(">I", len(body)) + kind + body + struct.pack(">I", zlib.crc32(kind + body) & 0xFFFFFFFF)
 
-    w = width if width is not None else stride * 8 // (depth * {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype])
-    data = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, 0))
+    data = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, interlace))
     if palette is not None:
         data += chunk(b"PLTE", bytes(np.asarray(palette, dtype=np.uint8).ravel()))
-    data += chunk(b"IDAT", zlib.compress(bytes(raw))) + chunk(b"IEND", b"")
+    data += chunk(b"IDAT", zlib.compress(raw)) + chunk(b"IEND", b"")
     with open(path, "wb") as f:
         f.write(data)
+
+
+def _png(path, rows: np.ndarray, ctype: int, depth: int, palette=None, width=None):
+    """rows: [h][stride] packed sample bytes; filter type y % 5 on row y."""
+    h, stride = rows.shape
+    chans = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+    bpp = max(1, chans * depth // 8)
+    w = width if width is not None else stride * 8 // (depth * chans)
+    _write_png(path, w, h, ctype, depth, _filtered(rows, bpp), palette)
+
+
+ADAM7 = ((0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2))
+
+
+def _png_adam7(path, px: np.ndarray, ctype: int, depth: int):
+    """px: [h][w][channels] samples (8-bit, or 0/1 for depth 1); Adam7 order,
+    each pass's scanlines filtered on their own (empty passes omitted)."""
+    h, w, chans = px.shape
+    bpp = max(1, chans * depth // 8)
+    raw = b""
+    for x0, y0, dx, dy in ADAM7:
+        sub = px[y0::dy, x0::dx]
+        if sub.size == 0:
+            continue
+        rows = sub.reshape(sub.shape[0], -1).astype(np.uint8)
+        if depth == 1:
+            rows = np.packbits(rows, axis=1)
+        raw += _filtered(rows, bpp)
+    _write_png(path, w, h, ctype, depth, raw, interlace=1)
 
 
 def test_png_color_types_and_filters(tmp_path):
@@ -78,6 +108,18 @@ def test_png_color_types_and_filters(tmp_path):
     bits = rng.integers(0, 2, (5, 11), dtype=np.uint8)
     _png(p, np.packbits(bits, axis=1), 0, 1, width=11)
     assert np.array_equal(ingest.read_image(p)[:, :, 0], bits * 255)
+
+
+@pytest.mark.parametrize("h,w", [(1, 1), (3, 2), (5, 9), (17, 13), (8, 8)])
+def test_png_adam7_interlaced(tmp_path, h, w):
+    rng = np.random.default_rng(h * 100 + w)
+    p = str(tmp_path / "i.png")
+    rgb = rng.integers(0, 256, (h, w, 3), dtype=np.uint8)
+    _png_adam7(p, rgb, 2, 8)
+    assert np.array_equal(ingest.read_image(p), rgb)
+    bits = rng.integers(0, 2, (h, w, 1), dtype=np.uint8)
+    _png_adam7(p, bits, 0, 1)
+    assert np.array_equal(ingest.read_image(p)[:, :, 0], bits[:, :, 0] * 255)
 
 
 def test_pnm_formats(tmp_path):
