@@ -7,7 +7,7 @@ oracle/_ref/libref.so.  Only possible where the reference sources exist; the
 tests that use it skip otherwise.  Recipe (what build() runs):
 
   gcc -O2 -ffp-contract=off -fPIC -c oracle/oracle.c -o oracle/_ref/oracle.o
-  g++ -O2 -ffp-contract=off -std=c++17 -DNDEBUG -fPIC -shared \
+  g++ -O2 -ffp-contract=off -std=c++17 -DNDEBUG -DMPT_LOG_LEVEL=WARN -Wno-attributes -fPIC -shared -fopenmp \
       -I oracle/ref/shim -I <reference>/src oracle/ref/ref_driver.cpp \
       oracle/_ref/oracle.o -o oracle/_ref/libref.so
 """
@@ -32,6 +32,8 @@ def build_if_available(force: bool = False):
     if not available():
         return None
     srcs = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(ORACLE, "oracle.c"), os.path.join(ORACLE, "oracle.h")]
+    for d, _, files in os.walk(os.path.join(HERE, "shim")):
+        srcs += [os.path.join(d, f) for f in files]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(s) <= os.path.getmtime(LIB) for s in srcs):
         return LIB
     os.makedirs(OUT, exist_ok=True)
@@ -39,7 +41,8 @@ def build_if_available(force: bool = False):
     subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-std=c11", "-c",
                            os.path.join(ORACLE, "oracle.c"), "-o", obj])
     tmp = LIB + ".tmp%d" % os.getpid()
-    subprocess.check_call(["g++", "-O2", "-ffp-contract=off", "-std=c++17", "-DNDEBUG", "-fPIC", "-shared",
+    subprocess.check_call(["g++", "-O2", "-ffp-contract=off", "-std=c++17", "-DNDEBUG", "-DMPT_LOG_LEVEL=WARN",
+                           "-Wno-attributes", "-fPIC", "-shared",
                            "-fopenmp", "-I", os.path.join(HERE, "shim"), "-I", REFERENCE_SRC,
                            os.path.join(HERE, "ref_driver.cpp"), obj, "-o", tmp, "-lm"])
     os.replace(tmp, LIB)
@@ -60,5 +63,48 @@ def lib():
         L.ref_dmv_edges.argtypes = [P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_longlong, ctypes.c_double, P, P]
         L.ref_interpolate.argtypes = [ctypes.c_int, ctypes.c_int, P, P, ctypes.c_double, P]
         L.ref_goal_l2.argtypes = [P, ctypes.c_double, P, P]
+        D = ctypes.c_double
+        L.ref_plan_solve.restype = ctypes.c_int
+        L.ref_plan_solve.argtypes = [ctypes.c_int, P, P, P, P, P, P, D, D, D, D, ctypes.c_int, ctypes.c_ulonglong,
+                                     ctypes.c_int, D, P, ctypes.c_int, P, P, P, P]
         _lib = L
     return _lib
+
+
+PLANNERS = {"prrt": 0, "prrt_star": 1, "pprm": 2}
+
+
+def plan_solve(desc: dict, seed: int, algo: str = "prrt", threads: int = 1, time_limit_s: float = 30.0,
+               goal_bias: float = 0.01, path_cap: int = 100000):
+    """One of the reference's own planners -- PRRT (src/mpt/prrt.hpp), PRRT*
+    with k-nearest rewiring (src/mpt/prrt_star.hpp) or PPRM (src/mpt/pprm.hpp)
+    -- on a scene dict of mpt_gb300.scenes (grid, planar arm or rigid mesh):
+    the oracle's valid(), the reference's DMV (or the joint-step edge check of
+    arm scenes) as link(), GoalState, setRange(range) and setGoalBias (PRRT and
+    PRRT*), uniform samples in [lo, hi] (uniform rotations for SE(3)), the goal
+    added with addGoal (PPRM).  Until the first solution or the time limit;
+    threads 1 runs the single_threaded variant, 0 the OpenMP worker pool.
+
+    Returns dict(solved, path [m][D], nodes, solve_s, cost)."""
+    import numpy as np
+
+    from oracle import _ptr, make_scene, make_space
+
+    L = lib()
+    sc, keep = make_scene(desc)
+    sp = make_space(int(desc["metric"]), int(desc["dim"]), desc.get("weights", (1.0, 1.0)))
+    D = int(desc["dim"])
+    arrs = [np.ascontiguousarray(desc[k], dtype=np.float64) for k in ("lo", "hi", "start", "goal")]
+    path = np.empty((path_cap, D), dtype=np.float64)
+    plen = ctypes.c_int(0)
+    nodes = ctypes.c_longlong(0)
+    secs = ctypes.c_double(0)
+    cost = ctypes.c_double(0)
+    r = L.ref_plan_solve(PLANNERS[algo], ctypes.byref(sc), ctypes.byref(sp), *[_ptr(a) for a in arrs],
+                         float(desc["goal_radius"]), float(desc["range"]), float(goal_bias), float(desc["edge_step"]),
+                         int(desc["resolution"]), int(seed), int(threads), float(time_limit_s), _ptr(path), path_cap,
+                         ctypes.byref(plen), ctypes.byref(nodes), ctypes.byref(secs), ctypes.byref(cost))
+    if r < 0:
+        raise ValueError("no reference planner instantiation for metric %s dim %d" % (desc["metric"], D))
+    return {"solved": bool(r), "path": path[:min(plen.value, path_cap)].copy(), "nodes": nodes.value,
+            "solve_s": secs.value, "cost": cost.value}

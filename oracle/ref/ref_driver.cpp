@@ -7,16 +7,28 @@
 //   src/mpt/lp_space.hpp, so2_space.hpp, so3_space.hpp    interpolate()
 //   src/mpt/discrete_motion_validator.hpp                 DMV bisection
 //   src/mpt/goal_state.hpp                                GoalState
+//   src/mpt/prrt.hpp, prrt_star.hpp, pprm.hpp (impl/)      the PRRT, PRRT* and PPRM planners
 // State validity comes from the oracle (orc_state_valid), so a mismatch
 // between ref_dmv_edges and orc_valid_edges isolates the DMV restatement.
+#include <omp.h>
+
 #include <array>
+#include <chrono>
+#include <cmath>
 #include <cstdint>
+#include <random>
+#include <tuple>
+#include <type_traits>
+#include <vector>
 
 #include <mpt/lp_space.hpp>
 #include <mpt/so2_space.hpp>
 #include <mpt/so3_space.hpp>
 #include <mpt/goal_state.hpp>
 #include <mpt/discrete_motion_validator.hpp>
+#include <mpt/prrt.hpp>
+#include <mpt/prrt_star.hpp>
+#include <mpt/pprm.hpp>
 
 #include "../oracle.h"
 
@@ -59,6 +71,194 @@ void interp(const double* a, const double* b, double t, double* out) {
     for (std::size_t d = 0; d < D; ++d) out[d] = q[d];
 }
 
+// SE(3) states (x, y, z, w, px, py, pz) under the oracle's weighted metric
+// w0 * acos|q1.q2| + w1 * |p1 - p2| (cartesian_space.hpp:43-68 with SO3 and
+// L2 elements).  nigh's Cartesian space and MPT's SE3 state need Eigen, so
+// this project-written space stands in; its distance and interpolate are the
+// oracle's, reached by the reference's templates through argument-dependent
+// lookup.
+struct SE3Tag {};
+using SE3Space = nm::Space<std::array<double, 7>, SE3Tag>;
+
+}  // namespace
+
+namespace unc::robotics::nigh::metric {
+template <>
+struct Space<std::array<double, 7>, SE3Tag> {
+    using Type = std::array<double, 7>;
+    using Distance = double;
+    static constexpr int kDimensions = 7;
+    orc_space sp{3, 7, {2.0, 1.0}};
+    constexpr unsigned dimensions() const { return 7; }
+    Distance distance(const Type& a, const Type& b) const { return orc_distance(&sp, a.data(), b.data()); }
+};
+}  // namespace unc::robotics::nigh::metric
+
+namespace {
+
+std::array<double, 7> interpolate(const SE3Space& space, const std::array<double, 7>& a,
+                                  const std::array<double, 7>& b, double t) {
+    std::array<double, 7> q;
+    orc_interpolate(&space.sp, a.data(), b.data(), t, q.data());
+    return q;
+}
+
+// A SeedSequence that gives each generator seeded from it its own stream:
+// the planner seeds every worker's RNG from one seed object
+// (impl/prrt/prrt.hpp:341-344), in worker order.
+struct WorkerSeed {
+    using result_type = std::uint32_t;
+    std::uint64_t seed;
+    mutable std::uint32_t calls = 0;
+    template <class It>
+    void generate(It first, It last) const {
+        std::seed_seq seq{std::uint32_t(seed), std::uint32_t(seed >> 32), calls++};
+        seq.generate(first, last);
+    }
+};
+
+// A Scenario (the contract of impl/scenario_*.hpp) over an oracle scene: the
+// oracle's valid(), link() by the reference's DMV (resolution 0) or the
+// oracle's joint-step edge check (resolution 1), uniform samples in the box,
+// GoalState(radius, goal).
+template <class S, std::size_t D>
+struct OracleScenario {
+    using Space = S;
+    using State = std::array<double, D>;
+    const orc_scene* sc;
+    const orc_space* sp;
+    std::array<double, D> lo, hi;
+    double step;
+    int resolution;
+    Space space_;
+    mpt::GoalState<Space> goal_;
+
+    OracleScenario(const orc_scene* s, const orc_space* p, const double* l, const double* h, const double* g,
+                   double radius, double st, int res)
+        : sc(s), sp(p), step(st), resolution(res), space_(make_space(p)), goal_(radius, arr(g)) {
+        lo = arr(l);
+        hi = arr(h);
+    }
+    static Space make_space(const orc_space* p) {
+        Space s{};
+        if constexpr (std::is_same_v<Space, SE3Space>) s.sp = *p;
+        return s;
+    }
+    static State arr(const double* v) {
+        State q;
+        for (std::size_t d = 0; d < D; ++d) q[d] = v[d];
+        return q;
+    }
+    const Space& space() const { return space_; }
+    const mpt::GoalState<Space>& goal() const { return goal_; }
+    // uniform in the box, Shoemake's uniform rotation for SE(3)
+    // (impl/uniform_sampler_so3.hpp:55-68); handed to the planners through
+    // sampler() (impl/scenario_sampler.hpp, case 2)
+    struct BoxSampler {
+        std::array<double, D> lo, hi;
+        template <class RNG>
+        State operator()(RNG& rng) const {
+            State q;
+            std::size_t d0 = 0;
+            if constexpr (std::is_same_v<Space, SE3Space>) {
+                std::uniform_real_distribution<double> u01(0.0, 1.0);
+                double a = u01(rng), b = 2 * M_PI * u01(rng), c = 2 * M_PI * u01(rng);
+                double s1 = std::sqrt(1.0 - a), s2 = std::sqrt(a);
+                q[0] = s1 * std::sin(b);
+                q[1] = s1 * std::cos(b);
+                q[2] = s2 * std::sin(c);
+                q[3] = s2 * std::cos(c);
+                d0 = 4;
+            }
+            for (std::size_t d = d0; d < D; ++d) q[d] = std::uniform_real_distribution<double>(lo[d], hi[d])(rng);
+            return q;
+        }
+    };
+    BoxSampler sampler() const { return BoxSampler{lo, hi}; }
+    bool valid(const State& q) const { return orc_state_valid(sc, q.data()) != 0; }
+    bool link(const State& a, const State& b) const {
+        if (resolution == 0) {
+            long long cnt = 0;
+            mpt::DiscreteMotionValidator<Space, Validator<Space>> v(space_, step, sc, &cnt);
+            return v(a, b);
+        }
+        uint8_t ok = 0;
+        int64_t samples = 0;
+        orc_valid_edges(sc, sp, a.data(), b.data(), 1, step, resolution, &ok, &samples, 1);
+        return ok != 0;
+    }
+};
+
+template <class P, class State, class = void>
+struct has_add_goal : std::false_type {};
+template <class P, class State>
+struct has_add_goal<P, State, std::void_t<decltype(std::declval<P&>().addGoal(std::declval<State>()))>>
+    : std::true_type {};
+
+// addStart (and addGoal for PPRM), solve until the first solution or the time
+// limit, then the solution path and its cost in the space's metric
+template <class Planner, class Scen>
+int run_planner(Planner& planner, const Scen& scen, const double* start, const double* goal, double range,
+                double goal_bias, double time_limit_s, double* path, int path_cap, int* path_len, long long* nodes,
+                double* solve_s, double* cost) {
+    using State = typename Scen::State;
+    constexpr std::size_t D = std::tuple_size_v<State>;
+    if constexpr (!has_add_goal<Planner, State>::value) {
+        planner.setRange(range);
+        planner.setGoalBias(goal_bias);
+    }
+    planner.addStart(Scen::arr(start));
+    if constexpr (has_add_goal<Planner, State>::value) planner.addGoal(Scen::arr(goal));
+    auto t0 = std::chrono::steady_clock::now();
+    planner.solveFor([&] { return planner.solved(); },
+                     std::chrono::duration_cast<std::chrono::steady_clock::duration>(
+                         std::chrono::duration<double>(time_limit_s)));
+    *solve_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    *nodes = (long long)planner.size();
+    std::vector<State> sol = planner.solution();
+    *path_len = (int)sol.size();
+    *cost = 0;
+    for (std::size_t i = 0; i < sol.size(); ++i) {
+        if ((int)i < path_cap)
+            for (std::size_t d = 0; d < D; ++d) path[i * D + d] = sol[i][d];
+        if (i) *cost += scen.space().distance(sol[i - 1], sol[i]);
+    }
+    return planner.solved() ? 1 : 0;
+}
+
+// Alg1 / AlgN: the planner's single-threaded and OpenMP-pool variants
+template <class Space, std::size_t D, class Alg1, class AlgN>
+int plan_solve(const orc_scene* sc, const orc_space* sp, const double* lo, const double* hi, const double* start,
+               const double* goal, double goal_radius, double range, double goal_bias, double step, int resolution,
+               std::uint64_t seed, int threads, double time_limit_s, double* path, int path_cap, int* path_len,
+               long long* nodes, double* solve_s, double* cost) {
+    using Scen = OracleScenario<Space, D>;
+    Scen scen(sc, sp, lo, hi, goal, goal_radius, step, resolution);
+    WorkerSeed ws{seed};
+    orc_state_valid(sc, start);  // builds the oracle's mesh BVH before any worker thread reads it
+    if (threads == 1) {
+        mpt::Planner<Scen, Alg1> planner(scen, ws);
+        return run_planner(planner, scen, start, goal, range, goal_bias, time_limit_s, path, path_cap, path_len,
+                           nodes, solve_s, cost);
+    }
+    int saved = omp_get_max_threads();
+    if (threads > 0) omp_set_num_threads(threads);
+    mpt::Planner<Scen, AlgN> planner(scen, ws);
+    omp_set_num_threads(saved);
+    return run_planner(planner, scen, start, goal, range, goal_bias, time_limit_s, path, path_cap, path_len, nodes,
+                       solve_s, cost);
+}
+
+template <class Space, std::size_t D, class... A>
+int plan_algo(int algo, A... args) {
+    switch (algo) {
+    case 0: return plan_solve<Space, D, mpt::PRRT<mpt::single_threaded>, mpt::PRRT<>>(args...);
+    case 1: return plan_solve<Space, D, mpt::PRRTStar<mpt::single_threaded>, mpt::PRRTStar<>>(args...);
+    case 2: return plan_solve<Space, D, mpt::PPRM<mpt::single_threaded>, mpt::PPRM<>>(args...);
+    }
+    return -1;
+}
+
 }  // namespace
 
 extern "C" {
@@ -91,6 +291,35 @@ int ref_goal_l2(const double* goal, double radius, const double* q, double* dist
     auto r = g(S{}, std::array<double, 2>{q[0], q[1]});
     *dist_out = r.second;
     return r.first ? 1 : 0;
+}
+
+// One of the reference's own planners on an oracle scene, until the first
+// solution or time_limit_s.  algo 0: PRRT (src/mpt/prrt.hpp;
+// impl/prrt/prrt.hpp:149-316,358-452), 1: PRRT* with k-nearest rewiring
+// (src/mpt/prrt_star.hpp; impl/prrt_star/prrt_star.hpp), 2: PPRM
+// (src/mpt/pprm.hpp; impl/pprm/pprm.hpp, start and goal added, no range).
+// metric/dim: 0/2 (grid), 1/10 (planar arm) or 3/7 (SE(3) rigid body).
+// threads 1 = single_threaded, 0 = all OpenMP threads.  Returns 1 solved,
+// 0 not solved, -1 unsupported.  path receives up to path_cap waypoints;
+// *path_len is the full count.
+int ref_plan_solve(int algo, const orc_scene* sc, const orc_space* sp, const double* lo, const double* hi,
+                   const double* start, const double* goal, double goal_radius, double range, double goal_bias,
+                   double step, int resolution, unsigned long long seed, int threads, double time_limit_s,
+                   double* path, int path_cap, int* path_len, long long* nodes, double* solve_s, double* cost) {
+    std::uint64_t sd = seed;
+    if (sp->metric == 0 && sp->dim == 2)
+        return plan_algo<nm::Space<std::array<double, 2>, nm::LP<2>>, 2>(
+            algo, sc, sp, lo, hi, start, goal, goal_radius, range, goal_bias, step, resolution, sd, threads,
+            time_limit_s, path, path_cap, path_len, nodes, solve_s, cost);
+    if (sp->metric == 1 && sp->dim == 10)
+        return plan_algo<nm::Space<std::array<double, 10>, nm::SO2<1>>, 10>(
+            algo, sc, sp, lo, hi, start, goal, goal_radius, range, goal_bias, step, resolution, sd, threads,
+            time_limit_s, path, path_cap, path_len, nodes, solve_s, cost);
+    if (sp->metric == 3 && sp->dim == 7)
+        return plan_algo<SE3Space, 7>(algo, sc, sp, lo, hi, start, goal, goal_radius, range, goal_bias, step,
+                                      resolution, sd, threads, time_limit_s, path, path_cap, path_len, nodes,
+                                      solve_s, cost);
+    return -1;
 }
 
 }  // extern "C"

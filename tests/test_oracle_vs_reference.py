@@ -98,3 +98,51 @@ def test_goal_state(orc):
         dist = orc.distance(orc.make_space(0, 2), q, g)
         assert hit == int(dist <= r)
         assert d.value == (0.0 if dist <= r else dist - r)
+
+
+def _check_reference_solution(orc, sc, r, steered=True):
+    """The acceptance rules of test/planner_integration_test.hpp:219-291 on a
+    path from the reference's own planner, judged by the oracle's checker.
+    steered: every edge within the range (PRRT; PRRT* rewiring and PPRM link
+    k-nearest neighbours at any distance)."""
+    path = r["path"]
+    sp = orc.make_space(sc["metric"], sc["dim"])
+    assert r["solved"] and len(path) >= 2
+    assert np.array_equal(path[0], np.asarray(sc["start"], dtype=np.float64))  # the start, exactly
+    assert orc.distance(sp, path[-1], sc["goal"]) <= sc["goal_radius"]
+    assert orc.valid_states(sc, sp, path).all()
+    ok, _ = orc.valid_edges(sc, sp, path[:-1], path[1:], sc["edge_step"], sc["resolution"])
+    assert ok.all()
+    steps = np.array([orc.distance(sp, path[i], path[i + 1]) for i in range(len(path) - 1)])
+    assert not steered or (steps <= sc["range"] * (1 + 1e-12)).all()
+    assert abs(steps.sum() - r["cost"]) <= 1e-9 * r["cost"]
+
+
+@pytest.mark.parametrize("mk,seed,threads", [(scenes.grid_scene, 0, 1), (scenes.grid_scene, 1, 1),
+                                             (scenes.grid_scene, 2, 0), (scenes.arm_scene, 0, 1)])
+def test_reference_prrt_on_oracle_scenes(orc, mk, seed, threads):
+    """The reference's PRRT planner (src/mpt/prrt.hpp, impl/prrt/prrt.hpp),
+    compiled in place over the project-written nigh stand-in (exact brute-force
+    NN), plans on the oracle's scene definitions -- valid() from the oracle,
+    link() by the reference's DMV (grid) or the joint-step check (arm) -- and
+    the oracle's checker accepts every path it returns.  threads 0 runs the
+    reference's OpenMP worker pool with the concurrent NN container."""
+    sc = mk()
+    r = ref.plan_solve(sc, seed, threads=threads, time_limit_s=60.0)
+    _check_reference_solution(orc, sc, r)
+    assert r["nodes"] >= len(r["path"])
+
+
+@pytest.mark.parametrize("mk,algo", [(scenes.grid_scene, "prrt_star"), (scenes.grid_scene, "pprm"),
+                                     (scenes.arm_scene, "prrt_star"), (scenes.arm_scene, "pprm")])
+def test_reference_prrt_star_and_pprm_on_oracle_scenes(orc, mk, algo):
+    """The reference's PRRT* (src/mpt/prrt_star.hpp, k-nearest rewiring through
+    the stand-in's nearest(nbh, q, k)) and PPRM (src/mpt/pprm.hpp: start and
+    goal added, k-nearest roadmap, Dijkstra solution), single-threaded, on the
+    oracle's scene definitions: the oracle's checker accepts their paths."""
+    sc = mk()
+    r = ref.plan_solve(sc, 1000, algo=algo, threads=1, time_limit_s=60.0)
+    _check_reference_solution(orc, sc, r, steered=False)
+    if algo == "pprm":
+        sp = orc.make_space(sc["metric"], sc["dim"])
+        assert orc.distance(sp, r["path"][-1], sc["goal"]) == 0.0  # the goal added with addGoal
