@@ -806,10 +806,14 @@ static void plan_sample(const orc_space* sp, const orc_plan_params* pp, const do
     }
 }
 
-/* One wavefront's candidates (prrt.hpp:411-442): sample i, its nearest tree
- * node par[i] among the first n states, the steered new state nw[i] and
- * ok[i] = valid(new) && link(near, new), all against the tree as it stood
- * before the wavefront. */
+/* Sample i of wavefront w of the planners' sample stream, without goal bias
+ * (plan_sample); lets the reference's one-sample-at-a-time planners be fed
+ * the same states in the same order. */
+void orc_sample_state(const orc_space* sp, const orc_plan_params* pp, const double* lo, const double* hi,
+                      uint32_t i, uint32_t w, double* q) {
+    plan_sample(sp, pp, lo, hi, NULL, -1, i, w, q);
+}
+
 /* Nearest-neighbour search of the replays: 0 the brute-force scan (the
  * definition), 1 the exact kd-tree above built over the tree's states once
  * per wavefront -- the same (distance, lowest id) answer -- or 2 the kd-tree
@@ -818,6 +822,10 @@ static void plan_sample(const orc_space* sp, const orc_plan_params* pp, const do
 static int g_plan_kd = 0;
 void orc_set_plan_nn(int mode) { g_plan_kd = mode; }
 
+/* One wavefront's candidates (prrt.hpp:411-442): sample i, its nearest tree
+ * node par[i] among the first n states, the steered new state nw[i] and
+ * ok[i] = valid(new) && link(near, new), all against the tree as it stood
+ * before the wavefront. */
 static void plan_wave(const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp, const double* lo,
                       const double* hi, const double* goal, int goal_index, int w, double range, double inv,
                       const double* states, int64_t n, double* nw, int32_t* par, uint8_t* ok, int nthreads) {

@@ -66,6 +66,9 @@ typedef struct {
     int64_t max_nodes;
 } orc_plan_params;
 double orc_uniform(uint64_t seed, uint32_t i, uint32_t w, uint32_t j);
+/* sample i of wavefront w of the planners' sample stream (no goal bias) */
+void orc_sample_state(const orc_space* sp, const orc_plan_params* pp, const double* lo, const double* hi,
+                      uint32_t i, uint32_t w, double* q);
 /* nearest-neighbour search of the replays: 0 brute force (default), 1 the
  * exact kd-tree, 2 the kd-tree up to 7 dimensions (same answers; for CPU
  * timing runs) */

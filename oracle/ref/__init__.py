@@ -64,6 +64,9 @@ def lib():
         L.ref_interpolate.argtypes = [ctypes.c_int, ctypes.c_int, P, P, ctypes.c_double, P]
         L.ref_goal_l2.argtypes = [P, ctypes.c_double, P, P]
         D = ctypes.c_double
+        L.ref_stream_graph.restype = ctypes.c_int
+        L.ref_stream_graph.argtypes = [ctypes.c_int, P, P, P, P, P, P, P, ctypes.c_longlong, P, ctypes.c_longlong, P,
+                                       P, ctypes.c_longlong, P]
         L.ref_plan_solve.restype = ctypes.c_int
         L.ref_plan_solve.argtypes = [ctypes.c_int, P, P, P, P, P, P, D, D, D, D, ctypes.c_int, ctypes.c_ulonglong,
                                      ctypes.c_int, D, P, ctypes.c_int, P, P, P, P]
@@ -108,3 +111,41 @@ def plan_solve(desc: dict, seed: int, algo: str = "prrt", threads: int = 1, time
         raise ValueError("no reference planner instantiation for metric %s dim %d" % (desc["metric"], D))
     return {"solved": bool(r), "path": path[:min(plen.value, path_cap)].copy(), "nodes": nodes.value,
             "solve_s": secs.value, "cost": cost.value}
+
+
+def stream_graph(desc: dict, params: dict, algo: str, nsamples: int, vcap: int = 1 << 20, ecap: int = 1 << 22):
+    """The reference's own PRRT or PPRM, single-threaded, fed nsamples states
+    of the planners' sample stream (params["seed"], wavefront size
+    params["wavefront"]) instead of its RNG: PRRT from the scene's start with
+    setRange(params["range"]) and no goal bias; PPRM with the start and the goal
+    added first.  The graph through visitGraph: (vertex states [nv][D], edges
+    [ne][2][D] as (from, to) state pairs -- PRRT node -> parent, PPRM every edge
+    from both ends)."""
+    import numpy as np
+
+    from oracle import PlanParams, _ptr, make_scene, make_space
+
+    L = lib()
+    sc, keep = make_scene(desc)
+    sp = make_space(int(desc["metric"]), int(desc["dim"]), desc.get("weights", (1.0, 1.0)))
+    pp = PlanParams()
+    for k in ("range", "goal_bias", "goal_radius", "edge_step"):
+        setattr(pp, k, float(params[k]))
+    pp.resolution = int(params["resolution"])
+    pp.wavefront = int(params["wavefront"])
+    pp.seed = int(params["seed"])
+    pp.max_nodes = int(params["max_nodes"])
+    D = int(desc["dim"])
+    arrs = [np.ascontiguousarray(desc[k], dtype=np.float64) for k in ("lo", "hi", "start", "goal")]
+    v = np.empty((vcap, D), dtype=np.float64)
+    e = np.empty((ecap, 2, D), dtype=np.float64)
+    nv = ctypes.c_longlong(0)
+    ne = ctypes.c_longlong(0)
+    r = L.ref_stream_graph(PLANNERS[algo], ctypes.byref(sc), ctypes.byref(sp), ctypes.byref(pp),
+                           *[_ptr(a) for a in arrs], int(nsamples), _ptr(v), vcap, ctypes.byref(nv), _ptr(e), ecap,
+                           ctypes.byref(ne))
+    if r == -1:
+        raise ValueError("no reference stream instantiation for %s on metric %s dim %d" % (algo, desc["metric"], D))
+    if r == -2:
+        raise ValueError("vcap/ecap too small (%d vertices, %d edges)" % (nv.value, ne.value))
+    return v[:nv.value].copy(), e[:ne.value].copy()

@@ -15,6 +15,7 @@
 #include <array>
 #include <chrono>
 #include <cmath>
+#include <limits>
 #include <cstdint>
 #include <random>
 #include <tuple>
@@ -189,6 +190,99 @@ struct OracleScenario {
     }
 };
 
+// The planners' sample stream (orc_sample_state) as an MPT sampler: the c-th
+// call returns sample c % W of wavefront c / W and ignores the RNG, so the
+// reference's one-sample-at-a-time planners see the states the oracle's
+// replays draw, in the same order.  Single-threaded use only.
+template <std::size_t D>
+struct StreamSampler {
+    const orc_space* sp;
+    const orc_plan_params* pp;
+    const double* lo;
+    const double* hi;
+    std::uint64_t* count;
+    template <class RNG>
+    std::array<double, D> operator()(RNG&) const {
+        std::uint64_t c = (*count)++;
+        std::uint64_t W = std::uint64_t(pp->wavefront);
+        std::array<double, D> q;
+        orc_sample_state(sp, pp, lo, hi, std::uint32_t(c % W), std::uint32_t(c / W), q.data());
+        return q;
+    }
+};
+
+template <class S, std::size_t D>
+struct StreamScenario : OracleScenario<S, D> {
+    StreamSampler<D> stream;
+    StreamScenario(const OracleScenario<S, D>& base, const StreamSampler<D>& st)
+        : OracleScenario<S, D>(base), stream(st) {}
+    StreamSampler<D> sampler() const { return stream; }
+};
+
+// visitGraph visitor: vertex states, and one (from, to) state pair per edge
+template <std::size_t D>
+struct GraphCollector {
+    double* v;
+    long long vcap;
+    long long* nv;
+    double* e;
+    long long ecap;
+    long long* ne;
+    std::array<double, D> from{};
+    void vertex(const std::array<double, D>& q) {
+        if (*nv < vcap)
+            for (std::size_t d = 0; d < D; ++d) v[*nv * D + d] = q[d];
+        ++*nv;
+        from = q;
+    }
+    void edge(const std::array<double, D>& to) {
+        if (*ne < ecap)
+            for (std::size_t d = 0; d < D; ++d) {
+                e[*ne * 2 * D + d] = from[d];
+                e[*ne * 2 * D + D + d] = to[d];
+            }
+        ++*ne;
+    }
+};
+
+template <class S, std::size_t D>
+int stream_graph(int algo, const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp, const double* lo,
+                 const double* hi, const double* start, const double* goal, long long nsamples, double* v,
+                 long long vcap, long long* nv, double* e, long long ecap, long long* ne) {
+    OracleScenario<S, D> base(sc, sp, lo, hi, goal, pp->goal_radius, pp->edge_step, pp->resolution);
+    std::uint64_t count = 0;
+    StreamScenario<S, D> scen(base, StreamSampler<D>{sp, pp, lo, hi, &count});
+    orc_state_valid(sc, start);
+    auto done = [&] { return count >= std::uint64_t(nsamples); };
+    GraphCollector<D> out{v, vcap, nv, e, ecap, ne};
+    *nv = 0;
+    *ne = 0;
+    if (algo == 0) {
+        mpt::Planner<StreamScenario<S, D>, mpt::PRRT<mpt::single_threaded>> planner(scen, WorkerSeed{pp->seed});
+        planner.setRange(pp->range > 0 ? pp->range : std::numeric_limits<double>::infinity());
+        planner.setGoalBias(0);
+        planner.addStart(OracleScenario<S, D>::arr(start));
+        planner.solve(done);
+        planner.visitGraph(out);
+    } else if (algo == 1) {
+        mpt::Planner<StreamScenario<S, D>, mpt::PRRTStar<mpt::single_threaded>> planner(scen, WorkerSeed{pp->seed});
+        planner.setRange(pp->range > 0 ? pp->range : std::numeric_limits<double>::infinity());
+        planner.setGoalBias(0);
+        planner.addStart(OracleScenario<S, D>::arr(start));
+        planner.solve(done);
+        planner.visitGraph(out);
+    } else if (algo == 2) {
+        mpt::Planner<StreamScenario<S, D>, mpt::PPRM<mpt::single_threaded>> planner(scen, WorkerSeed{pp->seed});
+        planner.addStart(OracleScenario<S, D>::arr(start));
+        planner.addGoal(OracleScenario<S, D>::arr(goal));
+        planner.solve(done);
+        planner.visitGraph(out);
+    } else {
+        return -1;
+    }
+    return (*nv <= vcap && *ne <= ecap) ? 0 : -2;
+}
+
 template <class P, class State, class = void>
 struct has_add_goal : std::false_type {};
 template <class P, class State>
@@ -319,6 +413,28 @@ int ref_plan_solve(int algo, const orc_scene* sc, const orc_space* sp, const dou
         return plan_algo<SE3Space, 7>(algo, sc, sp, lo, hi, start, goal, goal_radius, range, goal_bias, step,
                                       resolution, sd, threads, time_limit_s, path, path_cap, path_len, nodes,
                                       solve_s, cost);
+    return -1;
+}
+
+// The reference's PRRT (algo 0) or PRRT* (algo 1; both with setRange(pp->range)
+// and goal bias 0) or PPRM (algo 2; start then goal added), single-threaded, fed nsamples states of
+// the planners' sample stream (StreamSampler, wavefront size pp->wavefront).
+// The graph comes back through visitGraph: *nv vertex states in v (D doubles
+// each) and *ne edges in e as (from state, to state) pairs (2D doubles each;
+// PRRT, PRRT*: node -> parent; PPRM: every roadmap edge from both of its ends).
+// Returns 0, -1 unsupported, -2 when vcap or ecap was too small.
+int ref_stream_graph(int algo, const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp,
+                     const double* lo, const double* hi, const double* start, const double* goal,
+                     long long nsamples, double* v, long long vcap, long long* nv, double* e, long long ecap,
+                     long long* ne) {
+    if (sp->metric == 0 && sp->dim == 2)
+        return stream_graph<nm::Space<std::array<double, 2>, nm::LP<2>>, 2>(algo, sc, sp, pp, lo, hi, start, goal,
+                                                                           nsamples, v, vcap, nv, e, ecap, ne);
+    if (sp->metric == 1 && sp->dim == 10)
+        return stream_graph<nm::Space<std::array<double, 10>, nm::SO2<1>>, 10>(
+            algo, sc, sp, pp, lo, hi, start, goal, nsamples, v, vcap, nv, e, ecap, ne);
+    if (sp->metric == 3 && sp->dim == 7)
+        return stream_graph<SE3Space, 7>(algo, sc, sp, pp, lo, hi, start, goal, nsamples, v, vcap, nv, e, ecap, ne);
     return -1;
 }
 

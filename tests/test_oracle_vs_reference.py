@@ -146,3 +146,104 @@ def test_reference_prrt_star_and_pprm_on_oracle_scenes(orc, mk, algo):
     if algo == "pprm":
         sp = orc.make_space(sc["metric"], sc["dim"])
         assert orc.distance(sp, r["path"][-1], sc["goal"]) == 0.0  # the goal added with addGoal
+
+
+def _stream_params(sc, W, seed, max_nodes=1 << 16):
+    return {"range": sc["range"], "goal_bias": 0.0, "goal_radius": sc["goal_radius"], "edge_step": sc["edge_step"],
+            "resolution": sc["resolution"], "wavefront": W, "seed": seed, "max_nodes": max_nodes}
+
+
+def _ids(states):
+    ids = {s.tobytes(): i for i, s in enumerate(states)}
+    assert len(ids) == len(states)
+    return ids
+
+
+@pytest.mark.parametrize("mk,nsamples", [(scenes.grid_scene, 3000), (scenes.arm_scene, 1500),
+                                         (scenes.mesh_scene, 300)])
+def test_reference_prrt_on_the_sample_stream_equals_the_replay(orc, mk, nsamples):
+    """Fed the planners' sample stream one state at a time (goal bias 0), the
+    reference's own PRRT (impl/prrt/prrt.hpp:411-452) grows exactly the tree of
+    the oracle's replay at wavefront size 1: the same states bit for bit, each
+    with the same parent.  (SE(3) interpolation in the reference build is the
+    oracle's: MPT's Cartesian interpolate needs Eigen.)"""
+    sc = mk()
+    sp = orc.make_space(sc["metric"], sc["dim"], sc["weights"])
+    p = _stream_params(sc, 1, 11, nsamples + 1)
+    st, par, _ = orc.plan(sc, sp, p, sc["lo"], sc["hi"], sc["start"], sc["goal"], nsamples, False)
+    V, E = ref.stream_graph(sc, p, "prrt", nsamples)
+    ids = _ids(st)
+    assert len(st) > 50
+    assert {v.tobytes() for v in V} == set(ids) and len(V) == len(st)
+    assert {(ids[a.tobytes()], ids[b.tobytes()]) for a, b in E} == {(i, int(par[i])) for i in range(1, len(st))}
+
+
+@pytest.mark.parametrize("mk,nsamples", [(scenes.grid_scene, 2000), (scenes.arm_scene, 1000)])
+def test_reference_prrt_star_on_the_sample_stream_equals_the_replay(orc, mk, nsamples):
+    """The reference's PRRT* (impl/prrt_star/prrt_star.hpp:505-657, k-nearest
+    rewiring, factor 1.1) on the sample stream against the oracle's PRRT* replay
+    at wavefront size 1: the same states, and on the grid the same parent for
+    every node.  Parents may differ only where two candidates give the same
+    cost: the reference orders candidates with std::sort, which is not stable,
+    while the replay breaks such ties by (distance, id).  Such ties are common
+    under the arm's summed SO(2) distance; there every node's cost along the
+    reference's parent chain still equals the replay's (to 1e-12: the replay
+    sums path costs by pointer jumping, in another order)."""
+    sc = mk()
+    sp = orc.make_space(sc["metric"], sc["dim"], sc["weights"])
+    p = _stream_params(sc, 1, 11, nsamples + 1)
+    st, par, costs, _, rewires = orc.plan_star(sc, sp, p, sc["lo"], sc["hi"], sc["start"], sc["goal"], nsamples, 1.1)
+    V, E = ref.stream_graph(sc, p, "prrt_star", nsamples)
+    ids = _ids(st)
+    assert {v.tobytes() for v in V} == set(ids) and len(V) == len(st)
+    rpar = np.full(len(st), -1, dtype=np.int64)
+    for a, b in E:
+        rpar[ids[a.tobytes()]] = ids[b.tobytes()]
+    rcost = np.full(len(st), np.nan)
+
+    def cost(i):
+        chain = []
+        while np.isnan(rcost[i]):
+            if rpar[i] < 0:
+                rcost[i] = 0.0
+                break
+            chain.append(i)
+            i = rpar[i]
+        for j in reversed(chain):
+            rcost[j] = rcost[rpar[j]] + orc.distance(sp, st[rpar[j]], st[j])
+        return rcost
+
+    for i in range(len(st)):
+        cost(i)
+    assert np.allclose(rcost, costs, rtol=1e-12, atol=0)
+    differ = np.nonzero(rpar != par)[0]
+    if mk is scenes.grid_scene:
+        assert rewires > 50 and len(differ) == 0
+    for i in differ:
+        c0 = costs[par[i]] + orc.distance(sp, st[par[i]], st[i])
+        c1 = costs[rpar[i]] + orc.distance(sp, st[rpar[i]], st[i])
+        assert abs(c0 - c1) <= 1e-12 * c0
+
+
+@pytest.mark.parametrize("mk,nsamples", [(scenes.grid_scene, 1920), (scenes.arm_scene, 6400),
+                                         (scenes.mesh_scene, 128)])
+def test_reference_pprm_on_the_sample_stream_equals_the_replay(orc, mk, nsamples):
+    """The reference's PPRM (impl/pprm/pprm.hpp:141-371: start and goal added,
+    then one sample at a time, k = ceil((e + e/dim) ln(n+1)) nearest, an edge to
+    every neighbour the link accepts) fed the planners' sample stream builds
+    exactly the oracle's replay roadmap -- the roadmap the GPU PPRM is tested
+    equal to: the same nodes bit for bit and the same undirected edges, each
+    visited from both ends."""
+    sc = mk()
+    sp = orc.make_space(sc["metric"], sc["dim"], sc["weights"])
+    W = 64
+    p = _stream_params(sc, W, 12, 1 << 20)
+    r = orc.prm(sc, sp, p, sc["lo"], sc["hi"], sc["goal"], sc["start"], sc["goal"], nsamples // W, False)
+    V, E = ref.stream_graph(sc, p, "pprm", nsamples)
+    ids = _ids(r["states"])
+    ef, et, _ = r["edges"]
+    assert len(ef) > 10
+    assert {v.tobytes() for v in V} == set(ids) and len(V) == len(ids)
+    got = [frozenset((ids[a.tobytes()], ids[b.tobytes()])) for a, b in E]
+    assert len(got) == 2 * len(ef)
+    assert set(got) == {frozenset((int(a), int(b))) for a, b in zip(ef, et)}
