@@ -66,7 +66,7 @@ def lib():
         D = ctypes.c_double
         L.ref_stream_graph.restype = ctypes.c_int
         L.ref_stream_graph.argtypes = [ctypes.c_int, P, P, P, P, P, P, P, ctypes.c_longlong, P, ctypes.c_longlong, P,
-                                       P, ctypes.c_longlong, P]
+                                       P, ctypes.c_longlong, P, P, ctypes.c_longlong, P]
         L.ref_plan_solve.restype = ctypes.c_int
         L.ref_plan_solve.argtypes = [ctypes.c_int, P, P, P, P, P, P, D, D, D, D, ctypes.c_int, ctypes.c_ulonglong,
                                      ctypes.c_int, D, P, ctypes.c_int, P, P, P, P]
@@ -114,13 +114,14 @@ def plan_solve(desc: dict, seed: int, algo: str = "prrt", threads: int = 1, time
 
 
 def stream_graph(desc: dict, params: dict, algo: str, nsamples: int, vcap: int = 1 << 20, ecap: int = 1 << 22):
-    """The reference's own PRRT or PPRM, single-threaded, fed nsamples states
-    of the planners' sample stream (params["seed"], wavefront size
-    params["wavefront"]) instead of its RNG: PRRT from the scene's start with
-    setRange(params["range"]) and no goal bias; PPRM with the start and the goal
+    """The reference's own PRRT, PRRT* or PPRM, single-threaded, fed nsamples
+    states of the planners' sample stream (params["seed"], wavefront size
+    params["wavefront"]) instead of its RNG: PRRT and PRRT* from the scene's
+    start with setRange(params["range"]) and no goal bias; PPRM with the start and the goal
     added first.  The graph through visitGraph: (vertex states [nv][D], edges
     [ne][2][D] as (from, to) state pairs -- PRRT node -> parent, PPRM every edge
-    from both ends)."""
+    from both ends, path [m][D]) where path is PPRM's solution() when solved
+    (empty otherwise and for PRRT / PRRT*)."""
     import numpy as np
 
     from oracle import PlanParams, _ptr, make_scene, make_space
@@ -141,11 +142,14 @@ def stream_graph(desc: dict, params: dict, algo: str, nsamples: int, vcap: int =
     e = np.empty((ecap, 2, D), dtype=np.float64)
     nv = ctypes.c_longlong(0)
     ne = ctypes.c_longlong(0)
+    pcap = 1 << 16
+    path = np.empty((pcap, D), dtype=np.float64)
+    plen = ctypes.c_longlong(0)
     r = L.ref_stream_graph(PLANNERS[algo], ctypes.byref(sc), ctypes.byref(sp), ctypes.byref(pp),
                            *[_ptr(a) for a in arrs], int(nsamples), _ptr(v), vcap, ctypes.byref(nv), _ptr(e), ecap,
-                           ctypes.byref(ne))
+                           ctypes.byref(ne), _ptr(path), pcap, ctypes.byref(plen))
     if r == -1:
         raise ValueError("no reference stream instantiation for %s on metric %s dim %d" % (algo, desc["metric"], D))
     if r == -2:
         raise ValueError("vcap/ecap too small (%d vertices, %d edges)" % (nv.value, ne.value))
-    return v[:nv.value].copy(), e[:ne.value].copy()
+    return v[:nv.value].copy(), e[:ne.value].copy(), path[:plen.value].copy()

@@ -248,7 +248,8 @@ struct GraphCollector {
 template <class S, std::size_t D>
 int stream_graph(int algo, const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp, const double* lo,
                  const double* hi, const double* start, const double* goal, long long nsamples, double* v,
-                 long long vcap, long long* nv, double* e, long long ecap, long long* ne) {
+                 long long vcap, long long* nv, double* e, long long ecap, long long* ne, double* path,
+                 long long pcap, long long* plen) {
     OracleScenario<S, D> base(sc, sp, lo, hi, goal, pp->goal_radius, pp->edge_step, pp->resolution);
     std::uint64_t count = 0;
     StreamScenario<S, D> scen(base, StreamSampler<D>{sp, pp, lo, hi, &count});
@@ -257,6 +258,12 @@ int stream_graph(int algo, const orc_scene* sc, const orc_space* sp, const orc_p
     GraphCollector<D> out{v, vcap, nv, e, ecap, ne};
     *nv = 0;
     *ne = 0;
+    *plen = 0;
+    auto take_path = [&](const std::vector<std::array<double, D>>& sol) {
+        *plen = (long long)sol.size();
+        for (long long i = 0; i < *plen && i < pcap; ++i)
+            for (std::size_t d = 0; d < D; ++d) path[i * D + d] = sol[std::size_t(i)][d];
+    };
     if (algo == 0) {
         mpt::Planner<StreamScenario<S, D>, mpt::PRRT<mpt::single_threaded>> planner(scen, WorkerSeed{pp->seed});
         planner.setRange(pp->range > 0 ? pp->range : std::numeric_limits<double>::infinity());
@@ -277,10 +284,11 @@ int stream_graph(int algo, const orc_scene* sc, const orc_space* sp, const orc_p
         planner.addGoal(OracleScenario<S, D>::arr(goal));
         planner.solve(done);
         planner.visitGraph(out);
+        if (planner.solved()) take_path(planner.solution());
     } else {
         return -1;
     }
-    return (*nv <= vcap && *ne <= ecap) ? 0 : -2;
+    return (*nv <= vcap && *ne <= ecap && *plen <= pcap) ? 0 : -2;
 }
 
 template <class P, class State, class = void>
@@ -422,19 +430,21 @@ int ref_plan_solve(int algo, const orc_scene* sc, const orc_space* sp, const dou
 // The graph comes back through visitGraph: *nv vertex states in v (D doubles
 // each) and *ne edges in e as (from state, to state) pairs (2D doubles each;
 // PRRT, PRRT*: node -> parent; PPRM: every roadmap edge from both of its ends).
-// Returns 0, -1 unsupported, -2 when vcap or ecap was too small.
+// PPRM also returns its solution() (the Dijkstra path of src/mpt/impl/
+// djikstras.hpp) in path when solved: *plen states, 0 when not solved.
+// Returns 0, -1 unsupported, -2 when vcap, ecap or pcap was too small.
 int ref_stream_graph(int algo, const orc_scene* sc, const orc_space* sp, const orc_plan_params* pp,
                      const double* lo, const double* hi, const double* start, const double* goal,
                      long long nsamples, double* v, long long vcap, long long* nv, double* e, long long ecap,
-                     long long* ne) {
+                     long long* ne, double* path, long long pcap, long long* plen) {
     if (sp->metric == 0 && sp->dim == 2)
         return stream_graph<nm::Space<std::array<double, 2>, nm::LP<2>>, 2>(algo, sc, sp, pp, lo, hi, start, goal,
-                                                                           nsamples, v, vcap, nv, e, ecap, ne);
+                                                                           nsamples, v, vcap, nv, e, ecap, ne, path, pcap, plen);
     if (sp->metric == 1 && sp->dim == 10)
         return stream_graph<nm::Space<std::array<double, 10>, nm::SO2<1>>, 10>(
-            algo, sc, sp, pp, lo, hi, start, goal, nsamples, v, vcap, nv, e, ecap, ne);
+            algo, sc, sp, pp, lo, hi, start, goal, nsamples, v, vcap, nv, e, ecap, ne, path, pcap, plen);
     if (sp->metric == 3 && sp->dim == 7)
-        return stream_graph<SE3Space, 7>(algo, sc, sp, pp, lo, hi, start, goal, nsamples, v, vcap, nv, e, ecap, ne);
+        return stream_graph<SE3Space, 7>(algo, sc, sp, pp, lo, hi, start, goal, nsamples, v, vcap, nv, e, ecap, ne, path, pcap, plen);
     return -1;
 }
 

@@ -171,7 +171,7 @@ def test_reference_prrt_on_the_sample_stream_equals_the_replay(orc, mk, nsamples
     sp = orc.make_space(sc["metric"], sc["dim"], sc["weights"])
     p = _stream_params(sc, 1, 11, nsamples + 1)
     st, par, _ = orc.plan(sc, sp, p, sc["lo"], sc["hi"], sc["start"], sc["goal"], nsamples, False)
-    V, E = ref.stream_graph(sc, p, "prrt", nsamples)
+    V, E, _ = ref.stream_graph(sc, p, "prrt", nsamples)
     ids = _ids(st)
     assert len(st) > 50
     assert {v.tobytes() for v in V} == set(ids) and len(V) == len(st)
@@ -193,7 +193,7 @@ def test_reference_prrt_star_on_the_sample_stream_equals_the_replay(orc, mk, nsa
     sp = orc.make_space(sc["metric"], sc["dim"], sc["weights"])
     p = _stream_params(sc, 1, 11, nsamples + 1)
     st, par, costs, _, rewires = orc.plan_star(sc, sp, p, sc["lo"], sc["hi"], sc["start"], sc["goal"], nsamples, 1.1)
-    V, E = ref.stream_graph(sc, p, "prrt_star", nsamples)
+    V, E, _ = ref.stream_graph(sc, p, "prrt_star", nsamples)
     ids = _ids(st)
     assert {v.tobytes() for v in V} == set(ids) and len(V) == len(st)
     rpar = np.full(len(st), -1, dtype=np.int64)
@@ -233,13 +233,13 @@ def test_reference_pprm_on_the_sample_stream_equals_the_replay(orc, mk, nsamples
     every neighbour the link accepts) fed the planners' sample stream builds
     exactly the oracle's replay roadmap -- the roadmap the GPU PPRM is tested
     equal to: the same nodes bit for bit and the same undirected edges, each
-    visited from both ends."""
+    visited from both ends -- and returns the same solution path."""
     sc = mk()
     sp = orc.make_space(sc["metric"], sc["dim"], sc["weights"])
     W = 64
     p = _stream_params(sc, W, 12, 1 << 20)
     r = orc.prm(sc, sp, p, sc["lo"], sc["hi"], sc["goal"], sc["start"], sc["goal"], nsamples // W, False)
-    V, E = ref.stream_graph(sc, p, "pprm", nsamples)
+    V, E, path = ref.stream_graph(sc, p, "pprm", nsamples)
     ids = _ids(r["states"])
     ef, et, _ = r["edges"]
     assert len(ef) > 10
@@ -247,3 +247,8 @@ def test_reference_pprm_on_the_sample_stream_equals_the_replay(orc, mk, nsamples
     got = [frozenset((ids[a.tobytes()], ids[b.tobytes()])) for a, b in E]
     assert len(got) == 2 * len(ef)
     assert set(got) == {frozenset((int(a), int(b))) for a, b in zip(ef, et)}
+    # solution(): the reference's Dijkstra (src/mpt/impl/djikstras.hpp) and the
+    # replay's (orc_prm_dijkstra) return the same path
+    want = r["states"][r["path"]]
+    assert len(want) > 0 or mk is scenes.mesh_scene
+    assert len(path) == len(want) and np.array_equal(path.view(np.int64), want.view(np.int64))
