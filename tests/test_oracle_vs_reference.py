@@ -178,12 +178,13 @@ def test_reference_prrt_on_the_sample_stream_equals_the_replay(orc, mk, nsamples
     assert {(ids[a.tobytes()], ids[b.tobytes()]) for a, b in E} == {(i, int(par[i])) for i in range(1, len(st))}
 
 
-@pytest.mark.parametrize("mk,nsamples", [(scenes.grid_scene, 2000), (scenes.arm_scene, 1000)])
+@pytest.mark.parametrize("mk,nsamples", [(scenes.grid_scene, 2000), (scenes.arm_scene, 1000),
+                                         (scenes.mesh_scene, 300)])
 def test_reference_prrt_star_on_the_sample_stream_equals_the_replay(orc, mk, nsamples):
     """The reference's PRRT* (impl/prrt_star/prrt_star.hpp:505-657, k-nearest
     rewiring, factor 1.1) on the sample stream against the oracle's PRRT* replay
-    at wavefront size 1: the same states, and on the grid the same parent for
-    every node.  Parents may differ only where two candidates give the same
+    at wavefront size 1: the same states, and on the grid and SE(3) the same
+    parent for every node.  Parents may differ only where two candidates give the same
     cost: the reference orders candidates with std::sort, which is not stable,
     while the replay breaks such ties by (distance, id).  Such ties are common
     under the arm's summed SO(2) distance; there every node's cost along the
@@ -217,8 +218,10 @@ def test_reference_prrt_star_on_the_sample_stream_equals_the_replay(orc, mk, nsa
         cost(i)
     assert np.allclose(rcost, costs, rtol=1e-12, atol=0)
     differ = np.nonzero(rpar != par)[0]
+    if mk is not scenes.arm_scene:
+        assert len(differ) == 0
     if mk is scenes.grid_scene:
-        assert rewires > 50 and len(differ) == 0
+        assert rewires > 50
     for i in differ:
         c0 = costs[par[i]] + orc.distance(sp, st[par[i]], st[i])
         c1 = costs[rpar[i]] + orc.distance(sp, st[rpar[i]], st[i])
