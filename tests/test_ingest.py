@@ -65,9 +65,9 @@ def _png(path, rows: np.ndarray, ctype: int, depth: int, palette=None, width=Non
 ADAM7 = ((0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2))
 
 
-def _png_adam7(path, px: np.ndarray, ctype: int, depth: int):
-    """px: [h][w][channels] samples (8-bit, or 0/1 for depth 1); Adam7 order,
-    each pass's scanlines filtered on their own (empty passes omitted)."""
+def _png_adam7(path, px: np.ndarray, ctype: int, depth: int, palette=None):
+    """px: [h][w][channels] samples of the given bit depth; Adam7 order, each
+    pass's scanlines packed and filtered on their own (empty passes omitted)."""
     h, w, chans = px.shape
     bpp = max(1, chans * depth // 8)
     raw = b""
@@ -75,11 +75,16 @@ def _png_adam7(path, px: np.ndarray, ctype: int, depth: int):
         sub = px[y0::dy, x0::dx]
         if sub.size == 0:
             continue
-        rows = sub.reshape(sub.shape[0], -1).astype(np.uint8)
-        if depth == 1:
-            rows = np.packbits(rows, axis=1)
+        vals = sub.reshape(sub.shape[0], -1).astype(np.int64)
+        if depth < 8:  # MSB-first bit packing, rows padded to whole bytes
+            bits = (vals[:, :, None] >> np.arange(depth - 1, -1, -1)) & 1
+            rows = np.packbits(bits.reshape(vals.shape[0], -1).astype(np.uint8), axis=1)
+        elif depth == 16:
+            rows = vals.astype(">u2").view(np.uint8).reshape(vals.shape[0], -1)
+        else:
+            rows = vals.astype(np.uint8)
         raw += _filtered(rows, bpp)
-    _write_png(path, w, h, ctype, depth, raw, interlace=1)
+    _write_png(path, w, h, ctype, depth, raw, palette=palette, interlace=1)
 
 
 def test_png_color_types_and_filters(tmp_path):
@@ -117,9 +122,17 @@ def test_png_adam7_interlaced(tmp_path, h, w):
     rgb = rng.integers(0, 256, (h, w, 3), dtype=np.uint8)
     _png_adam7(p, rgb, 2, 8)
     assert np.array_equal(ingest.read_image(p), rgb)
-    bits = rng.integers(0, 2, (h, w, 1), dtype=np.uint8)
-    _png_adam7(p, bits, 0, 1)
-    assert np.array_equal(ingest.read_image(p)[:, :, 0], bits[:, :, 0] * 255)
+    for depth in (1, 2, 4):  # sub-byte grey, scaled to 8 bits
+        g = rng.integers(0, 1 << depth, (h, w, 1), dtype=np.uint8)
+        _png_adam7(p, g, 0, depth)
+        assert np.array_equal(ingest.read_image(p)[:, :, 0], g[:, :, 0] * (255 // ((1 << depth) - 1)))
+    pal = rng.integers(0, 256, (16, 3), dtype=np.uint8)  # 4-bit palette
+    idx = rng.integers(0, 16, (h, w, 1), dtype=np.uint8)
+    _png_adam7(p, idx, 3, 4, palette=pal)
+    assert np.array_equal(ingest.read_image(p), pal[idx[:, :, 0]])
+    rgba16 = rng.integers(0, 65536, (h, w, 4))  # 16-bit RGBA: high bytes, alpha dropped
+    _png_adam7(p, rgba16, 6, 16)
+    assert np.array_equal(ingest.read_image(p), (rgba16[:, :, :3] >> 8).astype(np.uint8))
 
 
 def test_pnm_formats(tmp_path):
