@@ -26,6 +26,15 @@ ROOT = os.path.dirname(HERE)
 L2, SO2, SO3, SE3, L1 = 0, 1, 2, 3, 4
 
 
+# MPTG_ORACLE_SANITIZE=1 selects a second build with AddressSanitizer and
+# UndefinedBehaviorSanitizer (aborting on the first report), for running the
+# oracle's tests under the sanitizers; the process must preload libasan.
+SANITIZE = bool(os.environ.get("MPTG_ORACLE_SANITIZE"))
+SANITIZE_FLAGS = ["-fsanitize=address,undefined", "-fno-sanitize-recover=undefined", "-fno-omit-frame-pointer", "-g"]
+if SANITIZE:
+    LIB_PATH = os.path.join(BUILD_DIR, "liborc_san.so")
+
+
 def build(force: bool = False) -> str:
     """Compile oracle.c into _build/liborc.so (gcc, OpenMP, no FP contraction)."""
     src = os.path.join(HERE, "oracle.c")
@@ -38,6 +47,8 @@ def build(force: bool = False) -> str:
     tmp = LIB_PATH + ".tmp%d" % os.getpid()
     cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
            "-std=c11", "-o", tmp, src, "-lm"]
+    if SANITIZE:
+        cmd[1:1] = SANITIZE_FLAGS
     subprocess.check_call(cmd)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH

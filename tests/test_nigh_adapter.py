@@ -34,3 +34,20 @@ def test_nigh_adapter_links_against_libmptg(tmp_path):
     from mpt_gb300 import build
     libdir = os.path.dirname(build.build())
     subprocess.check_call(FLAGS + ["-L", libdir, "-lmptg", "-Wl,-rpath," + libdir, "-o", str(tmp_path / "na_gpu")])
+
+
+def test_nigh_adapter_under_sanitizers(tmp_path):
+    """The same program built with AddressSanitizer and UndefinedBehaviorSanitizer
+    (aborting on the first report): the adapter, the reference planners over it
+    and the CPU stand-in stay inside their buffers."""
+    exe = str(tmp_path / "nigh_adapter_san")
+    try:
+        subprocess.check_call(FLAGS + ["-fsanitize=address,undefined", "-fno-sanitize-recover=undefined",
+                                       "-fno-omit-frame-pointer", "-g",
+                                       os.path.join(ROOT, "tests", "cpp", "fake_mptg_nn.cpp"), "-o", exe])
+    except subprocess.CalledProcessError:
+        pytest.skip("sanitizer runtimes not available to g++")
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=600,
+                       env=dict(os.environ, ASAN_OPTIONS="detect_leaks=0"))
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "nigh adapter OK" in r.stdout and "runtime error" not in r.stderr
