@@ -17,7 +17,8 @@
 // gpu_scene() does not compile: arbitrary C++ valid()/link() code cannot run
 // on the device, and there is no CPU fallback.
 //
-// Option tags (src/mpt/planner_tags.hpp): gpu_wavefront<W>, report_stats<b>;
+// Option tags (src/mpt/planner_tags.hpp): gpu_wavefront<W>, report_stats<b>,
+// gpu_device<id>;
 // max_threads<N>, single_threaded and hardware_concurrency are accepted and
 // have no effect (wavefronts replace the worker pool).
 #pragma once
@@ -44,12 +45,18 @@ template <int N> struct max_threads {};
 using single_threaded = max_threads<1>;
 using hardware_concurrency = max_threads<0>;
 template <bool enabled> struct report_stats {};
+// the CUDA device a planner creates its context on (the constructor's default)
+template <int index> struct gpu_device {};
 
 namespace impl {
 template <class... O> struct options;
 template <> struct options<> {
     static constexpr int wavefront = 4096;
     static constexpr bool stats = false;
+    static constexpr int device = 0;
+};
+template <int D, class... O> struct options<gpu_device<D>, O...> : options<O...> {
+    static constexpr int device = D;
 };
 template <int W, class... O> struct options<gpu_wavefront<W>, O...> : options<O...> {
     static constexpr int wavefront = W;
@@ -65,6 +72,7 @@ template <int N, class... O> struct options<max_threads<N>, O...> : options<O...
 template <class... Options> struct PRRT {
     static constexpr int wavefront = impl::options<Options...>::wavefront;
     static constexpr bool stats = impl::options<Options...>::stats;
+    static constexpr int device = impl::options<Options...>::device;
 };
 
 // ---- goal and scene descriptions --------------------------------------------
@@ -189,7 +197,8 @@ protected:
 public:
     // prrt.hpp:149-157; the default seed draws fresh entropy (random_device_seed.hpp)
     explicit Planner(const Scenario& scenario = Scenario(), uint64_t seed = std::random_device{}(),
-                     size_t maxNodes = size_t(1) << 21, int device = 0)
+                     size_t maxNodes = size_t(1) << 21,
+                     int device = impl::options<Options...>::device)
         : scenario_(scenario), seed_(seed), maxNodes_(maxNodes) {
         if (mptg_create(&ctx_, device) != MPTG_OK) throw std::runtime_error("mptg: no usable GPU");
         auto d = impl::desc_of(scenario_.gpu_scene());
@@ -345,7 +354,8 @@ class Planner<Scenario, PRRTStar<Options...>> : public Planner<Scenario, PRRT<Op
 
 public:
     explicit Planner(const Scenario& scenario = Scenario(), uint64_t seed = std::random_device{}(),
-                     size_t maxNodes = size_t(1) << 21, int device = 0)
+                     size_t maxNodes = size_t(1) << 21,
+                     int device = impl::options<Options...>::device)
         : Base(scenario, seed, maxNodes, device) {
         this->rewire_ = true;
     }
@@ -389,7 +399,8 @@ private:
 
 public:
     explicit Planner(const Scenario& scenario = Scenario(), uint64_t seed = std::random_device{}(),
-                     size_t maxNodes = size_t(1) << 21, int device = 0)
+                     size_t maxNodes = size_t(1) << 21,
+                     int device = impl::options<Options...>::device)
         : scenario_(scenario) {
         if (mptg_create(&ctx_, device) != MPTG_OK) throw std::runtime_error("mptg: no usable GPU");
         auto d = impl::desc_of(scenario_.gpu_scene());

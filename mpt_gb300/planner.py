@@ -44,6 +44,13 @@ class max_threads:  # noqa: N801
         self.n = int(n)
 
 
+class gpu_device:  # noqa: N801
+    """The CUDA device a planner creates its context on when none is given."""
+
+    def __init__(self, index: int):
+        self.index = int(index)
+
+
 single_threaded = max_threads(1)
 hardware_concurrency = max_threads(0)
 
@@ -56,19 +63,22 @@ class PRRT:
     def __init__(self, *options):
         self.wavefront = 4096
         self.report_stats = False
+        self.device = 0
         for o in options:
             if isinstance(o, gpu_wavefront):
                 self.wavefront = o.n
             elif isinstance(o, report_stats):
                 self.report_stats = o.enabled
+            elif isinstance(o, gpu_device):
+                self.device = o.index
             elif isinstance(o, max_threads):
                 pass
             else:
                 raise TypeError("unknown PRRT option %r" % (o,))
 
     def __eq__(self, other):
-        return isinstance(other, PRRT) and (self.wavefront, self.report_stats) == (other.wavefront,
-                                                                                   other.report_stats)
+        return isinstance(other, PRRT) and (self.wavefront, self.report_stats, self.device) == (
+            other.wavefront, other.report_stats, other.device)
 
 
 class PRRTStar(PRRT):
@@ -160,9 +170,9 @@ class Planner:
                  ctx: Context | None = None, max_nodes: int = 1 << 20):
         self.lib = load()
         _sig(self.lib)
-        self.ctx = ctx or Context(0)
-        self.scenario = scenario
         self.algorithm = algorithm or PRRT()
+        self.ctx = ctx or Context(self.algorithm.device)
+        self.scenario = scenario
         if seed is None:  # RandomDeviceSeed: fresh entropy (src/mpt/random_device_seed.hpp:62-88)
             seed = int.from_bytes(np.random.default_rng().bytes(8), "little")
         self.seed = int(seed) & ((1 << 64) - 1)
@@ -414,9 +424,9 @@ class PPRMPlanner(Planner):
                  ctx: Context | None = None, max_nodes: int = 1 << 20):
         self.lib = load()
         _sig(self.lib)
-        self.ctx = ctx or Context(0)
-        self.scenario = scenario
         self.algorithm = algorithm or PPRM()
+        self.ctx = ctx or Context(self.algorithm.device)
+        self.scenario = scenario
         if seed is None:
             seed = int.from_bytes(np.random.default_rng().bytes(8), "little")
         self.seed = int(seed) & ((1 << 64) - 1)
@@ -574,5 +584,5 @@ def autotune_wavefront(ctx: Context, scenario: Scenario, start, candidates=(256,
     return best.value, {c: med[i] for i, c in enumerate(candidates)}
 
 
-__all__ = ["Planner", "PRRTStar", "autotune_wavefront", "PRRT", "Scenario", "GoalState", "gpu_wavefront", "report_stats", "max_threads",
-           "single_threaded", "hardware_concurrency", "MptgError"]
+__all__ = ["Planner", "PRRTStar", "PPRM", "autotune_wavefront", "PRRT", "Scenario", "GoalState", "gpu_wavefront",
+           "gpu_device", "report_stats", "max_threads", "single_threaded", "hardware_concurrency", "MptgError"]

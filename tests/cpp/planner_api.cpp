@@ -40,6 +40,7 @@ int main() {
     static_assert(PRRT<gpu_wavefront<512>, single_threaded, report_stats<true>>::wavefront ==
                   PRRT<report_stats<true>, gpu_wavefront<512>, single_threaded>::wavefront);
     static_assert(PRRT<report_stats<true>, gpu_wavefront<512>>::stats);
+    static_assert(PRRT<gpu_wavefront<64>, gpu_device<1>>::device == 1 && PRRT<gpu_wavefront<64>>::device == 0);
 
     WallScenario sc;
     Planner<WallScenario, PRRT<gpu_wavefront<1024>, report_stats<true>>> planner(sc, 42);

@@ -23,3 +23,13 @@ def test_planner_dispatches_pprm():
     assert type(obj) is P.PPRMPlanner
     assert type(P.Planner.__new__(P.Planner, None, P.PRRTStar())) is P.Planner
     assert type(P.Planner.__new__(P.Planner, None, None)) is P.Planner
+
+
+def test_gpu_device_tag():
+    """gpu_device(i) picks the device of the context a Planner creates when it
+    is given none (the C++ header's gpu_device<i>)."""
+    assert P.PRRT().device == 0
+    a = P.PRRT(P.gpu_device(1), P.gpu_wavefront(64))
+    assert a.device == 1 and a == P.PRRT(P.gpu_wavefront(64), P.gpu_device(1))
+    assert a != P.PRRT(P.gpu_wavefront(64))
+    assert P.PPRM(P.gpu_device(2)).device == 2
