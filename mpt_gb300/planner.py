@@ -20,7 +20,9 @@ because wavefronts replace the worker pool.
 from __future__ import annotations
 
 import ctypes
+import json
 import math
+import os
 import time
 
 import numpy as np
@@ -552,12 +554,49 @@ class PPRMPlanner(Planner):
     visitGraph = visit_graph
 
 
+def autotune_cache_key(scenario: Scenario, candidates, max_nodes: int) -> str:
+    """Key of an autotuner result: scene kind, metric, dimension, the tree
+    capacity's power-of-two bucket and the candidate sizes."""
+    d = scenario.desc
+    bucket = max(0, int(max_nodes) - 1).bit_length()
+    return "%s/m%d/d%d/n2^%d/%s" % (d["kind"], int(d["metric"]), int(d["dim"]), bucket,
+                                     ",".join(str(int(c)) for c in candidates))
+
+
+def _cache_load(path: str) -> dict:
+    try:
+        with open(path) as f:
+            data = json.load(f)
+        return data if isinstance(data, dict) else {}
+    except (OSError, ValueError):
+        return {}
+
+
+def _cache_store(path: str, key: str, best: int, med: dict):
+    data = _cache_load(path)
+    data[key] = {"best": int(best), "median_s": {str(k): float(v) for k, v in med.items()}}
+    tmp = "%s.tmp%d" % (path, os.getpid())
+    with open(tmp, "w") as f:
+        json.dump(data, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
 def autotune_wavefront(ctx: Context, scenario: Scenario, start, candidates=(256, 512, 1024, 2048, 4096, 8192),
                        trials: int = 3, time_limit: float = 2.0, seed: int = 1, max_nodes: int = 1 << 21,
-                       goal_bias: float = 0.01, range_: float | None = None):
+                       goal_bias: float = 0.01, range_: float | None = None, cache: str | None = None):
     """Native wavefront-size autotuner (mptg_autotune_wavefront): the size with
     the lowest median time to the first solution over `trials` seeds.
-    Returns (best size, {size: median seconds})."""
+    Returns (best size, {size: median seconds}).
+
+    cache: a JSON file of earlier results keyed by autotune_cache_key (scene
+    kind, metric, dimension, capacity bucket, candidates).  A hit returns the
+    stored result without running the GPU; a miss runs the tuner and stores
+    its result."""
+    key = autotune_cache_key(scenario, candidates, max_nodes) if cache else None
+    if cache:
+        hit = _cache_load(cache).get(key)
+        if hit:
+            return int(hit["best"]), {int(k): float(v) for k, v in hit["median_s"].items()}
     lib = load()
     _sig(lib)
     scene = Scene(ctx, scenario.desc)
@@ -581,8 +620,11 @@ def autotune_wavefront(ctx: Context, scenario: Scenario, start, candidates=(256,
                                               scenario.goal.radius, cand, len(candidates), int(trials),
                                               float(time_limit), ctypes.byref(best), med))
     scene.close()
-    return best.value, {c: med[i] for i, c in enumerate(candidates)}
+    result = {c: med[i] for i, c in enumerate(candidates)}
+    if cache:
+        _cache_store(cache, key, best.value, result)
+    return best.value, result
 
 
-__all__ = ["Planner", "PRRTStar", "PPRM", "autotune_wavefront", "PRRT", "Scenario", "GoalState", "gpu_wavefront",
+__all__ = ["Planner", "PRRTStar", "PPRM", "autotune_wavefront", "autotune_cache_key", "PRRT", "Scenario", "GoalState", "gpu_wavefront",
            "gpu_device", "report_stats", "max_threads", "single_threaded", "hardware_concurrency", "MptgError"]

@@ -33,3 +33,21 @@ def test_gpu_device_tag():
     assert a.device == 1 and a == P.PRRT(P.gpu_wavefront(64), P.gpu_device(1))
     assert a != P.PRRT(P.gpu_wavefront(64))
     assert P.PPRM(P.gpu_device(2)).device == 2
+
+
+def test_autotune_cache_hit_needs_no_gpu(tmp_path):
+    """A cached autotuner result (keyed by scene kind, metric, dimension,
+    capacity bucket and candidates) is returned without running the tuner;
+    other keys in the file are kept when a result is stored."""
+    from mpt_gb300 import scenes
+    sc = P.Scenario(scenes.grid_scene())
+    cache = str(tmp_path / "tune.json")
+    key = P.autotune_cache_key(sc, (256, 512), 1 << 20)
+    assert key == "grid/m0/d2/n2^20/256,512"
+    assert P.autotune_cache_key(sc, (256, 512), (1 << 20) + 1) != key
+    P._cache_store(cache, "other", 64, {64: 0.5})
+    P._cache_store(cache, key, 512, {256: 0.02, 512: 0.01})
+    best, med = P.autotune_wavefront(None, sc, sc.desc["start"], candidates=(256, 512), max_nodes=1 << 20,
+                                     cache=cache)
+    assert best == 512 and med == {256: 0.02, 512: 0.01}
+    assert set(P._cache_load(cache)) == {"other", key}
