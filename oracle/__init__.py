@@ -399,3 +399,24 @@ def tri_tri(t1, t2) -> bool:
     t1 = np.ascontiguousarray(t1, dtype=np.float64).reshape(9)
     t2 = np.ascontiguousarray(t2, dtype=np.float64).reshape(9)
     return bool(lib().orc_tri_tri(_ptr(t1), _ptr(t2)))
+
+
+def sample_states(space: Space, seed: int, lo, hi, n: int, wavefront: int = 4096) -> np.ndarray:
+    """The first n states of the planners' sample stream: state c is sample
+    c % wavefront of wavefront c / wavefront (orc_sample_state, no goal bias)."""
+    L = lib()
+    if not getattr(L, "_sample_sig", False):
+        P = ctypes.c_void_p
+        L.orc_sample_state.argtypes = [P, P, P, P, ctypes.c_uint32, ctypes.c_uint32, P]
+        L._sample_sig = True
+    pp = PlanParams()
+    pp.wavefront = int(wavefront)
+    pp.seed = int(seed)
+    lo = np.ascontiguousarray(lo, dtype=np.float64)
+    hi = np.ascontiguousarray(hi, dtype=np.float64)
+    out = np.empty((n, space.dim), dtype=np.float64)
+    W = int(wavefront)
+    for c in range(n):
+        L.orc_sample_state(ctypes.byref(space), ctypes.byref(pp), _ptr(lo), _ptr(hi), c % W, c // W,
+                           out[c:].ctypes.data_as(ctypes.c_void_p))
+    return out

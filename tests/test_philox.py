@@ -47,3 +47,23 @@ int main(){ for (unsigned i=0;i<50;++i) printf("%a\n", phx_uniform(0x1234567890a
     want = [orc.uniform(0x1234567890abcdef, i * 7919, i, i % 17) for i in range(50)]
     assert got == want
     assert all(0.0 <= u < 1.0 for u in got)
+
+
+def test_sample_stream_meets_the_reference_sampler_tests(orc):
+    """The planners' sample stream (the oracle's restatement of the device
+    sampler) against the reference's sampler tests: unit quaternions within
+    4 eps (test/uniform_sampler_so3_test.cpp:42-59; 250,000 draws here), L2
+    samples inside their box (test/uniform_sampler_lp_test.cpp:41-60), SO(2)
+    angles in [-pi, pi) (impl/uniform_sampler_so2.hpp:57-64)."""
+    import numpy as np
+    eps = np.finfo(np.float64).eps
+    q = orc.sample_states(orc.make_space(orc.SO3, 4), 7, [-1] * 4, [1] * 4, 250000)
+    assert (np.abs((q * q).sum(axis=1) - 1.0) < 4 * eps).all()
+    se3 = orc.sample_states(orc.make_space(orc.SE3, 7, (2.0, 1.0)), 8, [-1, -1, -1, -1, 1, 2, 3],
+                            [1, 1, 1, 1, 4, 6, 8], 20000)
+    assert (np.abs((se3[:, :4] ** 2).sum(axis=1) - 1.0) < 4 * eps).all()
+    assert ((se3[:, 4:] >= [1, 2, 3]) & (se3[:, 4:] <= [4, 6, 8])).all()
+    lp = orc.sample_states(orc.make_space(orc.L2, 3), 9, [1, 2, 3], [4, 6, 8], 20000)
+    assert ((lp >= [1, 2, 3]) & (lp <= [4, 6, 8])).all()
+    so2 = orc.sample_states(orc.make_space(orc.SO2, 10), 10, [-np.pi] * 10, [np.pi] * 10, 20000)
+    assert ((so2 >= -np.pi) & (so2 < np.pi)).all()
