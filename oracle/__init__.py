@@ -420,3 +420,20 @@ def sample_states(space: Space, seed: int, lo, hi, n: int, wavefront: int = 4096
         L.orc_sample_state(ctypes.byref(space), ctypes.byref(pp), _ptr(lo), _ptr(hi), c % W, c // W,
                            out[c:].ctypes.data_as(ctypes.c_void_p))
     return out
+
+
+def prm_dijkstra(n: int, flags, efrom, eto, edist):
+    """Shortest roadmap path (orc_prm_dijkstra) over undirected edges from any
+    node with flag bit 1 to the nearest node with flag bit 2: (node ids, cost)."""
+    L = lib()
+    P = ctypes.c_void_p
+    L.orc_prm_dijkstra.restype = ctypes.c_int64
+    L.orc_prm_dijkstra.argtypes = [ctypes.c_int64, P, ctypes.c_int64, P, P, P, P, P]
+    flags = np.ascontiguousarray(flags, dtype=np.uint8)
+    ef = np.ascontiguousarray(efrom, dtype=np.int32)
+    et = np.ascontiguousarray(eto, dtype=np.int32)
+    ed = np.ascontiguousarray(edist, dtype=np.float64)
+    path = np.empty(max(int(n), 1), dtype=np.int32)
+    cost = ctypes.c_double(0.0)
+    m = L.orc_prm_dijkstra(int(n), _ptr(flags), len(ef), _ptr(ef), _ptr(et), _ptr(ed), _ptr(path), ctypes.byref(cost))
+    return path[:m].copy(), cost.value

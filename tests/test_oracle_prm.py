@@ -64,3 +64,15 @@ def test_prm_roadmap_rules(orc):
             assert (max(a, b), min(a, b)) in edges
             c += orc.distance(sp, X[a], X[b])
         assert abs(c - r["cost"]) <= 1e-9 * c
+
+
+def test_dijkstra_reference_known_answer(orc):
+    """The graph of test/djikstras_test.cpp:55-101 (seven vertices, eleven
+    undirected weighted edges, start 0, goal 4): the shortest path is
+    0-1-3-2-4."""
+    edges = [(0, 1, 1.0), (1, 3, 2.0), (0, 3, 3.1), (2, 4, 4.0), (0, 4, 10.3), (3, 2, 3.0), (0, 2, 6.2),
+             (0, 5, 1.5), (5, 6, 9.5), (6, 4, 9.9), (1, 2, 7.0)]
+    flags = [1, 0, 0, 0, 2, 0, 0]
+    path, cost = orc.prm_dijkstra(7, flags, [e[0] for e in edges], [e[1] for e in edges], [e[2] for e in edges])
+    assert list(path) == [0, 1, 3, 2, 4]
+    assert cost == ((1.0 + 2.0) + 3.0) + 4.0
