@@ -154,6 +154,12 @@ int planner_checks(const char* name, Setup setup) {
 
 }  // namespace
 
+// the strategy option is found in any position of the pack, as nigh's are
+// (test/pack_nearest_test.cpp)
+static_assert(std::is_same_v<mpt::impl::pack_nearest_t<GpuKDTree, mpt::single_threaded>, GpuKDTree>);
+static_assert(std::is_same_v<mpt::impl::pack_nearest_t<mpt::report_stats<true>, GpuKDTree>, GpuKDTree>);
+static_assert(std::is_same_v<mpt::PRRT<GpuKDTree, mpt::single_threaded>, mpt::PRRT<mpt::single_threaded, GpuKDTree>>);
+
 int main() {
     auto range = [](auto& p) { p.setRange(5); };
     auto goal = [](auto& p) { p.addGoal(State{90, 10}); };
