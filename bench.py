@@ -126,6 +126,13 @@ def _whole_job_rate(ws: int, units_per_rank_step: int, steps: int, max_seconds: 
     return ws * units_per_rank_step * steps / max_seconds
 
 
+# The headline workload; both arms print this same config (the per-step query
+# counts differ and are stated beside it).
+NN_CONFIG = {"workload": "nn_so2x10_1M", "tree_nodes": N_TREE,
+             "tree": "seeded uniform SO(2)^10 states (planar 10-link arm), inserted in batches of 65,536",
+             "queries": "seeded uniform SO(2)^10 states", "answer": "exact FP64 nearest, lowest id on ties"}
+
+
 def _workload(seed_base=20261205):
     from mpt_gb300 import scenes
     sc = scenes.arm_scene()
@@ -164,6 +171,110 @@ def edge_rates(ctx, m, stream, torch):
         out[name] = {"edges_per_s": len(da) * 3 / (e0.elapsed_time(e1) / 1000.0), "edges_per_launch": len(da),
                      "valid_fraction": float(eo.float().mean().item())}
         scene.close()
+    return out
+
+
+def _nn_roofline(cnt, steps, nq, D, avg_s, peak, kernel):
+    """Algorithmic bytes of one NN launch from the device counters, over the
+    launch time, against the HBM peak (the same formula as the headline)."""
+    per = {k: v / steps for k, v in cnt.items()}
+    alg = (per["points_evaluated"] * (4 * D + 4) + per["internal_visited"] * (16 + 8 * D) + per["leaves_visited"] * 16
+           + per["reranked"] * 8 * D + nq * (8 * D + 12))
+    ach = alg / avg_s / 1e9
+    return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "kernel": kernel,
+            "alg_bytes_per_launch": alg, "counters_per_launch": per}
+
+
+def _grow_tree(ctx, sc, n, seed, W=65536):
+    """A planner-grown tree: the plain wavefront PRRT on the scene (goal bias 0,
+    no stop at the goal) until it holds n nodes.  Returns (planner, seconds)."""
+    from mpt_gb300 import planner as P
+    pl = P.Planner(P.Scenario(sc), P.PRRT(P.gpu_wavefront(W)), seed=seed, ctx=ctx, max_nodes=n)
+    pl.set_goal_bias(0.0)
+    pl.add_start(sc["start"])
+    t0 = time.perf_counter()
+    for _ in range(4096):
+        if pl.size() >= n:
+            break
+        pl.run(8)
+    return pl, time.perf_counter() - t0
+
+
+def nn_1m_section(ctx, m, torch, steps=5, peak=None, cpu_sample=2048):
+    """NN queries/s against 1,048,576-node trees of the three scenes: seeded
+    uniform states (2-D grid, L2; SE(3) w = 2/1) and trees grown by the
+    planner itself to 1M nodes (10-link arm, SO(2)^10; SE(3); grid).  65,536
+    seeded uniform queries per step, L2 flushed between steps, CUDA events on
+    the launching stream; ids and distances checked against the oracle's exact
+    CPU kd-tree on a sample, which is also timed on all host cores."""
+    import oracle
+    from mpt_gb300 import scenes
+    peak = peak or _peaks()[0]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    cores = os.cpu_count()
+    out = {}
+    cases = [("grid_l2_uniform", scenes.grid_scene, "uniform"), ("se3_uniform", scenes.mesh_scene, "uniform"),
+             ("arm_so2x10_planner_grown", scenes.arm_scene, "grown"), ("se3_planner_grown", scenes.mesh_scene, "grown"),
+             ("grid_l2_planner_grown", scenes.grid_scene, "grown")]
+    for name, mk, how in cases:
+        sc = mk()
+        D = sc["dim"]
+        pl = None
+        t0 = time.perf_counter()
+        if how == "uniform":
+            tree = m.Tree(ctx, sc["metric"], D, N_TREE, sc["weights"])
+            pts = scenes.uniform_states(sc, N_TREE, 4100 + D)
+            dp = torch.from_numpy(pts).cuda()
+            for lo in range(0, N_TREE, BATCH):
+                tree.insert(dp[lo:lo + BATCH])
+            del dp
+            torch.cuda.synchronize()
+        else:
+            pl, _ = _grow_tree(ctx, sc, N_TREE, 4200 + D)
+            tree = pl.tree()
+            pts = tree.states()
+        build_s = time.perf_counter() - t0
+        q = scenes.uniform_states(sc, BATCH, 4300 + D)
+        dq = torch.from_numpy(q).cuda()
+        di = torch.empty(BATCH, dtype=torch.int32, device="cuda")
+        dd = torch.empty(BATCH, dtype=torch.float64, device="cuda")
+        for _ in range(3):
+            tree.nearest(dq, di, dd, stream=stream)
+        torch.cuda.synchronize()
+        tree.counters(reset=True)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for s_, (a, b) in enumerate(ev):
+            flush.fill_(s_ & 0xff)
+            a.record(stream)
+            tree.nearest(dq, di, dd, stream=stream)
+            b.record(stream)
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev)
+        cnt = tree.counters(reset=True)
+        gi, gd = di[:cpu_sample].cpu().numpy(), dd[:cpu_sample].cpu().numpy()
+        # the oracle's exact CPU kd-tree over the same states, all host cores
+        osp = oracle.make_space(sc["metric"], D, sc["weights"])
+        ot = oracle.KDTree(osp, pts, 8)
+        ot.nearest(q[:64], cores)
+        t1 = time.perf_counter()
+        ci, cd = ot.nearest(q[:cpu_sample], cores)
+        cpu_s = time.perf_counter() - t1
+        avg = ms / 1000.0 / steps
+        out[name] = {"tree_nodes": len(pts), "tree": how, "queries_per_step": BATCH, "steps": steps,
+                     "queries_per_s": BATCH * steps / (ms / 1000.0), "ms_per_step": ms / steps,
+                     "tree_build_s": build_s,
+                     "roofline": _nn_roofline(cnt, steps, BATCH, D, avg, peak, "k_nearest<metric %d>" % sc["metric"]),
+                     "cpu_kdtree": {"queries_per_s": cpu_sample / cpu_s, "cores": cores, "sample": cpu_sample,
+                                    "kind": "port (oracle exact kd-tree, leaf 8)"},
+                     "ids_equal_oracle": bool(np.array_equal(gi, ci)),
+                     "max_abs_dist_err_vs_fp64_oracle": float(np.max(np.abs(gd - cd)))}
+        del ot
+        if pl is not None:
+            tree.close()
+            pl.close()
+        else:
+            tree.close()
     return out
 
 
@@ -206,64 +317,78 @@ def _solve_stats(ctx, sc, W, seeds, cap_s, surrogate=None, points=1, want_path=F
     return (res, first_path) if want_path else res
 
 
-def solve_times(ctx, seeds=5, cap_s=20.0, tune=True, cpu=True):
+SOLVE_SCENES = [("grid_1024", "grid_scene", 2048), ("arm_10link", "arm_scene", 4096), ("se3_mesh", "mesh_scene", 4096)]
+
+
+def solve_times(ctx, seeds=None, cap_s=20.0, tune=True):
     """Wall time to the first solution of the plain wavefront planner per scene
-    (p50 over seeds), at the default wavefront and at the one the native
-    autotuner picks (tuned on seeds 500.. of the same query)."""
+    (p50 over seeds 1000..), at the default wavefront and at the one the native
+    autotuner picks (tuned on seeds 500.. of the same query).  seeds: per-scene
+    counts (default grid 20, arm 10, SE(3) 20)."""
     from mpt_gb300 import planner as P
     from mpt_gb300 import scenes
+    seeds = seeds or {"grid_1024": 20, "arm_10link": 10, "se3_mesh": 20}
     res = {}
-    for name, mk, W in [("grid_1024", scenes.grid_scene, 2048), ("arm_10link", scenes.arm_scene, 4096),
-                        ("se3_mesh", scenes.mesh_scene, 4096)]:
-        sc = mk()
-        dflt, fp = _solve_stats(ctx, sc, W, seeds, cap_s, want_path=True)
-        r = {"default": dflt}
-        if cpu:
-            # the oracle's replay of the same wavefront planner (identical tree, all host
-            # cores; the exact kd-tree NN where it pays) on the first seed: a CPU port of the same run
-            import oracle
-            sp = oracle.make_space(sc["metric"], sc["dim"], sc["weights"])
-            prm = {"range": sc["range"], "goal_bias": 0.01, "goal_radius": sc["goal_radius"],
-                   "edge_step": sc["edge_step"], "resolution": sc["resolution"], "wavefront": W, "seed": 1000,
-                   "max_nodes": 1 << 21}
-            oracle.set_plan_nn("auto")
-            try:
-                t0 = time.perf_counter()
-                st, par, g = oracle.plan(sc, sp, prm, sc["lo"], sc["hi"], sc["start"], sc["goal"], 400, True)
-                cpu_s = time.perf_counter() - t0
-            finally:
-                oracle.set_plan_nn("brute")
-            gpu_first = r["default"]["seed_times_s"][0]
-            # the replay's best goal path (lowest cost, summed from the start) against the GPU's
-            same_path = None
-            if len(g) and fp is not None:
-                best = None
-                for gi in g:
-                    chain = [int(gi)]
-                    while par[chain[-1]] >= 0:
-                        chain.append(int(par[chain[-1]]))
-                    chain.reverse()
-                    c = 0.0
-                    for a, b in zip(chain[:-1], chain[1:]):
-                        c += oracle.distance(sp, st[a], st[b])
-                    if best is None or c < best[0]:
-                        best = (c, chain)
-                same_path = bool(len(best[1]) == len(fp[0]) and np.array_equal(st[best[1]], fp[0]) and
-                                 abs(best[0] - fp[1]) <= 1e-12 * max(1.0, best[0]))
-            r["cpu_port_seed1000"] = {"kind": "port (oracle replay of the same wavefront planner; exact CPU "
-                                              "kd-tree NN up to 7 dimensions, brute force above)",
-                                      "cores": os.cpu_count(), "wavefront": W, "s": cpu_s, "solved": len(g) > 0,
-                                      "nodes": len(st), "gpu_same_seed_s": gpu_first,
-                                      "ratio": cpu_s / gpu_first if gpu_first else None,
-                                      "same_path_and_cost_as_gpu": same_path}
+    for name, mk, W in SOLVE_SCENES:
+        sc = getattr(scenes, mk)()
+        n = seeds[name] if isinstance(seeds, dict) else int(seeds)
+        r = {"default": _solve_stats(ctx, sc, W, n, cap_s)}
         if tune:
             t0 = time.perf_counter()
             best, med = P.autotune_wavefront(ctx, P.Scenario(sc), sc["start"], trials=7, time_limit=1.0, seed=500)
             r["autotune"] = {"best": best, "median_s": {str(k): v for k, v in med.items()},
                              "tuning_s": time.perf_counter() - t0}
-            r["tuned"] = _solve_stats(ctx, sc, best, seeds, cap_s)
+            r["tuned"] = _solve_stats(ctx, sc, best, n, cap_s)
         res[name] = r
     return res
+
+
+# The reference's planners timed on this host: (scene, planner, threads) ->
+# (seeds, cap s).  threads 0 = every host core (the reference's OpenMP worker
+# pool); 1 = its single_threaded variant.  Bounded so the section stays within
+# about two minutes: the arm and SE(3) runs are validity-bound on the CPU and
+# take seconds each.
+REF_PLAN_RUNS = {
+    "grid_1024": {"prrt": [(1, 20, 5.0), (0, 20, 5.0)], "prrt_star": [(1, 20, 5.0), (0, 20, 5.0)],
+                  "pprm": [(1, 20, 5.0), (0, 20, 5.0)]},
+    "arm_10link": {"prrt": [(1, 3, 8.0), (0, 5, 8.0)], "prrt_star": [(0, 3, 8.0)],
+                   "pprm": [(1, 10, 8.0), (0, 10, 8.0)]},
+    "se3_mesh": {"prrt": [(0, 5, 8.0)], "prrt_star": [(0, 3, 8.0)], "pprm": [(0, 3, 8.0)]},
+}
+
+
+def reference_planners(runs=None):
+    """Time to the first solution of the reference's own PRRT, PRRT* and PPRM
+    (src/mpt/prrt.hpp, prrt_star.hpp, pprm.hpp, compiled by oracle/ref from the
+    reference headers) on the same three scenes, on this host's cores: the
+    oracle's valid(), the reference's DiscreteMotionValidator (joint-step check
+    on the arm), and the project-written exact NN container standing in for
+    nigh (absent from the reference).  An unsolved seed counts as the cap.
+    Returns None where the reference headers are not present."""
+    from oracle import ref
+    from mpt_gb300 import scenes
+    if not ref.available():
+        return None
+    ref.lib()
+    runs = runs or REF_PLAN_RUNS
+    out = {"kind": "reference (the reference's planners compiled from its headers; NN and collision stand-ins)",
+           "host_cores": os.cpu_count()}
+    for name, mk, _ in SOLVE_SCENES:
+        sc = getattr(scenes, mk)()
+        per = {}
+        for algo, cfgs in runs.get(name, {}).items():
+            for threads, nseeds, cap in cfgs:
+                rows = [ref.plan_solve(sc, 1000 + s_, algo=algo, threads=threads, time_limit_s=cap)
+                        for s_ in range(nseeds)]
+                t = sorted(r_["solve_s"] if r_["solved"] else cap for r_ in rows)
+                solved = [r_ for r_ in rows if r_["solved"]]
+                key = "%s_%s" % (algo, "1_core" if threads == 1 else "all_cores")
+                per[key] = {"threads": threads or os.cpu_count(), "seeds": nseeds, "cap_s": cap, "solved": len(solved),
+                            "p50_s": statistics.median(t), "max_s": t[-1],
+                            "median_cost": statistics.median([r_["cost"] for r_ in solved]) if solved else None,
+                            "median_nodes": statistics.median([r_["nodes"] for r_ in solved]) if solved else None}
+        out[name] = per
+    return out
 
 
 def _labelled_mesh_states(m, ctx, sc, n, seed):
@@ -534,7 +659,7 @@ def run_reference(args):
             "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform SO(2)^10 states)",
-            "config": {"workload": "nn_so2x10_1M", "tree_nodes": N_TREE, "queries_per_step": sample},
+            "config": dict(NN_CONFIG), "queries_per_step": sample,
             "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": cores, "kind": "port",
                              "sample": "%d queries per step against the full 1,048,576-node tree" % sample},
             "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -551,9 +676,11 @@ def run_gpu(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     ctx = m.Context(local)
-    if args.edges_only or args.solve_only or args.star_only or args.prm_only or args.sg_only:
+    if args.edges_only or args.solve_only or args.star_only or args.prm_only or args.sg_only or args.nn1m_only:
         # profiling modes: one secondary section alone
-        if args.edges_only:
+        if args.nn1m_only:
+            out = {"nn_1m": nn_1m_section(ctx, m, torch)}
+        elif args.edges_only:
             out = {"edge_checks": edge_rates(ctx, m, torch.cuda.current_stream(), torch)}
         elif args.star_only:
             out = {"prrt_star": prrt_star_section(ctx)}
@@ -563,6 +690,8 @@ def run_gpu(args):
             out = {"surrogate": surrogate_rates(ctx, m, torch, n_train=1 << 18, epochs=1)[0]}
         else:
             out = {"time_to_solve": solve_times(ctx, seeds=args.solve_seeds)}
+            if not args.no_ref_planners:
+                out["reference_planners"] = reference_planners()
         out["gpu_launches"] = ctx.kernel_launches()
         if rank == 0:
             print(json.dumps(out))
@@ -650,7 +779,9 @@ def run_gpu(args):
     # results of the host path equal the device path
     assert np.array_equal(hi.numpy(), tree.nearest(hq[(args.steps - 1) % nbuf])[0])
 
-    # secondary figures: edge checks/s (three scenes) and time to solve
+    # secondary figures: NN@1M on the other scenes and on planner-grown trees,
+    # edge checks/s (three scenes) and time to solve
+    nn1m = nn_1m_section(ctx, m, torch, peak=_peaks()[0]) if not args.no_nn1m else None
     edges = edge_rates(ctx, m, stream, torch)
     solves = solve_times(ctx) if not args.no_solve else None
     w_se3 = solves["se3_mesh"]["autotune"]["best"] if solves and "autotune" in solves["se3_mesh"] else None
@@ -664,10 +795,13 @@ def run_gpu(args):
     star = prrt_star_section(ctx, wave_for) if not (args.no_solve or args.no_star) else None
     prm = prm_section(ctx) if not (args.no_solve or args.no_prm) else None
 
-    # CPU baselines: oracle kd-tree and DMV on the host cores, bounded samples
+    # CPU baselines: oracle kd-tree and DMV on the host cores, bounded samples;
+    # the reference's own DMV and planners where its headers are present
     cpu = None
+    ref_plans = None
     if rank == 0:
         import oracle
+        from oracle import ref as oref
         from mpt_gb300 import scenes
         for name, mk in [("grid_1024", scenes.grid_scene), ("arm_10link", scenes.arm_scene),
                          ("se3_mesh", scenes.mesh_scene)]:
@@ -676,9 +810,19 @@ def run_gpu(args):
             osp = oracle.make_space(scx["metric"], scx["dim"], scx["weights"])
             oracle.valid_edges(scx, osp, ea[:64], eb[:64], scx["edge_step"], scx["resolution"])
             t0 = time.perf_counter()
-            oracle.valid_edges(scx, osp, ea, eb, scx["edge_step"], scx["resolution"])
+            want, _ = oracle.valid_edges(scx, osp, ea, eb, scx["edge_step"], scx["resolution"])
             edges[name]["cpu_edges_per_s"] = len(ea) / (time.perf_counter() - t0)
             edges[name]["cpu_cores"] = os.cpu_count()
+            if scx["resolution"] == 0 and oref.available():
+                # the reference's DiscreteMotionValidator itself (the arm's joint-step
+                # check has no reference counterpart: its demo bisects in L-infinity)
+                oref.dmv_edges(scx, ea[:64], eb[:64], scx["edge_step"])
+                t0 = time.perf_counter()
+                got, _ = oref.dmv_edges(scx, ea, eb, scx["edge_step"])
+                edges[name]["reference_dmv_edges_per_s"] = len(ea) / (time.perf_counter() - t0)
+                edges[name]["reference_dmv_equals_oracle"] = bool(np.array_equal(got, want))
+        if not args.no_solve and not args.no_ref_planners:
+            ref_plans = reference_planners()
         osp = oracle.make_space(sc["metric"], sc["dim"])
         ot = oracle.KDTree(osp, pts, 8)
         sample = 2048
@@ -698,8 +842,8 @@ def run_gpu(args):
                 "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
                 "data": "synthetic (seeded uniform SO(2)^10 states)",
-                "config": {"workload": "nn_so2x10_1M", "tree_nodes": N_TREE, "queries_per_step": nqb,
-                           "l2": "flushed (256 MiB write) between steps", "parallelism": "replicas"},
+                "config": dict(NN_CONFIG), "queries_per_step": nqb,
+                "l2": "flushed (256 MiB write) between steps", "parallelism": "replicas",
                 "e2e": {"value": e2e_val, "unit": "queries/s", "h2d_bytes_per_step": nqb * D * 8,
                         "d2h_bytes_per_step": nqb * 12},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -710,9 +854,13 @@ def run_gpu(args):
                              "kernel": "k_nearest<SO2,16>", "alg_bytes_per_launch": alg_bytes,
                              "counters_per_launch": per_launch},
                 "cpu_baseline": cpu,
+                "nn_1m": nn1m,
                 "edge_checks": {"unit": "edges/s", "per_scene": edges,
-                                "cpu_kind": "port (oracle DMV + exact validity, all host cores)"},
-                "time_to_solve": {"unit": "s", "planner": "plain wavefront PRRT (GPU)", "per_scene": solves},
+                                "cpu_kind": "port (oracle DMV + exact validity, all host cores)",
+                                "reference_kind": "the reference's DiscreteMotionValidator over the oracle's valid(), "
+                                                  "all host cores"},
+                "time_to_solve": {"unit": "s", "planner": "plain wavefront PRRT (GPU)", "per_scene": solves,
+                                  "reference_planners": ref_plans},
                 "learned_surrogate_se3": learned,
                 "batch_serving": serving,
                 "prrt_star": star,
@@ -734,6 +882,9 @@ def main():
     ap.add_argument("--nn-only", action="store_true", help="time the NN kernel only (profiling)")
     ap.add_argument("--no-solve", action="store_true", help="skip the time-to-solve, surrogate and serving runs")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-surrogate comparison")
+    ap.add_argument("--no-nn1m", action="store_true", help="skip the NN@1M runs of the other scenes")
+    ap.add_argument("--no-ref-planners", action="store_true", help="skip timing the reference's own planners")
+    ap.add_argument("--nn1m-only", action="store_true", help="the NN@1M runs of the other scenes only (profiling)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched serving run")
     ap.add_argument("--no-star", action="store_true", help="skip the PRRT* comparison")
     ap.add_argument("--star-only", action="store_true", help="the PRRT* comparison only (profiling)")
@@ -743,7 +894,7 @@ def main():
                     help="surrogate training (262,144 states, 1 epoch) and scoring rates only (profiling)")
     ap.add_argument("--edges-only", action="store_true", help="edge checks/s of the three scenes only (profiling)")
     ap.add_argument("--solve-only", action="store_true", help="time to solve of the three scenes only (profiling)")
-    ap.add_argument("--solve-seeds", type=int, default=5)
+    ap.add_argument("--solve-seeds", type=int, default=None, help="seeds per scene (default grid 20, arm 10, SE(3) 20)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

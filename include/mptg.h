@@ -114,13 +114,16 @@ mptg_status mptg_nearest_linear(mptg_tree* tree, const double* queries, size_t n
  * its own allocator.  Same results as mptg_nearest_linear on a tree holding
  * the same points (ids are row indices; lowest id on ties; -1 and +inf when
  * n == 0).  points, queries, idx_out and dist_out must be device memory of
- * the context's GPU; weights may be NULL (1, 1) or host memory.
+ * the context's GPU (or managed memory); host buffers and buffers of another
+ * GPU return MPTG_ERR_INVALID_ARG.  weights may be NULL (1, 1) or host memory.
  * Working memory is one static device array built into the library
  * (4 MiB + 256 bytes on every GPU that loads the library, kept until the
  * process exits), so n is at most 65,536 points of at most 16 dimensions;
  * a larger n returns MPTG_ERR_INVALID_ARG.  A device's first call looks up
  * the array's device address with cudaGetSymbolAddress and caches it: make
- * that first call before any stream capture.  All calls share the array and
+ * that first call before any stream capture.  A cudaDeviceReset after it
+ * leaves that cached address stale: do not call the entry point again in the
+ * same process after a device reset.  All calls share the array and
  * it keeps the last call's contents (each call clears what must start at
  * zero), so calls whose work overlaps on the GPU race: order them on one
  * stream.  Invalid points (NaN, SO2 angles outside [-pi, pi], non-unit
@@ -231,6 +234,12 @@ mptg_status mptg_planner_solution(mptg_planner* planner, double* path, size_t ca
 /* PRRT::visitGraph (prrt.hpp:300-316): all states and parent ids (-1 for starts). */
 mptg_status mptg_planner_graph(mptg_planner* planner, double* states, int32_t* parents, size_t cap,
                                size_t* n);
+/* The planner's nearest-neighbour container -- PRRT's nn_ member, the nigh
+ * tree its workers query (src/mpt/impl/prrt/prrt.hpp:121-122,406-409) -- as a
+ * borrowed tree handle: mptg_nearest / mptg_nearest_k / mptg_nearest_linear /
+ * mptg_tree_counters work on it; it stays owned by the planner (do not
+ * destroy or insert into it) and is valid until the planner is destroyed. */
+mptg_status mptg_planner_tree(mptg_planner* planner, mptg_tree** tree);
 /* ---- learned collision surrogate ------------------------------------
  * No counterpart in the reference.  An MLP in -> 256 -> 256 -> 256 -> 256 -> 1
  * (SiLU, BF16 weights/activations, FP32 accumulation) predicting the logit

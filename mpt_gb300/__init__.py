@@ -81,6 +81,18 @@ class Tree:
         _check(ctx.h, self.lib.mptg_tree_create(ctx.h, metric, dim, w.ctypes.data, capacity, ctypes.byref(h)))
         self.h = h
 
+    @classmethod
+    def borrow(cls, ctx: Context, handle, metric: int, dim: int, weights=(1.0, 1.0), owner=None):
+        """A Tree view of a handle another object owns (mptg_planner_tree):
+        queries only; closing it does not destroy the tree."""
+        t = cls.__new__(cls)
+        t.ctx, t.lib = ctx, ctx.lib
+        t.metric, t.dim = metric, dim
+        t._w = np.asarray(weights, dtype=np.float64)
+        t.h = handle
+        t._owner = owner
+        return t
+
     # nearest-neighbour strategies (mptg_nn_strategy)
     AUTO, KDTREE, EXHAUSTIVE = 0, 1, 2
 
@@ -141,7 +153,8 @@ class Tree:
 
     def close(self):
         if getattr(self, "h", None):
-            self.lib.mptg_tree_destroy(self.h)
+            if getattr(self, "_owner", None) is None:
+                self.lib.mptg_tree_destroy(self.h)
             self.h = None
 
     def __del__(self):

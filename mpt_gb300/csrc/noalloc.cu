@@ -14,7 +14,9 @@
 // process exits.  Host code must not pass the symbol itself to a kernel: on
 // the host it names a host-side stand-in, not device memory.  The device
 // address is looked up once per device with cudaGetSymbolAddress (on that
-// device's first call) and cached.
+// device's first call) and cached; a cudaDeviceReset (or any other reset of
+// the device's primary context) after that first call leaves the cached
+// address stale, so the entry point must not be called again in that process.
 #include "metrics.cuh"
 
 #define MPTG_NOALLOC_MAX_POINTS 65536
@@ -44,6 +46,18 @@ mptg_status scratch_address(mptg_ctx* ctx, float** out) {
     }
     *out = g_scratch_addr[dev];
     return MPTG_OK;
+}
+
+// true when p is memory that kernels on `device` can use directly: device
+// memory allocated on that device, or managed memory
+bool on_device(const void* p, int device) {
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (attr.type == cudaMemoryTypeManaged) return true;
+    return attr.type == cudaMemoryTypeDevice && attr.device == device;
 }
 
 // FP32 copy of the points into the scratch array, input checks and the
@@ -168,10 +182,12 @@ extern "C" mptg_status mptg_nearest_linear_noalloc(mptg_ctx* ctx, mptg_metric me
                          "fixed static array", MPTG_NOALLOC_MAX_POINTS, n);
     if (nq > (size_t)INT32_MAX / 32) return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "too many queries");
     if (nq == 0) return MPTG_OK;
-    if ((n && !mptg_is_device_ptr(points)) || !mptg_is_device_ptr(queries) || !mptg_is_device_ptr(idx_out) ||
-        !mptg_is_device_ptr(dist_out))
+    const int dev = ctx->device;
+    if ((n && !on_device(points, dev)) || !on_device(queries, dev) || !on_device(idx_out, dev) ||
+        !on_device(dist_out, dev))
         return mptg_fail(ctx, MPTG_ERR_INVALID_ARG,
-                         "mptg_nearest_linear_noalloc needs device buffers (host buffers would need staging memory)");
+                         "mptg_nearest_linear_noalloc needs device buffers of the context's GPU %d (host buffers "
+                         "would need staging memory; another GPU's buffers would need peer access)", dev);
     double w0 = weights ? weights[0] : 1.0, w1 = weights ? weights[1] : 1.0;
     if (metric == MPTG_METRIC_SE3 && !(w0 > 0 && w1 > 0))
         return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "SE3 weights must be positive");

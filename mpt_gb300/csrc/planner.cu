@@ -1040,6 +1040,12 @@ mptg_status mptg_planner_solution(mptg_planner* p, double* path, size_t cap, siz
     return planner_solution(p, path, cap, len, cost, true);
 }
 
+mptg_status mptg_planner_tree(mptg_planner* p, mptg_tree** tree) {
+    if (!p || !tree) return MPTG_ERR_INVALID_ARG;
+    *tree = p->tree;
+    return MPTG_OK;
+}
+
 mptg_status mptg_planner_graph(mptg_planner* p, double* states, int32_t* parents, size_t cap, size_t* n) {
     if (!p || !n) return MPTG_ERR_INVALID_ARG;
     size_t sz = 0;

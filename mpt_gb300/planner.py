@@ -27,7 +27,7 @@ import time
 
 import numpy as np
 
-from . import Context, MptgError, Scene, _check, load
+from . import Context, MptgError, Scene, Tree, _check, load
 
 
 # ------------------------------------------------------------------ option tags
@@ -136,6 +136,7 @@ def _sig(L):
         ("mptg_planner_goals", ctypes.c_int, [P, ctypes.POINTER(S)]),
         ("mptg_planner_solution", ctypes.c_int, [P, P, S, ctypes.POINTER(S), ctypes.POINTER(ctypes.c_double)]),
         ("mptg_planner_graph", ctypes.c_int, [P, P, P, S, ctypes.POINTER(S)]),
+        ("mptg_planner_tree", ctypes.c_int, [P, ctypes.POINTER(P)]),
         ("mptg_planner_stats", ctypes.c_int, [P, P]),
         ("mptg_planner_timers", ctypes.c_int, [P, P]),
         ("mptg_planner_set_rewire", ctypes.c_int, [P, ctypes.c_int, ctypes.c_double]),
@@ -341,6 +342,15 @@ class Planner:
         _check(self.ctx.h, self.lib.mptg_planner_graph(self.h, states.ctypes.data, parents.ctypes.data, n.value,
                                                        ctypes.byref(n)))
         return states, parents
+
+    def tree(self):
+        """The planner's nearest-neighbour tree (PRRT's nn_, prrt.hpp:121-122) as a
+        borrowed ``Tree``: nearest / nearest_k / counters on the planner-grown
+        tree.  Owned by the planner; valid while the planner is open."""
+        self._create()
+        h = ctypes.c_void_p()
+        _check(self.ctx.h, self.lib.mptg_planner_tree(self.h, ctypes.byref(h)))
+        return Tree.borrow(self.ctx, h, self.scene.metric, self.scene.dim, self.scene.weights, owner=self)
 
     def visit_graph(self, visitor):
         states, parents = self.graph()

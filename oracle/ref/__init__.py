@@ -1,14 +1,16 @@
 """Reference-built checker -- TEST INFRASTRUCTURE ONLY.
 
-Compiles the MPT reference's own headers (from the reference source tree,
-read in place; nothing is copied) through ref_driver.cpp against the
+Compiles the MPT reference's own headers through ref_driver.cpp against the
 project-written nigh/Eigen stand-ins in shim/, together with the oracle, into
-oracle/_ref/libref.so.  Only possible where the reference sources exist; the
-tests that use it skip otherwise.  Recipe (what build() runs):
+oracle/_ref/libref.so.  The headers come from MPT_REFERENCE_SRC when that is
+set, else from the git-ignored copy that oracle/ref/stage.py writes into
+oracle/_ref/src (the copy travels with oracle/_ref to hosts without a
+reference tree, so the checker builds there too).  The tests that use it skip
+where neither exists.  Recipe (what build_if_available() runs):
 
   gcc -O2 -ffp-contract=off -fPIC -c oracle/oracle.c -o oracle/_ref/oracle.o
   g++ -O2 -ffp-contract=off -std=c++17 -DNDEBUG -DMPT_LOG_LEVEL=WARN -Wno-attributes -fPIC -shared -fopenmp \
-      -I oracle/ref/shim -I <reference>/src oracle/ref/ref_driver.cpp \
+      -I oracle/ref/shim -I <reference src> oracle/ref/ref_driver.cpp \
       oracle/_ref/oracle.o -o oracle/_ref/libref.so
 """
 from __future__ import annotations
@@ -21,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
 LIB = os.path.join(OUT, "libref.so")
-REFERENCE_SRC = os.environ.get("MPT_REFERENCE_SRC", "/root/reference/src")
+REFERENCE_SRC = os.environ.get("MPT_REFERENCE_SRC") or os.path.join(OUT, "src")
 
 
 def available() -> bool:
@@ -34,6 +36,9 @@ def build_if_available(force: bool = False):
     srcs = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(ORACLE, "oracle.c"), os.path.join(ORACLE, "oracle.h")]
     for d, _, files in os.walk(os.path.join(HERE, "shim")):
         srcs += [os.path.join(d, f) for f in files]
+    marker = os.path.join(REFERENCE_SRC, "STAGED_FILES")
+    if os.path.exists(marker):
+        srcs.append(marker)
     if not force and os.path.exists(LIB) and all(os.path.getmtime(s) <= os.path.getmtime(LIB) for s in srcs):
         return LIB
     os.makedirs(OUT, exist_ok=True)
@@ -61,6 +66,8 @@ def lib():
         L = ctypes.CDLL(path)
         P = ctypes.c_void_p
         L.ref_dmv_edges.argtypes = [P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_longlong, ctypes.c_double, P, P]
+        L.ref_dmv_edges_mt.argtypes = [P, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_longlong, ctypes.c_double, P, P,
+                                       ctypes.c_int]
         L.ref_interpolate.argtypes = [ctypes.c_int, ctypes.c_int, P, P, ctypes.c_double, P]
         L.ref_goal_l2.argtypes = [P, ctypes.c_double, P, P]
         D = ctypes.c_double
@@ -75,6 +82,30 @@ def lib():
 
 
 PLANNERS = {"prrt": 0, "prrt_star": 1, "pprm": 2}
+
+
+def dmv_edges(desc: dict, a, b, step: float, threads: int = 0):
+    """The reference's DiscreteMotionValidator (discrete_motion_validator.hpp:
+    71-130) over the oracle's valid(), per edge on `threads` OpenMP threads
+    (0 = all): (booleans uint8 [n], valid() calls int64 [n]).  Grid (L2, 2-D),
+    planar arm (SO(2)^10) and SE(3) (weights 2/1, the reference's slerp with
+    glibc acos/sin) scenes."""
+    import numpy as np
+
+    from oracle import _ptr, make_scene
+
+    L = lib()
+    sc, keep = make_scene(desc)
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    n = a.shape[0]
+    out = np.empty(n, np.uint8)
+    cnt = np.empty(n, np.int64)
+    r = L.ref_dmv_edges_mt(ctypes.byref(sc), int(desc["metric"]), int(desc["dim"]), _ptr(a), _ptr(b), n, float(step),
+                           _ptr(out), _ptr(cnt), int(threads))
+    if r != 0:
+        raise ValueError("no reference DMV instantiation for metric %s dim %s" % (desc["metric"], desc["dim"]))
+    return out, cnt
 
 
 def plan_solve(desc: dict, seed: int, algo: str = "prrt", threads: int = 1, time_limit_s: float = 30.0,

@@ -12,6 +12,7 @@
 // between ref_dmv_edges and orc_valid_edges isolates the DMV restatement.
 #include <omp.h>
 
+#include <algorithm>
 #include <array>
 #include <chrono>
 #include <cmath>
@@ -102,6 +103,51 @@ std::array<double, 7> interpolate(const SE3Space& space, const std::array<double
     std::array<double, 7> q;
     orc_interpolate(&space.sp, a.data(), b.data(), t, q.data());
     return q;
+}
+
+// The same SE(3) metric evaluated with glibc's acos, and interpolated by the
+// reference's own SO(3) slerp (so3_space.hpp:44-83, glibc acos/sin) on the
+// quaternion and its L2 interpolate (lp_space.hpp:44-54) on the position, as
+// nigh's Cartesian space combines its parts (cartesian_space.hpp:43-68).  The
+// DMV over this space is the reference's SE(3) motion check with the
+// reference's own transcendental functions; only valid() is the oracle's.
+struct SE3GlibcTag {};
+using SE3GlibcSpace = nm::Space<std::array<double, 7>, SE3GlibcTag>;
+
+}  // namespace
+
+namespace unc::robotics::nigh::metric {
+template <>
+struct Space<std::array<double, 7>, SE3GlibcTag> {
+    using Type = std::array<double, 7>;
+    using Distance = double;
+    static constexpr int kDimensions = 7;
+    double w0 = 2.0, w1 = 1.0;
+    constexpr unsigned dimensions() const { return 7; }
+    Distance distance(const Type& a, const Type& b) const {
+        double d = std::abs(a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3]);
+        if (d > 1.0) d = 1.0;
+        double s = 0;
+        for (int i = 4; i < 7; ++i) {
+            double x = a[i] - b[i];
+            s += x * x;
+        }
+        return w0 * std::acos(d) + w1 * std::sqrt(s);
+    }
+};
+}  // namespace unc::robotics::nigh::metric
+
+namespace {
+
+std::array<double, 7> interpolate(const SE3GlibcSpace&, const std::array<double, 7>& a,
+                                  const std::array<double, 7>& b, double t) {
+    nm::Space<std::array<double, 4>, nm::SO3> so3;
+    nm::Space<std::array<double, 3>, nm::LP<2>> r3;
+    std::array<double, 4> qa{a[0], a[1], a[2], a[3]}, qb{b[0], b[1], b[2], b[3]};
+    std::array<double, 3> pa{a[4], a[5], a[6]}, pb{b[4], b[5], b[6]};
+    std::array<double, 4> q = mpt::interpolate(so3, qa, qb, t);
+    std::array<double, 3> p = mpt::interpolate(r3, pa, pb, t);
+    return {q[0], q[1], q[2], q[3], p[0], p[1], p[2]};
 }
 
 // A SeedSequence that gives each generator seeded from it its own stream:
@@ -365,12 +411,30 @@ int plan_algo(int algo, A... args) {
 
 extern "C" {
 
-// metric: 0 L2 (dim 2 or 3), 1 SO2 (dim 1 or 10), 2 SO3 (dim 4); returns 0 on success
+// metric: 0 L2 (dim 2), 1 SO2 (dim 10), 3 SE3 with weights (2, 1) and glibc's
+// acos/sin (dim 7); returns 0 on success
 int ref_dmv_edges(const orc_scene* sc, int metric, int dim, const double* a, const double* b, long long n,
                   double step, uint8_t* out, long long* samples) {
     if (metric == 0 && dim == 2) dmv<nm::Space<std::array<double, 2>, nm::LP<2>>, 2>(sc, a, b, n, step, out, samples);
     else if (metric == 1 && dim == 10) dmv<nm::Space<std::array<double, 10>, nm::SO2<1>>, 10>(sc, a, b, n, step, out, samples);
+    else if (metric == 3 && dim == 7) dmv<SE3GlibcSpace, 7>(sc, a, b, n, step, out, samples);
     else return 1;
+    return 0;
+}
+
+// ref_dmv_edges over nthreads OpenMP threads (0 = all), edges split evenly:
+// the reference's motion check timed on the host's cores
+int ref_dmv_edges_mt(const orc_scene* sc, int metric, int dim, const double* a, const double* b, long long n,
+                     double step, uint8_t* out, long long* samples, int nthreads) {
+    if (!((metric == 0 && dim == 2) || (metric == 1 && dim == 10) || (metric == 3 && dim == 7))) return 1;
+    orc_state_valid(sc, a);  // builds the oracle's mesh BVH before any thread reads it
+    int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+    long long chunk = (n + nt - 1) / nt;
+#pragma omp parallel for num_threads(nt) schedule(static, 1)
+    for (int t = 0; t < nt; ++t) {
+        long long lo = t * chunk, hi = std::min(n, lo + chunk);
+        if (lo < hi) ref_dmv_edges(sc, metric, dim, a + lo * dim, b + lo * dim, hi - lo, step, out + lo, samples + lo);
+    }
     return 0;
 }
 

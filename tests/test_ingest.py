@@ -167,8 +167,9 @@ def test_obstacle_filter_tolerance():
 
 
 def test_reference_demo_png_decodes():
-    from oracle.ref import REFERENCE_SRC
-    path = os.path.join(os.path.dirname(REFERENCE_SRC), "demo", "png_planning_input.png")
+    from oracle.ref import stage
+    src = os.environ.get("MPT_REFERENCE_SRC") or stage.DEFAULT_SOURCE
+    path = os.path.join(os.path.dirname(src), "demo", "png_planning_input.png")
     if not os.path.exists(path):
         pytest.skip("reference demo image not present")
     sc = ingest.png_grid_scene(path, (430.0, 1300.0), (3150.0, 950.0))

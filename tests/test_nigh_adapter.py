@@ -1,9 +1,10 @@
-"""CPU: the nigh adapter (include/mptg_nigh.hpp) under the reference's own
-PRRT, PRRT* and PPRM, compiled in place (skipped where the reference sources
-are absent).  The program runs against the CPU stand-in of the C ABI's
-nearest-neighbour calls (tests/cpp/fake_mptg_nn.cpp), which checks the
-adapter's bookkeeping; a second build links the same program against the real
-libmptg to check the adapter's calls against the ABI it ships with."""
+"""The nigh adapter (include/mptg_nigh.hpp) under the reference's own PRRT,
+PRRT* and PPRM, compiled from the reference headers (staged into
+oracle/_ref/src; skipped where they are absent).  On the CPU the program runs
+against the CPU stand-in of the C ABI's nearest-neighbour calls
+(tests/cpp/fake_mptg_nn.cpp), which checks the adapter's bookkeeping, and a
+second build links it against the real libmptg; on the GPU that second build
+runs, with the device kd-tree answering every query."""
 import os
 import subprocess
 
@@ -34,6 +35,24 @@ def test_nigh_adapter_links_against_libmptg(tmp_path):
     from mpt_gb300 import build
     libdir = os.path.dirname(build.build())
     subprocess.check_call(FLAGS + ["-L", libdir, "-lmptg", "-Wl,-rpath," + libdir, "-o", str(tmp_path / "na_gpu")])
+
+
+@pytest.mark.gpu
+def test_nigh_adapter_on_gpu(tmp_path):
+    """MPT's own PRRT (single-threaded and with its OpenMP workers), PRRT* and
+    PPRM over PRRT<mpt_gb300::GpuKDTree> and friends, with every nearest and
+    k-nearest call answered by the device kd-tree of the real libmptg: the
+    container checks against brute force and the planners' acceptance rules
+    (test/planner_integration_test.hpp:219-291) pass."""
+    from mpt_gb300 import build
+    libdir = os.path.dirname(build.build())
+    exe = str(tmp_path / "na_gpu")
+    subprocess.check_call(FLAGS + ["-L", libdir, "-lmptg", "-Wl,-rpath," + libdir, "-o", exe])
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "nigh adapter OK" in r.stdout
+    for name in ("PRRT:", "PRRT, OpenMP workers:", "PRRT*:", "PPRM:"):
+        assert name in r.stdout
 
 
 def test_nigh_adapter_under_sanitizers(tmp_path):

@@ -255,3 +255,56 @@ def test_reference_pprm_on_the_sample_stream_equals_the_replay(orc, mk, nsamples
     want = r["states"][r["path"]]
     assert len(want) > 0 or mk is scenes.mesh_scene
     assert len(path) == len(want) and np.array_equal(path.view(np.int64), want.view(np.int64))
+
+
+def _near_contact_edges(sc, n, seed):
+    """SE(3) edges that start near a box face (scenes.near_contact_states) and
+    end within the steer range: translation toward a random state, rotation a
+    fraction of the way toward a random orientation."""
+    a = scenes.near_contact_states(sc, n, seed)
+    c = scenes.uniform_states(sc, n, seed + 1)
+    rng = np.random.default_rng(seed + 2)
+    b = np.empty_like(a)
+    for i in range(n):
+        frac = rng.uniform(0.2, 1.0)
+        dp = c[i, 4:] - a[i, 4:]
+        t = min(1.0, sc["range"] * frac / max(np.linalg.norm(dp), 1e-12))
+        qa, qc = a[i, :4], c[i, :4]
+        if np.dot(qa, qc) < 0:
+            qc = -qc
+        q = qa + (qc - qa) * min(1.0, 0.5 * frac)
+        b[i] = np.concatenate([q / np.linalg.norm(q), a[i, 4:] + dp * t])
+    return a, b
+
+
+def test_se3_dmv_with_glibc_slerp_agrees(orc):
+    """The SE(3) motion check of the reference's own code -- its
+    DiscreteMotionValidator over its SO(3) slerp (so3_space.hpp:44-83) and L2
+    interpolate, with glibc's acos/sin and a glibc-acos metric for the step
+    count -- against the oracle's, which uses the deterministic mptg_acos /
+    mptg_sin (the functions the device shares).  On 1,500 edges starting at
+    free states near box faces (where a last-ulp change of a sample state is most likely to flip
+    a collision test), every boolean and every count of valid() calls agree:
+    the two transcendental implementations do not change a single SE(3) edge
+    decision on this set."""
+    L = ref.lib()
+    sc = scenes.mesh_scene()
+    sp = orc.make_space(sc["metric"], sc["dim"], sc["weights"])
+    a, b = _near_contact_edges(sc, 16000, 4242)
+    free = np.nonzero(orc.valid_states(sc, sp, a) == 1)[0][:1500]  # the edge's outcome rests on its samples
+    a = np.ascontiguousarray(a[free])
+    b = np.ascontiguousarray(b[free])
+    csc, keep = orc.make_scene(sc)
+    n = len(a)
+    out = np.empty(n, np.uint8)
+    cnt = np.empty(n, np.int64)
+    assert L.ref_dmv_edges(ctypes.byref(csc), 3, 7, _p(a), _p(b), n, sc["edge_step"], _p(out), _p(cnt)) == 0
+    got = np.empty(n, np.uint8)
+    gcnt = np.empty(n, np.int64)
+    for i in range(n):
+        g, c = orc.valid_edges(sc, sp, a[i:i + 1], b[i:i + 1], sc["edge_step"], 0, nthreads=1)
+        got[i], gcnt[i] = g[0], c
+    # a mixed set: both outcomes present, and edges long enough to need many samples
+    assert n == 1500 and 0.1 < out.mean() < 0.9 and cnt.max() > 20
+    disagree = np.nonzero((got != out) | (gcnt != cnt))[0]
+    assert len(disagree) == 0, [(int(i), int(got[i]), int(out[i]), int(gcnt[i]), int(cnt[i])) for i in disagree[:10]]
