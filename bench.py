@@ -218,6 +218,7 @@ def nn_1m_section(ctx, m, torch, steps=5, peak=None, cpu_sample=2048):
              ("arm_so2x10_planner_grown", scenes.arm_scene, "grown"), ("se3_planner_grown", scenes.mesh_scene, "grown"),
              ("grid_l2_planner_grown", scenes.grid_scene, "grown")]
     for name, mk, how in cases:
+        _progress("NN@1M: " + name)
         sc = mk()
         D = sc["dim"]
         pl = None
@@ -351,9 +352,9 @@ def solve_times(ctx, seeds=None, cap_s=20.0, tune=True):
 REF_PLAN_RUNS = {
     "grid_1024": {"prrt": [(1, 20, 5.0), (0, 20, 5.0)], "prrt_star": [(1, 20, 5.0), (0, 20, 5.0)],
                   "pprm": [(1, 20, 5.0), (0, 20, 5.0)]},
-    "arm_10link": {"prrt": [(1, 3, 8.0), (0, 5, 8.0)], "prrt_star": [(0, 3, 8.0)],
-                   "pprm": [(1, 10, 8.0), (0, 10, 8.0)]},
-    "se3_mesh": {"prrt": [(0, 5, 8.0)], "prrt_star": [(0, 3, 8.0)], "pprm": [(0, 3, 8.0)]},
+    "arm_10link": {"prrt": [(1, 2, 5.0), (0, 5, 5.0)], "prrt_star": [(0, 2, 5.0)],
+                   "pprm": [(1, 10, 5.0), (0, 10, 5.0)]},
+    "se3_mesh": {"prrt": [(0, 5, 5.0)], "prrt_star": [(0, 2, 5.0)], "pprm": [(0, 2, 5.0)]},
 }
 
 
@@ -667,6 +668,15 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def _progress(msg):
+    """One line per bench section on stderr (the JSON line goes to stdout)."""
+    sys.stderr.write("[bench %.1fs] %s\n" % (time.perf_counter() - _T0, msg))
+    sys.stderr.flush()
+
+
+_T0 = time.perf_counter()
+
+
 def run_gpu(args):
     import torch
     import mpt_gb300 as m
@@ -696,6 +706,7 @@ def run_gpu(args):
         if rank == 0:
             print(json.dumps(out))
         return
+    _progress("headline tree")
     sc, pts = _workload()
     tree = m.Tree(ctx, sc["metric"], sc["dim"], N_TREE)
     t0 = time.perf_counter()
@@ -758,6 +769,7 @@ def run_gpu(args):
                               "counters_per_launch": per_launch, "gpu_launches": launches}))
         return
 
+    _progress("headline e2e")
     # end to end through the C ABI with pinned host buffers
     hq_pinned = [torch.from_numpy(x).pin_memory() for x in hq]
     hi = torch.empty(nqb, dtype=torch.int32).pin_memory()
@@ -781,20 +793,28 @@ def run_gpu(args):
 
     # secondary figures: NN@1M on the other scenes and on planner-grown trees,
     # edge checks/s (three scenes) and time to solve
+    _progress("NN@1M of the other scenes")
     nn1m = nn_1m_section(ctx, m, torch, peak=_peaks()[0]) if not args.no_nn1m else None
+    _progress("edge checks")
     edges = edge_rates(ctx, m, stream, torch)
+    _progress("time to solve")
     solves = solve_times(ctx) if not args.no_solve else None
     w_se3 = solves["se3_mesh"]["autotune"]["best"] if solves and "autotune" in solves["se3_mesh"] else None
+    _progress("learned surrogate")
     learned = (learned_vs_plain(ctx, m, torch, wavefront_tuned=w_se3)
                if not (args.no_solve or args.no_learned) else None)
     wave_for = None
     if solves and all("autotune" in solves[k] for k in solves):
         wave_for = {"grid": solves["grid_1024"]["autotune"]["best"], "arm": solves["arm_10link"]["autotune"]["best"],
                     "mesh": solves["se3_mesh"]["autotune"]["best"]}
+    _progress("batched serving")
     serving = batch_serving(m, ctx, wave_for=wave_for) if not (args.no_solve or args.no_batch) else None
+    _progress("PRRT*")
     star = prrt_star_section(ctx, wave_for) if not (args.no_solve or args.no_star) else None
+    _progress("PPRM")
     prm = prm_section(ctx) if not (args.no_solve or args.no_prm) else None
 
+    _progress("CPU baselines")
     # CPU baselines: oracle kd-tree and DMV on the host cores, bounded samples;
     # the reference's own DMV and planners where its headers are present
     cpu = None
@@ -822,6 +842,7 @@ def run_gpu(args):
                 edges[name]["reference_dmv_edges_per_s"] = len(ea) / (time.perf_counter() - t0)
                 edges[name]["reference_dmv_equals_oracle"] = bool(np.array_equal(got, want))
         if not args.no_solve and not args.no_ref_planners:
+            _progress("reference planners")
             ref_plans = reference_planners()
         osp = oracle.make_space(sc["metric"], sc["dim"])
         ot = oracle.KDTree(osp, pts, 8)
@@ -851,7 +872,7 @@ def run_gpu(args):
                              "traffic_source": "ncu dram__bytes_read+write of a 32,768-query launch, scaled by "
                                                "queries (profiles/k_nearest_so2x10_1M.md)",
                              "peak_source": peak_kind,
-                             "kernel": "k_nearest<SO2,16>", "alg_bytes_per_launch": alg_bytes,
+                             "kernel": "k_nearest<SO2,10>", "alg_bytes_per_launch": alg_bytes,
                              "counters_per_launch": per_launch},
                 "cpu_baseline": cpu,
                 "nn_1m": nn1m,
@@ -873,6 +894,8 @@ def run_gpu(args):
 
 
 def main():
+    import faulthandler
+    faulthandler.enable()  # a native crash prints the Python stack on stderr
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)

@@ -1,0 +1,322 @@
+// bplan.cu - the wavefront PRRT as one persistent thread block per query.
+//
+// The multi-kernel wavefront of planner.cu spends most of a small query's
+// time on launches and host round trips: a first path across the 1024^2 grid
+// needs about 60 wavefronts, each of which is a handful of tiny kernels, two
+// host synchronisations and a kd-tree insert.  This kernel runs the same
+// wavefront loop -- PRRT::Worker::addSample of src/mpt/impl/prrt/prrt.hpp:
+// 411-452 for W samples at once -- without leaving the GPU: one 1024-thread
+// block per query, the tree's FP32 node copy in shared memory, every phase
+// separated by a block barrier, and the stop conditions (solved, node budget,
+// wavefront count, time) decided on the device.
+//
+// Per wavefront (identical, bit for bit, to plan_wavefront in planner.cu):
+//   goal pick and samples   the Philox stream of sampler.cuh, sample i of
+//                           wavefront w; at most one goal sample (the lowest
+//                           i whose bias draw hits) until the first solution
+//   nearest                 exact FP64 nearest node, lowest id on ties: an
+//                           FP32 sweep over the shared-memory copy (W samples
+//                           x P = 1024 / W node slices) re-ranks in FP64 every
+//                           node that could reach the slice's best (err32),
+//                           then the slices merge
+//   steer                   interpolate to `range` (skip when d == 0)
+//   link                    the DMV of the grid scene (scene.cu's two phases,
+//                           a warp per edge, the same sample order and counts)
+//   insert                  block scan of the accepted flags in sample order,
+//                           node budget, parent ids, goal flags
+// The kd-tree is brought up to date by the host after the block returns.
+#include "bplan.cuh"
+#include "grid.cuh"
+#include "sampler.cuh"
+#include "umma.cuh"
+
+namespace {
+
+struct BSmem {
+    float2* pts;   // [cap] FP32 node copy
+    double* q;     // [W][2] samples
+    double* nw;    // [W][2] new states
+    double* nd;    // [W] nearest distance
+    double* bd;    // [T] per-thread best distance of its node slice
+    int* ni;       // [W] nearest id (-1: none)
+    int* fl;       // [W] bit 0 link valid, bit 1 skipped (d == 0)
+    int* bi;       // [T] per-thread best id
+};
+
+__device__ __forceinline__ BSmem carve(unsigned char* base, int cap, int W, int T) {
+    BSmem s;
+    size_t o = 0;
+    s.pts = reinterpret_cast<float2*>(base + o); o += (size_t)cap * sizeof(float2);
+    s.q = reinterpret_cast<double*>(base + o); o += (size_t)W * 2 * sizeof(double);
+    s.nw = reinterpret_cast<double*>(base + o); o += (size_t)W * 2 * sizeof(double);
+    s.nd = reinterpret_cast<double*>(base + o); o += (size_t)W * sizeof(double);
+    s.bd = reinterpret_cast<double*>(base + o); o += (size_t)T * sizeof(double);
+    s.ni = reinterpret_cast<int*>(base + o); o += (size_t)W * sizeof(int);
+    s.fl = reinterpret_cast<int*>(base + o); o += (size_t)W * sizeof(int);
+    s.bi = reinterpret_cast<int*>(base + o);
+    return s;
+}
+
+size_t smem_bytes(int cap, int W, int T) {
+    return (size_t)cap * sizeof(float2) + (size_t)W * (2 + 2 + 1) * sizeof(double) + (size_t)T * sizeof(double) +
+           (size_t)W * 2 * sizeof(int) + (size_t)T * sizeof(int);
+}
+
+__device__ __forceinline__ float maxabs_ru(double x, double y) {
+    return fmaxf(__double2float_ru(fabs(x)), __double2float_ru(fabs(y)));
+}
+
+// cap_alloc / W_alloc: the shared-memory layout of this launch (the largest
+// job's); every job of the launch fits in it
+__global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob* __restrict__ jobs, int cap_alloc,
+                                                                 int W_alloc) {
+    extern __shared__ __align__(16) unsigned char bp_smem[];
+    __shared__ int s_n, s_goals, s_maxabs, s_gidx, s_stop, s_total;
+    __shared__ int s_wsum[32];
+    __shared__ unsigned long long s_cnt;
+    const BPlanJob& J = jobs[blockIdx.x];
+    const int T = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5, nwarps = T >> 5;
+    const int W = J.W, cap = J.cap;
+    const BSmem S = carve(bp_smem, cap_alloc, W_alloc, T);
+    if (t == 0) {
+        s_n = J.ctr->n;
+        s_goals = J.ctr->goals;
+        s_maxabs = 0;
+        s_cnt = 0;
+    }
+    __syncthreads();
+    for (int j = t; j < s_n; j += T) {
+        const double x = J.states[2 * j], y = J.states[2 * j + 1];
+        S.pts[j] = make_float2(__double2float_rn(x), __double2float_rn(y));
+        atomicMax(&s_maxabs, __float_as_int(maxabs_ru(x, y)));
+    }
+    uint32_t wave = J.ctr->wave;
+    int waves_run = 0, status = BPLAN_DONE;
+    unsigned long long samples = 0, accepted = 0;
+    const int P = T / W;  // node slices per sample
+    const uint64_t t0 = umma::globaltimer_ns();
+    __syncthreads();
+    for (;;) {
+        // the run loop's stop checks (mptg_planner_run), decided by one thread
+        if (t == 0) {
+            int st = 0;
+            if (J.stop_when_solved && s_goals > 0) st = 1;
+            else if ((size_t)s_n >= J.max_nodes) st = 1;
+            else if (J.max_waves > 0 && waves_run >= J.max_waves) st = 1;
+            else if (s_n + W > cap) st = 2;
+            else if (J.deadline_ns && umma::globaltimer_ns() - t0 >= J.deadline_ns) st = 1;
+            s_stop = st;
+            s_gidx = INT_MAX;
+        }
+        __syncthreads();
+        if (s_stop) {
+            status = s_stop == 2 ? BPLAN_FULL : BPLAN_DONE;
+            break;
+        }
+        const int n = s_n;
+        // goal sample: the lowest index whose bias draw hits (k_plan_goalpick)
+        const bool bias_on = s_goals == 0 && J.has_goal && J.goal_bias > 0;
+        if (bias_on && t < W && phx_uniform(J.seed, (uint32_t)t, wave, 16) < J.goal_bias) atomicMin(&s_gidx, t);
+        __syncthreads();
+        if (t < W) {
+            double* q = S.q + 2 * t;
+            if (bias_on && t == s_gidx) {
+                q[0] = J.goal[0];
+                q[1] = J.goal[1];
+            } else {
+                sample_uniform_state(MPTG_METRIC_L2, 2, J.seed, (uint32_t)t, wave, J.lo, J.hi, q);
+            }
+        }
+        __syncthreads();
+        // nearest: sample t % W over node slice t / W
+        if (t < P * W) {
+            const int i = t % W, part = t / W;
+            const double* qd = S.q + 2 * i;
+            const float q32[2] = {__double2float_rn(qd[0]), __double2float_rn(qd[1])};
+            const float M = fmaxf(__int_as_float(s_maxabs), maxabs_ru(qd[0], qd[1]));
+            const float E = err32<MPTG_METRIC_L2>(2, M, 1.f, 1.f);
+            double best = INFINITY;
+            int bid = INT_MAX;
+            float bup = INFINITY;
+            for (int j = part; j < n; j += P) {
+                const float2 pj = S.pts[j];
+                const float p32[2] = {pj.x, pj.y};
+                const float d32 = dist32<MPTG_METRIC_L2, 2>(q32, p32, 1.f, 1.f);
+                // every node that could beat or tie the best in exact arithmetic
+                if (__fsub_rd(d32, E) <= bup) {
+                    const double d = l2_dist64(qd, J.states + 2 * j, 2);
+                    if (d < best || (d == best && j < bid)) {
+                        best = d;
+                        bid = j;
+                        bup = __double2float_ru(best);
+                    }
+                }
+            }
+            S.bd[t] = best;
+            S.bi[t] = bid;
+        }
+        __syncthreads();
+        // merge the slices, then steer (k_plan_steer)
+        if (t < W) {
+            double best = S.bd[t];
+            int bid = S.bi[t];
+            for (int p = 1; p < P; ++p) {
+                const double d = S.bd[p * W + t];
+                const int id = S.bi[p * W + t];
+                if (d < best || (d == best && id < bid)) {
+                    best = d;
+                    bid = id;
+                }
+            }
+            const int id = bid == INT_MAX ? -1 : bid;
+            const double* s = S.q + 2 * t;
+            double* nw = S.nw + 2 * t;
+            S.ni[t] = id;
+            S.nd[t] = best;
+            const bool skip = id < 0 || best == 0.0 || !(best == best);  // prrt.hpp:425
+            if (!skip && best > J.range) {
+                const double a[2] = {J.states[2 * id], J.states[2 * id + 1]};
+                interp64(MPTG_METRIC_L2, 2, a, s, __ddiv_rn(J.range, best), nw);
+            } else {
+                nw[0] = s[0];
+                nw[1] = s[1];
+            }
+            S.fl[t] = skip ? 2 : 0;
+        }
+        __syncthreads();
+        // link(near, new): warp per edge, k_grid_edges_a then k_grid_edges_b
+        for (int e = warp; e < W; e += nwarps) {
+            const bool skip = (S.fl[e] & 2) != 0;
+            const double* Bp = S.nw + 2 * e;
+            const double B[2] = {Bp[0], Bp[1]};
+            double A[2];
+            if (skip) {
+                A[0] = S.q[2 * e];
+                A[1] = S.q[2 * e + 1];
+            } else {
+                const int id = S.ni[e];
+                A[0] = J.states[2 * id];
+                A[1] = J.states[2 * id + 1];
+            }
+            unsigned long long cnt = 1;
+            bool ok = grid_valid_f(J.scene, B);
+            long long steps = ok ? grid_edge_steps(A, B, J.inv_step) : 0;
+            if (steps < 0) ok = false;
+            if (ok && steps >= 2) {
+                float a32[2], dir32[2];
+                for (int d = 0; d < 2; ++d) {
+                    a32[d] = __double2float_rn(A[d]);
+                    dir32[d] = __double2float_rn(__dsub_rn(B[d], A[d]));
+                }
+                const float eps =
+                    8.f * U32 * (fabsf(a32[0]) + fabsf(a32[1]) + fabsf(dir32[0]) + fabsf(dir32[1]) + 1.f);
+                const int Mi = (int)steps - 1;
+                const int R = (Mi + 31) / 32;
+                const double delta = __ddiv_rn(1.0, (double)steps);
+                unsigned long long lc = 0;
+                for (int r = 0; ok && r < R; ++r) {
+                    const int k = 1 + lane * R + r;
+                    bool v = true;
+                    if (k <= Mi) {
+                        ++lc;
+                        const float tt = (float)k / (float)steps;
+                        const int res = grid_valid32(J.scene, fmaf(dir32[0], tt, a32[0]), fmaf(dir32[1], tt, a32[1]), eps);
+                        if (res == VF_UNSURE) {
+                            double qs[2];
+                            interp64(MPTG_METRIC_L2, 2, A, B, __dmul_rn((double)k, delta), qs);
+                            v = grid_valid64(J.scene, qs);
+                        } else {
+                            v = res == VF_VALID;
+                        }
+                    }
+                    if (__any_sync(0xffffffffu, !v)) ok = false;
+                }
+                for (int o = 16; o > 0; o >>= 1) lc += __shfl_xor_sync(0xffffffffu, lc, o);
+                cnt += lc;
+            }
+            if (lane == 0) {
+                if (ok) S.fl[e] |= 1;
+                if (J.nsamp) atomicAdd(&s_cnt, cnt);
+            }
+        }
+        __syncthreads();
+        // accepted samples in sample order (k_plan_scan / k_plan_scatter)
+        const int f = (t < W && S.fl[t] == 1) ? 1 : 0;
+        const unsigned m = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) s_wsum[warp] = __popc(m);
+        __syncthreads();
+        if (warp == 0) {
+            const int v = lane < nwarps ? s_wsum[lane] : 0;
+            int x = v;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            s_wsum[lane] = x - v;
+            if (lane == 31) s_total = x;
+        }
+        __syncthreads();
+        const int nacc = s_total;
+        const size_t room = J.max_nodes - (size_t)n;
+        const int keep = (size_t)nacc > room ? (int)room : nacc;  // node budget: the first accepted samples
+        if (f) {
+            const int pos = s_wsum[warp] + __popc(m & ((1u << lane) - 1u));
+            if (pos < keep) {
+                const int id = n + pos;
+                const double* nw = S.nw + 2 * t;
+                J.states[2 * id] = nw[0];
+                J.states[2 * id + 1] = nw[1];
+                S.pts[id] = make_float2(__double2float_rn(nw[0]), __double2float_rn(nw[1]));
+                J.parent[id] = S.ni[t];
+                // GoalState::operator() (src/mpt/goal_state.hpp:64-69): d <= radius
+                const uint8_t g = (J.has_goal && dist64(MPTG_METRIC_L2, 2, 1.0, 1.0, nw, J.goal) <= J.goal_radius)
+                                      ? 1 : 0;
+                J.goalf[id] = g;
+                if (g) atomicAdd(&s_goals, 1);
+                atomicMax(&s_maxabs, __float_as_int(maxabs_ru(nw[0], nw[1])));
+            }
+        }
+        __syncthreads();
+        if (t == 0) s_n = n + keep;
+        samples += (unsigned long long)W;
+        accepted += (unsigned long long)keep;
+        ++waves_run;
+        ++wave;
+        __syncthreads();
+    }
+    if (t == 0) {
+        J.ctr->n = s_n;
+        J.ctr->wave = wave;
+        J.ctr->goals = s_goals;
+        J.ctr->maxabs_bits = s_maxabs;
+        J.ctr->status = status;
+        J.ctr->waves_run = waves_run;
+        J.ctr->samples = samples;
+        J.ctr->accepted = accepted;
+        if (J.nsamp) atomicAdd(J.nsamp, s_cnt);
+    }
+}
+
+}  // namespace
+
+bool bplan_supported(const mptg_scene* sc, int wavefront, int resolution) {
+    return sc->kind == MPTG_SCENE_GRID && resolution == 0 && wavefront >= 1 && wavefront <= BPLAN_THREADS;
+}
+
+mptg_status bplan_launch(mptg_ctx* ctx, const BPlanJob* djobs, int njobs, int max_W, int max_cap, cudaStream_t s) {
+    if (njobs <= 0) return MPTG_OK;
+    if (max_W < 1 || max_W > BPLAN_THREADS || max_cap < 1 || max_cap > BPLAN_MAX_NODES)
+        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "block planner: wavefront %d / capacity %d out of range", max_W,
+                         max_cap);
+    const size_t bytes = smem_bytes(max_cap, max_W, BPLAN_THREADS);
+    static int configured = -1;
+    if (configured != ctx->device) {
+        MPTG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_bplan_grid, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)smem_bytes(BPLAN_MAX_NODES, BPLAN_THREADS, BPLAN_THREADS)));
+        configured = ctx->device;
+    }
+    k_bplan_grid<<<njobs, BPLAN_THREADS, bytes, s>>>(djobs, max_cap, max_W);
+    MPTG_LAUNCHED(ctx);
+    MPTG_CUDA_TRY(ctx, cudaGetLastError());
+    return MPTG_OK;
+}

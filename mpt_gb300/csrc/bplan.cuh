@@ -1,0 +1,48 @@
+// bplan.cuh - interface of the persistent block planner (bplan.cu).
+#pragma once
+#include "scene.cuh"
+
+// Counters a persistent run reads at its start and leaves at its end.
+struct BPlanCounters {
+    int n;                          // nodes in the tree
+    uint32_t wave;                  // wavefront index of the next wavefront (the sample stream's w)
+    int goals;                      // goal nodes found so far (this run and earlier ones)
+    int maxabs_bits;                // largest |coordinate| of a stored state, FP32 bits (error bound)
+    int status;                     // BPLAN_* below
+    int waves_run;                  // wavefronts this run completed
+    unsigned long long samples;     // samples drawn by this run
+    unsigned long long accepted;    // nodes added by this run
+};
+
+enum { BPLAN_DONE = 0, BPLAN_FULL = 1 };  // FULL: the next wavefront could overflow the block's node capacity
+
+// One query of the persistent planner: the wavefront PRRT of planner.cu, with
+// every step inside one thread block (the grid scene).
+struct BPlanJob {
+    SceneView scene;
+    const double* lo;
+    const double* hi;
+    const double* goal;
+    int has_goal;
+    double goal_bias, range, goal_radius, inv_step;
+    uint64_t seed;
+    double* states;                 // [cap][2] node states (the first n given)
+    int* parent;                    // [cap] parent ids (the planner's array)
+    uint8_t* goalf;                 // [cap] goal flag per node
+    BPlanCounters* ctr;
+    unsigned long long* nsamp;      // link states checked (may be null)
+    size_t max_nodes;               // the planner's node budget
+    int cap;                        // node capacity of this block (<= BPLAN_MAX_NODES)
+    int W;                          // wavefront size (<= BPLAN_THREADS)
+    int max_waves;                  // wavefronts to run (<= 0: no limit)
+    int stop_when_solved;
+    uint64_t deadline_ns;           // globaltimer deadline (0: none)
+};
+
+#define BPLAN_THREADS 1024
+#define BPLAN_MAX_NODES 16384       // FP32 node copy in shared memory: 128 KB
+
+// Runs njobs jobs (device array), one thread block each, on stream s.
+mptg_status bplan_launch(mptg_ctx* ctx, const BPlanJob* djobs, int njobs, int max_W, int max_cap, cudaStream_t s);
+// true when the scene and parameters are ones the block planner runs
+bool bplan_supported(const mptg_scene* sc, int wavefront, int resolution);

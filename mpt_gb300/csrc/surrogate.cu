@@ -10,21 +10,31 @@
 // activations, FP32 accumulation; FP32 master weights, Adam, BCE-with-logits.
 //   layer 0 (in -> 256) and the output layer (256 -> 1): CUDA cores
 //   layers 1-3 (256 -> 256), forward, input-gradient and weight-gradient
-//   products: BF16 tensor-core GEMM (mma.sync m16n8k16, FP32 accumulate),
-//   tiles 128 x 128 x 32, fused epilogues (bias + SiLU; SiLU'; split-K sums)
-// The network is tiny next to the collision checks it screens (0.4 MFLOP per
-// state forward), so the GEMM is sized for correctness and simplicity.
+//   products: k_sg_umma, a tcgen05 GEMM -- operand tiles moved by TMA
+//   (128-byte swizzle) through a 4-stage mbarrier ring, one thread issuing
+//   128 x 256 x 16 UMMAs into a TMEM accumulator, the epilogue reading TMEM
+//   with tcgen05.ld and fusing bias + SiLU (forward), SiLU' (backward), the
+//   split-K sums (weight gradients), or, when scoring, the output layer
+// The scoring path stores no FP32 pre-activations and no transposes: only the
+// BF16 activations the next layer reads, and the logits.
 #include <cuda_bf16.h>
 
 #include "metrics.cuh"
 #include "philox.cuh"
+#include "umma.cuh"
+
+#include <mutex>
 
 #define SG_W 256
 #define SG_MAXIN 16
-#define SG_TM 128
-#define SG_TN 128
-#define SG_TK 32
-#define SG_PAD 8
+#define SG_TM 128                                 // rows per CTA (UMMA M)
+#define SG_BK 64                                  // K per pipeline stage: one 128-byte swizzle row
+#define SG_STAGES 4
+#define SG_A_BYTES (SG_TM * SG_BK * 2)            // 16 KB
+#define SG_B_BYTES (SG_W * SG_BK * 2)             // 32 KB: all 256 outputs (UMMA N = 256)
+#define SG_STAGE_BYTES (SG_A_BYTES + SG_B_BYTES)
+#define SG_SMEM (SG_STAGES * SG_STAGE_BYTES + 1024 + 256)
+#define SG_TIMEOUT_NS 2000000000ull               // a GEMM takes microseconds; 2 s means something is wrong
 
 typedef __nv_bfloat16 bf16;
 
@@ -56,6 +66,7 @@ struct mptg_surrogate {
     double* dstates = nullptr;    // staging for host inputs [cap][in]
     uint8_t* dlabels = nullptr;
     float* dlogits = nullptr;
+    int* err = nullptr;           // device error word: a tcgen05 GEMM wait ran out (1 load, 2 MMA, 3 epilogue)
     // held by a planner from scoring until its stream has consumed the logits,
     // since the activation buffers above are shared
     std::mutex mu;
@@ -87,12 +98,14 @@ __device__ __forceinline__ float sg_dsilu(float z) {
 }
 
 // ------------------------------------------------------------------ tensor-core GEMM
-// C[m][n] = sum_k A[m][k] * B[n][k]  (A: [M][lda], B: [N][ldb], K contiguous)
-// blockIdx.z splits K into ranges of kspan.  8 warps: 4 (M) x 2 (N), 32 x 64 each.
-enum { EPI_FWD = 0, EPI_BWD = 1, EPI_GRAD = 2 };
+// C[m][n] = sum_k A[m][k] * B[n][k] for the 128 rows m of tile blockIdx.y and
+// all 256 n, over the K range of split blockIdx.z (kblocks * 64 elements).
+// A and B are K-major BF16 ([rows][ld]) read through TMA tensor maps.
+enum { EPI_FWD = 0, EPI_BWD = 1, EPI_GRAD = 2, EPI_SCORE = 3, EPI_SCORE_OUT = 4 };
 
 struct EpiArgs {
     // forward: z = acc + bias; Z[m][n] = z; H[m][n] = silu(z) (bf16), HT[n][m]
+    // scoring: H only; scoring output: zout[m] = sum_n silu(z) w4[n] + b4
     const float* bias;
     float* Z;
     bf16* H;
@@ -102,98 +115,179 @@ struct EpiArgs {
     const float* Zin;
     bf16* dZ;
     bf16* dZT;
-    // gradient: G[m][n] += acc * gscale
+    // gradient: G[m][n] += acc
     float* G;
     int ldc;
+    const float* w4;
+    const float* b4;
+    float* zout;
 };
 
-__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, const uint32_t* b) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
 }
 
+// Warp roles: warp 0 lane 0 issues the TMA loads, warp 1 lane 0 the UMMAs;
+// then all four warps run the epilogue, warp w on TMEM lanes (= tile rows)
+// 32w .. 32w + 31.  Every wait is bounded (SG_TIMEOUT_NS); a wait that runs
+// out sets *err, drains the loads already issued, frees TMEM and returns.
 template <int EPI>
-__global__ void __launch_bounds__(256) k_sg_gemm(const bf16* __restrict__ A, int lda, const bf16* __restrict__ B,
-                                                 int ldb, int kspan, EpiArgs ep) {
-    __shared__ __align__(16) bf16 As[SG_TM][SG_TK + SG_PAD];
-    __shared__ __align__(16) bf16 Bs[SG_TN][SG_TK + SG_PAD];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int wm = warp >> 1, wn = warp & 1;
-    const int g = lane >> 2, tg = lane & 3;
-    const int m0 = blockIdx.y * SG_TM, n0 = blockIdx.x * SG_TN;
-    const int k0 = blockIdx.z * kspan;
-    float acc[2][8][4];
-#pragma unroll
-    for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-#pragma unroll
-            for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
-
-    for (int kt = k0; kt < k0 + kspan; kt += SG_TK) {
-        // 128 rows x 32 bf16 = 512 x 16-byte vectors per operand: 2 per thread
-#pragma unroll
-        for (int v = 0; v < 2; ++v) {
-            int idx = tid + v * 256;
-            int r = idx >> 2, c = (idx & 3) * 8;
-            *reinterpret_cast<uint4*>(&As[r][c]) =
-                *reinterpret_cast<const uint4*>(&A[(size_t)(m0 + r) * lda + kt + c]);
-            *reinterpret_cast<uint4*>(&Bs[r][c]) =
-                *reinterpret_cast<const uint4*>(&B[(size_t)(n0 + r) * ldb + kt + c]);
+__global__ void __launch_bounds__(128, 1) k_sg_umma(const __grid_constant__ CUtensorMap ta,
+                                                    const __grid_constant__ CUtensorMap tb, int kblocks, EpiArgs ep,
+                                                    int* __restrict__ err) {
+    extern __shared__ uint8_t sg_smem_raw[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t raw = umma::smem_u32(sg_smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;  // the 128-byte swizzle needs 1024-byte aligned tiles
+    uint8_t* smem = sg_smem_raw + (base - raw);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + SG_STAGES * SG_STAGE_BYTES);
+    uint64_t* empty = full + SG_STAGES;
+    uint64_t* accf = empty + SG_STAGES;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(accf + 1);
+    int* counts = reinterpret_cast<int*>(tslot + 1);  // [0] stages loaded, [1] stages consumed
+    const int m0 = blockIdx.y * SG_TM;
+    const int k0 = blockIdx.z * kblocks * SG_BK;
+    if (tid == 0) {
+        for (int s = 0; s < SG_STAGES; ++s) {
+            umma::mbar_init(&full[s], 1);
+            umma::mbar_init(&empty[s], 1);
         }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < SG_TK; kk += 16) {
-            uint32_t af[2][4], bfr[8][2];
-#pragma unroll
-            for (int i = 0; i < 2; ++i) {
-                int r = wm * 32 + i * 16 + g;
-                af[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][kk + tg * 2]);
-                af[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + tg * 2]);
-                af[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][kk + tg * 2 + 8]);
-                af[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + tg * 2 + 8]);
-            }
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                int n = wn * 64 + j * 8 + g;
-                bfr[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[n][kk + tg * 2]);
-                bfr[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[n][kk + tg * 2 + 8]);
-            }
-#pragma unroll
-            for (int i = 0; i < 2; ++i)
-#pragma unroll
-                for (int j = 0; j < 8; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
-        }
-        __syncthreads();
+        umma::mbar_init(accf, 1);
+        counts[0] = counts[1] = 0;
+        umma::fence_mbar_init();
     }
-    // epilogue: acc[i][j] holds rows (g, g+8) x cols (2tg, 2tg+1) of a 16 x 8 tile
+    if (warp == 0) {
+        umma::tmem_alloc(tslot, SG_W);  // 256 FP32 columns x 128 lanes: the 128 x 256 accumulator
+        umma::tmem_relinquish();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint64_t deadline = umma::globaltimer_ns() + SG_TIMEOUT_NS;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int kb = 0;
+            for (; kb < kblocks; ++kb) {
+                const int s = kb % SG_STAGES;
+                if (kb >= SG_STAGES && !umma::mbar_wait(&empty[s], ((kb / SG_STAGES) - 1) & 1, deadline)) {
+                    atomicExch(err, 1);
+                    break;
+                }
+                uint8_t* sa = smem + s * SG_STAGE_BYTES;
+                umma::mbar_arrive_expect_tx(&full[s], SG_STAGE_BYTES);
+                umma::tma_load_2d(sa, &ta, &full[s], k0 + kb * SG_BK, m0);
+                umma::tma_load_2d(sa + SG_A_BYTES, &tb, &full[s], k0 + kb * SG_BK, 0);
+            }
+            counts[0] = kb;
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = umma::idesc_bf16_f32(SG_TM, SG_W);
+            int kb = 0;
+            for (; kb < kblocks; ++kb) {
+                const int s = kb % SG_STAGES;
+                if (!umma::mbar_wait(&full[s], (kb / SG_STAGES) & 1, deadline)) {
+                    atomicExch(err, 2);
+                    break;
+                }
+                umma::fence_after_sync();
+                const uint32_t sa = base + s * SG_STAGE_BYTES, sb = sa + SG_A_BYTES;
 #pragma unroll
-    for (int i = 0; i < 2; ++i)
+                for (int k = 0; k < SG_BK / 16; ++k)
+                    umma::mma_bf16(tmem, umma::sdesc_k128(sa + 32 * k), umma::sdesc_k128(sb + 32 * k), idesc,
+                                   (kb | k) != 0);
+                umma::mma_commit(&empty[s]);  // the stage is free once these UMMAs have read it
+            }
+            counts[1] = kb;
+            umma::mma_commit(accf);  // the accumulator is ready once every UMMA has completed
+        }
+        __syncwarp();
+    }
+    const bool ok = umma::mbar_wait(accf, 0, deadline + SG_TIMEOUT_NS);
+    umma::fence_after_sync();
+    if (!ok) {
+        if (tid == 0) atomicExch(err, 3);
+    } else {
+        const int row = warp * 32 + lane;
+        const size_t m = (size_t)(m0 + row);
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+        float out = 0.f;
+#pragma unroll 1
+        for (int c = 0; c < SG_W; c += 16) {
+            float v[16];
+            umma::tmem_ld16(trow + c, v);
+            if (EPI == EPI_GRAD) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
+                for (int j = 0; j < 16; ++j) atomicAdd(&ep.G[m * ep.ldc + c + j], v[j]);
+            } else if (EPI == EPI_BWD) {
+                const float4* zi = reinterpret_cast<const float4*>(ep.Zin + m * SG_W + c);
+                float zin[16];
 #pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                int m = m0 + wm * 32 + i * 16 + g + (r >= 2 ? 8 : 0);
-                int n = n0 + wn * 64 + j * 8 + tg * 2 + (r & 1);
-                float v = acc[i][j][r];
+                for (int j = 0; j < 4; ++j) {
+                    float4 t = zi[j];
+                    zin[4 * j] = t.x; zin[4 * j + 1] = t.y; zin[4 * j + 2] = t.z; zin[4 * j + 3] = t.w;
+                }
+                uint32_t pk[8];
+#pragma unroll
+                for (int j = 0; j < 16; j += 2) {
+                    float a = v[j] * sg_dsilu(zin[j]), b = v[j + 1] * sg_dsilu(zin[j + 1]);
+                    pk[j / 2] = pack_bf16x2(a, b);
+                    __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162*>(&pk[j / 2]);
+                    ep.dZT[(size_t)(c + j) * ep.ldt + m] = h.x;
+                    ep.dZT[(size_t)(c + j + 1) * ep.ldt + m] = h.y;
+                }
+                uint4* o = reinterpret_cast<uint4*>(ep.dZ + m * SG_W + c);
+                o[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                o[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+            } else {
+                float z[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) z[j] = v[j] + __ldg(&ep.bias[c + j]);
                 if (EPI == EPI_FWD) {
-                    float z = v + ep.bias[n];
-                    ep.Z[(size_t)m * SG_W + n] = z;
-                    bf16 h = __float2bfloat16_rn(sg_silu(z));
-                    ep.H[(size_t)m * SG_W + n] = h;
-                    ep.HT[(size_t)n * ep.ldt + m] = h;
-                } else if (EPI == EPI_BWD) {
-                    float dz = v * sg_dsilu(ep.Zin[(size_t)m * SG_W + n]);
-                    bf16 h = __float2bfloat16_rn(dz);
-                    ep.dZ[(size_t)m * SG_W + n] = h;
-                    ep.dZT[(size_t)n * ep.ldt + m] = h;
+                    float4* zo = reinterpret_cast<float4*>(ep.Z + m * SG_W + c);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) zo[j] = make_float4(z[4 * j], z[4 * j + 1], z[4 * j + 2], z[4 * j + 3]);
+                }
+                if (EPI == EPI_SCORE_OUT) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        out = fmaf(__bfloat162float(__float2bfloat16_rn(sg_silu(z[j]))),
+                                   __bfloat162float(__float2bfloat16_rn(__ldg(&ep.w4[c + j]))), out);
                 } else {
-                    atomicAdd(&ep.G[(size_t)m * ep.ldc + n], v);
+                    uint32_t pk[8];
+#pragma unroll
+                    for (int j = 0; j < 16; j += 2) pk[j / 2] = pack_bf16x2(sg_silu(z[j]), sg_silu(z[j + 1]));
+                    uint4* o = reinterpret_cast<uint4*>(ep.H + m * SG_W + c);
+                    o[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                    o[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                    if (EPI == EPI_FWD) {
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162*>(&pk[j]);
+                            ep.HT[(size_t)(c + 2 * j) * ep.ldt + m] = h.x;
+                            ep.HT[(size_t)(c + 2 * j + 1) * ep.ldt + m] = h.y;
+                        }
+                    }
                 }
             }
+        }
+        if (EPI == EPI_SCORE_OUT) ep.zout[m] = out + __ldg(ep.b4);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    // loads issued but never consumed (a wait ran out) must land before the
+    // shared memory they write is released
+    if (tid == 0 && counts[1] < counts[0]) {
+        const uint64_t drain = umma::globaltimer_ns() + SG_TIMEOUT_NS;
+        for (int kb = counts[1]; kb < counts[0]; ++kb)
+            umma::mbar_wait(&full[kb % SG_STAGES], (kb / SG_STAGES) & 1, drain);
+    }
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, SG_W);
 }
 
 // ------------------------------------------------------------------ CUDA-core parts
@@ -220,10 +314,10 @@ __global__ void k_sg_layer0(const bf16* __restrict__ X, int in, const float* __r
     float z = b0[n];
     for (int k = 0; k < in; ++k)
         z = fmaf(__bfloat162float(X[(size_t)m * SG_MAXIN + k]), __bfloat162float(__float2bfloat16_rn(W0[n * in + k])), z);
-    Z[idx] = z;
+    if (Z) Z[idx] = z;  // training keeps the pre-activation and the transpose; scoring does not
     bf16 h = __float2bfloat16_rn(sg_silu(z));
     H[idx] = h;
-    HT[(size_t)n * M + m] = h;
+    if (HT) HT[(size_t)n * M + m] = h;
 }
 
 // output layer: zout[m] = H3[m] . w4 + b4 (warp per sample)
@@ -381,24 +475,113 @@ static mptg_status sg_reserve(mptg_surrogate* s, size_t cap) {
     return MPTG_OK;
 }
 
-// forward over M (multiple of 128) rows already in s->X
-static void sg_forward(mptg_surrogate* s, int M, cudaStream_t st) {
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against libcuda)
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// TMA map of a K-major BF16 matrix [rows][ld] whose first `cols` elements per
+// row are the K extent: 64 x box_rows boxes with the 128-byte swizzle
+static bool bf16_map(CUtensorMap* m, const bf16* base, uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows) {
+    EncodeTiledFn f = encode_tiled();
+    if (!f) return false;
+    cuuint64_t dims[2] = {cols, rows};
+    cuuint64_t strides[1] = {ld * sizeof(bf16)};
+    cuuint32_t box[2] = {SG_BK, box_rows};
+    cuuint32_t es[2] = {1, 1};
+    return f(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(base), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// C = A B^T for A [rowsA][lda] (rowsA a multiple of 128) and B [256][ldb],
+// both over K (a multiple of 64) elements; K split into CTAs of kblocks * 64
+template <int EPI>
+static mptg_status sg_gemm(mptg_surrogate* s, const bf16* A, int rowsA, int lda, const bf16* B, int ldb, int K,
+                           int kblocks, const EpiArgs& ep, cudaStream_t st) {
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        cudaFuncSetAttribute(k_sg_umma<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, SG_SMEM);
+    });
+    CUtensorMap ta, tb;
+    if (!bf16_map(&ta, A, (uint64_t)rowsA, (uint64_t)K, (uint64_t)lda, SG_TM) ||
+        !bf16_map(&tb, B, SG_W, (uint64_t)K, (uint64_t)ldb, SG_W))
+        return mptg_fail(s->ctx, MPTG_ERR_CUDA, "surrogate GEMM: cuTensorMapEncodeTiled failed");
+    dim3 grid(1, rowsA / SG_TM, (K / SG_BK) / kblocks);
+    k_sg_umma<EPI><<<grid, 128, SG_SMEM, st>>>(ta, tb, kblocks, ep, s->err);
+    MPTG_LAUNCHED(s->ctx);
+    MPTG_CUDA_TRY(s->ctx, cudaGetLastError());
+    return MPTG_OK;
+}
+
+// reads and clears the device error word (synchronises the stream)
+static mptg_status sg_check(mptg_surrogate* s, cudaStream_t st) {
+    int e = 0;
+    MPTG_CUDA_TRY(s->ctx, cudaMemcpyAsync(&e, s->err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MPTG_CUDA_TRY(s->ctx, cudaStreamSynchronize(st));
+    if (e) {
+        MPTG_CUDA_TRY(s->ctx, cudaMemsetAsync(s->err, 0, sizeof(int), st));
+        return mptg_fail(s->ctx, MPTG_ERR_TIMEOUT, "surrogate tensor-core GEMM: a pipeline wait ran out (%s)",
+                         e == 1 ? "operand load" : e == 2 ? "UMMA issue" : "accumulator");
+    }
+    return MPTG_OK;
+}
+
+// forward over M (multiple of 128) rows already in s->X.  Training keeps every
+// layer's pre-activations, activations and transposes for the backward pass;
+// scoring (train = false) writes only the BF16 activations and the logits.
+static mptg_status sg_forward(mptg_surrogate* s, int M, bool train, cudaStream_t st) {
     SgLayout L = sg_layout(s->in);
     const size_t MW = (size_t)M * SG_W;
-    k_sg_layer0<<<mptg_blocks(MW, 256), 256, 0, st>>>(s->X, s->in, s->P + L.W0, s->P + L.b0, M, s->Z, s->H, s->HT);
+    k_sg_layer0<<<mptg_blocks(MW, 256), 256, 0, st>>>(s->X, s->in, s->P + L.W0, s->P + L.b0, M,
+                                                      train ? s->Z : nullptr, s->H, train ? s->HT : nullptr);
+    MPTG_LAUNCHED(s->ctx);
+    mptg_status r;
     for (int l = 1; l <= 3; ++l) {
         EpiArgs ep{};
         ep.bias = s->P + L.b[l];
-        ep.Z = s->Z + l * MW;
-        ep.H = s->H + l * MW;
-        ep.HT = s->HT + l * MW;
         ep.ldt = M;
-        dim3 grid(SG_W / SG_TN, M / SG_TM, 1);
-        k_sg_gemm<EPI_FWD><<<grid, 256, 0, st>>>(s->H + (l - 1) * MW, SG_W, s->Wb + (size_t)(l - 1) * SG_W * SG_W,
-                                                 SG_W, SG_W, ep);
+        const bf16* A = s->H + (l - 1) * MW;
+        const bf16* B = s->Wb + (size_t)(l - 1) * SG_W * SG_W;
+        if (train) {
+            ep.Z = s->Z + l * MW;
+            ep.H = s->H + l * MW;
+            ep.HT = s->HT + l * MW;
+            r = sg_gemm<EPI_FWD>(s, A, M, SG_W, B, SG_W, SG_W, SG_W / SG_BK, ep, st);
+        } else if (l < 3) {
+            ep.H = s->H + l * MW;
+            r = sg_gemm<EPI_SCORE>(s, A, M, SG_W, B, SG_W, SG_W, SG_W / SG_BK, ep, st);
+        } else {
+            ep.w4 = s->P + L.w4;
+            ep.b4 = s->P + L.b4;
+            ep.zout = s->zout;
+            r = sg_gemm<EPI_SCORE_OUT>(s, A, M, SG_W, B, SG_W, SG_W, SG_W / SG_BK, ep, st);
+        }
+        if (r) return r;
     }
-    k_sg_out<<<mptg_blocks((size_t)M * 32, 256), 256, 0, st>>>(s->H + 3 * MW, s->P + L.w4, s->P + L.b4, M, s->zout);
-    s->ctx->launches += 5;
+    if (train) {
+        k_sg_out<<<mptg_blocks((size_t)M * 32, 256), 256, 0, st>>>(s->H + 3 * MW, s->P + L.w4, s->P + L.b4, M,
+                                                                   s->zout);
+        MPTG_LAUNCHED(s->ctx);
+    }
+    return MPTG_OK;
 }
 
 extern "C" {
@@ -425,6 +608,8 @@ mptg_status mptg_surrogate_create(mptg_ctx* ctx, int in_dim, const double* scale
     if (e == cudaSuccess) e = cudaMalloc((void**)&s->Wb, 3 * SG_W * SG_W * sizeof(bf16));
     if (e == cudaSuccess) e = cudaMalloc((void**)&s->WTb, 3 * SG_W * SG_W * sizeof(bf16));
     if (e == cudaSuccess) e = cudaMalloc((void**)&s->loss, sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&s->err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(s->err, 0, sizeof(int));
     if (e != cudaSuccess) {
         cudaGetLastError();
         delete s;
@@ -449,7 +634,7 @@ mptg_status mptg_surrogate_destroy(mptg_surrogate* s) {
     if (!s) return MPTG_ERR_INVALID_ARG;
     cudaDeviceSynchronize();
     void* ptrs[] = {s->P, s->G, s->Mo, s->Vo, s->Wb, s->WTb, s->X, s->Z, s->H, s->HT, s->dZ, s->dZT, s->dH,
-                    s->zout, s->dzout, s->dstates, s->dlabels, s->dlogits, s->loss};
+                    s->zout, s->dzout, s->dstates, s->dlabels, s->dlogits, s->loss, s->err};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete s;
@@ -491,7 +676,7 @@ mptg_status mptg_surrogate_score_dev(mptg_surrogate* s, const double* dstates, i
                                           st));
     k_sg_inputs<<<mptg_blocks(M, 256), 256, 0, st>>>(dstates, n, s->in, s->dstates, s->dstates + SG_MAXIN, M, s->X);
     MPTG_LAUNCHED(s->ctx);
-    sg_forward(s, M, st);
+    if ((r = sg_forward(s, M, false, st))) return r;
     MPTG_CUDA_TRY(s->ctx, cudaMemcpyAsync(dlogits, s->zout, n * sizeof(float), cudaMemcpyDeviceToDevice, st));
     return MPTG_OK;
 }
@@ -507,7 +692,10 @@ mptg_status mptg_surrogate_score(mptg_surrogate* s, const double* states, size_t
     if ((r = mptg_stage_out_alloc(s->ctx, logits, n * sizeof(float), st, &bo))) return r;
     if ((r = mptg_surrogate_score_dev(s, (const double*)bq.dptr, (int)n, (float*)bo.dptr, st))) return r;
     MPTG_CUDA_TRY(s->ctx, cudaGetLastError());
-    return mptg_stage_finish(s->ctx, st, &bo, 1, &bq, 1);
+    if ((r = mptg_stage_finish(s->ctx, st, &bo, 1, &bq, 1))) return r;
+    // host buffers: the call has synchronised anyway, so report a GEMM wait that ran out
+    if (!mptg_is_device_ptr(logits)) return sg_check(s, st);
+    return MPTG_OK;
 }
 
 // One Adam step on a batch: loss and gradients of BCE-with-logits, labels 1 =
@@ -542,7 +730,7 @@ mptg_status mptg_surrogate_train_step(mptg_surrogate* s, const double* states, c
     MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(s->dstates + SG_MAXIN, s->shift, sizeof(s->shift), cudaMemcpyHostToDevice, st));
     k_sg_inputs<<<mptg_blocks(M, 256), 256, 0, st>>>(dq, M, s->in, s->dstates, s->dstates + SG_MAXIN, M, s->X);
     MPTG_LAUNCHED(ctx);
-    sg_forward(s, M, st);
+    if ((r = sg_forward(s, M, true, st))) return r;
     // loss and output-layer gradients
     MPTG_CUDA_TRY(ctx, cudaMemsetAsync(s->G, 0, s->nparam * sizeof(float), st));
     MPTG_CUDA_TRY(ctx, cudaMemsetAsync(s->loss, 0, sizeof(float), st));
@@ -553,26 +741,26 @@ mptg_status mptg_surrogate_train_step(mptg_surrogate* s, const double* states, c
     // hidden layers 3, 2, 1: weight and bias gradients, then back through W
     for (int l = 3; l >= 1; --l) {
         k_sg_colsum<<<SG_W, 256, 0, st>>>(s->dZT, M, s->G + L.b[l]);
+        MPTG_LAUNCHED(ctx);
         EpiArgs eg{};
         eg.G = s->G + L.W[l];
         eg.ldc = SG_W;
-        int splits = M / 128;  // K (= batch) split into spans of 128
-        dim3 gg(SG_W / SG_TN, SG_W / SG_TM, splits);
-        // dW[out][in] = sum_m dZ[m][out] H_{l-1}[m][in]: A = dZ^T [out][M], B = H^T [in][M]
-        k_sg_gemm<EPI_GRAD><<<gg, 256, 0, st>>>(s->dZT, M, s->HT + (size_t)(l - 1) * MW, M, 128, eg);
+        // dW[out][in] = sum_m dZ[m][out] H_{l-1}[m][in]: A = dZ^T [out][M], B = H^T [in][M];
+        // K (= the batch) split over CTAs of 4 (or 2) stages, summed by the epilogue's atomics
+        const int kb = (M / SG_BK) % 4 == 0 ? 4 : 2;
+        if ((r = sg_gemm<EPI_GRAD>(s, s->dZT, SG_W, M, s->HT + (size_t)(l - 1) * MW, M, M, kb, eg, st))) return r;
         // dH_{l-1} = dZ_l W_l, then * silu'(Z_{l-1})
         EpiArgs eb{};
         eb.Zin = s->Z + (size_t)(l - 1) * MW;
         eb.dZ = s->dZ;
         eb.dZT = s->dZT;
         eb.ldt = M;
-        dim3 gb(SG_W / SG_TN, M / SG_TM, 1);
         // the GEMM reads dZ/dZT of layer l while writing layer l-1's into the same
         // buffers: stage through dH
         MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(s->dH, s->dZ, MW * sizeof(bf16), cudaMemcpyDeviceToDevice, st));
-        k_sg_gemm<EPI_BWD><<<gb, 256, 0, st>>>((const bf16*)s->dH, SG_W, s->WTb + (size_t)(l - 1) * SG_W * SG_W,
-                                               SG_W, SG_W, eb);
-        ctx->launches += 3;
+        if ((r = sg_gemm<EPI_BWD>(s, (const bf16*)s->dH, M, SG_W, s->WTb + (size_t)(l - 1) * SG_W * SG_W, SG_W, SG_W,
+                                  SG_W / SG_BK, eb, st)))
+            return r;
     }
     // layer 0
     k_sg_colsum<<<SG_W, 256, 0, st>>>(s->dZT, M, s->G + L.b0);
@@ -590,6 +778,7 @@ mptg_status mptg_surrogate_train_step(mptg_surrogate* s, const double* states, c
     if (loss_out) {
         MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(loss_out, s->loss, sizeof(float), cudaMemcpyDeviceToHost, st));
         MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+        if ((r = sg_check(s, st))) return r;
     }
     MPTG_CUDA_TRY(ctx, cudaGetLastError());
     return MPTG_OK;

@@ -497,6 +497,9 @@ __device__ __forceinline__ float cell_lb(const TreeView& t, int c, float myq, in
 __device__ __forceinline__ void rerank_step(const TreeView& t, const double* __restrict__ qd, int lane, bool have,
                                             int pid, float d32, float E, double& best, int& bidx, float& bestf_up,
                                             unsigned long long& nrerank) {
+    // most buckets hold no point that can reach the current best: leave
+    // before the bucket-minimum reduction (the candidate set is unchanged)
+    if (!__any_sync(0xffffffffu, have && __fsub_rd(d32, E) <= bestf_up)) return;
     float m = d32;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));

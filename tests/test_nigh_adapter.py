@@ -15,7 +15,9 @@ if not ref.available():
     pytest.skip("reference sources not present", allow_module_level=True)
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-FLAGS = ["g++", "-std=c++17", "-O2", "-Wall", "-fopenmp", "-DNDEBUG", "-DMPT_LOG_LEVEL=WARN", "-Wno-attributes",
+# -ffp-contract=off: the brute-force distances the program checks against must
+# round like the library's (g++ contracts a*b+c into FMA on Arm by default)
+FLAGS = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-Wall", "-fopenmp", "-DNDEBUG", "-DMPT_LOG_LEVEL=WARN", "-Wno-attributes",
          "-Wno-unused-variable", "-I", os.path.join(ROOT, "include"),
          "-I", os.path.join(ROOT, "oracle", "ref", "shim"), "-I", ref.REFERENCE_SRC,
          os.path.join(ROOT, "tests", "cpp", "nigh_adapter.cpp")]
