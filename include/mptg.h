@@ -234,6 +234,15 @@ mptg_status mptg_planner_solution(mptg_planner* planner, double* path, size_t ca
 /* PRRT::visitGraph (prrt.hpp:300-316): all states and parent ids (-1 for starts). */
 mptg_status mptg_planner_graph(mptg_planner* planner, double* states, int32_t* parents, size_t cap,
                                size_t* n);
+/* Where the wavefronts run (no reference counterpart: an execution choice).
+ * mode 1 (the default): on grid scenes with wavefronts of up to 1,024 samples
+ * (PRRT, no surrogate), mptg_planner_run runs its wavefronts inside one
+ * persistent thread block -- nearest neighbours, steering, the motion check,
+ * the ordered insert and the stop conditions all on the device -- for up to
+ * 16,384 nodes, then updates the kd-tree; beyond that, and everywhere else,
+ * the multi-kernel wavefront runs.  mode 0: always the multi-kernel
+ * wavefront.  Both build the same tree, state for state. */
+mptg_status mptg_planner_set_persistent(mptg_planner* planner, int mode);
 /* The planner's nearest-neighbour container -- PRRT's nn_ member, the nigh
  * tree its workers query (src/mpt/impl/prrt/prrt.hpp:121-122,406-409) -- as a
  * borrowed tree handle: mptg_nearest / mptg_nearest_k / mptg_nearest_linear /

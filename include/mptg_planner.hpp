@@ -246,30 +246,22 @@ public:
         return g > 0;
     }
 
-    // prrt.hpp:194-201: doneFn is polled between wavefronts
+    // prrt.hpp:194-201: doneFn is polled between calls of up to kPollWavefronts
+    // wavefronts, each of which also ends at the first solution
+    static constexpr int kPollWavefronts = 16;
     template <class DoneFn>
     void solve(DoneFn done) {
-        if (size() == 0) throw std::runtime_error("there are no valid initial states");
-        create();
-        double st[8];
-        while (!done()) {
-            impl::check(ctx_, mptg_planner_stats(planner_, st));
-            double before = st[7];
-            int s = 0;
-            impl::check(ctx_, mptg_planner_run(planner_, 1, 0.0, 0, &s));
-            impl::check(ctx_, mptg_planner_stats(planner_, st));
-            if (st[7] == before) break;  // node budget reached
-        }
+        solve_until_(done, false, std::chrono::steady_clock::time_point{});
     }
     template <class Rep, class Period>
     void solveFor(const std::chrono::duration<Rep, Period>& d) {
         auto end = std::chrono::steady_clock::now() + d;
-        solve([&] { return std::chrono::steady_clock::now() >= end; });
+        solve_until_([&] { return std::chrono::steady_clock::now() >= end; }, true, end);
     }
     template <class DoneFn, class Rep, class Period>
     void solveFor(DoneFn done, const std::chrono::duration<Rep, Period>& d) {
         auto end = std::chrono::steady_clock::now() + d;
-        solve([&] { return std::chrono::steady_clock::now() >= end || done(); });
+        solve_until_([&] { return std::chrono::steady_clock::now() >= end || done(); }, true, end);
     }
     template <class Clock, class Duration>
     void solveUntil(const std::chrono::time_point<Clock, Duration>& t) {
@@ -278,6 +270,27 @@ public:
     template <class DoneFn, class Clock, class Duration>
     void solveUntil(DoneFn done, const std::chrono::time_point<Clock, Duration>& t) {
         solve([&] { return Clock::now() >= t || done(); });
+    }
+
+    // with a deadline, each call's time limit is what is left until `end`
+    template <class DoneFn>
+    void solve_until_(DoneFn done, bool has_deadline, std::chrono::steady_clock::time_point end) {
+        if (size() == 0) throw std::runtime_error("there are no valid initial states");
+        create();
+        double st[8];
+        while (!done()) {
+            double left = 0.0;
+            if (has_deadline) {
+                left = std::chrono::duration<double>(end - std::chrono::steady_clock::now()).count();
+                if (left <= 0) break;
+            }
+            impl::check(ctx_, mptg_planner_stats(planner_, st));
+            double before = st[7];
+            int s = 0;
+            impl::check(ctx_, mptg_planner_run(planner_, kPollWavefronts, left, solved() ? 0 : 1, &s));
+            impl::check(ctx_, mptg_planner_stats(planner_, st));
+            if (st[7] == before) break;  // node budget reached
+        }
     }
 
     // prrt.hpp:263-274

@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
             if (J.stop_when_solved && s_goals > 0) st = 1;
             else if ((size_t)s_n >= J.max_nodes) st = 1;
             else if (J.max_waves > 0 && waves_run >= J.max_waves) st = 1;
-            else if (s_n + W > cap) st = 2;
+            else if ((size_t)s_n + (size_t)W > (size_t)cap && (size_t)cap < J.max_nodes) st = 2;
             else if (J.deadline_ns && umma::globaltimer_ns() - t0 >= J.deadline_ns) st = 1;
             s_stop = st;
             s_gidx = INT_MAX;

@@ -17,6 +17,7 @@
 #include "scene.cuh"
 #include "tree.cuh"
 #include "sampler.cuh"
+#include "bplan.cuh"
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -126,6 +127,16 @@ struct mptg_planner {
     cudaEvent_t sev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     double t_star[4] = {0, 0, 0, 0};    // k-NN, choose parent, rewire, costs (seconds)
     bool star_timed = false;            // sev recorded in the current wavefront
+    // persistent block planner (bplan.cu): grid scenes, wavefronts <= 1024
+    int bp_mode = 1;                    // 0 off, 1 used wherever it applies
+    int bp_cap = 0;                     // node capacity of the buffers below
+    double* bp_states = nullptr;        // [bp_cap][2]
+    uint8_t* bp_goalf = nullptr;        // [bp_cap]
+    BPlanCounters* bp_ctr = nullptr;
+    BPlanJob* bp_job = nullptr;
+    BPlanCounters* bp_hctr = nullptr;   // pinned
+    uint8_t* bp_hgoal = nullptr;        // pinned [bp_cap]
+    uint64_t stat_bp_waves = 0;         // wavefronts run inside the block planner
 };
 
 extern "C" mptg_status mptg_surrogate_score_dev(mptg_surrogate* s, const double* dstates, int n, float* dlogits,
@@ -543,12 +554,14 @@ static void planner_free(mptg_planner* p) {
                     p->near_c, p->new_c, p->cmap, p->ok_c, p->keep, p->path_ids, p->path_out, p->sg_pts,
                     p->cost, p->elen, p->pj_s, p->pj_a, p->pj_a2, p->bbits, p->bid, p->knn_i, p->knn_d, p->pv,
                     p->s_pair, p->s_rcost, p->s_ok, p->s_ea, p->s_eb, p->dnear, p->cpar, p->ccost, p->celen,
-                    p->s_cnt, p->nrw, p->rank, p->decided};
+                    p->s_cnt, p->nrw, p->rank, p->decided, p->bp_states, p->bp_goalf, p->bp_ctr, p->bp_job};
     if (p->stream) cudaStreamSynchronize(p->stream);
     for (void* x : ptrs)
         if (x) cudaFree(x);
     if (p->hbuf) cudaFreeHost(p->hbuf);
     if (p->hgoal) cudaFreeHost(p->hgoal);
+    if (p->bp_hctr) cudaFreeHost(p->bp_hctr);
+    if (p->bp_hgoal) cudaFreeHost(p->bp_hgoal);
     scratch_free(&p->scratch);
     for (cudaEvent_t e : p->ev)
         if (e) cudaEventDestroy(e);
@@ -613,6 +626,7 @@ static mptg_status planner_reset(mptg_planner* p, const mptg_plan_params* prm, b
     p->stat_seconds = 0;
     for (double& t : p->t_phase) t = 0;
     p->stat_rewire_tests = 0;
+    p->stat_bp_waves = 0;
     for (double& t : p->t_star) t = 0;
     if (p->nrw) MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->nrw, 0, sizeof(unsigned long long), p->stream));
     return MPTG_OK;
@@ -837,7 +851,96 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
     return MPTG_OK;
 }
 
+static bool bp_applies(const mptg_planner* p) {
+    return p->bp_mode && !p->star && !p->sg && bplan_supported(p->scene, p->prm.wavefront, p->prm.resolution);
+}
+
+// Wavefronts inside the persistent block planner until a stop condition
+// (solved, node budget, wavefront count, time) or its node capacity; then the
+// kd-tree takes the new nodes and the host its goals.  *waves: wavefronts run.
+static mptg_status run_persistent(mptg_planner* p, int max_waves, double time_limit_s, int stop_when_solved,
+                                  int* waves) {
+    mptg_ctx* ctx = p->ctx;
+    cudaStream_t s = p->stream;
+    *waves = 0;
+    size_t n0 = 0;
+    mptg_tree_size(p->tree, &n0);
+    const int W = p->prm.wavefront;
+    const int cap = p->bp_states ? p->bp_cap : (int)std::min<size_t>(p->prm.max_nodes, BPLAN_MAX_NODES);
+    if (n0 >= p->prm.max_nodes || std::min<size_t>(n0 + W, p->prm.max_nodes) > (size_t)cap) return MPTG_OK;
+    if (!p->bp_states) {
+        cudaError_t e = cudaMalloc((void**)&p->bp_states, (size_t)cap * 2 * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&p->bp_goalf, cap);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&p->bp_ctr, sizeof(BPlanCounters));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&p->bp_job, sizeof(BPlanJob));
+        if (e == cudaSuccess) e = cudaMallocHost((void**)&p->bp_hctr, sizeof(BPlanCounters));
+        if (e == cudaSuccess) e = cudaMallocHost((void**)&p->bp_hgoal, cap);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return mptg_fail(ctx, MPTG_ERR_OOM, "block planner buffers: %s", cudaGetErrorString(e));
+        }
+        p->bp_cap = cap;
+    }
+    const PlanView v = plan_view(p);
+    BPlanJob j{};
+    j.scene = scene_view(p->scene);
+    j.lo = p->lo;
+    j.hi = p->hi;
+    j.goal = p->goal;
+    j.has_goal = p->has_goal;
+    j.goal_bias = v.goal_bias;
+    j.range = v.range;
+    j.goal_radius = v.goal_radius;
+    j.inv_step = 1.0 / p->prm.edge_step;
+    j.seed = v.seed;
+    j.states = p->bp_states;
+    j.parent = p->parent;
+    j.goalf = p->bp_goalf;
+    j.ctr = p->bp_ctr;
+    j.nsamp = p->nsamp;
+    j.max_nodes = p->prm.max_nodes;
+    j.cap = p->bp_cap;
+    j.W = W;
+    j.max_waves = max_waves;
+    j.stop_when_solved = stop_when_solved;
+    j.deadline_ns = time_limit_s > 0 ? (uint64_t)(time_limit_s * 1e9) : 0;
+    BPlanCounters* h = p->bp_hctr;
+    *h = BPlanCounters{};
+    h->n = (int)n0;
+    h->wave = p->wave;
+    h->goals = (int)p->goals.size();
+    mptg_status st = mptg_tree_states(p->tree, 0, n0, p->bp_states, s);
+    if (st) return st;
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_job, &j, sizeof(j), cudaMemcpyHostToDevice, s));
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_ctr, h, sizeof(*h), cudaMemcpyHostToDevice, s));
+    if ((st = bplan_launch(ctx, p->bp_job, 1, W, p->bp_cap, s))) return st;
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(h, p->bp_ctr, sizeof(*h), cudaMemcpyDeviceToHost, s));
+    MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    const size_t n1 = (size_t)h->n;
+    p->wave = h->wave;
+    p->stat_samples += h->samples;
+    p->stat_accepted += h->accepted;
+    p->stat_wavefronts += (uint64_t)h->waves_run;
+    p->stat_bp_waves += (uint64_t)h->waves_run;
+    *waves = h->waves_run;
+    if (n1 > n0) {
+        const size_t k = n1 - n0;
+        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_hgoal, p->bp_goalf + n0, k, cudaMemcpyDeviceToHost, s));
+        if ((st = mptg_tree_insert(p->tree, p->bp_states + n0 * 2, k, s))) return st;
+        MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        for (size_t i = 0; i < k; ++i)
+            if (p->bp_hgoal[i]) p->goals.push_back((int)(n0 + i));
+    }
+    return MPTG_OK;
+}
+
 extern "C" {
+
+mptg_status mptg_planner_set_persistent(mptg_planner* p, int mode) {
+    if (!p || mode < 0 || mode > 1) return MPTG_ERR_INVALID_ARG;
+    p->bp_mode = mode;
+    return MPTG_OK;
+}
 
 mptg_status mptg_planner_create(mptg_ctx* ctx, mptg_scene* scene, const mptg_plan_params* prm, const double* lo,
                                 const double* hi, mptg_planner** out) {
@@ -963,7 +1066,12 @@ mptg_status mptg_planner_run(mptg_planner* p, int max_wavefronts, double time_li
     MPTG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     auto t0 = std::chrono::steady_clock::now();
     mptg_status st = MPTG_OK;
-    for (int it = 0; max_wavefronts <= 0 || it < max_wavefronts; ++it) {
+    int it = 0;
+    if (bp_applies(p) && !(stop_when_solved && !p->goals.empty()))
+        st = run_persistent(p, max_wavefronts, time_limit_s, stop_when_solved, &it);
+    // the multi-kernel wavefront: every other case, and what remains of this
+    // call once the block planner's node capacity is reached
+    for (; !st && (max_wavefronts <= 0 || it < max_wavefronts); ++it) {
         if (stop_when_solved && !p->goals.empty()) break;
         mptg_tree_size(p->tree, &n);
         if (n >= p->prm.max_nodes) break;

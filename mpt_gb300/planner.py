@@ -137,6 +137,7 @@ def _sig(L):
         ("mptg_planner_solution", ctypes.c_int, [P, P, S, ctypes.POINTER(S), ctypes.POINTER(ctypes.c_double)]),
         ("mptg_planner_graph", ctypes.c_int, [P, P, P, S, ctypes.POINTER(S)]),
         ("mptg_planner_tree", ctypes.c_int, [P, ctypes.POINTER(P)]),
+        ("mptg_planner_set_persistent", ctypes.c_int, [P, ctypes.c_int]),
         ("mptg_planner_stats", ctypes.c_int, [P, P]),
         ("mptg_planner_timers", ctypes.c_int, [P, P]),
         ("mptg_planner_set_rewire", ctypes.c_int, [P, ctypes.c_int, ctypes.c_double]),
@@ -185,8 +186,17 @@ class Planner:
         self._rewire_factor = 1.1
         self._starts = []
         self._surrogate = None
+        self._persistent = 1
         self.scene = Scene(self.ctx, scenario.desc)
         self.h = None
+
+    def set_persistent(self, on: bool):
+        """Run wavefronts inside the persistent block planner where it applies
+        (grid scenes, wavefront <= 1024; the default) or always as separate
+        kernels (False).  The two build the same tree."""
+        self._persistent = 1 if on else 0
+        if self.h is not None:
+            _check(self.ctx.h, self.lib.mptg_planner_set_persistent(self.h, self._persistent))
 
     def set_surrogate(self, surrogate, threshold: float = 0.0, points: int = 1):
         """Cull edges the surrogate scores above `threshold` (collision logit)
@@ -258,6 +268,7 @@ class Planner:
         _check(self.ctx.h, self.lib.mptg_planner_create(self.ctx.h, self.scene.h, ctypes.byref(prm),
                                                         sc.lo.ctypes.data, sc.hi.ctypes.data, ctypes.byref(h)))
         self.h = h
+        _check(self.ctx.h, self.lib.mptg_planner_set_persistent(h, self._persistent))
         g = np.ascontiguousarray(sc.goal.state, dtype=np.float64)
         _check(self.ctx.h, self.lib.mptg_planner_set_goal(h, g.ctypes.data, sc.goal.radius))
         if self.algorithm.rewire:
@@ -276,14 +287,23 @@ class Planner:
                                                      int(stop_when_solved), ctypes.byref(solved)))
         return bool(solved.value)
 
-    def solve(self, done_fn):
-        """Runs wavefronts until done_fn() is true (polled between wavefronts)."""
+    # wavefronts per call between polls of done_fn: each call also stops at the
+    # first solution, so a solve until solved() ends on the wavefront that finds it
+    POLL_WAVEFRONTS = 16
+
+    def solve(self, done_fn, deadline: float | None = None):
+        """Runs wavefronts until done_fn() is true: polled between calls of up
+        to POLL_WAVEFRONTS wavefronts, each of which ends early at the first
+        solution or at the deadline (time.monotonic())."""
         if self.size() == 0:
             raise RuntimeError("there are no valid initial states")
         self._create()
         while not done_fn():
             before = self.stats()["wavefront_counter"]
-            self.run(1)
+            left = 0.0 if deadline is None else deadline - time.monotonic()
+            if deadline is not None and left <= 0:
+                break
+            self.run(self.POLL_WAVEFRONTS, time_limit=left, stop_when_solved=not self.solved())
             if self.stats()["wavefront_counter"] == before:  # node budget exhausted
                 break
 
@@ -293,9 +313,9 @@ class Planner:
 
     def solve_until(self, deadline: float, done_fn=None):
         if done_fn is None:
-            self.solve(lambda: time.monotonic() >= deadline)
+            self.solve(lambda: time.monotonic() >= deadline, deadline)
         else:
-            self.solve(lambda: time.monotonic() >= deadline or done_fn())
+            self.solve(lambda: time.monotonic() >= deadline or done_fn(), deadline)
 
     def solved(self) -> bool:
         if self.h is None:
@@ -480,11 +500,16 @@ class PPRMPlanner(Planner):
                                                  int(stop_when_solved), ctypes.byref(solved)))
         return bool(solved.value)
 
-    def solve(self, done_fn):
-        """Runs wavefronts until done_fn() is true (polled between wavefronts)."""
+    def solve(self, done_fn, deadline: float | None = None):
+        """Runs wavefronts until done_fn() is true: polled between calls of up
+        to POLL_WAVEFRONTS wavefronts, each of which ends early at the first
+        solution or at the deadline (time.monotonic())."""
         while not done_fn():
             before = self.stats()["wavefronts"]
-            self.run(1)
+            left = 0.0 if deadline is None else deadline - time.monotonic()
+            if deadline is not None and left <= 0:
+                break
+            self.run(self.POLL_WAVEFRONTS, time_limit=left, stop_when_solved=not self.solved())
             if self.stats()["wavefronts"] == before:  # node budget exhausted
                 break
 
