@@ -279,7 +279,7 @@ def nn_1m_section(ctx, m, torch, steps=5, peak=None, cpu_sample=2048):
     return out
 
 
-def _solve_stats(ctx, sc, W, seeds, cap_s, surrogate=None, points=1, want_path=False):
+def _solve_stats(ctx, sc, W, seeds, cap_s, surrogate=None, points=1, want_path=False, candidates=1):
     """p50/p99 wall time to the first solution over seeds 1000.., with the phase timers."""
     from mpt_gb300 import planner as P
     import oracle
@@ -289,7 +289,7 @@ def _solve_stats(ctx, sc, W, seeds, cap_s, surrogate=None, points=1, want_path=F
     for s in range(seeds):
         pl = P.Planner(P.Scenario(sc), P.PRRT(P.gpu_wavefront(W)), seed=1000 + s, ctx=ctx, max_nodes=1 << 21)
         if surrogate is not None:
-            pl.set_surrogate(surrogate, threshold=2.0, points=points)
+            pl.set_surrogate(surrogate, threshold=2.0, points=points, candidates=candidates)
         pl.add_start(sc["start"])
         t0 = time.perf_counter()
         pl.solve_for(cap_s, lambda: pl.solved())
@@ -446,18 +446,29 @@ def surrogate_rates(ctx, m, torch, n_train=1 << 22, epochs=10):
     return res, sg, sc
 
 
-def learned_vs_plain(ctx, m, torch, seeds=5, cap_s=20.0, n_train=1 << 22, epochs=10, wavefront_tuned=None):
+LEARNED_MODES = (("plain", 0, 1), ("learned_new_state", 1, 1), ("learned_edge_4pts", 4, 1),
+                 ("learned_biased_x4", 1, 4))
+
+
+def learned_vs_plain(ctx, m, torch, seeds=20, cap_s=20.0, n_train=1 << 22, epochs=10, wavefront_tuned=None):
     """Learned collision surrogate on the SE(3) scene: training throughput, held-out
     FP/FN rates, scoring throughput against the bf16 tensor peak, and time to
-    solve with the surrogate culling edges versus the plain planner (same seeds)."""
+    solve versus the plain planner on the same seeds: culling by the new state's
+    logit, by 4 points per edge, and surrogate-biased sampling (each slot keeps
+    the lowest-risk of 4 candidate edges, then the same culling).  Every solved
+    path is re-validated by the CPU checker."""
     res, sg, sc = surrogate_rates(ctx, m, torch, n_train, epochs)
-    # plain versus learned at the configured wavefront (4096) and at the
-    # autotuned one for this scene, same seeds
+    # at the configured wavefront (4096) and at the autotuned one for this scene
     Ws = sorted({4096, int(wavefront_tuned or 4096)})
     for W in Ws:
-        for mode, points in (("plain", 0), ("learned_new_state", 1), ("learned_edge_4pts", 4)):
-            res["%s_w%d" % (mode, W)] = _solve_stats(ctx, sc, W, seeds, cap_s, sg if points else None, points)
-    return res
+        for mode, points, cand in LEARNED_MODES:
+            res["%s_w%d" % (mode, W)] = _solve_stats(ctx, sc, W, seeds, cap_s, sg if points else None, points,
+                                                     candidates=cand)
+        plain = res["plain_w%d" % W]["p50_s"]
+        res["p50_speedup_vs_plain_w%d" % W] = {mode: (plain / res["%s_w%d" % (mode, W)]["p50_s"]
+                                                      if plain and res["%s_w%d" % (mode, W)]["p50_s"] else None)
+                                               for mode, _, _ in LEARNED_MODES[1:]}
+    return res, sg
 
 
 def prrt_star_section(ctx, wave_for=None, refine_s=1.0, seeds=3):
@@ -563,7 +574,7 @@ def prm_section(ctx, seeds=3, cap_s=20.0):
     return out
 
 
-def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0, wave_for=None):
+def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0, wave_for=None, surrogate=None):
     """Config of the serving benchmark: n queries uniform over the three scenes,
     start and goal rejection-sampled valid, node budgets log-uniform in
     [1k, 200k]; wavefront = the scene's autotuned size (wave_for[kind]) when
@@ -597,16 +608,21 @@ def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0, wave_for=None):
         W = wave_for[d["kind"]] if wave_for else budget // 16
         W = int(min(4096, budget // 4, max(256, W)))
         sc = P.Scenario(d, P.GoalState(d["goal_radius"], b))
-        qs.append(Query(sc, a, seed=seed + i, max_nodes=budget, wavefront=W, time_limit=time_limit))
+        q = Query(sc, a, seed=seed + i, max_nodes=budget, wavefront=W, time_limit=time_limit)
+        if surrogate is not None and d["kind"] == "mesh":  # the surrogate is trained on the SE(3) scene
+            q.surrogate, q.threshold, q.surrogate_candidates = surrogate, 2.0, 4
+        qs.append(q)
     return qs
 
 
-def batch_serving(m, ctx, n=512, concurrency=8, seq_sample=64, wave_for=None):
+def batch_serving(m, ctx, n=512, concurrency=8, seq_sample=64, wave_for=None, surrogate=None):
     """Batched multi-query serving: queries/s and time to solution over n queries
     with `concurrency` concurrent planners, against the same planner running the
-    queries one after another (on the first seq_sample queries)."""
+    queries one after another (on the first seq_sample queries).  Grid queries
+    run as persistent block planners; with a surrogate, the SE(3) queries use
+    surrogate-biased sampling and culling."""
     from mpt_gb300.batch import plan_batch
-    qs = batch_queries(m, ctx, n, wave_for=wave_for)
+    qs = batch_queries(m, ctx, n, wave_for=wave_for, surrogate=surrogate)
     plan_batch(ctx, qs[:8], concurrency=concurrency)  # warm-up: planners, kernels
     t0 = time.perf_counter()
     r = plan_batch(ctx, qs, concurrency=concurrency)
@@ -801,14 +817,19 @@ def run_gpu(args):
     solves = solve_times(ctx) if not args.no_solve else None
     w_se3 = solves["se3_mesh"]["autotune"]["best"] if solves and "autotune" in solves["se3_mesh"] else None
     _progress("learned surrogate")
-    learned = (learned_vs_plain(ctx, m, torch, wavefront_tuned=w_se3)
-               if not (args.no_solve or args.no_learned) else None)
+    learned, sg = (learned_vs_plain(ctx, m, torch, wavefront_tuned=w_se3)
+                   if not (args.no_solve or args.no_learned) else (None, None))
     wave_for = None
     if solves and all("autotune" in solves[k] for k in solves):
         wave_for = {"grid": solves["grid_1024"]["autotune"]["best"], "arm": solves["arm_10link"]["autotune"]["best"],
                     "mesh": solves["se3_mesh"]["autotune"]["best"]}
     _progress("batched serving")
-    serving = batch_serving(m, ctx, wave_for=wave_for) if not (args.no_solve or args.no_batch) else None
+    serving = None
+    if not (args.no_solve or args.no_batch):
+        serving = {"plain": batch_serving(m, ctx, wave_for=wave_for)}
+        if sg is not None:
+            _progress("batched serving with the surrogate")
+            serving["surrogate"] = batch_serving(m, ctx, wave_for=wave_for, surrogate=sg)
     _progress("PRRT*")
     star = prrt_star_section(ctx, wave_for) if not (args.no_solve or args.no_star) else None
     _progress("PPRM")

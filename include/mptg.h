@@ -277,6 +277,14 @@ mptg_status mptg_planner_set_surrogate(mptg_planner* planner, mptg_surrogate* su
  * and interpolate(near, new, j/points) for 1 <= j < points; the edge is culled
  * when any of them exceeds the threshold. */
 mptg_status mptg_planner_set_surrogate_points(mptg_planner* planner, int points);
+/* Surrogate-biased sampling (1 .. 16, default 1 = off): each wavefront slot
+ * draws `candidates` samples, finds their nearest nodes and steers all of
+ * them, the surrogate scores every candidate edge, and the slot keeps the one
+ * whose highest collision logit is lowest (candidate 0 is the plain planner's
+ * sample; the goal sample always keeps its slot).  The kept edge is culled or
+ * exact-checked as above: an edge still enters the tree only after the exact
+ * check.  No reference counterpart (the learned part of the planner). */
+mptg_status mptg_planner_set_surrogate_bias(mptg_planner* planner, int candidates);
 
 /* WorkerStats (prrt.hpp:63-101): [0] wavefronts, [1] samples, [2] nodes
  * added, [3] tree size, [4] goals, [5] states checked by link, [6] seconds in
@@ -334,6 +342,7 @@ typedef struct {
     int surrogate_points;       /* as mptg_planner_set_surrogate_points (<= 1: the new state only) */
     double* path;               /* optional host buffer of path_cap states */
     size_t path_cap;
+    int surrogate_candidates;   /* as mptg_planner_set_surrogate_bias (<= 1: off) */
 } mptg_query;
 
 typedef struct {

@@ -25,7 +25,7 @@ class _Query(ctypes.Structure):
                 ("goal_radius", ctypes.c_double), ("params", _Params), ("lo", ctypes.c_void_p),
                 ("hi", ctypes.c_void_p), ("time_limit_s", ctypes.c_double), ("surrogate", ctypes.c_void_p),
                 ("surrogate_threshold", ctypes.c_double), ("surrogate_points", ctypes.c_int),
-                ("path", ctypes.c_void_p), ("path_cap", ctypes.c_size_t)]
+                ("path", ctypes.c_void_p), ("path_cap", ctypes.c_size_t), ("surrogate_candidates", ctypes.c_int)]
 
 
 class _Result(ctypes.Structure):
@@ -62,6 +62,7 @@ class Query:
     surrogate: object | None = None   # mpt_gb300.surrogate.Surrogate
     threshold: float = 0.0
     surrogate_points: int = 1         # states scored per candidate edge
+    surrogate_candidates: int = 1     # candidate edges per wavefront slot (surrogate-biased sampling)
     path_cap: int = 4096
 
 
@@ -109,6 +110,7 @@ def plan_batch(ctx: Context, queries: list[Query], concurrency: int = 8) -> list
             p.surrogate = h.value if isinstance(h, ctypes.c_void_p) else h
             p.surrogate_threshold = float(q.threshold)
             p.surrogate_points = int(q.surrogate_points)
+            p.surrogate_candidates = int(q.surrogate_candidates)
         p.path, p.path_cap = path.ctypes.data, q.path_cap
     out = (_Result * len(queries))()
     _check(ctx.h, L.mptg_plan_batch(ctx.h, qs, len(queries), int(concurrency), out))

@@ -85,6 +85,19 @@ struct mptg_planner {
     int sg_points = 1;          // states scored per candidate edge
     double* sg_pts = nullptr;   // [sg_points][cap_wave][D] when sg_points > 1
     int sg_pts_cap = 1;         // sg_points the logits/sg_pts buffers hold
+    // surrogate-biased sampling: each wavefront slot takes the lowest-risk of
+    // sg_bias candidate edges (candidate buffers hold cap_wave * sg_bias)
+    int sg_bias = 1;
+    int sg_bias_cap = 0;
+    double* b_samp = nullptr;
+    int* b_nidx = nullptr;
+    double* b_ndist = nullptr;
+    double* b_near = nullptr;
+    double* b_new = nullptr;
+    uint8_t* b_skip = nullptr;
+    double* b_pts = nullptr;    // [P][W * sg_bias][D]
+    float* b_logits = nullptr;  // [P][W * sg_bias]
+    int b_pts_cap = 0;          // P the two buffers above hold
     // every call of this planner runs on its own non-blocking stream, with its
     // own validity scratch, so planners on one scene can run concurrently
     cudaStream_t stream = nullptr;
@@ -288,6 +301,63 @@ __global__ void k_plan_keep(int W, int P, const uint8_t* __restrict__ skip, cons
     for (int j = 0; j < P; ++j) cull = cull || logit[(size_t)j * W + i] > thr;
     keep[i] = (!skip[i] && !cull) ? 1 : 0;
     ok[i] = 0;
+}
+
+// candidate c = j*W + i (j < B) of a biased wavefront: Philox sample c of the
+// wavefront (j = 0 is the plain planner's sample i; the goal sample, when
+// picked, replaces candidate 0 of its slot)
+__global__ void k_plan_sample_cand(PlanView p, int W, int B, uint32_t wave, const int* __restrict__ goal_index,
+                                   double* __restrict__ out) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= W * B) return;
+    double* q = out + (size_t)c * p.D;
+    if (goal_index != nullptr && c == *goal_index) {
+        for (int d = 0; d < p.D; ++d) q[d] = p.goal[d];
+        return;
+    }
+    sample_uniform_state(p.metric, p.D, p.seed, (uint32_t)c, wave, p.lo, p.hi, q);
+}
+
+// Slot i takes, of its candidates j*W + i, the one whose highest collision
+// logit over its P scored points is lowest (a skipped candidate only when all
+// are; ties: the lowest j); the goal sample's slot keeps the goal.  The
+// chosen candidate's sample, nearest node, edge and logits fill slot i.
+__global__ void k_plan_bias_select(int W, int B, int P, int D, const int* __restrict__ goal_index,
+                                   const double* __restrict__ csamp, const int* __restrict__ cnidx,
+                                   const double* __restrict__ cndist, const double* __restrict__ cnear,
+                                   const double* __restrict__ cnew, const uint8_t* __restrict__ cskip,
+                                   const float* __restrict__ clogit, double* __restrict__ samp, int* __restrict__ nidx,
+                                   double* __restrict__ ndist, double* __restrict__ nearst, double* __restrict__ newst,
+                                   uint8_t* __restrict__ skip, float* __restrict__ logit) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W) return;
+    const size_t WB = (size_t)W * B;
+    int best = 0;
+    if (!(goal_index != nullptr && i == *goal_index)) {
+        float bl = INFINITY;
+        bool bskip = true;
+        for (int j = 0; j < B; ++j) {
+            const size_t c = (size_t)j * W + i;
+            float l = -INFINITY;
+            for (int k = 0; k < P; ++k) l = fmaxf(l, clogit[k * WB + c]);
+            const bool sk = cskip[c] != 0;
+            if (j == 0 || (bskip && !sk) || (sk == bskip && l < bl)) {
+                best = j;
+                bl = l;
+                bskip = sk;
+            }
+        }
+    }
+    const size_t c = (size_t)best * W + i;
+    for (int d = 0; d < D; ++d) {
+        samp[(size_t)i * D + d] = csamp[c * D + d];
+        nearst[(size_t)i * D + d] = cnear[c * D + d];
+        newst[(size_t)i * D + d] = cnew[c * D + d];
+    }
+    nidx[i] = cnidx[c];
+    ndist[i] = cndist[c];
+    skip[i] = cskip[c];
+    for (int k = 0; k < P; ++k) logit[(size_t)k * W + i] = clogit[k * WB + c];
 }
 
 __global__ void k_plan_cgather(PlanView p, int W, const int* __restrict__ scan, const int* __restrict__ bsum,
@@ -554,7 +624,8 @@ static void planner_free(mptg_planner* p) {
                     p->near_c, p->new_c, p->cmap, p->ok_c, p->keep, p->path_ids, p->path_out, p->sg_pts,
                     p->cost, p->elen, p->pj_s, p->pj_a, p->pj_a2, p->bbits, p->bid, p->knn_i, p->knn_d, p->pv,
                     p->s_pair, p->s_rcost, p->s_ok, p->s_ea, p->s_eb, p->dnear, p->cpar, p->ccost, p->celen,
-                    p->s_cnt, p->nrw, p->rank, p->decided, p->bp_states, p->bp_goalf, p->bp_ctr, p->bp_job};
+                    p->s_cnt, p->nrw, p->rank, p->decided, p->bp_states, p->bp_goalf, p->bp_ctr, p->bp_job,
+                    p->b_samp, p->b_nidx, p->b_ndist, p->b_near, p->b_new, p->b_skip, p->b_pts, p->b_logits};
     if (p->stream) cudaStreamSynchronize(p->stream);
     for (void* x : ptrs)
         if (x) cudaFree(x);
@@ -747,12 +818,26 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
         k_plan_goalpick<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->wave, gidx);
         MPTG_LAUNCHED(ctx);
     }
-    k_plan_sample<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->wave, gidx, p->samp);
-    mptg_status st = mptg_tree_nearest_dev(p->tree, p->samp, W, p->nidx, p->ndist, s, false);
-    if (st) return st;
-    k_plan_steer<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->samp, p->nidx, p->ndist, mptg_tree_states_dev(p->tree),
-                                                     p->nearst, p->newst, p->skip);
-    ctx->launches += 2;
+    const bool biased = p->sg && p->sg_bias > 1;
+    mptg_status st;
+    if (biased) {
+        // W * B candidate edges, NN and steer for all of them
+        const int B = p->sg_bias, WB = W * B;
+        k_plan_sample_cand<<<mptg_blocks(WB, 128), 128, 0, s>>>(v, W, B, p->wave, gidx, p->b_samp);
+        MPTG_LAUNCHED(ctx);
+        if ((st = mptg_tree_nearest_dev(p->tree, p->b_samp, WB, p->b_nidx, p->b_ndist, s, false))) return st;
+        k_plan_steer<<<mptg_blocks(WB, 128), 128, 0, s>>>(v, WB, p->b_samp, p->b_nidx, p->b_ndist,
+                                                          mptg_tree_states_dev(p->tree), p->b_near, p->b_new,
+                                                          p->b_skip);
+        MPTG_LAUNCHED(ctx);
+    } else {
+        k_plan_sample<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->wave, gidx, p->samp);
+        st = mptg_tree_nearest_dev(p->tree, p->samp, W, p->nidx, p->ndist, s, false);
+        if (st) return st;
+        k_plan_steer<<<mptg_blocks(W, 128), 128, 0, s>>>(v, W, p->samp, p->nidx, p->ndist,
+                                                         mptg_tree_states_dev(p->tree), p->nearst, p->newst, p->skip);
+        ctx->launches += 2;
+    }
     MPTG_CUDA_TRY(ctx, cudaEventRecord(p->ev[1], s));
     int nblk = (W + PLAN_SCAN_BLOCK - 1) / PLAN_SCAN_BLOCK;
     if (p->sg) {
@@ -762,15 +847,34 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
             // the surrogate's activation buffers are shared between planners:
             // hold it until this stream has consumed its logits
             const int P = p->sg_points;
-            if (P > 1) {
-                MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->sg_pts, p->newst, (size_t)W * p->D * sizeof(double),
-                                                   cudaMemcpyDeviceToDevice, s));
-                k_plan_edge_points<<<mptg_blocks((size_t)W * (P - 1), 128), 128, 0, s>>>(v, W, P, p->nearst, p->newst,
-                                                                                         p->sg_pts);
-                MPTG_LAUNCHED(ctx);
-            }
             std::lock_guard<std::mutex> lock(*mptg_surrogate_mutex(p->sg));
-            if ((st = mptg_surrogate_score_dev(p->sg, P > 1 ? p->sg_pts : p->newst, W * P, p->logits, s))) return st;
+            if (biased) {
+                // score every candidate edge, then each slot takes its lowest-risk candidate
+                const int B = p->sg_bias, WB = W * B;
+                if (P > 1) {
+                    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->b_pts, p->b_new, (size_t)WB * p->D * sizeof(double),
+                                                       cudaMemcpyDeviceToDevice, s));
+                    k_plan_edge_points<<<mptg_blocks((size_t)WB * (P - 1), 128), 128, 0, s>>>(v, WB, P, p->b_near,
+                                                                                              p->b_new, p->b_pts);
+                    MPTG_LAUNCHED(ctx);
+                }
+                if ((st = mptg_surrogate_score_dev(p->sg, P > 1 ? p->b_pts : p->b_new, WB * P, p->b_logits, s)))
+                    return st;
+                k_plan_bias_select<<<mptg_blocks(W, 128), 128, 0, s>>>(
+                    W, B, P, p->D, gidx, p->b_samp, p->b_nidx, p->b_ndist, p->b_near, p->b_new, p->b_skip,
+                    p->b_logits, p->samp, p->nidx, p->ndist, p->nearst, p->newst, p->skip, p->logits);
+                MPTG_LAUNCHED(ctx);
+            } else {
+                if (P > 1) {
+                    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->sg_pts, p->newst, (size_t)W * p->D * sizeof(double),
+                                                       cudaMemcpyDeviceToDevice, s));
+                    k_plan_edge_points<<<mptg_blocks((size_t)W * (P - 1), 128), 128, 0, s>>>(v, W, P, p->nearst,
+                                                                                             p->newst, p->sg_pts);
+                    MPTG_LAUNCHED(ctx);
+                }
+                if ((st = mptg_surrogate_score_dev(p->sg, P > 1 ? p->sg_pts : p->newst, W * P, p->logits, s)))
+                    return st;
+            }
             k_plan_keep<<<mptg_blocks(W, 256), 256, 0, s>>>(W, P, p->skip, p->logits, p->sg_thr, p->keep, p->ok);
             k_plan_scan<<<nblk, PLAN_SCAN_BLOCK, 0, s>>>(W, p->keep, p->skip, p->scan, p->bsum);
             k_plan_scan_top<<<1, 1024, 0, s>>>(nblk, p->bsum);
@@ -1214,6 +1318,43 @@ mptg_status mptg_planner_set_surrogate_points(mptg_planner* p, int points) {
         p->sg_pts_cap = points;
     }
     p->sg_points = points;
+    if (p->sg_bias > 1 && points > p->b_pts_cap) return mptg_planner_set_surrogate_bias(p, p->sg_bias);
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_set_surrogate_bias(mptg_planner* p, int candidates) {
+    if (!p) return MPTG_ERR_INVALID_ARG;
+    if (candidates < 1 || candidates > 16)
+        return mptg_fail(p->ctx, MPTG_ERR_INVALID_ARG, "candidates per wavefront slot must be in [1, 16]");
+    const size_t W = p->cap_wave, D = p->D, P = (size_t)std::max(p->sg_points, p->sg_pts_cap);
+    if (candidates > 1 && (candidates > p->sg_bias_cap || (int)P > p->b_pts_cap)) {
+        MPTG_CUDA_TRY(p->ctx, cudaStreamSynchronize(p->stream));
+        void* old[] = {p->b_samp, p->b_nidx, p->b_ndist, p->b_near, p->b_new, p->b_skip, p->b_pts, p->b_logits};
+        for (void* x : old)
+            if (x) cudaFree(x);
+        const int B = std::max(candidates, p->sg_bias_cap);
+        const size_t WB = W * B;
+        cudaError_t e = cudaSuccess;
+#define ALLOC(ptr, bytes) if (e == cudaSuccess) e = cudaMalloc((void**)&(ptr), (bytes))
+        ALLOC(p->b_samp, WB * D * sizeof(double));
+        ALLOC(p->b_nidx, WB * sizeof(int));
+        ALLOC(p->b_ndist, WB * sizeof(double));
+        ALLOC(p->b_near, WB * D * sizeof(double));
+        ALLOC(p->b_new, WB * D * sizeof(double));
+        ALLOC(p->b_skip, WB);
+        ALLOC(p->b_pts, WB * P * D * sizeof(double));
+        ALLOC(p->b_logits, WB * P * sizeof(float));
+#undef ALLOC
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            p->sg_bias_cap = 0;
+            p->b_pts_cap = 0;
+            return mptg_fail(p->ctx, MPTG_ERR_OOM, "surrogate bias buffers: %s", cudaGetErrorString(e));
+        }
+        p->sg_bias_cap = B;
+        p->b_pts_cap = (int)P;
+    }
+    p->sg_bias = candidates;
     return MPTG_OK;
 }
 
@@ -1346,6 +1487,7 @@ static mptg_status batch_query(mptg_ctx* ctx, const mptg_query& q, const BatchCa
     if ((st = planner_reset(p, &q.params, true, q.lo, q.hi))) return st;
     if ((st = mptg_planner_set_surrogate(p, q.surrogate, q.surrogate_threshold))) return st;
     if ((st = mptg_planner_set_surrogate_points(p, q.surrogate ? std::max(1, q.surrogate_points) : 1))) return st;
+    if ((st = mptg_planner_set_surrogate_bias(p, q.surrogate ? std::max(1, q.surrogate_candidates) : 1))) return st;
     if ((st = mptg_planner_add_start(p, q.start))) return st;
     if ((st = mptg_planner_set_goal(p, q.goal, q.goal_radius))) return st;
     const auto t = std::chrono::steady_clock::now();

@@ -198,19 +198,23 @@ class Planner:
         if self.h is not None:
             _check(self.ctx.h, self.lib.mptg_planner_set_persistent(self.h, self._persistent))
 
-    def set_surrogate(self, surrogate, threshold: float = 0.0, points: int = 1):
+    def set_surrogate(self, surrogate, threshold: float = 0.0, points: int = 1, candidates: int = 1):
         """Cull edges the surrogate scores above `threshold` (collision logit)
         before the exact check: the new state and points-1 interior states of
-        each candidate edge are scored.  None removes it."""
-        self._surrogate = (surrogate, float(threshold), int(points)) if surrogate is not None else None
+        each candidate edge are scored.  candidates > 1: each wavefront slot
+        keeps the lowest-risk of that many candidate edges (surrogate-biased
+        sampling).  None removes it."""
+        self._surrogate = ((surrogate, float(threshold), int(points), int(candidates)) if surrogate is not None
+                           else None)
         if self.h is not None:
             self._apply_surrogate()
 
     def _apply_surrogate(self):
         from . import surrogate as S
         S._sig(self.lib)
-        sg, thr, pts = self._surrogate if self._surrogate else (None, 0.0, 1)
+        sg, thr, pts, cand = self._surrogate if self._surrogate else (None, 0.0, 1, 1)
         _check(self.ctx.h, self.lib.mptg_planner_set_surrogate_points(self.h, pts))
+        _check(self.ctx.h, self.lib.mptg_planner_set_surrogate_bias(self.h, cand))
         _check(self.ctx.h, self.lib.mptg_planner_set_surrogate(self.h, sg.h if sg else None, thr))
 
     # -- configuration (prrt.hpp:159-175)

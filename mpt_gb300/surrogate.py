@@ -27,6 +27,7 @@ def _sig(L):
         ("mptg_surrogate_score", [P, P, S, P, P]),
         ("mptg_planner_set_surrogate", [P, P, ctypes.c_double]),
         ("mptg_planner_set_surrogate_points", [P, ctypes.c_int]),
+        ("mptg_planner_set_surrogate_bias", [P, ctypes.c_int]),
     ]:
         f = getattr(L, name)
         f.restype = ctypes.c_int

@@ -8,7 +8,9 @@
 * training on exact-checker labels learns the SE(3) scene (held-out accuracy,
   false-positive / false-negative rates reported);
 * the surrogate-culled planner returns only exact-validated paths and spends
-  fewer exact checks than the plain planner for the same wavefronts."""
+  fewer exact checks than the plain planner for the same wavefronts; with
+  surrogate-biased sampling (lowest-risk of 4 candidate edges per slot) its
+  tree grows faster per wavefront and stays deterministic."""
 import numpy as np
 import pytest
 
@@ -79,11 +81,13 @@ def test_surrogate_planner_exact_paths_and_fewer_checks(ctx, orc, trained):
     sc, sg, _ = trained
     waves = 6
     stats = {}
-    for mode in ("plain", "surrogate"):
+    for mode in ("plain", "surrogate", "biased"):
         pl = P.Planner(P.Scenario(sc), P.PRRT(P.gpu_wavefront(4096)), seed=17, ctx=ctx, max_nodes=1 << 20)
         pl.add_start(sc["start"])
         if mode == "surrogate":
             pl.set_surrogate(sg, threshold=2.0)
+        elif mode == "biased":
+            pl.set_surrogate(sg, threshold=2.0, candidates=4)
         pl.run(waves)
         st = pl.stats()
         stats[mode] = st
@@ -98,3 +102,22 @@ def test_surrogate_planner_exact_paths_and_fewer_checks(ctx, orc, trained):
         stats["plain"]["link_states_checked"], stats["surrogate"]["link_states_checked"],
         stats["plain"]["tree_size"], stats["surrogate"]["tree_size"]))
     assert stats["surrogate"]["link_states_checked"] < stats["plain"]["link_states_checked"]
+    # biased sampling keeps the lowest-risk of 4 candidates: more of the exact
+    # checks pass, so the tree grows faster per wavefront
+    assert stats["biased"]["tree_size"] > stats["plain"]["tree_size"]
+
+
+def test_biased_sampling_is_deterministic(ctx, trained):
+    """The same seed gives the same tree with surrogate-biased sampling."""
+    from mpt_gb300 import planner as P
+    sc, sg, _ = trained
+    out = []
+    for _ in range(2):
+        pl = P.Planner(P.Scenario(sc), P.PRRT(P.gpu_wavefront(512)), seed=23, ctx=ctx, max_nodes=1 << 20)
+        pl.add_start(sc["start"])
+        pl.set_surrogate(sg, threshold=2.0, points=2, candidates=4)
+        pl.run(8)
+        out.append(pl.graph())
+        pl.close()
+    (s0, p0), (s1, p1) = out
+    assert len(s0) > 100 and np.array_equal(s0, s1) and np.array_equal(p0, p1)
