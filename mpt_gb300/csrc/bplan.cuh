@@ -36,11 +36,16 @@ struct BPlanJob {
     int W;                          // wavefront size (<= BPLAN_THREADS)
     int max_waves;                  // wavefronts to run (<= 0: no limit)
     int stop_when_solved;
-    uint64_t deadline_ns;           // globaltimer deadline (0: none)
+    uint64_t deadline_ns;           // time limit of the run (0: none)
+    // bucket grid of the nearest-neighbour search: gx x gy cells of size
+    // cell_size from (cell_ox, cell_oy), gx * gy <= BPLAN_CELLS
+    float cell_ox, cell_oy, cell_size, cell_inv;
+    int gx, gy;
 };
 
 #define BPLAN_THREADS 1024
 #define BPLAN_MAX_NODES 16384       // FP32 node copy in shared memory: 128 KB
+#define BPLAN_CELLS 4096            // bucket-grid cells (64 x 64 over the sampling box)
 
 // Runs njobs jobs (device array), one thread block each, on stream s.
 mptg_status bplan_launch(mptg_ctx* ctx, const BPlanJob* djobs, int njobs, int max_W, int max_cap, cudaStream_t s);

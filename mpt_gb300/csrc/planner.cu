@@ -49,6 +49,7 @@ struct mptg_planner {
     double* goal = nullptr;
     int has_goal = 0;
     std::vector<double> goal_host;
+    double lo_host[MPTG_MAX_DIM] = {0}, hi_host[MPTG_MAX_DIM] = {0};  // sampling bounds
     int* parent = nullptr;
     // wavefront buffers
     double* samp = nullptr;
@@ -150,6 +151,10 @@ struct mptg_planner {
     BPlanCounters* bp_hctr = nullptr;   // pinned
     uint8_t* bp_hgoal = nullptr;        // pinned [bp_cap]
     uint64_t stat_bp_waves = 0;         // wavefronts run inside the block planner
+    // bp_states[0, bp_n) mirrors the planner's first bp_n nodes; the kd-tree
+    // holds a prefix of them and takes the rest (bp_flush) only when
+    // something other than the block planner needs it
+    size_t bp_n = 0;
 };
 
 extern "C" mptg_status mptg_surrogate_score_dev(mptg_surrogate* s, const double* dstates, int n, float* dlogits,
@@ -643,6 +648,25 @@ static void planner_free(mptg_planner* p) {
     delete p;
 }
 
+// nodes of the planner: the kd-tree's plus those the block planner added
+// that the kd-tree has not taken yet
+static size_t planner_n(const mptg_planner* p) {
+    size_t n = 0;
+    mptg_tree_size(p->tree, &n);
+    return std::max(n, p->bp_n);
+}
+
+// the kd-tree takes the block planner's pending nodes
+static mptg_status bp_flush(mptg_planner* p) {
+    size_t n = 0;
+    mptg_tree_size(p->tree, &n);
+    if (p->bp_n <= n) return MPTG_OK;
+    mptg_status st = mptg_tree_insert(p->tree, p->bp_states + n * 2, p->bp_n - n, p->stream);
+    if (st) return st;
+    MPTG_CUDA_TRY(p->ctx, cudaStreamSynchronize(p->stream));
+    return MPTG_OK;
+}
+
 static mptg_status check_params(mptg_ctx* ctx, const mptg_scene* scene, const mptg_plan_params* prm) {
     if (prm->wavefront < 1 || prm->wavefront > (1 << 20))
         return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "wavefront must be in [1, 2^20]");
@@ -662,6 +686,10 @@ static mptg_status set_bounds(mptg_planner* p, const double* lo, const double* h
     for (int d = 0; d < D; ++d) {
         l[d] = lo ? lo[d] : (p->metric == MPTG_METRIC_SO2 ? -MPTG_PI : 0.0);
         h[d] = hi ? hi[d] : (p->metric == MPTG_METRIC_SO2 ? MPTG_PI : 1.0);
+    }
+    for (int d = 0; d < D; ++d) {
+        p->lo_host[d] = l[d];
+        p->hi_host[d] = h[d];
     }
     MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(p->lo, l, D * sizeof(double), cudaMemcpyHostToDevice, p->stream));
     MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(p->hi, h, D * sizeof(double), cudaMemcpyHostToDevice, p->stream));
@@ -685,6 +713,7 @@ static mptg_status planner_reset(mptg_planner* p, const mptg_plan_params* prm, b
     MPTG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     mptg_status st = mptg_tree_clear(p->tree, p->stream);
     if (st) return st;
+    p->bp_n = 0;
     MPTG_CUDA_TRY(ctx, cudaMemsetAsync(p->nsamp, 0, sizeof(unsigned long long), p->stream));
     if (bounds && (st = set_bounds(p, lo, hi))) return st;
     MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(p->stream));
@@ -805,6 +834,8 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
     mptg_ctx* ctx = p->ctx;
     const int W = p->prm.wavefront;
     *added = 0;
+    mptg_status st0 = bp_flush(p);
+    if (st0) return st0;
     size_t n0 = 0;
     mptg_tree_size(p->tree, &n0);
     if (n0 >= p->prm.max_nodes) return MPTG_OK;
@@ -967,8 +998,7 @@ static mptg_status run_persistent(mptg_planner* p, int max_waves, double time_li
     mptg_ctx* ctx = p->ctx;
     cudaStream_t s = p->stream;
     *waves = 0;
-    size_t n0 = 0;
-    mptg_tree_size(p->tree, &n0);
+    const size_t n0 = planner_n(p);
     const int W = p->prm.wavefront;
     const int cap = p->bp_states ? p->bp_cap : (int)std::min<size_t>(p->prm.max_nodes, BPLAN_MAX_NODES);
     if (n0 >= p->prm.max_nodes || std::min<size_t>(n0 + W, p->prm.max_nodes) > (size_t)cap) return MPTG_OK;
@@ -1008,13 +1038,28 @@ static mptg_status run_persistent(mptg_planner* p, int max_waves, double time_li
     j.max_waves = max_waves;
     j.stop_when_solved = stop_when_solved;
     j.deadline_ns = time_limit_s > 0 ? (uint64_t)(time_limit_s * 1e9) : 0;
+    {
+        // 64 x 64 cells over the sampling box (square cells on its longer side)
+        const double sx = p->hi_host[0] - p->lo_host[0], sy = p->hi_host[1] - p->lo_host[1];
+        double cs = std::max(sx, sy) / 64.0;
+        if (!(cs > 0) || !std::isfinite(cs)) cs = 1.0;
+        j.cell_size = (float)cs;
+        j.cell_inv = (float)(1.0 / cs);
+        j.cell_ox = (float)p->lo_host[0];
+        j.cell_oy = (float)p->lo_host[1];
+        j.gx = std::max(1, std::min(64, (int)std::ceil(sx / cs)));
+        j.gy = std::max(1, std::min(64, (int)std::ceil(sy / cs)));
+    }
     BPlanCounters* h = p->bp_hctr;
     *h = BPlanCounters{};
     h->n = (int)n0;
     h->wave = p->wave;
     h->goals = (int)p->goals.size();
-    mptg_status st = mptg_tree_states(p->tree, 0, n0, p->bp_states, s);
-    if (st) return st;
+    mptg_status st = MPTG_OK;
+    if (p->bp_n != n0) {  // nodes added elsewhere since the last block run: mirror the tree
+        if ((st = mptg_tree_states(p->tree, 0, n0, p->bp_states, s))) return st;
+        p->bp_n = n0;
+    }
     MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_job, &j, sizeof(j), cudaMemcpyHostToDevice, s));
     MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_ctr, h, sizeof(*h), cudaMemcpyHostToDevice, s));
     if ((st = bplan_launch(ctx, p->bp_job, 1, W, p->bp_cap, s))) return st;
@@ -1029,11 +1074,13 @@ static mptg_status run_persistent(mptg_planner* p, int max_waves, double time_li
     *waves = h->waves_run;
     if (n1 > n0) {
         const size_t k = n1 - n0;
-        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_hgoal, p->bp_goalf + n0, k, cudaMemcpyDeviceToHost, s));
-        if ((st = mptg_tree_insert(p->tree, p->bp_states + n0 * 2, k, s))) return st;
-        MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
-        for (size_t i = 0; i < k; ++i)
-            if (p->bp_hgoal[i]) p->goals.push_back((int)(n0 + i));
+        p->bp_n = n1;  // the kd-tree takes them when it is next needed (bp_flush)
+        if (h->goals > (int)p->goals.size()) {
+            MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_hgoal, p->bp_goalf + n0, k, cudaMemcpyDeviceToHost, s));
+            MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+            for (size_t i = 0; i < k; ++i)
+                if (p->bp_hgoal[i]) p->goals.push_back((int)(n0 + i));
+        }
     }
     return MPTG_OK;
 }
@@ -1132,10 +1179,12 @@ mptg_status mptg_planner_reset(mptg_planner* p, const mptg_plan_params* params) 
 
 mptg_status mptg_planner_add_start(mptg_planner* p, const double* q) {
     if (!p || !q) return MPTG_ERR_INVALID_ARG;
+    mptg_status st = bp_flush(p);
+    if (st) return st;
     size_t n = 0;
     mptg_tree_size(p->tree, &n);
     if (n >= p->prm.max_nodes) return mptg_fail(p->ctx, MPTG_ERR_CAPACITY, "node budget reached");
-    mptg_status st = mptg_tree_insert(p->tree, q, 1, p->stream);
+    st = mptg_tree_insert(p->tree, q, 1, p->stream);
     if (st) return st;
     const int minus1 = -1;
     MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(p->parent + n, &minus1, sizeof(int), cudaMemcpyHostToDevice, p->stream));
@@ -1162,8 +1211,7 @@ mptg_status mptg_planner_run(mptg_planner* p, int max_wavefronts, double time_li
                              int* solved) {
     if (!p) return MPTG_ERR_INVALID_ARG;
     mptg_ctx* ctx = p->ctx;
-    size_t n = 0;
-    mptg_tree_size(p->tree, &n);
+    size_t n = planner_n(p);
     if (n == 0) return mptg_fail(ctx, MPTG_ERR_NO_START, "there are no valid initial states");
     if (p->solving) return mptg_fail(ctx, MPTG_ERR_ALREADY_SOLVING, "already solving");
     p->solving = true;
@@ -1177,7 +1225,7 @@ mptg_status mptg_planner_run(mptg_planner* p, int max_wavefronts, double time_li
     // call once the block planner's node capacity is reached
     for (; !st && (max_wavefronts <= 0 || it < max_wavefronts); ++it) {
         if (stop_when_solved && !p->goals.empty()) break;
-        mptg_tree_size(p->tree, &n);
+        n = planner_n(p);
         if (n >= p->prm.max_nodes) break;
         double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (time_limit_s > 0 && el >= time_limit_s) break;
@@ -1193,7 +1241,8 @@ mptg_status mptg_planner_run(mptg_planner* p, int max_wavefronts, double time_li
 
 mptg_status mptg_planner_size(mptg_planner* p, size_t* n) {
     if (!p || !n) return MPTG_ERR_INVALID_ARG;
-    return mptg_tree_size(p->tree, n);
+    *n = planner_n(p);
+    return MPTG_OK;
 }
 
 mptg_status mptg_planner_goals(mptg_planner* p, size_t* n) {
@@ -1212,7 +1261,10 @@ static mptg_status planner_solution(mptg_planner* p, double* path, size_t cap, s
     if (p->goals.empty()) return MPTG_OK;
     MPTG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     double* hd = reinterpret_cast<double*>(p->hbuf + 8);  // 2 doubles of the pinned words
-    const double* states = mptg_tree_states_dev(p->tree);
+    size_t tn = 0;
+    mptg_tree_size(p->tree, &tn);
+    // the block planner's mirror holds every node when the kd-tree lags behind it
+    const double* states = p->bp_n > tn ? p->bp_states : mptg_tree_states_dev(p->tree);
     // best goal by path cost; goals are visited newest first with strict <,
     // as PRRT::bestSolution walks its push_front list (prrt.hpp:219-234)
     double best = INFINITY;
@@ -1254,18 +1306,24 @@ mptg_status mptg_planner_solution(mptg_planner* p, double* path, size_t cap, siz
 
 mptg_status mptg_planner_tree(mptg_planner* p, mptg_tree** tree) {
     if (!p || !tree) return MPTG_ERR_INVALID_ARG;
+    mptg_status st = bp_flush(p);
+    if (st) return st;
     *tree = p->tree;
     return MPTG_OK;
 }
 
 mptg_status mptg_planner_graph(mptg_planner* p, double* states, int32_t* parents, size_t cap, size_t* n) {
     if (!p || !n) return MPTG_ERR_INVALID_ARG;
-    size_t sz = 0;
-    mptg_tree_size(p->tree, &sz);
+    size_t tn = 0;
+    mptg_tree_size(p->tree, &tn);
+    const size_t sz = planner_n(p);
     *n = sz;
     if (!states && !parents) return MPTG_OK;
     if (sz > cap) return mptg_fail(p->ctx, MPTG_ERR_CAPACITY, "graph of %zu nodes does not fit %zu", sz, cap);
-    if (states) {
+    if (states && p->bp_n > tn) {  // the block planner's mirror holds every node
+        MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(states, p->bp_states, sz * 2 * sizeof(double), cudaMemcpyDefault,
+                                              p->stream));
+    } else if (states) {
         mptg_status st = mptg_tree_states(p->tree, 0, sz, states, p->stream);
         if (st) return st;
     }
@@ -1450,8 +1508,7 @@ mptg_status mptg_planner_stats(mptg_planner* p, double out[8]) {
     unsigned long long ns = 0;
     MPTG_CUDA_TRY(p->ctx, cudaMemcpyAsync(&ns, p->nsamp, sizeof(ns), cudaMemcpyDeviceToHost, p->stream));
     MPTG_CUDA_TRY(p->ctx, cudaStreamSynchronize(p->stream));
-    size_t n = 0;
-    mptg_tree_size(p->tree, &n);
+    const size_t n = planner_n(p);
     out[0] = (double)p->stat_wavefronts;
     out[1] = (double)p->stat_samples;
     out[2] = (double)p->stat_accepted;
@@ -1495,7 +1552,7 @@ static mptg_status batch_query(mptg_ctx* ctx, const mptg_query& q, const BatchCa
     st = mptg_planner_run(p, 0, q.time_limit_s, 1, &solved);
     r.solve_s = seconds_since(t);
     r.solved = solved;
-    mptg_tree_size(p->tree, &r.nodes);
+    r.nodes = planner_n(p);
     r.wavefronts = (size_t)p->stat_wavefronts;
     if (st) return st;
     return planner_solution(p, q.path, q.path_cap, &r.path_len, &r.cost, false);

@@ -431,20 +431,6 @@ __global__ void k_seg_d(SegState* __restrict__ cur, const int* __restrict__ perm
 
 // ------------------------------------------------------------------ search
 
-// Bucket contents stream through a search once per visit, while the node
-// records and cells near the root are revisited by every warp: loading the
-// buckets without allocating in L1 leaves the L1 to the nodes.
-__device__ __forceinline__ float ldg_stream(const float* p) {
-    float v;
-    asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
-    return v;
-}
-__device__ __forceinline__ int ldg_stream(const int* p) {
-    int v;
-    asm("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(v) : "l"(p));
-    return v;
-}
-
 __device__ __forceinline__ float warp_sum16(float v) {
     v += __shfl_xor_sync(0xffffffffu, v, 8);
     v += __shfl_xor_sync(0xffffffffu, v, 4);
@@ -639,10 +625,10 @@ __global__ void __launch_bounds__(256, 4) k_nearest(TreeView t, const double* __
         int pid = -1;
         if (have) {
             size_t b = (size_t)nd.y;
-            pid = ldg_stream(&t.bids[b * MPTG_BUCKET + lane]);
+            pid = __ldg(&t.bids[b * MPTG_BUCKET + lane]);
             float p[DMAX];
 #pragma unroll
-            for (int d = 0; d < DMAX; ++d) p[d] = d < D ? ldg_stream(&t.bpts[(b * D + d) * MPTG_BUCKET + lane]) : 0.f;
+            for (int d = 0; d < DMAX; ++d) p[d] = d < D ? __ldg(&t.bpts[(b * D + d) * MPTG_BUCKET + lane]) : 0.f;
             d32 = dist32<MK, DMAX>(q, p, t.w0f, t.w1f);
             if (!(d32 == d32)) d32 = INFINITY;
         }

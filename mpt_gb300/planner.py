@@ -255,6 +255,12 @@ class Planner:
         else:
             _check(self.ctx.h, self.lib.mptg_planner_add_start(self.h, q.ctypes.data))
 
+    def prepare(self):
+        """Create the device planner now -- its tree, buffers and the starts
+        added so far -- as the reference's constructor and addStart do, so
+        that the first solve does not pay for the allocations."""
+        self._create()
+
     def _create(self):
         if self.h is not None:
             return
@@ -620,7 +626,7 @@ def _cache_store(path: str, key: str, best: int, med: dict):
     os.replace(tmp, path)
 
 
-def autotune_wavefront(ctx: Context, scenario: Scenario, start, candidates=(256, 512, 1024, 2048, 4096, 8192),
+def autotune_wavefront(ctx: Context, scenario: Scenario, start, candidates=(64, 128, 256, 512, 1024, 2048, 4096, 8192),
                        trials: int = 3, time_limit: float = 2.0, seed: int = 1, max_nodes: int = 1 << 21,
                        goal_bias: float = 0.01, range_: float | None = None, cache: str | None = None):
     """Native wavefront-size autotuner (mptg_autotune_wavefront): the size with

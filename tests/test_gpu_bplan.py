@@ -103,6 +103,7 @@ def test_block_planner_solves_and_paths_revalidate(ctx, orc):
     times = []
     for seed in range(1000, 1010):
         pl = _planner(ctx, sc, 128, seed, 1 << 20, goal_bias=0.01)
+        pl.prepare()
         t0 = time.perf_counter()
         pl.solve_for(20.0, lambda: pl.solved())
         times.append(time.perf_counter() - t0)
