@@ -306,108 +306,7 @@ __device__ __noinline__ bool pair_hits64(const double* R, const double* P, const
     return tri_tri64(wt, et);
 }
 
-// True when the plane of triangle U certainly separates the points V0..V2:
-// every d_i = n.(V_i - U0), n = (U1 - U0) x (U2 - U0), lies beyond its error
-// bound with one sign.  The FP32 coordinates are within eps (per coordinate)
-// of the FP64 coordinates tri_tri64 uses, and X bounds every |coordinate|.
-// Bound (2-norms bounded by the computed L1 norms): the differences move by
-// a = 4 eps + u|.| (perturbation plus rounding), the normal by
-// nu = |e1| a2 + |e2| a1 + a1 a2 + 4u|e1||e2| (perturbation plus the cross
-// product's rounding), each d by |n| w + |w| nu + 2 nu w + 3u|n||w| (the dot
-// product's rounding), plus the FP64 test's own rounding (far below
-// 1e-13 (|e1||e2| + |n|)(X + 1)).  Then every FP64 distance in tri_tri64 has
-// the FP32 sign and none is 0, so the test returns false at this plane.
-// The three signed distances d[i] = n.(V_i - U0) and their common bound E.
-__device__ __forceinline__ float plane_dists32(const float* U, const float* V, float eps, float X, float* dv) {
-    const float e1x = U[3] - U[0], e1y = U[4] - U[1], e1z = U[5] - U[2];
-    const float e2x = U[6] - U[0], e2y = U[7] - U[1], e2z = U[8] - U[2];
-    const float nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
-    const float l1 = fabsf(e1x) + fabsf(e1y) + fabsf(e1z), l2 = fabsf(e2x) + fabsf(e2y) + fabsf(e2z);
-    const float ln = fabsf(nx) + fabsf(ny) + fabsf(nz);
-    const float a1 = 4.f * eps + U32 * l1, a2 = 4.f * eps + U32 * l2;
-    const float nu = l1 * a2 + l2 * a1 + a1 * a2 + 4.f * U32 * l1 * l2;
-    float lw = 0.f;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const float wx = V[3 * i] - U[0], wy = V[3 * i + 1] - U[1], wz = V[3 * i + 2] - U[2];
-        dv[i] = fmaf(nx, wx, fmaf(ny, wy, nz * wz));
-        lw = fmaxf(lw, fabsf(wx) + fabsf(wy) + fabsf(wz));
-    }
-    const float w = 4.f * eps + U32 * lw;
-    return ((ln + nu) * w + (lw + w) * nu + nu * w + 3.f * U32 * ln * lw +
-            1e-13f * (l1 * l2 + ln) * (X + 1.f)) * 1.01f + 1e-30f;
-}
-
-__device__ __forceinline__ bool plane_separates32(const float* U, const float* V, float eps, float X) {
-    float d[3];
-    const float E = plane_dists32(U, V, eps, X, d);
-    return fminf(d[0], fminf(d[1], d[2])) > E || fmaxf(d[0], fmaxf(d[1], d[2])) < -E;
-}
-
-// orient3d(p, q, a, b) = (q - p) . ((a - p) x (b - p)) in FP32, and in *err a
-// bound on its distance from the exact value at the FP64 coordinates (every
-// FP32 coordinate within eps of its FP64 counterpart).  Each difference is
-// off by at most dl = 2 eps + u max|.| per component (2-norm <= 2 dl); with
-// L1 norms la, lb, lc (grown by 3 dl to cover the exact vectors) the
-// perturbation moves the determinant by <= 2dl(lb lc + la lc + la lb) +
-// 4dl^2(la + lb + lc) + 8dl^3, and the FP32 cross and dot products round by
-// <= 5u la lb lc (6u taken).
-__device__ __forceinline__ float orient3d32(const float* p, const float* q, const float* a, const float* b, float eps,
-                                            float* err) {
-    const float ax = q[0] - p[0], ay = q[1] - p[1], az = q[2] - p[2];
-    const float bx = a[0] - p[0], by = a[1] - p[1], bz = a[2] - p[2];
-    const float cx = b[0] - p[0], cy = b[1] - p[1], cz = b[2] - p[2];
-    const float x = by * cz - bz * cy, y = bz * cx - bx * cz, z = bx * cy - by * cx;
-    const float det = fmaf(ax, x, fmaf(ay, y, az * z));
-    float la = fabsf(ax) + fabsf(ay) + fabsf(az), lb = fabsf(bx) + fabsf(by) + fabsf(bz);
-    float lc = fabsf(cx) + fabsf(cy) + fabsf(cz);
-    const float dl = 2.f * eps + U32 * fmaxf(la, fmaxf(lb, lc));
-    la += 3.f * dl;
-    lb += 3.f * dl;
-    lc += 3.f * dl;
-    *err = (2.f * dl * (lb * lc + la * lc + la * lb) + 4.f * dl * dl * (la + lb + lc) + 8.f * dl * dl * dl +
-            6.f * U32 * la * lb * lc) * 1.01f + 1e-30f;
-    return det;
-}
-
-// The segment PQ, whose ends lie strictly on opposite sides of triangle T's
-// plane, passes through T's interior: the three orientations of PQ against
-// T's edges are certainly nonzero and of one sign.
-__device__ __forceinline__ bool pierces32(const float* P, const float* Q, const float* T, float eps) {
-    float e0, e1, e2;
-    const float s0 = orient3d32(P, Q, T, T + 3, eps, &e0);
-    const float s1 = orient3d32(P, Q, T + 3, T + 6, eps, &e1);
-    const float s2 = orient3d32(P, Q, T + 6, T, eps, &e2);
-    return (s0 > e0 && s1 > e1 && s2 > e2) || (s0 < -e0 && s1 < -e1 && s2 < -e2);
-}
-
-// FP32 verdict on a triangle pair that Moller's FP64 test (tri_tri64) is
-// certain to share: -1 = separated (a plane separates the other triangle's
-// vertices), 1 = intersecting, 0 = undecided.
-// Intersecting: every vertex of each triangle lies beyond its bound on a
-// definite side of the other's plane, both triangles straddle the other's
-// plane, and an edge of one crossing the other's plane certainly passes
-// through the other's interior.  Then the FP64 coordinates describe
-// triangles that cross along a segment of length far above FP64 rounding:
-// the FP64 test sees the same signs, takes a non-degenerate interval branch,
-// and finds the two intervals on the planes' common line overlapping.
-__device__ __forceinline__ int tri_pair32(const float* V, const float* U, float eps, float X) {
-    float dv[3], du[3];
-    const float Ev = plane_dists32(U, V, eps, X, dv);  // V's vertices against U's plane
-    if (fminf(dv[0], fminf(dv[1], dv[2])) > Ev || fmaxf(dv[0], fmaxf(dv[1], dv[2])) < -Ev) return -1;
-    const float Eu = plane_dists32(V, U, eps, X, du);  // U's vertices against V's plane
-    if (fminf(du[0], fminf(du[1], du[2])) > Eu || fmaxf(du[0], fmaxf(du[1], du[2])) < -Eu) return -1;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-        if (!(fabsf(dv[i]) > Ev) || !(fabsf(du[i]) > Eu)) return 0;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const int j = i == 2 ? 0 : i + 1;
-        if ((dv[i] > 0.f) != (dv[j] > 0.f) && pierces32(V + 3 * i, V + 3 * j, U, eps)) return 1;
-        if ((du[i] > 0.f) != (du[j] > 0.f) && pierces32(U + 3 * i, U + 3 * j, V, eps)) return 1;
-    }
-    return 0;
-}
+#include "tri32.cuh"
 
 #define MESH_DETAIL_THREADS 128
 #define MESH_CAND 512   // environment leaves within the robot's bounding sphere
