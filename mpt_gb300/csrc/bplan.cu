@@ -41,6 +41,7 @@ struct BSmem {
     int* ni;        // [W] nearest id (-1: none)
     int* fl;        // [W] bit 0 link valid, bit 1 skipped (d == 0)
     int* head;      // [BPLAN_CELLS] first node of each bucket-grid cell (-1: empty)
+    int* ccount;    // [BPLAN_CELLS / 16] nodes in each block of 4 x 4 cells
     short* nxt;     // [cap] next node in the same cell (-1: end)
 };
 
@@ -54,13 +55,14 @@ __device__ __forceinline__ BSmem carve(unsigned char* base, int cap, int W) {
     s.ni = reinterpret_cast<int*>(base + o); o += (size_t)W * sizeof(int);
     s.fl = reinterpret_cast<int*>(base + o); o += (size_t)W * sizeof(int);
     s.head = reinterpret_cast<int*>(base + o); o += (size_t)BPLAN_CELLS * sizeof(int);
+    s.ccount = reinterpret_cast<int*>(base + o); o += (size_t)(BPLAN_CELLS / 16) * sizeof(int);
     s.nxt = reinterpret_cast<short*>(base + o);
     return s;
 }
 
 size_t smem_bytes(int cap, int W) {
     return (size_t)cap * sizeof(float2) + (size_t)W * (2 + 2 + 1) * sizeof(double) + (size_t)W * 2 * sizeof(int) +
-           (size_t)BPLAN_CELLS * sizeof(int) + (size_t)cap * sizeof(short);
+           (size_t)(BPLAN_CELLS + BPLAN_CELLS / 16) * sizeof(int) + (size_t)cap * sizeof(short);
 }
 
 // bucket-grid cell of an FP32 point (clamped to the grid: a point outside the
@@ -80,6 +82,13 @@ __device__ __forceinline__ void bucket_insert(const BPlanJob& J, const BSmem& S,
     const float2 p = S.pts[j];
     const int c = cell_of(J, p.x, p.y, &cx, &cy);
     S.nxt[j] = (short)atomicExch(&S.head[c], j);
+    atomicAdd(&S.ccount[(cy >> 2) * ((J.gx + 3) >> 2) + (cx >> 2)], 1);
+}
+
+// FP32 distance from q to the rectangle [x0, x1] x [y0, y1] (0 inside)
+__device__ __forceinline__ float rect_dist(const float* q, float x0, float x1, float y0, float y1) {
+    const float dx = fmaxf(fmaxf(x0 - q[0], q[0] - x1), 0.f), dy = fmaxf(fmaxf(y0 - q[1], q[1] - y1), 0.f);
+    return sqrtf(dx * dx + dy * dy);
 }
 
 // The nodes of one cell against the best so far: every node that could beat
@@ -125,6 +134,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
         s_cnt = 0;
     }
     for (int c = t; c < J.gx * J.gy; c += T) S.head[c] = -1;
+    for (int c = t; c < BPLAN_CELLS / 16; c += T) S.ccount[c] = 0;
     __syncthreads();
     for (int j = t; j < s_n; j += T) {
         const double x = J.states[2 * j], y = J.states[2 * j + 1];
@@ -169,38 +179,55 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
             }
         }
         __syncthreads();
-        // nearest: thread per sample, bucket-grid cells in rings of growing
-        // Chebyshev distance around the sample's cell.  A node r >= 1 rings out
-        // is at least (r - 1) cells away in one axis (less the cell-boundary
-        // fuzz), so the search ends once that bound minus E exceeds the best.
+        // nearest: thread per sample over the bucket grid, two levels: blocks
+        // of 4 x 4 cells in rings of growing Chebyshev distance around the
+        // sample's block, skipping empty blocks, then the cells of a block
+        // and their nodes.  A block or cell whose rectangle lies farther than
+        // the best (less the boundary fuzz and E) holds no node that can
+        // reach it; a block R >= 1 rings out lies at least (R - 1) blocks
+        // away, which ends the search.
         if (t < W) {
             const double* qd = S.q + 2 * t;
             const float q32[2] = {__double2float_rn(qd[0]), __double2float_rn(qd[1])};
             const float M = fmaxf(__int_as_float(s_maxabs), maxabs_ru(qd[0], qd[1]));
             const float E = err32<MPTG_METRIC_L2>(2, M, 1.f, 1.f);
-            const float fuzz = 1e-3f * J.cell_size + 1e-3f;
+            const float cs = J.cell_size, fuzz = 1e-3f * cs + 1e-3f;
+            const int bgx = (J.gx + 3) >> 2, bgy = (J.gy + 3) >> 2;
             double best = INFINITY;
             int bid = INT_MAX;
             float bup = INFINITY;
             int cx, cy;
             cell_of(J, q32[0], q32[1], &cx, &cy);
-            const int rmax = max(J.gx, J.gy);
-            for (int r = 0; r <= rmax; ++r) {
-                if (r >= 1 && (float)(r - 1) * J.cell_size - fuzz - E > bup) break;
-                if (r == 0) {
-                    scan_cell(J, S, cy * J.gx + cx, q32, qd, E, best, bid, bup);
+            const int bx = cx >> 2, by = cy >> 2;
+            const int Rmax = max(bgx, bgy);
+            auto visit_block = [&](int X, int Y) {
+                if (S.ccount[Y * bgx + X] == 0) return;
+                const float x0 = J.cell_ox + (float)(4 * X) * cs, y0 = J.cell_oy + (float)(4 * Y) * cs;
+                if (rect_dist(q32, x0, x0 + 4.f * cs, y0, y0 + 4.f * cs) - fuzz - E > bup) return;
+                for (int y = 4 * Y; y < min(4 * Y + 4, J.gy); ++y)
+                    for (int x = 4 * X; x < min(4 * X + 4, J.gx); ++x) {
+                        const int c = y * J.gx + x;
+                        if (S.head[c] < 0) continue;
+                        const float fx = J.cell_ox + (float)x * cs, fy = J.cell_oy + (float)y * cs;
+                        if (rect_dist(q32, fx, fx + cs, fy, fy + cs) - fuzz - E > bup) continue;
+                        scan_cell(J, S, c, q32, qd, E, best, bid, bup);
+                    }
+            };
+            for (int R = 0; R <= Rmax; ++R) {
+                if (R >= 1 && (float)(R - 1) * 4.f * cs - fuzz - E > bup) break;
+                if (R == 0) {
+                    visit_block(bx, by);
                     continue;
                 }
-                const int x0 = max(cx - r, 0), x1 = min(cx + r, J.gx - 1);
-                if (cy - r >= 0)
-                    for (int x = x0; x <= x1; ++x) scan_cell(J, S, (cy - r) * J.gx + x, q32, qd, E, best, bid, bup);
-                if (cy + r < J.gy)
-                    for (int x = x0; x <= x1; ++x) scan_cell(J, S, (cy + r) * J.gx + x, q32, qd, E, best, bid, bup);
-                const int y0 = max(cy - r + 1, 0), y1 = min(cy + r - 1, J.gy - 1);
-                if (cx - r >= 0)
-                    for (int y = y0; y <= y1; ++y) scan_cell(J, S, y * J.gx + cx - r, q32, qd, E, best, bid, bup);
-                if (cx + r < J.gx)
-                    for (int y = y0; y <= y1; ++y) scan_cell(J, S, y * J.gx + cx + r, q32, qd, E, best, bid, bup);
+                const int X0 = max(bx - R, 0), X1 = min(bx + R, bgx - 1);
+                if (by - R >= 0)
+                    for (int X = X0; X <= X1; ++X) visit_block(X, by - R);
+                if (by + R < bgy)
+                    for (int X = X0; X <= X1; ++X) visit_block(X, by + R);
+                for (int Y = max(by - R + 1, 0); Y <= min(by + R - 1, bgy - 1); ++Y) {
+                    if (bx - R >= 0) visit_block(bx - R, Y);
+                    if (bx + R < bgx) visit_block(bx + R, Y);
+                }
             }
             // steer (k_plan_steer)
             const int id = bid == INT_MAX ? -1 : bid;
