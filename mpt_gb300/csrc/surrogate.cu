@@ -128,6 +128,66 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
     return *reinterpret_cast<uint32_t*>(&h);
 }
 
+// The fused epilogue of 16 accumulator columns c .. c+15 of row m (v = the
+// FP32 sums), per EPI; `out` accumulates the scoring output layer.
+template <int EPI>
+__device__ __forceinline__ void sg_epilogue16(const EpiArgs& ep, size_t m, int c, const float (&v)[16], float& out) {
+    if (EPI == EPI_GRAD) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) atomicAdd(&ep.G[m * ep.ldc + c + j], v[j]);
+    } else if (EPI == EPI_BWD) {
+        const float4* zi = reinterpret_cast<const float4*>(ep.Zin + m * SG_W + c);
+        float zin[16];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float4 t = zi[j];
+            zin[4 * j] = t.x; zin[4 * j + 1] = t.y; zin[4 * j + 2] = t.z; zin[4 * j + 3] = t.w;
+        }
+        uint32_t pk[8];
+#pragma unroll
+        for (int j = 0; j < 16; j += 2) {
+            float a = v[j] * sg_dsilu(zin[j]), b = v[j + 1] * sg_dsilu(zin[j + 1]);
+            pk[j / 2] = pack_bf16x2(a, b);
+            __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162*>(&pk[j / 2]);
+            ep.dZT[(size_t)(c + j) * ep.ldt + m] = h.x;
+            ep.dZT[(size_t)(c + j + 1) * ep.ldt + m] = h.y;
+        }
+        uint4* o = reinterpret_cast<uint4*>(ep.dZ + m * SG_W + c);
+        o[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        o[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+    } else {
+        float z[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) z[j] = v[j] + __ldg(&ep.bias[c + j]);
+        if (EPI == EPI_FWD) {
+            float4* zo = reinterpret_cast<float4*>(ep.Z + m * SG_W + c);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) zo[j] = make_float4(z[4 * j], z[4 * j + 1], z[4 * j + 2], z[4 * j + 3]);
+        }
+        if (EPI == EPI_SCORE_OUT) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                out = fmaf(__bfloat162float(__float2bfloat16_rn(sg_silu(z[j]))),
+                           __bfloat162float(__float2bfloat16_rn(__ldg(&ep.w4[c + j]))), out);
+        } else {
+            uint32_t pk[8];
+#pragma unroll
+            for (int j = 0; j < 16; j += 2) pk[j / 2] = pack_bf16x2(sg_silu(z[j]), sg_silu(z[j + 1]));
+            uint4* o = reinterpret_cast<uint4*>(ep.H + m * SG_W + c);
+            o[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            o[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+            if (EPI == EPI_FWD) {
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162*>(&pk[j]);
+                    ep.HT[(size_t)(c + 2 * j) * ep.ldt + m] = h.x;
+                    ep.HT[(size_t)(c + 2 * j + 1) * ep.ldt + m] = h.y;
+                }
+            }
+        }
+    }
+}
+
 // Warp roles: warp 0 lane 0 issues the TMA loads, warp 1 lane 0 the UMMAs;
 // then all four warps run the epilogue, warp w on TMEM lanes (= tile rows)
 // 32w .. 32w + 31.  Every wait is bounded (SG_TIMEOUT_NS); a wait that runs
@@ -220,60 +280,7 @@ __global__ void __launch_bounds__(128, 1) k_sg_umma(const __grid_constant__ CUte
         for (int c = 0; c < SG_W; c += 16) {
             float v[16];
             umma::tmem_ld16(trow + c, v);
-            if (EPI == EPI_GRAD) {
-#pragma unroll
-                for (int j = 0; j < 16; ++j) atomicAdd(&ep.G[m * ep.ldc + c + j], v[j]);
-            } else if (EPI == EPI_BWD) {
-                const float4* zi = reinterpret_cast<const float4*>(ep.Zin + m * SG_W + c);
-                float zin[16];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    float4 t = zi[j];
-                    zin[4 * j] = t.x; zin[4 * j + 1] = t.y; zin[4 * j + 2] = t.z; zin[4 * j + 3] = t.w;
-                }
-                uint32_t pk[8];
-#pragma unroll
-                for (int j = 0; j < 16; j += 2) {
-                    float a = v[j] * sg_dsilu(zin[j]), b = v[j + 1] * sg_dsilu(zin[j + 1]);
-                    pk[j / 2] = pack_bf16x2(a, b);
-                    __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162*>(&pk[j / 2]);
-                    ep.dZT[(size_t)(c + j) * ep.ldt + m] = h.x;
-                    ep.dZT[(size_t)(c + j + 1) * ep.ldt + m] = h.y;
-                }
-                uint4* o = reinterpret_cast<uint4*>(ep.dZ + m * SG_W + c);
-                o[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-                o[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
-            } else {
-                float z[16];
-#pragma unroll
-                for (int j = 0; j < 16; ++j) z[j] = v[j] + __ldg(&ep.bias[c + j]);
-                if (EPI == EPI_FWD) {
-                    float4* zo = reinterpret_cast<float4*>(ep.Z + m * SG_W + c);
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) zo[j] = make_float4(z[4 * j], z[4 * j + 1], z[4 * j + 2], z[4 * j + 3]);
-                }
-                if (EPI == EPI_SCORE_OUT) {
-#pragma unroll
-                    for (int j = 0; j < 16; ++j)
-                        out = fmaf(__bfloat162float(__float2bfloat16_rn(sg_silu(z[j]))),
-                                   __bfloat162float(__float2bfloat16_rn(__ldg(&ep.w4[c + j]))), out);
-                } else {
-                    uint32_t pk[8];
-#pragma unroll
-                    for (int j = 0; j < 16; j += 2) pk[j / 2] = pack_bf16x2(sg_silu(z[j]), sg_silu(z[j + 1]));
-                    uint4* o = reinterpret_cast<uint4*>(ep.H + m * SG_W + c);
-                    o[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-                    o[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
-                    if (EPI == EPI_FWD) {
-#pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162*>(&pk[j]);
-                            ep.HT[(size_t)(c + 2 * j) * ep.ldt + m] = h.x;
-                            ep.HT[(size_t)(c + 2 * j + 1) * ep.ldt + m] = h.y;
-                        }
-                    }
-                }
-            }
+            sg_epilogue16<EPI>(ep, m, c, v, out);
         }
         if (EPI == EPI_SCORE_OUT) ep.zout[m] = out + __ldg(ep.b4);
     }
@@ -288,6 +295,163 @@ __global__ void __launch_bounds__(128, 1) k_sg_umma(const __grid_constant__ CUte
     }
     __syncthreads();
     if (warp == 0) umma::tmem_dealloc(tmem, SG_W);
+}
+
+// ------------------------------------------------------------------ persistent GEMM (K = 256)
+// C = A B^T with B the 256 x 256 weights, for every 128-row tile of A, by one
+// CTA per SM that loops over tiles (tile = blockIdx.x + i * gridDim.x):
+//   warp 0   TMA: the weights once (four 64-wide K slices, 128 KB, resident),
+//            then each tile's four A slices through a 4-stage ring
+//   warp 1   UMMA: per tile, 4 x 4 MMAs 128 x 256 x 16 into one of two TMEM
+//            accumulators (2 x 256 columns), then a commit to its `full` barrier
+//   warps 2-5 epilogue: TMEM lanes 32 (w % 4) .. +31, the fused per-row work of
+//            sg_epilogue16, then an arrive on the accumulator's `empty` barrier
+// so the epilogue of one tile overlaps the loads and UMMAs of the next.  All
+// waits are bounded as in k_sg_umma.
+#define SGP_THREADS 192
+#define SGP_B_BYTES (4 * SG_W * SG_BK * 2)   // 128 KB of resident weights
+#define SGP_SMEM (SGP_B_BYTES + SG_STAGES * SG_A_BYTES + 1024 + 256)
+
+template <int EPI>
+__global__ void __launch_bounds__(SGP_THREADS, 1) k_sg_umma_p(const __grid_constant__ CUtensorMap ta,
+                                                              const __grid_constant__ CUtensorMap tb, int ntiles,
+                                                              EpiArgs ep, int* __restrict__ err) {
+    extern __shared__ uint8_t sg_smem_raw[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t raw = umma::smem_u32(sg_smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    uint8_t* smem = sg_smem_raw + (base - raw);
+    uint8_t* sB = smem;                     // [4][256][64] bf16, swizzled
+    uint8_t* sA = smem + SGP_B_BYTES;       // [stage][128][64] bf16, swizzled
+    uint64_t* bfull = reinterpret_cast<uint64_t*>(sA + SG_STAGES * SG_A_BYTES);
+    uint64_t* afull = bfull + 1;
+    uint64_t* aempty = afull + SG_STAGES;
+    uint64_t* accfull = aempty + SG_STAGES;
+    uint64_t* accempty = accfull + 2;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(accempty + 2);
+    int* counts = reinterpret_cast<int*>(tslot + 1);  // [0] A slices loaded, [1] consumed, [2] weights loaded
+    const int my_tiles = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    if (tid == 0) {
+        umma::mbar_init(bfull, 1);
+        for (int s = 0; s < SG_STAGES; ++s) {
+            umma::mbar_init(&afull[s], 1);
+            umma::mbar_init(&aempty[s], 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            umma::mbar_init(&accfull[a], 1);
+            umma::mbar_init(&accempty[a], 128);
+        }
+        counts[0] = counts[1] = counts[2] = 0;
+        umma::fence_mbar_init();
+    }
+    if (warp == 0) {
+        umma::tmem_alloc(tslot, 2 * SG_W);
+        umma::tmem_relinquish();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint64_t deadline = umma::globaltimer_ns() + SG_TIMEOUT_NS;
+
+    if (warp == 0) {
+        if (lane == 0 && my_tiles > 0) {
+            umma::mbar_arrive_expect_tx(bfull, SGP_B_BYTES);
+            for (int kb = 0; kb < 4; ++kb) umma::tma_load_2d(sB + kb * (SG_W * SG_BK * 2), &tb, bfull, kb * SG_BK, 0);
+            counts[2] = 1;
+            int g = 0;
+            bool ok = true;
+            for (int i = 0; ok && i < my_tiles; ++i) {
+                const int m0 = ((int)blockIdx.x + i * (int)gridDim.x) * SG_TM;
+                for (int kb = 0; kb < 4; ++kb, ++g) {
+                    const int s = g % SG_STAGES;
+                    if (g >= SG_STAGES && !umma::mbar_wait(&aempty[s], ((g / SG_STAGES) - 1) & 1, deadline)) {
+                        atomicExch(err, 1);
+                        ok = false;
+                        break;
+                    }
+                    umma::mbar_arrive_expect_tx(&afull[s], SG_A_BYTES);
+                    umma::tma_load_2d(sA + s * SG_A_BYTES, &ta, &afull[s], kb * SG_BK, m0);
+                }
+            }
+            counts[0] = g;
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0 && my_tiles > 0) {
+            constexpr uint32_t idesc = umma::idesc_bf16_f32(SG_TM, SG_W);
+            bool ok = umma::mbar_wait(bfull, 0, deadline);
+            if (!ok) atomicExch(err, 2);
+            umma::fence_after_sync();
+            int g = 0;
+            for (int i = 0; ok && i < my_tiles; ++i) {
+                const int acc = i & 1;
+                if (i >= 2 && !umma::mbar_wait(&accempty[acc], ((i >> 1) - 1) & 1, deadline)) {
+                    atomicExch(err, 2);
+                    ok = false;
+                    break;
+                }
+                umma::fence_after_sync();
+                const uint32_t d = tmem + (uint32_t)(acc * SG_W);
+                for (int kb = 0; kb < 4; ++kb, ++g) {
+                    const int s = g % SG_STAGES;
+                    if (!umma::mbar_wait(&afull[s], (g / SG_STAGES) & 1, deadline)) {
+                        atomicExch(err, 2);
+                        ok = false;
+                        break;
+                    }
+                    umma::fence_after_sync();
+                    const uint32_t a0 = base + SGP_B_BYTES + s * SG_A_BYTES;
+                    const uint32_t b0 = base + kb * (SG_W * SG_BK * 2);
+#pragma unroll
+                    for (int k = 0; k < SG_BK / 16; ++k)
+                        umma::mma_bf16(d, umma::sdesc_k128(a0 + 32 * k), umma::sdesc_k128(b0 + 32 * k), idesc,
+                                       (kb | k) != 0);
+                    umma::mma_commit(&aempty[s]);
+                }
+                if (ok) umma::mma_commit(&accfull[acc]);
+            }
+            counts[1] = g;
+        }
+        __syncwarp();
+    } else {
+        // epilogue warps: lane group (warp % 4) of each accumulator
+        const int grp = warp & 3;
+        const uint32_t lane_off = (uint32_t)(grp * 32) << 16;
+        for (int i = 0; i < my_tiles; ++i) {
+            const int acc = i & 1;
+            const bool ok = umma::mbar_wait(&accfull[acc], (i >> 1) & 1, deadline);
+            __syncwarp();
+            if (!ok) {
+                if (lane == 0) atomicExch(err, 3);
+                break;
+            }
+            umma::fence_after_sync();
+            const size_t m = (size_t)(((int)blockIdx.x + i * (int)gridDim.x) * SG_TM + grp * 32 + lane);
+            const uint32_t trow = tmem + lane_off + (uint32_t)(acc * SG_W);
+            float out = 0.f;
+#pragma unroll 1
+            for (int c = 0; c < SG_W; c += 16) {
+                float v[16];
+                umma::tmem_ld16(trow + c, v);
+                sg_epilogue16<EPI>(ep, m, c, v, out);
+            }
+            if (EPI == EPI_SCORE_OUT) ep.zout[m] = out + __ldg(ep.b4);
+            umma::fence_before_sync();
+            umma::mbar_arrive(&accempty[acc]);
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    // loads issued but never consumed (a wait ran out) must land before the
+    // shared memory they write is released
+    if (tid == 0) {
+        const uint64_t drain = umma::globaltimer_ns() + SG_TIMEOUT_NS;
+        if (counts[2] && counts[1] == 0) umma::mbar_wait(bfull, 0, drain);
+        for (int g = counts[1]; g < counts[0]; ++g) umma::mbar_wait(&afull[g % SG_STAGES], (g / SG_STAGES) & 1, drain);
+    }
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, 2 * SG_W);
 }
 
 // ------------------------------------------------------------------ CUDA-core parts
@@ -531,6 +695,26 @@ static mptg_status sg_gemm(mptg_surrogate* s, const bf16* A, int rowsA, int lda,
     return MPTG_OK;
 }
 
+// C = A B^T over K = 256 for A [rowsA][256] (rowsA a multiple of 128) and the
+// weights B [256][256]: the persistent kernel, one CTA per SM at most
+template <int EPI>
+static mptg_status sg_gemm_p(mptg_surrogate* s, const bf16* A, int rowsA, const bf16* B, const EpiArgs& ep,
+                             cudaStream_t st) {
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        cudaFuncSetAttribute(k_sg_umma_p<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, SGP_SMEM);
+    });
+    CUtensorMap ta, tb;
+    if (!bf16_map(&ta, A, (uint64_t)rowsA, SG_W, SG_W, SG_TM) || !bf16_map(&tb, B, SG_W, SG_W, SG_W, SG_W))
+        return mptg_fail(s->ctx, MPTG_ERR_CUDA, "surrogate GEMM: cuTensorMapEncodeTiled failed");
+    const int tiles = rowsA / SG_TM;
+    const int grid = std::min(tiles, std::max(1, s->ctx->sms));
+    k_sg_umma_p<EPI><<<grid, SGP_THREADS, SGP_SMEM, st>>>(ta, tb, tiles, ep, s->err);
+    MPTG_LAUNCHED(s->ctx);
+    MPTG_CUDA_TRY(s->ctx, cudaGetLastError());
+    return MPTG_OK;
+}
+
 // reads and clears the device error word (synchronises the stream)
 static mptg_status sg_check(mptg_surrogate* s, cudaStream_t st) {
     int e = 0;
@@ -564,15 +748,15 @@ static mptg_status sg_forward(mptg_surrogate* s, int M, bool train, cudaStream_t
             ep.Z = s->Z + l * MW;
             ep.H = s->H + l * MW;
             ep.HT = s->HT + l * MW;
-            r = sg_gemm<EPI_FWD>(s, A, M, SG_W, B, SG_W, SG_W, SG_W / SG_BK, ep, st);
+            r = sg_gemm_p<EPI_FWD>(s, A, M, B, ep, st);
         } else if (l < 3) {
             ep.H = s->H + l * MW;
-            r = sg_gemm<EPI_SCORE>(s, A, M, SG_W, B, SG_W, SG_W, SG_W / SG_BK, ep, st);
+            r = sg_gemm_p<EPI_SCORE>(s, A, M, B, ep, st);
         } else {
             ep.w4 = s->P + L.w4;
             ep.b4 = s->P + L.b4;
             ep.zout = s->zout;
-            r = sg_gemm<EPI_SCORE_OUT>(s, A, M, SG_W, B, SG_W, SG_W, SG_W / SG_BK, ep, st);
+            r = sg_gemm_p<EPI_SCORE_OUT>(s, A, M, B, ep, st);
         }
         if (r) return r;
     }
@@ -758,8 +942,7 @@ mptg_status mptg_surrogate_train_step(mptg_surrogate* s, const double* states, c
         // the GEMM reads dZ/dZT of layer l while writing layer l-1's into the same
         // buffers: stage through dH
         MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(s->dH, s->dZ, MW * sizeof(bf16), cudaMemcpyDeviceToDevice, st));
-        if ((r = sg_gemm<EPI_BWD>(s, (const bf16*)s->dH, M, SG_W, s->WTb + (size_t)(l - 1) * SG_W * SG_W, SG_W, SG_W,
-                                  SG_W / SG_BK, eb, st)))
+        if ((r = sg_gemm_p<EPI_BWD>(s, (const bf16*)s->dH, M, s->WTb + (size_t)(l - 1) * SG_W * SG_W, eb, st)))
             return r;
     }
     // layer 0

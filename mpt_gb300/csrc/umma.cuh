@@ -38,6 +38,11 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
                  : "memory");
 }
 
+// a plain arrive (count 1) by this thread
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 // Wait for the phase with the given parity to complete.  Bounded: returns
 // false once the wall-clock deadline (globaltimer, ns) has passed, so a
 // kernel never spins for ever on a barrier that will not complete.
