@@ -451,7 +451,7 @@ LEARNED_MODES = (("plain", 0, 1), ("learned_new_state", 1, 1), ("learned_edge_4p
                  ("learned_biased_x4", 1, 4))
 
 
-def learned_vs_plain(ctx, m, torch, seeds=20, cap_s=20.0, n_train=1 << 22, epochs=10, wavefront_tuned=None):
+def learned_vs_plain(ctx, m, torch, seeds=50, cap_s=20.0, n_train=1 << 22, epochs=10, wavefront_tuned=None):
     """Learned collision surrogate on the SE(3) scene: training throughput, held-out
     FP/FN rates, scoring throughput against the bf16 tensor peak, and time to
     solve versus the plain planner on the same seeds: culling by the new state's
