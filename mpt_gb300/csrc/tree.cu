@@ -444,12 +444,6 @@ __device__ __forceinline__ float so2_w32(float x) {
     return fminf(x, TWO_PI_F - x);
 }
 
-// dimension term of the SO(2)^n cell bound: the wrapped distance from q to
-// the interval [lo, hi] (0 inside)
-__device__ __forceinline__ float so2_term(float q, float lo, float hi) {
-    return (q < lo || q > hi) ? fminf(so2_w32(q - lo), so2_w32(q - hi)) : 0.f;
-}
-
 // lower bound of the distance from the query to a cell whose interval on
 // dimension d is [lo, hi] in lane d (lanes >= D ignored)
 template <int MK>
@@ -574,17 +568,6 @@ __global__ void __launch_bounds__(256, 4) k_nearest(TreeView t, const double* __
     float bestf_up = INFINITY;
     unsigned long long n_int = 0, n_leaf = 0, n_pts = 0, n_rr = 0;
 
-    // SO(2)^n cell bounds are sums of per-dimension terms, and a child's cell
-    // differs from its parent's in one dimension: its bound is the parent's
-    // plus that term's change, one shuffle from the split dimension's lane
-    // instead of a warp reduction.  Each such update rounds twice below the
-    // largest possible bound pi (D + 1), and a path has at most
-    // MPTG_MAX_DEPTH of them, so the cell tests take that much more slack.
-    constexpr bool INC = MK == MPTG_METRIC_SO2;
-    float Ec = E;
-    if constexpr (INC) Ec = __fadd_ru(E, (float)(MPTG_MAX_DEPTH + 1) * 2.f * U32 * PI_F * (float)(D + 1));
-    float oc = 0.f, lbc = 0.f;  // this lane's term of the current cell; the current cell's bound
-
     int sp = 0;
     int s0n = 0, s1n = 0;
     float s0l = 0.f, s1l = 0.f;
@@ -597,10 +580,6 @@ __global__ void __launch_bounds__(256, 4) k_nearest(TreeView t, const double* __
     int4 nd = __ldg(&t.nodes[0]);
     float clo = 0.f, chi = 0.f;
     if (lane < D) { clo = __ldg(&t.cell_lo[lane]); chi = __ldg(&t.cell_hi[lane]); }
-    if constexpr (INC) {
-        oc = so2_term(myq, clo, chi);
-        lbc = warp_sum16(oc);
-    }
     while (true) {
         if (nd.x >= 0) {
             ++n_int;
@@ -609,29 +588,15 @@ __global__ void __launch_bounds__(256, 4) k_nearest(TreeView t, const double* __
             const float split = __int_as_float(nd.z);
             const float qv = __shfl_sync(0xffffffffu, myq, s);
             const bool goLeft = qv < split;
-            float lb;
-            if constexpr (INC) {
-                float dfar = 0.f, dnear = 0.f;
-                if (lane == s) {
-                    const float ofar = goLeft ? so2_term(myq, split, chi) : so2_term(myq, clo, split);
-                    const float onear = goLeft ? so2_term(myq, clo, split) : so2_term(myq, split, chi);
-                    dfar = ofar - oc;
-                    dnear = onear - oc;
-                    oc = onear;
-                }
-                lb = lbc + __shfl_sync(0xffffffffu, dfar, s);
-                lbc = lbc + __shfl_sync(0xffffffffu, dnear, s);
-            } else {
-                float flo = clo, fhi = chi;
-                if (lane == s) {
-                    if (goLeft) flo = split;
-                    else fhi = split;
-                }
-                lb = cell_lb_vals<MK>(t, myq, flo, fhi, lane);
+            float flo = clo, fhi = chi;
+            if (lane == s) {
+                if (goLeft) flo = split;
+                else fhi = split;
             }
+            float lb = cell_lb_vals<MK>(t, myq, flo, fhi, lane);
             const int farc = goLeft ? c + 1 : c;
             // the builder keeps depth <= MPTG_MAX_DEPTH < 64, so the stack never fills
-            if (__fsub_rd(lb, Ec) <= bestf_up && sp < 64) {
+            if (__fsub_rd(lb, E) <= bestf_up && sp < 64) {
                 if (sp < 32) {
                     if (lane == sp) { s0n = farc; s0l = lb; }
                 } else {
@@ -670,7 +635,6 @@ __global__ void __launch_bounds__(256, 4) k_nearest(TreeView t, const double* __
         rerank_step(t, qd, lane, have, pid, d32, E, best, bidx, bestf_up, n_rr);
         // pop the next far child whose bound can still beat the best
         bool found = false;
-        float lbp = 0.f;
         while (sp > 0) {
             --sp;
             int src = sp & 31;
@@ -678,17 +642,13 @@ __global__ void __launch_bounds__(256, 4) k_nearest(TreeView t, const double* __
             float lb;
             if (sp < 32) { nn = __shfl_sync(0xffffffffu, s0n, src); lb = __shfl_sync(0xffffffffu, s0l, src); }
             else { nn = __shfl_sync(0xffffffffu, s1n, src); lb = __shfl_sync(0xffffffffu, s1l, src); }
-            if (__fsub_rd(lb, Ec) <= bestf_up) { node = nn; lbp = lb; found = true; break; }
+            if (__fsub_rd(lb, E) <= bestf_up) { node = nn; found = true; break; }
         }
         if (!found) break;
         nd = __ldg(&t.nodes[node]);
         if (lane < D) {
             clo = __ldg(&t.cell_lo[(size_t)node * D + lane]);
             chi = __ldg(&t.cell_hi[(size_t)node * D + lane]);
-        }
-        if constexpr (INC) {
-            oc = so2_term(myq, clo, chi);
-            lbc = lbp;
         }
     }
     if (lane == 0) {
