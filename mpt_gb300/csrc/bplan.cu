@@ -48,7 +48,8 @@ struct BSmem {
 __device__ __forceinline__ BSmem carve(unsigned char* base, int cap, int W) {
     BSmem s;
     size_t o = 0;
-    s.pts = reinterpret_cast<float2*>(base + o); o += (size_t)cap * sizeof(float2);
+    // the node copy is padded to 16 bytes: the link phase reads q as float4
+    s.pts = reinterpret_cast<float2*>(base + o); o += (size_t)((cap + 1) & ~1) * sizeof(float2);
     s.q = reinterpret_cast<double*>(base + o); o += (size_t)W * 2 * sizeof(double);
     s.nw = reinterpret_cast<double*>(base + o); o += (size_t)W * 2 * sizeof(double);
     s.nd = reinterpret_cast<double*>(base + o); o += (size_t)W * sizeof(double);
@@ -61,7 +62,7 @@ __device__ __forceinline__ BSmem carve(unsigned char* base, int cap, int W) {
 }
 
 size_t smem_bytes(int cap, int W) {
-    return (size_t)cap * sizeof(float2) + (size_t)W * (2 + 2 + 1) * sizeof(double) + (size_t)W * 2 * sizeof(int) +
+    return (size_t)((cap + 1) & ~1) * sizeof(float2) + (size_t)W * (2 + 2 + 1) * sizeof(double) + (size_t)W * 2 * sizeof(int) +
            (size_t)(BPLAN_CELLS + BPLAN_CELLS / 16) * sizeof(int) + (size_t)cap * sizeof(short);
 }
 
@@ -145,6 +146,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
     uint32_t wave = J.ctr->wave;
     int waves_run = 0, status = BPLAN_DONE;
     unsigned long long samples = 0, accepted = 0;
+    unsigned long long cyc0 = 0, cyc1 = 0, cyc2 = 0, tc = 0;  // phase cycles, kept by thread 0
     const uint64_t t0 = umma::globaltimer_ns();
     __syncthreads();
     for (;;) {
@@ -164,6 +166,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
             status = s_stop == 2 ? BPLAN_FULL : BPLAN_DONE;
             break;
         }
+        if (t == 0) tc = clock64();
         const int n = s_n;
         // goal sample: the lowest index whose bias draw hits (k_plan_goalpick)
         const bool bias_on = s_goals == 0 && J.has_goal && J.goal_bias > 0;
@@ -246,35 +249,56 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
             S.fl[t] = skip ? 2 : 0;
         }
         __syncthreads();
-        // link(near, new): warp per edge, k_grid_edges_a then k_grid_edges_b
-        for (int e = warp; e < W; e += nwarps) {
-            const bool skip = (S.fl[e] & 2) != 0;
-            const double* Bp = S.nw + 2 * e;
-            const double B[2] = {Bp[0], Bp[1]};
+        if (t == 0) {
+            const unsigned long long c = clock64();
+            cyc0 += c - tc;
+            tc = c;
+        }
+        // link(near, new), as k_grid_edges_a / k_grid_edges_b: phase A thread
+        // per edge (the end state, the step count and the FP32 set-up of the
+        // interior samples, all the FP64 work of an edge), phase B warp per
+        // edge with interior samples (FP32 per sample, FP64 only when unsure).
+        // Phase A's set-up replaces the edge's sample (S.q: a32, dir32) and
+        // nearest distance (S.nd: eps, steps), which are not needed again.
+        if (t < W) {
+            const bool skip = (S.fl[t] & 2) != 0;
+            const double B[2] = {S.nw[2 * t], S.nw[2 * t + 1]};
             double A[2];
             if (skip) {
-                A[0] = S.q[2 * e];
-                A[1] = S.q[2 * e + 1];
+                A[0] = S.q[2 * t];
+                A[1] = S.q[2 * t + 1];
             } else {
-                const int id = S.ni[e];
+                const int id = S.ni[t];
                 A[0] = J.states[2 * id];
                 A[1] = J.states[2 * id + 1];
             }
-            unsigned long long cnt = 1;
             bool ok = grid_valid_f(J.scene, B);
             long long steps = ok ? grid_edge_steps(A, B, J.inv_step) : 0;
             if (steps < 0) ok = false;
+            float4 setup = make_float4(0.f, 0.f, 0.f, 0.f);
+            float eps = 0.f;
             if (ok && steps >= 2) {
-                float a32[2], dir32[2];
-                for (int d = 0; d < 2; ++d) {
-                    a32[d] = __double2float_rn(A[d]);
-                    dir32[d] = __double2float_rn(__dsub_rn(B[d], A[d]));
-                }
-                const float eps =
-                    8.f * U32 * (fabsf(a32[0]) + fabsf(a32[1]) + fabsf(dir32[0]) + fabsf(dir32[1]) + 1.f);
-                const int Mi = (int)steps - 1;
+                setup = make_float4(__double2float_rn(A[0]), __double2float_rn(A[1]),
+                                    __double2float_rn(__dsub_rn(B[0], A[0])), __double2float_rn(__dsub_rn(B[1], A[1])));
+                eps = 8.f * U32 * (fabsf(setup.x) + fabsf(setup.y) + fabsf(setup.z) + fabsf(setup.w) + 1.f);
+            } else {
+                steps = 0;
+            }
+            reinterpret_cast<float4*>(S.q)[t] = setup;
+            reinterpret_cast<float2*>(S.nd)[t] = make_float2(eps, __int_as_float((int)steps));
+            if (ok) S.fl[t] |= 1;
+        }
+        __syncthreads();
+        for (int e = warp; e < W; e += nwarps) {
+            const float2 es = reinterpret_cast<const float2*>(S.nd)[e];
+            const int steps = __float_as_int(es.y);
+            unsigned long long cnt = 1;
+            if (steps >= 2) {
+                const float4 su = reinterpret_cast<const float4*>(S.q)[e];
+                const float eps = es.x;
+                const int Mi = steps - 1;
                 const int R = (Mi + 31) / 32;
-                const double delta = __ddiv_rn(1.0, (double)steps);
+                bool ok = true;
                 unsigned long long lc = 0;
                 for (int r = 0; ok && r < R; ++r) {
                     const int k = 1 + lane * R + r;
@@ -282,10 +306,14 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
                     if (k <= Mi) {
                         ++lc;
                         const float tt = (float)k / (float)steps;
-                        const int res = grid_valid32(J.scene, fmaf(dir32[0], tt, a32[0]), fmaf(dir32[1], tt, a32[1]), eps);
+                        const int res = grid_valid32(J.scene, fmaf(su.z, tt, su.x), fmaf(su.w, tt, su.y), eps);
                         if (res == VF_UNSURE) {
+                            // the exact FP64 sample, as the CPU checker computes it
+                            const int id = S.ni[e];
+                            const double A[2] = {J.states[2 * id], J.states[2 * id + 1]};
+                            const double B[2] = {S.nw[2 * e], S.nw[2 * e + 1]};
                             double qs[2];
-                            interp64(MPTG_METRIC_L2, 2, A, B, __dmul_rn((double)k, delta), qs);
+                            interp64(MPTG_METRIC_L2, 2, A, B, __dmul_rn((double)k, __ddiv_rn(1.0, (double)steps)), qs);
                             v = grid_valid64(J.scene, qs);
                         } else {
                             v = res == VF_VALID;
@@ -295,13 +323,16 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
                 }
                 for (int o = 16; o > 0; o >>= 1) lc += __shfl_xor_sync(0xffffffffu, lc, o);
                 cnt += lc;
+                if (lane == 0 && !ok) S.fl[e] &= ~1;
             }
-            if (lane == 0) {
-                if (ok) S.fl[e] |= 1;
-                if (J.nsamp) atomicAdd(&s_cnt, cnt);
-            }
+            if (lane == 0 && J.nsamp) atomicAdd(&s_cnt, cnt);
         }
         __syncthreads();
+        if (t == 0) {
+            const unsigned long long c = clock64();
+            cyc1 += c - tc;
+            tc = c;
+        }
         // accepted samples in sample order (k_plan_scan / k_plan_scatter)
         const int f = (t < W && S.fl[t] == 1) ? 1 : 0;
         const unsigned m = __ballot_sync(0xffffffffu, f);
@@ -346,6 +377,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
         ++waves_run;
         ++wave;
         __syncthreads();
+        if (t == 0) cyc2 += clock64() - tc;
     }
     if (t == 0) {
         J.ctr->n = s_n;
@@ -356,6 +388,9 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
         J.ctr->waves_run = waves_run;
         J.ctr->samples = samples;
         J.ctr->accepted = accepted;
+        J.ctr->cyc[0] = cyc0;
+        J.ctr->cyc[1] = cyc1;
+        J.ctr->cyc[2] = cyc2;
         if (J.nsamp) atomicAdd(J.nsamp, s_cnt);
     }
 }

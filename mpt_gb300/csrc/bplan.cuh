@@ -12,6 +12,7 @@ struct BPlanCounters {
     int waves_run;                  // wavefronts this run completed
     unsigned long long samples;     // samples drawn by this run
     unsigned long long accepted;    // nodes added by this run
+    unsigned long long cyc[3];      // SM cycles in sample + nearest + steer, link, insert (this run)
 };
 
 enum { BPLAN_DONE = 0, BPLAN_FULL = 1 };  // FULL: the next wavefront could overflow the block's node capacity

@@ -986,6 +986,23 @@ static mptg_status plan_wavefront(mptg_planner* p, cudaStream_t s, int* added) {
     return MPTG_OK;
 }
 
+// the block planner's buffers (node capacity min(max_nodes, BPLAN_MAX_NODES))
+static mptg_status bp_alloc(mptg_planner* p) {
+    const int cap = (int)std::min<size_t>(p->prm.max_nodes, BPLAN_MAX_NODES);
+    cudaError_t e = cudaMalloc((void**)&p->bp_states, (size_t)cap * 2 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&p->bp_goalf, cap);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&p->bp_ctr, sizeof(BPlanCounters));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&p->bp_job, sizeof(BPlanJob));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&p->bp_hctr, sizeof(BPlanCounters));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&p->bp_hgoal, cap);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return mptg_fail(p->ctx, MPTG_ERR_OOM, "block planner buffers: %s", cudaGetErrorString(e));
+    }
+    p->bp_cap = cap;
+    return MPTG_OK;
+}
+
 static bool bp_applies(const mptg_planner* p) {
     return p->bp_mode && !p->star && !p->sg && bplan_supported(p->scene, p->prm.wavefront, p->prm.resolution);
 }
@@ -998,23 +1015,12 @@ static mptg_status run_persistent(mptg_planner* p, int max_waves, double time_li
     mptg_ctx* ctx = p->ctx;
     cudaStream_t s = p->stream;
     *waves = 0;
+    mptg_status st0 = MPTG_OK;
     const size_t n0 = planner_n(p);
     const int W = p->prm.wavefront;
     const int cap = p->bp_states ? p->bp_cap : (int)std::min<size_t>(p->prm.max_nodes, BPLAN_MAX_NODES);
     if (n0 >= p->prm.max_nodes || std::min<size_t>(n0 + W, p->prm.max_nodes) > (size_t)cap) return MPTG_OK;
-    if (!p->bp_states) {
-        cudaError_t e = cudaMalloc((void**)&p->bp_states, (size_t)cap * 2 * sizeof(double));
-        if (e == cudaSuccess) e = cudaMalloc((void**)&p->bp_goalf, cap);
-        if (e == cudaSuccess) e = cudaMalloc((void**)&p->bp_ctr, sizeof(BPlanCounters));
-        if (e == cudaSuccess) e = cudaMalloc((void**)&p->bp_job, sizeof(BPlanJob));
-        if (e == cudaSuccess) e = cudaMallocHost((void**)&p->bp_hctr, sizeof(BPlanCounters));
-        if (e == cudaSuccess) e = cudaMallocHost((void**)&p->bp_hgoal, cap);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            return mptg_fail(ctx, MPTG_ERR_OOM, "block planner buffers: %s", cudaGetErrorString(e));
-        }
-        p->bp_cap = cap;
-    }
+    if (!p->bp_states && (st0 = bp_alloc(p))) return st0;
     const PlanView v = plan_view(p);
     BPlanJob j{};
     j.scene = scene_view(p->scene);
@@ -1062,9 +1068,23 @@ static mptg_status run_persistent(mptg_planner* p, int max_waves, double time_li
     }
     MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_job, &j, sizeof(j), cudaMemcpyHostToDevice, s));
     MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_ctr, h, sizeof(*h), cudaMemcpyHostToDevice, s));
+    MPTG_CUDA_TRY(ctx, cudaEventRecord(p->ev[0], s));
     if ((st = bplan_launch(ctx, p->bp_job, 1, W, p->bp_cap, s))) return st;
+    MPTG_CUDA_TRY(ctx, cudaEventRecord(p->ev[1], s));
     MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(h, p->bp_ctr, sizeof(*h), cudaMemcpyDeviceToHost, s));
     MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    {
+        // the phase timers (nearest, valid motion, insert) share the block's
+        // time in proportion to the SM cycles it spent in each phase
+        float ms = 0.f;
+        MPTG_CUDA_TRY(ctx, cudaEventElapsedTime(&ms, p->ev[0], p->ev[1]));
+        const double tot = (double)(h->cyc[0] + h->cyc[1] + h->cyc[2]);
+        if (tot > 0) {
+            p->t_phase[0] += 1e-3 * ms * (double)h->cyc[0] / tot;
+            p->t_phase[2] += 1e-3 * ms * (double)h->cyc[1] / tot;
+            p->t_phase[3] += 1e-3 * ms * (double)h->cyc[2] / tot;
+        }
+    }
     const size_t n1 = (size_t)h->n;
     p->wave = h->wave;
     p->stat_samples += h->samples;
@@ -1156,6 +1176,11 @@ mptg_status mptg_planner_create(mptg_ctx* ctx, mptg_scene* scene, const mptg_pla
         return mptg_fail(ctx, MPTG_ERR_OOM, "planner allocation failed: %s", cudaGetErrorString(e));
     }
     if ((st = set_bounds(p, lo, hi))) { planner_free(p); return st; }
+    // grid planners run on the block planner: its buffers now, not in the first solve
+    if (bplan_supported(scene, prm->wavefront, prm->resolution) && (st = bp_alloc(p))) {
+        planner_free(p);
+        return st;
+    }
     e = cudaMemsetAsync(p->nsamp, 0, sizeof(unsigned long long), p->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
     if (e != cudaSuccess) {

@@ -141,7 +141,6 @@ def test_phase_timers_and_wavefront_autotuner(ctx):
     from mpt_gb300 import planner as P
     sc = scenes.grid_scene()
     pl = _planner(ctx, sc, 512, 3, 200000)
-    pl.set_persistent(False)  # the phase timers time the multi-kernel wavefront's phases
     pl.solve_for(20.0, lambda: pl.solved())
     t = pl.timers()
     st = pl.stats()
