@@ -116,16 +116,24 @@ int build_rec(const std::vector<double>& tris, std::vector<int>& idx, int start,
 
 // ------------------------------------------------------------------ device helpers
 
-__device__ __forceinline__ void quat_mat64(const double* q, double* R) {
-    // same expression order as the CPU checker (oracle.c quat_to_mat)
-    double x = q[0], y = q[1], z = q[2], w = q[3];
-    double tx = __dmul_rn(2.0, x), ty = __dmul_rn(2.0, y), tz = __dmul_rn(2.0, z);
-    double twx = __dmul_rn(tx, w), twy = __dmul_rn(ty, w), twz = __dmul_rn(tz, w);
-    double txx = __dmul_rn(tx, x), txy = __dmul_rn(ty, x), txz = __dmul_rn(tz, x);
-    double tyy = __dmul_rn(ty, y), tyz = __dmul_rn(tz, y), tzz = __dmul_rn(tz, z);
-    R[0] = __dsub_rn(1.0, __dadd_rn(tyy, tzz)); R[1] = __dsub_rn(txy, twz); R[2] = __dadd_rn(txz, twy);
-    R[3] = __dadd_rn(txy, twz); R[4] = __dsub_rn(1.0, __dadd_rn(txx, tzz)); R[5] = __dsub_rn(tyz, twx);
-    R[6] = __dsub_rn(txz, twy); R[7] = __dadd_rn(tyz, twx); R[8] = __dsub_rn(1.0, __dadd_rn(txx, tyy));
+
+// Entry k (row-major) of the rotation matrix of the unit quaternion
+// (x, y, z, w), with the CPU checker's expressions (oracle.c quat_to_mat):
+// products p1 = (2a) b and p2 = (2c) d of quaternion components (t_a = 2a
+// first, then t_a b), the diagonal 1 - (p1 + p2), the rest p1 + p2 or
+// p1 - p2 (= p1 + (-p2) exactly).  One instruction sequence for every k, so
+// that nine lanes compute the nine entries together; the operand indices
+// a, b, c, d into (x, y, z, w) are packed two bits per k.
+__device__ __forceinline__ double quat_entry64(const double* q, int k) {
+    const double x = q[0], y = q[1], z = q[2], w = q[3];
+    auto pick = [&](unsigned table) {
+        const unsigned i = (table >> (2 * k)) & 3u;
+        return i == 0 ? x : i == 1 ? y : i == 2 ? z : w;
+    };
+    const double p1 = __dmul_rn(__dmul_rn(2.0, pick(0xa865u)), pick(0x4401u));
+    const double p2 = __dmul_rn(__dmul_rn(2.0, pick(0x1129au)), pick(0x1fefeu));
+    const double sum = __dadd_rn(p1, (0x62u >> k) & 1u ? -p2 : p2);
+    return (0x111u >> k) & 1u ? __dsub_rn(1.0, sum) : sum;
 }
 
 __device__ __forceinline__ void xform64(const double* R, const double* p, const double* v, double* o) {
@@ -419,15 +427,34 @@ __global__ void __launch_bounds__(MESH_DETAIL_THREADS, 8) k_mesh_detail(MeshView
     const int tid = threadIdx.x;
     __shared__ int dead;
     const double* s = q + (size_t)i * D;
+    // one read of the edge's result for the whole block (other blocks may
+    // clear it at any time, so per-thread reads could disagree)
+    if (tid == 0) dead = sample_edge && __ldcg(&edge_out[sample_edge[i]]) == 0;
+    __syncthreads();
+    if (dead) {  // block-uniform
+        if (tid == 0) out[i] = 0;
+        return;
+    }
+    // the pose: lanes 0-8 the rotation entries, lanes 9-11 the position (an
+    // FP64 instruction costs the FP64 pipe the same for one active lane as
+    // for 32, so the entries are computed side by side, not by one thread)
+    if (tid < 12) {
+        double v;
+        if (tid < 9) {
+            v = quat_entry64(s, tid);
+            R[tid] = v;
+        } else {
+            v = s[4 + tid - 9];
+            P[tid - 9] = v;
+        }
+        const float f = (float)v;
+        if (tid < 9) R32[tid] = f;
+        else P32[tid - 9] = f;
+    }
+    __syncwarp();
     if (tid == 0) {
-        // one read of the edge's result for the whole block (other blocks may
-        // clear it at any time, so per-thread reads could disagree)
-        dead = sample_edge && __ldcg(&edge_out[sample_edge[i]]) == 0;
-        quat_mat64(s, R);
-        P[0] = s[4]; P[1] = s[5]; P[2] = s[6];
-        for (int k = 0; k < 9; ++k) R32[k] = (float)R[k];
         float pm = 0.f;
-        for (int k = 0; k < 3; ++k) { P32[k] = (float)P[k]; pm = fmaxf(pm, fabsf(P32[k])); }
+        for (int k = 0; k < 3; ++k) pm = fmaxf(pm, fabsf(P32[k]));
         pm = pm * (1.f + 2.f * U32);
         // FP32 world vertex fma(R, v, P) against xform64: <= u(5|v|_1 + 4|P|);
         // FP32 environment coordinates: <= u |x|
@@ -442,10 +469,6 @@ __global__ void __launch_bounds__(MESH_DETAIL_THREADS, 8) k_mesh_detail(MeshView
         hit = 0;
     }
     __syncthreads();
-    if (dead) {  // block-uniform
-        if (tid == 0) out[i] = 0;
-        return;
-    }
     const float eps = eps_s, X = X_s;
     // 1. candidates: environment leaves within the bounding sphere (center p,
     //    radius reach plus a margin far above FP32 rounding)
