@@ -376,21 +376,39 @@ def reference_planners(runs=None):
     out = {"kind": "reference (the reference's planners compiled from its headers; NN and collision stand-ins)",
            "host_cores": os.cpu_count()}
     for name, mk, _ in SOLVE_SCENES:
-        sc = getattr(scenes, mk)()
         per = {}
         for algo, cfgs in runs.get(name, {}).items():
             for threads, nseeds, cap in cfgs:
-                rows = [ref.plan_solve(sc, 1000 + s_, algo=algo, threads=threads, time_limit_s=cap)
-                        for s_ in range(nseeds)]
+                key = "%s_%s" % (algo, "1_core" if threads == 1 else "all_cores")
+                _progress("reference %s %s" % (name, key))
+                # each configuration in a child process: a crash inside the
+                # reference's code is recorded, not fatal to the bench
+                p = subprocess.run([sys.executable, os.path.abspath(__file__), "--ref-plan-child", mk, algo,
+                                    str(threads), str(nseeds), str(cap)], capture_output=True, text=True,
+                                   timeout=nseeds * (cap + 30) + 120)
+                rows = [json.loads(l_) for l_ in p.stdout.splitlines() if l_.startswith("{")]
                 t = sorted(r_["solve_s"] if r_["solved"] else cap for r_ in rows)
                 solved = [r_ for r_ in rows if r_["solved"]]
-                key = "%s_%s" % (algo, "1_core" if threads == 1 else "all_cores")
                 per[key] = {"threads": threads or os.cpu_count(), "seeds": nseeds, "cap_s": cap, "solved": len(solved),
-                            "p50_s": statistics.median(t), "max_s": t[-1],
+                            "p50_s": statistics.median(t) if t else None, "max_s": t[-1] if t else None,
                             "median_cost": statistics.median([r_["cost"] for r_ in solved]) if solved else None,
                             "median_nodes": statistics.median([r_["nodes"] for r_ in solved]) if solved else None}
+                if p.returncode != 0 or len(rows) < nseeds:
+                    per[key]["incomplete"] = {"seeds_finished": len(rows), "returncode": p.returncode,
+                                              "stderr_tail": p.stderr[-200:]}
         out[name] = per
     return out
+
+
+def _ref_plan_child(mk, algo, threads, nseeds, cap):
+    """Child process of reference_planners: one JSON line per seed."""
+    from oracle import ref
+    from mpt_gb300 import scenes
+    sc = getattr(scenes, mk)()
+    for s_ in range(nseeds):
+        r_ = ref.plan_solve(sc, 1000 + s_, algo=algo, threads=threads, time_limit_s=cap)
+        print(json.dumps({"seed": 1000 + s_, "solved": r_["solved"], "solve_s": r_["solve_s"], "cost": r_["cost"],
+                          "nodes": r_["nodes"]}), flush=True)
 
 
 def _labelled_mesh_states(m, ctx, sc, n, seed):
@@ -941,7 +959,12 @@ def main():
     ap.add_argument("--edges-only", action="store_true", help="edge checks/s of the three scenes only (profiling)")
     ap.add_argument("--solve-only", action="store_true", help="time to solve of the three scenes only (profiling)")
     ap.add_argument("--solve-seeds", type=int, default=None, help="seeds per scene (default grid 20, arm 10, SE(3) 20)")
+    ap.add_argument("--ref-plan-child", nargs=5, default=None, help=argparse.SUPPRESS)
     args = ap.parse_args()
+    if args.ref_plan_child:
+        mk, algo, threads, nseeds, cap = args.ref_plan_child
+        _ref_plan_child(mk, algo, int(threads), int(nseeds), float(cap))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

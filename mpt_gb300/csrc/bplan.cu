@@ -18,8 +18,8 @@
 //                           thread per sample over a bucket grid of the
 //                           nodes in shared memory (cells searched in rings
 //                           until the ring's distance bound passes the best);
-//                           every node that could reach the best (err32) is
-//                           re-ranked in FP64
+//                           FP32 distances decide wherever they are 2 err32
+//                           apart, FP64 only near ties and for the winner
 //   steer                   interpolate to `range` (skip when d == 0)
 //   link                    the DMV of the grid scene (scene.cu's two phases,
 //                           a warp per edge, the same sample order and counts)
@@ -92,23 +92,51 @@ __device__ __forceinline__ float rect_dist(const float* q, float x0, float x1, f
     return sqrtf(dx * dx + dy * dy);
 }
 
-// The nodes of one cell against the best so far: every node that could beat
-// or tie it in exact arithmetic is re-ranked in FP64 (lowest id on ties).
+// Nearest-node search state of one sample.  The winner is kept by its FP32
+// distance: a node whose FP32 distance lies more than 2E below the winner's
+// is certainly nearer in FP64 as well (|d32 - d64| <= E), so it replaces the
+// winner without any FP64 arithmetic; only a near tie (within 2E) computes
+// both FP64 distances and compares (distance, id) as the FP64 search does.
+// bup stays an upper bound of the winner's FP64 distance.  The FP64 distance
+// of the final winner is computed once (nn_finish).
+struct NNState {
+    int wid = INT_MAX;      // winner (INT_MAX: none yet)
+    float wd32 = INFINITY;  // its FP32 distance
+    double wd64 = -1.0;     // its FP64 distance once computed (< 0: not yet)
+    float bup = INFINITY;
+};
+
+// The nodes of one cell against the winner so far.
 __device__ __forceinline__ void scan_cell(const BPlanJob& J, const BSmem& S, int c, const float* q32, const double* qd,
-                                          float E, double& best, int& bid, float& bup) {
+                                          float E, NNState& st) {
     for (int j = S.head[c]; j >= 0; j = S.nxt[j]) {
         const float2 pj = S.pts[j];
         const float p32[2] = {pj.x, pj.y};
         const float d32 = dist32<MPTG_METRIC_L2, 2>(q32, p32, 1.f, 1.f);
-        if (__fsub_rd(d32, E) <= bup) {
-            const double d = l2_dist64(qd, J.states + 2 * j, 2);
-            if (d < best || (d == best && j < bid)) {
-                best = d;
-                bid = j;
-                bup = __double2float_ru(best);
-            }
+        if (!(__fsub_rd(d32, E) <= st.bup)) continue;  // cannot beat or tie the winner (or NaN)
+        if (st.wid == INT_MAX || __fadd_ru(d32, E) < __fsub_rd(st.wd32, E)) {
+            st.wid = j;
+            st.wd32 = d32;
+            st.wd64 = -1.0;
+            st.bup = __fadd_ru(d32, E);
+            continue;
         }
+        if (st.wd64 < 0.0) st.wd64 = l2_dist64(qd, J.states + 2 * st.wid, 2);
+        const double d = l2_dist64(qd, J.states + 2 * j, 2);
+        if (d < st.wd64 || (d == st.wd64 && j < st.wid)) {
+            st.wid = j;
+            st.wd32 = d32;
+            st.wd64 = d;
+        }
+        st.bup = __double2float_ru(st.wd64);
     }
+}
+
+// the winner's FP64 distance (INFINITY without a winner)
+__device__ __forceinline__ double nn_finish(const BPlanJob& J, const double* qd, NNState& st) {
+    if (st.wid == INT_MAX) return INFINITY;
+    if (st.wd64 < 0.0) st.wd64 = l2_dist64(qd, J.states + 2 * st.wid, 2);
+    return st.wd64;
 }
 
 __device__ __forceinline__ float maxabs_ru(double x, double y) {
@@ -196,9 +224,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
             const float E = err32<MPTG_METRIC_L2>(2, M, 1.f, 1.f);
             const float cs = J.cell_size, fuzz = 1e-3f * cs + 1e-3f;
             const int bgx = (J.gx + 3) >> 2, bgy = (J.gy + 3) >> 2;
-            double best = INFINITY;
-            int bid = INT_MAX;
-            float bup = INFINITY;
+            NNState st;
             int cx, cy;
             cell_of(J, q32[0], q32[1], &cx, &cy);
             const int bx = cx >> 2, by = cy >> 2;
@@ -206,18 +232,18 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
             auto visit_block = [&](int X, int Y) {
                 if (S.ccount[Y * bgx + X] == 0) return;
                 const float x0 = J.cell_ox + (float)(4 * X) * cs, y0 = J.cell_oy + (float)(4 * Y) * cs;
-                if (rect_dist(q32, x0, x0 + 4.f * cs, y0, y0 + 4.f * cs) - fuzz - E > bup) return;
+                if (rect_dist(q32, x0, x0 + 4.f * cs, y0, y0 + 4.f * cs) - fuzz - E > st.bup) return;
                 for (int y = 4 * Y; y < min(4 * Y + 4, J.gy); ++y)
                     for (int x = 4 * X; x < min(4 * X + 4, J.gx); ++x) {
                         const int c = y * J.gx + x;
                         if (S.head[c] < 0) continue;
                         const float fx = J.cell_ox + (float)x * cs, fy = J.cell_oy + (float)y * cs;
-                        if (rect_dist(q32, fx, fx + cs, fy, fy + cs) - fuzz - E > bup) continue;
-                        scan_cell(J, S, c, q32, qd, E, best, bid, bup);
+                        if (rect_dist(q32, fx, fx + cs, fy, fy + cs) - fuzz - E > st.bup) continue;
+                        scan_cell(J, S, c, q32, qd, E, st);
                     }
             };
             for (int R = 0; R <= Rmax; ++R) {
-                if (R >= 1 && (float)(R - 1) * 4.f * cs - fuzz - E > bup) break;
+                if (R >= 1 && (float)(R - 1) * 4.f * cs - fuzz - E > st.bup) break;
                 if (R == 0) {
                     visit_block(bx, by);
                     continue;
@@ -232,8 +258,9 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
                     if (bx + R < bgx) visit_block(bx + R, Y);
                 }
             }
+            const double best = nn_finish(J, qd, st);
             // steer (k_plan_steer)
-            const int id = bid == INT_MAX ? -1 : bid;
+            const int id = st.wid == INT_MAX ? -1 : st.wid;
             const double* s = qd;
             double* nw = S.nw + 2 * t;
             S.ni[t] = id;

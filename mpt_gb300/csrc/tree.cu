@@ -546,16 +546,10 @@ __device__ __forceinline__ void load_query(const double* __restrict__ qd, int D,
         if (lane == d) myq = q[d];
 }
 
-// order (may be null): warp w answers query order[w], so that neighbouring
-// warps, sorted by tree region, reuse each other's nodes in L1
+// One query (index qi) answered by the calling warp.
 template <int MK, int DMAX>
-__global__ void __launch_bounds__(256, 4) k_nearest(TreeView t, const double* __restrict__ q64, int nq,
-                                                 const int* __restrict__ order, int* __restrict__ out_idx,
-                                                 double* __restrict__ out_d) {
-    const int lane = threadIdx.x & 31;
-    const int wi = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-    if (wi >= nq) return;
-    const int qi = order ? __ldg(&order[wi]) : wi;
+__device__ __forceinline__ void nearest_one(const TreeView& t, const double* __restrict__ q64, int qi, int lane,
+                                            int* __restrict__ out_idx, double* __restrict__ out_d) {
     const int D = t.D;
     const double* qd = q64 + (size_t)qi * D;
     float q[DMAX];
@@ -661,6 +655,29 @@ __global__ void __launch_bounds__(256, 4) k_nearest(TreeView t, const double* __
             atomicAdd(&t.stats[3], n_pts);
             atomicAdd(&t.stats[4], n_rr);
         }
+    }
+}
+
+// Warp per query.  order (may be null): the w-th query answered is
+// order[w], so that neighbouring warps, sorted by tree region, reuse each
+// other's nodes in L1.  qnext (may be null, else zeroed before the launch):
+// a grid of resident warps only; each warp answers query w = its warp id,
+// then takes w = (warps in the grid) + atomicAdd(qnext, 1) until w >= nq, so
+// no warp slot idles while the slowest query of its block finishes (query
+// costs vary several-fold).
+template <int MK, int DMAX>
+__global__ void __launch_bounds__(256, 4) k_nearest(TreeView t, const double* __restrict__ q64, int nq,
+                                                 const int* __restrict__ order, int* __restrict__ out_idx,
+                                                 double* __restrict__ out_d, int* __restrict__ qnext) {
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (int)(((size_t)gridDim.x * blockDim.x) >> 5);
+    int wi = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    while (wi < nq) {
+        nearest_one<MK, DMAX>(t, q64, order ? __ldg(&order[wi]) : wi, lane, out_idx, out_d);
+        if (!qnext) break;
+        int nx = 0;
+        if (lane == 0) nx = atomicAdd(qnext, 1);
+        wi = nwarps + __shfl_sync(0xffffffffu, nx, 0);
     }
 }
 
@@ -1761,7 +1778,7 @@ mptg_status mptg_tree_nearest_dev(mptg_tree* t, const double* dq, int nq, int* d
             cudaFree(t->qorder);
             t->qkey = t->qorder = nullptr;
             t->qcap = 0;
-            if (!t->qhist) MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&t->qhist, MPTG_QSORT_BINS * sizeof(int)));
+            if (!t->qhist) MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&t->qhist, (MPTG_QSORT_BINS + 1) * sizeof(int)));
             MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&t->qkey, (size_t)nq * sizeof(int)));
             MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&t->qorder, (size_t)nq * sizeof(int)));
             t->qcap = (size_t)nq;
@@ -1783,8 +1800,18 @@ mptg_status mptg_tree_nearest_dev(mptg_tree* t, const double* dq, int nq, int* d
         unsigned grid = mptg_blocks((size_t)nq, 256);
         DISPATCH_METRIC(t->metric, t->D, k_nearest_packet, grid, 256, s, v, dq, nq, order, didx, dd);
     } else {
+        // more queries than resident warps (4 blocks of 8 per SM): a resident
+        // grid taking queries from a counter (qhist's last slot)
         unsigned grid = mptg_blocks((size_t)nq * 32, 256);
-        DISPATCH_METRIC(t->metric, t->D, k_nearest, grid, 256, s, v, dq, nq, order, didx, dd);
+        int* qnext = nullptr;
+        const unsigned resident = 4u * (unsigned)ctx->sms;
+        if (grid > 2 * resident) {
+            if (!t->qhist) MPTG_CUDA_TRY(ctx, cudaMalloc((void**)&t->qhist, (MPTG_QSORT_BINS + 1) * sizeof(int)));
+            qnext = t->qhist + MPTG_QSORT_BINS;
+            MPTG_CUDA_TRY(ctx, cudaMemsetAsync(qnext, 0, sizeof(int), s));
+            grid = resident;
+        }
+        DISPATCH_METRIC(t->metric, t->D, k_nearest, grid, 256, s, v, dq, nq, order, didx, dd, qnext);
     }
     MPTG_LAUNCHED(ctx);
     return MPTG_OK;
