@@ -78,12 +78,18 @@ __device__ __forceinline__ int cell_of(const BPlanJob& J, float x, float y, int*
     return iy * J.gx + ix;
 }
 
-__device__ __forceinline__ void bucket_insert(const BPlanJob& J, const BSmem& S, int j) {
+// node j into its cell's list, its block's count and the cell rectangle of
+// all nodes (bb: min x, max x, min y, max y)
+__device__ __forceinline__ void bucket_insert(const BPlanJob& J, const BSmem& S, int* bb, int j) {
     int cx, cy;
     const float2 p = S.pts[j];
     const int c = cell_of(J, p.x, p.y, &cx, &cy);
     S.nxt[j] = (short)atomicExch(&S.head[c], j);
     atomicAdd(&S.ccount[(cy >> 2) * ((J.gx + 3) >> 2) + (cx >> 2)], 1);
+    atomicMin(&bb[0], cx);
+    atomicMax(&bb[1], cx);
+    atomicMin(&bb[2], cy);
+    atomicMax(&bb[3], cy);
 }
 
 // FP32 distance from q to the rectangle [x0, x1] x [y0, y1] (0 inside)
@@ -98,7 +104,7 @@ __device__ __forceinline__ float rect_dist(const float* q, float x0, float x1, f
 // winner without any FP64 arithmetic; only a near tie (within 2E) computes
 // both FP64 distances and compares (distance, id) as the FP64 search does.
 // bup stays an upper bound of the winner's FP64 distance.  The FP64 distance
-// of the final winner is computed once (nn_finish).
+// of the final winner is computed once, by the steer step.
 struct NNState {
     int wid = INT_MAX;      // winner (INT_MAX: none yet)
     float wd32 = INFINITY;  // its FP32 distance
@@ -106,14 +112,17 @@ struct NNState {
     float bup = INFINITY;
 };
 
-// The nodes of one cell against the winner so far.
+// The nodes of one cell against the winner so far; gb, an upper bound of
+// the FP64 distance of a node found by another thread of the group, prunes
+// as well (a node beyond it cannot win).
 __device__ __forceinline__ void scan_cell(const BPlanJob& J, const BSmem& S, int c, const float* q32, const double* qd,
-                                          float E, NNState& st) {
+                                          float E, NNState& st, float gb) {
     for (int j = S.head[c]; j >= 0; j = S.nxt[j]) {
         const float2 pj = S.pts[j];
         const float p32[2] = {pj.x, pj.y};
         const float d32 = dist32<MPTG_METRIC_L2, 2>(q32, p32, 1.f, 1.f);
-        if (!(__fsub_rd(d32, E) <= st.bup)) continue;  // cannot beat or tie the winner (or NaN)
+        const float lo = __fsub_rd(d32, E);
+        if (!(lo <= st.bup) || lo > gb) continue;  // cannot beat or tie a winner (or NaN)
         if (st.wid == INT_MAX || __fadd_ru(d32, E) < __fsub_rd(st.wd32, E)) {
             st.wid = j;
             st.wd32 = d32;
@@ -132,11 +141,54 @@ __device__ __forceinline__ void scan_cell(const BPlanJob& J, const BSmem& S, int
     }
 }
 
-// the winner's FP64 distance (INFINITY without a winner)
-__device__ __forceinline__ double nn_finish(const BPlanJob& J, const double* qd, NNState& st) {
-    if (st.wid == INT_MAX) return INFINITY;
-    if (st.wd64 < 0.0) st.wd64 = l2_dist64(qd, J.states + 2 * st.wid, 2);
-    return st.wd64;
+// The exact winner of a group (lowest FP64 distance, then lowest id) from its
+// threads' winners: a thread whose winner's lower bound exceeds another's
+// upper bound cannot hold it; the one thread left, or else the FP64
+// distances of the ones left, decide.  The winning thread writes the id to
+// S.ni[g] and its FP64 distance to S.nd[g] (-1 when not yet computed; -1 id
+// and INFINITY without any node).
+__device__ __forceinline__ void nn_group_winner(const BPlanJob& J, const BSmem& S, int g, int r, int G, unsigned gmask,
+                                                const double* qd, float E, NNState& st) {
+    const bool have = st.wid != INT_MAX;
+    const float up = !have ? INFINITY : st.wd64 >= 0.0 ? __double2float_ru(st.wd64) : __fadd_ru(st.wd32, E);
+    const float lo = !have ? INFINITY : st.wd64 >= 0.0 ? __double2float_rd(st.wd64) : __fsub_rd(st.wd32, E);
+    float U = up;
+    for (int o = 1; o < G; o <<= 1) U = fminf(U, __shfl_xor_sync(gmask, U, o));
+    const bool cont = have && lo <= U;
+    const unsigned cm = __ballot_sync(gmask, cont) & gmask;
+    if (cm == 0) {  // no node in the tree
+        if (r == 0) {
+            S.ni[g] = -1;
+            S.nd[g] = INFINITY;
+        }
+        return;
+    }
+    if (__popc(cm) == 1) {
+        if (cont) {
+            S.ni[g] = st.wid;
+            S.nd[g] = st.wd64;
+        }
+        return;
+    }
+    double d = INFINITY;
+    int id = INT_MAX;
+    if (cont) {
+        if (st.wd64 < 0.0) st.wd64 = l2_dist64(qd, J.states + 2 * st.wid, 2);
+        d = st.wd64;
+        id = st.wid;
+    }
+    for (int o = 1; o < G; o <<= 1) {
+        const double od = __shfl_xor_sync(gmask, d, o);
+        const int oi = __shfl_xor_sync(gmask, id, o);
+        if (od < d || (od == d && oi < id)) {
+            d = od;
+            id = oi;
+        }
+    }
+    if (r == 0) {
+        S.ni[g] = id;
+        S.nd[g] = d;
+    }
 }
 
 __device__ __forceinline__ float maxabs_ru(double x, double y) {
@@ -151,16 +203,21 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
     extern __shared__ __align__(16) unsigned char bp_smem[];
     __shared__ int s_n, s_goals, s_maxabs, s_gidx, s_stop, s_total;
     __shared__ int s_wsum[32];
+    __shared__ int s_bb[4];
     __shared__ unsigned long long s_cnt;
     const BPlanJob& J = jobs[blockIdx.x];
     const int T = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5, nwarps = T >> 5;
     const int W = J.W, cap = J.cap;
+    int G = 1;  // threads per sample in the nearest search
+    while (G < 32 && 2 * G * W <= T) G <<= 1;
     const BSmem S = carve(bp_smem, cap_alloc, W_alloc);
     if (t == 0) {
         s_n = J.ctr->n;
         s_goals = J.ctr->goals;
         s_maxabs = 0;
         s_cnt = 0;
+        s_bb[0] = s_bb[2] = INT_MAX;
+        s_bb[1] = s_bb[3] = -1;
     }
     for (int c = t; c < J.gx * J.gy; c += T) S.head[c] = -1;
     for (int c = t; c < BPLAN_CELLS / 16; c += T) S.ccount[c] = 0;
@@ -169,7 +226,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
         const double x = J.states[2 * j], y = J.states[2 * j + 1];
         S.pts[j] = make_float2(__double2float_rn(x), __double2float_rn(y));
         atomicMax(&s_maxabs, __float_as_int(maxabs_ru(x, y)));
-        bucket_insert(J, S, j);
+        bucket_insert(J, S, s_bb, j);
     }
     uint32_t wave = J.ctr->wave;
     int waves_run = 0, status = BPLAN_DONE;
@@ -210,61 +267,81 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
             }
         }
         __syncthreads();
-        // nearest: thread per sample over the bucket grid, two levels: blocks
-        // of 4 x 4 cells in rings of growing Chebyshev distance around the
-        // sample's block, skipping empty blocks, then the cells of a block
-        // and their nodes.  A block or cell whose rectangle lies farther than
-        // the best (less the boundary fuzz and E) holds no node that can
-        // reach it; a block R >= 1 rings out lies at least (R - 1) blocks
-        // away, which ends the search.
-        if (t < W) {
-            const double* qd = S.q + 2 * t;
-            const float q32[2] = {__double2float_rn(qd[0]), __double2float_rn(qd[1])};
-            const float M = fmaxf(__int_as_float(s_maxabs), maxabs_ru(qd[0], qd[1]));
-            const float E = err32<MPTG_METRIC_L2>(2, M, 1.f, 1.f);
-            const float cs = J.cell_size, fuzz = 1e-3f * cs + 1e-3f;
-            const int bgx = (J.gx + 3) >> 2, bgy = (J.gy + 3) >> 2;
-            NNState st;
-            int cx, cy;
-            cell_of(J, q32[0], q32[1], &cx, &cy);
-            const int bx = cx >> 2, by = cy >> 2;
-            const int Rmax = max(bgx, bgy);
-            auto visit_block = [&](int X, int Y) {
-                if (S.ccount[Y * bgx + X] == 0) return;
-                const float x0 = J.cell_ox + (float)(4 * X) * cs, y0 = J.cell_oy + (float)(4 * Y) * cs;
-                if (rect_dist(q32, x0, x0 + 4.f * cs, y0, y0 + 4.f * cs) - fuzz - E > st.bup) return;
-                for (int y = 4 * Y; y < min(4 * Y + 4, J.gy); ++y)
-                    for (int x = 4 * X; x < min(4 * X + 4, J.gx); ++x) {
-                        const int c = y * J.gx + x;
-                        if (S.head[c] < 0) continue;
-                        const float fx = J.cell_ox + (float)x * cs, fy = J.cell_oy + (float)y * cs;
-                        if (rect_dist(q32, fx, fx + cs, fy, fy + cs) - fuzz - E > st.bup) continue;
-                        scan_cell(J, S, c, q32, qd, E, st);
+        // nearest: a group of G threads per sample (G = 1024 / W rounded down
+        // to a power of two, at most 32) over the bucket grid, two levels:
+        // blocks of 4 x 4 cells in rings of growing Chebyshev distance around
+        // the sample's block, clipped to the blocks that hold nodes (s_bb),
+        // the (block, cell) pairs of a ring dealt round-robin to the group.
+        // A block or cell whose rectangle lies farther than the group's best
+        // (less the boundary fuzz and E) holds no node that can reach it; a
+        // block R >= 1 rings out lies at least (R - 1) blocks away, which ends
+        // the search.  The group's winner is then exact (nn_group_winner).
+        {
+            const int g = t / G, r = t % G;
+            if (g < W) {
+                const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+                const double* qd = S.q + 2 * g;
+                const float q32[2] = {__double2float_rn(qd[0]), __double2float_rn(qd[1])};
+                const float M = fmaxf(__int_as_float(s_maxabs), maxabs_ru(qd[0], qd[1]));
+                const float E = err32<MPTG_METRIC_L2>(2, M, 1.f, 1.f);
+                const float cs = J.cell_size, fuzz = 1e-3f * cs + 1e-3f;
+                const int bgx = (J.gx + 3) >> 2;
+                NNState st;
+                float gb = INFINITY;  // the group's best upper bound, as of the last ring
+                int cx, cy;
+                cell_of(J, q32[0], q32[1], &cx, &cy);
+                const int bx = cx >> 2, by = cy >> 2;
+                const int X0 = s_bb[0] >> 2, X1 = s_bb[1] >> 2, Y0 = s_bb[2] >> 2, Y1 = s_bb[3] >> 2;
+                if (X0 <= X1) {
+                    // rings nearer than the node blocks' rectangle are empty
+                    const int R0 = max(max(X0 - bx, bx - X1), max(max(Y0 - by, by - Y1), 0));
+                    const int Rmax = max(max(bx - X0, X1 - bx), max(by - Y0, Y1 - by));
+                    for (int R = R0; R <= Rmax; ++R) {
+                        if (R >= 1 && (float)(R - 1) * 4.f * cs - fuzz - E > gb) break;
+                        // ring R within [X0, X1] x [Y0, Y1]: top row, bottom row, left and right columns
+                        const int xa = max(bx - R, X0), xb = min(bx + R, X1);
+                        const int ya = max(by - R + 1, Y0), yb = min(by + R - 1, Y1);
+                        const int nrow = xb >= xa ? xb - xa + 1 : 0, ncol = yb >= ya ? yb - ya + 1 : 0;
+                        const int ntop = (by - R >= Y0 && by - R <= Y1) ? nrow : 0;
+                        const int nbot = (R > 0 && by + R >= Y0 && by + R <= Y1) ? nrow : 0;
+                        const int nlft = (R > 0 && bx - R >= X0 && bx - R <= X1) ? ncol : 0;
+                        const int nrgt = (R > 0 && bx + R >= X0 && bx + R <= X1) ? ncol : 0;
+                        const int nb = ntop + nbot + nlft + nrgt;
+                        for (int f = r; f < 16 * nb; f += G) {
+                            int k = f >> 4, X, Y;
+                            if (k < ntop) { X = xa + k; Y = by - R; }
+                            else if ((k -= ntop) < nbot) { X = xa + k; Y = by + R; }
+                            else if ((k -= nbot) < nlft) { X = bx - R; Y = ya + k; }
+                            else { X = bx + R; Y = ya + (k - nlft); }
+                            if (S.ccount[Y * bgx + X] == 0) continue;
+                            const float cap = fminf(st.bup, gb);
+                            const float x0 = J.cell_ox + (float)(4 * X) * cs, y0 = J.cell_oy + (float)(4 * Y) * cs;
+                            if (rect_dist(q32, x0, x0 + 4.f * cs, y0, y0 + 4.f * cs) - fuzz - E > cap) continue;
+                            const int x = 4 * X + (f & 3), y = 4 * Y + ((f >> 2) & 3);
+                            if (x >= J.gx || y >= J.gy) continue;
+                            const int c = y * J.gx + x;
+                            if (S.head[c] < 0) continue;
+                            const float fx = J.cell_ox + (float)x * cs, fy = J.cell_oy + (float)y * cs;
+                            if (rect_dist(q32, fx, fx + cs, fy, fy + cs) - fuzz - E > cap) continue;
+                            scan_cell(J, S, c, q32, qd, E, st, gb);
+                        }
+                        float b = st.bup;
+                        for (int o = 1; o < G; o <<= 1) b = fminf(b, __shfl_xor_sync(gmask, b, o));
+                        gb = b;
                     }
-            };
-            for (int R = 0; R <= Rmax; ++R) {
-                if (R >= 1 && (float)(R - 1) * 4.f * cs - fuzz - E > st.bup) break;
-                if (R == 0) {
-                    visit_block(bx, by);
-                    continue;
                 }
-                const int X0 = max(bx - R, 0), X1 = min(bx + R, bgx - 1);
-                if (by - R >= 0)
-                    for (int X = X0; X <= X1; ++X) visit_block(X, by - R);
-                if (by + R < bgy)
-                    for (int X = X0; X <= X1; ++X) visit_block(X, by + R);
-                for (int Y = max(by - R + 1, 0); Y <= min(by + R - 1, bgy - 1); ++Y) {
-                    if (bx - R >= 0) visit_block(bx - R, Y);
-                    if (bx + R < bgx) visit_block(bx + R, Y);
-                }
+                nn_group_winner(J, S, g, r, G, gmask, qd, E, st);
             }
-            const double best = nn_finish(J, qd, st);
-            // steer (k_plan_steer)
-            const int id = st.wid == INT_MAX ? -1 : st.wid;
-            const double* s = qd;
-            double* nw = S.nw + 2 * t;
-            S.ni[t] = id;
+        }
+        __syncthreads();
+        // steer (k_plan_steer), thread per sample
+        if (t < W) {
+            const double* s = S.q + 2 * t;
+            const int id = S.ni[t];
+            double best = S.nd[t];
+            if (id >= 0 && best < 0.0) best = l2_dist64(s, J.states + 2 * id, 2);
             S.nd[t] = best;
+            double* nw = S.nw + 2 * t;
             const bool skip = id < 0 || best == 0.0 || !(best == best);  // prrt.hpp:425
             if (!skip && best > J.range) {
                 const double a[2] = {J.states[2 * id], J.states[2 * id + 1]};
@@ -387,7 +464,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
                 J.states[2 * id] = nw[0];
                 J.states[2 * id + 1] = nw[1];
                 S.pts[id] = make_float2(__double2float_rn(nw[0]), __double2float_rn(nw[1]));
-                bucket_insert(J, S, id);
+                bucket_insert(J, S, s_bb, id);
                 J.parent[id] = S.ni[t];
                 // GoalState::operator() (src/mpt/goal_state.hpp:64-69): d <= radius
                 const uint8_t g = (J.has_goal && dist64(MPTG_METRIC_L2, 2, 1.0, 1.0, nw, J.goal) <= J.goal_radius)

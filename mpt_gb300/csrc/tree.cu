@@ -479,6 +479,27 @@ __device__ __forceinline__ float cell_lb_vals(const TreeView& t, float myq, floa
     }
 }
 
+// cell_lb_vals for L1, L2 and SO(2)^n with every dimension held twice, by
+// lanes d and d + 16 (dl = lane & 15): the xor reduction over 16 lanes then
+// leaves the sum in all 32 lanes, with no broadcast (the same additions in
+// the same order as warp_sum16, so the same bound bit for bit).
+template <int MK>
+__device__ __forceinline__ float cell_lb_half(int D, float myq, float lo, float hi, int dl) {
+    float o = 0.f;
+    if constexpr (MK == MPTG_METRIC_SO2) {
+        if (dl < D && (myq < lo || myq > hi)) o = fminf(so2_w32(myq - lo), so2_w32(myq - hi));
+    } else {
+        o = dl < D ? fmaxf(fmaxf(lo - myq, myq - hi), 0.f) : 0.f;
+        if constexpr (MK == MPTG_METRIC_L2) o = o * o;
+    }
+    o += __shfl_xor_sync(0xffffffffu, o, 8);
+    o += __shfl_xor_sync(0xffffffffu, o, 4);
+    o += __shfl_xor_sync(0xffffffffu, o, 2);
+    o += __shfl_xor_sync(0xffffffffu, o, 1);
+    if constexpr (MK == MPTG_METRIC_L2) return sqrtf(o);
+    else return o;
+}
+
 // lower bound of the distance from the query to node `c`'s stored cell
 template <int MK>
 __device__ __forceinline__ float cell_lb(const TreeView& t, int c, float myq, int lane) {
@@ -556,6 +577,14 @@ __device__ __forceinline__ void nearest_one(const TreeView& t, const double* __r
     float myq, M;
     load_query<MK, DMAX>(qd, D, lane, q, myq, M, t);
     const float E = err32<MK>(D, M, t.w0f, t.w1f);
+    // L1 / L2 / SO(2)^n: each half-warp holds every dimension (cell_lb_half)
+    constexpr bool HALF = (MK == MPTG_METRIC_L1 || MK == MPTG_METRIC_L2 || MK == MPTG_METRIC_SO2) && DMAX <= 16;
+    const int dl = HALF ? (lane & 15) : lane;
+    if constexpr (HALF) {
+#pragma unroll
+        for (int d = 0; d < DMAX; ++d)
+            if (dl == d) myq = q[d];
+    }
 
     double best = INFINITY;
     int bidx = INT_MAX;
@@ -566,28 +595,33 @@ __device__ __forceinline__ void nearest_one(const TreeView& t, const double* __r
     int s0n = 0, s1n = 0;
     float s0l = 0.f, s1l = 0.f;
     int node = 0;
-    // The current node's record and cell live in registers: lane d < D holds
-    // the cell's interval on dimension d.  A child's cell is its parent's with
-    // one bound replaced by the split (as k_seg_c builds them), so descending
-    // needs no cell load; only a pop reloads a cell.  Both children's records
-    // arrive with one load (lanes 0/1), so each level costs one round trip.
+    // The current node's record and cell live in registers: lane d < D (and
+    // d + 16 under HALF) holds the cell's interval on dimension d.  A child's
+    // cell is its parent's with one bound replaced by the split (as k_seg_c
+    // builds them), so descending needs no cell load; only a pop reloads a
+    // cell.  The near child's record is loaded (one address for the whole
+    // warp) as soon as the side is known, and arrives while the far child's
+    // bound is computed, so each level costs one round trip.
     int4 nd = __ldg(&t.nodes[0]);
     float clo = 0.f, chi = 0.f;
-    if (lane < D) { clo = __ldg(&t.cell_lo[lane]); chi = __ldg(&t.cell_hi[lane]); }
+    if (dl < D) { clo = __ldg(&t.cell_lo[dl]); chi = __ldg(&t.cell_hi[dl]); }
     while (true) {
         if (nd.x >= 0) {
             ++n_int;
             const int c = nd.y, s = nd.x;
-            const int4 ch = __ldg(&t.nodes[c + (lane & 1)]);
             const float split = __int_as_float(nd.z);
             const float qv = __shfl_sync(0xffffffffu, myq, s);
             const bool goLeft = qv < split;
+            const int nearc = goLeft ? c : c + 1;
+            const int4 nn = __ldg(&t.nodes[nearc]);
             float flo = clo, fhi = chi;
-            if (lane == s) {
+            if (dl == s) {
                 if (goLeft) flo = split;
                 else fhi = split;
             }
-            float lb = cell_lb_vals<MK>(t, myq, flo, fhi, lane);
+            float lb;
+            if constexpr (HALF) lb = cell_lb_half<MK>(D, myq, flo, fhi, dl);
+            else lb = cell_lb_vals<MK>(t, myq, flo, fhi, lane);
             const int farc = goLeft ? c + 1 : c;
             // the builder keeps depth <= MPTG_MAX_DEPTH < 64, so the stack never fills
             if (__fsub_rd(lb, E) <= bestf_up && sp < 64) {
@@ -598,16 +632,12 @@ __device__ __forceinline__ void nearest_one(const TreeView& t, const double* __r
                 }
                 ++sp;
             }
-            if (lane == s) {
+            if (dl == s) {
                 if (goLeft) chi = split;
                 else clo = split;
             }
-            const int src = goLeft ? 0 : 1;
-            nd.x = __shfl_sync(0xffffffffu, ch.x, src);
-            nd.y = __shfl_sync(0xffffffffu, ch.y, src);
-            nd.z = __shfl_sync(0xffffffffu, ch.z, src);
-            nd.w = __shfl_sync(0xffffffffu, ch.w, src);
-            node = goLeft ? c : c + 1;
+            nd = nn;
+            node = nearc;
             continue;
         }
         // leaf
@@ -640,9 +670,9 @@ __device__ __forceinline__ void nearest_one(const TreeView& t, const double* __r
         }
         if (!found) break;
         nd = __ldg(&t.nodes[node]);
-        if (lane < D) {
-            clo = __ldg(&t.cell_lo[(size_t)node * D + lane]);
-            chi = __ldg(&t.cell_hi[(size_t)node * D + lane]);
+        if (dl < D) {
+            clo = __ldg(&t.cell_lo[(size_t)node * D + dl]);
+            chi = __ldg(&t.cell_hi[(size_t)node * D + dl]);
         }
     }
     if (lane == 0) {
