@@ -290,6 +290,12 @@ mptg_status mptg_planner_set_surrogate_bias(mptg_planner* planner, int candidate
  * added, [3] tree size, [4] goals, [5] states checked by link, [6] seconds in
  * run, [7] wavefront counter. */
 mptg_status mptg_planner_stats(mptg_planner* planner, double out[8]);
+/* Persistent block planner (grid scenes, mptg_planner_set_persistent), summed
+ * over its runs: [0..5] SM cycles in the sample, nearest-search, steer, link
+ * set-up, link-sample and insert phases; [6] near ties of the nearest search
+ * decided in FP64, [7] interior samples decided in FP64, [8] edge step counts
+ * decided in FP64.  No reference counterpart (a profile of this planner). */
+mptg_status mptg_planner_block_profile(mptg_planner* planner, double out[9]);
 /* Planner<Scenario, PRRTStar<...>> (src/mpt/prrt_star.hpp:56-95): wavefronts
  * with k-nearest rewiring (rewire_k_nearest, the reference default):
  * k = ceil(rewire_factor * e * (1 + 1/dim) * ln(n + 1)), at most 64

@@ -116,7 +116,7 @@ struct NNState {
 // the FP64 distance of a node found by another thread of the group, prunes
 // as well (a node beyond it cannot win).
 __device__ __forceinline__ void scan_cell(const BPlanJob& J, const BSmem& S, int c, const float* q32, const double* qd,
-                                          float E, NNState& st, float gb) {
+                                          float E, NNState& st, float gb, unsigned long long* ties) {
     for (int j = S.head[c]; j >= 0; j = S.nxt[j]) {
         const float2 pj = S.pts[j];
         const float p32[2] = {pj.x, pj.y};
@@ -130,6 +130,7 @@ __device__ __forceinline__ void scan_cell(const BPlanJob& J, const BSmem& S, int
             st.bup = __fadd_ru(d32, E);
             continue;
         }
+        atomicAdd(ties, 1ull);
         if (st.wd64 < 0.0) st.wd64 = l2_dist64(qd, J.states + 2 * st.wid, 2);
         const double d = l2_dist64(qd, J.states + 2 * j, 2);
         if (d < st.wd64 || (d == st.wd64 && j < st.wid)) {
@@ -204,6 +205,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
     __shared__ int s_n, s_goals, s_maxabs, s_gidx, s_stop, s_total;
     __shared__ int s_wsum[32];
     __shared__ int s_bb[4];
+    __shared__ unsigned long long s_prof[3];  // FP64 fallbacks: near ties, unsure samples, step counts
     __shared__ unsigned long long s_cnt;
     const BPlanJob& J = jobs[blockIdx.x];
     const int T = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5, nwarps = T >> 5;
@@ -216,6 +218,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
         s_goals = J.ctr->goals;
         s_maxabs = 0;
         s_cnt = 0;
+        s_prof[0] = s_prof[1] = s_prof[2] = 0;
         s_bb[0] = s_bb[2] = INT_MAX;
         s_bb[1] = s_bb[3] = -1;
     }
@@ -231,7 +234,15 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
     uint32_t wave = J.ctr->wave;
     int waves_run = 0, status = BPLAN_DONE;
     unsigned long long samples = 0, accepted = 0;
-    unsigned long long cyc0 = 0, cyc1 = 0, cyc2 = 0, tc = 0;  // phase cycles, kept by thread 0
+    unsigned long long cyc[6] = {0, 0, 0, 0, 0, 0}, tc = 0;  // phase cycles, kept by thread 0
+    // thread 0, after a barrier: the cycles since the last mark go to phase i
+    auto mark = [&](int i) {
+        if (t == 0) {
+            const unsigned long long c = clock64();
+            cyc[i] += c - tc;
+            tc = c;
+        }
+    };
     const uint64_t t0 = umma::globaltimer_ns();
     __syncthreads();
     for (;;) {
@@ -267,6 +278,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
             }
         }
         __syncthreads();
+        mark(0);
         // nearest: a group of G threads per sample (G = 1024 / W rounded down
         // to a power of two, at most 32) over the bucket grid, two levels:
         // blocks of 4 x 4 cells in rings of growing Chebyshev distance around
@@ -323,7 +335,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
                             if (S.head[c] < 0) continue;
                             const float fx = J.cell_ox + (float)x * cs, fy = J.cell_oy + (float)y * cs;
                             if (rect_dist(q32, fx, fx + cs, fy, fy + cs) - fuzz - E > cap) continue;
-                            scan_cell(J, S, c, q32, qd, E, st, gb);
+                            scan_cell(J, S, c, q32, qd, E, st, gb, &s_prof[0]);
                         }
                         float b = st.bup;
                         for (int o = 1; o < G; o <<= 1) b = fminf(b, __shfl_xor_sync(gmask, b, o));
@@ -334,6 +346,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
             }
         }
         __syncthreads();
+        mark(1);
         // steer (k_plan_steer), thread per sample
         if (t < W) {
             const double* s = S.q + 2 * t;
@@ -353,11 +366,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
             S.fl[t] = skip ? 2 : 0;
         }
         __syncthreads();
-        if (t == 0) {
-            const unsigned long long c = clock64();
-            cyc0 += c - tc;
-            tc = c;
-        }
+        mark(2);
         // link(near, new), as k_grid_edges_a / k_grid_edges_b: phase A thread
         // per edge (the end state, the step count and the FP32 set-up of the
         // interior samples, all the FP64 work of an edge), phase B warp per
@@ -377,7 +386,9 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
                 A[1] = J.states[2 * id + 1];
             }
             bool ok = grid_valid_f(J.scene, B);
-            long long steps = ok ? grid_edge_steps(A, B, J.inv_step) : 0;
+            bool used64 = false;
+            long long steps = ok ? grid_edge_steps(A, B, J.inv_step, &used64) : 0;
+            if (used64) atomicAdd(&s_prof[2], 1ull);
             if (steps < 0) ok = false;
             float4 setup = make_float4(0.f, 0.f, 0.f, 0.f);
             float eps = 0.f;
@@ -393,6 +404,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
             if (ok) S.fl[t] |= 1;
         }
         __syncthreads();
+        mark(3);
         for (int e = warp; e < W; e += nwarps) {
             const float2 es = reinterpret_cast<const float2*>(S.nd)[e];
             const int steps = __float_as_int(es.y);
@@ -412,6 +424,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
                         const float tt = (float)k / (float)steps;
                         const int res = grid_valid32(J.scene, fmaf(su.z, tt, su.x), fmaf(su.w, tt, su.y), eps);
                         if (res == VF_UNSURE) {
+                            atomicAdd(&s_prof[1], 1ull);
                             // the exact FP64 sample, as the CPU checker computes it
                             const int id = S.ni[e];
                             const double A[2] = {J.states[2 * id], J.states[2 * id + 1]};
@@ -432,11 +445,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
             if (lane == 0 && J.nsamp) atomicAdd(&s_cnt, cnt);
         }
         __syncthreads();
-        if (t == 0) {
-            const unsigned long long c = clock64();
-            cyc1 += c - tc;
-            tc = c;
-        }
+        mark(4);
         // accepted samples in sample order (k_plan_scan / k_plan_scatter)
         const int f = (t < W && S.fl[t] == 1) ? 1 : 0;
         const unsigned m = __ballot_sync(0xffffffffu, f);
@@ -481,7 +490,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
         ++waves_run;
         ++wave;
         __syncthreads();
-        if (t == 0) cyc2 += clock64() - tc;
+        mark(5);
     }
     if (t == 0) {
         J.ctr->n = s_n;
@@ -492,9 +501,10 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
         J.ctr->waves_run = waves_run;
         J.ctr->samples = samples;
         J.ctr->accepted = accepted;
-        J.ctr->cyc[0] = cyc0;
-        J.ctr->cyc[1] = cyc1;
-        J.ctr->cyc[2] = cyc2;
+        for (int i = 0; i < 6; ++i) J.ctr->cyc[i] = cyc[i];
+        J.ctr->ties = s_prof[0];
+        J.ctr->unsure = s_prof[1];
+        J.ctr->steps64 = s_prof[2];
         if (J.nsamp) atomicAdd(J.nsamp, s_cnt);
     }
 }

@@ -12,7 +12,12 @@ struct BPlanCounters {
     int waves_run;                  // wavefronts this run completed
     unsigned long long samples;     // samples drawn by this run
     unsigned long long accepted;    // nodes added by this run
-    unsigned long long cyc[3];      // SM cycles in sample + nearest + steer, link, insert (this run)
+    // SM cycles of this run per phase: samples, nearest search, steer, link
+    // set-up (thread per edge), link samples (warp per edge), insert
+    unsigned long long cyc[6];
+    // FP64 fallbacks of this run: near ties of the nearest search, unsure
+    // interior samples (warps), step counts left to FP64
+    unsigned long long ties, unsure, steps64;
 };
 
 enum { BPLAN_DONE = 0, BPLAN_FULL = 1 };  // FULL: the next wavefront could overflow the block's node capacity

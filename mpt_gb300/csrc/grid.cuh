@@ -39,7 +39,8 @@ __device__ __forceinline__ bool grid_valid_f(const SceneView& s, const double* q
 // grid edge step count ceil(|a - b| * inv) (the L2 metric, dist64) with an
 // FP32 filter: FP64 only when the FP32 value lies within its error bound of
 // an integer
-__device__ __forceinline__ long long grid_edge_steps(const double* A, const double* B, double inv) {
+__device__ __forceinline__ long long grid_edge_steps(const double* A, const double* B, double inv,
+                                                    bool* used64 = nullptr) {
     float dx = __double2float_rn(A[0]) - __double2float_rn(B[0]);
     float dy = __double2float_rn(A[1]) - __double2float_rn(B[1]);
     float m32 = sqrtf(dx * dx + dy * dy);
@@ -51,6 +52,7 @@ __device__ __forceinline__ long long grid_edge_steps(const double* A, const doub
         float lo = ceilf(x - e), hi = ceilf(x + e);
         if (lo == hi && x < 1e7f) return (long long)lo;
     }
+    if (used64) *used64 = true;
     double sd = ceil(__dmul_rn(l2_dist64(A, B, 2), inv));
     if (!(sd >= 0.0) || sd > (double)MPTG_MAX_EDGE_SAMPLES) return -1;
     return (long long)sd;

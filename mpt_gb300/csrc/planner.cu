@@ -144,6 +144,7 @@ struct mptg_planner {
     // persistent block planner (bplan.cu): grid scenes, wavefronts <= 1024
     int bp_mode = 1;                    // 0 off, 1 used wherever it applies
     int bp_cap = 0;                     // node capacity of the buffers below
+    double bp_prof[9] = {};             // block planner: SM cycles per phase, FP64 fallback counts
     double* bp_states = nullptr;        // [bp_cap][2]
     uint8_t* bp_goalf = nullptr;        // [bp_cap]
     BPlanCounters* bp_ctr = nullptr;
@@ -1078,12 +1079,17 @@ static mptg_status run_persistent(mptg_planner* p, int max_waves, double time_li
         // time in proportion to the SM cycles it spent in each phase
         float ms = 0.f;
         MPTG_CUDA_TRY(ctx, cudaEventElapsedTime(&ms, p->ev[0], p->ev[1]));
-        const double tot = (double)(h->cyc[0] + h->cyc[1] + h->cyc[2]);
+        double tot = 0;
+        for (int i = 0; i < 6; ++i) tot += (double)h->cyc[i];
         if (tot > 0) {
-            p->t_phase[0] += 1e-3 * ms * (double)h->cyc[0] / tot;
-            p->t_phase[2] += 1e-3 * ms * (double)h->cyc[1] / tot;
-            p->t_phase[3] += 1e-3 * ms * (double)h->cyc[2] / tot;
+            p->t_phase[0] += 1e-3 * ms * (double)(h->cyc[0] + h->cyc[1] + h->cyc[2]) / tot;
+            p->t_phase[2] += 1e-3 * ms * (double)(h->cyc[3] + h->cyc[4]) / tot;
+            p->t_phase[3] += 1e-3 * ms * (double)h->cyc[5] / tot;
         }
+        for (int i = 0; i < 6; ++i) p->bp_prof[i] += (double)h->cyc[i];
+        p->bp_prof[6] += (double)h->ties;
+        p->bp_prof[7] += (double)h->unsure;
+        p->bp_prof[8] += (double)h->steps64;
     }
     const size_t n1 = (size_t)h->n;
     p->wave = h->wave;
@@ -1525,6 +1531,12 @@ mptg_status mptg_planner_rewire_stats(mptg_planner* p, double out[6]) {
 mptg_status mptg_planner_timers(mptg_planner* p, double out[4]) {
     if (!p || !out) return MPTG_ERR_INVALID_ARG;
     for (int k = 0; k < 4; ++k) out[k] = p->t_phase[k];
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_block_profile(mptg_planner* p, double out[9]) {
+    if (!p || !out) return MPTG_ERR_INVALID_ARG;
+    for (int i = 0; i < 9; ++i) out[i] = p->bp_prof[i];
     return MPTG_OK;
 }
 

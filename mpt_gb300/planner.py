@@ -140,6 +140,7 @@ def _sig(L):
         ("mptg_planner_set_persistent", ctypes.c_int, [P, ctypes.c_int]),
         ("mptg_planner_stats", ctypes.c_int, [P, P]),
         ("mptg_planner_timers", ctypes.c_int, [P, P]),
+        ("mptg_planner_block_profile", ctypes.c_int, [P, P]),
         ("mptg_planner_set_rewire", ctypes.c_int, [P, ctypes.c_int, ctypes.c_double]),
         ("mptg_planner_rewire_stats", ctypes.c_int, [P, P]),
         ("mptg_planner_costs", ctypes.c_int, [P, P, S, ctypes.POINTER(S)]),
@@ -394,6 +395,15 @@ class Planner:
         _check(self.ctx.h, self.lib.mptg_planner_stats(self.h, out))
         keys = ["wavefronts", "samples", "nodes_added", "tree_size", "goals", "link_states_checked", "seconds",
                 "wavefront_counter"]
+        return dict(zip(keys, [float(v) for v in out]))
+
+    def block_profile(self) -> dict:
+        """The persistent block planner's SM cycles per phase and FP64 fallback
+        counts, summed over its runs (mptg_planner_block_profile)."""
+        out = (ctypes.c_double * 9)()
+        _check(self.ctx.h, self.lib.mptg_planner_block_profile(self.h, out))
+        keys = ["cyc_sample", "cyc_nearest", "cyc_steer", "cyc_link_setup", "cyc_link_samples", "cyc_insert",
+                "near_ties_fp64", "samples_fp64", "step_counts_fp64"]
         return dict(zip(keys, [float(v) for v in out]))
 
     def costs(self) -> np.ndarray:
