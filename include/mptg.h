@@ -243,6 +243,14 @@ mptg_status mptg_planner_graph(mptg_planner* planner, double* states, int32_t* p
  * the multi-kernel wavefront runs.  mode 0: always the multi-kernel
  * wavefront.  Both build the same tree, state for state. */
 mptg_status mptg_planner_set_persistent(mptg_planner* planner, int mode);
+/* The block planner's nearest-node search (no reference counterpart: a tuning
+ * knob of this planner).  A wavefront of W samples over n nodes with
+ * W * n <= brute_pairs sweeps every node in FP32 and re-ranks the nodes within
+ * the FP32 error bound of the least in FP64; a larger one searches rings of a
+ * bucket grid.  Both return the exact FP64 nearest node (lowest id on ties),
+ * so the setting changes the speed only.  Default 2^24, which covers every
+ * wavefront of up to 1,024 samples over the block planner's 16,384 nodes. */
+mptg_status mptg_planner_set_block_search(mptg_planner* planner, long long brute_pairs);
 /* The planner's nearest-neighbour container -- PRRT's nn_ member, the nigh
  * tree its workers query (src/mpt/impl/prrt/prrt.hpp:121-122,406-409) -- as a
  * borrowed tree handle: mptg_nearest / mptg_nearest_k / mptg_nearest_linear /

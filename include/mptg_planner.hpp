@@ -23,6 +23,7 @@
 // have no effect (wavefronts replace the worker pool).
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <chrono>
 #include <cstdint>
@@ -246,9 +247,10 @@ public:
         return g > 0;
     }
 
-    // prrt.hpp:194-201: doneFn is polled between calls of up to kPollWavefronts
-    // wavefronts, each of which also ends at the first solution
-    static constexpr int kPollWavefronts = 16;
+    // prrt.hpp:194-201: doneFn is polled between calls of up to kPollSeconds
+    // of wavefronts (at least one), each of which also ends at the first
+    // solution and at the node budget
+    static constexpr double kPollSeconds = 0.005;
     template <class DoneFn>
     void solve(DoneFn done) {
         solve_until_(done, false, std::chrono::steady_clock::time_point{});
@@ -277,19 +279,16 @@ public:
     void solve_until_(DoneFn done, bool has_deadline, std::chrono::steady_clock::time_point end) {
         if (size() == 0) throw std::runtime_error("there are no valid initial states");
         create();
-        double st[8];
         while (!done()) {
-            double left = 0.0;
+            double limit = kPollSeconds;
             if (has_deadline) {
-                left = std::chrono::duration<double>(end - std::chrono::steady_clock::now()).count();
+                double left = std::chrono::duration<double>(end - std::chrono::steady_clock::now()).count();
                 if (left <= 0) break;
+                limit = std::min(limit, left);
             }
-            impl::check(ctx_, mptg_planner_stats(planner_, st));
-            double before = st[7];
             int s = 0;
-            impl::check(ctx_, mptg_planner_run(planner_, kPollWavefronts, left, solved() ? 0 : 1, &s));
-            impl::check(ctx_, mptg_planner_stats(planner_, st));
-            if (st[7] == before) break;  // node budget reached
+            impl::check(ctx_, mptg_planner_run(planner_, 0, limit, solved() ? 0 : 1, &s));
+            if (size() >= maxNodes_) break;  // node budget reached
         }
     }
 

@@ -14,12 +14,15 @@
 //   goal pick and samples   the Philox stream of sampler.cuh, sample i of
 //                           wavefront w; at most one goal sample (the lowest
 //                           i whose bias draw hits) until the first solution
-//   nearest                 exact FP64 nearest node, lowest id on ties:
-//                           thread per sample over a bucket grid of the
-//                           nodes in shared memory (cells searched in rings
-//                           until the ring's distance bound passes the best);
-//                           FP32 distances decide wherever they are 2 err32
-//                           apart, FP64 only near ties and for the winner
+//   nearest                 exact FP64 nearest node, lowest id on ties,
+//                           over the FP32 node copy in shared memory: while
+//                           W x nodes is small, an exhaustive FP32 sweep
+//                           (four samples per node read) and an FP64 re-rank
+//                           of the nodes within 2 err32 of the least; beyond
+//                           that, groups of threads per sample over a bucket
+//                           grid (cells searched in rings until the ring's
+//                           distance bound passes the best), FP32 deciding
+//                           wherever distances are 2 err32 apart
 //   steer                   interpolate to `range` (skip when d == 0)
 //   link                    the DMV of the grid scene (scene.cu's two phases,
 //                           a warp per edge, the same sample order and counts)
@@ -196,6 +199,202 @@ __device__ __forceinline__ float maxabs_ru(double x, double y) {
     return fmaxf(__double2float_ru(fabs(x)), __double2float_ru(fabs(y)));
 }
 
+// Squared FP32 distance, evaluated as dist32<L2, 2> evaluates it before its
+// square root.  sqrtf is correctly rounded and so monotone: the node with the
+// least squared value has the least dist32, and sqrtf of the least squared
+// value is the least dist32 itself.
+__device__ __forceinline__ float sq32(float qx, float qy, float2 p) {
+    const float tx = qx - p.x, ty = qy - p.y;
+    return fmaf(ty, ty, fmaf(tx, tx, 0.f));
+}
+
+// The nearest search's per-sample slots, laid over the new-state array S.nw
+// (16 bytes per sample), which the steer step writes only after the search.
+struct BruteSlots {
+    int* cnt;       // [W] candidates of each sample (pass 2)
+    float* maxabs;  // [W] largest |coordinate| of the sample, rounded up
+    float2* q32;    // [W] the sample rounded to FP32
+};
+__device__ __forceinline__ BruteSlots brute_slots(const BSmem& S, int W) {
+    unsigned char* base = reinterpret_cast<unsigned char*>(S.nw);
+    return BruteSlots{reinterpret_cast<int*>(base), reinterpret_cast<float*>(base + 4 * (size_t)W),
+                      reinterpret_cast<float2*>(base + 8 * (size_t)W)};
+}
+
+// The pass-2 bound of one sample: (min32 + 2E)^2 (1 + 2^-21), each step
+// rounded up, with min32 the sqrt of the sample's least squared FP32 distance
+// (S.fl) and E the FP32 error bound for its coordinates and the tree's.  Every
+// node whose correctly rounded dist32 is within min32 + 2E has its squared
+// value within this bound (sqrtf is off by at most half an ulp).
+__device__ __forceinline__ float brute_thr2(const BSmem& S, const BruteSlots& B, int s, float maxabs) {
+    const float M = fmaxf(maxabs, B.maxabs[s]);
+    const float E = err32<MPTG_METRIC_L2>(2, M, 1.f, 1.f);
+    const float thr = __fadd_ru(sqrtf(__int_as_float(S.fl[s])), __fmul_ru(2.f, E));
+    return __fmul_ru(__fmul_ru(thr, thr), 1.0000005f);
+}
+
+// Exhaustive nearest-node search for small wavefronts on small trees, where
+// the ring search spends its time walking cell lists.  Samples go in groups
+// of four; the P threads of a group (a power of two, all the block's threads
+// shared out) each take every P-th node of the FP32 copy, so a node read from
+// shared memory serves four distances.
+//   pass 1  per thread and sample, the least squared FP32 distance over its
+//           nodes, that node, and the second least; the least over the
+//           block's threads is min32 squared;
+//   pass 2  the candidates of each sample, the nodes with dist32 <= min32 + 2E
+//           (squared, against brute_thr2): a thread's least is one, and a
+//           thread whose second least is one as well holds two or more, so
+//           the count is exact up to two and the lowest id of a sole
+//           candidate is known without a second sweep;
+//   pass 3  a sample with two or more candidates gets a warp, which sweeps
+//           all nodes again, gathers the candidates into lanes and ranks them
+//           by (FP64 distance, id).
+// The exact winner p* has dist32(p*) <= d64(p*) + E <= d64(argmin32) + E <=
+// min32 + 2E, and so does every node that ties it in FP64, so the candidates
+// hold all of them: the result is the FP64 argmin with the lowest id, the
+// ring search's answer.  A sole candidate is the winner without any FP64
+// arithmetic; its FP64 distance is left (S.nd = -1) to the steer step, which
+// computes it for a whole warp of samples at once.  The FP64 pipe costs the
+// same per warp instruction however few lanes are active, so FP64 work is kept
+// to full warps: one FP64 distance per lane, never one thread's alone.
+// On entry S.fl[s] holds +inf (FP32 bits), S.ni[s] INT_MAX and the slots
+// (brute_slots) a zero count and the sample in FP32 for every sample s < W;
+// on return S.ni[s] is the winner
+// (INT_MAX without nodes) and S.nd[s] its FP64 distance or -1.  Every thread
+// of the block calls this.
+__device__ void nn_brute(const BPlanJob& J, const BSmem& S, int W, int n, float maxabs,
+                         unsigned long long* fp64_evals) {
+    const int T = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int NG = (W + 3) >> 2;
+    int P = 1;
+    while (2 * P * NG <= T) P <<= 1;
+    const int g = t / P, r = t % P, s0 = 4 * g;
+    const int PW = P < 32 ? P : 32;  // lanes of a group within one warp
+    const BruteSlots B = brute_slots(S, W);
+    int* cnt = B.cnt;
+    float qx[4], qy[4], m[4];
+    bool act[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        act[k] = g < NG && s0 + k < W;
+        const float2 q = B.q32[act[k] ? s0 + k : 0];
+        qx[k] = q.x;
+        qy[k] = q.y;
+        m[k] = INFINITY;
+    }
+    // per sample: the least squared distance of this thread's nodes, its node
+    // and the second least (a second node within the bound needs pass 3)
+    float m2[4];
+    int id[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        m2[k] = INFINITY;
+        id[k] = INT_MAX;
+    }
+    const int jstart = g < NG ? r : n;
+#pragma unroll 2
+    for (int j = jstart; j < n; j += P) {
+        const float2 p = S.pts[j];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float sq = sq32(qx[k], qy[k], p);
+            const bool lt = sq < m[k];
+            m2[k] = fminf(m2[k], fmaxf(sq, m[k]));
+            m[k] = fminf(m[k], sq);
+            id[k] = lt ? j : id[k];
+        }
+    }
+    float mw[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        mw[k] = m[k];
+        for (int o = 1; o < PW; o <<= 1) mw[k] = fminf(mw[k], __shfl_xor_sync(0xffffffffu, mw[k], o));
+        if (act[k] && (lane & (PW - 1)) == 0 && mw[k] < INFINITY) atomicMin(&S.fl[s0 + k], __float_as_int(mw[k]));
+    }
+    __syncthreads();
+    // candidates: a thread whose second least lies within the bound holds two
+    // or more; otherwise it holds its least alone, or none
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (!act[k]) continue;
+        const float thr2 = brute_thr2(S, B, s0 + k, maxabs);
+        const int c = (m[k] <= thr2 ? 1 : 0) + (m2[k] <= thr2 ? 1 : 0);
+        if (!c) continue;
+        atomicAdd(&cnt[s0 + k], c);
+        atomicMin(&S.ni[s0 + k], id[k]);
+    }
+    __syncthreads();
+    const int nwarps = T >> 5;
+    unsigned long long evals = 0;
+    for (int s = warp; s < W; s += nwarps) {
+        const int cs = cnt[s];
+        if (cs < 2) {
+            if (cs == 1 && lane == 0) S.nd[s] = -1.0;  // the sole candidate (S.ni) wins
+            continue;
+        }
+        const double* qd = S.q + 2 * s;
+        const float t2 = brute_thr2(S, B, s, maxabs);
+        const float sx = B.q32[s].x, sy = B.q32[s].y;
+        // best (FP64 distance bits, id): non-negative doubles order as their bits
+        long long bk = LLONG_MAX;
+        int bid = INT_MAX;
+        int myc = -1, nc = 0;  // candidate held by this lane; candidates held
+        auto flush = [&]() {
+            long long key = LLONG_MAX;
+            int cid = INT_MAX;
+            if (myc >= 0) {
+                key = __double_as_longlong(l2_dist64(qd, J.states + 2 * myc, 2));
+                cid = myc;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, cid, o);
+                if (ok < key || (ok == key && oi < cid)) {
+                    key = ok;
+                    cid = oi;
+                }
+            }
+            if (key < bk || (key == bk && cid < bid)) {
+                bk = key;
+                bid = cid;
+            }
+            evals += (unsigned long long)nc;
+            myc = -1;
+            nc = 0;
+        };
+        for (int base = 0; base < n; base += 32) {
+            const int j = base + lane;
+            unsigned mask = __ballot_sync(0xffffffffu, j < n && sq32(sx, sy, S.pts[j < n ? j : 0]) <= t2);
+            while (mask) {
+                const int b = __ffs(mask) - 1;
+                mask &= mask - 1;
+                if (lane == nc) myc = base + b;
+                if (++nc == 32) flush();
+            }
+        }
+        if (nc) flush();
+        if (lane == 0) {
+            S.ni[s] = bid;
+            S.nd[s] = __longlong_as_double(bk);
+        }
+    }
+    if (lane == 0 && evals) atomicAdd(fp64_evals, evals);
+}
+
+// GoalState's test d(q, goal) <= radius in FP64, decided by the FP32 distance
+// wherever it lies farther than its error bound E from the radius:
+// d64 >= d32 - E > radius, or d64 <= d32 + E < radius.  Only a state within E
+// of the goal sphere computes the FP64 distance.
+__device__ __forceinline__ bool goal_reached(const double* q, const double* goal, double radius) {
+    const float a[2] = {__double2float_rn(q[0]), __double2float_rn(q[1])};
+    const float b[2] = {__double2float_rn(goal[0]), __double2float_rn(goal[1])};
+    const float d32 = dist32<MPTG_METRIC_L2, 2>(a, b, 1.f, 1.f);
+    const float E = err32<MPTG_METRIC_L2>(2, fmaxf(maxabs_ru(q[0], q[1]), maxabs_ru(goal[0], goal[1])), 1.f, 1.f);
+    if (__fsub_rd(d32, E) > __double2float_ru(radius)) return false;
+    if (__fadd_ru(d32, E) < __double2float_rd(radius)) return true;
+    return dist64(MPTG_METRIC_L2, 2, 1.0, 1.0, q, goal) <= radius;
+}
+
 // cap_alloc / W_alloc: the shared-memory layout of this launch (the largest
 // job's); every job of the launch fits in it
 __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob* __restrict__ jobs, int cap_alloc,
@@ -276,6 +475,17 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
             } else {
                 sample_uniform_state(MPTG_METRIC_L2, 2, J.seed, (uint32_t)t, wave, J.lo, J.hi, q);
             }
+            // the exhaustive search's per-sample slots (nn_brute): its FP32
+            // copy of the sample and the sample's largest |coordinate|, made
+            // here by one thread per sample, so that the search converts no
+            // double (conversions from FP64 use the slow FP64 pipe)
+            S.fl[t] = 0x7f800000;
+            S.nd[t] = INFINITY;
+            S.ni[t] = INT_MAX;
+            const BruteSlots b = brute_slots(S, W);
+            b.cnt[t] = 0;
+            b.maxabs[t] = maxabs_ru(q[0], q[1]);
+            b.q32[t] = make_float2(__double2float_rn(q[0]), __double2float_rn(q[1]));
         }
         __syncthreads();
         mark(0);
@@ -288,7 +498,9 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
         // (less the boundary fuzz and E) holds no node that can reach it; a
         // block R >= 1 rings out lies at least (R - 1) blocks away, which ends
         // the search.  The group's winner is then exact (nn_group_winner).
-        {
+        if ((long long)W * n <= J.brute_pairs) {
+            nn_brute(J, S, W, n, __int_as_float(s_maxabs), &s_prof[0]);
+        } else {
             const int g = t / G, r = t % G;
             if (g < W) {
                 const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
@@ -350,7 +562,8 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
         // steer (k_plan_steer), thread per sample
         if (t < W) {
             const double* s = S.q + 2 * t;
-            const int id = S.ni[t];
+            int id = S.ni[t];
+            if (id == INT_MAX) S.ni[t] = id = -1;  // no node (nn_brute)
             double best = S.nd[t];
             if (id >= 0 && best < 0.0) best = l2_dist64(s, J.states + 2 * id, 2);
             S.nd[t] = best;
@@ -476,8 +689,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
                 bucket_insert(J, S, s_bb, id);
                 J.parent[id] = S.ni[t];
                 // GoalState::operator() (src/mpt/goal_state.hpp:64-69): d <= radius
-                const uint8_t g = (J.has_goal && dist64(MPTG_METRIC_L2, 2, 1.0, 1.0, nw, J.goal) <= J.goal_radius)
-                                      ? 1 : 0;
+                const uint8_t g = J.has_goal && goal_reached(nw, J.goal, J.goal_radius) ? 1 : 0;
                 J.goalf[id] = g;
                 if (g) atomicAdd(&s_goals, 1);
                 atomicMax(&s_maxabs, __float_as_int(maxabs_ru(nw[0], nw[1])));

@@ -15,8 +15,10 @@ struct BPlanCounters {
     // SM cycles of this run per phase: samples, nearest search, steer, link
     // set-up (thread per edge), link samples (warp per edge), insert
     unsigned long long cyc[6];
-    // FP64 fallbacks of this run: near ties of the nearest search, unsure
-    // interior samples (warps), step counts left to FP64
+    // FP64 fallbacks of this run: FP64 distances of the nearest search (the
+    // ring search's near ties; every candidate of the exhaustive search,
+    // winners included), unsure interior samples (warps), step counts left
+    // to FP64
     unsigned long long ties, unsure, steps64;
 };
 
@@ -47,11 +49,16 @@ struct BPlanJob {
     // cell_size from (cell_ox, cell_oy), gx * gy <= BPLAN_CELLS
     float cell_ox, cell_oy, cell_size, cell_inv;
     int gx, gy;
+    long long brute_pairs;          // W x nodes up to this: exhaustive nearest search (nn_brute)
 };
 
 #define BPLAN_THREADS 1024
 #define BPLAN_MAX_NODES 16384       // FP32 node copy in shared memory: 128 KB
 #define BPLAN_CELLS 4096            // bucket-grid cells (64 x 64 over the sampling box)
+// default of BPlanJob::brute_pairs: wavefronts with W x nodes up to this many
+// pairs search their nearest nodes exhaustively (nn_brute); larger ones by
+// rings of the bucket grid
+#define BPLAN_BRUTE_PAIRS (1LL << 24)
 
 // Runs njobs jobs (device array), one thread block each, on stream s.
 mptg_status bplan_launch(mptg_ctx* ctx, const BPlanJob* djobs, int njobs, int max_W, int max_cap, cudaStream_t s);

@@ -149,6 +149,8 @@ struct mptg_planner {
     uint8_t* bp_goalf = nullptr;        // [bp_cap]
     BPlanCounters* bp_ctr = nullptr;
     BPlanJob* bp_job = nullptr;
+    BPlanJob* bp_hjob = nullptr;        // pinned: the job's copy is asynchronous
+    long long bp_brute_pairs = BPLAN_BRUTE_PAIRS;
     BPlanCounters* bp_hctr = nullptr;   // pinned
     uint8_t* bp_hgoal = nullptr;        // pinned [bp_cap]
     uint64_t stat_bp_waves = 0;         // wavefronts run inside the block planner
@@ -637,6 +639,7 @@ static void planner_free(mptg_planner* p) {
         if (x) cudaFree(x);
     if (p->hbuf) cudaFreeHost(p->hbuf);
     if (p->hgoal) cudaFreeHost(p->hgoal);
+    if (p->bp_hjob) cudaFreeHost(p->bp_hjob);
     if (p->bp_hctr) cudaFreeHost(p->bp_hctr);
     if (p->bp_hgoal) cudaFreeHost(p->bp_hgoal);
     scratch_free(&p->scratch);
@@ -994,6 +997,7 @@ static mptg_status bp_alloc(mptg_planner* p) {
     if (e == cudaSuccess) e = cudaMalloc((void**)&p->bp_goalf, cap);
     if (e == cudaSuccess) e = cudaMalloc((void**)&p->bp_ctr, sizeof(BPlanCounters));
     if (e == cudaSuccess) e = cudaMalloc((void**)&p->bp_job, sizeof(BPlanJob));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&p->bp_hjob, sizeof(BPlanJob));
     if (e == cudaSuccess) e = cudaMallocHost((void**)&p->bp_hctr, sizeof(BPlanCounters));
     if (e == cudaSuccess) e = cudaMallocHost((void**)&p->bp_hgoal, cap);
     if (e != cudaSuccess) {
@@ -1045,6 +1049,7 @@ static mptg_status run_persistent(mptg_planner* p, int max_waves, double time_li
     j.max_waves = max_waves;
     j.stop_when_solved = stop_when_solved;
     j.deadline_ns = time_limit_s > 0 ? (uint64_t)(time_limit_s * 1e9) : 0;
+    j.brute_pairs = p->bp_brute_pairs;
     {
         // 64 x 64 cells over the sampling box (square cells on its longer side)
         const double sx = p->hi_host[0] - p->lo_host[0], sy = p->hi_host[1] - p->lo_host[1];
@@ -1067,7 +1072,8 @@ static mptg_status run_persistent(mptg_planner* p, int max_waves, double time_li
         if ((st = mptg_tree_states(p->tree, 0, n0, p->bp_states, s))) return st;
         p->bp_n = n0;
     }
-    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_job, &j, sizeof(j), cudaMemcpyHostToDevice, s));
+    *p->bp_hjob = j;  // the previous run's copy ended at its synchronisation
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_job, p->bp_hjob, sizeof(j), cudaMemcpyHostToDevice, s));
     MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_ctr, h, sizeof(*h), cudaMemcpyHostToDevice, s));
     MPTG_CUDA_TRY(ctx, cudaEventRecord(p->ev[0], s));
     if ((st = bplan_launch(ctx, p->bp_job, 1, W, p->bp_cap, s))) return st;
@@ -1116,6 +1122,12 @@ extern "C" {
 mptg_status mptg_planner_set_persistent(mptg_planner* p, int mode) {
     if (!p || mode < 0 || mode > 1) return MPTG_ERR_INVALID_ARG;
     p->bp_mode = mode;
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_set_block_search(mptg_planner* p, long long brute_pairs) {
+    if (!p || brute_pairs < 0) return MPTG_ERR_INVALID_ARG;
+    p->bp_brute_pairs = brute_pairs;
     return MPTG_OK;
 }
 

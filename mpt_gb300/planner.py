@@ -138,6 +138,7 @@ def _sig(L):
         ("mptg_planner_graph", ctypes.c_int, [P, P, P, S, ctypes.POINTER(S)]),
         ("mptg_planner_tree", ctypes.c_int, [P, ctypes.POINTER(P)]),
         ("mptg_planner_set_persistent", ctypes.c_int, [P, ctypes.c_int]),
+        ("mptg_planner_set_block_search", ctypes.c_int, [P, ctypes.c_longlong]),
         ("mptg_planner_stats", ctypes.c_int, [P, P]),
         ("mptg_planner_timers", ctypes.c_int, [P, P]),
         ("mptg_planner_block_profile", ctypes.c_int, [P, P]),
@@ -188,6 +189,7 @@ class Planner:
         self._starts = []
         self._surrogate = None
         self._persistent = 1
+        self._brute_pairs = None
         self.scene = Scene(self.ctx, scenario.desc)
         self.h = None
 
@@ -198,6 +200,14 @@ class Planner:
         self._persistent = 1 if on else 0
         if self.h is not None:
             _check(self.ctx.h, self.lib.mptg_planner_set_persistent(self.h, self._persistent))
+
+    def set_block_search(self, brute_pairs: int):
+        """The block planner's nearest search: wavefronts with W x nodes up to
+        brute_pairs sweep every node, larger ones search a bucket grid; the
+        answers are the same (mptg_planner_set_block_search)."""
+        self._brute_pairs = int(brute_pairs)
+        if self.h is not None:
+            _check(self.ctx.h, self.lib.mptg_planner_set_block_search(self.h, self._brute_pairs))
 
     def set_surrogate(self, surrogate, threshold: float = 0.0, points: int = 1, candidates: int = 1):
         """Cull edges the surrogate scores above `threshold` (collision logit)
@@ -280,6 +290,8 @@ class Planner:
                                                         sc.lo.ctypes.data, sc.hi.ctypes.data, ctypes.byref(h)))
         self.h = h
         _check(self.ctx.h, self.lib.mptg_planner_set_persistent(h, self._persistent))
+        if self._brute_pairs is not None:
+            _check(self.ctx.h, self.lib.mptg_planner_set_block_search(h, self._brute_pairs))
         g = np.ascontiguousarray(sc.goal.state, dtype=np.float64)
         _check(self.ctx.h, self.lib.mptg_planner_set_goal(h, g.ctypes.data, sc.goal.radius))
         if self.algorithm.rewire:
@@ -298,24 +310,28 @@ class Planner:
                                                      int(stop_when_solved), ctypes.byref(solved)))
         return bool(solved.value)
 
-    # wavefronts per call between polls of done_fn: each call also stops at the
-    # first solution, so a solve until solved() ends on the wavefront that finds it
-    POLL_WAVEFRONTS = 16
+    # seconds of wavefronts per call between polls of done_fn: each call also
+    # stops at the first solution, so a solve until solved() ends on the
+    # wavefront that finds it; a call runs at least one wavefront
+    POLL_SECONDS = 0.005
 
     def solve(self, done_fn, deadline: float | None = None):
         """Runs wavefronts until done_fn() is true: polled between calls of up
-        to POLL_WAVEFRONTS wavefronts, each of which ends early at the first
-        solution or at the deadline (time.monotonic())."""
+        to POLL_SECONDS of wavefronts, each of which ends early at the first
+        solution or at the deadline (time.monotonic()), or when the node
+        budget is reached."""
         if self.size() == 0:
             raise RuntimeError("there are no valid initial states")
         self._create()
         while not done_fn():
-            before = self.stats()["wavefront_counter"]
-            left = 0.0 if deadline is None else deadline - time.monotonic()
-            if deadline is not None and left <= 0:
-                break
-            self.run(self.POLL_WAVEFRONTS, time_limit=left, stop_when_solved=not self.solved())
-            if self.stats()["wavefront_counter"] == before:  # node budget exhausted
+            limit = self.POLL_SECONDS
+            if deadline is not None:
+                left = deadline - time.monotonic()
+                if left <= 0:
+                    break
+                limit = min(limit, left)
+            self.run(0, time_limit=limit, stop_when_solved=not self.solved())
+            if self.size() >= self.max_nodes:  # node budget reached
                 break
 
     def solve_for(self, seconds: float, done_fn=None):
@@ -636,7 +652,7 @@ def _cache_store(path: str, key: str, best: int, med: dict):
     os.replace(tmp, path)
 
 
-def autotune_wavefront(ctx: Context, scenario: Scenario, start, candidates=(64, 128, 256, 512, 1024, 2048, 4096, 8192),
+def autotune_wavefront(ctx: Context, scenario: Scenario, start, candidates=(32, 48, 64, 128, 256, 512, 1024, 2048, 4096, 8192),
                        trials: int = 3, time_limit: float = 2.0, seed: int = 1, max_nodes: int = 1 << 21,
                        goal_bias: float = 0.01, range_: float | None = None, cache: str | None = None):
     """Native wavefront-size autotuner (mptg_autotune_wavefront): the size with

@@ -51,6 +51,23 @@ def test_block_planner_replays_oracle(ctx, orc, W, waves):
     pl.close()
 
 
+@pytest.mark.parametrize("brute_pairs", [0, 1 << 40])
+def test_block_planner_nearest_searches_agree(ctx, orc, brute_pairs):
+    """The bucket-grid ring search (brute_pairs 0) and the exhaustive sweep
+    (every wavefront) each build the oracle's tree."""
+    sc = scenes.grid_scene()
+    for W, waves in ((32, 50), (512, 10)):
+        pl = _planner(ctx, sc, W, 41, 1 << 20)
+        pl.set_block_search(brute_pairs)
+        pl.run(waves)
+        states, parents = pl.graph()
+        ws, wp, wg = _oracle(orc, sc, W, 41, 1 << 20, waves, False)
+        assert len(ws) > 100
+        assert _same(states, ws) and np.array_equal(parents, wp)
+        assert pl.stats()["goals"] == len(wg)
+        pl.close()
+
+
 def test_block_planner_equals_multi_kernel_until_solved(ctx):
     """Solved runs (stop at the first solution, goal sample on): the block
     planner and the multi-kernel path return the same tree, path, cost and
