@@ -322,6 +322,39 @@ def _solve_stats(ctx, sc, W, seeds, cap_s, surrogate=None, points=1, want_path=F
 SOLVE_SCENES = [("grid_1024", "grid_scene", 2048), ("arm_10link", "arm_scene", 4096), ("se3_mesh", "mesh_scene", 4096)]
 
 
+def block_planner_sweep(ctx, widths=(32, 48, 64, 128), seeds=10, cap_s=20.0):
+    """The persistent block planner (k_bplan_grid) on the grid: time to the first
+    solution per wavefront size, with its wavefronts, its kernel time per
+    wavefront and the split of that time over the phases (the block's own
+    SM-cycle counters, at the bench's measured clock)."""
+    from mpt_gb300 import planner as P
+    from mpt_gb300 import scenes
+    sc = scenes.grid_scene()
+    out = {}
+    for W in widths:
+        times, waves, prof = [], [], []
+        for s in range(seeds):
+            pl = P.Planner(P.Scenario(sc), P.PRRT(P.gpu_wavefront(W)), seed=1000 + s, ctx=ctx, max_nodes=1 << 21)
+            pl.add_start(sc["start"])
+            pl.prepare()
+            t0 = time.perf_counter()
+            pl.solve_for(cap_s, lambda: pl.solved())
+            dt = time.perf_counter() - t0
+            if pl.solved():
+                times.append(dt)
+            waves.append(pl.stats()["wavefronts"])
+            prof.append(pl.block_profile())
+            pl.close()
+        tot = {k: sum(p[k] for p in prof) for k in prof[0]}
+        cyc = sum(v for k, v in tot.items() if k.startswith("cyc_"))
+        out[str(W)] = {"p50_s": statistics.median(times) if times else None, "solved": len(times), "seeds": seeds,
+                       "median_wavefronts": statistics.median(waves),
+                       "kernel_cycles_per_wavefront": cyc / max(1.0, sum(waves)),
+                       "phase_share": {k[4:]: round(v / cyc, 3) for k, v in tot.items() if k.startswith("cyc_") and cyc},
+                       "fp64_fallbacks": {k: int(v) for k, v in tot.items() if not k.startswith("cyc_")}}
+    return out
+
+
 def solve_times(ctx, seeds=None, cap_s=20.0, tune=True):
     """Wall time to the first solution of the plain wavefront planner per scene
     (p50 over seeds 1000..), at the default wavefront and at the one the native
@@ -449,10 +482,15 @@ def surrogate_rates(ctx, m, torch, n_train=1 << 22, epochs=10):
     for _ in range(3):
         sg.lib.mptg_surrogate_score(sg.h, dq.data_ptr(), len(qt), dz.data_ptr(), stream.cuda_stream)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nvtx = getattr(torch.cuda, "nvtx", None)
+    if nvtx is not None:  # lets a profiler pick these launches (ncu --nvtx --nvtx-include sg_score/)
+        nvtx.range_push("sg_score")
     e0.record(stream)
     for _ in range(10):
         sg.lib.mptg_surrogate_score(sg.h, dq.data_ptr(), len(qt), dz.data_ptr(), stream.cuda_stream)
     e1.record(stream)
+    if nvtx is not None:
+        nvtx.range_pop()
     torch.cuda.synchronize()
     score_s = e0.elapsed_time(e1) / 1000.0 / 10
     flops_fwd = 2.0 * (7 * 256 + 3 * 256 * 256 + 256)
@@ -598,7 +636,7 @@ def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0, wave_for=None, surr
     """Config of the serving benchmark: n queries uniform over the three scenes,
     start and goal rejection-sampled valid, node budgets log-uniform in
     [1k, 200k]; wavefront = the scene's autotuned size (wave_for[kind]) when
-    given, else budget/16, clipped to [256, 4096] and to the budget/4."""
+    given, else budget/16 clipped to [256, 4096]; at most budget/4."""
     from mpt_gb300 import planner as P
     from mpt_gb300 import scenes
     from mpt_gb300.batch import Query
@@ -625,8 +663,8 @@ def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0, wave_for=None, surr
         a, b = pools[k][used[k]], pools[k][used[k] + 1]
         used[k] += 2
         budget = int(round(math.exp(rng.uniform(math.log(1000), math.log(200000)))))
-        W = wave_for[d["kind"]] if wave_for else budget // 16
-        W = int(min(4096, budget // 4, max(256, W)))
+        W = wave_for[d["kind"]] if wave_for else min(4096, max(256, budget // 16))
+        W = int(max(1, min(W, budget // 4)))
         sc = P.Scenario(d, P.GoalState(d["goal_radius"], b))
         q = Query(sc, a, seed=seed + i, max_nodes=budget, wavefront=W, time_limit=time_limit)
         if surrogate is not None and d["kind"] == "mesh":  # the surrogate is trained on the SE(3) scene
@@ -638,9 +676,9 @@ def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0, wave_for=None, surr
 def batch_serving(m, ctx, n=512, concurrency=8, seq_sample=64, wave_for=None, surrogate=None):
     """Batched multi-query serving: queries/s and time to solution over n queries
     with `concurrency` concurrent planners, against the same planner running the
-    queries one after another (on the first seq_sample queries).  Grid queries
-    run as persistent block planners; with a surrogate, the SE(3) queries use
-    surrogate-biased sampling and culling."""
+    queries one after another (on the first seq_sample queries).  The grid
+    queries run together as one persistent launch, a thread block each; with a
+    surrogate, the SE(3) queries use surrogate-biased sampling and culling."""
     from mpt_gb300.batch import plan_batch
     qs = batch_queries(m, ctx, n, wave_for=wave_for, surrogate=surrogate)
     plan_batch(ctx, qs[:8], concurrency=concurrency)  # warm-up: planners, kernels
@@ -722,7 +760,8 @@ def run_gpu(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     ctx = m.Context(local)
-    if args.edges_only or args.solve_only or args.star_only or args.prm_only or args.sg_only or args.nn1m_only:
+    if (args.edges_only or args.solve_only or args.star_only or args.prm_only or args.sg_only or args.nn1m_only
+            or args.bplan_only):
         # profiling modes: one secondary section alone
         if args.nn1m_only:
             out = {"nn_1m": nn_1m_section(ctx, m, torch)}
@@ -734,6 +773,8 @@ def run_gpu(args):
             out = {"pprm": prm_section(ctx)}
         elif args.sg_only:
             out = {"surrogate": surrogate_rates(ctx, m, torch, n_train=1 << 18, epochs=1)[0]}
+        elif args.bplan_only:
+            out = {"block_planner": block_planner_sweep(ctx, seeds=args.solve_seeds or 10)}
         else:
             out = {"time_to_solve": solve_times(ctx, seeds=args.solve_seeds)}
             if not args.no_ref_planners:
@@ -835,6 +876,8 @@ def run_gpu(args):
     edges = edge_rates(ctx, m, stream, torch)
     _progress("time to solve")
     solves = solve_times(ctx) if not args.no_solve else None
+    _progress("block planner sweep")
+    bplan = block_planner_sweep(ctx) if not args.no_solve else None
     w_se3 = solves["se3_mesh"]["autotune"]["best"] if solves and "autotune" in solves["se3_mesh"] else None
     _progress("learned surrogate")
     learned, sg = (learned_vs_plain(ctx, m, torch, wavefront_tuned=w_se3)
@@ -922,7 +965,7 @@ def run_gpu(args):
                                 "reference_kind": "the reference's DiscreteMotionValidator over the oracle's valid(), "
                                                   "all host cores"},
                 "time_to_solve": {"unit": "s", "planner": "plain wavefront PRRT (GPU)", "per_scene": solves,
-                                  "reference_planners": ref_plans},
+                                  "reference_planners": ref_plans, "block_planner_grid": bplan},
                 "learned_surrogate_se3": learned,
                 "batch_serving": serving,
                 "prrt_star": star,
@@ -957,6 +1000,7 @@ def main():
     ap.add_argument("--sg-only", action="store_true",
                     help="surrogate training (262,144 states, 1 epoch) and scoring rates only (profiling)")
     ap.add_argument("--edges-only", action="store_true", help="edge checks/s of the three scenes only (profiling)")
+    ap.add_argument("--bplan-only", action="store_true", help="the block planner's wavefront sweep only (profiling)")
     ap.add_argument("--solve-only", action="store_true", help="time to solve of the three scenes only (profiling)")
     ap.add_argument("--solve-seeds", type=int, default=None, help="seeds per scene (default grid 20, arm 10, SE(3) 20)")
     ap.add_argument("--ref-plan-child", nargs=5, default=None, help=argparse.SUPPRESS)

@@ -339,9 +339,14 @@ mptg_status mptg_planner_reset(mptg_planner* planner, const mptg_plan_params* pa
  * Many independent planning queries (one start, one GoalState each) over
  * shared scenes.  `concurrency` host workers (<= 0: 8) each own one CUDA
  * stream and reuse one planner per scene between queries, so the wavefronts
- * of different queries overlap on the GPU.  A query's planner behaves exactly
- * as mptg_planner_create + add_start + set_goal + run(stop_when_solved)
- * with the same parameters: the same seed gives the same tree and path. */
+ * of different queries overlap on the GPU.  The grid queries that the
+ * persistent block planner takes (resolution 0, wavefront <= 1,024, no
+ * surrogate) do not use the workers: they run together as one launch, one
+ * thread block per query, while the workers take the rest; a query whose block
+ * fills its 16,384 nodes unsolved is then run from its start by a worker.  A
+ * query behaves exactly as mptg_planner_create + add_start + set_goal +
+ * run(stop_when_solved) with the same parameters: the same seed gives the
+ * same tree and path. */
 typedef struct {
     mptg_scene* scene;
     const double* start;        /* [dim], host */

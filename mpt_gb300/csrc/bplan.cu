@@ -717,6 +717,8 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
         J.ctr->ties = s_prof[0];
         J.ctr->unsure = s_prof[1];
         J.ctr->steps64 = s_prof[2];
+        J.ctr->start_ns = t0;
+        J.ctr->end_ns = umma::globaltimer_ns();
         if (J.nsamp) atomicAdd(J.nsamp, s_cnt);
     }
 }

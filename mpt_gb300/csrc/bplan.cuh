@@ -20,6 +20,8 @@ struct BPlanCounters {
     // winners included), unsure interior samples (warps), step counts left
     // to FP64
     unsigned long long ties, unsure, steps64;
+    // the device's global timer (ns) when the block started and when it ended
+    unsigned long long start_ns, end_ns;
 };
 
 enum { BPLAN_DONE = 0, BPLAN_FULL = 1 };  // FULL: the next wavefront could overflow the block's node capacity

@@ -1012,6 +1012,20 @@ static bool bp_applies(const mptg_planner* p) {
     return p->bp_mode && !p->star && !p->sg && bplan_supported(p->scene, p->prm.wavefront, p->prm.resolution);
 }
 
+// the ring search's bucket grid: 64 x 64 cells over the sampling box (square
+// cells on its longer side)
+static void bp_cells(BPlanJob& j, const double* lo, const double* hi) {
+    const double sx = hi[0] - lo[0], sy = hi[1] - lo[1];
+    double cs = std::max(sx, sy) / 64.0;
+    if (!(cs > 0) || !std::isfinite(cs)) cs = 1.0;
+    j.cell_size = (float)cs;
+    j.cell_inv = (float)(1.0 / cs);
+    j.cell_ox = (float)lo[0];
+    j.cell_oy = (float)lo[1];
+    j.gx = std::max(1, std::min(64, (int)std::ceil(sx / cs)));
+    j.gy = std::max(1, std::min(64, (int)std::ceil(sy / cs)));
+}
+
 // Wavefronts inside the persistent block planner until a stop condition
 // (solved, node budget, wavefront count, time) or its node capacity; then the
 // kd-tree takes the new nodes and the host its goals.  *waves: wavefronts run.
@@ -1050,18 +1064,7 @@ static mptg_status run_persistent(mptg_planner* p, int max_waves, double time_li
     j.stop_when_solved = stop_when_solved;
     j.deadline_ns = time_limit_s > 0 ? (uint64_t)(time_limit_s * 1e9) : 0;
     j.brute_pairs = p->bp_brute_pairs;
-    {
-        // 64 x 64 cells over the sampling box (square cells on its longer side)
-        const double sx = p->hi_host[0] - p->lo_host[0], sy = p->hi_host[1] - p->lo_host[1];
-        double cs = std::max(sx, sy) / 64.0;
-        if (!(cs > 0) || !std::isfinite(cs)) cs = 1.0;
-        j.cell_size = (float)cs;
-        j.cell_inv = (float)(1.0 / cs);
-        j.cell_ox = (float)p->lo_host[0];
-        j.cell_oy = (float)p->lo_host[1];
-        j.gx = std::max(1, std::min(64, (int)std::ceil(sx / cs)));
-        j.gy = std::max(1, std::min(64, (int)std::ceil(sy / cs)));
-    }
+    bp_cells(j, p->lo_host, p->hi_host);
     BPlanCounters* h = p->bp_hctr;
     *h = BPlanCounters{};
     h->n = (int)n0;
@@ -1607,6 +1610,218 @@ static mptg_status batch_query(mptg_ctx* ctx, const mptg_query& q, const BatchCa
     return planner_solution(p, q.path, q.path_cap, &r.path_len, &r.cost, false);
 }
 
+// ---- the grid queries of a batch as one persistent launch
+// The batch's grid queries that the block planner takes (a grid scene at
+// resolution 0, W <= 1024, no surrogate) run together: one k_bplan_grid block
+// per query, all in one launch on a stream of their own, while the host
+// workers take the other queries.  Each block runs exactly the wavefronts a
+// single planner runs (run_persistent with stop_when_solved), so it builds
+// the same tree, and the solution is read as planner_solution reads it
+// (k_plan_path over the goals, newest first, strict <).  A query whose block
+// fills its 16,384 nodes unsolved goes back to the workers, which run it from
+// its start (the same tree again, so the same answer; only the block's time
+// is lost).
+struct GridBatch {
+    std::vector<size_t> idx;        // query indices, one block each
+    std::vector<size_t> retry;      // queries the workers must run (capacity reached)
+    std::vector<BPlanJob> jobs;
+    std::vector<size_t> off;        // arena offset of each job's buffers
+    unsigned char* arena = nullptr;
+    BPlanCounters* hctr = nullptr;  // pinned
+    cudaStream_t s = nullptr;
+    std::chrono::steady_clock::time_point t_launch;
+    int maxW = 0, maxcap = 0;
+    size_t ctr_off = 0, job_off = 0, scratch_off = 0;
+};
+
+static bool grid_batch_eligible(const mptg_query& q) {
+    if (q.surrogate || q.params.max_nodes < 1) return false;
+    if (!bplan_supported(q.scene, q.params.wavefront, q.params.resolution)) return false;
+    for (int d = 0; d < 2; ++d)
+        if (!std::isfinite(q.start[d]) || !std::isfinite(q.goal[d])) return false;
+    return true;
+}
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// each job's node 0 (the start, no parent, no goal flag) and its goal and
+// sampling bounds, from rec[k] = start, goal, lo, hi (8 doubles)
+__global__ void k_gb_init(const BPlanJob* __restrict__ jobs, int K, const double* __restrict__ rec) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    const BPlanJob& j = jobs[k];
+    const double* r = rec + 8 * (size_t)k;
+    j.states[0] = r[0];
+    j.states[1] = r[1];
+    j.parent[0] = -1;
+    j.goalf[0] = 0;
+    double* v = const_cast<double*>(j.goal);  // goal, lo, hi: 6 doubles in the job's buffers
+    for (int i = 0; i < 6; ++i) v[i] = r[2 + i];
+}
+
+static void grid_batch_free(GridBatch& g) {
+    if (g.s) cudaStreamSynchronize(g.s);
+    if (g.arena) cudaFree(g.arena);
+    if (g.hctr) cudaFreeHost(g.hctr);
+    if (g.s) cudaStreamDestroy(g.s);
+    g.arena = nullptr;
+    g.hctr = nullptr;
+    g.s = nullptr;
+}
+
+// buffers, jobs and the launch (asynchronous)
+static mptg_status grid_batch_launch(mptg_ctx* ctx, const mptg_query* qs, GridBatch& g) {
+    const size_t K = g.idx.size();
+    size_t o = 0;
+    g.off.resize(K);
+    for (size_t k = 0; k < K; ++k) {
+        const mptg_query& q = qs[g.idx[k]];
+        const int cap = (int)std::min<size_t>(q.params.max_nodes, BPLAN_MAX_NODES);
+        g.maxcap = std::max(g.maxcap, cap);
+        g.maxW = std::max(g.maxW, q.params.wavefront);
+        g.off[k] = o;  // states [cap][2], parent [cap], goal flags [cap], goal / lo / hi
+        o += align256((size_t)cap * 16) + align256((size_t)cap * 4) + align256((size_t)cap) + 256;
+    }
+    g.ctr_off = o;
+    o += align256(K * sizeof(BPlanCounters));
+    g.job_off = o;
+    o += align256(K * sizeof(BPlanJob));
+    g.scratch_off = o;  // k_plan_path: cost and length, path ids, gathered states
+    o += 256 + align256((size_t)g.maxcap * 4) + align256((size_t)g.maxcap * 16);
+    const size_t rec_off = o;  // the jobs' start, goal and bounds for k_gb_init
+    o += align256(K * 8 * sizeof(double));
+    cudaError_t e = cudaMalloc((void**)&g.arena, o);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&g.hctr, K * sizeof(BPlanCounters));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g.s, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return mptg_fail(ctx, MPTG_ERR_OOM, "batch of grid queries: %s", cudaGetErrorString(e));
+    }
+    std::vector<double> rec(K * 8);
+    g.jobs.resize(K);
+    for (size_t k = 0; k < K; ++k) {
+        const mptg_query& q = qs[g.idx[k]];
+        const mptg_plan_params& prm = q.params;
+        const int cap = (int)std::min<size_t>(prm.max_nodes, BPLAN_MAX_NODES);
+        unsigned char* base = g.arena + g.off[k];
+        const size_t o_par = align256((size_t)cap * 16), o_gf = o_par + align256((size_t)cap * 4),
+                     o_vec = o_gf + align256((size_t)cap);
+        double* vec = rec.data() + 8 * k + 2;  // goal, lo, hi: the planner's bounds rule (set_bounds)
+        rec[8 * k] = q.start[0];
+        rec[8 * k + 1] = q.start[1];
+        for (int d = 0; d < 2; ++d) {
+            vec[d] = q.goal[d];
+            vec[2 + d] = q.lo ? q.lo[d] : 0.0;
+            vec[4 + d] = q.hi ? q.hi[d] : 1.0;
+        }
+        BPlanJob& j = g.jobs[k];
+        j = BPlanJob{};
+        j.scene = scene_view(q.scene);
+        j.goal = reinterpret_cast<const double*>(base + o_vec);
+        j.lo = j.goal + 2;
+        j.hi = j.goal + 4;
+        j.has_goal = 1;
+        j.goal_bias = prm.goal_bias;
+        j.range = prm.range > 0 ? prm.range : INFINITY;
+        j.goal_radius = q.goal_radius;
+        j.inv_step = 1.0 / prm.edge_step;
+        j.seed = prm.seed;
+        j.states = reinterpret_cast<double*>(base);
+        j.parent = reinterpret_cast<int*>(base + o_par);
+        j.goalf = base + o_gf;
+        j.ctr = reinterpret_cast<BPlanCounters*>(g.arena + g.ctr_off) + k;
+        j.nsamp = nullptr;
+        j.max_nodes = prm.max_nodes;
+        j.cap = cap;
+        j.W = prm.wavefront;
+        j.max_waves = 0;
+        j.stop_when_solved = 1;
+        j.deadline_ns = q.time_limit_s > 0 ? (uint64_t)(q.time_limit_s * 1e9) : 0;
+        j.brute_pairs = BPLAN_BRUTE_PAIRS;
+        bp_cells(j, vec + 2, vec + 4);
+        g.hctr[k] = BPlanCounters{};
+        g.hctr[k].n = 1;
+    }
+    // pageable copies are staged before they return, so `rec` may go
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(g.arena + rec_off, rec.data(), rec.size() * sizeof(double),
+                                       cudaMemcpyHostToDevice, g.s));
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(g.arena + g.ctr_off, g.hctr, K * sizeof(BPlanCounters), cudaMemcpyHostToDevice,
+                                       g.s));
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(g.arena + g.job_off, g.jobs.data(), K * sizeof(BPlanJob),
+                                       cudaMemcpyHostToDevice, g.s));
+    k_gb_init<<<mptg_blocks(K, 128), 128, 0, g.s>>>(reinterpret_cast<const BPlanJob*>(g.arena + g.job_off), (int)K,
+                                                   reinterpret_cast<const double*>(g.arena + rec_off));
+    MPTG_LAUNCHED(ctx);
+    g.t_launch = std::chrono::steady_clock::now();
+    mptg_status st = bplan_launch(ctx, reinterpret_cast<const BPlanJob*>(g.arena + g.job_off), (int)K, g.maxW,
+                                  g.maxcap, g.s);
+    if (st) return st;
+    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(g.hctr, g.arena + g.ctr_off, K * sizeof(BPlanCounters), cudaMemcpyDeviceToHost,
+                                       g.s));
+    return MPTG_OK;
+}
+
+// waits for the launch and fills the results; queries to run again go to g.retry
+static mptg_status grid_batch_finish(mptg_ctx* ctx, const mptg_query* qs, GridBatch& g, mptg_result* out,
+                                     std::chrono::steady_clock::time_point t0) {
+    MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(g.s));
+    const size_t K = g.idx.size();
+    unsigned long long first = ~0ull;
+    for (size_t k = 0; k < K; ++k) first = std::min(first, g.hctr[k].start_ns);
+    const double launch_s = std::chrono::duration<double>(g.t_launch - t0).count();
+    double hd[2];
+    std::vector<uint8_t> gf;
+    mptg_status st = MPTG_OK;
+    for (size_t k = 0; k < K && !st; ++k) {
+        const BPlanCounters& h = g.hctr[k];
+        const mptg_query& q = qs[g.idx[k]];
+        if (h.status == BPLAN_FULL && h.goals == 0) {
+            g.retry.push_back(g.idx[k]);
+            continue;
+        }
+        mptg_result& r = out[g.idx[k]];
+        r = mptg_result{};
+        r.cost = INFINITY;
+        r.solved = h.goals > 0;
+        r.nodes = (size_t)h.n;
+        r.wavefronts = (size_t)h.waves_run;
+        // from the launch's first block to this block's end: a query that
+        // waited for a free SM counts its wait
+        r.solve_s = 1e-9 * (double)(h.end_ns - first);
+        r.finish_s = launch_s + r.solve_s;
+        if (!r.solved) continue;
+        const BPlanJob& j = g.jobs[k];
+        gf.resize((size_t)h.n);
+        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(gf.data(), j.goalf, (size_t)h.n, cudaMemcpyDeviceToHost, g.s));
+        MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(g.s));
+        double* sc = reinterpret_cast<double*>(g.arena + g.scratch_off);
+        int* ids = reinterpret_cast<int*>(g.arena + g.scratch_off + 256);
+        double* gath = reinterpret_cast<double*>(g.arena + g.scratch_off + 256 + align256((size_t)g.maxcap * 4));
+        double best = INFINITY;
+        int bestg = -1, bestlen = 0;
+        for (int i = h.n; i-- > 1;) {  // goals newest first, strict < (planner_solution); 0 is the start
+            if (!gf[i]) continue;
+            k_plan_path<<<1, 1, 0, g.s>>>(i, j.parent, j.states, 2, MPTG_METRIC_L2, 1.0, 1.0, 0, nullptr, sc);
+            MPTG_LAUNCHED(ctx);
+            MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(hd, sc, 2 * sizeof(double), cudaMemcpyDeviceToHost, g.s));
+            MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(g.s));
+            if (hd[0] < best || bestg < 0) { best = hd[0]; bestg = i; bestlen = (int)hd[1]; }
+        }
+        r.cost = best;
+        r.path_len = (size_t)bestlen;
+        if (q.path && (size_t)bestlen <= q.path_cap) {
+            k_plan_path<<<1, 1, 0, g.s>>>(bestg, j.parent, j.states, 2, MPTG_METRIC_L2, 1.0, 1.0, bestlen, ids, sc);
+            MPTG_LAUNCHED(ctx);
+            k_plan_gather<<<mptg_blocks(bestlen * 2, 256), 256, 0, g.s>>>(ids, bestlen, j.states, 2, gath);
+            MPTG_LAUNCHED(ctx);
+            MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(q.path, gath, (size_t)bestlen * 2 * sizeof(double), cudaMemcpyDefault,
+                                               g.s));
+            MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(g.s));
+        }
+    }
+    return st;
+}
+
 mptg_status mptg_plan_batch(mptg_ctx* ctx, const mptg_query* qs, size_t n, int concurrency, mptg_result* out) {
     if (!ctx) return MPTG_ERR_INVALID_ARG;
     if (n == 0) return MPTG_OK;
@@ -1624,35 +1839,64 @@ mptg_status mptg_plan_batch(mptg_ctx* ctx, const mptg_query* qs, size_t n, int c
         c.first = std::max(c.first, q.params.max_nodes);
         c.second = std::max(c.second, q.params.wavefront);
     }
+    MPTG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    // the grid queries the block planner takes run as one launch; the workers
+    // take the rest
+    GridBatch gb;
+    std::vector<size_t> rest;
+    for (size_t i = 0; i < n; ++i) (grid_batch_eligible(qs[i]) ? gb.idx : rest).push_back(i);
+    const auto t0 = std::chrono::steady_clock::now();
+    bool grid_launched = false;
+    if (!gb.idx.empty()) {
+        if (grid_batch_launch(ctx, qs, gb) == MPTG_OK) {
+            grid_launched = true;
+        } else {  // no room for the launch: the workers take these queries as well
+            grid_batch_free(gb);
+            rest.insert(rest.end(), gb.idx.begin(), gb.idx.end());
+            std::sort(rest.begin(), rest.end());
+        }
+    }
     size_t workers = concurrency > 0 ? (size_t)concurrency : 8;
-    workers = std::min(workers, n);
+    workers = std::max<size_t>(1, std::min(workers, rest.size()));
     std::atomic<size_t> next{0};
     std::mutex mu;
     mptg_status first = MPTG_OK;
-    const auto t0 = std::chrono::steady_clock::now();
-    auto work = [&]() {
+    auto one = [&](size_t i, std::map<mptg_scene*, mptg_planner*>& mine, bool dev_ok) {
+        mptg_result& r = out[i];
+        r = mptg_result{};
+        r.cost = INFINITY;
+        mptg_status st = dev_ok ? batch_query(ctx, qs[i], caps, mine, r)
+                                : mptg_fail(ctx, MPTG_ERR_CUDA, "cudaSetDevice failed in a batch worker");
+        r.status = st;
+        r.finish_s = seconds_since(t0);
+        if (st) {
+            std::lock_guard<std::mutex> lock(mu);
+            if (first == MPTG_OK) first = st;
+        }
+    };
+    auto work = [&](bool main_thread) {
         std::map<mptg_scene*, mptg_planner*> mine;
         const bool dev_ok = cudaSetDevice(ctx->device) == cudaSuccess;
-        for (size_t i; (i = next.fetch_add(1)) < n;) {
-            mptg_result& r = out[i];
-            r = mptg_result{};
-            r.cost = INFINITY;
-            mptg_status st = dev_ok ? batch_query(ctx, qs[i], caps, mine, r)
-                                    : mptg_fail(ctx, MPTG_ERR_CUDA, "cudaSetDevice failed in a batch worker");
-            r.status = st;
-            r.finish_s = seconds_since(t0);
+        if (main_thread && grid_launched) {
+            // the launch's results; the queries that filled their block run here
+            mptg_status st = grid_batch_finish(ctx, qs, gb, out, t0);
             if (st) {
                 std::lock_guard<std::mutex> lock(mu);
                 if (first == MPTG_OK) first = st;
+                for (size_t i : gb.idx) out[i].status = st;
+            } else {
+                for (size_t i : gb.retry) one(i, mine, dev_ok);
             }
         }
+        for (size_t k; (k = next.fetch_add(1)) < rest.size();) one(rest[k], mine, dev_ok);
         for (auto& kv : mine)
             if (kv.second) planner_free(kv.second);
     };
     std::vector<std::thread> pool;
-    for (size_t k = 1; k < workers; ++k) pool.emplace_back(work);
-    work();
+    for (size_t k = 1; k < workers; ++k) pool.emplace_back(work, false);
+    work(true);
     for (auto& th : pool) th.join();
+    grid_batch_free(gb);
     return first;
 }
 

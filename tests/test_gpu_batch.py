@@ -75,6 +75,28 @@ def test_batch_equals_single_planners(ctx, three):
         assert 0 < r["solve_s"] <= r["finish_s"]
 
 
+def test_batch_grid_queries_in_one_launch(ctx, three):
+    """More grid queries than SMs, run as one persistent launch (one block per
+    query): every one returns what a single planner returns, including the
+    ones whose budget or whose block's 16,384 nodes run out first."""
+    from mpt_gb300 import planner as P
+    from mpt_gb300.batch import Query, plan_batch
+    sc = three["grid"]
+    scen = P.Scenario(sc)
+    qs = []
+    for i in range(170):
+        W = (32, 48, 64, 128, 1000)[i % 5]
+        budget = (400, 3000, 20000)[i % 3] if W < 1000 else 30000
+        qs.append(Query(scen, sc["start"], seed=900 + i, max_nodes=budget, wavefront=W, goal_bias=0.05))
+    res = plan_batch(ctx, qs, concurrency=4)
+    assert all(r["status"] == 0 for r in res)
+    assert sum(r["solved"] for r in res) > 50 and not all(r["solved"] for r in res)
+    for q, r in zip(qs, res):
+        _same(r, _single(ctx, q))
+        assert r["nodes"] <= q.max_nodes
+        assert 0 < r["solve_s"] <= r["finish_s"]
+
+
 def test_batch_with_surrogate_equals_single(ctx, three):
     from mpt_gb300.batch import plan_batch
     from mpt_gb300.surrogate import Surrogate, se3_normalisation
