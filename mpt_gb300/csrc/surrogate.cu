@@ -130,8 +130,10 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
 
 // The fused epilogue of 16 accumulator columns c .. c+15 of row m (v = the
 // FP32 sums), per EPI; `out` accumulates the scoring output layer.
+// bias and w4 are ep.bias and ep.w4, or copies of them in shared memory.
 template <int EPI>
-__device__ __forceinline__ void sg_epilogue16(const EpiArgs& ep, size_t m, int c, const float (&v)[16], float& out) {
+__device__ __forceinline__ void sg_epilogue16(const EpiArgs& ep, const float* bias, const float* w4, size_t m, int c,
+                                              const float (&v)[16], float& out) {
     if (EPI == EPI_GRAD) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) atomicAdd(&ep.G[m * ep.ldc + c + j], v[j]);
@@ -158,7 +160,7 @@ __device__ __forceinline__ void sg_epilogue16(const EpiArgs& ep, size_t m, int c
     } else {
         float z[16];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) z[j] = v[j] + __ldg(&ep.bias[c + j]);
+        for (int j = 0; j < 16; ++j) z[j] = v[j] + bias[c + j];
         if (EPI == EPI_FWD) {
             float4* zo = reinterpret_cast<float4*>(ep.Z + m * SG_W + c);
 #pragma unroll
@@ -168,7 +170,7 @@ __device__ __forceinline__ void sg_epilogue16(const EpiArgs& ep, size_t m, int c
 #pragma unroll
             for (int j = 0; j < 16; ++j)
                 out = fmaf(__bfloat162float(__float2bfloat16_rn(sg_silu(z[j]))),
-                           __bfloat162float(__float2bfloat16_rn(__ldg(&ep.w4[c + j]))), out);
+                           __bfloat162float(__float2bfloat16_rn(w4[c + j])), out);
         } else {
             uint32_t pk[8];
 #pragma unroll
@@ -280,7 +282,7 @@ __global__ void __launch_bounds__(128, 1) k_sg_umma(const __grid_constant__ CUte
         for (int c = 0; c < SG_W; c += 16) {
             float v[16];
             umma::tmem_ld16(trow + c, v);
-            sg_epilogue16<EPI>(ep, m, c, v, out);
+            sg_epilogue16<EPI>(ep, ep.bias, ep.w4, m, c, v, out);
         }
         if (EPI == EPI_SCORE_OUT) ep.zout[m] = out + __ldg(ep.b4);
     }
@@ -304,13 +306,25 @@ __global__ void __launch_bounds__(128, 1) k_sg_umma(const __grid_constant__ CUte
 //            then each tile's four A slices through a 4-stage ring
 //   warp 1   UMMA: per tile, 4 x 4 MMAs 128 x 256 x 16 into one of two TMEM
 //            accumulators (2 x 256 columns), then a commit to its `full` barrier
-//   warps 2-5 epilogue: TMEM lanes 32 (w % 4) .. +31, the fused per-row work of
-//            sg_epilogue16, then an arrive on the accumulator's `empty` barrier
-// so the epilogue of one tile overlaps the loads and UMMAs of the next.  All
-// waits are bounded as in k_sg_umma.
-#define SGP_THREADS 192
+//   warps 2-17 epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (the rows
+//            its lane group may access) and the 64 columns of quarter
+//            (w - 2) / 4, runs the fused per-row work of sg_epilogue16 on
+//            them, then arrives on the accumulator's `empty` barrier
+// so the epilogue of one tile overlaps the loads and UMMAs of the next.  The
+// epilogue is the long part of a tile (a sigmoid per element against 16 UMMAs
+// per tile), so four warps share each lane group and each SM sub-partition
+// holds four of them to hide their latencies.  The bias and output weights
+// are read from shared memory.  The scoring output layer's dot product is
+// summed per quarter; the quarter-0 warp adds the other three quarters'
+// partial sums (in quarter order, so every run gives the same bits) once a
+// `ready` barrier says they are written, and only then arrives on `empty`, so
+// the next tile on that accumulator cannot overwrite the partial sums early.
+// All waits are bounded as in k_sg_umma.
+#define SGP_EPI_WARPS 16
+#define SGP_THREADS (64 + 32 * SGP_EPI_WARPS)
 #define SGP_B_BYTES (4 * SG_W * SG_BK * 2)   // 128 KB of resident weights
-#define SGP_SMEM (SGP_B_BYTES + SG_STAGES * SG_A_BYTES + 1024 + 256)
+#define SGP_F_BYTES ((2 * SG_W + 2 * 4 * SG_TM) * 4)  // bias, w4, partial sums [2][4][128]
+#define SGP_SMEM (SGP_B_BYTES + SG_STAGES * SG_A_BYTES + SGP_F_BYTES + 1024 + 256)
 
 template <int EPI>
 __global__ void __launch_bounds__(SGP_THREADS, 1) k_sg_umma_p(const __grid_constant__ CUtensorMap ta,
@@ -323,12 +337,16 @@ __global__ void __launch_bounds__(SGP_THREADS, 1) k_sg_umma_p(const __grid_const
     uint8_t* smem = sg_smem_raw + (base - raw);
     uint8_t* sB = smem;                     // [4][256][64] bf16, swizzled
     uint8_t* sA = smem + SGP_B_BYTES;       // [stage][128][64] bf16, swizzled
-    uint64_t* bfull = reinterpret_cast<uint64_t*>(sA + SG_STAGES * SG_A_BYTES);
+    float* sbias = reinterpret_cast<float*>(sA + SG_STAGES * SG_A_BYTES);
+    float* sw4 = sbias + SG_W;
+    float* spart = sw4 + SG_W;              // [acc][quarter][row] output-layer partial sums
+    uint64_t* bfull = reinterpret_cast<uint64_t*>(spart + 2 * 4 * SG_TM);
     uint64_t* afull = bfull + 1;
     uint64_t* aempty = afull + SG_STAGES;
     uint64_t* accfull = aempty + SG_STAGES;
     uint64_t* accempty = accfull + 2;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(accempty + 2);
+    uint64_t* pready = accempty + 2;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(pready + 2);
     int* counts = reinterpret_cast<int*>(tslot + 1);  // [0] A slices loaded, [1] consumed, [2] weights loaded
     const int my_tiles = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     if (tid == 0) {
@@ -339,10 +357,15 @@ __global__ void __launch_bounds__(SGP_THREADS, 1) k_sg_umma_p(const __grid_const
         }
         for (int a = 0; a < 2; ++a) {
             umma::mbar_init(&accfull[a], 1);
-            umma::mbar_init(&accempty[a], 128);
+            umma::mbar_init(&accempty[a], 32 * SGP_EPI_WARPS);
+            umma::mbar_init(&pready[a], 32 * (SGP_EPI_WARPS - 4));
         }
         counts[0] = counts[1] = counts[2] = 0;
         umma::fence_mbar_init();
+    }
+    for (int i = tid; i < SG_W; i += SGP_THREADS) {
+        sbias[i] = ep.bias ? __ldg(&ep.bias[i]) : 0.f;
+        sw4[i] = ep.w4 ? __ldg(&ep.w4[i]) : 0.f;
     }
     if (warp == 0) {
         umma::tmem_alloc(tslot, 2 * SG_W);
@@ -415,8 +438,8 @@ __global__ void __launch_bounds__(SGP_THREADS, 1) k_sg_umma_p(const __grid_const
         }
         __syncwarp();
     } else {
-        // epilogue warps: lane group (warp % 4) of each accumulator
-        const int grp = warp & 3;
+        // epilogue warps: lane group (warp % 4), column quarter (warp - 2) / 4
+        const int grp = warp & 3, qtr = (warp - 2) >> 2, row = grp * 32 + lane;
         const uint32_t lane_off = (uint32_t)(grp * 32) << 16;
         for (int i = 0; i < my_tiles; ++i) {
             const int acc = i & 1;
@@ -427,16 +450,32 @@ __global__ void __launch_bounds__(SGP_THREADS, 1) k_sg_umma_p(const __grid_const
                 break;
             }
             umma::fence_after_sync();
-            const size_t m = (size_t)(((int)blockIdx.x + i * (int)gridDim.x) * SG_TM + grp * 32 + lane);
+            const size_t m = (size_t)(((int)blockIdx.x + i * (int)gridDim.x) * SG_TM + row);
             const uint32_t trow = tmem + lane_off + (uint32_t)(acc * SG_W);
             float out = 0.f;
-#pragma unroll 1
-            for (int c = 0; c < SG_W; c += 16) {
+#pragma unroll
+            for (int c = 64 * qtr; c < 64 * qtr + 64; c += 16) {
                 float v[16];
                 umma::tmem_ld16(trow + c, v);
-                sg_epilogue16<EPI>(ep, m, c, v, out);
+                sg_epilogue16<EPI>(ep, sbias, sw4, m, c, v, out);
             }
-            if (EPI == EPI_SCORE_OUT) ep.zout[m] = out + __ldg(ep.b4);
+            if (EPI == EPI_SCORE_OUT) {
+                float* part = spart + acc * 4 * SG_TM;
+                if (qtr) {
+                    part[qtr * SG_TM + row] = out;
+                    umma::mbar_arrive(&pready[acc]);  // release: the partial sum is written
+                } else {
+                    const bool got = umma::mbar_wait(&pready[acc], (i >> 1) & 1, deadline);
+                    if (got) {
+                        out += part[SG_TM + row];
+                        out += part[2 * SG_TM + row];
+                        out += part[3 * SG_TM + row];
+                        ep.zout[m] = out + __ldg(ep.b4);
+                    } else if (lane == 0) {
+                        atomicExch(err, 3);
+                    }
+                }
+            }
             umma::fence_before_sync();
             umma::mbar_arrive(&accempty[acc]);
         }
