@@ -379,10 +379,13 @@ typedef struct {
 /* Project-written autotuner for the wavefront size of one scene and query:
  * plans `trials` seeds (params->seed, +1, ...) from start to the goal for each
  * candidate size (stop at the first solution, time_limit_s each; unsolved
- * counts as the limit) and returns in *best the size with the lowest median
- * time to solution; median_s (ncand entries, may be NULL) receives the
- * medians.  The time to solution is governed by tree depth (wavefronts
- * needed) times per-wavefront latency, so the best size is scene-dependent. */
+ * counts as the limit), then 2 * trials more seeds for the three sizes with
+ * the lowest medians, and returns in *best the one of those three with the
+ * lowest median time to solution over all its seeds; median_s (ncand
+ * entries, may be NULL) receives each size's median over the seeds it ran.
+ * The time to solution is governed by tree depth (wavefronts needed) times
+ * per-wavefront latency, so the best size is scene-dependent; the second
+ * stage keeps a heavy-tailed scene's pick from resting on a few seeds. */
 mptg_status mptg_autotune_wavefront(mptg_ctx* ctx, mptg_scene* scene, const mptg_plan_params* params,
                                     const double* lo, const double* hi, const double* start, const double* goal,
                                     double goal_radius, const int* candidates, int ncand, int trials,

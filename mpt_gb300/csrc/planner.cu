@@ -22,6 +22,7 @@
 #include <atomic>
 #include <chrono>
 #include <map>
+#include <numeric>
 #include <thread>
 
 #define PLAN_SCAN_BLOCK 1024
@@ -1919,28 +1920,55 @@ mptg_status mptg_autotune_wavefront(mptg_ctx* ctx, mptg_scene* scene, const mptg
     mptg_planner* p = nullptr;
     mptg_status st = mptg_planner_create(ctx, scene, &cp, lo, hi, &p);
     if (st) return st;
-    double best_t = INFINITY;
-    *best = candidates[0];
-    for (int c = 0; c < ncand && !st; ++c) {
-        std::vector<double> ts;
-        for (int t = 0; t < trials && !st; ++t) {
+    // times to solution of `n` more seeds from seed offset `first` at size W
+    // (unsolved: the limit)
+    auto trial_times = [&](int W, int first, int n, std::vector<double>& ts) -> mptg_status {
+        for (int t = first; t < first + n; ++t) {
             mptg_plan_params q = *params;
-            q.wavefront = candidates[c];
+            q.wavefront = W;
             q.seed = params->seed + (uint64_t)t;
-            if ((st = planner_reset(p, &q, false, nullptr, nullptr))) break;
-            if ((st = mptg_planner_set_goal(p, goal, goal_radius))) break;
-            if ((st = mptg_planner_add_start(p, start))) break;
+            mptg_status r;
+            if ((r = planner_reset(p, &q, false, nullptr, nullptr))) return r;
+            if ((r = mptg_planner_set_goal(p, goal, goal_radius))) return r;
+            if ((r = mptg_planner_add_start(p, start))) return r;
             int solved = 0;
             const auto t0 = std::chrono::steady_clock::now();
-            if ((st = mptg_planner_run(p, 0, time_limit_s, 1, &solved))) break;
+            if ((r = mptg_planner_run(p, 0, time_limit_s, 1, &solved))) return r;
             const double dt = seconds_since(t0);
             ts.push_back(solved ? dt : std::max(dt, time_limit_s));
         }
-        if (st) break;
-        std::sort(ts.begin(), ts.end());
-        const double med = ts[ts.size() / 2];
-        if (median_s) median_s[c] = med;
-        if (med < best_t) { best_t = med; *best = candidates[c]; }
+        return MPTG_OK;
+    };
+    auto median = [](std::vector<double> v) {
+        std::sort(v.begin(), v.end());
+        return v[v.size() / 2];
+    };
+    // stage 1: `trials` seeds per candidate; stage 2: the three best get twice
+    // as many seeds more, and the lowest median over all their seeds wins
+    // (heavy-tailed scenes make a median of a few seeds noisy)
+    std::vector<std::vector<double>> times(ncand);
+    std::vector<double> med(ncand, INFINITY);
+    for (int c = 0; c < ncand && !st; ++c) {
+        st = trial_times(candidates[c], 0, trials, times[c]);
+        if (!st) med[c] = median(times[c]);
+    }
+    std::vector<int> order(ncand);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return med[a] < med[b]; });
+    for (int r = 0; r < std::min(3, ncand) && ncand > 1 && !st; ++r) {
+        const int c = order[r];
+        st = trial_times(candidates[c], trials, 2 * trials, times[c]);
+        if (!st) med[c] = median(times[c]);
+    }
+    double best_t = INFINITY;
+    *best = candidates[0];
+    for (int c = 0; c < ncand && !st; ++c) {
+        if (median_s) median_s[c] = med[c];
+        const bool finalist = ncand == 1 || times[c].size() > (size_t)trials;
+        if (finalist && med[c] < best_t) {
+            best_t = med[c];
+            *best = candidates[c];
+        }
     }
     planner_free(p);
     return st;

@@ -655,9 +655,11 @@ def _cache_store(path: str, key: str, best: int, med: dict):
 def autotune_wavefront(ctx: Context, scenario: Scenario, start, candidates=(32, 48, 64, 128, 256, 512, 1024, 2048, 4096, 8192),
                        trials: int = 3, time_limit: float = 2.0, seed: int = 1, max_nodes: int = 1 << 21,
                        goal_bias: float = 0.01, range_: float | None = None, cache: str | None = None):
-    """Native wavefront-size autotuner (mptg_autotune_wavefront): the size with
-    the lowest median time to the first solution over `trials` seeds.
-    Returns (best size, {size: median seconds}).
+    """Native wavefront-size autotuner (mptg_autotune_wavefront): `trials`
+    seeds per size, then 2 * trials more for the three sizes with the lowest
+    median time to the first solution; the lowest median of those three over
+    all their seeds wins.  Returns (best size, {size: median seconds over the
+    seeds it ran}).
 
     cache: a JSON file of earlier results keyed by autotune_cache_key (scene
     kind, metric, dimension, capacity bucket, candidates).  A hit returns the
