@@ -299,10 +299,13 @@ mptg_status mptg_planner_set_surrogate_bias(mptg_planner* planner, int candidate
  * run, [7] wavefront counter. */
 mptg_status mptg_planner_stats(mptg_planner* planner, double out[8]);
 /* Persistent block planner (grid scenes, mptg_planner_set_persistent), summed
- * over its runs: [0..5] SM cycles in the sample, nearest-search, steer, link
- * set-up, link-sample and insert phases; [6] near ties of the nearest search
- * decided in FP64, [7] interior samples decided in FP64, [8] edge step counts
- * decided in FP64.  No reference counterpart (a profile of this planner). */
+ * over its runs: SM cycles in [0] the sample phase, [1] the nearest-search
+ * phase, which also runs each sample's steer and link set-up as soon as its
+ * nearest node is known, [2] and [3] zero (earlier separate phases), [4] the
+ * link-sample phase and [5] the insert phase; [6] FP64 distances of the
+ * nearest search beyond the winners', [7] interior samples decided in FP64,
+ * [8] edge step counts decided in FP64.  No reference counterpart (a profile
+ * of this planner). */
 mptg_status mptg_planner_block_profile(mptg_planner* planner, double out[9]);
 /* Planner<Scenario, PRRTStar<...>> (src/mpt/prrt_star.hpp:56-95): wavefronts
  * with k-nearest rewiring (rewire_k_nearest, the reference default):

@@ -23,8 +23,10 @@
 //                           grid (cells searched in rings until the ring's
 //                           distance bound passes the best), FP32 deciding
 //                           wherever distances are 2 err32 apart
-//   steer                   interpolate to `range` (skip when d == 0)
-//   link                    the DMV of the grid scene (scene.cu's two phases,
+//   steer and link set-up   per sample, as soon as its nearest node is known
+//                           (steer_setup): interpolate to `range` (skip when
+//                           d == 0), then the DMV's end state and step count
+//   link samples            the DMV's interior samples (scene.cu's phase B,
 //                           a warp per edge, the same sample order and counts)
 //   insert                  block scan of the accepted flags in sample order,
 //                           node budget, parent ids, goal flags
@@ -208,17 +210,71 @@ __device__ __forceinline__ float sq32(float qx, float qy, float2 p) {
     return fmaf(ty, ty, fmaf(tx, tx, 0.f));
 }
 
-// The nearest search's per-sample slots, laid over the new-state array S.nw
-// (16 bytes per sample), which the steer step writes only after the search.
+// The nearest search's per-sample slots, laid over the bucket grid's cell
+// heads (16 KB, 16 bytes per sample), which only the ring search uses; a
+// wavefront that runs the ring search rebuilds the grid first.
 struct BruteSlots {
     int* cnt;       // [W] candidates of each sample (pass 2)
     float* maxabs;  // [W] largest |coordinate| of the sample, rounded up
     float2* q32;    // [W] the sample rounded to FP32
 };
+static_assert(BPLAN_THREADS * 16 <= BPLAN_CELLS * 4, "the per-sample slots fit over the cell heads");
 __device__ __forceinline__ BruteSlots brute_slots(const BSmem& S, int W) {
-    unsigned char* base = reinterpret_cast<unsigned char*>(S.nw);
+    unsigned char* base = reinterpret_cast<unsigned char*>(S.head);
     return BruteSlots{reinterpret_cast<int*>(base), reinterpret_cast<float*>(base + 4 * (size_t)W),
                       reinterpret_cast<float2*>(base + 8 * (size_t)W)};
+}
+
+// Steer and the link set-up of sample t, whose nearest node is id (INT_MAX or
+// -1: none) at FP64 distance best (< 0: not computed yet).  Steer as
+// k_plan_steer (prrt.hpp:425-435): skip when d == 0, else interpolate from
+// the node to `range`; then phase A of the grid DMV (k_grid_edges_a): the end
+// state, the step count and the FP32 set-up of the interior samples, all the
+// FP64 work of the edge.  Everything it reads or writes belongs to sample t
+// (S.q / S.nd slots t, which take the set-up, S.nw, S.fl, S.ni), so threads
+// may run it for different samples without a barrier between the steps.
+__device__ void steer_setup(const BPlanJob& J, const BSmem& S, int t, int id, double best,
+                            unsigned long long* steps64) {
+    if (id == INT_MAX) id = -1;
+    S.ni[t] = id;
+    const double s[2] = {S.q[2 * t], S.q[2 * t + 1]};
+    double A[2] = {s[0], s[1]};
+    if (id >= 0) {
+        A[0] = J.states[2 * id];
+        A[1] = J.states[2 * id + 1];
+        if (best < 0.0) best = l2_dist64(s, A, 2);
+    }
+    double B[2];
+    const bool skip = id < 0 || best == 0.0 || !(best == best);  // prrt.hpp:425
+    if (!skip && best > J.range) {
+        interp64(MPTG_METRIC_L2, 2, A, s, __ddiv_rn(J.range, best), B);
+    } else {
+        B[0] = s[0];
+        B[1] = s[1];
+    }
+    if (skip) {  // the edge of a skipped sample starts at the sample itself
+        A[0] = s[0];
+        A[1] = s[1];
+    }
+    S.nw[2 * t] = B[0];
+    S.nw[2 * t + 1] = B[1];
+    bool ok = grid_valid_f(J.scene, B);
+    bool used64 = false;
+    long long steps = ok ? grid_edge_steps(A, B, J.inv_step, &used64) : 0;
+    if (used64) atomicAdd(steps64, 1ull);
+    if (steps < 0) ok = false;
+    float4 setup = make_float4(0.f, 0.f, 0.f, 0.f);
+    float eps = 0.f;
+    if (ok && steps >= 2) {
+        setup = make_float4(__double2float_rn(A[0]), __double2float_rn(A[1]),
+                            __double2float_rn(__dsub_rn(B[0], A[0])), __double2float_rn(__dsub_rn(B[1], A[1])));
+        eps = 8.f * U32 * (fabsf(setup.x) + fabsf(setup.y) + fabsf(setup.z) + fabsf(setup.w) + 1.f);
+    } else {
+        steps = 0;
+    }
+    reinterpret_cast<float4*>(S.q)[t] = setup;
+    reinterpret_cast<float2*>(S.nd)[t] = make_float2(eps, __int_as_float((int)steps));
+    S.fl[t] = (skip ? 2 : 0) | (ok ? 1 : 0);
 }
 
 // The pass-2 bound of one sample: (min32 + 2E)^2 (1 + 2^-21), each step
@@ -253,17 +309,19 @@ __device__ __forceinline__ float brute_thr2(const BSmem& S, const BruteSlots& B,
 // min32 + 2E, and so does every node that ties it in FP64, so the candidates
 // hold all of them: the result is the FP64 argmin with the lowest id, the
 // ring search's answer.  A sole candidate is the winner without any FP64
-// arithmetic; its FP64 distance is left (S.nd = -1) to the steer step, which
-// computes it for a whole warp of samples at once.  The FP64 pipe costs the
-// same per warp instruction however few lanes are active, so FP64 work is kept
-// to full warps: one FP64 distance per lane, never one thread's alone.
+// arithmetic; its FP64 distance is computed by steer_setup, which thread s
+// runs for sample s, one lane per sample.  The FP64 pipe costs the same per
+// warp instruction however few lanes are active, so FP64 work is kept to
+// full warps wherever it is not a single sample's own chain.  Each sample's
+// steer and link set-up (steer_setup) run as soon as its winner is known, by
+// the warp that ranked it or by thread s, with no barrier in between, so the
+// FP64 chains of different samples overlap with each other and with pass 3.
 // On entry S.fl[s] holds +inf (FP32 bits), S.ni[s] INT_MAX and the slots
 // (brute_slots) a zero count and the sample in FP32 for every sample s < W;
-// on return S.ni[s] is the winner
-// (INT_MAX without nodes) and S.nd[s] its FP64 distance or -1.  Every thread
-// of the block calls this.
+// on return every sample has been through steer_setup.  Every thread of the
+// block calls this.
 __device__ void nn_brute(const BPlanJob& J, const BSmem& S, int W, int n, float maxabs,
-                         unsigned long long* fp64_evals) {
+                         unsigned long long* fp64_evals, unsigned long long* steps64) {
     const int T = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const int NG = (W + 3) >> 2;
     int P = 1;
@@ -327,11 +385,7 @@ __device__ void nn_brute(const BPlanJob& J, const BSmem& S, int W, int n, float 
     const int nwarps = T >> 5;
     unsigned long long evals = 0;
     for (int s = warp; s < W; s += nwarps) {
-        const int cs = cnt[s];
-        if (cs < 2) {
-            if (cs == 1 && lane == 0) S.nd[s] = -1.0;  // the sole candidate (S.ni) wins
-            continue;
-        }
+        if (cnt[s] < 2) continue;
         const double* qd = S.q + 2 * s;
         const float t2 = brute_thr2(S, B, s, maxabs);
         const float sx = B.q32[s].x, sy = B.q32[s].y;
@@ -373,12 +427,13 @@ __device__ void nn_brute(const BPlanJob& J, const BSmem& S, int W, int n, float 
             }
         }
         if (nc) flush();
-        if (lane == 0) {
-            S.ni[s] = bid;
-            S.nd[s] = __longlong_as_double(bk);
-        }
+        __syncwarp();
+        if (lane == 0) steer_setup(J, S, s, bid, __longlong_as_double(bk), steps64);
     }
     if (lane == 0 && evals) atomicAdd(fp64_evals, evals);
+    // a sole candidate (S.ni) is the winner; its FP64 distance is computed by
+    // steer_setup, one lane per sample
+    if (t < W && cnt[t] < 2) steer_setup(J, S, t, S.ni[t], -1.0, steps64);
 }
 
 // GoalState's test d(q, goal) <= radius in FP64, decided by the FP32 distance
@@ -421,14 +476,11 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
         s_bb[0] = s_bb[2] = INT_MAX;
         s_bb[1] = s_bb[3] = -1;
     }
-    for (int c = t; c < J.gx * J.gy; c += T) S.head[c] = -1;
-    for (int c = t; c < BPLAN_CELLS / 16; c += T) S.ccount[c] = 0;
     __syncthreads();
     for (int j = t; j < s_n; j += T) {
         const double x = J.states[2 * j], y = J.states[2 * j + 1];
         S.pts[j] = make_float2(__double2float_rn(x), __double2float_rn(y));
         atomicMax(&s_maxabs, __float_as_int(maxabs_ru(x, y)));
-        bucket_insert(J, S, s_bb, j);
     }
     uint32_t wave = J.ctr->wave;
     int waves_run = 0, status = BPLAN_DONE;
@@ -499,8 +551,19 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
         // block R >= 1 rings out lies at least (R - 1) blocks away, which ends
         // the search.  The group's winner is then exact (nn_group_winner).
         if ((long long)W * n <= J.brute_pairs) {
-            nn_brute(J, S, W, n, __int_as_float(s_maxabs), &s_prof[0]);
+            nn_brute(J, S, W, n, __int_as_float(s_maxabs), &s_prof[0], &s_prof[2]);
         } else {
+            // the bucket grid of the n nodes, built for this wavefront (the
+            // exhaustive search keeps its per-sample slots over the cell heads)
+            for (int c = t; c < J.gx * J.gy; c += T) S.head[c] = -1;
+            for (int c = t; c < BPLAN_CELLS / 16; c += T) S.ccount[c] = 0;
+            if (t == 0) {
+                s_bb[0] = s_bb[2] = INT_MAX;
+                s_bb[1] = s_bb[3] = -1;
+            }
+            __syncthreads();
+            for (int j = t; j < n; j += T) bucket_insert(J, S, s_bb, j);
+            __syncthreads();
             const int g = t / G, r = t % G;
             if (g < W) {
                 const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
@@ -556,68 +619,11 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
                 }
                 nn_group_winner(J, S, g, r, G, gmask, qd, E, st);
             }
+            __syncthreads();
+            if (t < W) steer_setup(J, S, t, S.ni[t], S.nd[t], &s_prof[2]);
         }
         __syncthreads();
-        mark(1);
-        // steer (k_plan_steer), thread per sample
-        if (t < W) {
-            const double* s = S.q + 2 * t;
-            int id = S.ni[t];
-            if (id == INT_MAX) S.ni[t] = id = -1;  // no node (nn_brute)
-            double best = S.nd[t];
-            if (id >= 0 && best < 0.0) best = l2_dist64(s, J.states + 2 * id, 2);
-            S.nd[t] = best;
-            double* nw = S.nw + 2 * t;
-            const bool skip = id < 0 || best == 0.0 || !(best == best);  // prrt.hpp:425
-            if (!skip && best > J.range) {
-                const double a[2] = {J.states[2 * id], J.states[2 * id + 1]};
-                interp64(MPTG_METRIC_L2, 2, a, s, __ddiv_rn(J.range, best), nw);
-            } else {
-                nw[0] = s[0];
-                nw[1] = s[1];
-            }
-            S.fl[t] = skip ? 2 : 0;
-        }
-        __syncthreads();
-        mark(2);
-        // link(near, new), as k_grid_edges_a / k_grid_edges_b: phase A thread
-        // per edge (the end state, the step count and the FP32 set-up of the
-        // interior samples, all the FP64 work of an edge), phase B warp per
-        // edge with interior samples (FP32 per sample, FP64 only when unsure).
-        // Phase A's set-up replaces the edge's sample (S.q: a32, dir32) and
-        // nearest distance (S.nd: eps, steps), which are not needed again.
-        if (t < W) {
-            const bool skip = (S.fl[t] & 2) != 0;
-            const double B[2] = {S.nw[2 * t], S.nw[2 * t + 1]};
-            double A[2];
-            if (skip) {
-                A[0] = S.q[2 * t];
-                A[1] = S.q[2 * t + 1];
-            } else {
-                const int id = S.ni[t];
-                A[0] = J.states[2 * id];
-                A[1] = J.states[2 * id + 1];
-            }
-            bool ok = grid_valid_f(J.scene, B);
-            bool used64 = false;
-            long long steps = ok ? grid_edge_steps(A, B, J.inv_step, &used64) : 0;
-            if (used64) atomicAdd(&s_prof[2], 1ull);
-            if (steps < 0) ok = false;
-            float4 setup = make_float4(0.f, 0.f, 0.f, 0.f);
-            float eps = 0.f;
-            if (ok && steps >= 2) {
-                setup = make_float4(__double2float_rn(A[0]), __double2float_rn(A[1]),
-                                    __double2float_rn(__dsub_rn(B[0], A[0])), __double2float_rn(__dsub_rn(B[1], A[1])));
-                eps = 8.f * U32 * (fabsf(setup.x) + fabsf(setup.y) + fabsf(setup.z) + fabsf(setup.w) + 1.f);
-            } else {
-                steps = 0;
-            }
-            reinterpret_cast<float4*>(S.q)[t] = setup;
-            reinterpret_cast<float2*>(S.nd)[t] = make_float2(eps, __int_as_float((int)steps));
-            if (ok) S.fl[t] |= 1;
-        }
-        __syncthreads();
-        mark(3);
+        mark(1);  // nearest search, steer and link set-up
         for (int e = warp; e < W; e += nwarps) {
             const float2 es = reinterpret_cast<const float2*>(S.nd)[e];
             const int steps = __float_as_int(es.y);
@@ -686,7 +692,6 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
                 J.states[2 * id] = nw[0];
                 J.states[2 * id + 1] = nw[1];
                 S.pts[id] = make_float2(__double2float_rn(nw[0]), __double2float_rn(nw[1]));
-                bucket_insert(J, S, s_bb, id);
                 J.parent[id] = S.ni[t];
                 // GoalState::operator() (src/mpt/goal_state.hpp:64-69): d <= radius
                 const uint8_t g = J.has_goal && goal_reached(nw, J.goal, J.goal_radius) ? 1 : 0;

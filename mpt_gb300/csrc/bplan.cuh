@@ -12,8 +12,10 @@ struct BPlanCounters {
     int waves_run;                  // wavefronts this run completed
     unsigned long long samples;     // samples drawn by this run
     unsigned long long accepted;    // nodes added by this run
-    // SM cycles of this run per phase: samples, nearest search, steer, link
-    // set-up (thread per edge), link samples (warp per edge), insert
+    // SM cycles of this run per phase: [0] samples, [1] nearest search with
+    // each sample's steer and link set-up (one phase: a sample's steer starts
+    // as soon as its nearest node is known), [2] and [3] unused (zero),
+    // [4] link samples (warp per edge), [5] insert
     unsigned long long cyc[6];
     // FP64 fallbacks of this run: FP64 distances of the nearest search (the
     // ring search's near ties; every candidate of the exhaustive search,

@@ -418,6 +418,8 @@ class Planner:
         counts, summed over its runs (mptg_planner_block_profile)."""
         out = (ctypes.c_double * 9)()
         _check(self.ctx.h, self.lib.mptg_planner_block_profile(self.h, out))
+        # cyc_nearest covers each sample's steer and link set-up as well;
+        # cyc_steer and cyc_link_setup stay zero
         keys = ["cyc_sample", "cyc_nearest", "cyc_steer", "cyc_link_setup", "cyc_link_samples", "cyc_insert",
                 "near_ties_fp64", "samples_fp64", "step_counts_fp64"]
         return dict(zip(keys, [float(v) for v in out]))
@@ -538,14 +540,17 @@ class PPRMPlanner(Planner):
 
     def solve(self, done_fn, deadline: float | None = None):
         """Runs wavefronts until done_fn() is true: polled between calls of up
-        to POLL_WAVEFRONTS wavefronts, each of which ends early at the first
-        solution or at the deadline (time.monotonic())."""
+        to POLL_SECONDS of wavefronts (at least one), each of which ends early
+        at the first solution or at the deadline (time.monotonic())."""
         while not done_fn():
             before = self.stats()["wavefronts"]
-            left = 0.0 if deadline is None else deadline - time.monotonic()
-            if deadline is not None and left <= 0:
-                break
-            self.run(self.POLL_WAVEFRONTS, time_limit=left, stop_when_solved=not self.solved())
+            limit = self.POLL_SECONDS
+            if deadline is not None:
+                left = deadline - time.monotonic()
+                if left <= 0:
+                    break
+                limit = min(limit, left)
+            self.run(0, time_limit=limit, stop_when_solved=not self.solved())
             if self.stats()["wavefronts"] == before:  # node budget exhausted
                 break
 
