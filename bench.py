@@ -636,7 +636,12 @@ def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0, wave_for=None, surr
     """Config of the serving benchmark: n queries uniform over the three scenes,
     start and goal rejection-sampled valid, node budgets log-uniform in
     [1k, 200k]; wavefront = the scene's autotuned size (wave_for[kind]) when
-    given, else budget/16 clipped to [256, 4096]; at most budget/4."""
+    given, else budget/16 clipped to [256, 4096]; at most budget/4.  Off the
+    grid a wavefront is several kernels and host round trips (0.3-1 ms), so
+    there the size grows with the budget to at least budget/128: a query that
+    cannot be solved within its budget then ends after about 128 wavefronts
+    instead of a thousand (the grid's persistent block planner runs a
+    wavefront in microseconds and keeps the tuned size)."""
     from mpt_gb300 import planner as P
     from mpt_gb300 import scenes
     from mpt_gb300.batch import Query
@@ -664,6 +669,8 @@ def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0, wave_for=None, surr
         used[k] += 2
         budget = int(round(math.exp(rng.uniform(math.log(1000), math.log(200000)))))
         W = wave_for[d["kind"]] if wave_for else min(4096, max(256, budget // 16))
+        if d["kind"] != "grid":
+            W = min(4096, max(W, budget // 128))
         W = int(max(1, min(W, budget // 4)))
         sc = P.Scenario(d, P.GoalState(d["goal_radius"], b))
         q = Query(sc, a, seed=seed + i, max_nodes=budget, wavefront=W, time_limit=time_limit)
