@@ -67,6 +67,9 @@ struct mptg_surrogate {
     uint8_t* dlabels = nullptr;
     float* dlogits = nullptr;
     int* err = nullptr;           // device error word: a tcgen05 GEMM wait ran out (1 load, 2 MMA, 3 epilogue)
+    double* dnorm = nullptr;      // scale [16], shift [16] on the device (the fused scorer)
+    CUtensorMap wmap;             // the three hidden layers' BF16 weights, [768][256] (the fused scorer)
+    bool wmap_ok = false;
     // held by a planner from scoring until its stream has consumed the logits,
     // since the activation buffers above are shared
     std::mutex mu;
@@ -493,6 +496,264 @@ __global__ void __launch_bounds__(SGP_THREADS, 1) k_sg_umma_p(const __grid_const
     if (warp == 0) umma::tmem_dealloc(tmem, 2 * SG_W);
 }
 
+// ------------------------------------------------------------------ fused scorer
+// Logits of n states by the whole MLP in one persistent launch, the
+// activations never leaving the SM: one CTA per SM loops over 128-row tiles.
+// Per tile:
+//   layer 0  the epilogue warps normalise their row's state and compute its
+//            64 columns of SiLU(W0 x + b0) on CUDA cores (k_sg_inputs and
+//            k_sg_layer0's arithmetic), written as BF16 into the A tile in
+//            shared memory in the layout TMA's 128-byte swizzle gives (16-byte
+//            chunk c of row r of a 64-wide K slice at chunk c ^ (r % 8));
+//   layers 1-3  warp 1 issues the 16 UMMAs 128 x 256 x 16 of the layer (A from
+//            that tile, B the layer's weights) into the TMEM accumulator; the
+//            epilogue warps read it back and write SiLU(acc + bias) as the next
+//            layer's A tile over the one just consumed, or, after layer 3, the
+//            output layer's dot product (quarter sums added in quarter order);
+// while warp 0 streams the three layers' weights (128 KB each) from L2
+// through a four-stage TMA ring of 64-wide K slices, so the next layer's
+// weights arrive during the current epilogue.  HBM traffic is the states in
+// and the logits out.  The arithmetic equals k_sg_inputs + k_sg_layer0 +
+// three k_sg_umma_p launches (the same UMMA sequence and epilogue steps), so
+// the logits are the same bits.  Barriers: a_ready (512 epilogue threads: A
+// written and the accumulator read), acc_full (commit of a layer's UMMAs),
+// w_full / w_empty per ring stage, pready (the output layer's quarter sums);
+// every wait is bounded as in k_sg_umma.
+#define SGF_THREADS (64 + 32 * SGP_EPI_WARPS)
+#define SGF_A_BYTES (SG_TM * SG_W * 2)              // 64 KB: the A tile, 4 K slices of 16 KB
+#define SGF_WSTAGE (SG_W * SG_BK * 2)               // 32 KB: one 64-wide K slice of a layer's weights
+#define SGF_F_FLOATS (SG_MAXIN * SG_W + 5 * SG_W + 4 * SG_TM)  // W0 (BF16-rounded, [k][n]), b0, b1-b3, w4, partial sums
+#define SGF_SMEM (SGF_A_BYTES + SG_STAGES * SGF_WSTAGE + SGF_F_FLOATS * 4 + 1024 + 256)
+
+struct FusedArgs {
+    const double* states;  // [n][in]
+    int n, in;
+    const double* norm;    // scale [16], shift [16]
+    const float* W0;       // [256][in] FP32 master
+    const float* b0;
+    const float* b1;
+    const float* b2;
+    const float* b3;
+    const float* w4;
+    const float* b4;
+    float* out;            // [n] logits
+};
+
+// the BF16 pair (a, b) as one 32-bit word, low half a
+__device__ __forceinline__ uint32_t sgf_pack(float a, float b) { return pack_bf16x2(a, b); }
+
+// 64 BF16 values of row r (column quarter q) into the swizzled A tile
+__device__ __forceinline__ void sgf_store_row(uint8_t* sA, int r, int q, const uint32_t (&pk)[32]) {
+    uint8_t* row = sA + (size_t)q * (SG_TM * SG_BK * 2) + (size_t)r * 128;
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+        *reinterpret_cast<uint4*>(row + ((c ^ (r & 7)) << 4)) =
+            make_uint4(pk[4 * c], pk[4 * c + 1], pk[4 * c + 2], pk[4 * c + 3]);
+}
+
+__global__ void __launch_bounds__(SGF_THREADS, 1) k_sg_score_fused(const __grid_constant__ CUtensorMap tw, int ntiles,
+                                                                 FusedArgs fa, int* __restrict__ err) {
+    extern __shared__ uint8_t sg_smem_raw[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t raw = umma::smem_u32(sg_smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    uint8_t* smem = sg_smem_raw + (base - raw);
+    uint8_t* sA = smem;                                  // [4][128][64] bf16, swizzled
+    uint8_t* sW = smem + SGF_A_BYTES;                    // [stage][256][64] bf16, swizzled
+    float* sW0 = reinterpret_cast<float*>(sW + SG_STAGES * SGF_WSTAGE);  // [k][256]
+    float* sb0 = sW0 + SG_MAXIN * SG_W;
+    float* sb = sb0 + SG_W;                              // [3][256] b1, b2, b3
+    float* sw4 = sb + 3 * SG_W;
+    float* spart = sw4 + SG_W;                           // [4][128]
+    uint64_t* a_ready = reinterpret_cast<uint64_t*>(spart + 4 * SG_TM);
+    uint64_t* acc_full = a_ready + 1;
+    uint64_t* pready = acc_full + 1;
+    uint64_t* w_full = pready + 1;
+    uint64_t* w_empty = w_full + SG_STAGES;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(w_empty + SG_STAGES);
+    int* counts = reinterpret_cast<int*>(tslot + 1);    // [0] weight slices loaded, [1] consumed
+    const int my_tiles = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int nslices = my_tiles * 3 * 4;
+    if (tid == 0) {
+        umma::mbar_init(a_ready, 32 * SGP_EPI_WARPS);
+        umma::mbar_init(acc_full, 1);
+        umma::mbar_init(pready, 32 * (SGP_EPI_WARPS - 4));
+        for (int s = 0; s < SG_STAGES; ++s) {
+            umma::mbar_init(&w_full[s], 1);
+            umma::mbar_init(&w_empty[s], 1);
+        }
+        counts[0] = counts[1] = 0;
+        umma::fence_mbar_init();
+    }
+    for (int i = tid; i < SG_W; i += SGF_THREADS) {
+        for (int k = 0; k < SG_MAXIN; ++k)
+            sW0[k * SG_W + i] = k < fa.in ? __bfloat162float(__float2bfloat16_rn(__ldg(&fa.W0[i * fa.in + k]))) : 0.f;
+        sb0[i] = __ldg(&fa.b0[i]);
+        sb[i] = __ldg(&fa.b1[i]);
+        sb[SG_W + i] = __ldg(&fa.b2[i]);
+        sb[2 * SG_W + i] = __ldg(&fa.b3[i]);
+        sw4[i] = __ldg(&fa.w4[i]);
+    }
+    if (warp == 0) {
+        umma::tmem_alloc(tslot, SG_W);
+        umma::tmem_relinquish();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint64_t deadline = umma::globaltimer_ns() + SG_TIMEOUT_NS;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int g = 0;
+            for (; g < nslices; ++g) {  // slice g: layer (g / 4) % 3, K block g % 4
+                const int s = g % SG_STAGES;
+                if (g >= SG_STAGES && !umma::mbar_wait(&w_empty[s], ((g / SG_STAGES) - 1) & 1, deadline)) {
+                    atomicExch(err, 1);
+                    break;
+                }
+                umma::mbar_arrive_expect_tx(&w_full[s], SGF_WSTAGE);
+                umma::tma_load_2d(sW + s * SGF_WSTAGE, &tw, &w_full[s], (g & 3) * SG_BK, ((g >> 2) % 3) * SG_W);
+            }
+            counts[0] = g;
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = umma::idesc_bf16_f32(SG_TM, SG_W);
+            int g = 0;
+            bool ok = true;
+            for (int u = 0; ok && u < my_tiles * 3; ++u) {  // u: (tile, layer)
+                if (!umma::mbar_wait(a_ready, u & 1, deadline)) {
+                    atomicExch(err, 2);
+                    break;
+                }
+                umma::fence_after_sync();
+                for (int kb = 0; kb < 4; ++kb, ++g) {
+                    const int s = g % SG_STAGES;
+                    if (!umma::mbar_wait(&w_full[s], (g / SG_STAGES) & 1, deadline)) {
+                        atomicExch(err, 2);
+                        ok = false;
+                        break;
+                    }
+                    umma::fence_after_sync();
+                    const uint32_t a0 = base + kb * (SG_TM * SG_BK * 2);
+                    const uint32_t b0 = base + SGF_A_BYTES + s * SGF_WSTAGE;
+#pragma unroll
+                    for (int k = 0; k < SG_BK / 16; ++k)
+                        umma::mma_bf16(tmem, umma::sdesc_k128(a0 + 32 * k), umma::sdesc_k128(b0 + 32 * k), idesc,
+                                       (kb | k) != 0);
+                    umma::mma_commit(&w_empty[s]);
+                }
+                if (ok) umma::mma_commit(acc_full);
+            }
+            counts[1] = g;
+        }
+        __syncwarp();
+    } else {
+        // epilogue warps: lane group (warp % 4) = rows, quarter (warp - 2) / 4 = columns
+        const int grp = warp & 3, qtr = (warp - 2) >> 2, row = grp * 32 + lane;
+        const uint32_t trow = tmem + ((uint32_t)(grp * 32) << 16);
+        bool ok = true;
+        for (int i = 0; ok && i < my_tiles; ++i) {
+            const int m = ((int)blockIdx.x + i * (int)gridDim.x) * SG_TM + row;
+            // layer 0 (k_sg_inputs, k_sg_layer0): BF16 inputs, FP32 sums over k in order
+            float x[SG_MAXIN];
+#pragma unroll
+            for (int k = 0; k < SG_MAXIN; ++k) {
+                float v = 0.f;
+                if (m < fa.n && k < fa.in)
+                    v = (float)((__ldg(&fa.states[(size_t)m * fa.in + k]) - fa.norm[SG_MAXIN + k]) * fa.norm[k]);
+                x[k] = __bfloat162float(__float2bfloat16_rn(v));
+            }
+            {
+                uint32_t pk[32];
+#pragma unroll
+                for (int j = 0; j < 64; j += 2) {
+                    float z2[2];
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int nc = 64 * qtr + j + h;
+                        float z = sb0[nc];
+#pragma unroll
+                        for (int k = 0; k < SG_MAXIN; ++k)
+                            if (k < fa.in) z = fmaf(x[k], sW0[k * SG_W + nc], z);
+                        z2[h] = sg_silu(z);
+                    }
+                    pk[j / 2] = sgf_pack(z2[0], z2[1]);
+                }
+                sgf_store_row(sA, row, qtr, pk);
+            }
+            umma::fence_proxy_async();
+            umma::fence_before_sync();
+            umma::mbar_arrive(a_ready);
+            for (int l = 1; l <= 3; ++l) {
+                const int u = 3 * i + (l - 1);
+                if (!umma::mbar_wait(acc_full, u & 1, deadline)) {
+                    if (lane == 0) atomicExch(err, 3);
+                    ok = false;
+                    break;
+                }
+                umma::fence_after_sync();
+                const float* bias = sb + (l - 1) * SG_W;
+                if (l < 3) {
+                    uint32_t pk[32];
+#pragma unroll
+                    for (int c = 0; c < 64; c += 16) {
+                        float v[16];
+                        umma::tmem_ld16(trow + 64 * qtr + c, v);
+#pragma unroll
+                        for (int j = 0; j < 16; j += 2)
+                            pk[(c + j) / 2] = sgf_pack(sg_silu(v[j] + bias[64 * qtr + c + j]),
+                                                       sg_silu(v[j + 1] + bias[64 * qtr + c + j + 1]));
+                    }
+                    sgf_store_row(sA, row, qtr, pk);
+                    umma::fence_proxy_async();
+                    umma::fence_before_sync();
+                    umma::mbar_arrive(a_ready);
+                } else {
+                    float out = 0.f;
+#pragma unroll
+                    for (int c = 0; c < 64; c += 16) {
+                        float v[16];
+                        umma::tmem_ld16(trow + 64 * qtr + c, v);
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const int nc = 64 * qtr + c + j;
+                            out = fmaf(__bfloat162float(__float2bfloat16_rn(sg_silu(v[j] + bias[nc]))),
+                                       __bfloat162float(__float2bfloat16_rn(sw4[nc])), out);
+                        }
+                    }
+                    umma::fence_before_sync();
+                    if (qtr) {
+                        spart[qtr * SG_TM + row] = out;
+                        umma::mbar_arrive(pready);
+                    } else if (umma::mbar_wait(pready, i & 1, deadline)) {
+                        out += spart[SG_TM + row];
+                        out += spart[2 * SG_TM + row];
+                        out += spart[3 * SG_TM + row];
+                        if (m < fa.n) fa.out[m] = out + __ldg(fa.b4);
+                    } else {
+                        if (lane == 0) atomicExch(err, 3);
+                        ok = false;
+                    }
+                }
+            }
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    // weight slices loaded but never consumed (a wait ran out) must land
+    // before the shared memory they write is released
+    if (tid == 0) {
+        const uint64_t drain = umma::globaltimer_ns() + SG_TIMEOUT_NS;
+        for (int g = counts[1]; g < counts[0]; ++g) umma::mbar_wait(&w_full[g % SG_STAGES], (g / SG_STAGES) & 1, drain);
+    }
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, SG_W);
+}
+
 // ------------------------------------------------------------------ CUDA-core parts
 
 // inputs: FP64 states -> normalised BF16 features, padded to 16
@@ -833,11 +1094,16 @@ mptg_status mptg_surrogate_create(mptg_ctx* ctx, int in_dim, const double* scale
     if (e == cudaSuccess) e = cudaMalloc((void**)&s->loss, sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc((void**)&s->err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(s->err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&s->dnorm, 2 * SG_MAXIN * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(s->dnorm, s->scale, SG_MAXIN * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(s->dnorm + SG_MAXIN, s->shift, SG_MAXIN * sizeof(double), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         cudaGetLastError();
         delete s;
         return mptg_fail(ctx, MPTG_ERR_OOM, "surrogate parameters: %s", cudaGetErrorString(e));
     }
+    s->wmap_ok = bf16_map(&s->wmap, s->Wb, 3 * SG_W, SG_W, SG_W, SG_W);
     cudaMemset(s->Mo, 0, pb);
     cudaMemset(s->Vo, 0, pb);
     cudaMemset(s->G, 0, pb);
@@ -857,7 +1123,7 @@ mptg_status mptg_surrogate_destroy(mptg_surrogate* s) {
     if (!s) return MPTG_ERR_INVALID_ARG;
     cudaDeviceSynchronize();
     void* ptrs[] = {s->P, s->G, s->Mo, s->Vo, s->Wb, s->WTb, s->X, s->Z, s->H, s->HT, s->dZ, s->dZT, s->dH,
-                    s->zout, s->dzout, s->dstates, s->dlabels, s->dlogits, s->loss, s->err};
+                    s->zout, s->dzout, s->dstates, s->dlabels, s->dlogits, s->loss, s->err, s->dnorm};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete s;
@@ -887,20 +1153,34 @@ mptg_status mptg_surrogate_set(mptg_surrogate* s, const float* in, size_t n) {
     return MPTG_OK;
 }
 
-// internal: logits for n device states (used by the planner)
+// internal: logits for n device states (used by the planner): the fused
+// scorer, one launch, no activation buffers
 mptg_status mptg_surrogate_score_dev(mptg_surrogate* s, const double* dstates, int n, float* dlogits, cudaStream_t st) {
     if (n <= 0) return MPTG_OK;
-    mptg_status r = sg_reserve(s, (size_t)n);
-    if (r) return r;
-    int M = (n + SG_TM - 1) / SG_TM * SG_TM;
-    // scale/shift travel in the first 32 doubles of the staging buffer
-    MPTG_CUDA_TRY(s->ctx, cudaMemcpyAsync(s->dstates, s->scale, sizeof(s->scale), cudaMemcpyHostToDevice, st));
-    MPTG_CUDA_TRY(s->ctx, cudaMemcpyAsync(s->dstates + SG_MAXIN, s->shift, sizeof(s->shift), cudaMemcpyHostToDevice,
-                                          st));
-    k_sg_inputs<<<mptg_blocks(M, 256), 256, 0, st>>>(dstates, n, s->in, s->dstates, s->dstates + SG_MAXIN, M, s->X);
+    if (!s->wmap_ok) return mptg_fail(s->ctx, MPTG_ERR_CUDA, "surrogate scorer: cuTensorMapEncodeTiled failed");
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        cudaFuncSetAttribute(k_sg_score_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, SGF_SMEM);
+    });
+    SgLayout L = sg_layout(s->in);
+    FusedArgs fa;
+    fa.states = dstates;
+    fa.n = n;
+    fa.in = s->in;
+    fa.norm = s->dnorm;
+    fa.W0 = s->P + L.W0;
+    fa.b0 = s->P + L.b0;
+    fa.b1 = s->P + L.b[1];
+    fa.b2 = s->P + L.b[2];
+    fa.b3 = s->P + L.b[3];
+    fa.w4 = s->P + L.w4;
+    fa.b4 = s->P + L.b4;
+    fa.out = dlogits;
+    const int tiles = (n + SG_TM - 1) / SG_TM;
+    const int grid = std::min(tiles, std::max(1, s->ctx->sms));
+    k_sg_score_fused<<<grid, SGF_THREADS, SGF_SMEM, st>>>(s->wmap, tiles, fa, s->err);
     MPTG_LAUNCHED(s->ctx);
-    if ((r = sg_forward(s, M, false, st))) return r;
-    MPTG_CUDA_TRY(s->ctx, cudaMemcpyAsync(dlogits, s->zout, n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    MPTG_CUDA_TRY(s->ctx, cudaGetLastError());
     return MPTG_OK;
 }
 

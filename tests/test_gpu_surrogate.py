@@ -53,6 +53,28 @@ def test_forward_and_gradients_match_reference(ctx):
     assert np.isfinite(p2).all() and not np.array_equal(p2, p.astype(np.float32))
 
 
+def test_fused_scorer_on_ragged_batches(ctx):
+    """The one-launch scorer (k_sg_score_fused: every layer on the SM, several
+    128-row tiles per CTA, a partial last tile): each row's logit is the same
+    bits whatever batch it is scored in, repeated calls agree, and rows from
+    the start, middle and end of a 50,001-state batch match the reference MLP."""
+    from mpt_gb300.surrogate import Surrogate, se3_normalisation
+    from oracle import mlp
+    sc = scenes.mesh_scene()
+    scale, shift = se3_normalisation(sc["lo"], sc["hi"])
+    sg = Surrogate(ctx, 7, scale, shift, seed=4)
+    x = scenes.uniform_states(sc, 50001, 23)
+    z = sg.score(x)
+    assert z.shape == (50001,) and np.isfinite(z).all()
+    assert np.array_equal(sg.score(x).view(np.int32), z.view(np.int32))
+    for lo, hi in ((0, 1000), (20000, 20129), (49990, 50001)):
+        assert np.array_equal(sg.score(x[lo:hi]).view(np.int32), z[lo:hi].view(np.int32))
+    p = sg.params().astype(np.float64)
+    idx = np.r_[0:200, 25000:25200, 49801:50001]
+    zr, _ = mlp.forward(p, (x[idx] - shift) * scale, 7)
+    assert np.all(np.abs(z[idx] - zr) <= 0.02 + 0.02 * np.abs(zr)), np.abs(z[idx] - zr).max()
+
+
 @pytest.fixture(scope="module")
 def trained(ctx):
     from mpt_gb300.surrogate import Surrogate, se3_normalisation
