@@ -359,10 +359,11 @@ def solve_times(ctx, seeds=None, cap_s=20.0, tune=True):
     """Wall time to the first solution of the plain wavefront planner per scene
     (p50 over seeds 1000..), at the default wavefront and at the one the native
     autotuner picks (tuned on seeds 500.. of the same query).  seeds: per-scene
-    counts (default grid 20, arm 10, SE(3) 20)."""
+    counts (default grid 50, arm 20, SE(3) 50: the arm's solves take up to
+    seconds each)."""
     from mpt_gb300 import planner as P
     from mpt_gb300 import scenes
-    seeds = seeds or {"grid_1024": 20, "arm_10link": 10, "se3_mesh": 20}
+    seeds = seeds or {"grid_1024": 50, "arm_10link": 20, "se3_mesh": 50}
     res = {}
     for name, mk, W in SOLVE_SCENES:
         sc = getattr(scenes, mk)()
