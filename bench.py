@@ -1010,7 +1010,7 @@ def main():
     ap.add_argument("--edges-only", action="store_true", help="edge checks/s of the three scenes only (profiling)")
     ap.add_argument("--bplan-only", action="store_true", help="the block planner's wavefront sweep only (profiling)")
     ap.add_argument("--solve-only", action="store_true", help="time to solve of the three scenes only (profiling)")
-    ap.add_argument("--solve-seeds", type=int, default=None, help="seeds per scene (default grid 20, arm 10, SE(3) 20)")
+    ap.add_argument("--solve-seeds", type=int, default=None, help="seeds per scene (default grid 50, arm 20, SE(3) 50)")
     ap.add_argument("--ref-plan-child", nargs=5, default=None, help=argparse.SUPPRESS)
     args = ap.parse_args()
     if args.ref_plan_child:
