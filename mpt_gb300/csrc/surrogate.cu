@@ -511,10 +511,11 @@ __global__ void __launch_bounds__(SGP_THREADS, 1) k_sg_umma_p(const __grid_const
 
 // ------------------------------------------------------------------ fused scorer
 // Logits of n states by the whole MLP in one persistent launch, the
-// activations never leaving the SM: one CTA per SM loops over 128-row tiles.
-// Per tile:
+// activations never leaving the SM.  Each CTA loops over 128-row tiles; two
+// CTAs share an SM, so one's tensor-core phase runs while the other's
+// CUDA-core phase does.  Per tile:
 //   layer 0  the epilogue warps normalise their row's state and compute its
-//            64 columns of SiLU(W0 x + b0) on CUDA cores (k_sg_inputs and
+//            columns of SiLU(W0 x + b0) on CUDA cores (k_sg_inputs and
 //            k_sg_layer0's arithmetic), written as BF16 into the A tile in
 //            shared memory in the layout TMA's 128-byte swizzle gives (16-byte
 //            chunk c of row r of a 64-wide K slice at chunk c ^ (r % 8));
@@ -522,21 +523,27 @@ __global__ void __launch_bounds__(SGP_THREADS, 1) k_sg_umma_p(const __grid_const
 //            that tile, B the layer's weights) into the TMEM accumulator; the
 //            epilogue warps read it back and write SiLU(acc + bias) as the next
 //            layer's A tile over the one just consumed, or, after layer 3, the
-//            output layer's dot product (quarter sums added in quarter order);
+//            output layer's dot product (a chain per 64-column quarter, the
+//            quarters added in order);
 // while warp 0 streams the three layers' weights (128 KB each) from L2
-// through a four-stage TMA ring of 64-wide K slices, so the next layer's
-// weights arrive during the current epilogue.  HBM traffic is the states in
-// and the logits out.  The arithmetic equals k_sg_inputs + k_sg_layer0 +
-// three k_sg_umma_p launches (the same UMMA sequence and epilogue steps), so
-// the logits are the same bits.  Barriers: a_ready (512 epilogue threads: A
+// through a TMA ring of 64-wide K slices.  HBM traffic is the states in and
+// the logits out.  The arithmetic equals k_sg_inputs + k_sg_layer0 + three
+// k_sg_umma_p launches (the same UMMA sequence and epilogue steps), so the
+// logits are the same bits.  Barriers: a_ready (the epilogue threads: A
 // written and the accumulator read), acc_full (commit of a layer's UMMAs),
-// w_full / w_empty per ring stage, pready (the output layer's quarter sums);
+// w_full / w_empty per ring stage, pready (the output layer's partial sums);
 // every wait is bounded as in k_sg_umma.
-#define SGF_THREADS (64 + 32 * SGP_EPI_WARPS)
+#define SGF_EPI 8                                   // epilogue warps: two per TMEM lane group
+#define SGF_PARTS (SGF_EPI / 4)                     // column parts per row
+#define SGF_PCOLS (SG_W / SGF_PARTS)                // columns per part (128)
+#define SGF_STAGES 1                                // weight ring stages (one 32 KB slice)
+#define SGF_CTAS 2                                  // CTAs per SM
+#define SGF_THREADS (64 + 32 * SGF_EPI)
 #define SGF_A_BYTES (SG_TM * SG_W * 2)              // 64 KB: the A tile, 4 K slices of 16 KB
 #define SGF_WSTAGE (SG_W * SG_BK * 2)               // 32 KB: one 64-wide K slice of a layer's weights
-#define SGF_F_FLOATS (SG_MAXIN * SG_W + 5 * SG_W + 4 * SG_TM)  // W0 (BF16-rounded, [k][n]), b0, b1-b3, w4, partial sums
-#define SGF_SMEM (SGF_A_BYTES + SG_STAGES * SGF_WSTAGE + SGF_F_FLOATS * 4 + 1024 + 256)
+// W0 (BF16-rounded, [k][n] for k < in), b0, b1-b3, w4, quarter sums [4][128]
+#define SGF_F_FLOATS(in) ((in) * SG_W + 5 * SG_W + 4 * SG_TM)
+#define SGF_SMEM(in) (SGF_A_BYTES + SGF_STAGES * SGF_WSTAGE + SGF_F_FLOATS(in) * 4 + 1024 + 256)
 
 struct FusedArgs {
     const double* states;  // [n][in]
@@ -555,17 +562,18 @@ struct FusedArgs {
 // the BF16 pair (a, b) as one 32-bit word, low half a
 __device__ __forceinline__ uint32_t sgf_pack(float a, float b) { return pack_bf16x2(a, b); }
 
-// 64 BF16 values of row r (column quarter q) into the swizzled A tile
-__device__ __forceinline__ void sgf_store_row(uint8_t* sA, int r, int q, const uint32_t (&pk)[32]) {
-    uint8_t* row = sA + (size_t)q * (SG_TM * SG_BK * 2) + (size_t)r * 128;
+// 64 BF16 values of row r (K slice kb) into the swizzled A tile
+__device__ __forceinline__ void sgf_store_row(uint8_t* sA, int r, int kb, const uint32_t (&pk)[32]) {
+    uint8_t* row = sA + (size_t)kb * (SG_TM * SG_BK * 2) + (size_t)r * 128;
 #pragma unroll
     for (int c = 0; c < 8; ++c)
         *reinterpret_cast<uint4*>(row + ((c ^ (r & 7)) << 4)) =
             make_uint4(pk[4 * c], pk[4 * c + 1], pk[4 * c + 2], pk[4 * c + 3]);
 }
 
-__global__ void __launch_bounds__(SGF_THREADS, 1) k_sg_score_fused(const __grid_constant__ CUtensorMap tw, int ntiles,
-                                                                 FusedArgs fa, int* __restrict__ err) {
+__global__ void __launch_bounds__(SGF_THREADS, SGF_CTAS) k_sg_score_fused(const __grid_constant__ CUtensorMap tw,
+                                                                        int ntiles, FusedArgs fa,
+                                                                        int* __restrict__ err) {
     extern __shared__ uint8_t sg_smem_raw[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t raw = umma::smem_u32(sg_smem_raw);
@@ -573,25 +581,25 @@ __global__ void __launch_bounds__(SGF_THREADS, 1) k_sg_score_fused(const __grid_
     uint8_t* smem = sg_smem_raw + (base - raw);
     uint8_t* sA = smem;                                  // [4][128][64] bf16, swizzled
     uint8_t* sW = smem + SGF_A_BYTES;                    // [stage][256][64] bf16, swizzled
-    float* sW0 = reinterpret_cast<float*>(sW + SG_STAGES * SGF_WSTAGE);  // [k][256]
-    float* sb0 = sW0 + SG_MAXIN * SG_W;
+    float* sW0 = reinterpret_cast<float*>(sW + SGF_STAGES * SGF_WSTAGE);  // [k][256], k < in
+    float* sb0 = sW0 + fa.in * SG_W;
     float* sb = sb0 + SG_W;                              // [3][256] b1, b2, b3
     float* sw4 = sb + 3 * SG_W;
-    float* spart = sw4 + SG_W;                           // [4][128]
+    float* spart = sw4 + SG_W;                           // [4][128] quarter sums
     uint64_t* a_ready = reinterpret_cast<uint64_t*>(spart + 4 * SG_TM);
     uint64_t* acc_full = a_ready + 1;
     uint64_t* pready = acc_full + 1;
     uint64_t* w_full = pready + 1;
-    uint64_t* w_empty = w_full + SG_STAGES;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(w_empty + SG_STAGES);
+    uint64_t* w_empty = w_full + SGF_STAGES;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(w_empty + SGF_STAGES);
     int* counts = reinterpret_cast<int*>(tslot + 1);    // [0] weight slices loaded, [1] consumed
     const int my_tiles = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     const int nslices = my_tiles * 3 * 4;
     if (tid == 0) {
-        umma::mbar_init(a_ready, 32 * SGP_EPI_WARPS);
+        umma::mbar_init(a_ready, 32 * SGF_EPI);
         umma::mbar_init(acc_full, 1);
-        umma::mbar_init(pready, 32 * (SGP_EPI_WARPS - 4));
-        for (int s = 0; s < SG_STAGES; ++s) {
+        umma::mbar_init(pready, 32 * (SGF_EPI - 4));
+        for (int s = 0; s < SGF_STAGES; ++s) {
             umma::mbar_init(&w_full[s], 1);
             umma::mbar_init(&w_empty[s], 1);
         }
@@ -599,8 +607,8 @@ __global__ void __launch_bounds__(SGF_THREADS, 1) k_sg_score_fused(const __grid_
         umma::fence_mbar_init();
     }
     for (int i = tid; i < SG_W; i += SGF_THREADS) {
-        for (int k = 0; k < SG_MAXIN; ++k)
-            sW0[k * SG_W + i] = k < fa.in ? __bfloat162float(__float2bfloat16_rn(__ldg(&fa.W0[i * fa.in + k]))) : 0.f;
+        for (int k = 0; k < fa.in; ++k)
+            sW0[k * SG_W + i] = __bfloat162float(__float2bfloat16_rn(__ldg(&fa.W0[i * fa.in + k])));
         sb0[i] = __ldg(&fa.b0[i]);
         sb[i] = __ldg(&fa.b1[i]);
         sb[SG_W + i] = __ldg(&fa.b2[i]);
@@ -621,8 +629,8 @@ __global__ void __launch_bounds__(SGF_THREADS, 1) k_sg_score_fused(const __grid_
         if (lane == 0) {
             int g = 0;
             for (; g < nslices; ++g) {  // slice g: layer (g / 4) % 3, K block g % 4
-                const int s = g % SG_STAGES;
-                if (g >= SG_STAGES && !umma::mbar_wait(&w_empty[s], ((g / SG_STAGES) - 1) & 1, deadline)) {
+                const int s = g % SGF_STAGES;
+                if (g >= SGF_STAGES && !umma::mbar_wait(&w_empty[s], ((g / SGF_STAGES) - 1) & 1, deadline)) {
                     atomicExch(err, 1);
                     break;
                 }
@@ -644,8 +652,8 @@ __global__ void __launch_bounds__(SGF_THREADS, 1) k_sg_score_fused(const __grid_
                 }
                 umma::fence_after_sync();
                 for (int kb = 0; kb < 4; ++kb, ++g) {
-                    const int s = g % SG_STAGES;
-                    if (!umma::mbar_wait(&w_full[s], (g / SG_STAGES) & 1, deadline)) {
+                    const int s = g % SGF_STAGES;
+                    if (!umma::mbar_wait(&w_full[s], (g / SGF_STAGES) & 1, deadline)) {
                         atomicExch(err, 2);
                         ok = false;
                         break;
@@ -665,8 +673,8 @@ __global__ void __launch_bounds__(SGF_THREADS, 1) k_sg_score_fused(const __grid_
         }
         __syncwarp();
     } else {
-        // epilogue warps: lane group (warp % 4) = rows, quarter (warp - 2) / 4 = columns
-        const int grp = warp & 3, qtr = (warp - 2) >> 2, row = grp * 32 + lane;
+        // epilogue warps: lane group (warp % 4) = rows, part (warp - 2) / 4 = columns
+        const int grp = warp & 3, part = (warp - 2) >> 2, row = grp * 32 + lane;
         const uint32_t trow = tmem + ((uint32_t)(grp * 32) << 16);
         bool ok = true;
         for (int i = 0; ok && i < my_tiles; ++i) {
@@ -680,14 +688,14 @@ __global__ void __launch_bounds__(SGF_THREADS, 1) k_sg_score_fused(const __grid_
                     v = (float)((__ldg(&fa.states[(size_t)m * fa.in + k]) - fa.norm[SG_MAXIN + k]) * fa.norm[k]);
                 x[k] = __bfloat162float(__float2bfloat16_rn(v));
             }
-            {
+#pragma unroll 1
+            for (int kb = part * (SGF_PCOLS / 64); kb < (part + 1) * (SGF_PCOLS / 64); ++kb) {
                 // per column z = b0 + x0 w0 + x1 w1 + ... in k order, 16
-                // columns at a time with the weights read as float4 (the
-                // per-k guard is uniform over the block)
+                // columns at a time with the weights read as float4
                 uint32_t pk[32];
 #pragma unroll
                 for (int c = 0; c < 64; c += 16) {
-                    const int n0 = 64 * qtr + c;
+                    const int n0 = 64 * kb + c;
                     float z[16];
 #pragma unroll
                     for (int j = 0; j < 16; j += 4) {
@@ -709,7 +717,7 @@ __global__ void __launch_bounds__(SGF_THREADS, 1) k_sg_score_fused(const __grid_
 #pragma unroll
                     for (int j = 0; j < 16; j += 2) pk[(c + j) / 2] = sgf_pack(sg_silu(z[j]), sg_silu(z[j + 1]));
                 }
-                sgf_store_row(sA, row, qtr, pk);
+                sgf_store_row(sA, row, kb, pk);
             }
             umma::fence_proxy_async();
             umma::fence_before_sync();
@@ -724,41 +732,51 @@ __global__ void __launch_bounds__(SGF_THREADS, 1) k_sg_score_fused(const __grid_
                 umma::fence_after_sync();
                 const float* bias = sb + (l - 1) * SG_W;
                 if (l < 3) {
-                    uint32_t pk[32];
+#pragma unroll 1
+                    for (int kb = part * (SGF_PCOLS / 64); kb < (part + 1) * (SGF_PCOLS / 64); ++kb) {
+                        uint32_t pk[32];
 #pragma unroll
-                    for (int c = 0; c < 64; c += 16) {
-                        float v[16];
-                        umma::tmem_ld16(trow + 64 * qtr + c, v);
+                        for (int c = 0; c < 64; c += 16) {
+                            float v[16];
+                            umma::tmem_ld16(trow + 64 * kb + c, v);
 #pragma unroll
-                        for (int j = 0; j < 16; j += 2)
-                            pk[(c + j) / 2] = sgf_pack(sg_silu(v[j] + bias[64 * qtr + c + j]),
-                                                       sg_silu(v[j + 1] + bias[64 * qtr + c + j + 1]));
+                            for (int j = 0; j < 16; j += 2)
+                                pk[(c + j) / 2] = sgf_pack(sg_silu(v[j] + bias[64 * kb + c + j]),
+                                                           sg_silu(v[j + 1] + bias[64 * kb + c + j + 1]));
+                        }
+                        sgf_store_row(sA, row, kb, pk);
                     }
-                    sgf_store_row(sA, row, qtr, pk);
                     umma::fence_proxy_async();
                     umma::fence_before_sync();
                     umma::mbar_arrive(a_ready);
                 } else {
-                    float out = 0.f;
+                    float qs[SGF_PCOLS / 64];  // this thread's quarter sums
 #pragma unroll
-                    for (int c = 0; c < 64; c += 16) {
-                        float v[16];
-                        umma::tmem_ld16(trow + 64 * qtr + c, v);
+                    for (int h = 0; h < SGF_PCOLS / 64; ++h) {
+                        const int kb = part * (SGF_PCOLS / 64) + h;
+                        float out = 0.f;
 #pragma unroll
-                        for (int j = 0; j < 16; ++j) {
-                            const int nc = 64 * qtr + c + j;
-                            out = fmaf(__bfloat162float(__float2bfloat16_rn(sg_silu(v[j] + bias[nc]))),
-                                       __bfloat162float(__float2bfloat16_rn(sw4[nc])), out);
+                        for (int c = 0; c < 64; c += 16) {
+                            float v[16];
+                            umma::tmem_ld16(trow + 64 * kb + c, v);
+#pragma unroll
+                            for (int j = 0; j < 16; ++j) {
+                                const int nc = 64 * kb + c + j;
+                                out = fmaf(__bfloat162float(__float2bfloat16_rn(sg_silu(v[j] + bias[nc]))),
+                                           __bfloat162float(__float2bfloat16_rn(sw4[nc])), out);
+                            }
                         }
+                        qs[h] = out;
                     }
                     umma::fence_before_sync();
-                    if (qtr) {
-                        spart[qtr * SG_TM + row] = out;
+                    if (part) {
+#pragma unroll
+                        for (int h = 0; h < SGF_PCOLS / 64; ++h) spart[(part * (SGF_PCOLS / 64) + h) * SG_TM + row] = qs[h];
                         umma::mbar_arrive(pready);
                     } else if (umma::mbar_wait(pready, i & 1, deadline)) {
-                        out += spart[SG_TM + row];
-                        out += spart[2 * SG_TM + row];
-                        out += spart[3 * SG_TM + row];
+                        float out = qs[0];  // quarters added in order: 0, 1, 2, 3
+#pragma unroll
+                        for (int q = 1; q < 4; ++q) out += q < SGF_PCOLS / 64 ? qs[q < SGF_PCOLS / 64 ? q : 0] : spart[q * SG_TM + row];
                         if (m < fa.n) fa.out[m] = out + __ldg(fa.b4);
                     } else {
                         if (lane == 0) atomicExch(err, 3);
@@ -774,7 +792,7 @@ __global__ void __launch_bounds__(SGF_THREADS, 1) k_sg_score_fused(const __grid_
     // before the shared memory they write is released
     if (tid == 0) {
         const uint64_t drain = umma::globaltimer_ns() + SG_TIMEOUT_NS;
-        for (int g = counts[1]; g < counts[0]; ++g) umma::mbar_wait(&w_full[g % SG_STAGES], (g / SG_STAGES) & 1, drain);
+        for (int g = counts[1]; g < counts[0]; ++g) umma::mbar_wait(&w_full[g % SGF_STAGES], (g / SGF_STAGES) & 1, drain);
     }
     __syncthreads();
     if (warp == 0) umma::tmem_dealloc(tmem, SG_W);
@@ -1186,7 +1204,9 @@ mptg_status mptg_surrogate_score_dev(mptg_surrogate* s, const double* dstates, i
     if (!s->wmap_ok) return mptg_fail(s->ctx, MPTG_ERR_CUDA, "surrogate scorer: cuTensorMapEncodeTiled failed");
     static std::once_flag attr;
     std::call_once(attr, [] {
-        cudaFuncSetAttribute(k_sg_score_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, SGF_SMEM);
+        cudaFuncSetAttribute(k_sg_score_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, SGF_SMEM(SG_MAXIN));
+        // all of the SM's unified memory as shared memory, so two CTAs fit
+        cudaFuncSetAttribute(k_sg_score_fused, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     });
     SgLayout L = sg_layout(s->in);
     FusedArgs fa;
@@ -1203,8 +1223,8 @@ mptg_status mptg_surrogate_score_dev(mptg_surrogate* s, const double* dstates, i
     fa.b4 = s->P + L.b4;
     fa.out = dlogits;
     const int tiles = (n + SG_TM - 1) / SG_TM;
-    const int grid = std::min(tiles, std::max(1, s->ctx->sms));
-    k_sg_score_fused<<<grid, SGF_THREADS, SGF_SMEM, st>>>(s->wmap, tiles, fa, s->err);
+    const int grid = std::min(tiles, SGF_CTAS * std::max(1, s->ctx->sms));
+    k_sg_score_fused<<<grid, SGF_THREADS, SGF_SMEM(s->in), st>>>(s->wmap, tiles, fa, s->err);
     MPTG_LAUNCHED(s->ctx);
     MPTG_CUDA_TRY(s->ctx, cudaGetLastError());
     return MPTG_OK;
