@@ -251,6 +251,12 @@ mptg_status mptg_planner_set_persistent(mptg_planner* planner, int mode);
  * so the setting changes the speed only.  Default 2^24, which covers every
  * wavefront of up to 1,024 samples over the block planner's 16,384 nodes. */
 mptg_status mptg_planner_set_block_search(mptg_planner* planner, long long brute_pairs);
+/* Runs of the block planner replayed through its captured CUDA graph (no
+ * reference counterpart: a profile of this planner).  A planner captures one
+ * run (job and counters in, the block, counters out) on its stream the first
+ * time it uses the block planner, and replays it for every later run with the
+ * same wavefront size; if the capture fails it launches directly. */
+mptg_status mptg_planner_graph_runs(mptg_planner* planner, uint64_t* runs);
 /* The planner's nearest-neighbour container -- PRRT's nn_ member, the nigh
  * tree its workers query (src/mpt/impl/prrt/prrt.hpp:121-122,406-409) -- as a
  * borrowed tree handle: mptg_nearest / mptg_nearest_k / mptg_nearest_linear /

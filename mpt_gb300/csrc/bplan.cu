@@ -734,18 +734,24 @@ bool bplan_supported(const mptg_scene* sc, int wavefront, int resolution) {
     return sc->kind == MPTG_SCENE_GRID && resolution == 0 && wavefront >= 1 && wavefront <= BPLAN_THREADS;
 }
 
-mptg_status bplan_launch(mptg_ctx* ctx, const BPlanJob* djobs, int njobs, int max_W, int max_cap, cudaStream_t s) {
-    if (njobs <= 0) return MPTG_OK;
-    if (max_W < 1 || max_W > BPLAN_THREADS || max_cap < 1 || max_cap > BPLAN_MAX_NODES)
-        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "block planner: wavefront %d / capacity %d out of range", max_W,
-                         max_cap);
-    const size_t bytes = smem_bytes(max_cap, max_W);
+mptg_status bplan_configure(mptg_ctx* ctx) {
     static int configured = -1;
     if (configured != ctx->device) {
         MPTG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_bplan_grid, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)smem_bytes(BPLAN_MAX_NODES, BPLAN_THREADS)));
         configured = ctx->device;
     }
+    return MPTG_OK;
+}
+
+mptg_status bplan_launch(mptg_ctx* ctx, const BPlanJob* djobs, int njobs, int max_W, int max_cap, cudaStream_t s) {
+    if (njobs <= 0) return MPTG_OK;
+    if (max_W < 1 || max_W > BPLAN_THREADS || max_cap < 1 || max_cap > BPLAN_MAX_NODES)
+        return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "block planner: wavefront %d / capacity %d out of range", max_W,
+                         max_cap);
+    const size_t bytes = smem_bytes(max_cap, max_W);
+    mptg_status st = bplan_configure(ctx);
+    if (st) return st;
     k_bplan_grid<<<njobs, BPLAN_THREADS, bytes, s>>>(djobs, max_cap, max_W);
     MPTG_LAUNCHED(ctx);
     MPTG_CUDA_TRY(ctx, cudaGetLastError());

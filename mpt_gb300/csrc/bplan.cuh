@@ -64,6 +64,9 @@ struct BPlanJob {
 // rings of the bucket grid
 #define BPLAN_BRUTE_PAIRS (1LL << 24)
 
+// Sets the kernel's shared-memory limit on the context's device (once); done
+// by bplan_launch, and before a stream capture of it.
+mptg_status bplan_configure(mptg_ctx* ctx);
 // Runs njobs jobs (device array), one thread block each, on stream s.
 mptg_status bplan_launch(mptg_ctx* ctx, const BPlanJob* djobs, int njobs, int max_W, int max_cap, cudaStream_t s);
 // true when the scene and parameters are ones the block planner runs

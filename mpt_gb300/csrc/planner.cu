@@ -152,6 +152,13 @@ struct mptg_planner {
     BPlanJob* bp_job = nullptr;
     BPlanJob* bp_hjob = nullptr;        // pinned: the job's copy is asynchronous
     long long bp_brute_pairs = BPLAN_BRUTE_PAIRS;
+    // a run of the block planner as a CUDA graph (job and counters in from the
+    // pinned host copies, the block, the counters out), captured on the first
+    // run and replayed after; bp_graph_W: the wavefront it was captured for
+    cudaGraphExec_t bp_graph = nullptr;
+    int bp_graph_W = 0;
+    bool bp_graph_off = false;
+    uint64_t bp_graph_runs = 0;
     BPlanCounters* bp_hctr = nullptr;   // pinned
     uint8_t* bp_hgoal = nullptr;        // pinned [bp_cap]
     uint64_t stat_bp_waves = 0;         // wavefronts run inside the block planner
@@ -640,6 +647,7 @@ static void planner_free(mptg_planner* p) {
         if (x) cudaFree(x);
     if (p->hbuf) cudaFreeHost(p->hbuf);
     if (p->hgoal) cudaFreeHost(p->hgoal);
+    if (p->bp_graph) cudaGraphExecDestroy(p->bp_graph);
     if (p->bp_hjob) cudaFreeHost(p->bp_hjob);
     if (p->bp_hctr) cudaFreeHost(p->bp_hctr);
     if (p->bp_hgoal) cudaFreeHost(p->bp_hgoal);
@@ -1013,6 +1021,41 @@ static bool bp_applies(const mptg_planner* p) {
     return p->bp_mode && !p->star && !p->sg && bplan_supported(p->scene, p->prm.wavefront, p->prm.resolution);
 }
 
+// Captures a block-planner run as a CUDA graph on the planner's stream: the
+// job and counters copied in from the pinned host copies (read when the graph
+// runs, so the host fills them before each launch), the block, the counters
+// copied out.  A capture or instantiation that fails leaves the planner on the
+// direct launches for good (bp_graph_off); either way the work is the same.
+static void bp_capture(mptg_planner* p, int W) {
+    mptg_ctx* ctx = p->ctx;
+    cudaStream_t s = p->stream;
+    if (bplan_configure(ctx) != MPTG_OK) {  // the attribute call is not allowed inside a capture
+        p->bp_graph_off = true;
+        return;
+    }
+    cudaGraph_t g = nullptr;
+    bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+        bool counted = false;  // bplan_launch counted a launch that the capture only recorded
+        ok = cudaMemcpyAsync(p->bp_job, p->bp_hjob, sizeof(BPlanJob), cudaMemcpyHostToDevice, s) == cudaSuccess &&
+             cudaMemcpyAsync(p->bp_ctr, p->bp_hctr, sizeof(BPlanCounters), cudaMemcpyHostToDevice, s) ==
+                 cudaSuccess &&
+             (counted = bplan_launch(ctx, p->bp_job, 1, W, p->bp_cap, s) == MPTG_OK) &&
+             cudaMemcpyAsync(p->bp_hctr, p->bp_ctr, sizeof(BPlanCounters), cudaMemcpyDeviceToHost, s) == cudaSuccess;
+        const cudaError_t e = cudaStreamEndCapture(s, &g);
+        ok = ok && e == cudaSuccess && g;
+        if (counted) ctx->launches.fetch_sub(1, std::memory_order_relaxed);  // each replay counts one launch
+    }
+    if (ok && cudaGraphInstantiate(&p->bp_graph, g, 0) == cudaSuccess) {
+        p->bp_graph_W = W;
+    } else {
+        p->bp_graph = nullptr;
+        p->bp_graph_off = true;
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+}
+
 // the ring search's bucket grid: 64 x 64 cells over the sampling box (square
 // cells on its longer side)
 static void bp_cells(BPlanJob& j, const double* lo, const double* hi) {
@@ -1077,12 +1120,23 @@ static mptg_status run_persistent(mptg_planner* p, int max_waves, double time_li
         p->bp_n = n0;
     }
     *p->bp_hjob = j;  // the previous run's copy ended at its synchronisation
-    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_job, p->bp_hjob, sizeof(j), cudaMemcpyHostToDevice, s));
-    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_ctr, h, sizeof(*h), cudaMemcpyHostToDevice, s));
+    if (p->bp_graph && p->bp_graph_W != W) {
+        cudaGraphExecDestroy(p->bp_graph);
+        p->bp_graph = nullptr;
+    }
+    if (!p->bp_graph && !p->bp_graph_off) bp_capture(p, W);
     MPTG_CUDA_TRY(ctx, cudaEventRecord(p->ev[0], s));
-    if ((st = bplan_launch(ctx, p->bp_job, 1, W, p->bp_cap, s))) return st;
+    if (p->bp_graph) {
+        MPTG_CUDA_TRY(ctx, cudaGraphLaunch(p->bp_graph, s));
+        MPTG_LAUNCHED(ctx);
+        ++p->bp_graph_runs;
+    } else {
+        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_job, p->bp_hjob, sizeof(j), cudaMemcpyHostToDevice, s));
+        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(p->bp_ctr, h, sizeof(*h), cudaMemcpyHostToDevice, s));
+        if ((st = bplan_launch(ctx, p->bp_job, 1, W, p->bp_cap, s))) return st;
+        MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(h, p->bp_ctr, sizeof(*h), cudaMemcpyDeviceToHost, s));
+    }
     MPTG_CUDA_TRY(ctx, cudaEventRecord(p->ev[1], s));
-    MPTG_CUDA_TRY(ctx, cudaMemcpyAsync(h, p->bp_ctr, sizeof(*h), cudaMemcpyDeviceToHost, s));
     MPTG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     {
         // the phase timers (nearest, valid motion, insert) share the block's
@@ -1126,6 +1180,12 @@ extern "C" {
 mptg_status mptg_planner_set_persistent(mptg_planner* p, int mode) {
     if (!p || mode < 0 || mode > 1) return MPTG_ERR_INVALID_ARG;
     p->bp_mode = mode;
+    return MPTG_OK;
+}
+
+mptg_status mptg_planner_graph_runs(mptg_planner* p, uint64_t* runs) {
+    if (!p || !runs) return MPTG_ERR_INVALID_ARG;
+    *runs = p->bp_graph_runs;
     return MPTG_OK;
 }
 

@@ -139,6 +139,7 @@ def _sig(L):
         ("mptg_planner_tree", ctypes.c_int, [P, ctypes.POINTER(P)]),
         ("mptg_planner_set_persistent", ctypes.c_int, [P, ctypes.c_int]),
         ("mptg_planner_set_block_search", ctypes.c_int, [P, ctypes.c_longlong]),
+        ("mptg_planner_graph_runs", ctypes.c_int, [P, ctypes.POINTER(ctypes.c_uint64)]),
         ("mptg_planner_stats", ctypes.c_int, [P, P]),
         ("mptg_planner_timers", ctypes.c_int, [P, P]),
         ("mptg_planner_block_profile", ctypes.c_int, [P, P]),
@@ -412,6 +413,13 @@ class Planner:
         keys = ["wavefronts", "samples", "nodes_added", "tree_size", "goals", "link_states_checked", "seconds",
                 "wavefront_counter"]
         return dict(zip(keys, [float(v) for v in out]))
+
+    def graph_runs(self) -> int:
+        """Block-planner runs replayed through the planner's captured CUDA graph."""
+        n = ctypes.c_uint64(0)
+        if self.h is not None:
+            _check(self.ctx.h, self.lib.mptg_planner_graph_runs(self.h, ctypes.byref(n)))
+        return int(n.value)
 
     def block_profile(self) -> dict:
         """The persistent block planner's SM cycles per phase and FP64 fallback

@@ -112,6 +112,20 @@ def test_block_planner_node_budget_and_capacity_hand_over(ctx, orc):
     pl.close()
 
 
+def test_block_planner_runs_replay_a_captured_graph(ctx, orc):
+    """After its first run a planner replays the block planner through a CUDA
+    graph captured on its stream; the tree is still the oracle's replay."""
+    sc = scenes.grid_scene()
+    pl = _planner(ctx, sc, 48, 52, 1 << 20)
+    for _ in range(6):
+        pl.run(5)
+    assert pl.graph_runs() >= 5
+    states, parents = pl.graph()
+    ws, wp, _ = _oracle(orc, sc, 48, 52, 1 << 20, 30, False)
+    assert _same(states, ws) and np.array_equal(parents, wp)
+    pl.close()
+
+
 def test_block_planner_solves_and_paths_revalidate(ctx, orc):
     """The grid's time to a first solution through the block planner, and the
     oracle's checker on every returned path."""
