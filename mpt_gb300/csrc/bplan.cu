@@ -735,23 +735,26 @@ bool bplan_supported(const mptg_scene* sc, int wavefront, int resolution) {
 }
 
 mptg_status bplan_configure(mptg_ctx* ctx) {
-    static int configured = -1;
-    if (configured != ctx->device) {
-        MPTG_CUDA_TRY(ctx, cudaFuncSetAttribute(k_bplan_grid, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)smem_bytes(BPLAN_MAX_NODES, BPLAN_THREADS)));
-        configured = ctx->device;
-    }
+    // the caller has made ctx's device current (and may be capturing a graph,
+    // so nothing here may change the device)
+    MPTG_CUDA_TRY(ctx, mptg_once_per_device((const void*)k_bplan_grid, [] {
+        return cudaFuncSetAttribute(k_bplan_grid, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem_bytes(BPLAN_MAX_NODES, BPLAN_THREADS));
+    }));
     return MPTG_OK;
 }
 
-mptg_status bplan_launch(mptg_ctx* ctx, const BPlanJob* djobs, int njobs, int max_W, int max_cap, cudaStream_t s) {
+mptg_status bplan_launch(mptg_ctx* ctx, const BPlanJob* djobs, int njobs, int max_W, int max_cap, cudaStream_t s,
+                         bool configure) {
     if (njobs <= 0) return MPTG_OK;
     if (max_W < 1 || max_W > BPLAN_THREADS || max_cap < 1 || max_cap > BPLAN_MAX_NODES)
         return mptg_fail(ctx, MPTG_ERR_INVALID_ARG, "block planner: wavefront %d / capacity %d out of range", max_W,
                          max_cap);
     const size_t bytes = smem_bytes(max_cap, max_W);
-    mptg_status st = bplan_configure(ctx);
-    if (st) return st;
+    if (configure) {
+        mptg_status st = bplan_configure(ctx);
+        if (st) return st;
+    }
     k_bplan_grid<<<njobs, BPLAN_THREADS, bytes, s>>>(djobs, max_cap, max_W);
     MPTG_LAUNCHED(ctx);
     MPTG_CUDA_TRY(ctx, cudaGetLastError());

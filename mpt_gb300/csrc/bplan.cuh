@@ -67,7 +67,10 @@ struct BPlanJob {
 // Sets the kernel's shared-memory limit on the context's device (once); done
 // by bplan_launch, and before a stream capture of it.
 mptg_status bplan_configure(mptg_ctx* ctx);
-// Runs njobs jobs (device array), one thread block each, on stream s.
-mptg_status bplan_launch(mptg_ctx* ctx, const BPlanJob* djobs, int njobs, int max_W, int max_cap, cudaStream_t s);
+// Runs njobs jobs (device array), one thread block each, on stream s;
+// configure false: bplan_configure has run already (inside a stream capture
+// the launch makes no other runtime call).
+mptg_status bplan_launch(mptg_ctx* ctx, const BPlanJob* djobs, int njobs, int max_W, int max_cap, cudaStream_t s,
+                         bool configure = true);
 // true when the scene and parameters are ones the block planner runs
 bool bplan_supported(const mptg_scene* sc, int wavefront, int resolution);

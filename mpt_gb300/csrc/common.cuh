@@ -62,6 +62,25 @@ mptg_status mptg_stage_out_alloc(mptg_ctx* ctx, void* user, size_t bytes, cudaSt
 // copies an output temporary back to the caller (async) and releases temporaries
 mptg_status mptg_stage_finish(mptg_ctx* ctx, cudaStream_t s, DevBuf* outs, int nouts, DevBuf* ins, int nins);
 
+// Runs fn() (returning cudaError_t) the first time for (key, the current
+// device) and after any call that failed: for per-device one-time settings
+// such as cudaFuncSetAttribute, which applies to the current device only.
+// Thread-safe; the settings of different keys may run concurrently.
+template <class Fn>
+inline cudaError_t mptg_once_per_device(const void* key, Fn fn) {
+    static std::mutex mu;
+    static std::vector<std::pair<const void*, int>> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    for (const auto& d : done)
+        if (d.first == key && d.second == dev) return cudaSuccess;
+    e = fn();
+    if (e == cudaSuccess) done.emplace_back(key, dev);
+    return e;
+}
+
 static inline unsigned mptg_blocks(size_t n, unsigned threads) {
     return (unsigned)((n + threads - 1) / threads);
 }

@@ -1040,7 +1040,7 @@ static void bp_capture(mptg_planner* p, int W) {
         ok = cudaMemcpyAsync(p->bp_job, p->bp_hjob, sizeof(BPlanJob), cudaMemcpyHostToDevice, s) == cudaSuccess &&
              cudaMemcpyAsync(p->bp_ctr, p->bp_hctr, sizeof(BPlanCounters), cudaMemcpyHostToDevice, s) ==
                  cudaSuccess &&
-             (counted = bplan_launch(ctx, p->bp_job, 1, W, p->bp_cap, s) == MPTG_OK) &&
+             (counted = bplan_launch(ctx, p->bp_job, 1, W, p->bp_cap, s, false) == MPTG_OK) &&
              cudaMemcpyAsync(p->bp_hctr, p->bp_ctr, sizeof(BPlanCounters), cudaMemcpyDeviceToHost, s) == cudaSuccess;
         const cudaError_t e = cudaStreamEndCapture(s, &g);
         ok = ok && e == cudaSuccess && g;

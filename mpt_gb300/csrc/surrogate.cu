@@ -1024,10 +1024,9 @@ static bool bf16_map(CUtensorMap* m, const bf16* base, uint64_t rows, uint64_t c
 template <int EPI>
 static mptg_status sg_gemm(mptg_surrogate* s, const bf16* A, int rowsA, int lda, const bf16* B, int ldb, int K,
                            int kblocks, const EpiArgs& ep, cudaStream_t st) {
-    static std::once_flag attr;
-    std::call_once(attr, [] {
-        cudaFuncSetAttribute(k_sg_umma<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, SG_SMEM);
-    });
+    MPTG_CUDA_TRY(s->ctx, mptg_once_per_device((const void*)k_sg_umma<EPI>, [] {
+        return cudaFuncSetAttribute(k_sg_umma<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, SG_SMEM);
+    }));
     CUtensorMap ta, tb;
     if (!bf16_map(&ta, A, (uint64_t)rowsA, (uint64_t)K, (uint64_t)lda, SG_TM) ||
         !bf16_map(&tb, B, SG_W, (uint64_t)K, (uint64_t)ldb, SG_W))
@@ -1044,10 +1043,9 @@ static mptg_status sg_gemm(mptg_surrogate* s, const bf16* A, int rowsA, int lda,
 template <int EPI>
 static mptg_status sg_gemm_p(mptg_surrogate* s, const bf16* A, int rowsA, const bf16* B, const EpiArgs& ep,
                              cudaStream_t st) {
-    static std::once_flag attr;
-    std::call_once(attr, [] {
-        cudaFuncSetAttribute(k_sg_umma_p<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, SGP_SMEM);
-    });
+    MPTG_CUDA_TRY(s->ctx, mptg_once_per_device((const void*)k_sg_umma_p<EPI>, [] {
+        return cudaFuncSetAttribute(k_sg_umma_p<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, SGP_SMEM);
+    }));
     CUtensorMap ta, tb;
     if (!bf16_map(&ta, A, (uint64_t)rowsA, SG_W, SG_W, SG_TM) || !bf16_map(&tb, B, SG_W, SG_W, SG_W, SG_W))
         return mptg_fail(s->ctx, MPTG_ERR_CUDA, "surrogate GEMM: cuTensorMapEncodeTiled failed");
@@ -1202,12 +1200,13 @@ mptg_status mptg_surrogate_set(mptg_surrogate* s, const float* in, size_t n) {
 mptg_status mptg_surrogate_score_dev(mptg_surrogate* s, const double* dstates, int n, float* dlogits, cudaStream_t st) {
     if (n <= 0) return MPTG_OK;
     if (!s->wmap_ok) return mptg_fail(s->ctx, MPTG_ERR_CUDA, "surrogate scorer: cuTensorMapEncodeTiled failed");
-    static std::once_flag attr;
-    std::call_once(attr, [] {
-        cudaFuncSetAttribute(k_sg_score_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, SGF_SMEM(SG_MAXIN));
+    MPTG_CUDA_TRY(s->ctx, mptg_once_per_device((const void*)k_sg_score_fused, [] {
+        cudaError_t e =
+            cudaFuncSetAttribute(k_sg_score_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, SGF_SMEM(SG_MAXIN));
         // all of the SM's unified memory as shared memory, so two CTAs fit
-        cudaFuncSetAttribute(k_sg_score_fused, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    });
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sg_score_fused, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        return e;
+    }));
     SgLayout L = sg_layout(s->in);
     FusedArgs fa;
     fa.states = dstates;
