@@ -456,7 +456,8 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
                                                                  int W_alloc) {
     static_assert(BPLAN_MAX_NODES <= 32767, "node ids are kept as short in the cell lists");
     extern __shared__ __align__(16) unsigned char bp_smem[];
-    __shared__ int s_n, s_goals, s_maxabs, s_gidx, s_stop, s_total;
+    __shared__ int s_n, s_goals, s_maxabs, s_stop, s_total;
+    __shared__ int s_gidx[2];  // goal sample of the wavefronts of even / odd index
     __shared__ int s_wsum[32];
     __shared__ int s_bb[4];
     __shared__ unsigned long long s_prof[3];  // FP64 fallbacks: near ties, unsure samples, step counts
@@ -475,6 +476,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
         s_prof[0] = s_prof[1] = s_prof[2] = 0;
         s_bb[0] = s_bb[2] = INT_MAX;
         s_bb[1] = s_bb[3] = -1;
+        s_gidx[0] = s_gidx[1] = INT_MAX;
     }
     __syncthreads();
     for (int j = t; j < s_n; j += T) {
@@ -497,6 +499,12 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
     const uint64_t t0 = umma::globaltimer_ns();
     __syncthreads();
     for (;;) {
+        // goal sample: the lowest index whose bias draw hits (k_plan_goalpick),
+        // gathered before the stop check's barrier into this wavefront's slot
+        // (the other slot is cleared for the next wavefront meanwhile)
+        const bool bias_on = s_goals == 0 && J.has_goal && J.goal_bias > 0;
+        if (bias_on && t < W && phx_uniform(J.seed, (uint32_t)t, wave, 16) < J.goal_bias)
+            atomicMin(&s_gidx[wave & 1], t);
         // the run loop's stop checks (mptg_planner_run), decided by one thread
         if (t == 0) {
             int st = 0;
@@ -506,7 +514,7 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
             else if ((size_t)s_n + (size_t)W > (size_t)cap && (size_t)cap < J.max_nodes) st = 2;
             else if (J.deadline_ns && umma::globaltimer_ns() - t0 >= J.deadline_ns) st = 1;
             s_stop = st;
-            s_gidx = INT_MAX;
+            s_gidx[(wave + 1) & 1] = INT_MAX;
         }
         __syncthreads();
         if (s_stop) {
@@ -515,13 +523,9 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
         }
         if (t == 0) tc = clock64();
         const int n = s_n;
-        // goal sample: the lowest index whose bias draw hits (k_plan_goalpick)
-        const bool bias_on = s_goals == 0 && J.has_goal && J.goal_bias > 0;
-        if (bias_on && t < W && phx_uniform(J.seed, (uint32_t)t, wave, 16) < J.goal_bias) atomicMin(&s_gidx, t);
-        __syncthreads();
         if (t < W) {
             double* q = S.q + 2 * t;
-            if (bias_on && t == s_gidx) {
+            if (bias_on && t == s_gidx[wave & 1]) {
                 q[0] = J.goal[0];
                 q[1] = J.goal[1];
             } else {
@@ -665,27 +669,36 @@ __global__ void __launch_bounds__(BPLAN_THREADS, 1) k_bplan_grid(const BPlanJob*
         }
         __syncthreads();
         mark(4);
-        // accepted samples in sample order (k_plan_scan / k_plan_scatter)
+        // accepted samples in sample order (k_plan_scan / k_plan_scatter);
+        // a wavefront of at most 32 samples lies in warp 0, whose ballot is
+        // the whole scan (no barrier), others take a block scan of the warps
         const int f = (t < W && S.fl[t] == 1) ? 1 : 0;
         const unsigned m = __ballot_sync(0xffffffffu, f);
-        if (lane == 0) s_wsum[warp] = __popc(m);
-        __syncthreads();
-        if (warp == 0) {
-            const int v = lane < nwarps ? s_wsum[lane] : 0;
-            int x = v;
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= o) x += y;
-            }
-            s_wsum[lane] = x - v;
-            if (lane == 31) s_total = x;
-        }
-        __syncthreads();
-        const int nacc = s_total;
         const size_t room = J.max_nodes - (size_t)n;
-        const int keep = (size_t)nacc > room ? (int)room : nacc;  // node budget: the first accepted samples
+        int keep = 0, base = 0;
+        if (W <= 32) {
+            const int nacc = __popc(m);  // warp 0's; the other warps hold no sample
+            keep = (size_t)nacc > room ? (int)room : nacc;
+        } else {
+            if (lane == 0) s_wsum[warp] = __popc(m);
+            __syncthreads();
+            if (warp == 0) {
+                const int v = lane < nwarps ? s_wsum[lane] : 0;
+                int x = v;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= o) x += y;
+                }
+                s_wsum[lane] = x - v;
+                if (lane == 31) s_total = x;
+            }
+            __syncthreads();
+            const int nacc = s_total;
+            keep = (size_t)nacc > room ? (int)room : nacc;  // node budget: the first accepted samples
+            base = s_wsum[warp];
+        }
         if (f) {
-            const int pos = s_wsum[warp] + __popc(m & ((1u << lane) - 1u));
+            const int pos = base + __popc(m & ((1u << lane) - 1u));
             if (pos < keep) {
                 const int id = n + pos;
                 const double* nw = S.nw + 2 * t;

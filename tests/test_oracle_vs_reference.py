@@ -102,7 +102,7 @@ def test_goal_state(orc):
 
 def _check_reference_solution(orc, sc, r, steered=True):
     """The acceptance rules of test/planner_integration_test.hpp:219-291 on a
-    path from the reference's own planner, judged by the oracle's checker.
+    path from the reference's own planner, checked by the oracle's checker.
     steered: every edge within the range (PRRT; PRRT* rewiring and PPRM link
     k-nearest neighbours at any distance)."""
     path = r["path"]
