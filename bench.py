@@ -174,12 +174,21 @@ def edge_rates(ctx, m, stream, torch):
     return out
 
 
+def _nn_alg_bytes(per, nq, D):
+    """Algorithmic bytes of one k_nearest launch from its device counters: the
+    FP32 coordinates of every point evaluated (4D), an internal node's record
+    and cell bounds (16 + 8D), a leaf's record (16), a re-ranked candidate's
+    FP64 state and point id (8D + 4; the ids of the other points are not
+    read), and each query in and its answer out (8D + 12)."""
+    return (per["points_evaluated"] * 4 * D + per["internal_visited"] * (16 + 8 * D) + per["leaves_visited"] * 16
+            + per["reranked"] * (8 * D + 4) + nq * (8 * D + 12))
+
+
 def _nn_roofline(cnt, steps, nq, D, avg_s, peak, kernel):
     """Algorithmic bytes of one NN launch from the device counters, over the
     launch time, against the HBM peak (the same formula as the headline)."""
     per = {k: v / steps for k, v in cnt.items()}
-    alg = (per["points_evaluated"] * (4 * D + 4) + per["internal_visited"] * (16 + 8 * D) + per["leaves_visited"] * 16
-           + per["reranked"] * 8 * D + nq * (8 * D + 12))
+    alg = _nn_alg_bytes(per, nq, D)
     ach = alg / avg_s / 1e9
     return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "kernel": kernel,
             "alg_bytes_per_launch": alg, "counters_per_launch": per}
@@ -841,8 +850,7 @@ def run_gpu(args):
     # roofline of k_nearest: algorithmic bytes per launch from the device counters
     D = sc["dim"]
     per_launch = {k: v / args.steps for k, v in cnt.items()}
-    alg_bytes = (per_launch["points_evaluated"] * (4 * D + 4) + per_launch["internal_visited"] * (16 + 8 * D)
-                 + per_launch["leaves_visited"] * 16 + per_launch["reranked"] * 8 * D + nqb * (8 * D + 12))
+    alg_bytes = _nn_alg_bytes(per_launch, nqb, D)
     avg_s = total_ms / 1000.0 / args.steps
     peak, peak_kind = _peaks()
     achieved = alg_bytes / avg_s / 1e9

@@ -515,9 +515,11 @@ __device__ __forceinline__ float cell_lb(const TreeView& t, int c, float myq, in
 // Candidate step shared by the tree and the linear scan: each lane holds one
 // point (id pid, FP32 distance d32).  Every point that could beat or tie the
 // current best in exact arithmetic is re-ranked in FP64.
+// ids: when not null, the lane's point id is ids[lane], read only for a
+// candidate (most buckets have none), and pid is ignored.
 __device__ __forceinline__ void rerank_step(const TreeView& t, const double* __restrict__ qd, int lane, bool have,
                                             int pid, float d32, float E, double& best, int& bidx, float& bestf_up,
-                                            unsigned long long& nrerank) {
+                                            unsigned long long& nrerank, const int* __restrict__ ids = nullptr) {
     // most buckets hold no point that can reach the current best: leave
     // before the bucket-minimum reduction (the candidate set is unchanged)
     if (!__any_sync(0xffffffffu, have && __fsub_rd(d32, E) <= bestf_up)) return;
@@ -532,6 +534,7 @@ __device__ __forceinline__ void rerank_step(const TreeView& t, const double* __r
     double dd = INFINITY;
     int pp = INT_MAX;
     if (cand) {
+        if (ids) pid = __ldg(&ids[lane]);
         dd = dist64(t.metric, t.D, t.w0, t.w1, qd, t.states64 + (size_t)pid * t.D);
         pp = pid;
         if (!(dd == dd)) { dd = INFINITY; pp = INT_MAX; }
@@ -646,10 +649,8 @@ __device__ __forceinline__ void nearest_one(const TreeView& t, const double* __r
         n_pts += cnt;
         bool have = lane < cnt;
         float d32 = INFINITY;
-        int pid = -1;
+        const size_t b = (size_t)nd.y;
         if (have) {
-            size_t b = (size_t)nd.y;
-            pid = __ldg(&t.bids[b * MPTG_BUCKET + lane]);
             const float* bp = t.bpts + b * (size_t)D * MPTG_BUCKET + lane;  // dimension d at bp[32 d]
             float p[DMAX];
             if (D == DMAX) {  // the exact-dimension instantiation: no per-dimension guard
@@ -662,7 +663,7 @@ __device__ __forceinline__ void nearest_one(const TreeView& t, const double* __r
             d32 = dist32<MK, DMAX>(q, p, t.w0f, t.w1f);
             if (!(d32 == d32)) d32 = INFINITY;
         }
-        rerank_step(t, qd, lane, have, pid, d32, E, best, bidx, bestf_up, n_rr);
+        rerank_step(t, qd, lane, have, -1, d32, E, best, bidx, bestf_up, n_rr, t.bids + b * MPTG_BUCKET);
         // pop the next far child whose bound can still beat the best
         bool found = false;
         while (sp > 0) {
