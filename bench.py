@@ -35,8 +35,8 @@ N_TREE = 1 << 20
 BATCH = 65536
 N_EDGES = 65536
 # DRAM bytes (read + write) per query of k_nearest on the 1M-node tree, from one
-# ncu capture of a 32,768-query launch: 7.266 GB read + 7.6 MB written
-NN_DRAM_BYTES_PER_QUERY = (7.266e9 + 7.6e6) / 32768
+# ncu capture of a 32,768-query launch: 4.589 GB read + 6.6 MB written
+NN_DRAM_BYTES_PER_QUERY = (4.589e9 + 6.6e6) / 32768
 
 
 def _peaks():
