@@ -307,7 +307,7 @@ mptg_status mptg_planner_stats(mptg_planner* planner, double out[8]);
 /* Persistent block planner (grid scenes, mptg_planner_set_persistent), summed
  * over its runs: SM cycles in [0] the sample phase, [1] the nearest-search
  * phase, which also runs each sample's steer and link set-up as soon as its
- * nearest node is known, [2] and [3] zero (earlier separate phases), [4] the
+ * nearest node is known, [2] and [3] unused (zero), [4] the
  * link-sample phase and [5] the insert phase; [6] FP64 distances of the
  * nearest search beyond the winners', [7] interior samples decided in FP64,
  * [8] edge step counts decided in FP64.  No reference counterpart (a profile
