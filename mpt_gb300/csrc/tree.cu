@@ -1317,9 +1317,15 @@ __global__ void __launch_bounds__(256) k_nearest_k(TreeView t, const double* __r
         if (have) {
             size_t b = (size_t)nd.y;
             pid = __ldg(&t.bids[b * MPTG_BUCKET + lane]);
+            const float* bp = t.bpts + b * (size_t)D * MPTG_BUCKET + lane;  // dimension d at bp[32 d]
             float p[DMAX];
+            if (D == DMAX) {  // the exact-dimension instantiation: no per-dimension guard
 #pragma unroll
-            for (int d = 0; d < DMAX; ++d) p[d] = d < D ? __ldg(&t.bpts[(b * D + d) * MPTG_BUCKET + lane]) : 0.f;
+                for (int d = 0; d < DMAX; ++d) p[d] = __ldg(bp + d * MPTG_BUCKET);
+            } else {
+#pragma unroll
+                for (int d = 0; d < DMAX; ++d) p[d] = d < D ? __ldg(bp + d * MPTG_BUCKET) : 0.f;
+            }
             d32 = dist32<MK, DMAX>(q, p, t.w0f, t.w1f);
             if (!(d32 == d32)) d32 = INFINITY;
         }
