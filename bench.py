@@ -443,6 +443,55 @@ def reference_planners(runs=None):
     return out
 
 
+def reference_serving(sample=48, cap_s=2.0, seed=20261208):
+    """The serving batch's CPU baseline: the reference's own PRRT (all host
+    cores, its OpenMP worker pool) answering the first `sample` queries of the
+    512-query batch one after another, as one Planner per query, with the
+    same starts, goals and scenes, each until its first solution or cap_s (the
+    reference has no node budget).  A bounded sample of the batch; returns its
+    queries/s and time-to-solution figures.  None where the reference headers
+    are not present."""
+    from oracle import ref
+    if not ref.available():
+        return None
+    ref.lib()
+    p = subprocess.run([sys.executable, os.path.abspath(__file__), "--ref-serve-child", str(sample), str(cap_s),
+                        str(seed)], capture_output=True, text=True, timeout=sample * (cap_s + 30) + 300)
+    rows = [json.loads(l_) for l_ in p.stdout.splitlines() if l_.startswith("{")]
+    wall = sum(r_["wall_s"] for r_ in rows)
+    sol = sorted(r_["solve_s"] for r_ in rows if r_["solved"])
+    per = {}
+    for k in ("grid", "arm", "mesh"):
+        rk = [r_ for r_ in rows if r_["kind"] == k]
+        sk = sorted(r_["solve_s"] for r_ in rk if r_["solved"])
+        per[k] = {"queries": len(rk), "solved": len(sk), "p50_s": sk[len(sk) // 2] if sk else None}
+    out = {"kind": "reference PRRT (compiled from its headers; NN and collision stand-ins), all host cores",
+           "host_cores": os.cpu_count(), "queries": len(rows), "sample_of": 512, "cap_s": cap_s,
+           "wall_s": wall, "queries_per_s": len(rows) / wall if wall > 0 else None, "solved": len(sol),
+           "p50_solve_s": sol[len(sol) // 2] if sol else None, "per_scene": per}
+    if p.returncode != 0 or len(rows) < sample:
+        out["incomplete"] = {"queries_finished": len(rows), "returncode": p.returncode,
+                             "stderr_tail": p.stderr[-200:]}
+    return out
+
+
+def _ref_serve_child(sample, cap, seed):
+    """Child process of reference_serving: one JSON line per query."""
+    import oracle
+    from oracle import ref
+
+    def orc_valid(d, c):
+        return oracle.valid_states(d, oracle.make_space(d["metric"], d["dim"], d["weights"]), c)
+
+    for i, (d, a, b, budget) in enumerate(_serving_pairs(512, seed, orc_valid)[:sample]):
+        q = dict(d)
+        q["start"], q["goal"] = a, b
+        t0 = time.perf_counter()
+        r_ = ref.plan_solve(q, seed + i, algo="prrt", threads=0, time_limit_s=cap)
+        print(json.dumps({"i": i, "kind": d["kind"], "solved": r_["solved"], "solve_s": r_["solve_s"],
+                          "wall_s": time.perf_counter() - t0}), flush=True)
+
+
 def _ref_plan_child(mk, algo, threads, nseeds, cap):
     """Child process of reference_planners: one JSON line per seed."""
     from oracle import ref
@@ -642,6 +691,36 @@ def prm_section(ctx, seeds=3, cap_s=20.0):
     return out
 
 
+def _serving_pairs(n, seed, valid):
+    """The serving benchmark's queries without a GPU: per query its scene kind,
+    start, goal and node budget, the starts and goals rejection-sampled valid
+    by valid(desc, states) -> 1/0 per state (the GPU's validity or the
+    oracle's, which agree bit for bit)."""
+    from mpt_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    descs = [scenes.grid_scene(), scenes.arm_scene(), scenes.mesh_scene()]
+    kinds = rng.integers(0, 3, n)
+    pools = []
+    for k, d in enumerate(descs):
+        need = 2 * int((kinds == k).sum())
+        got = []
+        s = 0
+        while sum(len(g) for g in got) < need:
+            c = scenes.uniform_states(d, 8 * need + 64, seed + 17 * k + s)
+            got.append(c[valid(d, c) == 1])
+            s += 1
+        pools.append(np.concatenate(got)[:need])
+    used = [0, 0, 0]
+    out = []
+    for i in range(n):
+        k = int(kinds[i])
+        a, b = pools[k][used[k]], pools[k][used[k] + 1]
+        used[k] += 2
+        budget = int(round(math.exp(rng.uniform(math.log(1000), math.log(200000)))))
+        out.append((descs[k], a, b, budget))
+    return out
+
+
 def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0, wave_for=None, surrogate=None):
     """Config of the serving benchmark: n queries uniform over the three scenes,
     start and goal rejection-sampled valid, node budgets log-uniform in
@@ -653,31 +732,17 @@ def batch_queries(m, ctx, n, seed=20261208, time_limit=10.0, wave_for=None, surr
     instead of a thousand (the grid's persistent block planner runs a
     wavefront in microseconds and keeps the tuned size)."""
     from mpt_gb300 import planner as P
-    from mpt_gb300 import scenes
     from mpt_gb300.batch import Query
-    rng = np.random.default_rng(seed)
-    descs = [scenes.grid_scene(), scenes.arm_scene(), scenes.mesh_scene()]
-    kinds = rng.integers(0, 3, n)
-    pools = []
-    for k, d in enumerate(descs):
-        need = 2 * int((kinds == k).sum())
+
+    def gpu_valid(d, c):
         scene = m.Scene(ctx, d)
-        got = []
-        s = 0
-        while sum(len(g) for g in got) < need:
-            c = scenes.uniform_states(d, 8 * need + 64, seed + 17 * k + s)
-            got.append(c[scene.valid(c) == 1])
-            s += 1
-        scene.close()
-        pools.append(np.concatenate(got)[:need])
-    used = [0, 0, 0]
+        try:
+            return scene.valid(c)
+        finally:
+            scene.close()
+
     qs = []
-    for i in range(n):
-        k = int(kinds[i])
-        d = descs[k]
-        a, b = pools[k][used[k]], pools[k][used[k] + 1]
-        used[k] += 2
-        budget = int(round(math.exp(rng.uniform(math.log(1000), math.log(200000)))))
+    for i, (d, a, b, budget) in enumerate(_serving_pairs(n, seed, gpu_valid)):
         W = wave_for[d["kind"]] if wave_for else min(4096, max(256, budget // 16))
         if d["kind"] != "grid":
             W = min(4096, max(W, budget // 128))
@@ -944,6 +1009,9 @@ def run_gpu(args):
         if not args.no_solve and not args.no_ref_planners:
             _progress("reference planners")
             ref_plans = reference_planners()
+            if serving is not None:
+                _progress("reference serving sample")
+                serving["reference_sample"] = reference_serving()
         osp = oracle.make_space(sc["metric"], sc["dim"])
         ot = oracle.KDTree(osp, pts, 8)
         sample = 2048
@@ -1020,10 +1088,15 @@ def main():
     ap.add_argument("--solve-only", action="store_true", help="time to solve of the three scenes only (profiling)")
     ap.add_argument("--solve-seeds", type=int, default=None, help="seeds per scene (default grid 50, arm 20, SE(3) 50)")
     ap.add_argument("--ref-plan-child", nargs=5, default=None, help=argparse.SUPPRESS)
+    ap.add_argument("--ref-serve-child", nargs=3, default=None, help=argparse.SUPPRESS)
     args = ap.parse_args()
     if args.ref_plan_child:
         mk, algo, threads, nseeds, cap = args.ref_plan_child
         _ref_plan_child(mk, algo, int(threads), int(nseeds), float(cap))
+        return
+    if args.ref_serve_child:
+        sample, cap, seed = args.ref_serve_child
+        _ref_serve_child(int(sample), float(cap), int(seed))
         return
     if args.impl == "reference":
         run_reference(args)
