@@ -402,6 +402,21 @@ REF_PLAN_RUNS = {
 }
 
 
+def _run_child(argv, timeout):
+    """Runs this file as a child process with argv; returns (stdout, stderr,
+    returncode).  A child that outlives timeout is killed and reported with
+    returncode None and the lines it printed before, so one stuck run of the
+    reference's code cannot end the bench."""
+    try:
+        p = subprocess.run([sys.executable, os.path.abspath(__file__)] + argv, capture_output=True, text=True,
+                           timeout=timeout)
+        return p.stdout, p.stderr, p.returncode
+    except subprocess.TimeoutExpired as e:
+        def _s(x):
+            return x.decode(errors="replace") if isinstance(x, bytes) else (x or "")
+        return _s(e.stdout), _s(e.stderr) + "\ntimed out after %g s" % timeout, None
+
+
 def reference_planners(runs=None):
     """Time to the first solution of the reference's own PRRT, PRRT* and PPRM
     (src/mpt/prrt.hpp, prrt_star.hpp, pprm.hpp, compiled by oracle/ref from the
@@ -426,19 +441,18 @@ def reference_planners(runs=None):
                 _progress("reference %s %s" % (name, key))
                 # each configuration in a child process: a crash inside the
                 # reference's code is recorded, not fatal to the bench
-                p = subprocess.run([sys.executable, os.path.abspath(__file__), "--ref-plan-child", mk, algo,
-                                    str(threads), str(nseeds), str(cap)], capture_output=True, text=True,
-                                   timeout=nseeds * (cap + 30) + 120)
-                rows = [json.loads(l_) for l_ in p.stdout.splitlines() if l_.startswith("{")]
+                so, se, rc = _run_child(["--ref-plan-child", mk, algo, str(threads), str(nseeds), str(cap)],
+                                        nseeds * (cap + 30) + 120)
+                rows = [json.loads(l_) for l_ in so.splitlines() if l_.startswith("{")]
                 t = sorted(r_["solve_s"] if r_["solved"] else cap for r_ in rows)
                 solved = [r_ for r_ in rows if r_["solved"]]
                 per[key] = {"threads": threads or os.cpu_count(), "seeds": nseeds, "cap_s": cap, "solved": len(solved),
                             "p50_s": statistics.median(t) if t else None, "max_s": t[-1] if t else None,
                             "median_cost": statistics.median([r_["cost"] for r_ in solved]) if solved else None,
                             "median_nodes": statistics.median([r_["nodes"] for r_ in solved]) if solved else None}
-                if p.returncode != 0 or len(rows) < nseeds:
-                    per[key]["incomplete"] = {"seeds_finished": len(rows), "returncode": p.returncode,
-                                              "stderr_tail": p.stderr[-200:]}
+                if rc != 0 or len(rows) < nseeds:
+                    per[key]["incomplete"] = {"seeds_finished": len(rows), "returncode": rc,
+                                              "stderr_tail": se[-200:]}
         out[name] = per
     return out
 
@@ -455,9 +469,8 @@ def reference_serving(sample=48, cap_s=2.0, seed=20261208):
     if not ref.available():
         return None
     ref.lib()
-    p = subprocess.run([sys.executable, os.path.abspath(__file__), "--ref-serve-child", str(sample), str(cap_s),
-                        str(seed)], capture_output=True, text=True, timeout=sample * (cap_s + 30) + 300)
-    rows = [json.loads(l_) for l_ in p.stdout.splitlines() if l_.startswith("{")]
+    so, se, rc = _run_child(["--ref-serve-child", str(sample), str(cap_s), str(seed)], sample * (cap_s + 30) + 300)
+    rows = [json.loads(l_) for l_ in so.splitlines() if l_.startswith("{")]
     wall = sum(r_["wall_s"] for r_ in rows)
     sol = sorted(r_["solve_s"] for r_ in rows if r_["solved"])
     per = {}
@@ -469,9 +482,8 @@ def reference_serving(sample=48, cap_s=2.0, seed=20261208):
            "host_cores": os.cpu_count(), "queries": len(rows), "sample_of": 512, "cap_s": cap_s,
            "wall_s": wall, "queries_per_s": len(rows) / wall if wall > 0 else None, "solved": len(sol),
            "p50_solve_s": sol[len(sol) // 2] if sol else None, "per_scene": per}
-    if p.returncode != 0 or len(rows) < sample:
-        out["incomplete"] = {"queries_finished": len(rows), "returncode": p.returncode,
-                             "stderr_tail": p.stderr[-200:]}
+    if rc != 0 or len(rows) < sample:
+        out["incomplete"] = {"queries_finished": len(rows), "returncode": rc, "stderr_tail": se[-200:]}
     return out
 
 
