@@ -877,6 +877,19 @@ def run_gpu(args):
         if rank == 0:
             print(json.dumps(out))
         return
+    skipped = {}
+
+    def due(what):
+        """True while the bench is within --budget-s seconds of its start; a
+        secondary section due later is skipped and listed in the line, so the
+        one JSON line is printed however slow the host or the box is."""
+        el = time.perf_counter() - _T0
+        if el <= args.budget_s:
+            return True
+        skipped[what] = round(el, 1)
+        _progress("skipped %s (%.0f s elapsed, budget %.0f s)" % (what, el, args.budget_s))
+        return False
+
     _progress("headline tree")
     sc, pts = _workload()
     tree = m.Tree(ctx, sc["metric"], sc["dim"], N_TREE)
@@ -964,32 +977,32 @@ def run_gpu(args):
     # secondary figures: NN@1M on the other scenes and on planner-grown trees,
     # edge checks/s (three scenes) and time to solve
     _progress("NN@1M of the other scenes")
-    nn1m = nn_1m_section(ctx, m, torch, peak=_peaks()[0]) if not args.no_nn1m else None
+    nn1m = nn_1m_section(ctx, m, torch, peak=_peaks()[0]) if not args.no_nn1m and due("nn_1m") else None
     _progress("edge checks")
     edges = edge_rates(ctx, m, stream, torch)
     _progress("time to solve")
-    solves = solve_times(ctx) if not args.no_solve else None
+    solves = solve_times(ctx) if not args.no_solve and due("time_to_solve") else None
     _progress("block planner sweep")
-    bplan = block_planner_sweep(ctx) if not args.no_solve else None
+    bplan = block_planner_sweep(ctx) if not args.no_solve and due("block_planner_grid") else None
     w_se3 = solves["se3_mesh"]["autotune"]["best"] if solves and "autotune" in solves["se3_mesh"] else None
     _progress("learned surrogate")
     learned, sg = (learned_vs_plain(ctx, m, torch, wavefront_tuned=w_se3)
-                   if not (args.no_solve or args.no_learned) else (None, None))
+                   if not (args.no_solve or args.no_learned) and due("learned_surrogate_se3") else (None, None))
     wave_for = None
     if solves and all("autotune" in solves[k] for k in solves):
         wave_for = {"grid": solves["grid_1024"]["autotune"]["best"], "arm": solves["arm_10link"]["autotune"]["best"],
                     "mesh": solves["se3_mesh"]["autotune"]["best"]}
     _progress("batched serving")
     serving = None
-    if not (args.no_solve or args.no_batch):
+    if not (args.no_solve or args.no_batch) and due("batch_serving"):
         serving = {"plain": batch_serving(m, ctx, wave_for=wave_for)}
-        if sg is not None:
+        if sg is not None and due("batch_serving.surrogate"):
             _progress("batched serving with the surrogate")
             serving["surrogate"] = batch_serving(m, ctx, wave_for=wave_for, surrogate=sg)
     _progress("PRRT*")
-    star = prrt_star_section(ctx, wave_for) if not (args.no_solve or args.no_star) else None
+    star = prrt_star_section(ctx, wave_for) if not (args.no_solve or args.no_star) and due("prrt_star") else None
     _progress("PPRM")
-    prm = prm_section(ctx) if not (args.no_solve or args.no_prm) else None
+    prm = prm_section(ctx) if not (args.no_solve or args.no_prm) and due("pprm") else None
 
     _progress("CPU baselines")
     # CPU baselines: oracle kd-tree and DMV on the host cores, bounded samples;
@@ -1018,10 +1031,10 @@ def run_gpu(args):
                 got, _ = oref.dmv_edges(scx, ea, eb, scx["edge_step"])
                 edges[name]["reference_dmv_edges_per_s"] = len(ea) / (time.perf_counter() - t0)
                 edges[name]["reference_dmv_equals_oracle"] = bool(np.array_equal(got, want))
-        if not args.no_solve and not args.no_ref_planners:
+        if not args.no_solve and not args.no_ref_planners and due("reference_planners"):
             _progress("reference planners")
             ref_plans = reference_planners()
-            if serving is not None:
+            if serving is not None and due("batch_serving.reference_sample"):
                 _progress("reference serving sample")
                 serving["reference_sample"] = reference_serving()
         osp = oracle.make_space(sc["metric"], sc["dim"])
@@ -1068,6 +1081,8 @@ def run_gpu(args):
                 "pprm": prm,
                 "clocks": clk.summary(), "gpu_launches": launches, "tree_build_s": build_s,
                 "wall_s_timed": wall}
+        if skipped:
+            line["skipped_sections"] = {"budget_s": args.budget_s, "elapsed_s_at_skip": skipped}
         print(json.dumps(line))
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -1098,6 +1113,8 @@ def main():
     ap.add_argument("--edges-only", action="store_true", help="edge checks/s of the three scenes only (profiling)")
     ap.add_argument("--bplan-only", action="store_true", help="the block planner's wavefront sweep only (profiling)")
     ap.add_argument("--solve-only", action="store_true", help="time to solve of the three scenes only (profiling)")
+    ap.add_argument("--budget-s", type=float, default=900.0,
+                    help="seconds from the start after which the secondary sections are skipped")
     ap.add_argument("--solve-seeds", type=int, default=None, help="seeds per scene (default grid 50, arm 20, SE(3) 50)")
     ap.add_argument("--ref-plan-child", nargs=5, default=None, help=argparse.SUPPRESS)
     ap.add_argument("--ref-serve-child", nargs=3, default=None, help=argparse.SUPPRESS)
