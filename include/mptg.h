@@ -241,7 +241,10 @@ mptg_status mptg_planner_graph(mptg_planner* planner, double* states, int32_t* p
  * the ordered insert and the stop conditions all on the device -- for up to
  * 16,384 nodes, then updates the kd-tree; beyond that, and everywhere else,
  * the multi-kernel wavefront runs.  mode 0: always the multi-kernel
- * wavefront.  Both build the same tree, state for state. */
+ * wavefront.  Both build the same tree, state for state.  A run with neither a
+ * wavefront count nor a time limit launches the block in slices of at most
+ * 1 s of device time, relaunched while the tree can grow, so that no launch
+ * runs for ever when every sample's link is invalid. */
 mptg_status mptg_planner_set_persistent(mptg_planner* planner, int mode);
 /* The block planner's nearest-node search (no reference counterpart: a tuning
  * knob of this planner).  A wavefront of W samples over n nodes with
@@ -352,7 +355,8 @@ mptg_status mptg_planner_reset(mptg_planner* planner, const mptg_plan_params* pa
  * persistent block planner takes (resolution 0, wavefront <= 1,024, no
  * surrogate) do not use the workers: they run together as one launch, one
  * thread block per query, while the workers take the rest; a query whose block
- * fills its 16,384 nodes unsolved is then run from its start by a worker.  A
+ * fills its 16,384 nodes unsolved, or (no time limit) is still unsolved after
+ * 1 s of device time, is then run from its start by a worker.  A
  * query behaves exactly as mptg_planner_create + add_start + set_goal +
  * run(stop_when_solved) with the same parameters: the same seed gives the
  * same tree and path. */

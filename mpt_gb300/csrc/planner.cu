@@ -1070,6 +1070,10 @@ static void bp_cells(BPlanJob& j, const double* lo, const double* hi) {
     j.gy = std::max(1, std::min(64, (int)std::ceil(sy / cs)));
 }
 
+// Longest launch of the block planner (s of device time) when its caller sets
+// no limit: the launch stops at the first wavefront boundary past it.
+static constexpr double kBPlanSliceS = 1.0;
+
 // Wavefronts inside the persistent block planner until a stop condition
 // (solved, node budget, wavefront count, time) or its node capacity; then the
 // kd-tree takes the new nodes and the host its goals.  *waves: wavefronts run.
@@ -1326,8 +1330,21 @@ mptg_status mptg_planner_run(mptg_planner* p, int max_wavefronts, double time_li
     auto t0 = std::chrono::steady_clock::now();
     mptg_status st = MPTG_OK;
     int it = 0;
-    if (bp_applies(p) && !(stop_when_solved && !p->goals.empty()))
-        st = run_persistent(p, max_wavefronts, time_limit_s, stop_when_solved, &it);
+    if (bp_applies(p) && !(stop_when_solved && !p->goals.empty())) {
+        // a call with neither a wavefront count nor a time limit runs the block
+        // planner in launches of at most kBPlanSliceS seconds of device time,
+        // relaunched while the tree can still grow: a start the tree never
+        // leaves (every link invalid) would otherwise keep one launch running
+        // for ever.  The launches run the same wavefronts one launch would.
+        const bool unbounded = max_wavefronts <= 0 && !(time_limit_s > 0);
+        for (;;) {
+            int w = 0;
+            st = run_persistent(p, max_wavefronts, unbounded ? kBPlanSliceS : time_limit_s, stop_when_solved, &w);
+            it += w;
+            if (st || !unbounded || w == 0 || p->bp_hctr->status == BPLAN_FULL) break;
+            if ((stop_when_solved && !p->goals.empty()) || planner_n(p) >= p->prm.max_nodes) break;
+        }
+    }
     // the multi-kernel wavefront: every other case, and what remains of this
     // call once the block planner's node capacity is reached
     for (; !st && (max_wavefronts <= 0 || it < max_wavefronts); ++it) {
@@ -1797,7 +1814,9 @@ static mptg_status grid_batch_launch(mptg_ctx* ctx, const mptg_query* qs, GridBa
         j.W = prm.wavefront;
         j.max_waves = 0;
         j.stop_when_solved = 1;
-        j.deadline_ns = q.time_limit_s > 0 ? (uint64_t)(q.time_limit_s * 1e9) : 0;
+        // a query without a time limit gets one slice (grid_batch_finish sends
+        // a block that ends on it unsolved back to the workers)
+        j.deadline_ns = (uint64_t)((q.time_limit_s > 0 ? q.time_limit_s : kBPlanSliceS) * 1e9);
         j.brute_pairs = BPLAN_BRUTE_PAIRS;
         bp_cells(j, vec + 2, vec + 4);
         g.hctr[k] = BPlanCounters{};
@@ -1836,7 +1855,10 @@ static mptg_status grid_batch_finish(mptg_ctx* ctx, const mptg_query* qs, GridBa
     for (size_t k = 0; k < K && !st; ++k) {
         const BPlanCounters& h = g.hctr[k];
         const mptg_query& q = qs[g.idx[k]];
-        if (h.status == BPLAN_FULL && h.goals == 0) {
+        // unsolved with its block full, or (no time limit) stopped by the slice
+        // below its node budget: the workers run it from its start
+        if (h.goals == 0 &&
+            (h.status == BPLAN_FULL || (!(q.time_limit_s > 0) && (size_t)h.n < q.params.max_nodes))) {
             g.retry.push_back(g.idx[k]);
             continue;
         }
