@@ -845,6 +845,26 @@ def _progress(msg):
 _T0 = time.perf_counter()
 
 
+class SectionBudget:
+    """The secondary sections run while the bench is within budget_s seconds
+    of its start (t0); one due later is skipped and listed in `skipped`
+    (section -> seconds elapsed), so the one JSON line is printed however slow
+    the host or the box is."""
+
+    def __init__(self, budget_s, t0=None):
+        self.budget_s = budget_s
+        self.t0 = _T0 if t0 is None else t0
+        self.skipped = {}
+
+    def due(self, what):
+        el = time.perf_counter() - self.t0
+        if el <= self.budget_s:
+            return True
+        self.skipped[what] = round(el, 1)
+        _progress("skipped %s (%.0f s elapsed, budget %.0f s)" % (what, el, self.budget_s))
+        return False
+
+
 def run_gpu(args):
     import torch
     import mpt_gb300 as m
@@ -877,18 +897,8 @@ def run_gpu(args):
         if rank == 0:
             print(json.dumps(out))
         return
-    skipped = {}
-
-    def due(what):
-        """True while the bench is within --budget-s seconds of its start; a
-        secondary section due later is skipped and listed in the line, so the
-        one JSON line is printed however slow the host or the box is."""
-        el = time.perf_counter() - _T0
-        if el <= args.budget_s:
-            return True
-        skipped[what] = round(el, 1)
-        _progress("skipped %s (%.0f s elapsed, budget %.0f s)" % (what, el, args.budget_s))
-        return False
+    budget = SectionBudget(args.budget_s)
+    due, skipped = budget.due, budget.skipped
 
     _progress("headline tree")
     sc, pts = _workload()

@@ -1,6 +1,7 @@
 """CPU, two gloo ranks: the host side of `bench.py --gpus N` (replicas only) --
 rank/world parsing, the max-over-ranks timing rule, the whole-job rate, and
-the reference arm's rule that only rank 0 runs and prints."""
+the reference arm's rule that only rank 0 runs and prints; and on one process
+the bench's section time budget and its child-process time limit."""
 import os
 import socket
 import sys
@@ -91,3 +92,20 @@ def test_reference_arm_line(monkeypatch, capsys):
     assert line["config"] == bench.NN_CONFIG  # the same config as the GPU arm's line
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_section_budget_and_child_timeout():
+    """The bench's secondary sections stop starting once its time budget is
+    spent (each skipped one is listed), and a reference child run that outlives
+    its limit is reported (returncode None, what it printed kept) instead of
+    ending the bench."""
+    import time
+    sys.path.insert(0, ROOT)
+    import bench
+    b = bench.SectionBudget(60.0, t0=time.perf_counter())
+    assert b.due("nn_1m") and b.skipped == {}
+    b = bench.SectionBudget(1.0, t0=time.perf_counter() - 5.0)
+    assert not b.due("pprm") and not b.due("prrt_star")
+    assert set(b.skipped) == {"pprm", "prrt_star"} and all(v >= 5.0 for v in b.skipped.values())
+    so, se, rc = bench._run_child(["--ref-serve-child", "2", "0.5", "1"], 0.3)
+    assert rc is None and "timed out after 0.3 s" in se
