@@ -57,11 +57,16 @@ typedef struct mptg_tree mptg_tree;
 typedef struct mptg_scene mptg_scene;
 
 /* ---- context ------------------------------------------------------- */
+/* A context on one CUDA device: its streams, scratch and error message (no
+ * reference counterpart: the reference runs on the host's threads). */
 mptg_status mptg_create(mptg_ctx** ctx, int device);
 mptg_status mptg_destroy(mptg_ctx* ctx);
-/* Message of the last failed call on this context (static storage). */
+/* Message of the last failed call on this context (static storage): the text
+ * the reference puts in its exceptions, e.g. "there are no valid initial
+ * states" (src/mpt/impl/prrt/prrt.hpp:197-198); no exception crosses the ABI. */
 const char* mptg_last_error(mptg_ctx* ctx);
-/* Number of kernels this library has launched on the context (for audits). */
+/* Number of kernels this library has launched on the context (for audits;
+ * no reference counterpart). */
 uint64_t mptg_kernel_launches(mptg_ctx* ctx);
 
 /* ---- nearest-neighbour tree ----------------------------------------
@@ -70,10 +75,12 @@ uint64_t mptg_kernel_launches(mptg_ctx* ctx);
  * src/mpt/impl/prrt_star/prrt_star.hpp:182-183. */
 mptg_status mptg_tree_create(mptg_ctx* ctx, mptg_metric metric, int dim, const double* weights,
                              size_t capacity, mptg_tree** tree);
+/* the Nigh object's lifetime (a member of PRRT, src/mpt/impl/prrt/prrt.hpp:121-122) */
 mptg_status mptg_tree_destroy(mptg_tree* tree);
 /* nigh insert (src/mpt/impl/prrt/prrt.hpp:186,447): appends n states
  * (row-major n x dim doubles); their ids are size()..size()+n-1. */
 mptg_status mptg_tree_insert(mptg_tree* tree, const double* states, size_t n, void* stream);
+/* nigh size() (PRRT::size, src/mpt/impl/prrt/prrt.hpp:177-179) */
 mptg_status mptg_tree_size(mptg_tree* tree, size_t* n);
 /* Search strategy, as the reference picks a nigh strategy per planner
  * (src/mpt/impl/nearest_strategy.hpp:44-72; auto = nigh::auto_strategy_t).
@@ -87,7 +94,8 @@ mptg_status mptg_tree_set_strategy(mptg_tree* tree, int strategy);
 /* Remove every state, keeping the tree's allocations (no reference
  * counterpart: a reference planner is rebuilt for each query). */
 mptg_status mptg_tree_clear(mptg_tree* tree, void* stream);
-/* Copy states [first, first+n) out of the tree (row-major doubles). */
+/* Copy states [first, first+n) out of the tree (row-major doubles); the node
+ * states PRRT::visitGraph reads (src/mpt/impl/prrt/prrt.hpp:300-316). */
 mptg_status mptg_tree_states(mptg_tree* tree, size_t first, size_t n, double* out, void* stream);
 /* nigh nearest(q) (src/mpt/impl/prrt/prrt.hpp:406-409): for each of nq
  * queries the id of the nearest state and its exact FP64 distance; ties go to
@@ -132,7 +140,8 @@ mptg_status mptg_nearest_linear_noalloc(mptg_ctx* ctx, mptg_metric metric, int d
                                         const double* points, size_t n, const double* queries, size_t nq,
                                         int32_t* idx_out, double* dist_out, void* stream);
 
-/* Per-tree search counters accumulated since the last reset:
+/* Per-tree search counters accumulated since the last reset (no reference
+ * counterpart: the roofline's algorithmic-byte inputs):
  * [0] queries, [1] internal nodes visited, [2] leaves visited,
  * [3] points evaluated in FP32, [4] candidates re-ranked in FP64. */
 mptg_status mptg_tree_counters(mptg_tree* tree, uint64_t out[5], int reset);
@@ -165,9 +174,12 @@ typedef struct {
     double w_rot; double w_pos;
 } mptg_scene_desc;
 
+/* The Scenario's collision world (the three demo scenarios above) copied to
+ * the device; a planner's copy of its Scenario (src/mpt/impl/prrt/prrt.hpp:326). */
 mptg_status mptg_scene_create(mptg_ctx* ctx, const mptg_scene_desc* desc, mptg_scene** scene);
 mptg_status mptg_scene_destroy(mptg_scene* scene);
-/* State dimension and metric of a scene's configuration space. */
+/* State dimension and metric of a scene's configuration space (Scenario::space(),
+ * its Space's dimensions() and distance). */
 mptg_status mptg_scene_space(mptg_scene* scene, int* dim, int* metric, double weights[2]);
 
 /* Scenario::valid(q) batched (src/mpt/impl/prrt/prrt.hpp:439). */
@@ -211,6 +223,7 @@ typedef struct {
  * dimensions of SE3 are always sampled uniformly on SO(3)). */
 mptg_status mptg_planner_create(mptg_ctx* ctx, mptg_scene* scene, const mptg_plan_params* params,
                                 const double* lo, const double* hi, mptg_planner** planner);
+/* the Planner's destructor */
 mptg_status mptg_planner_destroy(mptg_planner* planner);
 /* PRRT::addStart (prrt.hpp:181-187); the start is not checked for validity, as in the reference */
 mptg_status mptg_planner_add_start(mptg_planner* planner, const double* q);
@@ -223,8 +236,9 @@ mptg_status mptg_planner_set_goal(mptg_planner* planner, const double* q, double
  * states"); a second concurrent call -> MPTG_ERR_ALREADY_SOLVING. */
 mptg_status mptg_planner_run(mptg_planner* planner, int max_wavefronts, double time_limit_s,
                              int stop_when_solved, int* solved);
+/* PRRT::size (prrt.hpp:177-179) */
 mptg_status mptg_planner_size(mptg_planner* planner, size_t* n);
-/* number of goal nodes found (PRRT::solved() is goals > 0) */
+/* number of goal nodes found (PRRT::solved() is goals > 0, prrt.hpp:203-205) */
 mptg_status mptg_planner_goals(mptg_planner* planner, size_t* n);
 /* PRRT::solution() (prrt.hpp:263-274): the best goal's path, start first,
  * len states of dim doubles, and its cost (prrt.hpp:208-234).  path may be
@@ -426,6 +440,7 @@ typedef struct mptg_prm mptg_prm;
 /* Planner<Scenario, PPRM<...>>(scenario, seed) (pprm.hpp:141-149); lo/hi as mptg_planner_create */
 mptg_status mptg_prm_create(mptg_ctx* ctx, mptg_scene* scene, const mptg_plan_params* params, const double* lo,
                             const double* hi, const double* goal, mptg_prm** prm);
+/* the Planner's destructor */
 mptg_status mptg_prm_destroy(mptg_prm* prm);
 /* PPRM::addStart / addGoal (pprm.hpp:155-170): addSample with the start or
  * goal flag; *id = the node id, or -1 when the state is invalid or a
@@ -438,17 +453,21 @@ mptg_status mptg_prm_add_goal(mptg_prm* prm, const double* q, int32_t* id);
  * reference throws "PPRM requires both start and goal configurations"). */
 mptg_status mptg_prm_run(mptg_prm* prm, int max_wavefronts, double time_limit_s, int stop_when_solved,
                          int* solved);
+/* PPRM::size (pprm.hpp:152-154), and the roadmap's edge count */
 mptg_status mptg_prm_size(mptg_prm* prm, size_t* nodes, size_t* edges);
-/* states [n][dim] (may be NULL), and the undirected edges (from, to,
- * distance), from > to, sorted by (from, to) (any may be NULL) */
+/* The roadmap PPRM::visitGraph walks (pprm.hpp:248-251,381-388): states
+ * [n][dim] (may be NULL), and the undirected edges (from, to, distance),
+ * from > to, sorted by (from, to) (any may be NULL) */
 mptg_status mptg_prm_graph(mptg_prm* prm, double* states, size_t cap_nodes, int32_t* from, int32_t* to,
                            double* dist, size_t cap_edges, size_t* n, size_t* ne);
 /* PPRM::solution() (pprm.hpp:232-243): Dijkstra from the start nodes to the
  * nearest goal node over the edge distances; len states, start first (path
  * may be NULL to query len and cost; cost = +inf and len = 0 when unsolved) */
 mptg_status mptg_prm_solution(mptg_prm* prm, double* path, size_t cap, size_t* len, double* cost);
-/* counters: [0] wavefronts, [1] samples, [2] valid samples, [3] duplicates
- * skipped, [4] links checked, [5] edges, [6] goal nodes, [7] solved */
+/* counters (PPRM::printStats, pprm.hpp:242-245, and PPRM::solved,
+ * pprm.hpp:185-187): [0] wavefronts, [1] samples, [2] valid samples,
+ * [3] duplicates skipped, [4] links checked, [5] edges, [6] goal nodes,
+ * [7] solved */
 mptg_status mptg_prm_stats(mptg_prm* prm, uint64_t out[8]);
 
 /* ---- scene ingestion helpers (host only) -------------------------------
