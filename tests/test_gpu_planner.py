@@ -5,8 +5,6 @@
 * solving: every returned path is re-validated by the oracle (endpoints,
   each edge's DMV link, cost = summed oracle distances);
 * the Planner mirror's API behaviour (reference: test/planner_integration_test.hpp:219-291)."""
-import math
-
 import numpy as np
 import pytest
 

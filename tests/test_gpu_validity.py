@@ -1,7 +1,5 @@
 """GPU parity: batched Scenario::valid and DiscreteMotionValidator edges
 through the C ABI against the oracle (bit-exact booleans)."""
-import math
-
 import numpy as np
 import pytest
 
