@@ -109,3 +109,17 @@ def test_section_budget_and_child_timeout():
     assert set(b.skipped) == {"pprm", "prrt_star"} and all(v >= 5.0 for v in b.skipped.values())
     so, se, rc = bench._run_child(["--ref-serve-child", "2", "0.5", "1"], 0.3)
     assert rc is None and "timed out after 0.3 s" in se
+
+
+def test_nn_roofline_bytes_formula():
+    """The headline roofline's algorithmic bytes per k_nearest launch: FP32
+    coordinates of each point evaluated (4D), an internal node's record and
+    cell bounds (16 + 8D), a leaf record (16), a re-ranked candidate's FP64
+    state and id (8D + 4), and each query in and answer out (8D + 12)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    D = 10
+    per = {"points_evaluated": 1000, "internal_visited": 100, "leaves_visited": 40, "reranked": 3}
+    want = 1000 * 40 + 100 * 96 + 40 * 16 + 3 * 84 + 2 * 92
+    assert bench._nn_alg_bytes(per, 2, D) == want
+    assert bench._nn_alg_bytes({k: 0 for k in per}, 0, D) == 0
