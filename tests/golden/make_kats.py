@@ -4,11 +4,12 @@ unit tests for the metric spaces, transcribed with their file:line.
 The expected values are the reference tests' own expressions (e.g.
 ``2*M_PI - 4.0``) evaluated in IEEE double, the arithmetic the C++ tests use;
 they are stored as hex floats so the comparison stays bit-exact.  Run from the
-repository root:  python tests/golden/make_kats.py
+repository root:  python tests/golden/make_kats.py [output path]
 """
 import json
 import math
 import os
+import sys
 
 PI = math.pi
 
@@ -73,7 +74,8 @@ cases.append({"src": "test/scaled_space_test.cpp:40-52", "op": "scaled_distance"
               "a": [1, 2, 3], "b": [1, 0, -1], "scale": 2.5,
               "expect": h(math.sqrt(0.0 + 2.0 * 2.0 + 4.0 * 4.0) * 5 / 2), "tol": 0})
 
-out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "kats.json")
+# an output path may be given (the reproducibility test writes to a temporary file)
+out = sys.argv[1] if len(sys.argv) > 1 else os.path.join(os.path.dirname(os.path.abspath(__file__)), "kats.json")
 with open(out, "w") as f:
     json.dump({"generated_by": "tests/golden/make_kats.py", "cases": cases}, f, indent=1)
 print("wrote", out, len(cases), "cases")

@@ -190,3 +190,14 @@ def test_tri_tri_cases(orc):
     assert orc.tri_tri(t1, [0.1, 0.1, 0, 2, 0.1, 0, 0.1, 2, 0])               # coplanar overlap
     assert not orc.tri_tri(t1, [2, 2, 0, 3, 2, 0, 2, 3, 0])                   # coplanar apart
     assert orc.tri_tri(t1, [1, 0, 0, 1, 0, 1, 2, 0, 0])                       # touching at a vertex
+
+
+def test_kats_file_is_what_its_script_writes(tmp_path):
+    """tests/golden/kats.json is exactly the output of the committed script."""
+    import subprocess
+    import sys
+    out = tmp_path / "kats.json"
+    subprocess.check_call([sys.executable, os.path.join(HERE, "golden", "make_kats.py"), str(out)],
+                          stdout=subprocess.DEVNULL)
+    with open(os.path.join(HERE, "golden", "kats.json"), "rb") as f:
+        assert out.read_bytes() == f.read()
