@@ -208,8 +208,12 @@ def _png_rgb(data: bytes) -> np.ndarray:
         raise ValueError("not a PNG file")
     pos, idat, plte, hdr = 8, [], None, None
     while pos < len(data):
+        if pos + 12 > len(data):
+            raise ValueError("truncated PNG chunk")
         n, kind = struct.unpack(">I4s", data[pos:pos + 8])
         body = data[pos + 8:pos + 8 + n]
+        if len(body) < n:
+            raise ValueError("truncated PNG chunk")
         pos += 12 + n
         if kind == b"IHDR":
             hdr = struct.unpack(">IIBBBBB", body)
@@ -222,8 +226,18 @@ def _png_rgb(data: bytes) -> np.ndarray:
     if hdr is None:
         raise ValueError("PNG without IHDR")
     w, h, depth, ctype, _, _, interlace = hdr
+    # the colour type / bit depth pairs of the PNG specification
+    if depth not in {0: (1, 2, 4, 8, 16), 2: (8, 16), 3: (1, 2, 4, 8), 4: (8, 16), 6: (8, 16)}.get(ctype, ()):
+        raise ValueError("unsupported PNG colour type %d with bit depth %d" % (ctype, depth))
+    if w < 1 or h < 1:
+        raise ValueError("PNG with an empty image")
+    if ctype == 3 and plte is None:
+        raise ValueError("palette PNG without PLTE")
     chans = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
-    raw = np.frombuffer(zlib.decompress(b"".join(idat)), dtype=np.uint8)
+    try:
+        raw = np.frombuffer(zlib.decompress(b"".join(idat)), dtype=np.uint8)
+    except zlib.error as e:
+        raise ValueError("corrupt PNG image data: %s" % e) from None
     if not interlace:
         px, _ = _png_samples(raw, w, h, depth, ctype)
     else:
@@ -240,6 +254,8 @@ def _png_rgb(data: bytes) -> np.ndarray:
             off += used
     px = px.reshape(h, w, chans)
     if ctype == 3:
+        if px.size and int(px.max()) >= len(plte):
+            raise ValueError("PNG palette index beyond its PLTE")
         return plte[px[:, :, 0]]
     if ctype in (0, 4):
         return np.repeat(px[:, :, :1], 3, axis=2)
@@ -248,46 +264,64 @@ def _png_rgb(data: bytes) -> np.ndarray:
 
 def _pnm_rgb(data: bytes) -> np.ndarray:
     magic = data[:2]
-    toks, pos = [], 2
+    toks, pos, end = [], 2, len(data)
     need = 2 if magic in (b"P1", b"P4") else 3
     while len(toks) < need:
-        while data[pos:pos + 1].isspace():
+        while pos < end and data[pos:pos + 1].isspace():
             pos += 1
         if data[pos:pos + 1] == b"#":
             while data[pos:pos + 1] not in (b"\n", b""):
                 pos += 1
             continue
         start = pos
-        while not data[pos:pos + 1].isspace():
+        while pos < end and not data[pos:pos + 1].isspace():
             pos += 1
+        if start == pos:
+            raise ValueError("truncated Netpbm header")
+        if not data[start:pos].isdigit():
+            raise ValueError("invalid Netpbm header value %r" % data[start:pos])
         toks.append(int(data[start:pos]))
     w, h = toks[0], toks[1]
     maxv = toks[2] if need == 3 else 1
+    if w < 1 or h < 1 or not 1 <= maxv <= 65535:
+        raise ValueError("invalid Netpbm size or maximum value")
     if magic in (b"P1", b"P2", b"P3"):
         body = re.sub(rb"#[^\n]*", b"", data[pos:])
         if magic == b"P1":
             vals = np.array([c - 48 for c in body if c in b"01"], dtype=np.int64)[:w * h]
+            if len(vals) < w * h:
+                raise ValueError("truncated Netpbm image data")
             g = np.where(vals.reshape(h, w) == 1, 0, 255).astype(np.uint8)
             return np.repeat(g[:, :, None], 3, axis=2)
-        vals = np.array(body.split(), dtype=np.int64)
         ch = 1 if magic == b"P2" else 3
+        try:
+            vals = np.array(body.split(), dtype=np.int64)
+        except ValueError:
+            raise ValueError("invalid Netpbm sample value") from None
+        if len(vals) < w * h * ch:
+            raise ValueError("truncated Netpbm image data")
         px = (vals[:w * h * ch] * 255 // maxv).astype(np.uint8).reshape(h, w, ch)
         return np.repeat(px, 3, axis=2) if ch == 1 else px
     pos += 1  # the single whitespace after the header
     if magic == b"P4":
         stride = (w + 7) // 8
+        if end - pos < stride * h:
+            raise ValueError("truncated Netpbm image data")
         bitsarr = np.unpackbits(np.frombuffer(data[pos:pos + stride * h], dtype=np.uint8).reshape(h, stride), axis=1)
         g = np.where(bitsarr[:, :w] == 1, 0, 255).astype(np.uint8)
         return np.repeat(g[:, :, None], 3, axis=2)
     ch = 1 if magic == b"P5" else 3
     dt = np.dtype(">u2") if maxv > 255 else np.dtype(np.uint8)
+    if end - pos < w * h * ch * dt.itemsize:
+        raise ValueError("truncated Netpbm image data")
     px = np.frombuffer(data[pos:pos + w * h * ch * dt.itemsize], dtype=dt).reshape(h, w, ch).astype(np.int64)
     px = (px * 255 // maxv).astype(np.uint8)
     return np.repeat(px, 3, axis=2) if ch == 1 else px
 
 
 def read_image(path: str) -> np.ndarray:
-    """RGB pixels [height][width][3] (uint8) of a PNG or Netpbm (P1-P6) file."""
+    """RGB pixels [height][width][3] (uint8) of a PNG or Netpbm (P1-P6) file.
+    A malformed, truncated or unsupported file raises ValueError."""
     with open(path, "rb") as f:
         data = f.read()
     if data[:8] == b"\x89PNG\r\n\x1a\n":

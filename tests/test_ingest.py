@@ -263,3 +263,60 @@ def test_se3_problem_from_files(tmp_path):
     assert pr["range"] == 2.5 and pr["weights"] == (50.0, 1.0)
     assert pr["edge_step"] == (math.sqrt(3 * 400.0) + 50 * math.pi / 2) * 0.01
     assert list(pr["lo"][4:]) == [0, 0, 0] and list(pr["hi"][4:]) == [20, 20, 20]
+
+
+@pytest.mark.timeout(10)
+@pytest.mark.parametrize("data", [
+    b"P5\n64",                          # header ends inside the width
+    b"P5",                              # no header at all
+    b"P6 2 # a comment to the end",     # comment, then nothing
+    b"P5 2 2 255\n\x00\x01\x02",        # one sample short
+    b"P4\n9 2\n\xff\xff\xff",           # one packed byte short
+    b"P2 2 2 255\n1 2 x 4\n",           # a sample that is not a number
+    b"P3 2 1 255\n1 2 3 4 5\n",         # one sample short
+    b"P1\n3 2\n1 0 1\n0\n",             # one bit short
+    b"P6 0 2 255\n",                    # empty image
+    b"P5 2 2 70000\n",                  # maximum value beyond 16 bits
+    b"P5 2 -2 255\n",                   # a signed size
+])
+def test_pnm_malformed_inputs_raise(tmp_path, data):
+    """A malformed or truncated Netpbm file is a ValueError, never a hang or
+    a numpy error (a header cut short used to loop for ever)."""
+    p = tmp_path / "bad.pnm"
+    p.write_bytes(data)
+    with pytest.raises(ValueError):
+        ingest.read_image(str(p))
+
+
+def test_png_malformed_inputs_raise(tmp_path):
+    """Unsupported colour type / depth pairs, a palette image without PLTE or
+    with an index beyond it, corrupt and truncated data: each a ValueError."""
+    rows = np.zeros((2, 2), dtype=np.uint8)
+    raw = _filtered(rows, 1)
+    cases = [dict(ctype=5, depth=8), dict(ctype=3, depth=16), dict(ctype=2, depth=4), dict(ctype=3, depth=8)]
+    for i, c in enumerate(cases):  # the last: a palette image without its PLTE
+        p = tmp_path / ("c%d.png" % i)
+        _write_png(p, 2, 2, c["ctype"], c["depth"], raw)
+        with pytest.raises(ValueError):
+            ingest.read_image(str(p))
+    p = tmp_path / "idx.png"  # index 7 into a 2-entry palette
+    _write_png(p, 2, 2, 3, 8, _filtered(np.array([[0, 1], [7, 0]], dtype=np.uint8), 1),
+               palette=[[0, 0, 0], [255, 255, 255]])
+    with pytest.raises(ValueError):
+        ingest.read_image(str(p))
+    good = tmp_path / "good.png"
+    _write_png(good, 2, 2, 0, 8, raw)
+    assert ingest.read_image(str(good)).shape == (2, 2, 3)
+    data = good.read_bytes()
+    for cut in (len(data) - 20, 40, 20):  # inside IDAT, inside a chunk header, inside IHDR
+        q = tmp_path / ("cut%d.png" % cut)
+        q.write_bytes(data[:cut])
+        with pytest.raises(ValueError):
+            ingest.read_image(str(q))
+    bad = bytearray(data)
+    i = data.index(b"IDAT") + 4
+    bad[i:i + 4] = b"\xff\xff\xff\xff"  # corrupt the compressed stream
+    q = tmp_path / "corrupt.png"
+    q.write_bytes(bytes(bad))
+    with pytest.raises(ValueError):
+        ingest.read_image(str(q))
